@@ -1,0 +1,136 @@
+"""ctypes front end of the C oracle (awe_oracle.c) - test infrastructure only.
+
+``build()`` compiles liboracle.so (exact float restatement) and
+liboracle64.so (same scheme, FP64 wavefields) with gcc and, when the
+reference sources are present, the reference's own CPU programs into
+oracle/_ref/ (via oracle/ref/Makefile).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+REF_OUT = os.path.join(HERE, "_ref")
+REF_SRC = "/root/reference/CODE"
+
+CFLAGS = ["-std=gnu99", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-Wall"]
+
+
+def build(with_reference: bool = True) -> None:
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(HERE, "awe_oracle.c")
+    for name, extra in (("liboracle.so", []), ("liboracle64.so", ["-DAWE_REAL_DOUBLE"])):
+        out = os.path.join(BUILD, name)
+        if not os.path.exists(out) or os.path.getmtime(out) < max(
+            os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "awe_oracle.h"))
+        ):
+            subprocess.check_call(["gcc", *CFLAGS, *extra, src, "-o", out, "-lm"])
+    if with_reference and os.path.isdir(REF_SRC):
+        subprocess.check_call(
+            ["make", "-s", "-C", os.path.join(HERE, "ref"), "REF=" + REF_SRC, "OUT=" + REF_OUT],
+            stdout=subprocess.DEVNULL,
+        )
+
+
+class Par(C.Structure):
+    _fields_ = [
+        ("n1", C.c_int), ("n2", C.c_int), ("n3", C.c_int),
+        ("d1", C.c_float), ("d2", C.c_float), ("d3", C.c_float),
+        ("o1", C.c_float), ("o2", C.c_float), ("o3", C.c_float),
+        ("nb", C.c_int), ("nt", C.c_int), ("dt", C.c_float),
+        ("fdorder", C.c_int), ("optfd", C.c_int), ("dabc", C.c_int), ("fsrf", C.c_int),
+        ("hybrid", C.c_int), ("expl", C.c_int), ("jsnap", C.c_int), ("bnds", C.c_int),
+        ("nthreads", C.c_int),
+    ]
+
+
+_libs: dict = {}
+
+
+def lib(fp64: bool = False):
+    name = "liboracle64.so" if fp64 else "liboracle.so"
+    if name not in _libs:
+        path = os.path.join(BUILD, name)
+        if not os.path.exists(path):
+            build(with_reference=False)
+        L = C.CDLL(path)
+        fp = C.POINTER(C.c_float)
+        for fn in ("orc_cart2d_cpu", "orc_cart3d_cpu"):
+            f = getattr(L, fn)
+            f.argtypes = [C.POINTER(Par), fp, fp, fp, C.c_int, fp, C.c_int, fp, fp, fp]
+            f.restype = C.c_int
+        L.orc_cart_padded.argtypes = [C.POINTER(Par)] + [C.POINTER(C.c_int)] * 4
+        L.orc_cart3d_cpu_steps.argtypes = [C.c_int] * 6
+        L.orc_cart3d_cpu_steps.restype = C.c_double
+        _libs[name] = L
+    return _libs[name]
+
+
+def _fp(a):
+    if a is None:
+        return None
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def make_par(p: dict) -> Par:
+    q = Par()
+    q.n1, q.n2, q.n3 = p["n"][0], p["n"][1], (p["n"][2] if len(p["n"]) > 2 else 1)
+    d = list(p["d"]) + [1.0] * (3 - len(p["d"]))
+    o = list(p["o"]) + [0.0] * (3 - len(p["o"]))
+    q.d1, q.d2, q.d3 = d
+    q.o1, q.o2, q.o3 = o
+    q.nb = p.get("nb", -1)
+    q.nt = p["nt"]
+    q.dt = p["dt"]
+    q.fdorder = p.get("fdorder", 4)
+    q.optfd = int(p.get("optfd", 0))
+    q.dabc = int(p.get("dabc", 0))
+    q.fsrf = int(p.get("fsrf", 0))
+    q.hybrid = int(p.get("hybrid", 0))
+    q.expl = int(p.get("expl", 0))
+    q.jsnap = p.get("jsnap", 0)
+    q.bnds = int(p.get("bnds", 0))
+    q.nthreads = p.get("nthreads", 0)
+    return q
+
+
+def padded(p: dict):
+    q = make_par(p)
+    vals = [C.c_int() for _ in range(4)]
+    lib().orc_cart_padded(C.byref(q), *[C.byref(v) for v in vals])
+    return tuple(v.value for v in vals)
+
+
+def cart_cpu(p: dict, vel, wav, sou, rec, den=None, fp64: bool = False):
+    """Run the scheme of MAWEFDcart{2D,3D}cpu.c.  Arrays are C-order numpy
+    float32 with axis 1 last (vel [n2][n1] or [n3][n2][n1]).  Returns
+    (dat [nt][nr], snaps [nsnap][...] or None)."""
+    q = make_par(p)
+    ndim = 3 if q.n3 > 1 else 2
+    nbd, n1p, n2p, n3p = padded(p)
+    vel = np.ascontiguousarray(vel, np.float32)
+    den = None if den is None else np.ascontiguousarray(den, np.float32)
+    wav = np.ascontiguousarray(wav, np.float32)
+    sou = np.ascontiguousarray(sou, np.float32).reshape(-1, ndim)
+    rec = np.ascontiguousarray(rec, np.float32).reshape(-1, ndim)
+    ns, nr = sou.shape[0], rec.shape[0]
+    dat = np.zeros((q.nt, nr), np.float32)
+    snaps = None
+    if q.jsnap > 0:
+        nsnap = (q.nt - 1) // q.jsnap + 1
+        frame = (n1p * n2p * n3p) if q.bnds else (q.n1 * q.n2 * q.n3)
+        snaps = np.zeros((nsnap, frame), np.float32)
+    fn = lib(fp64).orc_cart3d_cpu if ndim == 3 else lib(fp64).orc_cart2d_cpu
+    rc = fn(C.byref(q), _fp(vel), _fp(den), _fp(wav), ns, _fp(sou), nr, _fp(rec), _fp(dat), _fp(snaps))
+    if rc != 0:
+        raise RuntimeError("oracle returned %d" % rc)
+    return dat, snaps
+
+
+def cart3d_steps_seconds(n1pad, n2pad, n3pad, fdorder, nsteps, nthreads):
+    return lib().orc_cart3d_cpu_steps(n1pad, n2pad, n3pad, fdorder, nsteps, nthreads)
