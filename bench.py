@@ -1,0 +1,378 @@
+#!/usr/bin/env python
+"""Benchmark: 3D cartesian acoustic forward modelling (the 512^3 workload).
+
+One bench step = one complete forward run of the workload: 512 x 512 x 512
+model at 5 m (576^3 with the nb=32 padding), 8th-order Laplacian, nt = 3000
+steps of 0.005 us, Gaussian sponge + one-way ABC (dabc=y), one Ricker source
+(5 MHz) and a 128 x 128 receiver grid at z = 50 m.  The model is the seeded
+layered vacuum / ice (5 dust layers) / basalt model with 2D Gaussian-random
+interfaces.
+
+  value : padded cell-updates/s with model, wavelet and trace buffers
+          already resident in HBM (awe_forward_device), all ranks
+  e2e   : the same metric through awe_set_model + awe_set_geometry +
+          awe_forward with pinned host buffers (H2D of the model and
+          wavelet, D2H of the traces inside the timed region)
+
+--impl reference times the reference CPU implementation of the same update
+(the oracle port of ts_kernel.c step_forward_3d, OpenMP over all host cores)
+on a bounded sample of time steps of the same padded grid.
+
+Multi-GPU: shots are independent, so N ranks run N replicas (weak scaling,
+no collective on the data path); value = all ranks' cell-updates / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-updates/s & %HBM peak (3D acoustic)"
+UNIT = "cell-updates/s"
+BYTES_PER_CELL = 16  # read u_cur, read u_prev, read v^2dt^2, write u_next
+
+
+def workload(nt=3000):
+    return dict(name="3D cartesian acoustic forward, 512^3 at 5 m (576^3 padded, nb=32), 8th order, "
+                     "nt=%d, dabc=y, 1 Ricker source, 128x128 receivers" % nt,
+                n=(512, 512, 512), d=(5.0, 5.0, 5.0), o=(0.0, 0.0, 0.0), nt=nt, dt=0.005, nb=32, fdorder=8,
+                dabc=1, f0=5.0, seed=3)
+
+
+def gaussian_field(rng, shape, corr_cells):
+    """Zero-mean unit-std 2D Gaussian random field with a Gaussian
+    correlation of length corr_cells (FFT filter)."""
+    w = rng.standard_normal(shape)
+    ky = np.fft.fftfreq(shape[0])[:, None]
+    kx = np.fft.fftfreq(shape[1])[None, :]
+    filt = np.exp(-0.5 * (2 * np.pi) ** 2 * (kx ** 2 + ky ** 2) * corr_cells ** 2 / 2.0)
+    f = np.real(np.fft.ifft2(np.fft.fft2(w) * filt))
+    return (f - f.mean()) / (f.std() + 1e-12)
+
+
+def layered_model_3d(w):
+    """Vacuum 300 m/us down to a Gaussian-random surface (mean 200 m, std 30 m,
+    correlation 200 m); ice 168 m/us with 5 dust layers (+-5 %, 10-20 m);
+    basalt 110 m/us below a second random interface (mean 1800 m).
+    Returns [ny][nx][nz] float32 (axis 1 = z fastest)."""
+    rng = np.random.default_rng(w["seed"])
+    nz, nx, ny = w["n"]
+    dz, dx = w["d"][0], w["d"][1]
+    surf = 200.0 + 30.0 * gaussian_field(rng, (ny, nx), 200.0 / dx)
+    base = 1800.0 + 30.0 * gaussian_field(rng, (ny, nx), 200.0 / dx)
+    z = (np.arange(nz, dtype=np.float32) * dz)[None, None, :]
+    vel = np.full((ny, nx, nz), 168.0, np.float32)
+    for _ in range(5):
+        zd = rng.uniform(400.0, 1600.0)
+        th = rng.uniform(10.0, 20.0)
+        amp = rng.choice([0.95, 1.05])
+        depth = surf + (zd - 200.0)
+        band = np.abs(z - depth[:, :, None]) < 0.5 * th
+        vel[band] = 168.0 * amp
+    vel[z < surf[:, :, None].astype(np.float32)] = 300.0
+    vel[z >= base[:, :, None].astype(np.float32)] = 110.0
+    return vel
+
+
+def geometry(w):
+    nz, nx, ny = w["n"]
+    dx = w["d"][1]
+    xc, yc = 0.5 * (nx - 1) * dx, 0.5 * (ny - 1) * dx
+    sou = np.array([[xc, yc, 50.0]], np.float32)
+    gx = np.linspace(0.05, 0.95, 128) * (nx - 1) * dx
+    gy = np.linspace(0.05, 0.95, 128) * (ny - 1) * dx
+    X, Y = np.meshgrid(gx, gy, indexing="ij")
+    rec = np.stack([X.ravel(), Y.ravel(), np.full(X.size, 50.0)], 1).astype(np.float32)
+    return sou, rec
+
+
+def ricker(nt, dt, f0):
+    t = np.arange(nt) * dt - 1.5 / f0
+    a = (np.pi * f0 * t) ** 2
+    r = (1 - 2 * a) * np.exp(-a)
+    return (r / np.abs(r).max()).astype(np.float32)
+
+
+def padded_cells(w):
+    return int(np.prod([n + 2 * w["nb"] for n in w["n"]]))
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) >= 8:
+                rows.append(parts)
+        if not rows:
+            return None
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, name in enumerate(names):
+                if r[4 + k].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": float(rows[0][1]) if rows[0][1].replace(".", "").isdigit() else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per step-kernel launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "k_stepB_3d_o8_c3.txt")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch_full:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except Exception:
+        pass
+    return None
+
+
+def cpu_baseline(w, target_s=10.0):
+    """Oracle port of the reference CPU update (OpenMP, all host cores) on
+    the padded grid: returns (cell-updates/s, cores, sample description)."""
+    from oracle import oracle
+
+    oracle.build(with_reference=False)
+    cores = os.cpu_count() or 1
+    npad = [n + 2 * w["nb"] for n in w["n"]]
+    t1 = oracle.cart3d_steps_seconds(npad[0], npad[1], npad[2], w["fdorder"], 1, cores)
+    nsteps = int(max(1, min(20, target_s / max(t1, 1e-3))))
+    t = oracle.cart3d_steps_seconds(npad[0], npad[1], npad[2], w["fdorder"], nsteps, cores)
+    cells = float(np.prod(npad))
+    sample = "%d time steps of the %dx%dx%d padded grid (8th-order update of ts_kernel.c step_forward_3d, %d threads)" % (
+        nsteps, npad[0], npad[1], npad[2], cores)
+    return cells * nsteps / t, cores, sample, nsteps
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+        return dist, rank, world, local
+    return None, rank, world, local
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def allmax(dist, x):
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args):
+    dist, rank, world, local = dist_init()
+    if rank != 0:
+        return
+    w = workload()
+    from oracle import oracle
+
+    oracle.build(with_reference=False)
+    cores = os.cpu_count() or 1
+    npad = [n + 2 * w["nb"] for n in w["n"]]
+    cells = float(np.prod(npad))
+    t1 = oracle.cart3d_steps_seconds(npad[0], npad[1], npad[2], w["fdorder"], 1, cores)
+    per_step = int(max(1, min(10, 8.0 / max(t1, 1e-3))))
+    for _ in range(args.warmup):
+        oracle.cart3d_steps_seconds(npad[0], npad[1], npad[2], w["fdorder"], per_step, cores)
+    times = [oracle.cart3d_steps_seconds(npad[0], npad[1], npad[2], w["fdorder"], per_step, cores)
+             for _ in range(args.steps)]
+    total = sum(times)
+    value = cells * per_step * args.steps / total
+    sample = "%d time steps per bench step of the %dx%dx%d padded grid (oracle port of ts_kernel.c step_forward_3d, %d OpenMP threads)" % (
+        per_step, npad[0], npad[1], npad[2], cores)
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+           "data": "synthetic", "config": {"workload": w["name"], "sample": sample},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def run_ours(args):
+    import torch
+
+    import wavefield_imaging_gb300 as awe
+
+    dist, rank, world, local = dist_init()
+    torch.cuda.set_device(local)
+    w = workload(args.nt)
+    vel = layered_model_3d(w)
+    sou, rec = geometry(w)
+    wav = ricker(w["nt"], w["dt"], w["f0"])
+    prec = awe.EXACT if args.precision == "exact" else awe.FAST
+    desc = awe.make_desc(3, w["n"], w["d"], w["o"], w["nt"], w["dt"], nb=w["nb"], fdorder=w["fdorder"],
+                         dabc=w["dabc"], expl=1, precision=prec)
+    plan = awe.Plan(desc, device=local)
+    plan.set_model(vel)
+    plan.set_geometry(sou, rec)
+    nr = rec.shape[0]
+    d_wav = torch.from_numpy(wav).cuda()
+    d_dat = torch.zeros((plan.nsmp, nr), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.Stream()
+    cells = padded_cells(w)
+
+    def step():
+        plan.forward_device(d_wav.data_ptr(), 1, d_dat.data_ptr(), 0, stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    plan.profile(True)
+    barrier(dist)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    launches = 0
+    for _ in range(args.steps):
+        step()
+        launches += plan.last_launch_count()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(dist)
+    clocks = sampler.stop()
+    ms = ev0.elapsed_time(ev1)
+    kern_ms, kern_n = plan.profile_read()
+    plan.profile(False)
+    ms_max = allmax(dist, ms)
+    value = cells * w["nt"] * args.steps * world / (ms_max / 1e3)
+
+    # end to end through the public API with pinned host buffers
+    h_vel = torch.from_numpy(vel).pin_memory()
+    h_wav = torch.from_numpy(wav).pin_memory()
+    h_dat = torch.zeros((plan.nsmp, nr), dtype=torch.float32).pin_memory()
+    vel_np, wav_np, dat_np = h_vel.numpy(), h_wav.numpy(), h_dat.numpy()
+
+    def e2e_step():
+        plan.set_model(vel_np)
+        plan.set_geometry(sou, rec)
+        lib = awe.lib()
+        import ctypes as C
+        st = lib.awe_forward(plan.handle, wav_np.ctypes.data_as(C.POINTER(C.c_float)), 1,
+                             dat_np.ctypes.data_as(C.POINTER(C.c_float)), None)
+        if st != 0:
+            raise RuntimeError(lib.awe_last_error().decode())
+
+    e2e_step()
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    t1 = time.perf_counter()
+    e2e_s = allmax(dist, t1 - t0)
+    e2e_value = cells * w["nt"] * args.steps * world / e2e_s
+    check = float(np.abs(dat_np).max())
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peak()
+    avg_kernel_s = (kern_ms / 1e3) / max(kern_n, 1)
+    achieved = BYTES_PER_CELL * cells / avg_kernel_s / 1e9
+    traffic = profiled_traffic()
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+           "config": {"workload": w["name"], "padded_cells": cells, "interior_cells": int(np.prod(w["n"])),
+                      "precision": args.precision, "l2": "no flush: every step streams 3 fields of 764 MB (> 129 MB L2)",
+                      "parallelism": "replicas" if world > 1 else "single", "seed": w["seed"]},
+           "e2e": {"value": e2e_value, "unit": UNIT,
+                   "h2d_bytes_per_step": int(vel.nbytes + wav.nbytes + sou.nbytes + rec.nbytes),
+                   "d2h_bytes_per_step": int(plan.nsmp * nr * 4)},
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak, "traffic": traffic, "kernel": "k_stepB (3D, 8th order)",
+                        "peak_source": peak_kind, "avg_launch_us": avg_kernel_s * 1e6,
+                        "kernel_share": (kern_ms / ms) if ms > 0 else None},
+           "gpu_launches": int(launches), "clocks": clocks, "trace_max_abs": check}
+    if args.cpu_baseline:
+        v, cores, sample, _ = cpu_baseline(w)
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+    print(json.dumps(out))
+    plan.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fast", choices=["fast", "exact"])
+    ap.add_argument("--nt", type=int, default=3000, help="time steps (the workload is nt=3000)")
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,164 @@
+/* awe.h - C-ABI of the GB300-native acoustic wave-propagation engine.
+ *
+ * Drop-in boundary for the time-stepping path of the reference programs
+ * sfAWEFDcart2Dgpu, sfAWEFDcart3Dgpu, sfAWEFDspher2Dgpu and sfAWEFDspher3Dgpu
+ * (Nacnud04/wavefield_imaging, CODE/MAWEFD{cart,spher}{2D,3D}gpu.cu) and of
+ * the cartesian CPU programs MAWEFDcart{2D,3D}cpu.c whose 2N-order scheme the
+ * GPU programs lack.  Plain C types only: pointers, sizes, scalars.
+ *
+ * Each entry point replaces one stage of the reference program's main():
+ *   awe_plan_create   <- parameter parsing + fdutil_init/fdutil3d_init + the
+ *                        cudaMalloc block (MAWEFDcart2Dgpu.cu:74-166, :188-259;
+ *                        MAWEFDcart2Dcpu.c:116-235)
+ *   awe_set_model     <- sf_floatread(vel/den/rfl) + expand_cpu_2d/3d or
+ *                        expand2d/3d + cudaMemcpy (MAWEFDcart2Dgpu.cu:226-246;
+ *                        MAWEFDcart3Dcpu.c:257-293)
+ *   awe_set_geometry  <- pt2dread1/pt3dread1 + lint2d_make/lint3d_make +
+ *                        cudaMemcpy of weights (MAWEFDcart2Dgpu.cu:307-343;
+ *                        fdutil.c:1363-1539)
+ *   awe_forward       <- the time loop and the trace/snapshot output
+ *                        (MAWEFDcart2Dgpu.cu:362-511; MAWEFDcart3Dgpu.cu:380-477;
+ *                        MAWEFDspher2Dgpu.cu:341-435; MAWEFDspher3Dgpu.cu:449-566;
+ *                        MAWEFDcart2Dcpu.c:297-383; MAWEFDcart3Dcpu.c:295-366)
+ *   awe_plan_destroy  <- the cudaFree block (MAWEFDcart2Dgpu.cu:513-527)
+ *
+ * Conventions: the caller owns every host array; the library owns device
+ * state.  Every call returns an awe_status (never exits the process);
+ * awe_last_error() describes the last failure on the calling thread.  One
+ * plan per host thread at a time.  Arrays are C order with RSF axis 1
+ * fastest: a model is [n3][n2][n1] (n3 = 1 in 2D).
+ */
+#ifndef AWE_H
+#define AWE_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AWE_ABI_VERSION 1
+
+typedef enum {
+    AWE_OK = 0,
+    AWE_ERR_INVALID = 1,     /* bad argument or descriptor */
+    AWE_ERR_CUDA = 2,        /* CUDA runtime failure */
+    AWE_ERR_NOMEM = 3,       /* device or host allocation failed */
+    AWE_ERR_UNSUPPORTED = 4, /* combination of options not implemented */
+    AWE_ERR_NODEVICE = 5,    /* no usable CUDA device */
+    AWE_ERR_STATE = 6        /* call out of order (e.g. forward before set_model) */
+} awe_status;
+
+/* Coordinate system of the model axes. */
+typedef enum {
+    AWE_CART = 0, /* axes (z, x[, y]) - sfAWEFDcart{2D,3D}{gpu,cpu} */
+    AWE_SPHER = 1 /* axes (r, theta[, phi]) - sfAWEFDspher2Dgpu (polar), sfAWEFDspher3Dgpu */
+} awe_coords;
+
+/* Which reference program's scheme to follow. */
+typedef enum {
+    /* The GPU programs: 2nd-order Laplacian (cartesian, polar or spherical
+     * with metric terms), unscaled bilinear/trilinear injection into the
+     * current field before the update, quadratic-alpha sponge on both time
+     * levels, the one-way boundary and free-surface masks as those programs
+     * apply them. */
+    AWE_SCHEME_GPU = 0,
+    /* The cartesian CPU programs: 2N-order Laplacian (fdorder 2..20, optional
+     * least-squares coefficients, optional variable density), injection into
+     * the new field scaled by v^2 dt^2, Gaussian sponge + Clayton-Engquist
+     * one-way ABC (dabc=y) or the hybrid ABC (hybridbc=y). */
+    AWE_SCHEME_CPU = 1
+} awe_scheme;
+
+typedef enum {
+    AWE_FAST = 0, /* FP32 with fused multiply-adds */
+    AWE_EXACT = 1 /* FP32 in the reference CPU program's operation order and
+                     rounding (no contraction; its FP64 leapfrog sum emulated
+                     exactly in FP32 arithmetic) */
+} awe_precision;
+
+typedef struct {
+    int coords;    /* awe_coords */
+    int scheme;    /* awe_scheme */
+    int ndim;      /* 2 or 3 */
+    int n[3];      /* model size per axis (axis 1 fastest); n[2] = 1 in 2D */
+    float d[3];    /* spacing */
+    float o[3];    /* origin */
+    int nb;        /* padding / sponge width (nb=); < 0: the program default */
+    int nt;        /* time steps */
+    float dt;      /* time step */
+    int fdorder;   /* AWE_SCHEME_CPU: spatial order 2N (default 4); GPU: 2 */
+    int optfd;     /* AWE_SCHEME_CPU: least-squares optimal coefficients */
+    int dabc;      /* AWE_SCHEME_CPU: absorbing boundary */
+    int hybrid;    /* AWE_SCHEME_CPU: hybrid one-way ABC */
+    int fsrf;      /* free surface (free=) */
+    int expl;      /* CPU: one wavelet for all sources; GPU: reflectivity-scaled injection */
+    int refl;      /* AWE_SCHEME_GPU, cartesian 2D: injection scaled by an rfl image */
+    int jdata;     /* receiver sampling interval (jdata=), default 1 */
+    int jsnap;     /* snapshot interval; 0 = no snapshots */
+    int bnds;      /* snapshots include the padding (bnds=) */
+    int precision; /* awe_precision */
+} awe_desc;
+
+/* Derived sizes of a plan. */
+typedef struct {
+    int npad[3];       /* padded grid per axis (axis 1 fastest) */
+    int nbpad;         /* padding actually used */
+    int nsmp;          /* trace samples written by awe_forward */
+    int nsnap;         /* snapshots written by awe_forward */
+    size_t snap_elems; /* floats per snapshot */
+    size_t device_bytes; /* device memory held by the plan */
+} awe_info;
+
+typedef struct awe_plan awe_plan;
+
+/* Optional per-snapshot callback: frame is a host pointer valid during the call. */
+typedef void (*awe_snap_fn)(void *user, int isnap, int it, const float *frame, size_t nelem);
+
+const char *awe_version(void);
+const char *awe_last_error(void);
+const char *awe_status_string(awe_status s);
+
+awe_status awe_plan_create(const awe_desc *desc, int device, awe_plan **out);
+awe_status awe_plan_destroy(awe_plan *plan);
+awe_status awe_plan_info(const awe_plan *plan, awe_info *info);
+
+/* vel, den, rfl: host [n3][n2][n1] unpadded; den and rfl may be NULL. */
+awe_status awe_set_model(awe_plan *plan, const float *vel, const float *den, const float *rfl);
+
+/* Source and receiver coordinates, host, ndim floats per point in the
+ * reference's order: 2D (x, z) [polar: (r, theta)], 3D (x, y, z)
+ * [spherical: (r, phi, theta)]. */
+awe_status awe_set_geometry(awe_plan *plan, int ns, const float *sou, int nr, const float *rec);
+
+/* Host-buffer forward modelling: wav [nt][ncs] (ncs = 1 or ns); dat
+ * [nsmp][nr]; wfl (may be NULL) [nsnap][snap_elems].  Snapshots also go to
+ * the callback when one is set. */
+awe_status awe_forward(awe_plan *plan, const float *wav, int ncs, float *dat, float *wfl);
+
+/* Device-resident variant: d_wav, d_dat (and optional d_wfl) are device
+ * pointers; stream is a cudaStream_t (NULL = the plan's own stream).  The
+ * call is asynchronous with respect to the host when no snapshot callback is
+ * set. */
+awe_status awe_forward_device(awe_plan *plan, const float *d_wav, int ncs, float *d_dat, float *d_wfl,
+                              void *stream);
+
+awe_status awe_set_snapshot_callback(awe_plan *plan, awe_snap_fn fn, void *user);
+
+/* Waits for the plan's stream. */
+awe_status awe_synchronize(awe_plan *plan);
+
+/* Number of kernel launches issued by the last awe_forward / awe_forward_device. */
+long long awe_last_launch_count(const awe_plan *plan);
+
+/* Kernel timing: when enabled, the next forward run brackets every launch of
+ * the stencil (step) kernel with CUDA events on its stream; awe_profile_read
+ * returns their summed duration (ms) and the launch count after the run has
+ * completed.  Off by default. */
+awe_status awe_profile_enable(awe_plan *plan, int on);
+awe_status awe_profile_read(awe_plan *plan, double *step_kernel_ms, long long *step_launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

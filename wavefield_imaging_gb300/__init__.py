@@ -1,0 +1,13 @@
+"""GB300-native acoustic wave-propagation engine.
+
+Drop-in for the time-stepping path of Nacnud04/wavefield_imaging's
+sfAWEFD{cart,spher}{2D,3D}gpu programs (and the 2N-order scheme of its
+cartesian CPU programs): hand-written sm_103a CUDA kernels behind the C-ABI
+in include/awe.h, built into wavefield_imaging_gb300/_build/libawe.so.
+"""
+from .engine import (  # noqa: F401
+    CART, EXACT, FAST, SCHEME_CPU, SCHEME_GPU, SPHER, AweError, Desc, Plan, lib, make_desc,
+)
+
+__all__ = ["Plan", "Desc", "make_desc", "AweError", "lib", "CART", "SPHER", "SCHEME_CPU", "SCHEME_GPU", "FAST",
+           "EXACT"]

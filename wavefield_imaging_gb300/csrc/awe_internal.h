@@ -1,0 +1,98 @@
+// Internal declarations shared by the engine's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "awe.h"
+
+namespace awe {
+
+constexpr int kMaxNop = 10;  // fdorder <= 20, as the reference's optfd tables
+
+// Stencil coefficients, passed by value (kernel parameter space = constant bank).
+struct Coef {
+    float c0;                   // centre weight  (-2 * sum of all c)
+    float c[3][kMaxNop + 1];    // second-derivative weights / d^2 per axis (1..nop)
+    float b[3][kMaxNop + 1];    // first-derivative weights / d per axis (variable density)
+};
+
+// One interpolation point (source or receiver): flat index of the lowest
+// corner and the 4 (2D) or 8 (3D) weights in the reference's corner order.
+struct GeoPoint {
+    long long base;
+    float w[8];
+};
+
+// Padded grid, axis 1 fastest.
+struct Grid {
+    int n1, n2, n3;  // n3 = 1 in 2D
+    long long s2() const { return n1; }
+    long long s3() const { return (long long)n1 * n2; }
+    long long cells() const { return (long long)n1 * n2 * n3; }
+};
+
+// ---- scheme of the reference CPU programs (MAWEFDcart{2D,3D}cpu.c) ----
+struct StepBParams {
+    Grid g;
+    Coef k;
+    const float *w1, *w2, *w3;  // per-axis sponge factor (1 where undamped); null = no sponge
+    int damp_prev;              // prev level carries the sponge of the previous step
+    int sponge_new;             // apply the sponge to the new level in the step kernel
+    int shell;                  // cells within `shell` of a face are stored raw (boundary pass follows)
+};
+
+void launch_stepB(int ndim, int nop, bool exact, bool rho, const float *cur, float *nxt, const float *vel,
+                  const float *den, const StepBParams &p, cudaStream_t s);
+
+struct AbcB {
+    const float *zl, *zh;  // [n3][n2]
+    const float *xl, *xh;  // [n3][n1]
+    const float *yl, *yh;  // [n2][n1]
+};
+void launch_abconeB(int ndim, int nop, bool exact, int fsrf, float *uo, const float *um, const AbcB &a,
+                    const Grid &g, cudaStream_t s);
+void launch_hybridB(int ndim, int nop, int nbd, bool exact, int fsrf, float *uo, const float *um, const AbcB &a,
+                    const float *damp, const Grid &g, cudaStream_t s);
+void launch_band_sponge(int ndim, int width, bool exact, float *u, const float *w1, const float *w2,
+                        const float *w3, const Grid &g, cudaStream_t s);
+
+// injection into the new level scaled by vel (v^2 dt^2): u += (dd*w)*vel.
+// off[c] = flat offset of corner c from the point's base index.
+void launch_injectB_off(int ndim, bool exact, float *u, const float *vel, const GeoPoint *pts, int ns,
+                        const float *wav, int it, int ncs, bool one_wavelet, const long long *off, cudaStream_t s);
+
+// receiver gather; when w1 != null the sponge factors are applied to each node
+// value first (the field carries a pending sponge)
+void launch_extract_off(int ndim, bool exact, const float *u, const GeoPoint *pts, int nr, float *dat_row,
+                        const float *w1, const float *w2, const float *w3, const Grid &g, const long long *off,
+                        cudaStream_t s);
+
+// copy a window (or the whole padded grid) of u into dst, applying pending sponge
+void launch_snapshot(int ndim, const float *u, float *dst, const Grid &g, int f1, int f2, int f3, int m1, int m2,
+                     int m3, const float *w1, const float *w2, const float *w3, cudaStream_t s);
+
+// ---- host-side math (bit-identical to the reference's float evaluation) ----
+void fd_coefficients(int nop, int ndim, const float *dd, int optfd, Coef &k);
+void sponge_weights(int nb, std::vector<float> &w);   // fdutil.c sponge_make
+void hybrid_damp(int ntransit, std::vector<float> &w);  // MAWEFDcart*cpu.c damp_make
+// fdutil.c lint2d_make / lint3d_make for one point, in the reference's fdm
+// axes (z, x, y): origin of the padded grid, spacing, padded size.
+struct FdmAxes {
+    float oz, ox, oy, dz, dx, dy;
+    int nz, nx, ny;
+};
+struct Lint {
+    int jz, jx, jy;
+    float w[8];
+};
+Lint lint_make(int ndim, float x, float y, float z, const FdmAxes &f);
+void expand_model(int ndim, const float *a, float *b, int nb, const int *n);
+
+void set_error(const char *fmt, ...);
+
+}  // namespace awe

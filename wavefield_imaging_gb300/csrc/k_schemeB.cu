@@ -1,0 +1,441 @@
+// Kernels for the scheme of the reference's cartesian CPU programs
+// (CODE/MAWEFDcart{2D,3D}cpu.c + ts_kernel.c + fdutil.c): 2N-order
+// Laplacian, leapfrog in place over two time levels, Gaussian sponge,
+// Clayton-Engquist one-way ABC, v^2 dt^2-scaled injection.
+//
+// Time levels.  The reference keeps u0 (previous, overwritten by the new
+// level) and u1 (current); after the update and injection it applies the
+// ABC to u0 and the sponge to both u0 and u1, then swaps.  Here the sponge of
+// u1 is not written back: u1 is still being read by neighbouring cells, so
+// its sponge is applied when the value is next read (as "prev" in the next
+// step, or by the receiver gather / snapshot of this step).  The product is
+// the same float multiplication on the same value, so results are unchanged.
+// The new level is sponged in the step kernel except in the `shell` of cells
+// that the one-way ABC rewrites or reads, which the boundary kernels finish.
+#include <cuda_runtime.h>
+
+#include "awe_internal.h"
+#include "fp_exact.cuh"
+
+namespace awe {
+
+template <bool EXACT, int NDIM>
+__device__ __forceinline__ float damp_cell(float v, int i1, int i2, int i3, const float *__restrict__ w1,
+                                           const float *__restrict__ w2, const float *__restrict__ w3) {
+    // sponge3d_apply order: axis-1 faces, then axis 2, then axis 3
+    v = fmul<EXACT>(v, __ldg(w1 + i1));
+    v = fmul<EXACT>(v, __ldg(w2 + i2));
+    if constexpr (NDIM == 3) v = fmul<EXACT>(v, __ldg(w3 + i3));
+    return v;
+}
+
+// One time step, one thread per cell (grid: x = axis-1 tiles, y = axis 2, z = axis 3).
+template <int NOP, int NDIM, bool EXACT, bool RHO>
+__global__ void __launch_bounds__(256) k_stepB(const float *__restrict__ cur, float *__restrict__ nxt,
+                                               const float *__restrict__ vel, const float *__restrict__ rho,
+                                               const StepBParams p) {
+    const int i1 = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i2 = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i3 = (NDIM == 3) ? (int)blockIdx.z : 0;
+    const Grid g = p.g;
+    if (i1 >= g.n1 || i2 >= g.n2) return;
+    const long long s2 = g.n1, s3 = (long long)g.n1 * g.n2;
+    const long long i = i3 * s3 + i2 * s2 + i1;
+
+    float prv = nxt[i];
+    if (p.damp_prev) prv = damp_cell<EXACT, NDIM>(prv, i1, i2, i3, p.w1, p.w2, p.w3);
+
+    bool interior = i1 >= NOP && i1 < g.n1 - NOP && i2 >= NOP && i2 < g.n2 - NOP;
+    if (NDIM == 3) interior = interior && i3 >= NOP && i3 < g.n3 - NOP;
+    float out = prv;
+    if (interior) {
+        const float u = cur[i];
+        // ts_kernel.c:140-144 / :286-291: lap = u*c0 + sum_k [(z pair)*cz + (x pair)*cx (+ (y pair)*cy)]
+        float lap = fmul<EXACT>(u, p.k.c0);
+#pragma unroll
+        for (int k = 1; k <= NOP; k++) {
+            float t = fadd<EXACT>(fmul<EXACT>(fadd<EXACT>(__ldg(cur + i - k), __ldg(cur + i + k)), p.k.c[0][k]),
+                                  fmul<EXACT>(fadd<EXACT>(__ldg(cur + i - k * s2), __ldg(cur + i + k * s2)),
+                                              p.k.c[1][k]));
+            if constexpr (NDIM == 3)
+                t = fadd<EXACT>(
+                    t, fmul<EXACT>(fadd<EXACT>(__ldg(cur + i - k * s3), __ldg(cur + i + k * s3)), p.k.c[2][k]));
+            lap = fadd<EXACT>(lap, t);
+        }
+        if constexpr (RHO) {
+            // variable density, ts_kernel.c:145-155 / :292-305
+            float duz = 0.f, dux = 0.f, duy = 0.f, drz = 0.f, drx = 0.f, dry = 0.f;
+#pragma unroll
+            for (int k = 1; k <= NOP; k++) {
+                duz = fadd<EXACT>(duz, fmul<EXACT>(fsub<EXACT>(__ldg(cur + i + k), __ldg(cur + i - k)), p.k.b[0][k]));
+                dux = fadd<EXACT>(
+                    dux, fmul<EXACT>(fsub<EXACT>(__ldg(cur + i + k * s2), __ldg(cur + i - k * s2)), p.k.b[1][k]));
+                drz = fadd<EXACT>(drz, fmul<EXACT>(fsub<EXACT>(__ldg(rho + i + k), __ldg(rho + i - k)), p.k.b[0][k]));
+                drx = fadd<EXACT>(
+                    drx, fmul<EXACT>(fsub<EXACT>(__ldg(rho + i + k * s2), __ldg(rho + i - k * s2)), p.k.b[1][k]));
+                if constexpr (NDIM == 3) {
+                    duy = fadd<EXACT>(
+                        duy, fmul<EXACT>(fsub<EXACT>(__ldg(cur + i + k * s3), __ldg(cur + i - k * s3)), p.k.b[2][k]));
+                    dry = fadd<EXACT>(
+                        dry, fmul<EXACT>(fsub<EXACT>(__ldg(rho + i + k * s3), __ldg(rho + i - k * s3)), p.k.b[2][k]));
+                }
+            }
+            float dot = fadd<EXACT>(fmul<EXACT>(duz, drz), fmul<EXACT>(dux, drx));
+            if constexpr (NDIM == 3) dot = fadd<EXACT>(dot, fmul<EXACT>(duy, dry));
+            float q = EXACT ? __fdiv_rn(dot, __ldg(rho + i)) : dot / __ldg(rho + i);
+            lap = fsub<EXACT>(lap, q);
+        }
+        const float q = fmul<EXACT>(__ldg(vel + i), lap);
+        if constexpr (EXACT)
+            out = sum3_rn(q, __fadd_rn(u, u), -prv);
+        else
+            out = fmaf(__ldg(vel + i), lap, 2.f * u - prv);
+    }
+    if (p.sponge_new) {
+        bool raw = false;
+        if (p.shell > 0) {
+            const int s = p.shell;
+            raw = i1 < s || i1 >= g.n1 - s || i2 < s || i2 >= g.n2 - s;
+            if (NDIM == 3) raw = raw || i3 < s || i3 >= g.n3 - s;
+        }
+        if (!raw) out = damp_cell<EXACT, NDIM>(out, i1, i2, i3, p.w1, p.w2, p.w3);
+    }
+    nxt[i] = out;
+}
+
+template <int NOP, int NDIM, bool EXACT>
+static void dispatch_rho(bool rho, const float *cur, float *nxt, const float *vel, const float *den,
+                         const StepBParams &p, cudaStream_t s) {
+    dim3 block(64, 4, 1);
+    dim3 grid((p.g.n1 + 63) / 64, (p.g.n2 + 3) / 4, NDIM == 3 ? p.g.n3 : 1);
+    if (rho)
+        k_stepB<NOP, NDIM, EXACT, true><<<grid, block, 0, s>>>(cur, nxt, vel, den, p);
+    else
+        k_stepB<NOP, NDIM, EXACT, false><<<grid, block, 0, s>>>(cur, nxt, vel, den, p);
+}
+
+template <int NOP>
+static void dispatch_dim(int ndim, bool exact, bool rho, const float *cur, float *nxt, const float *vel,
+                         const float *den, const StepBParams &p, cudaStream_t s) {
+    if (ndim == 3) {
+        if (exact) dispatch_rho<NOP, 3, true>(rho, cur, nxt, vel, den, p, s);
+        else dispatch_rho<NOP, 3, false>(rho, cur, nxt, vel, den, p, s);
+    } else {
+        if (exact) dispatch_rho<NOP, 2, true>(rho, cur, nxt, vel, den, p, s);
+        else dispatch_rho<NOP, 2, false>(rho, cur, nxt, vel, den, p, s);
+    }
+}
+
+void launch_stepB(int ndim, int nop, bool exact, bool rho, const float *cur, float *nxt, const float *vel,
+                  const float *den, const StepBParams &p, cudaStream_t s) {
+    switch (nop) {
+        case 1: dispatch_dim<1>(ndim, exact, rho, cur, nxt, vel, den, p, s); break;
+        case 2: dispatch_dim<2>(ndim, exact, rho, cur, nxt, vel, den, p, s); break;
+        case 3: dispatch_dim<3>(ndim, exact, rho, cur, nxt, vel, den, p, s); break;
+        case 4: dispatch_dim<4>(ndim, exact, rho, cur, nxt, vel, den, p, s); break;
+        case 5: dispatch_dim<5>(ndim, exact, rho, cur, nxt, vel, den, p, s); break;
+        case 6: dispatch_dim<6>(ndim, exact, rho, cur, nxt, vel, den, p, s); break;
+        case 7: dispatch_dim<7>(ndim, exact, rho, cur, nxt, vel, den, p, s); break;
+        case 8: dispatch_dim<8>(ndim, exact, rho, cur, nxt, vel, den, p, s); break;
+        case 9: dispatch_dim<9>(ndim, exact, rho, cur, nxt, vel, den, p, s); break;
+        case 10: dispatch_dim<10>(ndim, exact, rho, cur, nxt, vel, den, p, s); break;
+        default: break;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// One-way ABC, abcone3d_apply (fdutil.c:2085-2177): three passes (axis 1,
+// axis 2, axis 3 faces), each a sequential sweep outward per line, as the
+// reference; a pass completes before the next reads its corners.
+template <bool EXACT>
+__device__ __forceinline__ float abc_update(float um_in, float um_c, float uo_in, float b) {
+    // uo = um[inner] + (um[c] - uo[inner]) * b
+    return fadd<EXACT>(um_in, fmul<EXACT>(fsub<EXACT>(um_c, uo_in), b));
+}
+
+template <bool EXACT>
+__global__ void k_abc_axis1(float *uo, const float *__restrict__ um, const float *__restrict__ bl,
+                            const float *__restrict__ bh, Grid g, int nop, int top) {
+    const long long line = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // (i3, i2)
+    if (line >= (long long)g.n2 * g.n3) return;
+    const long long c = line * g.n1;
+    const float l = bl[line], h = bh[line];
+    for (int iop = 0; iop < nop; iop++) {
+        if (top) {
+            int iz = nop - iop;
+            uo[c + iz] = abc_update<EXACT>(um[c + iz + 1], um[c + iz], uo[c + iz + 1], l);
+        }
+        int iz = g.n1 - nop + iop - 1;
+        uo[c + iz] = abc_update<EXACT>(um[c + iz - 1], um[c + iz], uo[c + iz - 1], h);
+    }
+}
+
+// axis-2 faces: one thread per (i3, i1); coefficients [n3][n1]
+template <bool EXACT>
+__global__ void k_abc_axis2(float *uo, const float *__restrict__ um, const float *__restrict__ bl,
+                            const float *__restrict__ bh, Grid g, int nop) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)g.n1 * g.n3) return;
+    const long long i3 = t / g.n1, i1 = t % g.n1;
+    const long long s2 = g.n1, base = i3 * g.n1 * (long long)g.n2 + i1;
+    const float l = bl[t], h = bh[t];
+    for (int iop = 0; iop < nop; iop++) {
+        long long c = base + (long long)(nop - iop) * s2;
+        uo[c] = abc_update<EXACT>(um[c + s2], um[c], uo[c + s2], l);
+        c = base + (long long)(g.n2 - nop + iop - 1) * s2;
+        uo[c] = abc_update<EXACT>(um[c - s2], um[c], uo[c - s2], h);
+    }
+}
+
+// axis-3 faces: one thread per (i2, i1); coefficients [n2][n1]
+template <bool EXACT>
+__global__ void k_abc_axis3(float *uo, const float *__restrict__ um, const float *__restrict__ bl,
+                            const float *__restrict__ bh, Grid g, int nop) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)g.n1 * g.n2) return;
+    const long long s3 = (long long)g.n1 * g.n2;
+    const float l = bl[t], h = bh[t];
+    for (int iop = 0; iop < nop; iop++) {
+        long long c = (long long)(nop - iop) * s3 + t;
+        uo[c] = abc_update<EXACT>(um[c + s3], um[c], uo[c + s3], l);
+        c = (long long)(g.n3 - nop + iop - 1) * s3 + t;
+        uo[c] = abc_update<EXACT>(um[c - s3], um[c], uo[c - s3], h);
+    }
+}
+
+void launch_abconeB(int ndim, int nop, bool exact, int fsrf, float *uo, const float *um, const AbcB &a,
+                    const Grid &g, cudaStream_t s) {
+    const int T = 128;
+    long long n = (long long)g.n2 * g.n3;
+    if (exact) k_abc_axis1<true><<<(n + T - 1) / T, T, 0, s>>>(uo, um, a.zl, a.zh, g, nop, !fsrf);
+    else k_abc_axis1<false><<<(n + T - 1) / T, T, 0, s>>>(uo, um, a.zl, a.zh, g, nop, !fsrf);
+    n = (long long)g.n1 * g.n3;
+    if (exact) k_abc_axis2<true><<<(n + T - 1) / T, T, 0, s>>>(uo, um, a.xl, a.xh, g, nop);
+    else k_abc_axis2<false><<<(n + T - 1) / T, T, 0, s>>>(uo, um, a.xl, a.xh, g, nop);
+    if (ndim == 3) {
+        n = (long long)g.n1 * g.n2;
+        if (exact) k_abc_axis3<true><<<(n + T - 1) / T, T, 0, s>>>(uo, um, a.yl, a.yh, g, nop);
+        else k_abc_axis3<false><<<(n + T - 1) / T, T, 0, s>>>(uo, um, a.yl, a.yh, g, nop);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Hybrid one-way ABC (apply_abc, MAWEFDcart2Dcpu.c:553-614 and
+// MAWEFDcart3Dcpu.c:533-625): the A1 update on the outer nop layers, then a
+// blend of the A1 value and the field over the next nbd-nop layers with
+// weights damp[ib]; free surface zeroes the first nbd+1 samples of axis 1.
+template <bool EXACT>
+__device__ __forceinline__ float blend(float bc, float u, float d) {
+    return fadd<EXACT>(fmul<EXACT>(bc, fsub<EXACT>(1.f, d)), fmul<EXACT>(u, d));
+}
+
+template <bool EXACT>
+__global__ void k_hybrid_axis(float *u2, const float *__restrict__ u1, const float *__restrict__ bl,
+                              const float *__restrict__ bh, const float *__restrict__ damp, Grid g, int axis,
+                              int nop, int nbd, int fsrf) {
+    // one thread per line along `axis`; line index enumerates the other two axes
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long nlines, base, stride;
+    int n;
+    if (axis == 1) {
+        nlines = (long long)g.n2 * g.n3;
+        if (t >= nlines) return;
+        base = t * g.n1;
+        stride = 1;
+        n = g.n1;
+    } else if (axis == 2) {
+        nlines = (long long)g.n1 * g.n3;
+        if (t >= nlines) return;
+        base = (t / g.n1) * g.n1 * (long long)g.n2 + t % g.n1;
+        stride = g.n1;
+        n = g.n2;
+    } else {
+        nlines = (long long)g.n1 * g.n2;
+        if (t >= nlines) return;
+        base = t;
+        stride = (long long)g.n1 * g.n2;
+        n = g.n3;
+    }
+    const float l = bl[t], h = bh[t];
+#define AT(a, k) a[base + (long long)(k) * stride]
+    for (int ib = nbd - nop; ib < nbd; ib++) {
+        int k = nbd - ib - 1;
+        AT(u2, k) = abc_update<EXACT>(AT(u1, k + 1), AT(u1, k), AT(u2, k + 1), l);
+        k = n - nbd + ib;
+        AT(u2, k) = abc_update<EXACT>(AT(u1, k - 1), AT(u1, k), AT(u2, k - 1), h);
+    }
+    if (damp)
+        for (int ib = 0; ib < nbd - nop; ib++) {
+            const float d = damp[ib];
+            int k = nbd - ib - 1;
+            float bc = abc_update<EXACT>(AT(u1, k + 1), AT(u1, k), AT(u2, k + 1), l);
+            AT(u2, k) = blend<EXACT>(bc, AT(u2, k), d);
+            k = n - nbd + ib;
+            bc = abc_update<EXACT>(AT(u1, k - 1), AT(u1, k), AT(u2, k - 1), h);
+            AT(u2, k) = blend<EXACT>(bc, AT(u2, k), d);
+        }
+    if (axis == 1 && fsrf)
+        for (int k = 0; k < nbd + 1; k++) AT(u2, k) = 0.f;
+#undef AT
+}
+
+void launch_hybridB(int ndim, int nop, int nbd, bool exact, int fsrf, float *uo, const float *um, const AbcB &a,
+                    const float *damp, const Grid &g, cudaStream_t s) {
+    const int T = 128;
+    const float *lo[3] = {a.zl, a.xl, a.yl}, *hi[3] = {a.zh, a.xh, a.yh};
+    long long nl[3] = {(long long)g.n2 * g.n3, (long long)g.n1 * g.n3, (long long)g.n1 * g.n2};
+    for (int ax = 1; ax <= ndim; ax++) {
+        long long n = nl[ax - 1];
+        if (exact)
+            k_hybrid_axis<true><<<(n + T - 1) / T, T, 0, s>>>(uo, um, lo[ax - 1], hi[ax - 1], damp, g, ax, nop, nbd,
+                                                              fsrf);
+        else
+            k_hybrid_axis<false><<<(n + T - 1) / T, T, 0, s>>>(uo, um, lo[ax - 1], hi[ax - 1], damp, g, ax, nop,
+                                                               nbd, fsrf);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Sponge over the cells within `width` of any face (each cell exactly once).
+template <bool EXACT, int NDIM>
+__global__ void k_band_sponge(float *u, const float *__restrict__ w1, const float *__restrict__ w2,
+                              const float *__restrict__ w3, Grid g, int width) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    // part A: axis-1 slabs (all i2, i3); part B: axis-2 slabs; part C: axis-3 slabs
+    const long long W = width, n1 = g.n1, n2 = g.n2, n3 = g.n3;
+    const long long inner1 = n1 - 2 * W, inner2 = n2 - 2 * W;
+    const long long nA = 2 * W * n2 * n3, nB = inner1 * 2 * W * n3, nC = (NDIM == 3) ? inner1 * inner2 * 2 * W : 0;
+    long long i1, i2, i3;
+    if (t < nA) {
+        long long k = t % (2 * W), r = t / (2 * W);
+        i1 = k < W ? k : n1 - 2 * W + k;
+        i2 = r % n2;
+        i3 = r / n2;
+    } else if (t < nA + nB) {
+        long long q = t - nA;
+        i1 = W + q % inner1;
+        long long r = q / inner1, k = r % (2 * W);
+        i2 = k < W ? k : n2 - 2 * W + k;
+        i3 = r / (2 * W);
+    } else if (t < nA + nB + nC) {
+        long long q = t - nA - nB;
+        i1 = W + q % inner1;
+        long long r = q / inner1;
+        i2 = W + r % inner2;
+        long long k = r / inner2;
+        i3 = k < W ? k : n3 - 2 * W + k;
+    } else
+        return;
+    const long long i = (i3 * n2 + i2) * n1 + i1;
+    u[i] = damp_cell<EXACT, NDIM>(u[i], (int)i1, (int)i2, (int)i3, w1, w2, w3);
+}
+
+void launch_band_sponge(int ndim, int width, bool exact, float *u, const float *w1, const float *w2, const float *w3,
+                        const Grid &g, cudaStream_t s) {
+    const long long W = width, n1 = g.n1, n2 = g.n2, n3 = g.n3;
+    long long total = 2 * W * n2 * n3 + (n1 - 2 * W) * 2 * W * n3;
+    if (ndim == 3) total += (n1 - 2 * W) * (n2 - 2 * W) * 2 * W;
+    const int T = 256;
+    long long blocks = (total + T - 1) / T;
+    if (ndim == 3) {
+        if (exact) k_band_sponge<true, 3><<<blocks, T, 0, s>>>(u, w1, w2, w3, g, width);
+        else k_band_sponge<false, 3><<<blocks, T, 0, s>>>(u, w1, w2, w3, g, width);
+    } else {
+        if (exact) k_band_sponge<true, 2><<<blocks, T, 0, s>>>(u, w1, w2, w3, g, width);
+        else k_band_sponge<false, 2><<<blocks, T, 0, s>>>(u, w1, w2, w3, g, width);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Injection into the new level, lint{2,3}d_inject[1]_with_vv
+// (fdutil.c:1688-1740): u[node] += (dd * w) * vel[node], sources and corners
+// in the reference's order (one thread, so coincident nodes add in order).
+template <bool EXACT>
+__global__ void k_injectB(float *u, const float *__restrict__ vel, const GeoPoint *__restrict__ pts, int ns,
+                          const float *__restrict__ wav, int it, int ncs, int one_wavelet, int ncorner,
+                          const long long *__restrict__ off) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    for (int s = 0; s < ns; s++) {
+        const float dd = one_wavelet ? wav[(long long)it * ncs] : wav[(long long)it * ncs + s];
+        const GeoPoint pt = pts[s];
+        for (int c = 0; c < ncorner; c++) {
+            const long long n = pt.base + off[c];
+            u[n] = fadd<EXACT>(u[n], fmul<EXACT>(fmul<EXACT>(dd, pt.w[c]), vel[n]));
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Receiver gather, lint{2,3}d_extract (fdutil.c:1596-1670):
+// d = sum_c u[node_c] * w_c, summed in corner order.
+template <bool EXACT, int NDIM>
+__global__ void k_extract(const float *__restrict__ u, const GeoPoint *__restrict__ pts, int nr, float *dat,
+                          const float *__restrict__ w1, const float *__restrict__ w2, const float *__restrict__ w3,
+                          Grid g, const long long *__restrict__ off) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nr) return;
+    const GeoPoint pt = pts[r];
+    constexpr int NC = NDIM == 3 ? 8 : 4;
+    float acc = 0.f;
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+        const long long n = pt.base + off[c];
+        float v = __ldg(u + n);
+        if (w1) {
+            const long long s3 = (long long)g.n1 * g.n2;
+            const int i3 = (int)(n / s3), rem = (int)(n % s3);
+            v = damp_cell<EXACT, NDIM>(v, rem % g.n1, rem / g.n1, i3, w1, w2, w3);
+        }
+        const float t = fmul<EXACT>(v, pt.w[c]);
+        acc = (c == 0) ? t : fadd<EXACT>(acc, t);
+    }
+    dat[r] = acc;
+}
+
+void launch_injectB_off(int ndim, bool exact, float *u, const float *vel, const GeoPoint *pts, int ns,
+                        const float *wav, int it, int ncs, bool one_wavelet, const long long *off, cudaStream_t s) {
+    if (ns <= 0) return;
+    const int nc = ndim == 3 ? 8 : 4;
+    if (exact) k_injectB<true><<<1, 32, 0, s>>>(u, vel, pts, ns, wav, it, ncs, one_wavelet, nc, off);
+    else k_injectB<false><<<1, 32, 0, s>>>(u, vel, pts, ns, wav, it, ncs, one_wavelet, nc, off);
+}
+
+void launch_extract_off(int ndim, bool exact, const float *u, const GeoPoint *pts, int nr, float *dat_row,
+                        const float *w1, const float *w2, const float *w3, const Grid &g, const long long *off,
+                        cudaStream_t s) {
+    if (nr <= 0) return;
+    const int T = 128, B = (nr + T - 1) / T;
+    if (ndim == 3) {
+        if (exact) k_extract<true, 3><<<B, T, 0, s>>>(u, pts, nr, dat_row, w1, w2, w3, g, off);
+        else k_extract<false, 3><<<B, T, 0, s>>>(u, pts, nr, dat_row, w1, w2, w3, g, off);
+    } else {
+        if (exact) k_extract<true, 2><<<B, T, 0, s>>>(u, pts, nr, dat_row, w1, w2, w3, g, off);
+        else k_extract<false, 2><<<B, T, 0, s>>>(u, pts, nr, dat_row, w1, w2, w3, g, off);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Snapshot: window [f .. f+m) of the padded grid (m = padded size for
+// bnds=y), pending sponge applied.
+template <int NDIM>
+__global__ void k_snapshot(const float *__restrict__ u, float *__restrict__ dst, Grid g, int f1, int f2, int f3,
+                           int m1, int m2, int m3, const float *__restrict__ w1, const float *__restrict__ w2,
+                           const float *__restrict__ w3) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)m1 * m2 * m3) return;
+    const int j1 = (int)(t % m1), j2 = (int)((t / m1) % m2), j3 = (int)(t / ((long long)m1 * m2));
+    const int i1 = f1 + j1, i2 = f2 + j2, i3 = f3 + j3;
+    float v = u[((long long)i3 * g.n2 + i2) * g.n1 + i1];
+    if (w1) v = damp_cell<true, NDIM>(v, i1, i2, i3, w1, w2, w3);
+    dst[t] = v;
+}
+
+void launch_snapshot(int ndim, const float *u, float *dst, const Grid &g, int f1, int f2, int f3, int m1, int m2,
+                     int m3, const float *w1, const float *w2, const float *w3, cudaStream_t s) {
+    const long long n = (long long)m1 * m2 * m3;
+    const int T = 256;
+    if (ndim == 3) k_snapshot<3><<<(n + T - 1) / T, T, 0, s>>>(u, dst, g, f1, f2, f3, m1, m2, m3, w1, w2, w3);
+    else k_snapshot<2><<<(n + T - 1) / T, T, 0, s>>>(u, dst, g, f1, f2, f3, m1, m2, m3, w1, w2, w3);
+}
+
+}  // namespace awe

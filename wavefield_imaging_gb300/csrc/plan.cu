@@ -1,0 +1,370 @@
+// C-ABI of the engine (include/awe.h): plan lifetime, model and geometry
+// upload, and the forward time loop.  The loop issues, per time step, the
+// fused step kernel and the few small kernels the reference's step order
+// needs around it (injection, boundary passes, receiver gather, snapshot).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "awe_internal.h"
+#include "plan_impl.h"
+
+namespace awe {
+const char *last_error();
+}
+
+using namespace awe;
+
+#define CUDA_TRY(expr)                                                                            \
+    do {                                                                                          \
+        cudaError_t e_ = (expr);                                                                  \
+        if (e_ != cudaSuccess) {                                                                  \
+            set_error("%s failed: %s (%s:%d)", #expr, cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return AWE_ERR_CUDA;                                                                  \
+        }                                                                                         \
+    } while (0)
+
+namespace awe {
+
+awe_status dev_alloc(awe_plan *p, void **ptr, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(ptr, bytes);
+    if (e != cudaSuccess) {
+        set_error("cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+        return AWE_ERR_NOMEM;
+    }
+    p->allocs.push_back({*ptr, bytes});
+    p->device_bytes += bytes;
+    return AWE_OK;
+}
+
+void dev_free(awe_plan *p, void *ptr) {
+    if (!ptr) return;
+    for (auto it = p->allocs.begin(); it != p->allocs.end(); ++it)
+        if (it->first == ptr) {
+            p->device_bytes -= it->second;
+            p->allocs.erase(it);
+            break;
+        }
+    cudaFree(ptr);
+}
+
+// Copy one snapshot frame to the host and hand it to the callback.
+awe_status deliver_snapshot(awe_plan *p, const float *d_frame, int isnap, int it, cudaStream_t s) {
+    if (!p->snap_cb) return AWE_OK;
+    const size_t bytes = p->snap_elems * sizeof(float);
+    if (p->h_pinned_bytes < bytes) {
+        if (p->h_pinned) cudaFreeHost(p->h_pinned);
+    for (cudaEvent_t e : p->prof_ev) cudaEventDestroy(e);
+        p->h_pinned = nullptr;
+        p->h_pinned_bytes = 0;
+        if (cudaMallocHost((void **)&p->h_pinned, bytes) != cudaSuccess) {
+            set_error("pinned snapshot buffer (%zu bytes) failed", bytes);
+            return AWE_ERR_NOMEM;
+        }
+        p->h_pinned_bytes = bytes;
+    }
+    CUDA_TRY(cudaMemcpyAsync(p->h_pinned, d_frame, bytes, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    p->snap_cb(p->snap_user, isnap, it, p->h_pinned, p->snap_elems);
+    return AWE_OK;
+}
+
+void prof_begin(awe_plan *p, cudaStream_t s) {
+    if (!p->profile) return;
+    const size_t need = 2 * (size_t)(p->prof_n + 1);
+    while (p->prof_ev.size() < need) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) {
+            p->profile = false;
+            return;
+        }
+        p->prof_ev.push_back(e);
+    }
+    cudaEventRecord(p->prof_ev[2 * p->prof_n], s);
+}
+
+void prof_end(awe_plan *p, cudaStream_t s) {
+    if (!p->profile || p->prof_ev.size() < 2 * (size_t)(p->prof_n + 1)) return;
+    cudaEventRecord(p->prof_ev[2 * p->prof_n + 1], s);
+    p->prof_n++;
+}
+
+}  // namespace awe
+
+static awe_status check_desc(const awe_desc *d) {
+    if (!d) {
+        set_error("null descriptor");
+        return AWE_ERR_INVALID;
+    }
+    if (d->ndim != 2 && d->ndim != 3) {
+        set_error("ndim must be 2 or 3 (got %d)", d->ndim);
+        return AWE_ERR_INVALID;
+    }
+    for (int a = 0; a < d->ndim; a++) {
+        if (d->n[a] < 1) {
+            set_error("axis %d has n=%d", a + 1, d->n[a]);
+            return AWE_ERR_INVALID;
+        }
+        if (!(d->d[a] > 0.f)) {
+            set_error("axis %d has spacing %g", a + 1, (double)d->d[a]);
+            return AWE_ERR_INVALID;
+        }
+    }
+    if (d->nt < 1 || !(d->dt > 0.f)) {
+        set_error("need nt >= 1 and dt > 0 (nt=%d dt=%g)", d->nt, (double)d->dt);
+        return AWE_ERR_INVALID;
+    }
+    if (d->scheme != AWE_SCHEME_CPU && d->scheme != AWE_SCHEME_GPU) {
+        set_error("unknown scheme %d", d->scheme);
+        return AWE_ERR_INVALID;
+    }
+    if (d->coords != AWE_CART && d->coords != AWE_SPHER) {
+        set_error("unknown coordinate system %d", d->coords);
+        return AWE_ERR_INVALID;
+    }
+    if (d->scheme == AWE_SCHEME_CPU) {
+        if (d->coords != AWE_CART) {
+            set_error("the 2N-order CPU scheme is cartesian only (as MAWEFDcart*cpu.c)");
+            return AWE_ERR_UNSUPPORTED;
+        }
+        int fo = d->fdorder ? d->fdorder : 4;
+        if (fo < 2 || fo > 2 * kMaxNop || (fo & 1)) {
+            set_error("fdorder must be even in [2, %d] (got %d)", 2 * kMaxNop, fo);
+            return AWE_ERR_INVALID;
+        }
+    } else {
+        if (d->fdorder != 0 && d->fdorder != 2) {
+            set_error("the GPU programs' scheme is second order (fdorder=%d)", d->fdorder);
+            return AWE_ERR_UNSUPPORTED;
+        }
+    }
+    if (d->jsnap < 0 || d->jdata < 0) {
+        set_error("jsnap and jdata must be >= 0");
+        return AWE_ERR_INVALID;
+    }
+    return AWE_OK;
+}
+
+extern "C" {
+
+const char *awe_version(void) { return "awe-gb300 1.0 (sm_103a)"; }
+const char *awe_last_error(void) { return awe::last_error(); }
+
+const char *awe_status_string(awe_status s) {
+    switch (s) {
+        case AWE_OK: return "ok";
+        case AWE_ERR_INVALID: return "invalid argument";
+        case AWE_ERR_CUDA: return "CUDA error";
+        case AWE_ERR_NOMEM: return "out of memory";
+        case AWE_ERR_UNSUPPORTED: return "unsupported";
+        case AWE_ERR_NODEVICE: return "no CUDA device";
+        case AWE_ERR_STATE: return "call out of order";
+    }
+    return "unknown";
+}
+
+awe_status awe_plan_create(const awe_desc *desc, int device, awe_plan **out) {
+    if (!out) {
+        set_error("null output pointer");
+        return AWE_ERR_INVALID;
+    }
+    *out = nullptr;
+    awe_status st = check_desc(desc);
+    if (st != AWE_OK) return st;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        set_error("no CUDA device visible");
+        return AWE_ERR_NODEVICE;
+    }
+    if (device < 0 || device >= ndev) {
+        set_error("device %d out of range (%d devices)", device, ndev);
+        return AWE_ERR_INVALID;
+    }
+    CUDA_TRY(cudaSetDevice(device));
+    awe_plan *p = new awe_plan();
+    p->d = *desc;
+    p->device = device;
+    if (p->d.jdata <= 0) p->d.jdata = 1;
+    if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete p;
+        set_error("cudaStreamCreate failed");
+        return AWE_ERR_CUDA;
+    }
+    st = (p->d.scheme == AWE_SCHEME_CPU) ? planB_init(p) : planA_init(p);
+    if (st != AWE_OK) {
+        awe_plan_destroy(p);
+        return st;
+    }
+    *out = p;
+    return AWE_OK;
+}
+
+awe_status awe_plan_destroy(awe_plan *p) {
+    if (!p) return AWE_OK;
+    cudaSetDevice(p->device);
+    if (p->stream) cudaStreamSynchronize(p->stream);
+    for (auto &a : p->allocs) cudaFree(a.first);
+    p->allocs.clear();
+    if (p->h_pinned) cudaFreeHost(p->h_pinned);
+    for (cudaEvent_t e : p->prof_ev) cudaEventDestroy(e);
+    if (p->stream) cudaStreamDestroy(p->stream);
+    delete p;
+    return AWE_OK;
+}
+
+awe_status awe_plan_info(const awe_plan *p, awe_info *info) {
+    if (!p || !info) {
+        set_error("null argument");
+        return AWE_ERR_INVALID;
+    }
+    info->npad[0] = p->g.n1;
+    info->npad[1] = p->g.n2;
+    info->npad[2] = p->g.n3;
+    info->nbpad = p->nbd;
+    info->nsmp = p->nsmp;
+    info->nsnap = p->nsnap;
+    info->snap_elems = p->snap_elems;
+    info->device_bytes = p->device_bytes;
+    return AWE_OK;
+}
+
+awe_status awe_set_model(awe_plan *p, const float *vel, const float *den, const float *rfl) {
+    if (!p || !vel) {
+        set_error("null plan or velocity");
+        return AWE_ERR_INVALID;
+    }
+    CUDA_TRY(cudaSetDevice(p->device));
+    awe_status st = (p->d.scheme == AWE_SCHEME_CPU) ? planB_model(p, vel, den) : planA_model(p, vel, rfl);
+    if (st == AWE_OK) p->model_set = true;
+    return st;
+}
+
+awe_status awe_set_geometry(awe_plan *p, int ns, const float *sou, int nr, const float *rec) {
+    if (!p || ns < 0 || nr < 0 || (ns > 0 && !sou) || (nr > 0 && !rec)) {
+        set_error("bad geometry arguments");
+        return AWE_ERR_INVALID;
+    }
+    CUDA_TRY(cudaSetDevice(p->device));
+    awe_status st = set_geometry_common(p, ns, sou, nr, rec);
+    if (st == AWE_OK) p->geom_set = true;
+    return st;
+}
+
+awe_status awe_set_snapshot_callback(awe_plan *p, awe_snap_fn fn, void *user) {
+    if (!p) {
+        set_error("null plan");
+        return AWE_ERR_INVALID;
+    }
+    p->snap_cb = fn;
+    p->snap_user = user;
+    return AWE_OK;
+}
+
+awe_status awe_synchronize(awe_plan *p) {
+    if (!p) return AWE_ERR_INVALID;
+    CUDA_TRY(cudaSetDevice(p->device));
+    CUDA_TRY(cudaStreamSynchronize(p->stream));
+    return AWE_OK;
+}
+
+long long awe_last_launch_count(const awe_plan *p) { return p ? p->launches : -1; }
+
+awe_status awe_profile_enable(awe_plan *p, int on) {
+    if (!p) return AWE_ERR_INVALID;
+    p->profile = on != 0;
+    p->prof_n = 0;
+    return AWE_OK;
+}
+
+awe_status awe_profile_read(awe_plan *p, double *ms, long long *n) {
+    if (!p || !ms || !n) return AWE_ERR_INVALID;
+    CUDA_TRY(cudaSetDevice(p->device));
+    double total = 0.0;
+    for (long long i = 0; i < p->prof_n; i++) {
+        float t = 0.f;
+        CUDA_TRY(cudaEventSynchronize(p->prof_ev[2 * i + 1]));
+        CUDA_TRY(cudaEventElapsedTime(&t, p->prof_ev[2 * i], p->prof_ev[2 * i + 1]));
+        total += t;
+    }
+    *ms = total;
+    *n = p->prof_n;
+    p->prof_n = 0;
+    return AWE_OK;
+}
+
+awe_status awe_forward_device(awe_plan *p, const float *d_wav, int ncs, float *d_dat, float *d_wfl, void *stream) {
+    if (!p || !d_wav || !d_dat) {
+        set_error("null plan, wavelet or data pointer");
+        return AWE_ERR_INVALID;
+    }
+    if (!p->model_set || !p->geom_set) {
+        set_error("awe_set_model and awe_set_geometry must precede awe_forward");
+        return AWE_ERR_STATE;
+    }
+    if (ncs != 1 && ncs != p->ns) {
+        set_error("wavelet has %d components; need 1 or ns=%d", ncs, p->ns);
+        return AWE_ERR_INVALID;
+    }
+    CUDA_TRY(cudaSetDevice(p->device));
+    cudaStream_t s = stream ? (cudaStream_t)stream : p->stream;
+    awe_status st = (p->d.scheme == AWE_SCHEME_CPU) ? planB_run(p, d_wav, ncs, d_dat, d_wfl, s)
+                                                     : planA_run(p, d_wav, ncs, d_dat, d_wfl, s);
+    if (st != AWE_OK) return st;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error("kernel launch failed: %s", cudaGetErrorString(e));
+        return AWE_ERR_CUDA;
+    }
+    return AWE_OK;
+}
+
+awe_status awe_forward(awe_plan *p, const float *wav, int ncs, float *dat, float *wfl) {
+    if (!p || !wav || !dat) {
+        set_error("null plan, wavelet or data pointer");
+        return AWE_ERR_INVALID;
+    }
+    if (!p->model_set || !p->geom_set) {
+        set_error("awe_set_model and awe_set_geometry must precede awe_forward");
+        return AWE_ERR_STATE;
+    }
+    CUDA_TRY(cudaSetDevice(p->device));
+    const size_t wav_bytes = (size_t)p->d.nt * ncs * sizeof(float);
+    const size_t dat_bytes = (size_t)p->nsmp * p->nr * sizeof(float);
+    float *d_wav = nullptr, *d_dat = nullptr, *d_wfl = nullptr;
+    awe_status st = dev_alloc(p, (void **)&d_wav, wav_bytes);
+    if (st == AWE_OK) st = dev_alloc(p, (void **)&d_dat, dat_bytes);
+    if (st == AWE_OK && wfl && p->nsnap > 0) st = dev_alloc(p, (void **)&d_wfl, p->nsnap * p->snap_elems * sizeof(float));
+    if (st == AWE_OK) {
+        cudaError_t e = cudaMemcpyAsync(d_wav, wav, wav_bytes, cudaMemcpyHostToDevice, p->stream);
+        if (e != cudaSuccess) {
+            set_error("wavelet upload failed: %s", cudaGetErrorString(e));
+            st = AWE_ERR_CUDA;
+        }
+    }
+    if (st == AWE_OK) st = awe_forward_device(p, d_wav, ncs, d_dat, d_wfl, nullptr);
+    if (st == AWE_OK) {
+        cudaError_t e = cudaMemcpyAsync(dat, d_dat, dat_bytes, cudaMemcpyDeviceToHost, p->stream);
+        if (e == cudaSuccess && d_wfl)
+            e = cudaMemcpyAsync(wfl, d_wfl, p->nsnap * p->snap_elems * sizeof(float), cudaMemcpyDeviceToHost,
+                                p->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+        if (e != cudaSuccess) {
+            set_error("result download failed: %s", cudaGetErrorString(e));
+            st = AWE_ERR_CUDA;
+        }
+    }
+    cudaStreamSynchronize(p->stream);
+    dev_free(p, d_wav);
+    dev_free(p, d_dat);
+    dev_free(p, d_wfl);
+    return st;
+}
+
+}  // extern "C"

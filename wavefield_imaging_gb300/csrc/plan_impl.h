@@ -1,0 +1,81 @@
+// The plan object behind the opaque awe_plan handle.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <utility>
+#include <vector>
+
+#include "awe_internal.h"
+
+struct awe_plan {
+    awe_desc d{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<std::pair<void *, size_t>> allocs;  // device allocations owned by the plan
+    size_t device_bytes = 0;
+
+    // grid
+    int ndim = 2, nop = 1, nbd = 0;
+    awe::Grid g{};          // padded, axis 1 fastest
+    float opad[3] = {0, 0, 0};  // padded origin per axis
+    awe::Coef k{};
+    int nsmp = 0, nsnap = 0;
+    size_t snap_elems = 0;
+    int snap_f[3] = {0, 0, 0}, snap_m[3] = {1, 1, 1};  // snapshot window in padded indices
+
+    // fields and model (device)
+    float *u[2] = {nullptr, nullptr};
+    float *vel = nullptr;  // scheme CPU: v^2 dt^2; scheme GPU: v
+    float *den = nullptr;
+    float *rfl = nullptr;
+    float *w[3] = {nullptr, nullptr, nullptr};  // per-axis sponge factors
+    float *abc[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    float *damp = nullptr;
+    std::vector<float> h_vel_raw;  // padded raw velocity (scheme GPU injection reflectivity, ABC tables)
+
+    // geometry
+    int ns = 0, nr = 0;
+    awe::GeoPoint *src = nullptr, *rec = nullptr;
+    long long *corner_off = nullptr;  // device [8]
+    long long h_corner_off[8] = {0};
+    std::vector<awe::GeoPoint> h_src, h_rec;
+    bool sponge_deferred = false;  // a source node lies in the sponge band outside the boundary shell
+
+    // scheme-GPU specific
+    float *aux = nullptr;  // scratch for boundary passes
+    float *metric = nullptr;  // per-index metric tables (spherical)
+
+    bool model_set = false, geom_set = false;
+    awe_snap_fn snap_cb = nullptr;
+    void *snap_user = nullptr;
+    float *h_pinned = nullptr;
+    size_t h_pinned_bytes = 0;
+    float *d_snap_tmp = nullptr;
+    long long launches = 0;
+
+    // optional per-launch timing of the step kernel
+    bool profile = false;
+    std::vector<cudaEvent_t> prof_ev;  // pairs (start, stop)
+    long long prof_n = 0;
+};
+
+namespace awe {
+awe_status dev_alloc(awe_plan *p, void **ptr, size_t bytes);
+void dev_free(awe_plan *p, void *ptr);
+awe_status deliver_snapshot(awe_plan *p, const float *d_frame, int isnap, int it, cudaStream_t s);
+
+awe_status set_geometry_common(awe_plan *p, int ns, const float *sou, int nr, const float *rec);
+
+// bracket one step-kernel launch with events when profiling is on
+void prof_begin(awe_plan *p, cudaStream_t s);
+void prof_end(awe_plan *p, cudaStream_t s);
+
+awe_status planB_init(awe_plan *p);
+awe_status planB_model(awe_plan *p, const float *vel, const float *den);
+awe_status planB_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, float *d_wfl, cudaStream_t s);
+
+awe_status planA_init(awe_plan *p);
+awe_status planA_model(awe_plan *p, const float *vel, const float *rfl);
+awe_status planA_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, float *d_wfl, cudaStream_t s);
+}  // namespace awe

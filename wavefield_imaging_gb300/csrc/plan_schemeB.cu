@@ -1,0 +1,320 @@
+// Host side of the CPU-program scheme (MAWEFDcart{2D,3D}cpu.c): padding,
+// coefficient tables, model preparation and the per-step launch sequence.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "awe_internal.h"
+#include "plan_impl.h"
+
+namespace awe {
+
+#define CUDA_TRY(expr)                                                                            \
+    do {                                                                                          \
+        cudaError_t e_ = (expr);                                                                  \
+        if (e_ != cudaSuccess) {                                                                  \
+            set_error("%s failed: %s (%s:%d)", #expr, cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return AWE_ERR_CUDA;                                                                  \
+        }                                                                                         \
+    } while (0)
+#define AWE_TRY(expr)                      \
+    do {                                   \
+        awe_status s_ = (expr);            \
+        if (s_ != AWE_OK) return s_;       \
+    } while (0)
+
+// cut2d / cut3d_slice first index (fdutil.c:574-717): floor((o - opad)/d) in float
+static int window_first(float o, float opad, float d) { return (int)(std::floor)((o - opad) / d); }
+
+static awe_status upload(awe_plan *p, float **dst, const float *src, size_t n) {
+    if (!*dst) AWE_TRY(dev_alloc(p, (void **)dst, n * sizeof(float)));
+    CUDA_TRY(cudaMemcpy(*dst, src, n * sizeof(float), cudaMemcpyHostToDevice));
+    return AWE_OK;
+}
+
+awe_status planB_init(awe_plan *p) {
+    awe_desc &d = p->d;
+    if (d.fdorder == 0) d.fdorder = 4;  // MAWEFDcart2Dcpu.c:126
+    p->ndim = d.ndim;
+    p->nop = d.fdorder / 2;
+    int nb = d.nb;
+    if (nb < p->nop) nb = p->nop;                              // :211
+    if (d.dabc && d.hybrid && nb <= p->nop) nb = 2 * p->nop;  // :212
+    p->nbd = nb;
+    const int n3 = d.ndim == 3 ? d.n[2] : 1;
+    p->g = Grid{d.n[0] + 2 * nb, d.n[1] + 2 * nb, d.ndim == 3 ? n3 + 2 * nb : 1};
+    for (int a = 0; a < d.ndim; a++) p->opad[a] = d.o[a] - nb * d.d[a];  // fdutil_init
+    float dd[3] = {d.d[0], d.d[1], d.ndim == 3 ? d.d[2] : 1.f};
+    fd_coefficients(p->nop, d.ndim, dd, d.optfd, p->k);
+
+    const size_t cells = (size_t)p->g.cells();
+    AWE_TRY(dev_alloc(p, (void **)&p->u[0], cells * sizeof(float)));
+    AWE_TRY(dev_alloc(p, (void **)&p->u[1], cells * sizeof(float)));
+    AWE_TRY(dev_alloc(p, (void **)&p->vel, cells * sizeof(float)));
+    AWE_TRY(dev_alloc(p, (void **)&p->corner_off, 8 * sizeof(long long)));
+
+    if (d.dabc && !d.hybrid) {
+        std::vector<float> w;
+        sponge_weights(nb, w);
+        const int len[3] = {p->g.n1, p->g.n2, p->g.n3};
+        for (int a = 0; a < 3; a++) {
+            std::vector<float> t(len[a], 1.f);
+            if (a < d.ndim)
+                for (int i = 0; i < nb && i < len[a]; i++) {
+                    t[i] = w[nb - i - 1];
+                    t[len[a] - 1 - i] = w[nb - i - 1];
+                }
+            AWE_TRY(upload(p, &p->w[a], t.data(), t.size()));
+        }
+    }
+    if (d.dabc && d.hybrid && nb - p->nop > 0) {
+        std::vector<float> dm;
+        hybrid_damp(nb - p->nop, dm);
+        AWE_TRY(upload(p, &p->damp, dm.data(), dm.size()));
+    }
+
+    p->nsmp = (d.nt - 1) / d.jdata + 1;
+    p->nsnap = d.jsnap > 0 ? (d.nt - 1) / d.jsnap + 1 : 0;
+    for (int a = 0; a < 3; a++) {
+        const int npad = a == 0 ? p->g.n1 : a == 1 ? p->g.n2 : p->g.n3;
+        if (a >= d.ndim) {
+            p->snap_f[a] = 0;
+            p->snap_m[a] = 1;
+        } else if (d.bnds) {
+            p->snap_f[a] = 0;
+            p->snap_m[a] = npad;
+        } else {
+            p->snap_f[a] = window_first(d.o[a], p->opad[a], d.d[a]);
+            p->snap_m[a] = d.n[a];
+        }
+    }
+    p->snap_elems = (size_t)p->snap_m[0] * p->snap_m[1] * p->snap_m[2];
+    return AWE_OK;
+}
+
+awe_status planB_model(awe_plan *p, const float *vel, const float *den) {
+    const awe_desc &d = p->d;
+    const Grid &g = p->g;
+    const size_t cells = (size_t)g.cells();
+    std::vector<float> v(cells);
+    expand_model(d.ndim, vel, v.data(), p->nbd, d.n);
+    const float dt = d.dt;
+    const int nb = p->nbd;
+    if (d.dabc) {
+        // abcone2d_make / abcone3d_make(nbd, dt, vel) on the raw velocity
+        // (fdutil.c:1919-2019): b = (1 - v dt/d) / (1 + v dt/d) at the first
+        // interior sample of each face
+        const long long s2 = g.n1, s3 = (long long)g.n1 * g.n2;
+        std::vector<float> zl((size_t)g.n2 * g.n3), zh(zl.size()), xl((size_t)g.n1 * g.n3), xh(xl.size()),
+            yl((size_t)g.n1 * g.n2), yh(yl.size());
+        auto coef = [](float vv, float dt_, float dd) {
+            float q = vv * dt_ / dd;
+            return (1 - q) / (1 + q);
+        };
+        for (int i3 = 0; i3 < g.n3; i3++)
+            for (int i2 = 0; i2 < g.n2; i2++) {
+                zl[(size_t)i3 * g.n2 + i2] = coef(v[i3 * s3 + i2 * s2 + nb], dt, d.d[0]);
+                zh[(size_t)i3 * g.n2 + i2] = coef(v[i3 * s3 + i2 * s2 + g.n1 - nb - 1], dt, d.d[0]);
+            }
+        for (int i3 = 0; i3 < g.n3; i3++)
+            for (int i1 = 0; i1 < g.n1; i1++) {
+                xl[(size_t)i3 * g.n1 + i1] = coef(v[i3 * s3 + nb * s2 + i1], dt, d.d[1]);
+                xh[(size_t)i3 * g.n1 + i1] = coef(v[i3 * s3 + (g.n2 - nb - 1) * s2 + i1], dt, d.d[1]);
+            }
+        if (d.ndim == 3)
+            for (int i2 = 0; i2 < g.n2; i2++)
+                for (int i1 = 0; i1 < g.n1; i1++) {
+                    yl[(size_t)i2 * g.n1 + i1] = coef(v[nb * s3 + i2 * s2 + i1], dt, d.d[2]);
+                    yh[(size_t)i2 * g.n1 + i1] = coef(v[(g.n3 - nb - 1) * s3 + i2 * s2 + i1], dt, d.d[2]);
+                }
+        AWE_TRY(upload(p, &p->abc[0], zl.data(), zl.size()));
+        AWE_TRY(upload(p, &p->abc[1], zh.data(), zh.size()));
+        AWE_TRY(upload(p, &p->abc[2], xl.data(), xl.size()));
+        AWE_TRY(upload(p, &p->abc[3], xh.data(), xh.size()));
+        if (d.ndim == 3) {
+            AWE_TRY(upload(p, &p->abc[4], yl.data(), yl.size()));
+            AWE_TRY(upload(p, &p->abc[5], yh.data(), yh.size()));
+        }
+    }
+    // v <- v^2 dt^2 (MAWEFDcart2Dcpu.c:290-291); free surface zeroes the
+    // first nb+1 samples of every axis-1 line (:292-295)
+    const float dt2 = dt * dt;
+    for (size_t i = 0; i < cells; i++) v[i] *= v[i] * dt2;
+    if (d.fsrf && !d.hybrid)
+        for (size_t line = 0; line < (size_t)g.n2 * g.n3; line++)
+            for (int i1 = 0; i1 < nb + 1 && i1 < g.n1; i1++) v[line * g.n1 + i1] = 0.f;
+    AWE_TRY(upload(p, &p->vel, v.data(), cells));
+    if (den) {
+        std::vector<float> r(cells);
+        expand_model(d.ndim, den, r.data(), p->nbd, d.n);
+        AWE_TRY(upload(p, &p->den, r.data(), cells));
+    }
+    return AWE_OK;
+}
+
+awe_status set_geometry_common(awe_plan *p, int ns, const float *sou, int nr, const float *rec) {
+    const awe_desc &d = p->d;
+    const Grid &g = p->g;
+    const int nd = d.ndim;
+    const long long s2 = g.n1, s3 = (long long)g.n1 * g.n2;
+    const bool spher = d.coords == AWE_SPHER;
+    // reference fdm axes: cartesian z=axis1, x=axis2, y=axis3; spherical
+    // programs map z=theta (axis 2), x=r (axis 1), y=phi (axis 3)
+    // (MAWEFDspher3Dgpu.cu:167-173, MAWEFDspher2Dgpu.cu:151)
+    FdmAxes f{};
+    long long sz, sx, sy;
+    if (!spher) {
+        f = FdmAxes{p->opad[0], p->opad[1], p->opad[2], d.d[0], d.d[1], nd == 3 ? d.d[2] : 1.f, g.n1, g.n2, g.n3};
+        sz = 1;
+        sx = s2;
+        sy = s3;
+    } else {
+        f = FdmAxes{p->opad[1], p->opad[0], p->opad[2], d.d[1], d.d[0], nd == 3 ? d.d[2] : 1.f, g.n2, g.n1, g.n3};
+        sz = s2;
+        sx = 1;
+        sy = s3;
+    }
+    // corner order of lint*_make weights: (z, x[, y]) bits 001=z, 010=x, 100=y
+    long long off[8];
+    for (int c = 0; c < 8; c++) off[c] = ((c & 1) ? sz : 0) + ((c & 2) ? sx : 0) + ((c & 4) ? sy : 0);
+    std::memcpy(p->h_corner_off, off, sizeof off);
+    CUDA_TRY(cudaMemcpy(p->corner_off, off, sizeof off, cudaMemcpyHostToDevice));
+
+    auto make = [&](const float *xyz, int n, std::vector<GeoPoint> &out) {
+        out.resize(n);
+        for (int i = 0; i < n; i++) {
+            float x, y = 0.f, z;
+            if (nd == 2) {
+                x = xyz[2 * i];
+                z = xyz[2 * i + 1];
+            } else {
+                x = xyz[3 * i];
+                y = xyz[3 * i + 1];
+                z = xyz[3 * i + 2];
+            }
+            Lint l = lint_make(nd, x, y, z, f);
+            GeoPoint gp;
+            gp.base = l.jz * sz + l.jx * sx + (nd == 3 ? l.jy * sy : 0);
+            std::memcpy(gp.w, l.w, sizeof gp.w);
+            out[i] = gp;
+        }
+    };
+    make(sou, ns, p->h_src);
+    make(rec, nr, p->h_rec);
+    if (p->src) dev_free(p, p->src);
+    if (p->rec) dev_free(p, p->rec);
+    p->src = p->rec = nullptr;
+    AWE_TRY(dev_alloc(p, (void **)&p->src, (ns > 0 ? ns : 1) * sizeof(GeoPoint)));
+    AWE_TRY(dev_alloc(p, (void **)&p->rec, (nr > 0 ? nr : 1) * sizeof(GeoPoint)));
+    if (ns) CUDA_TRY(cudaMemcpy(p->src, p->h_src.data(), ns * sizeof(GeoPoint), cudaMemcpyHostToDevice));
+    if (nr) CUDA_TRY(cudaMemcpy(p->rec, p->h_rec.data(), nr * sizeof(GeoPoint), cudaMemcpyHostToDevice));
+    p->ns = ns;
+    p->nr = nr;
+
+    // scheme CPU: a source node inside the sponge band but outside the
+    // boundary shell would be sponged before its injection by the fused
+    // step; such runs defer the whole sponge to after the injection
+    p->sponge_deferred = false;
+    if (d.scheme == AWE_SCHEME_CPU && d.dabc && !d.hybrid) {
+        const int shell = (nd == 3) ? p->nop + 2 : 0;
+        const int nc = nd == 3 ? 8 : 4;
+        for (const GeoPoint &gp : p->h_src)
+            for (int c = 0; c < nc; c++) {
+                if (gp.w[c] == 0.f) continue;
+                const long long n = gp.base + off[c];
+                const int i3 = (int)(n / s3), i2 = (int)((n % s3) / s2), i1 = (int)(n % s2);
+                const int ii[3] = {i1, i2, i3}, nn[3] = {g.n1, g.n2, g.n3};
+                bool band = false, inshell = false;
+                for (int a = 0; a < nd; a++) {
+                    const int dist = std::min(ii[a], nn[a] - 1 - ii[a]);
+                    band = band || dist < p->nbd;
+                    inshell = inshell || dist < shell;
+                }
+                if (band && !inshell) p->sponge_deferred = true;
+            }
+    }
+    return AWE_OK;
+}
+
+awe_status planB_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, float *d_wfl, cudaStream_t s) {
+    const awe_desc &d = p->d;
+    const Grid &g = p->g;
+    const bool exact = d.precision == AWE_EXACT;
+    const bool sponge = d.dabc && !d.hybrid;
+    const int shell = (d.ndim == 3 && sponge) ? p->nop + 2 : 0;
+    const size_t bytes = (size_t)g.cells() * sizeof(float);
+    long long launches = 0;
+
+    CUDA_TRY(cudaMemsetAsync(p->u[0], 0, bytes, s));
+    CUDA_TRY(cudaMemsetAsync(p->u[1], 0, bytes, s));
+    if (p->nsnap > 0 && !d_wfl && p->snap_cb && !p->d_snap_tmp)
+        AWE_TRY(dev_alloc(p, (void **)&p->d_snap_tmp, p->snap_elems * sizeof(float)));
+
+    StepBParams sp{};
+    sp.g = g;
+    sp.k = p->k;
+    sp.w1 = p->w[0];
+    sp.w2 = p->w[1];
+    sp.w3 = p->w[2];
+    sp.damp_prev = sponge;
+    sp.sponge_new = sponge && !p->sponge_deferred;
+    sp.shell = shell;
+    AbcB abc{p->abc[0], p->abc[1], p->abc[2], p->abc[3], p->abc[4], p->abc[5]};
+    const float *pw1 = sponge ? p->w[0] : nullptr;
+
+    float *cur = p->u[1], *nxt = p->u[0];
+    int row = 0, isnap = 0;
+    for (int it = 0; it < d.nt; it++) {
+        prof_begin(p, s);
+        launch_stepB(d.ndim, p->nop, exact, p->den != nullptr, cur, nxt, p->vel, p->den, sp, s);
+        prof_end(p, s);
+        launches++;
+        if (p->ns > 0) {
+            launch_injectB_off(d.ndim, exact, nxt, p->vel, p->src, p->ns, d_wav, it, ncs, ncs == 1, p->corner_off,
+                               s);
+            launches++;
+        }
+        if (d.dabc) {
+            if (d.hybrid) {
+                launch_hybridB(d.ndim, p->nop, p->nbd, exact, d.fsrf, nxt, cur, abc, p->damp, g, s);
+                launches += d.ndim;
+            } else {
+                if (d.ndim == 3) {
+                    launch_abconeB(3, p->nop, exact, d.fsrf, nxt, cur, abc, g, s);
+                    launches += 3;
+                }
+                if (p->sponge_deferred) {
+                    launch_band_sponge(d.ndim, std::max(p->nbd, shell), exact, nxt, p->w[0], p->w[1], p->w[2], g,
+                                       s);
+                    launches++;
+                } else if (shell > 0) {
+                    launch_band_sponge(d.ndim, shell, exact, nxt, p->w[0], p->w[1], p->w[2], g, s);
+                    launches++;
+                }
+            }
+        }
+        std::swap(cur, nxt);  // nxt now holds the time level `it` (sponge pending)
+        if (p->nsnap > 0 && it % d.jsnap == 0) {
+            float *frame = d_wfl ? d_wfl + (size_t)isnap * p->snap_elems : p->d_snap_tmp;
+            if (frame) {
+                launch_snapshot(d.ndim, nxt, frame, g, p->snap_f[0], p->snap_f[1], p->snap_f[2], p->snap_m[0],
+                                p->snap_m[1], p->snap_m[2], pw1, p->w[1], p->w[2], s);
+                launches++;
+                AWE_TRY(deliver_snapshot(p, frame, isnap, it, s));
+            }
+            isnap++;
+        }
+        if (it % d.jdata == 0) {
+            launch_extract_off(d.ndim, exact, nxt, p->rec, p->nr, d_dat + (size_t)row * p->nr, pw1, p->w[1],
+                               p->w[2], g, p->corner_off, s);
+            launches += p->nr > 0;
+            row++;
+        }
+    }
+    p->launches = launches;
+    return AWE_OK;
+}
+
+}  // namespace awe

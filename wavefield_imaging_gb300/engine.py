@@ -1,0 +1,208 @@
+"""Python front end of libawe.so (include/awe.h) over ctypes.
+
+The engine runs only on the GPU through its own CUDA kernels; there is no CPU
+fallback.  Importing works without a GPU; creating a plan without one raises
+``AweError`` (status AWE_ERR_NODEVICE).  A missing library raises
+immediately with the build command.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "libawe.so")
+
+CART, SPHER = 0, 1
+SCHEME_GPU, SCHEME_CPU = 0, 1
+FAST, EXACT = 0, 1
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "unsupported",
+          5: "no CUDA device", 6: "call out of order"}
+
+
+class AweError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__("%s: %s" % (STATUS.get(status, status), msg))
+        self.status = status
+
+
+class Desc(C.Structure):
+    _fields_ = [
+        ("coords", C.c_int), ("scheme", C.c_int), ("ndim", C.c_int),
+        ("n", C.c_int * 3), ("d", C.c_float * 3), ("o", C.c_float * 3),
+        ("nb", C.c_int), ("nt", C.c_int), ("dt", C.c_float),
+        ("fdorder", C.c_int), ("optfd", C.c_int), ("dabc", C.c_int), ("hybrid", C.c_int),
+        ("fsrf", C.c_int), ("expl", C.c_int), ("refl", C.c_int), ("jdata", C.c_int),
+        ("jsnap", C.c_int), ("bnds", C.c_int), ("precision", C.c_int),
+    ]
+
+
+class Info(C.Structure):
+    _fields_ = [("npad", C.c_int * 3), ("nbpad", C.c_int), ("nsmp", C.c_int), ("nsnap", C.c_int),
+                ("snap_elems", C.c_size_t), ("device_bytes", C.c_size_t)]
+
+
+SNAP_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_float), C.c_size_t)
+
+_lib = None
+
+
+def lib():
+    """Load libawe.so (built in-tree by wavefield_imaging_gb300.build)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libawe.so not built: run `python -m wavefield_imaging_gb300.build` (%s)" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        vp, fp = C.c_void_p, C.POINTER(C.c_float)
+        L.awe_version.restype = C.c_char_p
+        L.awe_last_error.restype = C.c_char_p
+        L.awe_status_string.restype = C.c_char_p
+        L.awe_status_string.argtypes = [C.c_int]
+        L.awe_plan_create.argtypes = [C.POINTER(Desc), C.c_int, C.POINTER(vp)]
+        L.awe_plan_destroy.argtypes = [vp]
+        L.awe_plan_info.argtypes = [vp, C.POINTER(Info)]
+        L.awe_set_model.argtypes = [vp, fp, fp, fp]
+        L.awe_set_geometry.argtypes = [vp, C.c_int, fp, C.c_int, fp]
+        L.awe_forward.argtypes = [vp, fp, C.c_int, fp, fp]
+        L.awe_forward_device.argtypes = [vp, vp, C.c_int, vp, vp, vp]
+        L.awe_set_snapshot_callback.argtypes = [vp, SNAP_FN, vp]
+        L.awe_synchronize.argtypes = [vp]
+        L.awe_last_launch_count.argtypes = [vp]
+        L.awe_last_launch_count.restype = C.c_longlong
+        L.awe_profile_enable.argtypes = [vp, C.c_int]
+        L.awe_profile_read.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
+        for name in ("awe_plan_create", "awe_plan_destroy", "awe_plan_info", "awe_set_model", "awe_set_geometry",
+                     "awe_forward", "awe_forward_device", "awe_set_snapshot_callback", "awe_synchronize",
+                     "awe_profile_enable", "awe_profile_read"):
+            getattr(L, name).restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _check(status: int):
+    if status != 0:
+        raise AweError(status, lib().awe_last_error().decode())
+
+
+def _fp(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def make_desc(ndim, n, d, o, nt, dt, coords=CART, scheme=SCHEME_CPU, nb=-1, fdorder=0, optfd=0, dabc=0,
+              hybrid=0, fsrf=0, expl=0, refl=0, jdata=1, jsnap=0, bnds=0, precision=FAST) -> Desc:
+    q = Desc()
+    q.coords, q.scheme, q.ndim = coords, scheme, ndim
+    n = list(n) + [1] * (3 - len(n))
+    d = list(d) + [1.0] * (3 - len(d))
+    o = list(o) + [0.0] * (3 - len(o))
+    for a in range(3):
+        q.n[a], q.d[a], q.o[a] = n[a], d[a], o[a]
+    q.nb, q.nt, q.dt = nb, nt, dt
+    q.fdorder, q.optfd, q.dabc, q.hybrid, q.fsrf = fdorder, int(optfd), int(dabc), int(hybrid), int(fsrf)
+    q.expl, q.refl, q.jdata, q.jsnap, q.bnds, q.precision = int(expl), int(refl), jdata, jsnap, int(bnds), precision
+    return q
+
+
+class Plan:
+    """One modelling set-up on one GPU: padded grid, model, geometry."""
+
+    def __init__(self, desc: Desc, device: int = 0):
+        self._h = C.c_void_p()
+        _check(lib().awe_plan_create(C.byref(desc), device, C.byref(self._h)))
+        self.desc = desc
+        info = Info()
+        _check(lib().awe_plan_info(self._h, C.byref(info)))
+        self.npad = tuple(info.npad)
+        self.nbpad = info.nbpad
+        self.nsmp = info.nsmp
+        self.nsnap = info.nsnap
+        self.snap_elems = info.snap_elems
+        self._cb = None
+        self.ns = self.nr = 0
+
+    @property
+    def handle(self):
+        return self._h
+
+    def device_bytes(self) -> int:
+        info = Info()
+        _check(lib().awe_plan_info(self._h, C.byref(info)))
+        return info.device_bytes
+
+    def set_model(self, vel, den=None, rfl=None):
+        vel = np.ascontiguousarray(vel, np.float32)
+        den = None if den is None else np.ascontiguousarray(den, np.float32)
+        rfl = None if rfl is None else np.ascontiguousarray(rfl, np.float32)
+        _check(lib().awe_set_model(self._h, _fp(vel), _fp(den), _fp(rfl)))
+
+    def set_geometry(self, sou, rec):
+        nd = self.desc.ndim
+        sou = np.ascontiguousarray(sou, np.float32).reshape(-1, nd)
+        rec = np.ascontiguousarray(rec, np.float32).reshape(-1, nd)
+        self.ns, self.nr = sou.shape[0], rec.shape[0]
+        _check(lib().awe_set_geometry(self._h, self.ns, _fp(sou), self.nr, _fp(rec)))
+
+    def forward(self, wav, snapshots: bool = False):
+        """wav: [nt] or [nt][ncs].  Returns dat [nsmp][nr] (and snaps
+        [nsnap][snap_elems] when snapshots=True)."""
+        wav = np.ascontiguousarray(wav, np.float32)
+        ncs = 1 if wav.ndim == 1 else wav.shape[1]
+        dat = np.zeros((self.nsmp, self.nr), np.float32)
+        wfl = np.zeros((self.nsnap, self.snap_elems), np.float32) if snapshots and self.nsnap else None
+        _check(lib().awe_forward(self._h, _fp(wav), ncs, _fp(dat), _fp(wfl)))
+        return (dat, wfl) if snapshots else dat
+
+    def forward_device(self, d_wav: int, ncs: int, d_dat: int, d_wfl: int = 0, stream: int = 0):
+        """Device-resident run: arguments are raw device pointers (ints)."""
+        _check(lib().awe_forward_device(self._h, C.c_void_p(d_wav), ncs, C.c_void_p(d_dat),
+                                        C.c_void_p(d_wfl) if d_wfl else None,
+                                        C.c_void_p(stream) if stream else None))
+
+    def set_snapshot_callback(self, fn):
+        """fn(isnap, it, frame: np.ndarray) called per snapshot (host copy)."""
+        if fn is None:
+            self._cb = None
+            _check(lib().awe_set_snapshot_callback(self._h, SNAP_FN(), None))
+            return
+
+        def tramp(_user, isnap, it, ptr, n):
+            fn(isnap, it, np.ctypeslib.as_array(ptr, shape=(n,)).copy())
+
+        self._cb = SNAP_FN(tramp)
+        _check(lib().awe_set_snapshot_callback(self._h, self._cb, None))
+
+    def synchronize(self):
+        _check(lib().awe_synchronize(self._h))
+
+    def profile(self, on: bool = True):
+        _check(lib().awe_profile_enable(self._h, int(on)))
+
+    def profile_read(self):
+        """(summed step-kernel milliseconds, step-kernel launches) of the last run."""
+        ms, n = C.c_double(), C.c_longlong()
+        _check(lib().awe_profile_read(self._h, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def last_launch_count(self) -> int:
+        return lib().awe_last_launch_count(self._h)
+
+    def close(self):
+        if self._h:
+            lib().awe_plan_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
