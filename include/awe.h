@@ -158,6 +158,28 @@ long long awe_last_launch_count(const awe_plan *plan);
 awe_status awe_profile_enable(awe_plan *plan, int on);
 awe_status awe_profile_read(awe_plan *plan, double *step_kernel_ms, long long *step_launches);
 
+/* 2D forward modelling without any device allocation.  No counterpart in
+ * the reference (its programs cudaMalloc everything in main()).  For callers
+ * that cannot call cudaMalloc - code inside a framework that owns the device
+ * memory pool, code captured into a larger CUDA graph, plug-ins that must not
+ * grow the device footprint at run time.  The caller passes device buffers
+ * for the inputs and output only: d_vel [n2][n1] (unpadded), d_wav [nt][ncs],
+ * d_sou [ns][2] and d_rec [nr][2] as (x, z) pairs, d_dat [nsmp][nr].  The
+ * wavefields, padded model, sponge tables and interpolation points live in
+ * one static device array of about 12.2 MiB that every GPU loading the
+ * library holds until exit.  Limits: padded n1*n2 <= 1048576, each padded
+ * axis <= 8192, nb <= 256, ns + nr <= 4096; larger requests return
+ * AWE_ERR_INVALID with the limit in awe_last_error().  Scheme
+ * AWE_SCHEME_CPU, cartesian, no hybrid ABC, no density, no snapshots; the
+ * result equals awe_forward's for the same descriptor.  The work is queued on
+ * `stream` (a cudaStream_t; NULL = legacy default stream) and is complete when
+ * the stream is.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current; make that first
+ * call before any stream capture.  All calls share the array: each call clears
+ * what must start at zero, and calls whose work overlaps on the GPU race. */
+awe_status awe_forward2d_noalloc(const awe_desc *desc, const float *d_vel, const float *d_wav, int ncs, int ns,
+                                 const float *d_sou, int nr, const float *d_rec, float *d_dat, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
