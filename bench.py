@@ -42,10 +42,10 @@ UNIT = "cell-updates/s"
 BYTES_PER_CELL = 16  # read u_cur, read u_prev, read v^2dt^2, write u_next
 
 
-def workload(nt=3000):
-    return dict(name="3D cartesian acoustic forward, 512^3 at 5 m (576^3 padded, nb=32), 8th order, "
-                     "nt=%d, dabc=y, 1 Ricker source, 128x128 receivers" % nt,
-                n=(512, 512, 512), d=(5.0, 5.0, 5.0), o=(0.0, 0.0, 0.0), nt=nt, dt=0.005, nb=32, fdorder=8,
+def workload(nt=3000, n=512):
+    return dict(name="3D cartesian acoustic forward, %d^3 at 5 m (%d^3 padded, nb=32), 8th order, "
+                     "nt=%d, dabc=y, 1 Ricker source, 128x128 receivers" % (n, n + 64, nt),
+                n=(n, n, n), d=(5.0, 5.0, 5.0), o=(0.0, 0.0, 0.0), nt=nt, dt=0.005, nb=32, fdorder=8,
                 dabc=1, f0=5.0, seed=3)
 
 
@@ -262,7 +262,7 @@ def run_ours(args):
 
     dist, rank, world, local = dist_init()
     torch.cuda.set_device(local)
-    w = workload(args.nt)
+    w = workload(args.nt, args.n)
     vel = layered_model_3d(w)
     sou, rec = geometry(w)
     wav = ricker(w["nt"], w["dt"], w["f0"])
@@ -347,7 +347,9 @@ def run_ours(args):
                    "h2d_bytes_per_step": int(vel.nbytes + wav.nbytes + sou.nbytes + rec.nbytes),
                    "d2h_bytes_per_step": int(plan.nsmp * nr * 4)},
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                        "frac": achieved / peak, "traffic": traffic, "kernel": "k_stepB (3D, 8th order)",
+                        "frac": achieved / peak, "traffic": traffic,
+                        "kernel": ("k_stepB3_o8 (TMA-staged, 3D 8th order)" if plan.step_kernel == "tma3d"
+                                   else "k_stepB (one thread per cell, 3D 8th order)"),
                         "peak_source": peak_kind, "avg_launch_us": avg_kernel_s * 1e6,
                         "kernel_share": (kern_ms / ms) if ms > 0 else None},
            "gpu_launches": int(launches), "clocks": clocks, "trace_max_abs": check}
@@ -366,6 +368,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fast", choices=["fast", "exact"])
     ap.add_argument("--nt", type=int, default=3000, help="time steps (the workload is nt=3000)")
+    ap.add_argument("--n", type=int, default=512, help="model edge (the workload is 512; smaller for profiling)")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     args = ap.parse_args()
     if args.impl == "reference":

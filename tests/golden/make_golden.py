@@ -73,6 +73,10 @@ CASES_3D = [
     dict(name="c3d_o8_hybrid", n=(20, 18, 18), nb=10, nt=110, fdorder=8, dabc=1, hybrid=1, expl=1, jsnap=0,
          seed=13),
     dict(name="c3d_o2_plain", n=(16, 18, 20), nb=-1, nt=100, fdorder=2, dabc=0, expl=1, jsnap=0, seed=14),
+    # padded axis 1 a multiple of 4: the shape the TMA-staged 3D kernel takes
+    dict(name="c3d_o8_tma_shape", n=(24, 20, 18), nb=8, nt=120, fdorder=8, dabc=1, expl=1, jsnap=60, seed=15),
+    dict(name="c3d_o8_tma_free", n=(28, 22, 20), nb=10, nt=100, fdorder=8, dabc=1, fsrf=1, expl=0, ns=2, jsnap=0,
+         seed=16),
 ]
 
 

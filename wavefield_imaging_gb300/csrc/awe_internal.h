@@ -1,6 +1,7 @@
 // Internal declarations shared by the engine's translation units.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstddef>
@@ -94,5 +95,17 @@ Lint lint_make(int ndim, float x, float y, float z, const FdmAxes &f);
 void expand_model(int ndim, const float *a, float *b, int nb, const int *n);
 
 void set_error(const char *fmt, ...);
+
+// ---- TMA-staged 3D 8th-order step (k_stepB3_tma.cu) ----
+struct Step3Launch {
+    int grid, L, ntz, ntx, nchunks, items;
+    size_t smem;
+};
+bool stepB3_tma_eligible(int ndim, int nop, bool rho, const Grid &g);
+bool stepB3_tma_maps(CUtensorMap *maps, float *const u[2], const float *vel, const Grid &g);
+Step3Launch stepB3_tma_shape(const Grid &g, int num_sms, int L);
+cudaError_t launch_stepB3_tma(bool exact, const CUtensorMap *maps, int icur, float *nxt, const StepBParams &sp,
+                              const Step3Launch &sh, unsigned long long *counter, unsigned long long base, int *err,
+                              cudaStream_t s);
 
 }  // namespace awe

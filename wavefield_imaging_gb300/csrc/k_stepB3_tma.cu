@@ -1,0 +1,316 @@
+// 3D 8th-order step of the CPU-program scheme, TMA-staged 2.5D blocking.
+//
+// A CTA owns a 64 (z) x 16 (x) tile and marches along y over a chunk of
+// planes.  For every plane it TMA-loads (cp.async.bulk.tensor, mbarrier
+// completion) the current level's 72 x 24 halo tile and the previous level
+// and v^2 dt^2 64 x 16 tiles into a 7-deep shared-memory ring, three planes
+// ahead of the compute.  y-neighbours come from a 9-plane register queue
+// (each thread owns a 4-cell z strip of one x column), z- and x-neighbours
+// from the halo tile in shared memory; the leapfrog update, the sponge of
+// the previous level (applied on read) and of the new level (outside the ABC
+// shell) are fused, and the 4-cell result is written with one 16-byte store.
+// Work items (tile, y-chunk) are handed out by a global atomic counter, so
+// the persistent grid (2 CTAs per SM) stays balanced.
+//
+// Operation order per cell is that of ts_kernel.c:286-307
+// (lap = u*c0 + sum_k [(z pair)*cz + (x pair)*cx + (y pair)*cy]), so the
+// EXACT instantiation is bit-identical to k_stepB.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include "awe_internal.h"
+#include "fp_exact.cuh"
+#include "tma.cuh"
+
+#include <algorithm>
+
+namespace awe {
+
+namespace s3 {
+constexpr int TZ = 64, TX = 16, HALO = 4, RING = 7, NOPQ = 4;
+constexpr int HZ = TZ + 2 * HALO, HX = TX + 2 * HALO;
+constexpr int NTHREADS = 256;
+constexpr uint32_t BYTES_HALO = HZ * HX * 4, BYTES_TILE = TZ * TX * 4;
+constexpr long long SPIN_LIMIT = 1ll << 22;
+
+struct __align__(128) Stage {
+    float cur[HX][HZ];
+    float prv[TX][TZ];
+    float vel[TX][TZ];
+};
+static_assert(sizeof(Stage) % 128 == 0, "stage size");
+}  // namespace s3
+
+struct Step3Params {
+    int n1, n2, n3;
+    float c0, cz[5], cx[5], cy[5];
+    const float *w1, *w2, *w3;
+    int damp_prev, sponge_new, shell;
+    int L, ntz, ntx, nchunks;
+    unsigned long long *counter;
+    unsigned long long base;
+    int *err;
+    float *nxt;
+};
+
+template <bool EXACT>
+__device__ __forceinline__ float damp3(float v, float a, float b, float c) {
+    return fmul<EXACT>(fmul<EXACT>(fmul<EXACT>(v, a), b), c);
+}
+
+template <bool EXACT>
+__global__ void __launch_bounds__(s3::NTHREADS, 2)
+    k_stepB3_o8(const __grid_constant__ CUtensorMap tm_cur, const __grid_constant__ CUtensorMap tm_prv,
+                const __grid_constant__ CUtensorMap tm_vel, const Step3Params p) {
+    using namespace s3;
+    extern __shared__ unsigned char smem_raw[];
+    Stage *st = reinterpret_cast<Stage *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    __shared__ __align__(8) uint64_t full[RING];
+    __shared__ int s_item;
+
+    const int tid = threadIdx.x;
+    const int zq = tid & 15, xi = tid >> 4;
+    if (tid == 0) {
+        for (int r = 0; r < RING; r++) mbar_init(&full[r], 1);
+        fence_mbar_init();
+        prefetch_tmap(&tm_cur);
+        prefetch_tmap(&tm_prv);
+        prefetch_tmap(&tm_vel);
+    }
+    // an earlier launch that gave up on a wait leaves the flag set: do nothing
+    if (__syncthreads_or(tid == 0 && *(volatile int *)p.err != 0)) return;
+
+    const int nitems = p.ntz * p.ntx * p.nchunks;
+    unsigned long long gbase = 0;  // running stage sequence (slot and parity)
+    for (;;) {
+        if (tid == 0) s_item = (int)(atomicAdd(p.counter, 1ull) - p.base);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= nitems || item < 0) break;
+        const int tile = item % (p.ntz * p.ntx), chunk = item / (p.ntz * p.ntx);
+        const int z0 = (tile % p.ntz) * TZ, x0 = (tile / p.ntz) * TX;
+        const int y0 = chunk * p.L, y1 = min(y0 + p.L, p.n3);
+        const int S = (y1 - y0) + 2 * NOPQ;
+
+        auto issue = [&](int s) {
+            const unsigned long long g = gbase + s;
+            const int slot = (int)(g % RING);
+            const bool out = s >= 2 * NOPQ;
+            mbar_expect_tx(&full[slot], BYTES_HALO + (out ? 2 * BYTES_TILE : 0));
+            tma_load_3d(&st[slot].cur[0][0], &tm_cur, &full[slot], z0 - HALO, x0 - HALO, y0 - NOPQ + s);
+            if (out) {
+                const int pl = y0 + s - 2 * NOPQ;
+                tma_load_3d(&st[slot].prv[0][0], &tm_prv, &full[slot], z0, x0, pl);
+                tma_load_3d(&st[slot].vel[0][0], &tm_vel, &full[slot], z0, x0, pl);
+            }
+        };
+        if (tid == 0)
+            for (int s = 0; s < RING && s < S; s++) issue(s);
+
+        // per-thread constants
+        const int zg = z0 + 4 * zq, x = x0 + xi;
+        const bool col_ok = x < p.n2 && zg < p.n1;
+        float wz[4], wx = 1.f;
+        bool zin[4], zshell[4];
+        const bool xin = x >= NOPQ && x < p.n2 - NOPQ;
+        const bool xshell = x < p.shell || x >= p.n2 - p.shell;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int z = zg + i;
+            wz[i] = (p.w1 && z < p.n1) ? __ldg(p.w1 + z) : 1.f;
+            zin[i] = z >= NOPQ && z < p.n1 - NOPQ;
+            zshell[i] = z < p.shell || z >= p.n1 - p.shell;
+        }
+        if (p.w2 && x < p.n2) wx = __ldg(p.w2 + x);
+
+        float q[9][4];  // y queue: plane y0-4+s lives in q[s % 9]
+#pragma unroll 1
+        for (int blk = 0; blk < S; blk += 9) {
+#pragma unroll
+            for (int u = 0; u < 9; u++) {
+                const int s = blk + u;
+                if (s < S) {
+                    const unsigned long long g = gbase + s;
+                    const int slot = (int)(g % RING);
+                    const bool bad = !mbar_wait(&full[slot], (uint32_t)((g / RING) & 1), SPIN_LIMIT);
+                    if (bad) atomicExch(p.err, 1);
+                    const float4 cq = *reinterpret_cast<const float4 *>(&st[slot].cur[xi + HALO][4 * zq + HALO]);
+                    q[u][0] = cq.x;
+                    q[u][1] = cq.y;
+                    q[u][2] = cq.z;
+                    q[u][3] = cq.w;
+                    if (s >= 2 * NOPQ) {
+                        const int y = y0 + s - 2 * NOPQ;
+                        const int hs = (int)((g - NOPQ) % RING);  // halo tile of plane y
+                        const float(*H)[HZ] = st[hs].cur;
+                        float zw[12];
+#pragma unroll
+                        for (int v = 0; v < 3; v++) {
+                            const float4 t = *reinterpret_cast<const float4 *>(&H[xi + HALO][4 * zq + 4 * v]);
+                            zw[4 * v] = t.x;
+                            zw[4 * v + 1] = t.y;
+                            zw[4 * v + 2] = t.z;
+                            zw[4 * v + 3] = t.w;
+                        }
+                        const int jc = (u + 1 + 4) % 9;  // queue slot of plane y: ((s - 8) + 4) % 9
+                        float lap[4];
+#pragma unroll
+                        for (int i = 0; i < 4; i++) lap[i] = fmul<EXACT>(zw[4 + i], p.c0);
+#pragma unroll
+                        for (int k = 1; k <= NOPQ; k++) {
+                            const float4 xm = *reinterpret_cast<const float4 *>(&H[xi + HALO - k][4 * zq + HALO]);
+                            const float4 xp = *reinterpret_cast<const float4 *>(&H[xi + HALO + k][4 * zq + HALO]);
+                            const float xmv[4] = {xm.x, xm.y, xm.z, xm.w}, xpv[4] = {xp.x, xp.y, xp.z, xp.w};
+#pragma unroll
+                            for (int i = 0; i < 4; i++) {
+                                const float zp = fadd<EXACT>(zw[4 + i - k], zw[4 + i + k]);
+                                const float xpair = fadd<EXACT>(xmv[i], xpv[i]);
+                                const float ypair = fadd<EXACT>(q[(jc + 9 - k) % 9][i], q[(jc + k) % 9][i]);
+                                float t = fadd<EXACT>(fmul<EXACT>(zp, p.cz[k]), fmul<EXACT>(xpair, p.cx[k]));
+                                t = fadd<EXACT>(t, fmul<EXACT>(ypair, p.cy[k]));
+                                lap[i] = fadd<EXACT>(lap[i], t);
+                            }
+                        }
+                        const float4 pv = *reinterpret_cast<const float4 *>(&st[slot].prv[xi][4 * zq]);
+                        const float4 vv = *reinterpret_cast<const float4 *>(&st[slot].vel[xi][4 * zq]);
+                        const float prv4[4] = {pv.x, pv.y, pv.z, pv.w}, vel4[4] = {vv.x, vv.y, vv.z, vv.w};
+                        const float wy = p.w3 ? __ldg(p.w3 + y) : 1.f;
+                        const bool yin = y >= NOPQ && y < p.n3 - NOPQ;
+                        const bool yshell = y < p.shell || y >= p.n3 - p.shell;
+                        float out[4];
+#pragma unroll
+                        for (int i = 0; i < 4; i++) {
+                            float pr = prv4[i];
+                            if (p.damp_prev) pr = damp3<EXACT>(pr, wz[i], wx, wy);
+                            float o = pr;
+                            if (zin[i] && xin && yin) {
+                                const float u0 = zw[4 + i];
+                                if constexpr (EXACT)
+                                    o = sum3_rn(__fmul_rn(vel4[i], lap[i]), __fadd_rn(u0, u0), -pr);
+                                else
+                                    o = fmaf(vel4[i], lap[i], 2.f * u0 - pr);
+                            }
+                            if (p.sponge_new && !(zshell[i] || xshell || yshell)) o = damp3<EXACT>(o, wz[i], wx, wy);
+                            out[i] = o;
+                        }
+                        if (col_ok) {
+                            float *dst = p.nxt + ((long long)y * p.n2 + x) * p.n1 + zg;
+                            *reinterpret_cast<float4 *>(dst) = make_float4(out[0], out[1], out[2], out[3]);
+                        }
+                    }
+                    if (__syncthreads_or(bad)) {
+                        // drain: wait (bounded) for every copy still in flight, then leave
+                        if (tid == 0) {
+                            const int issued = min(S, max(RING, s - NOPQ + RING));
+                            for (int t = s; t < issued; t++) {
+                                const unsigned long long gt = gbase + t;
+                                mbar_wait(&full[gt % RING], (uint32_t)((gt / RING) & 1), SPIN_LIMIT);
+                            }
+                        }
+                        __syncthreads();
+                        return;
+                    }
+                    if (tid == 0 && s >= NOPQ && s - NOPQ + RING < S) issue(s - NOPQ + RING);
+                }
+            }
+        }
+        gbase += S;
+    }
+}
+
+// cuTensorMapEncodeTiled, fetched from the driver at run time (no link-time libcuda dependency)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn g_encode = nullptr;
+
+static bool encode_fn() {
+    if (g_encode) return true;
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &fn, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+        return false;
+    g_encode = reinterpret_cast<EncodeTiledFn>(fn);
+    return true;
+}
+
+bool make_tmap_3d(CUtensorMap *m, const float *base, int n1, int n2, int n3, int b1, int b2) {
+    if (!encode_fn()) return false;
+    cuuint64_t dims[3] = {(cuuint64_t)n1, (cuuint64_t)n2, (cuuint64_t)n3};
+    cuuint64_t strides[2] = {(cuuint64_t)n1 * 4, (cuuint64_t)n1 * n2 * 4};
+    cuuint32_t box[3] = {(cuuint32_t)b1, (cuuint32_t)b2, 1};
+    cuuint32_t es[3] = {1, 1, 1};
+    CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(base), dims, strides, box, es,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+bool stepB3_tma_eligible(int ndim, int nop, bool rho, const Grid &g) {
+    return ndim == 3 && nop == 4 && !rho && g.n1 % 4 == 0 && g.n1 >= 16 && g.n2 >= 16 && g.n3 >= 9;
+}
+
+// tensor maps: [0] u[0] halo box, [1] u[1] halo box, [2] u[0] tile, [3] u[1] tile, [4] vel tile
+bool stepB3_tma_maps(CUtensorMap *maps, float *const u[2], const float *vel, const Grid &g) {
+    using namespace s3;
+    return make_tmap_3d(&maps[0], u[0], g.n1, g.n2, g.n3, HZ, HX) &&
+           make_tmap_3d(&maps[1], u[1], g.n1, g.n2, g.n3, HZ, HX) &&
+           make_tmap_3d(&maps[2], u[0], g.n1, g.n2, g.n3, TZ, TX) &&
+           make_tmap_3d(&maps[3], u[1], g.n1, g.n2, g.n3, TZ, TX) &&
+           make_tmap_3d(&maps[4], vel, g.n1, g.n2, g.n3, TZ, TX);
+}
+
+Step3Launch stepB3_tma_shape(const Grid &g, int num_sms, int L) {
+    using namespace s3;
+    Step3Launch s{};
+    s.L = L > 0 ? L : 64;
+    s.ntz = (g.n1 + TZ - 1) / TZ;
+    s.ntx = (g.n2 + TX - 1) / TX;
+    s.nchunks = (g.n3 + s.L - 1) / s.L;
+    s.items = s.ntz * s.ntx * s.nchunks;
+    s.grid = std::min(s.items, 2 * num_sms);
+    s.smem = RING * sizeof(Stage) + 128;
+    return s;
+}
+
+// launch one step: cur = u[icur], nxt = u[1-icur]
+cudaError_t launch_stepB3_tma(bool exact, const CUtensorMap *maps, int icur, float *nxt, const StepBParams &sp,
+                              const Step3Launch &sh, unsigned long long *counter, unsigned long long base, int *err,
+                              cudaStream_t s) {
+    Step3Params p{};
+    p.n1 = sp.g.n1;
+    p.n2 = sp.g.n2;
+    p.n3 = sp.g.n3;
+    p.c0 = sp.k.c0;
+    for (int k = 0; k <= 4; k++) {
+        p.cz[k] = sp.k.c[0][k];
+        p.cx[k] = sp.k.c[1][k];
+        p.cy[k] = sp.k.c[2][k];
+    }
+    p.w1 = sp.w1;
+    p.w2 = sp.w2;
+    p.w3 = sp.w3;
+    p.damp_prev = sp.damp_prev;
+    p.sponge_new = sp.sponge_new;
+    p.shell = sp.shell;
+    p.L = sh.L;
+    p.ntz = sh.ntz;
+    p.ntx = sh.ntx;
+    p.nchunks = sh.nchunks;
+    p.counter = counter;
+    p.base = base;
+    p.err = err;
+    p.nxt = nxt;
+    const CUtensorMap &cur = maps[icur], &prv = maps[2 + (1 - icur)], &vel = maps[4];
+    if (exact) {
+        cudaFuncSetAttribute(k_stepB3_o8<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem);
+        k_stepB3_o8<true><<<sh.grid, s3::NTHREADS, sh.smem, s>>>(cur, prv, vel, p);
+    } else {
+        cudaFuncSetAttribute(k_stepB3_o8<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem);
+        k_stepB3_o8<false><<<sh.grid, s3::NTHREADS, sh.smem, s>>>(cur, prv, vel, p);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace awe

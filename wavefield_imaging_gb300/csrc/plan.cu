@@ -97,6 +97,20 @@ void prof_end(awe_plan *p, cudaStream_t s) {
 
 }  // namespace awe
 
+// The pipelined step kernels bound every wait and raise a device flag instead
+// of hanging; surface it as a CUDA error once the stream has drained.
+static awe_status check_pipeline(awe_plan *p) {
+    if (!p->d_err) return AWE_OK;
+    int h = 0;
+    CUDA_TRY(cudaMemcpy(&h, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) {
+        cudaMemset(p->d_err, 0, sizeof(int));
+        set_error("a pipeline wait in the step kernel timed out; this run's results are invalid");
+        return AWE_ERR_CUDA;
+    }
+    return AWE_OK;
+}
+
 static awe_status check_desc(const awe_desc *d) {
     if (!d) {
         set_error("null descriptor");
@@ -232,6 +246,7 @@ awe_status awe_plan_info(const awe_plan *p, awe_info *info) {
     info->nsnap = p->nsnap;
     info->snap_elems = p->snap_elems;
     info->device_bytes = p->device_bytes;
+    info->step_kernel = p->use_tma ? 1 : 0;
     return AWE_OK;
 }
 
@@ -271,7 +286,7 @@ awe_status awe_synchronize(awe_plan *p) {
     if (!p) return AWE_ERR_INVALID;
     CUDA_TRY(cudaSetDevice(p->device));
     CUDA_TRY(cudaStreamSynchronize(p->stream));
-    return AWE_OK;
+    return check_pipeline(p);
 }
 
 long long awe_last_launch_count(const awe_plan *p) { return p ? p->launches : -1; }
@@ -364,6 +379,7 @@ awe_status awe_forward(awe_plan *p, const float *wav, int ncs, float *dat, float
     dev_free(p, d_wav);
     dev_free(p, d_dat);
     dev_free(p, d_wfl);
+    if (st == AWE_OK) st = check_pipeline(p);
     return st;
 }
 

@@ -54,6 +54,14 @@ struct awe_plan {
     float *d_snap_tmp = nullptr;
     long long launches = 0;
 
+    // TMA-staged 3D step (scheme CPU, 8th order)
+    bool use_tma = false;
+    CUtensorMap tmaps[5];
+    awe::Step3Launch tma_shape{};
+    unsigned long long *sched_counter = nullptr;
+    unsigned long long sched_base = 0;
+    int *d_err = nullptr;
+
     // optional per-launch timing of the step kernel
     bool profile = false;
     std::vector<cudaEvent_t> prof_ev;  // pairs (start, stop)

@@ -2,7 +2,9 @@
 // coefficient tables, model preparation and the per-step launch sequence.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -73,6 +75,23 @@ awe_status planB_init(awe_plan *p) {
         std::vector<float> dm;
         hybrid_damp(nb - p->nop, dm);
         AWE_TRY(upload(p, &p->damp, dm.data(), dm.size()));
+    }
+
+    // TMA-staged step kernel for the 3D 8th-order case; AWE_STEP_KERNEL=simple
+    // forces the one-thread-per-cell kernel (used by the tests to compare both)
+    const char *kern = std::getenv("AWE_STEP_KERNEL");
+    const bool force_simple = kern && std::strcmp(kern, "simple") == 0;
+    if (!force_simple && stepB3_tma_eligible(d.ndim, p->nop, false, p->g)) {
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device);
+        const char *lenv = std::getenv("AWE_TMA_CHUNK");
+        p->tma_shape = stepB3_tma_shape(p->g, sms > 0 ? sms : 1, lenv ? std::atoi(lenv) : 0);
+        AWE_TRY(dev_alloc(p, (void **)&p->sched_counter, sizeof(unsigned long long)));
+        AWE_TRY(dev_alloc(p, (void **)&p->d_err, sizeof(int)));
+        CUDA_TRY(cudaMemset(p->sched_counter, 0, sizeof(unsigned long long)));
+        CUDA_TRY(cudaMemset(p->d_err, 0, sizeof(int)));
+        p->sched_base = 0;
+        if (stepB3_tma_maps(p->tmaps, p->u, p->vel, p->g)) p->use_tma = true;
     }
 
     p->nsmp = (d.nt - 1) / d.jdata + 1;
@@ -265,10 +284,21 @@ awe_status planB_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, flo
     const float *pw1 = sponge ? p->w[0] : nullptr;
 
     float *cur = p->u[1], *nxt = p->u[0];
+    int icur = 1;
     int row = 0, isnap = 0;
     for (int it = 0; it < d.nt; it++) {
         prof_begin(p, s);
-        launch_stepB(d.ndim, p->nop, exact, p->den != nullptr, cur, nxt, p->vel, p->den, sp, s);
+        if (p->use_tma) {
+            cudaError_t e = launch_stepB3_tma(exact, p->tmaps, icur, nxt, sp, p->tma_shape, p->sched_counter,
+                                              p->sched_base, p->d_err, s);
+            p->sched_base += (unsigned long long)p->tma_shape.items + p->tma_shape.grid;
+            if (e != cudaSuccess) {
+                set_error("TMA step launch failed: %s", cudaGetErrorString(e));
+                return AWE_ERR_CUDA;
+            }
+        } else {
+            launch_stepB(d.ndim, p->nop, exact, p->den != nullptr, cur, nxt, p->vel, p->den, sp, s);
+        }
         prof_end(p, s);
         launches++;
         if (p->ns > 0) {
@@ -296,6 +326,7 @@ awe_status planB_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, flo
             }
         }
         std::swap(cur, nxt);  // nxt now holds the time level `it` (sponge pending)
+        icur ^= 1;
         if (p->nsnap > 0 && it % d.jsnap == 0) {
             float *frame = d_wfl ? d_wfl + (size_t)isnap * p->snap_elems : p->d_snap_tmp;
             if (frame) {

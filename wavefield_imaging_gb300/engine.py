@@ -42,7 +42,7 @@ class Desc(C.Structure):
 
 class Info(C.Structure):
     _fields_ = [("npad", C.c_int * 3), ("nbpad", C.c_int), ("nsmp", C.c_int), ("nsnap", C.c_int),
-                ("snap_elems", C.c_size_t), ("device_bytes", C.c_size_t)]
+                ("snap_elems", C.c_size_t), ("device_bytes", C.c_size_t), ("step_kernel", C.c_int)]
 
 
 SNAP_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_float), C.c_size_t)
@@ -121,6 +121,7 @@ class Plan:
         self.nsmp = info.nsmp
         self.nsnap = info.nsnap
         self.snap_elems = info.snap_elems
+        self.step_kernel = "tma3d" if info.step_kernel == 1 else "simple"
         self._cb = None
         self.ns = self.nr = 0
 
