@@ -58,6 +58,23 @@ int orc_cart2d_cpu(const orc_par *p, const float *vel, const float *den, const f
 int orc_cart3d_cpu(const orc_par *p, const float *vel, const float *den, const float *wav, int ns,
                    const float *sou, int nr, const float *rec, float *dat, float *snaps);
 
+/* Scheme of the GPU programs (awe_oracle_gpu.c).  kind: 0 sfAWEFDcart2Dgpu,
+ * 1 sfAWEFDcart3Dgpu (n1 == n2), 2 sfAWEFDspher2Dgpu (polar), 3
+ * sfAWEFDspher3Dgpu.  Model [n3][n2][n1] axis 1 fastest (z or r); points in
+ * the programs' order: (x,z), (x,y,z), (r,theta), (r,phi,theta).  wav: [nt]
+ * (the programs read wav[it]).  dat rows: nt/jdata (spherical 3D: nt). */
+typedef struct {
+    int n1, n2, n3;
+    float d1, d2, d3;
+    float o1, o2, o3;
+    int nb, nt;
+    float dt;
+    int jdata, jsnap, bnds, fsrf, expl, refl;
+} orc_gpar;
+
+int orc_gpu_forward(int kind, const orc_gpar *p, const float *vel, const float *rfl, const float *wav, int ns,
+                    const float *sou, int nr, const float *rec, float *dat, float *snaps);
+
 /* Time nsteps of the 3D scheme-B update on a padded grid (for the CPU
  * baseline): returns wall seconds.  Fields are allocated internally. */
 double orc_cart3d_cpu_steps(int n1pad, int n2pad, int n3pad, int fdorder, int nsteps, int nthreads);

@@ -25,10 +25,12 @@
 
 #define NOPA 4 /* cart_kernels.cu:401, spher_kernels.cu:402 */
 
-/* spongeKernel_2D/3D factor for index distance i (cart_kernels.cu:723-815) */
+/* spongeKernel_2D/3D factor for index distance i (cart_kernels.cu:723-815).
+ * The kernels are C++: log(alpha) with a float alpha is the float logarithm
+ * (logf), promoted to double; the rest of the expression is double. */
 static double sponge_damp(int i, int nb) {
     float alpha = 0.90;
-    return exp(-1.0 * fabs((pow((i - 1.0), 2) * log(alpha)) / (pow(nb, 2))));
+    return exp(-1.0 * fabs((pow((i - 1.0), 2) * (double)logf(alpha)) / (pow(nb, 2))));
 }
 
 /* sponge index for a cell; priority order as the kernel's argument order:
@@ -246,6 +248,10 @@ static int gpu_cart2d(const orc_gpar *P, const float *vel_in, const float *rfl_i
                 ppo[C2(ix, iz)] = damp_apply(ppo[C2(ix, iz)], i, tab);
                 if (ix > nxpad - nb) po[C2(ix, iz)] = 0;
             }
+        /* freeSurf_2D's threads past nxpad (grid rounded up to 8) zero the
+         * first samples of the next row (row = z in the kernel's x-fastest view) */
+        for (int iz = 0; iz + 1 < nzpad; iz++)
+            for (int k = 0; k < 8 * ((nxpad + 7) / 8) - nxpad; k++) po[C2(k, iz + 1)] = 0;
         if (snaps && P->jsnap > 0 && it % P->jsnap == 0) {
             if (P->bnds) {
                 memcpy(snaps + isnap * npad, po, npad * 4);
@@ -544,6 +550,9 @@ static int gpu_polar2d(const orc_gpar *P, const float *vel_in, const float *wav,
                 ppo[c] = damp_apply(ppo[c], i, tab);
                 if (P->fsrf && ira > nrapad - nb) po[c] = 0;
             }
+        if (P->fsrf) /* freeSurf_2D past nrapad: first samples of the next theta row */
+            for (int ith = 0; ith + 1 < nthpad; ith++)
+                for (int k = 0; k < 8 * ((nrapad + 7) / 8) - nrapad; k++) po[CP(ith + 1, k)] = 0;
         if (snaps && P->jsnap > 0 && it % P->jsnap == 0) {
             if (P->bnds) {
                 float *dst = snaps + isnap * npad;
@@ -649,6 +658,9 @@ static int gpu_spher3d(const orc_gpar *P, const float *vel_in, const float *wav,
                     ppo[c] = damp_apply(ppo[c], i, tab);
                     if (P->fsrf && ira > nrapad - nb) po[c] = 0;
                 }
+        if (P->fsrf) /* freeSurf_3D past nrapad: first samples of the next r line */
+            for (size_t line = 0; line + 1 < (size_t)nthpad * nphpad; line++)
+                for (int k = 0; k < 8 * ((nrapad + 7) / 8) - nrapad; k++) po[(line + 1) * nrapad + k] = 0;
         for (int r = 0; r < nr; r++) {
             const glint *c = &cr[r];
             size_t b = CS(c->jy, c->jz, c->jx);

@@ -23,13 +23,13 @@ CFLAGS = ["-std=gnu99", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-share
 
 def build(with_reference: bool = True) -> None:
     os.makedirs(BUILD, exist_ok=True)
-    src = os.path.join(HERE, "awe_oracle.c")
+    srcs = [os.path.join(HERE, "awe_oracle.c"), os.path.join(HERE, "awe_oracle_gpu.c")]
     for name, extra in (("liboracle.so", []), ("liboracle64.so", ["-DAWE_REAL_DOUBLE"])):
         out = os.path.join(BUILD, name)
         if not os.path.exists(out) or os.path.getmtime(out) < max(
-            os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "awe_oracle.h"))
+            [os.path.getmtime(x) for x in srcs] + [os.path.getmtime(os.path.join(HERE, "awe_oracle.h"))]
         ):
-            subprocess.check_call(["gcc", *CFLAGS, *extra, src, "-o", out, "-lm"])
+            subprocess.check_call(["gcc", *CFLAGS, *extra, *srcs, "-o", out, "-lm"])
     if with_reference and os.path.isdir(REF_SRC):
         subprocess.check_call(
             ["make", "-s", "-C", os.path.join(HERE, "ref"), "REF=" + REF_SRC, "OUT=" + REF_OUT],
@@ -49,6 +49,19 @@ class Par(C.Structure):
     ]
 
 
+class GPar(C.Structure):
+    _fields_ = [
+        ("n1", C.c_int), ("n2", C.c_int), ("n3", C.c_int),
+        ("d1", C.c_float), ("d2", C.c_float), ("d3", C.c_float),
+        ("o1", C.c_float), ("o2", C.c_float), ("o3", C.c_float),
+        ("nb", C.c_int), ("nt", C.c_int), ("dt", C.c_float),
+        ("jdata", C.c_int), ("jsnap", C.c_int), ("bnds", C.c_int), ("fsrf", C.c_int), ("expl", C.c_int),
+        ("refl", C.c_int),
+    ]
+
+
+GPU_KINDS = {"cart2d": 0, "cart3d": 1, "polar2d": 2, "spher3d": 3}
+
 _libs: dict = {}
 
 
@@ -65,6 +78,8 @@ def lib(fp64: bool = False):
             f.argtypes = [C.POINTER(Par), fp, fp, fp, C.c_int, fp, C.c_int, fp, fp, fp]
             f.restype = C.c_int
         L.orc_cart_padded.argtypes = [C.POINTER(Par)] + [C.POINTER(C.c_int)] * 4
+        L.orc_gpu_forward.argtypes = [C.c_int, C.POINTER(GPar), fp, fp, fp, C.c_int, fp, C.c_int, fp, fp, fp]
+        L.orc_gpu_forward.restype = C.c_int
         L.orc_cart3d_cpu_steps.argtypes = [C.c_int] * 6
         L.orc_cart3d_cpu_steps.restype = C.c_double
         _libs[name] = L
@@ -134,3 +149,68 @@ def cart_cpu(p: dict, vel, wav, sou, rec, den=None, fp64: bool = False):
 
 def cart3d_steps_seconds(n1pad, n2pad, n3pad, fdorder, nsteps, nthreads):
     return lib().orc_cart3d_cpu_steps(n1pad, n2pad, n3pad, fdorder, nsteps, nthreads)
+
+
+def make_gpar(p: dict) -> GPar:
+    q = GPar()
+    n = list(p["n"]) + [1] * (3 - len(p["n"]))
+    d = list(p["d"]) + [1.0] * (3 - len(p["d"]))
+    o = list(p["o"]) + [0.0] * (3 - len(p["o"]))
+    q.n1, q.n2, q.n3 = n
+    q.d1, q.d2, q.d3 = d
+    q.o1, q.o2, q.o3 = o
+    q.nb, q.nt, q.dt = p.get("nb", 4), p["nt"], p["dt"]
+    q.jdata, q.jsnap, q.bnds = p.get("jdata", 1), p.get("jsnap", 0), int(p.get("bnds", 0))
+    q.fsrf, q.expl, q.refl = int(p.get("fsrf", 0)), int(p.get("expl", 0)), int(p.get("refl", 0))
+    return q
+
+
+def gpu_shapes(kind: str, p: dict, nr: int):
+    """(data rows, snapshot frames, floats per frame) of a GPU-program run."""
+    n = list(p["n"]) + [1] * (3 - len(p["n"]))
+    nb = max(p.get("nb", 4), 4)
+    nt, jdata, jsnap = p["nt"], max(p.get("jdata", 1), 1), p.get("jsnap", 0)
+    rows = nt if kind == "spher3d" else nt // jdata
+    frames = (nt - 1) // jsnap + 1 if jsnap > 0 else 0
+    nd = 3 if kind in ("cart3d", "spher3d") else 2
+    if p.get("bnds", 0):
+        elems = int(np.prod([n[a] + 2 * nb for a in range(nd)]))
+    else:
+        elems = int(np.prod(n[:nd]))
+    return rows, frames, elems
+
+
+def gpu_scheme(kind: str, p: dict, vel, wav, sou, rec, rfl=None, use_reference_emulation: bool = False):
+    """Run the GPU-program scheme.  use_reference_emulation=True runs the
+    reference's own kernel files through the host emulation
+    (oracle/_ref/libgpuref.so, built only where the reference is present);
+    otherwise the oracle restatement.  Returns (dat, snaps)."""
+    nd = 3 if kind in ("cart3d", "spher3d") else 2
+    q = make_gpar(p)
+    vel = np.ascontiguousarray(vel, np.float32)
+    rfl = None if rfl is None else np.ascontiguousarray(rfl, np.float32)
+    wav = np.ascontiguousarray(wav, np.float32).ravel()
+    sou = np.ascontiguousarray(sou, np.float32).reshape(-1, nd)
+    rec = np.ascontiguousarray(rec, np.float32).reshape(-1, nd)
+    rows, frames, elems = gpu_shapes(kind, p, rec.shape[0])
+    dat = np.zeros((rows, rec.shape[0]), np.float32)
+    snaps = np.zeros((frames, elems), np.float32) if frames else None
+    args = (C.byref(q),)
+    if use_reference_emulation:
+        L = C.CDLL(os.path.join(REF_OUT, "libgpuref.so"))
+        fp = C.POINTER(C.c_float)
+        fn = getattr(L, "gpuref_" + kind)
+        if kind == "cart2d":
+            fn.argtypes = [C.POINTER(GPar), fp, fp, fp, C.c_int, fp, C.c_int, fp, fp, fp]
+            rc = fn(C.byref(q), _fp(vel), _fp(rfl), _fp(wav), sou.shape[0], _fp(sou), rec.shape[0], _fp(rec),
+                    _fp(dat), _fp(snaps))
+        else:
+            fn.argtypes = [C.POINTER(GPar), fp, fp, C.c_int, fp, C.c_int, fp, fp, fp]
+            rc = fn(C.byref(q), _fp(vel), _fp(wav), sou.shape[0], _fp(sou), rec.shape[0], _fp(rec), _fp(dat),
+                    _fp(snaps))
+    else:
+        rc = lib().orc_gpu_forward(GPU_KINDS[kind], *args, _fp(vel), _fp(rfl), _fp(wav), sou.shape[0], _fp(sou),
+                                   rec.shape[0], _fp(rec), _fp(dat), _fp(snaps))
+    if rc != 0:
+        raise RuntimeError("GPU-scheme run returned %d" % rc)
+    return dat, snaps

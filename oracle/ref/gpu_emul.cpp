@@ -106,6 +106,13 @@ static void launch_ordered(dim3 g, dim3 b, F f, K key) {
 
 static long long facedist(long long c, long long n) { return std::min(c, n - 1 - c); }
 
+// The free-surface kernels test only `ira > nrapad - nb` along the fast axis,
+// so the threads that round the grid up to a multiple of 8 write past the
+// end of each line: into the first samples of the next line, and past the
+// end of the array for the last line.  The emulation keeps that slack
+// behind every field so those writes stay in owned memory (and are dropped).
+static const size_t kSlack = 4096;
+
 extern "C" {
 
 typedef struct {
@@ -159,7 +166,7 @@ int gpuref_cart2d(const gpuref_par *P, const float *vel, const float *rfl, const
     }
     lint2d cs = lint2d_make(ns, ss, fdm), cr = lint2d_make(nr, rr, fdm);
     const size_t npad = (size_t)nxpad * nzpad;
-    std::vector<float> ppo(npad, 0.f), po(npad, 0.f), fpo(npad, 0.f), hpo(npad);
+    std::vector<float> ppo(npad + kSlack, 0.f), po(npad + kSlack, 0.f), fpo(npad + kSlack, 0.f);
     float **pz = sf_floatalloc2(nzpad, nxpad), **oslice = sf_floatalloc2(nz, nx);
     const int nsmp = nt / (P->jdata > 0 ? P->jdata : 1);
     std::vector<float> dd((size_t)nsmp * nr + nr, 0.f);
@@ -272,7 +279,7 @@ int gpuref_cart3d(const gpuref_par *P, const float *vel, const float *wav, int n
         rr[i].z = rec[3 * i + 2];
     }
     lint3d cs = lint3d_make(ns, ss, fdm), cr = lint3d_make(nr, rr, fdm);
-    std::vector<float> ppo(npad, 0.f), po(npad, 0.f), fpo(npad, 0.f);
+    std::vector<float> ppo(npad + kSlack, 0.f), po(npad + kSlack, 0.f), fpo(npad + kSlack, 0.f);
     float ***p3 = sf_floatalloc3(nzpad, nxpad, nypad), ***oslice = sf_floatalloc3(nz, nx, ny);
     const int jdata = P->jdata > 0 ? P->jdata : 1, nsmp = nt / jdata;
     std::vector<float> dd((size_t)(nsmp + 1) * nr, 0.f);
@@ -376,7 +383,7 @@ int gpuref_polar2d(const gpuref_par *P, const float *vel, const float *wav, int 
         rr[i].z = rec[2 * i + 1];
     }
     lint2d cs = lint2d_make(ns, ss, fdm), cr = lint2d_make(nr, rr, fdm);
-    std::vector<float> ppo(npad, 0.f), po(npad, 0.f), fpo(npad, 0.f);
+    std::vector<float> ppo(npad + kSlack, 0.f), po(npad + kSlack, 0.f), fpo(npad + kSlack, 0.f);
     float **pz = sf_floatalloc2(nthpad, nrapad), **oslice = sf_floatalloc2(nth, nra);
     const int nsmp = nt / (P->jdata > 0 ? P->jdata : 1);
     std::vector<float> dd((size_t)nsmp * nr + nr, 0.f);
@@ -460,7 +467,7 @@ int gpuref_spher3d(const gpuref_par *P, const float *vel, const float *wav, int 
         rr[i].z = rec[3 * i + 2];
     }
     lint3d cs = lint3d_make(ns, ss, fdm), cr = lint3d_make(nr, rr, fdm);
-    std::vector<float> ppo(npad, 0.f), po(npad, 0.f), fpo(npad, 0.f), row(nr > 0 ? nr : 1);
+    std::vector<float> ppo(npad + kSlack, 0.f), po(npad + kSlack, 0.f), fpo(npad + kSlack, 0.f), row(nr > 0 ? nr : 1);
     float ***oslice = sf_floatalloc3(nra, nth, nph);
     const dim3 g3((unsigned)ceil(nrapad / 8.0f), (unsigned)ceil(nphpad / 8.0f), (unsigned)ceil(nthpad / 8.0f)),
         b3(8, 8, 8);

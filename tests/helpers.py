@@ -8,7 +8,7 @@ import numpy as np
 GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
-def golden_paths(pattern="*.npz"):
+def golden_paths(pattern="c*.npz"):
     return sorted(glob.glob(os.path.join(GOLDEN_DIR, pattern)))
 
 

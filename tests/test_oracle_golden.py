@@ -11,7 +11,7 @@ import pytest
 
 from oracle import oracle
 
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "c*.npz")))
 
 
 def load(path):
@@ -45,3 +45,22 @@ def test_fp64_oracle_close_to_fp32():
     d64, _ = oracle.cart_cpu(par, a["vel"], a["wav"], a["sou"], a["rec"], den=a.get("den"), fp64=True)
     rel = np.linalg.norm(d32 - d64) / np.linalg.norm(d64)
     assert 0 < rel < 1e-4
+
+
+GOLDEN_A = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "A_*.npz")))
+
+
+@pytest.mark.parametrize("path", GOLDEN_A, ids=[os.path.basename(p)[:-4] for p in GOLDEN_A])
+def test_gpu_scheme_oracle_matches_reference_kernels_bit_exact(path):
+    """Fixtures from the reference's own CUDA kernel files run through the host
+    emulation of the GPU programs (tests/golden/make_golden_gpu.py)."""
+    par, a = load(path)
+    dat, snaps = oracle.gpu_scheme(par["kind"], par, a["vel"], a["wav"], a["sou"], a["rec"], rfl=a.get("rfl"))
+    assert np.array_equal(dat, a["dat"])
+    if "snaps" in a:
+        assert np.array_equal(snaps, a["snaps"])
+
+
+def test_gpu_scheme_golden_set_covers_programs():
+    kinds = {load(p)[0]["kind"] for p in GOLDEN_A}
+    assert kinds == {"cart2d", "cart3d", "polar2d", "spher3d"}

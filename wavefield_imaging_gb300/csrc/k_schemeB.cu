@@ -154,19 +154,26 @@ __device__ __forceinline__ float abc_update(float um_in, float um_c, float uo_in
 }
 
 template <bool EXACT>
-__global__ void k_abc_axis1(float *uo, const float *__restrict__ um, const float *__restrict__ bl,
+__global__ void k_abc_axis1(float *__restrict__ uo, const float *__restrict__ um, const float *__restrict__ bl,
                             const float *__restrict__ bh, Grid g, int nop, int top) {
-    const long long line = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // (i3, i2)
-    if (line >= (long long)g.n2 * g.n3) return;
-    const long long c = line * g.n1;
+    const int line = blockIdx.x * blockDim.x + threadIdx.x;  // (i3, i2)
+    if (line >= g.n2 * g.n3) return;
+    const long long c = (long long)line * g.n1;
     const float l = bl[line], h = bh[line];
-    for (int iop = 0; iop < nop; iop++) {
-        if (top) {
-            int iz = nop - iop;
-            uo[c + iz] = abc_update<EXACT>(um[c + iz + 1], um[c + iz], uo[c + iz + 1], l);
+    // the sweep keeps the value it just wrote in a register (the next cell
+    // reads it), so each face costs one pass over its nop+2 samples; the two
+    // faces touch disjoint samples, so their order does not matter
+    if (top) {
+        float next = uo[c + nop + 1];
+        for (int iz = nop; iz >= 1; iz--) {
+            next = abc_update<EXACT>(um[c + iz + 1], um[c + iz], next, l);
+            uo[c + iz] = next;
         }
-        int iz = g.n1 - nop + iop - 1;
-        uo[c + iz] = abc_update<EXACT>(um[c + iz - 1], um[c + iz], uo[c + iz - 1], h);
+    }
+    float prev = uo[c + g.n1 - nop - 2];
+    for (int iz = g.n1 - nop - 1; iz <= g.n1 - 2; iz++) {
+        prev = abc_update<EXACT>(um[c + iz - 1], um[c + iz], prev, h);
+        uo[c + iz] = prev;
     }
 }
 
@@ -296,53 +303,63 @@ void launch_hybridB(int ndim, int nop, int nbd, bool exact, int fsrf, float *uo,
 }
 
 // ---------------------------------------------------------------------------
-// Sponge over the cells within `width` of any face (each cell exactly once).
+// Sponge over the cells within `width` of any face, each cell exactly once:
+// axis-1 slabs (every line), then axis-2 slabs (axis-1 interior), then
+// axis-3 slabs (axis-1 and axis-2 interior).  32-bit index arithmetic; the
+// axis-2 and axis-3 parts run along axis 1 so their accesses coalesce.
 template <bool EXACT, int NDIM>
-__global__ void k_band_sponge(float *u, const float *__restrict__ w1, const float *__restrict__ w2,
-                              const float *__restrict__ w3, Grid g, int width) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    // part A: axis-1 slabs (all i2, i3); part B: axis-2 slabs; part C: axis-3 slabs
-    const long long W = width, n1 = g.n1, n2 = g.n2, n3 = g.n3;
-    const long long inner1 = n1 - 2 * W, inner2 = n2 - 2 * W;
-    const long long nA = 2 * W * n2 * n3, nB = inner1 * 2 * W * n3, nC = (NDIM == 3) ? inner1 * inner2 * 2 * W : 0;
-    long long i1, i2, i3;
-    if (t < nA) {
-        long long k = t % (2 * W), r = t / (2 * W);
-        i1 = k < W ? k : n1 - 2 * W + k;
-        i2 = r % n2;
-        i3 = r / n2;
-    } else if (t < nA + nB) {
-        long long q = t - nA;
-        i1 = W + q % inner1;
-        long long r = q / inner1, k = r % (2 * W);
-        i2 = k < W ? k : n2 - 2 * W + k;
-        i3 = r / (2 * W);
-    } else if (t < nA + nB + nC) {
-        long long q = t - nA - nB;
-        i1 = W + q % inner1;
-        long long r = q / inner1;
-        i2 = W + r % inner2;
-        long long k = r / inner2;
-        i3 = k < W ? k : n3 - 2 * W + k;
-    } else
-        return;
-    const long long i = (i3 * n2 + i2) * n1 + i1;
-    u[i] = damp_cell<EXACT, NDIM>(u[i], (int)i1, (int)i2, (int)i3, w1, w2, w3);
+__global__ void k_sponge_slab1(float *u, const float *__restrict__ w1, const float *__restrict__ w2,
+                               const float *__restrict__ w3, Grid g, int W) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int per = 2 * W;
+    if (t >= g.n2 * g.n3 * per) return;
+    const int line = t / per, k = t - line * per;
+    const int i1 = k < W ? k : g.n1 - per + k, i2 = line % g.n2, i3 = line / g.n2;
+    const long long i = (long long)line * g.n1 + i1;
+    u[i] = damp_cell<EXACT, NDIM>(u[i], i1, i2, i3, w1, w2, w3);
+}
+
+template <bool EXACT, int NDIM>
+__global__ void k_sponge_slab2(float *u, const float *__restrict__ w1, const float *__restrict__ w2,
+                               const float *__restrict__ w3, Grid g, int W) {
+    const int i1 = W + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i1 >= g.n1 - W) return;
+    const int k = blockIdx.y, i2 = k < W ? k : g.n2 - 2 * W + k, i3 = blockIdx.z;
+    const long long i = ((long long)i3 * g.n2 + i2) * g.n1 + i1;
+    u[i] = damp_cell<EXACT, NDIM>(u[i], i1, i2, i3, w1, w2, w3);
+}
+
+template <bool EXACT>
+__global__ void k_sponge_slab3(float *u, const float *__restrict__ w1, const float *__restrict__ w2,
+                               const float *__restrict__ w3, Grid g, int W) {
+    const int i1 = W + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i1 >= g.n1 - W) return;
+    const int i2 = W + blockIdx.y, k = blockIdx.z, i3 = k < W ? k : g.n3 - 2 * W + k;
+    const long long i = ((long long)i3 * g.n2 + i2) * g.n1 + i1;
+    u[i] = damp_cell<EXACT, 3>(u[i], i1, i2, i3, w1, w2, w3);
+}
+
+template <bool EXACT, int NDIM>
+static void band_sponge_t(int W, float *u, const float *w1, const float *w2, const float *w3, const Grid &g,
+                          cudaStream_t s) {
+    const int T = 128;
+    const long long n1tot = (long long)g.n2 * g.n3 * 2 * W;
+    k_sponge_slab1<EXACT, NDIM><<<(unsigned)((n1tot + 255) / 256), 256, 0, s>>>(u, w1, w2, w3, g, W);
+    const int inner1 = g.n1 - 2 * W;
+    if (inner1 <= 0) return;
+    k_sponge_slab2<EXACT, NDIM><<<dim3((inner1 + T - 1) / T, 2 * W, g.n3), T, 0, s>>>(u, w1, w2, w3, g, W);
+    if (NDIM == 3 && g.n2 - 2 * W > 0)
+        k_sponge_slab3<EXACT><<<dim3((inner1 + T - 1) / T, g.n2 - 2 * W, 2 * W), T, 0, s>>>(u, w1, w2, w3, g, W);
 }
 
 void launch_band_sponge(int ndim, int width, bool exact, float *u, const float *w1, const float *w2, const float *w3,
                         const Grid &g, cudaStream_t s) {
-    const long long W = width, n1 = g.n1, n2 = g.n2, n3 = g.n3;
-    long long total = 2 * W * n2 * n3 + (n1 - 2 * W) * 2 * W * n3;
-    if (ndim == 3) total += (n1 - 2 * W) * (n2 - 2 * W) * 2 * W;
-    const int T = 256;
-    long long blocks = (total + T - 1) / T;
     if (ndim == 3) {
-        if (exact) k_band_sponge<true, 3><<<blocks, T, 0, s>>>(u, w1, w2, w3, g, width);
-        else k_band_sponge<false, 3><<<blocks, T, 0, s>>>(u, w1, w2, w3, g, width);
+        if (exact) band_sponge_t<true, 3>(width, u, w1, w2, w3, g, s);
+        else band_sponge_t<false, 3>(width, u, w1, w2, w3, g, s);
     } else {
-        if (exact) k_band_sponge<true, 2><<<blocks, T, 0, s>>>(u, w1, w2, w3, g, width);
-        else k_band_sponge<false, 2><<<blocks, T, 0, s>>>(u, w1, w2, w3, g, width);
+        if (exact) band_sponge_t<true, 2>(width, u, w1, w2, w3, g, s);
+        else band_sponge_t<false, 2>(width, u, w1, w2, w3, g, s);
     }
 }
 

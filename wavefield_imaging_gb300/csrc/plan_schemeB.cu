@@ -318,10 +318,10 @@ awe_status planB_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, flo
                 if (p->sponge_deferred) {
                     launch_band_sponge(d.ndim, std::max(p->nbd, shell), exact, nxt, p->w[0], p->w[1], p->w[2], g,
                                        s);
-                    launches++;
+                    launches += d.ndim;  // one kernel per slab orientation
                 } else if (shell > 0) {
                     launch_band_sponge(d.ndim, shell, exact, nxt, p->w[0], p->w[1], p->w[2], g, s);
-                    launches++;
+                    launches += d.ndim;
                 }
             }
         }
