@@ -1,0 +1,126 @@
+"""The drop-in RSF programs (sfAWEFD{cart,spher}{2D,3D}gpu, sfAWEFDcart{2D,3D}cpu)
+run as the reference's are run: RSF inputs on the command line and standard
+input, data on standard output, wavefield to wfl=.  GPU cases feed each golden
+fixture's inputs to the program with precision=exact and compare the written
+data and wavefield files with the reference's outputs bit for bit; CPU cases
+cover argument handling, which needs no device."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from helpers import golden_paths, load_golden
+
+import wavefield_imaging_gb300 as awe
+from wavefield_imaging_gb300 import rsf
+from wavefield_imaging_gb300 import build as awe_build
+
+PROGRAM_OF_KIND = {"cart2d": "sfAWEFDcart2Dgpu", "cart3d": "sfAWEFDcart3Dgpu", "polar2d": "sfAWEFDspher2Dgpu",
+                   "spher3d": "sfAWEFDspher3Dgpu"}
+
+
+@pytest.fixture(scope="module")
+def bindir():
+    awe.lib()  # builds libawe.so when missing
+    return awe_build.build_programs()
+
+
+def yn(v):
+    return "y" if v else "n"
+
+
+def write_inputs(tmp, par, a):
+    nd = len(par["n"])
+    rsf.write(str(tmp / "vel.rsf"), a["vel"], [(n, o, d) for n, o, d in zip(par["n"], par["o"], par["d"])])
+    wav = a["wav"]
+    ncs = 1 if wav.ndim == 1 else wav.shape[1]
+    rsf.write(str(tmp / "wav.rsf"), wav.reshape(par["nt"], ncs), [(ncs, 0.0, 1.0), (par["nt"], 0.0, par["dt"])])
+    rsf.write(str(tmp / "sou.rsf"), a["sou"], [(nd, 0.0, 1.0), (a["sou"].shape[0], 0.0, 1.0)])
+    rsf.write(str(tmp / "rec.rsf"), a["rec"], [(nd, 0.0, 1.0), (a["rec"].shape[0], 0.0, 1.0)])
+    args = ["vel=" + str(tmp / "vel.rsf"), "sou=" + str(tmp / "sou.rsf"), "rec=" + str(tmp / "rec.rsf")]
+    for key in ("den", "rfl"):
+        if key in a:
+            rsf.write(str(tmp / (key + ".rsf")), a[key], [(n, o, d) for n, o, d in zip(par["n"], par["o"], par["d"])])
+            args.append("%s=%s" % (key, tmp / (key + ".rsf")))
+    return args
+
+
+def run_program(bindir, name, tmp, args):
+    out = tmp / "dat.rsf"
+    with open(tmp / "wav.rsf", "rb") as fin, open(out, "wb") as fout:
+        r = subprocess.run([os.path.join(bindir, name), *args, "wfl=" + str(tmp / "wfl.rsf")], stdin=fin,
+                           stdout=fout, stderr=subprocess.PIPE, timeout=300)
+    if r.returncode != 0:
+        raise AssertionError("%s failed: %s" % (name, r.stderr.decode()))
+    return out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", golden_paths("A_*.npz"), ids=lambda p: os.path.basename(p)[:-4])
+def test_gpu_program_matches_reference_outputs(bindir, tmp_path, path):
+    par, a = load_golden(path)
+    args = write_inputs(tmp_path, par, a)
+    jsnap = par.get("jsnap", 0)
+    args += ["nb=%d" % par["nb"], "jdata=%d" % par.get("jdata", 1), "snap=" + yn(jsnap > 0),
+             "bnds=" + yn(par.get("bnds", 0)), "free=" + yn(par.get("fsrf", 0)), "expl=" + yn(par.get("expl", 0)),
+             "precision=exact"]
+    if jsnap > 0:
+        args.append("jsnap=%d" % jsnap)
+    if par["kind"] == "cart2d":
+        args.append("refl=" + yn(par.get("refl", 0)))
+    out = run_program(bindir, PROGRAM_OF_KIND[par["kind"]], tmp_path, args)
+    dat, hdr = rsf.read(str(out))
+    np.testing.assert_array_equal(dat.reshape(a["dat"].shape), a["dat"])
+    assert int(hdr["n1"]) == a["rec"].shape[0]
+    if "snaps" in a:
+        wfl, _ = rsf.read(str(tmp_path / "wfl.rsf"))
+        np.testing.assert_array_equal(wfl.ravel(), a["snaps"].ravel())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", golden_paths("c*.npz"), ids=lambda p: os.path.basename(p)[:-4])
+def test_cpu_program_matches_reference_outputs(bindir, tmp_path, path):
+    par, a = load_golden(path)
+    args = write_inputs(tmp_path, par, a)
+    jsnap = par.get("jsnap", 0)
+    args += ["fdorder=%d" % par["fdorder"], "optfd=" + yn(par.get("optfd", 0)), "dabc=" + yn(par.get("dabc", 0)),
+             "free=" + yn(par.get("fsrf", 0)), "hybridbc=" + yn(par.get("hybrid", 0)),
+             "expl=" + yn(par.get("expl", 0)), "snap=" + yn(jsnap > 0), "bnds=" + yn(par.get("bnds", 0)),
+             "precision=exact"]
+    if par.get("nb", -1) >= 0:
+        args.append("nb=%d" % par["nb"])
+    if jsnap > 0:
+        args.append("jsnap=%d" % jsnap)
+    name = "sfAWEFDcart%dDcpu" % len(par["n"])
+    out = run_program(bindir, name, tmp_path, args)
+    dat, _ = rsf.read(str(out))
+    np.testing.assert_array_equal(dat.reshape(a["dat"].shape), a["dat"])
+    if "snaps" in a:
+        wfl, _ = rsf.read(str(tmp_path / "wfl.rsf"))
+        np.testing.assert_array_equal(wfl.ravel(), a["snaps"].ravel())
+
+
+def _run_bare(bindir, name, args):
+    return subprocess.run([os.path.join(bindir, name), *args], stdin=subprocess.DEVNULL, capture_output=True,
+                          timeout=60)
+
+
+@pytest.mark.parametrize("arg,msg", [("adj=y", "adj=y"), ("sinc=y", "sinc=y"), ("nqz=10", "snapshot windows")])
+def test_unsupported_options_stop_with_an_error(bindir, arg, msg):
+    r = _run_bare(bindir, "sfAWEFDcart2Dcpu", [arg])
+    assert r.returncode == 1
+    assert msg in r.stderr.decode()
+
+
+def test_missing_input_stops_with_an_error(bindir, tmp_path):
+    r = _run_bare(bindir, "sfAWEFDspher2Dgpu", ["vel=" + str(tmp_path / "absent.rsf")])
+    assert r.returncode == 1
+    assert r.stderr
+
+
+def test_every_program_name_is_installed(bindir):
+    for name in awe_build.PROGRAM_NAMES:
+        assert os.access(os.path.join(bindir, name), os.X_OK), name
+    r = _run_bare(bindir, "awe_prog", [])
+    assert r.returncode == 1

@@ -77,6 +77,34 @@ void launch_extract_off(int ndim, bool exact, const float *u, const GeoPoint *pt
 void launch_snapshot(int ndim, const float *u, float *dst, const Grid &g, int f1, int f2, int f3, int m1, int m2,
                      int m3, const float *w1, const float *w2, const float *w3, cudaStream_t s);
 
+// ---- scheme of the reference GPU programs (MAWEFD{cart,spher}{2D,3D}gpu.cu) ----
+struct StepAParams {
+    Grid g;
+    int geom;        // 0 cart 2D, 1 cart 3D, 2 polar 2D, 3 spherical 3D
+    int nd;          // 2 or 3
+    int nb;          // sponge width
+    int pri[3];      // sponge priority over memory axes (the kernel's x, y, z)
+    int mask;        // 0 none, 1 cart 2D x band, 2 cart 3D z < nb, 3 r band (polar/spherical)
+    int spill;       // samples of the next line zeroed by the free-surface grid rounding
+    int shell, shell_axes;  // boundary shell width and the axes it spans (bit a = axis a+1)
+    float dt2;
+    float dd1, dd2, dd3, dd4, dd5;  // divisors of the Laplacian terms
+    float a0;                       // polar centre weight -2/dra^2
+    const float *tr0, *tr1, *tr2, *tr3;  // per-radius tables
+    const float *tt0, *tt1;              // per-(theta, r) tables (spherical)
+    const double *dtab;                  // sponge factor by index (FP64, as the reference)
+    const float *ftab;                   // the same rounded to float (FAST mode)
+    float b2lo, b2hi;                    // 2D one-way coefficients at the last sample
+    const float *tb[6];                  // cart 3D one-way coefficient tables
+};
+void launch_stepA(int geom, bool exact, const float *cur, float *nxt, const float *vel, const StepAParams &p,
+                  cudaStream_t s);
+void launch_bcA(bool exact, const float *um, float *uo, float *aux, const StepAParams &p, cudaStream_t s);
+void launch_injectA(bool exact, int ndim, float *u, const GeoPoint *pts, const float *scale, int ns, const float *wav,
+                    int it, bool scaled, const long long *off, cudaStream_t s);
+void launch_snapshot_transpose2(const float *u, float *dst, const Grid &g, int f1, int f2, int m1, int m2,
+                                cudaStream_t s);
+
 // ---- host-side math (bit-identical to the reference's float evaluation) ----
 void fd_coefficients(int nop, int ndim, const float *dd, int optfd, Coef &k);
 void sponge_weights(int nb, std::vector<float> &w);   // fdutil.c sponge_make

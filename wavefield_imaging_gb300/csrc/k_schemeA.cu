@@ -1,0 +1,312 @@
+// Kernels for the scheme of the reference's GPU programs
+// (CODE/MAWEFD{cart,spher}{2D,3D}gpu.cu over cart_kernels.cu / spher_kernels.cu):
+// 2nd-order Laplacian (cartesian, polar, or spherical with metric terms),
+// injection into the current level before the update, one-way boundary,
+// quadratic-alpha sponge on both time levels, free-surface masks.
+//
+// Two buffers hold the time levels.  The reference shifts three (ppo <- po,
+// po <- fpo) and then sponges both po and ppo; here the new level overwrites
+// the previous one in place and the sponge of the level that becomes
+// "previous" is applied when it is next read, the same float operation on the
+// same value.  Cells that the one-way boundary rewrites or reads (the
+// `shell`) are stored unsponged by the step kernel and finished by a two-phase
+// boundary pass: phase 1 computes the boundary values from the unmodified
+// fields (every read sees the field before the pass - the race-free reading
+// of the reference's boundary kernels), phase 2 writes them with the sponge
+// and masks.
+#include <cuda_runtime.h>
+
+#include "awe_internal.h"
+#include "fp_exact.cuh"
+
+namespace awe {
+
+// reference sponge factor, FP64 as in spongeKernel_2D/3D
+template <bool EXACT>
+__device__ __forceinline__ float damp_a(float v, int i, const double *__restrict__ dtab,
+                                        const float *__restrict__ ftab) {
+    if (i == 0) return v;
+    if constexpr (EXACT) return (float)((double)v * dtab[i]);
+    else return v * ftab[i];
+}
+
+// sponge index: priority over memory axes pri[0..nd-1] (the kernel's x, y, z)
+__device__ __forceinline__ int sponge_index(const int *c, const int *n, const StepAParams &p) {
+    const int nb = p.nb;
+    bool low = false, high = false;
+    for (int k = 0; k < p.nd; k++) {
+        const int a = p.pri[k];
+        low = low || c[a] < nb;
+        high = high || c[a] > n[a] - nb;
+    }
+    if (low) {
+        for (int k = 0; k < p.nd; k++) {
+            const int a = p.pri[k];
+            if (c[a] < nb) return nb - c[a];
+        }
+    }
+    if (high) {
+        for (int k = 0; k < p.nd; k++) {
+            const int a = p.pri[k];
+            if (c[a] > n[a] - nb) return c[a] - (n[a] - nb);
+        }
+    }
+    return 0;
+}
+
+// free-surface masks (value forced to zero), see StepAParams::mask
+__device__ __forceinline__ bool masked(const int *c, const int *n, const StepAParams &p) {
+    switch (p.mask) {
+        case 1:  // cart 2D: x > nxpad - nb, plus the next-row spill of the rounded-up grid
+            return c[1] > n[1] - p.nb || (c[1] < p.spill && c[0] >= 1);
+        case 2:  // cart 3D (before the boundary): z < nb
+            return c[0] < p.nb;
+        case 3:  // polar / spherical: r > nrapad - nb, plus the next-line spill
+            return c[0] > n[0] - p.nb || (c[0] < p.spill && (c[1] >= 1 || c[2] >= 1));
+    }
+    return false;
+}
+
+__device__ __forceinline__ bool in_shell(const int *c, const int *n, const StepAParams &p) {
+    if (p.shell_axes == 0) return false;
+    for (int a = 0; a < 3; a++)
+        if ((p.shell_axes >> a) & 1)
+            if (c[a] < p.shell || c[a] >= n[a] - p.shell) return true;
+    return false;
+}
+
+template <int GEOM, bool EXACT>
+__device__ __forceinline__ float laplacian(const float *__restrict__ A, long long i, const int *c,
+                                           const StepAParams &p) {
+    const long long s2 = p.g.n1, s3 = (long long)p.g.n1 * p.g.n2;
+    const float u = A[i];
+    const float u2 = fadd<EXACT>(u, u);  // 2*p, exact
+    auto d2 = [&](float m, float pl) {   // (p[+1] - 2 p) + p[-1]
+        return fadd<EXACT>(fsub<EXACT>(pl, u2), m);
+    };
+    auto div = [&](float a, float b) { return EXACT ? __fdiv_rn(a, b) : a / b; };
+    if constexpr (GEOM == 0) {  // cart 2D (x = axis 2, z = axis 1): pxx + pzz
+        const float pxx = div(d2(A[i - s2], A[i + s2]), p.dd2);
+        const float pzz = div(d2(A[i - 1], A[i + 1]), p.dd1);
+        return fadd<EXACT>(pxx, pzz);
+    } else if constexpr (GEOM == 1) {  // cart 3D: (pxx + pyy) + pzz
+        const float pxx = div(d2(A[i - s2], A[i + s2]), p.dd2);
+        const float pyy = div(d2(A[i - s3], A[i + s3]), p.dd3);
+        const float pzz = div(d2(A[i - 1], A[i + 1]), p.dd1);
+        return fadd<EXACT>(fadd<EXACT>(pxx, pyy), pzz);
+    } else if constexpr (GEOM == 2) {  // polar (r = axis 1, theta = axis 2)
+        const int ir = c[0];
+        const float am = __ldg(p.tr0 + ir), ap = __ldg(p.tr1 + ir), b = __ldg(p.tr2 + ir), b0 = __ldg(p.tr3 + ir);
+        const float compra =
+            fadd<EXACT>(fadd<EXACT>(fmul<EXACT>(am, A[i - 1]), fmul<EXACT>(p.a0, u)), fmul<EXACT>(ap, A[i + 1]));
+        const float compth =
+            fadd<EXACT>(fadd<EXACT>(fmul<EXACT>(b, A[i - s2]), fmul<EXACT>(b0, u)), fmul<EXACT>(b, A[i + s2]));
+        return fadd<EXACT>(compra, compth);
+    } else {  // spherical (r = axis 1, theta = axis 2, phi = axis 3)
+        const int ir = c[0];
+        const float pra = div(fsub<EXACT>(A[i + 1], A[i - 1]), p.dd1);        // / (2 dra)
+        const float ppra = div(d2(A[i - 1], A[i + 1]), p.dd2);                  // / dra^2
+        const float pth = div(fsub<EXACT>(A[i + s2], A[i - s2]), p.dd3);      // / (2 dth)
+        const float ppth = div(d2(A[i - s2], A[i + s2]), p.dd4);                // / dth^2
+        const float ppph = div(d2(A[i - s3], A[i + s3]), p.dd5);                // / dph^2
+        const long long t = (long long)c[1] * p.g.n1 + ir;
+        const float A2 = __ldg(p.tr0 + ir), Cr = __ldg(p.tr1 + ir), B = __ldg(p.tt0 + t), D = __ldg(p.tt1 + t);
+        float lap = fadd<EXACT>(fmul<EXACT>(A2, pra), ppra);
+        lap = fadd<EXACT>(lap, fmul<EXACT>(B, pth));
+        lap = fadd<EXACT>(lap, fmul<EXACT>(Cr, ppth));
+        return fadd<EXACT>(lap, fmul<EXACT>(D, ppph));
+    }
+}
+
+// One step: nxt (previous level, sponge pending) <- new level.
+template <int GEOM, bool EXACT>
+__global__ void __launch_bounds__(256) k_stepA(const float *__restrict__ cur, float *__restrict__ nxt,
+                                               const float *__restrict__ vel, const StepAParams p) {
+    const int i1 = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i2 = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i3 = blockIdx.z;
+    const Grid g = p.g;
+    if (i1 >= g.n1 || i2 >= g.n2) return;
+    const int c[3] = {i1, i2, i3}, n[3] = {g.n1, g.n2, g.n3};
+    const long long i = ((long long)i3 * g.n2 + i2) * g.n1 + i1;
+    const int si = sponge_index(c, n, p);
+    const float q = damp_a<EXACT>(nxt[i], si, p.dtab, p.ftab);  // previous level, its sponge applied now
+    bool interior = true;
+    for (int a = 0; a < p.nd; a++) interior = interior && c[a] >= 4 && c[a] < n[a] - 4;
+    const float lap = interior ? laplacian<GEOM, EXACT>(cur, i, c, p) : 0.f;
+    const float v = __ldg(vel + i), u = cur[i];
+    // cart: (dt*dt)*(v*v*lap) + 2p - pp ; polar/spherical: (dt*dt)*(v*v)*lap + 2p - pp
+    float a;
+    if constexpr (GEOM <= 1)
+        a = fmul<EXACT>(p.dt2, fmul<EXACT>(fmul<EXACT>(v, v), lap));
+    else
+        a = fmul<EXACT>(fmul<EXACT>(p.dt2, fmul<EXACT>(v, v)), lap);
+    float f = fsub<EXACT>(fadd<EXACT>(a, fadd<EXACT>(u, u)), q);
+    if (!in_shell(c, n, p)) {
+        if (p.mask && masked(c, n, p)) f = 0.f;
+        f = damp_a<EXACT>(f, si, p.dtab, p.ftab);
+    }
+    nxt[i] = f;
+}
+
+template <bool EXACT>
+static void step_geom(int geom, const float *cur, float *nxt, const float *vel, const StepAParams &p, cudaStream_t s) {
+    dim3 block(64, 4, 1), grid((p.g.n1 + 63) / 64, (p.g.n2 + 3) / 4, p.g.n3);
+    switch (geom) {
+        case 0: k_stepA<0, EXACT><<<grid, block, 0, s>>>(cur, nxt, vel, p); break;
+        case 1: k_stepA<1, EXACT><<<grid, block, 0, s>>>(cur, nxt, vel, p); break;
+        case 2: k_stepA<2, EXACT><<<grid, block, 0, s>>>(cur, nxt, vel, p); break;
+        default: k_stepA<3, EXACT><<<grid, block, 0, s>>>(cur, nxt, vel, p); break;
+    }
+}
+
+void launch_stepA(int geom, bool exact, const float *cur, float *nxt, const float *vel, const StepAParams &p,
+                  cudaStream_t s) {
+    if (exact) step_geom<true>(geom, cur, nxt, vel, p, s);
+    else step_geom<false>(geom, cur, nxt, vel, p, s);
+}
+
+// ---------------------------------------------------------------------------
+// One-way boundary, phase 1: boundary values from the unmodified fields.
+// um = the level that just became "previous" (before its sponge), uo = the
+// new level as stored by the step kernel (unsponged inside the shell).
+template <bool EXACT>
+__device__ __forceinline__ float oneway(float um_n, float um_c, float uo_n, float b) {
+    return fadd<EXACT>(um_n, fmul<EXACT>(fsub<EXACT>(um_c, uo_n), b));
+}
+
+// 2D programs: rows 1..4 and n-5..n-2 of the swept axis, read from the last
+// sample of the other axis (the reference kernel's loop leaves that one).
+// geom 0: swept axis z (axis 1), other axis x (axis 2), rows limited to < nxpad
+// geom 2: swept axis theta (axis 2), other axis r (axis 1)
+template <bool EXACT>
+__global__ void k_bcA2_phase1(const float *__restrict__ um, const float *__restrict__ uo, float *__restrict__ aux,
+                              const StepAParams p) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const Grid g = p.g;
+    const bool cart = p.geom == 0;
+    const int nsw = cart ? g.n1 : g.n2, noth = cart ? g.n2 : g.n1;
+    if (t >= 8 * noth) return;
+    const int k = t / noth, o = t % noth;  // k: 0..3 top rows 1..4, 4..7 bottom rows n-5..n-2
+    const int row = k < 4 ? 1 + k : nsw - 5 + (k - 4);
+    if (cart && row >= g.n2) return;  // the kernel's `iz < nxpad` test
+    auto at = [&](int r, int oo) -> long long {
+        return cart ? (long long)oo * g.n1 + r : (long long)r * g.n1 + oo;
+    };
+    const int nbr = k < 4 ? row + 1 : row - 1;
+    const float b = k < 4 ? p.b2lo : p.b2hi;
+    aux[at(row, o)] = oneway<EXACT>(um[at(nbr, noth - 1)], um[at(row, o)], uo[at(nbr, noth - 1)], b);
+}
+
+// cart 3D (onewayBC_3D): cells within 4 (low) / 5 (high) of a face; the last
+// applicable face formula wins; neighbours read masked (z < nb zeroed).
+template <bool EXACT>
+__global__ void k_bcA3_phase1(const float *__restrict__ um, const float *__restrict__ uo, float *__restrict__ aux,
+                              const StepAParams p) {
+    const int i1 = blockIdx.x * blockDim.x + threadIdx.x;  // z
+    const int i2 = blockIdx.y, i3 = blockIdx.z;           // x, y
+    const Grid g = p.g;
+    if (i1 >= g.n1) return;
+    const int iz = i1, ix = i2, iy = i3;
+    const bool zl = iz <= 4, zh = iz >= g.n1 - 5, xl = ix <= 4, xh = ix >= g.n2 - 5, yl = iy <= 4, yh = iy >= g.n3 - 5;
+    if (!(zl || zh || xl || xh || yl || yh)) return;
+    const long long s2 = g.n1, s3 = (long long)g.n1 * g.n2, c = iy * s3 + ix * s2 + iz;
+    auto ps = [&](long long n, int nz) { return nz < p.nb ? 0.f : uo[n]; };  // freeSurf_3D before the boundary
+    const int nx = g.n2, nz = g.n1;
+    float val = 0.f;
+    if (zl) val = oneway<EXACT>(um[c + 1], um[c], ps(c + 1, iz + 1), p.tb[0][iy * nx + ix]);
+    if (zh) val = oneway<EXACT>(um[c - 1], um[c], ps(c - 1, iz - 1), p.tb[1][iy * nx + ix]);
+    if (xl) val = oneway<EXACT>(um[c + s2], um[c], ps(c + s2, iz), p.tb[2][iy * nz + iz]);
+    if (xh) val = oneway<EXACT>(um[c - s2], um[c], ps(c - s2, iz), p.tb[1][iy * nz + iz]);  // the z-high table, as the reference
+    if (yl) val = oneway<EXACT>(um[c + s3], um[c], ps(c + s3, iz), p.tb[4][iz * nx + ix]);
+    if (yh) val = oneway<EXACT>(um[c - s3], um[c], ps(c - s3, iz), p.tb[5][iz * nx + ix]);
+    aux[c] = val;
+}
+
+// phase 2: every shell cell gets its final value: the boundary value where
+// the boundary applies, else the (masked) new level; then sponge and masks.
+template <bool EXACT>
+__global__ void k_bcA_phase2(float *__restrict__ uo, const float *__restrict__ aux, const StepAParams p) {
+    const int i1 = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i2 = blockIdx.y, i3 = blockIdx.z;
+    const Grid g = p.g;
+    if (i1 >= g.n1) return;
+    const int c[3] = {i1, i2, i3}, n[3] = {g.n1, g.n2, g.n3};
+    if (!in_shell(c, n, p)) return;
+    const long long i = ((long long)i3 * g.n2 + i2) * g.n1 + i1;
+    bool bc;
+    if (p.geom == 0) bc = ((i1 >= 1 && i1 <= 4) || (i1 >= g.n1 - 5 && i1 <= g.n1 - 2)) && i1 < g.n2;
+    else if (p.geom == 2) bc = (i2 >= 1 && i2 <= 4) || (i2 >= g.n2 - 5 && i2 <= g.n2 - 2);
+    else bc = i1 <= 4 || i1 >= g.n1 - 5 || i2 <= 4 || i2 >= g.n2 - 5 || i3 <= 4 || i3 >= g.n3 - 5;
+    float v = uo[i];
+    if (p.geom == 1 && masked(c, n, p)) v = 0.f;  // cart 3D: free surface before the boundary
+    if (bc) v = aux[i];
+    v = damp_a<EXACT>(v, sponge_index(c, n, p), p.dtab, p.ftab);
+    if (p.geom != 1 && p.mask && masked(c, n, p)) v = 0.f;  // 2D programs: free surface after the sponge
+    uo[i] = v;
+}
+
+void launch_bcA(bool exact, const float *um, float *uo, float *aux, const StepAParams &p, cudaStream_t s) {
+    const Grid &g = p.g;
+    const int T = 128;
+    if (p.geom == 0 || p.geom == 2) {
+        const int noth = p.geom == 0 ? g.n2 : g.n1;
+        const int n = 8 * noth;
+        if (exact) k_bcA2_phase1<true><<<(n + T - 1) / T, T, 0, s>>>(um, uo, aux, p);
+        else k_bcA2_phase1<false><<<(n + T - 1) / T, T, 0, s>>>(um, uo, aux, p);
+    } else {
+        dim3 grid((g.n1 + T - 1) / T, g.n2, g.n3);
+        if (exact) k_bcA3_phase1<true><<<grid, T, 0, s>>>(um, uo, aux, p);
+        else k_bcA3_phase1<false><<<grid, T, 0, s>>>(um, uo, aux, p);
+    }
+    dim3 grid2((g.n1 + T - 1) / T, g.n2, g.n3);
+    if (exact) k_bcA_phase2<true><<<grid2, T, 0, s>>>(uo, aux, p);
+    else k_bcA_phase2<false><<<grid2, T, 0, s>>>(uo, aux, p);
+}
+
+// ---------------------------------------------------------------------------
+// Injection into the current level before the update
+// (inject_sources_{2D,3D}{_const,,_refl}): u[node] += (wa * w) [* scale],
+// sources and corners in order; the per-corner scale (reflectivity) is
+// constant over time and prepared on the host.
+template <bool EXACT>
+__global__ void k_injectA(float *u, const GeoPoint *__restrict__ pts, const float *__restrict__ scale, int ns,
+                          const float *__restrict__ wav, int it, int ncorner, int scaled,
+                          const long long *__restrict__ off) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    const float wa = wav[it];
+    for (int s = 0; s < ns; s++) {
+        const GeoPoint pt = pts[s];
+        for (int c = 0; c < ncorner; c++) {
+            const long long n = pt.base + off[c];
+            float a = fmul<EXACT>(wa, pt.w[c]);
+            if (scaled) a = fmul<EXACT>(a, scale[s * 8 + c]);
+            u[n] = fadd<EXACT>(u[n], a);
+        }
+    }
+}
+
+void launch_injectA(bool exact, int ndim, float *u, const GeoPoint *pts, const float *scale, int ns, const float *wav,
+                    int it, bool scaled, const long long *off, cudaStream_t s) {
+    if (ns <= 0) return;
+    const int nc = ndim == 3 ? 8 : 4;
+    if (exact) k_injectA<true><<<1, 32, 0, s>>>(u, pts, scale, ns, wav, it, nc, scaled, off);
+    else k_injectA<false><<<1, 32, 0, s>>>(u, pts, scale, ns, wav, it, nc, scaled, off);
+}
+
+// polar snapshots are theta-fastest ([r][theta]) as sfAWEFDspher2Dgpu writes them
+__global__ void k_snapshot_transpose2(const float *__restrict__ u, float *__restrict__ dst, Grid g, int f1, int f2,
+                                      int m1, int m2) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)m1 * m2) return;
+    const int j2 = (int)(t % m2), j1 = (int)(t / m2);  // dst[j1][j2], j2 (theta) fastest
+    dst[t] = u[(long long)(f2 + j2) * g.n1 + (f1 + j1)];
+}
+
+void launch_snapshot_transpose2(const float *u, float *dst, const Grid &g, int f1, int f2, int m1, int m2,
+                                cudaStream_t s) {
+    const long long n = (long long)m1 * m2;
+    k_snapshot_transpose2<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(u, dst, g, f1, f2, m1, m2);
+}
+
+}  // namespace awe

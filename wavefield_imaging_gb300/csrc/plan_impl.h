@@ -40,11 +40,15 @@ struct awe_plan {
     long long *corner_off = nullptr;  // device [8]
     long long h_corner_off[8] = {0};
     std::vector<awe::GeoPoint> h_src, h_rec;
+    std::vector<awe::Lint> h_src_lint;  // source corner indices in the reference's fdm axes
     bool sponge_deferred = false;  // a source node lies in the sponge band outside the boundary shell
 
     // scheme-GPU specific
-    float *aux = nullptr;  // scratch for boundary passes
-    float *metric = nullptr;  // per-index metric tables (spherical)
+    float *aux = nullptr;              // boundary values (phase 1 -> phase 2)
+    awe::StepAParams pa{};             // step / boundary parameters
+    std::vector<float> h_rfl_pad;      // padded reflectivity image (cart 2D refl=y)
+    float *inj_scale = nullptr;        // per source corner injection scale
+    int snap_transpose = 0;            // polar snapshots are theta-fastest
 
     bool model_set = false, geom_set = false;
     awe_snap_fn snap_cb = nullptr;

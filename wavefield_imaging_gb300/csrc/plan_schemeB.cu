@@ -201,8 +201,9 @@ awe_status set_geometry_common(awe_plan *p, int ns, const float *sou, int nr, co
     std::memcpy(p->h_corner_off, off, sizeof off);
     CUDA_TRY(cudaMemcpy(p->corner_off, off, sizeof off, cudaMemcpyHostToDevice));
 
-    auto make = [&](const float *xyz, int n, std::vector<GeoPoint> &out) {
+    auto make = [&](const float *xyz, int n, std::vector<GeoPoint> &out, std::vector<Lint> *keep) {
         out.resize(n);
+        if (keep) keep->resize(n);
         for (int i = 0; i < n; i++) {
             float x, y = 0.f, z;
             if (nd == 2) {
@@ -218,10 +219,11 @@ awe_status set_geometry_common(awe_plan *p, int ns, const float *sou, int nr, co
             gp.base = l.jz * sz + l.jx * sx + (nd == 3 ? l.jy * sy : 0);
             std::memcpy(gp.w, l.w, sizeof gp.w);
             out[i] = gp;
+            if (keep) (*keep)[i] = l;
         }
     };
-    make(sou, ns, p->h_src);
-    make(rec, nr, p->h_rec);
+    make(sou, ns, p->h_src, &p->h_src_lint);
+    make(rec, nr, p->h_rec, nullptr);
     if (p->src) dev_free(p, p->src);
     if (p->rec) dev_free(p, p->rec);
     p->src = p->rec = nullptr;

@@ -1,0 +1,230 @@
+/* Drop-in replacements for the reference's RSF programs
+ *   sfAWEFDcart2Dgpu  (CODE/MAWEFDcart2Dgpu.cu)
+ *   sfAWEFDcart3Dgpu  (CODE/MAWEFDcart3Dgpu.cu)
+ *   sfAWEFDspher2Dgpu (CODE/MAWEFDspher2Dgpu.cu)
+ *   sfAWEFDspher3Dgpu (CODE/MAWEFDspher3Dgpu.cu)
+ *   sfAWEFDcart2Dcpu  (CODE/MAWEFDcart2Dcpu.c, run on the GPU)
+ *   sfAWEFDcart3Dcpu  (CODE/MAWEFDcart3Dcpu.c, run on the GPU)
+ * on the engine's C-ABI (include/awe.h).  One source; the program name picks
+ * the geometry and the scheme.  Usage as the reference:
+ *
+ *   sfAWEFDcart2Dgpu < wav.rsf vel=vel.rsf sou=sou.rsf rec=rec.rsf [rfl=rfl.rsf] wfl=wfl.rsf > dat.rsf [params]
+ *
+ * Parameters and defaults are those of each program's main() (cited below).
+ * Extra parameter: precision=exact|fast (default fast; exact reproduces the
+ * reference's float/double evaluation bit for bit).
+ * Not provided: adj=y back-injection, sinc=y injection and the snapshot
+ * windows nq*=/oq*=/dq*= of the cpu programs (they stop with an error).
+ * Header differences: sfAWEFDspher3Dgpu's data and wavefield headers hold
+ * the rows and frames actually written (the reference declares nt/jdata rows
+ * and one frame more than it writes).
+ * Errors print to stderr and exit 1, as sf_error. */
+#include <libgen.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "awe.h"
+#include "rsfio.h"
+
+static void die(const char *what, const char *msg) {
+    fprintf(stderr, "%s: %s\n", what, msg);
+    exit(1);
+}
+
+static rsf_file *g_wfl = NULL;
+
+static void write_frame(void *user, int isnap, int it, const float *frame, size_t n) {
+    (void)user;
+    (void)isnap;
+    (void)it;
+    if (rsf_write(g_wfl, frame, n) != n) die("wfl", "short write");
+}
+
+int main(int argc, char **argv) {
+    rsf_init(argc, argv);
+    char name[256];
+    snprintf(name, sizeof name, "%s", argv[0]);
+    const char *prog = basename(name);
+    const int spher = strstr(prog, "spher") != NULL;
+    const int ndim = strstr(prog, "3D") != NULL ? 3 : 2;
+    const int cart2d = !spher && ndim == 2;
+    const int scheme = strstr(prog, "cpu") != NULL ? AWE_SCHEME_CPU : AWE_SCHEME_GPU;
+    if (scheme == AWE_SCHEME_CPU && spher) die(prog, "the spherical cpu programs are not provided");
+    if (!strstr(prog, "AWEFD")) die(prog, "run as sfAWEFD{cart,spher}{2D,3D}gpu or sfAWEFDcart{2D,3D}cpu");
+
+    /* flags and defaults: MAWEFDcart2Dgpu.cu:74-80, MAWEFDcart3Dgpu.cu:62-68,
+     * MAWEFDspher2Dgpu.cu:65-69, MAWEFDspher3Dgpu.cu:88-94,
+     * MAWEFDcart{2D,3D}cpu.c:116-128 */
+    int fsrf = 0, dabc = 0, snap, bnds, expl, refl = 0, adj = 0, verb = 0, sinc = 0;
+    if (scheme == AWE_SCHEME_CPU) {
+        snap = bnds = expl = 0;
+    } else {
+        snap = cart2d || (spher && ndim == 2);
+        bnds = cart2d;
+        expl = 1;
+        refl = cart2d;
+    }
+    if (!rsf_get_bool("free", &fsrf) && scheme == AWE_SCHEME_CPU) rsf_get_bool("fsrf", &fsrf);
+    rsf_get_bool("dabc", &dabc);
+    rsf_get_bool("snap", &snap);
+    rsf_get_bool("bnds", &bnds);
+    rsf_get_bool("expl", &expl);
+    if (cart2d && scheme == AWE_SCHEME_GPU) rsf_get_bool("refl", &refl);
+    rsf_get_bool("adj", &adj);
+    rsf_get_bool("verb", &verb);
+    rsf_get_bool("sinc", &sinc);
+    if (adj) die(prog, "adj=y (back-injection imaging) is not provided");
+    if (sinc) die(prog, "sinc=y injection is not provided");
+    {
+        static const char *win[] = {"nqz", "nqx", "nqy", "oqz", "oqx", "oqy", "dqz", "dqx", "dqy"};
+        for (int i = 0; i < 9; i++)
+            if (rsf_get_string(win[i])) die(prog, "snapshot windows (nq*/oq*/dq*) are not provided");
+    }
+    const char *prec_s = rsf_get_string("precision");
+    const int precision = (prec_s && strcmp(prec_s, "exact") == 0) ? AWE_EXACT : AWE_FAST;
+    int gpu = 0;
+    rsf_get_int("gpu", &gpu);
+
+    rsf_file *Fwav = rsf_input("in"), *Fvel = rsf_input("vel"), *Fsou = rsf_input("sou"), *Frec = rsf_input("rec");
+    if (!Fwav || !Fvel || !Fsou || !Frec) die(prog, rsf_error());
+    rsf_file *Frfl = NULL, *Fden = NULL;
+    if (scheme == AWE_SCHEME_GPU && cart2d && refl && expl) {
+        Frfl = rsf_input("rfl");
+        if (!Frfl) die(prog, rsf_error());
+    }
+    int cden = 0;
+    rsf_get_bool("cden", &cden);
+    if (scheme == AWE_SCHEME_CPU && !cden && rsf_get_string("den")) {
+        Fden = rsf_input("den");
+        if (!Fden) die(prog, rsf_error());
+    }
+
+    /* axes: wavelet n1 = components, n2 = time; model axes 1..ndim */
+    const int nt = rsf_n(Fwav, 2), ncs = rsf_n(Fwav, 1);
+    const float dt = rsf_d(Fwav, 2), ot = rsf_o(Fwav, 2);
+    awe_desc d;
+    memset(&d, 0, sizeof d);
+    d.coords = spher ? AWE_SPHER : AWE_CART;
+    d.scheme = scheme;
+    d.ndim = ndim;
+    for (int a = 0; a < 3; a++) {
+        d.n[a] = a < ndim ? rsf_n(Fvel, a + 1) : 1;
+        d.d[a] = a < ndim ? rsf_d(Fvel, a + 1) : 1.f;
+        d.o[a] = a < ndim ? rsf_o(Fvel, a + 1) : 0.f;
+    }
+    d.nb = -1;
+    rsf_get_int("nb", &d.nb);
+    d.nt = nt;
+    d.dt = dt;
+    d.jdata = 1;
+    rsf_get_int("jdata", &d.jdata);
+    d.jsnap = 0;
+    if (snap) {
+        d.jsnap = nt;
+        rsf_get_int("jsnap", &d.jsnap);
+    }
+    d.bnds = bnds;
+    d.fsrf = fsrf;
+    d.expl = expl;
+    d.refl = refl && expl;
+    d.precision = precision;
+    if (scheme == AWE_SCHEME_CPU) {
+        d.fdorder = 4;
+        rsf_get_int("fdorder", &d.fdorder);
+        rsf_get_bool("optfd", &d.optfd);
+        d.dabc = dabc;
+        rsf_get_bool("hybridbc", &d.hybrid);
+    }
+
+    /* points: n1 coordinates, count = n2 (* n3 for the programs that read it:
+     * MAWEFDcart2Dgpu.cu:120, MAWEFDcart3Dgpu.cu:105, MAWEFDspher2Dgpu.cu:104) */
+    const int ncoord = ndim;
+    const int use_n3 = scheme == AWE_SCHEME_GPU && !(spher && ndim == 3);
+    const int ns = rsf_n(Fsou, 2) * (use_n3 ? rsf_n(Fsou, 3) : 1);
+    const int nr = rsf_n(Frec, 2) * (use_n3 ? rsf_n(Frec, 3) : 1);
+    if (rsf_n(Fsou, 1) < ncoord || rsf_n(Frec, 1) < ncoord) die(prog, "sou/rec need one coordinate per axis on n1");
+    float *sou = malloc(sizeof(float) * (size_t)ns * ncoord), *rec = malloc(sizeof(float) * (size_t)nr * ncoord);
+    float tmp[4];
+    for (int i = 0; i < ns; i++) {
+        if (rsf_read(Fsou, tmp, (size_t)rsf_n(Fsou, 1)) != (size_t)rsf_n(Fsou, 1)) die(prog, "short read (sou)");
+        memcpy(sou + (size_t)i * ncoord, tmp, sizeof(float) * ncoord);
+    }
+    for (int i = 0; i < nr; i++) {
+        if (rsf_read(Frec, tmp, (size_t)rsf_n(Frec, 1)) != (size_t)rsf_n(Frec, 1)) die(prog, "short read (rec)");
+        memcpy(rec + (size_t)i * ncoord, tmp, sizeof(float) * ncoord);
+    }
+    const size_t nmodel = (size_t)d.n[0] * d.n[1] * d.n[2];
+    float *vel = malloc(sizeof(float) * nmodel), *rfl = NULL, *den = NULL;
+    if (rsf_read(Fvel, vel, nmodel) != nmodel) die(prog, "short read (vel)");
+    if (Frfl) {
+        rfl = malloc(sizeof(float) * nmodel);
+        if (rsf_read(Frfl, rfl, nmodel) != nmodel) die(prog, "short read (rfl)");
+    }
+    if (Fden) {
+        den = malloc(sizeof(float) * nmodel);
+        if (rsf_read(Fden, den, nmodel) != nmodel) die(prog, "short read (den)");
+    }
+    const size_t nwav = (size_t)nt * ncs;
+    float *wav = malloc(sizeof(float) * nwav);
+    if (rsf_read(Fwav, wav, nwav) != nwav) die(prog, "short read (wavelet)");
+    /* the GPU programs inject d_ww[it] for every source; the CPU programs one
+     * value per source per step (expl=n) or one for all (expl=y) */
+    int wcs = 1;
+    if (scheme == AWE_SCHEME_CPU && !expl) wcs = ns;
+    if (wcs > ncs && nwav < (size_t)nt * wcs) die(prog, "wavelet has fewer components than sources");
+
+    awe_plan *plan = NULL;
+    if (awe_plan_create(&d, gpu, &plan) != AWE_OK) die(prog, awe_last_error());
+    if (awe_set_model(plan, vel, den, scheme == AWE_SCHEME_GPU ? rfl : NULL) != AWE_OK) die(prog, awe_last_error());
+    if (awe_set_geometry(plan, ns, sou, nr, rec) != AWE_OK) die(prog, awe_last_error());
+    awe_info info;
+    awe_plan_info(plan, &info);
+
+    rsf_file *Fdat = rsf_output("out");
+    if (!Fdat) die(prog, rsf_error());
+    rsf_set_axis(Fdat, 1, nr, rsf_o(Frec, 2), rsf_d(Frec, 2), "r");
+    rsf_set_axis(Fdat, 2, info.nsmp, ot, dt * d.jdata, "t");
+    if (d.jsnap > 0) {
+        g_wfl = rsf_output("wfl");
+        if (!g_wfl) die(prog, rsf_error());
+        /* snapshot axes as each program writes them: bnds=y keeps the
+         * unpadded origin (an sf_setn-only update), except sfAWEFDcart2Dcpu
+         * whose padded axes carry the padded origin (MAWEFDcart2Dcpu.c:217-222) */
+        const int opad = bnds && scheme == AWE_SCHEME_CPU && ndim == 2;
+        float o[3];
+        for (int a = 0; a < 3; a++) o[a] = opad ? d.o[a] - info.nbpad * d.d[a] : d.o[a];
+        if (spher && ndim == 2) { /* theta fastest */
+            rsf_set_axis(g_wfl, 1, bnds ? info.npad[1] : d.n[1], o[1], d.d[1], "th");
+            rsf_set_axis(g_wfl, 2, bnds ? info.npad[0] : d.n[0], o[0], d.d[0], "ra");
+        } else {
+            const char *lab[2][3] = {{"z", "x", "y"}, {"ra", "th", "ph"}};
+            for (int a = 0; a < ndim; a++)
+                rsf_set_axis(g_wfl, a + 1, bnds ? info.npad[a] : d.n[a], o[a], d.d[a], lab[spher][a]);
+        }
+        rsf_set_axis(g_wfl, ndim + 1, info.nsnap, ot, dt * d.jsnap, "t");
+        awe_set_snapshot_callback(plan, write_frame, NULL);
+    }
+    float *dat = malloc(sizeof(float) * (size_t)info.nsmp * (nr > 0 ? nr : 1));
+    if (verb) fprintf(stderr, "%s: %d steps on a %d x %d x %d padded grid\n", prog, nt, info.npad[0], info.npad[1],
+                      info.npad[2]);
+    if (awe_forward(plan, wav, wcs, dat, NULL) != AWE_OK) die(prog, awe_last_error());
+    if (rsf_write(Fdat, dat, (size_t)info.nsmp * nr) != (size_t)info.nsmp * nr) die(prog, "short write (dat)");
+    awe_plan_destroy(plan);
+    rsf_close(Fdat);
+    if (g_wfl) rsf_close(g_wfl);
+    rsf_close(Fwav);
+    rsf_close(Fvel);
+    rsf_close(Fsou);
+    rsf_close(Frec);
+    if (Frfl) rsf_close(Frfl);
+    if (Fden) rsf_close(Fden);
+    free(sou);
+    free(rec);
+    free(vel);
+    free(rfl);
+    free(den);
+    free(wav);
+    free(dat);
+    return 0;
+}
