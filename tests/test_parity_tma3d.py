@@ -62,6 +62,21 @@ def test_exact_tma_free_surface_and_no_abc(fsrf, dabc):
     np.testing.assert_array_equal(dat, ref)
 
 
+@pytest.mark.parametrize("precision", [1, 0])
+def test_tma_tiles_inside_the_undamped_interior(precision):
+    """Tiles whose sponge factors are all 1 skip the sponge multiplies; a grid
+    with such tiles next to damped ones (axis 1 padded to 136: the tile
+    [64, 128) is undamped) must still match the oracle."""
+    par, vel, wav, sou, rec = _case(n=(120, 40, 28), nb=8, nt=110, seed=24)
+    dat, snaps, _ = run_engine(par, vel, wav, sou, rec, precision=precision)
+    ref, rsnaps = _oracle(par, vel, wav, sou, rec)
+    if precision == 1:
+        np.testing.assert_array_equal(dat, ref)
+        np.testing.assert_array_equal(snaps.ravel(), rsnaps.ravel())
+    else:
+        assert rel_l2(dat, ref) <= TOL
+
+
 def test_fast_tma_within_tolerance_and_matches_simple_kernel(monkeypatch):
     par, vel, wav, sou, rec = _case(n=(56, 48, 40), nb=10, nt=150, seed=23)
     dat, _, _ = run_engine(par, vel, wav, sou, rec, precision=0)

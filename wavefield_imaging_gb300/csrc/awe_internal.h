@@ -45,7 +45,12 @@ struct StepBParams {
     int damp_prev;              // prev level carries the sponge of the previous step
     int sponge_new;             // apply the sponge to the new level in the step kernel
     int shell;                  // cells within `shell` of a face are stored raw (boundary pass follows)
+    int ilo[3], ihi[3];         // per axis, every sponge factor in [ilo, ihi) is exactly 1
 };
+
+// [lo, hi): the indices of a sponge factor table whose entries are exactly 1
+// and that no entry != 1 lies between (the undamped interior of that axis)
+void undamped_range(const std::vector<float> &w, int &lo, int &hi);
 
 void launch_stepB(int ndim, int nop, bool exact, bool rho, const float *cur, float *nxt, const float *vel,
                   const float *den, const StepBParams &p, cudaStream_t s);

@@ -87,6 +87,17 @@ void sponge_weights(int nb, std::vector<float> &w) {
     }
 }
 
+void undamped_range(const std::vector<float> &w, int &lo, int &hi) {
+    const int n = (int)w.size();
+    lo = 0;
+    hi = n;
+    for (int i = 0; i < n / 2; i++)
+        if (w[i] != 1.f) lo = i + 1;
+    for (int i = n - 1; i >= n / 2; i--)
+        if (w[i] != 1.f) hi = i;
+    if (hi < lo) hi = lo;
+}
+
 // damp_make (MAWEFDcart2Dcpu.c:407-421): the same profile over nbd - nop cells
 void hybrid_damp(int ntransit, std::vector<float> &w) { sponge_weights(ntransit, w); }
 

@@ -177,6 +177,42 @@ __global__ void k_abc_axis1(float *__restrict__ uo, const float *__restrict__ um
     }
 }
 
+// The same sweep for nop == 4 and n1 % 4 == 0, n1 >= 16, with 16-byte
+// accesses: a face reads and writes inside the first (last) two float4 of
+// its line; the one sample of those float4s the face does not update is
+// stored back unchanged (no other thread of the launch touches the line).
+template <bool EXACT>
+__global__ void k_abc_axis1_v4(float *__restrict__ uo, const float *__restrict__ um, const float *__restrict__ bl,
+                               const float *__restrict__ bh, Grid g, int top) {
+    const int line = blockIdx.x * blockDim.x + threadIdx.x;
+    if (line >= g.n2 * g.n3) return;
+    const int q = g.n1 / 4;
+    const float4 *m = reinterpret_cast<const float4 *>(um + (long long)line * g.n1);
+    float4 *o = reinterpret_cast<float4 *>(uo + (long long)line * g.n1);
+    if (top) {  // iz = 4, 3, 2, 1 from uo[5]
+        const float l = bl[line];
+        const float4 ma = m[0], mb = m[1];
+        const float4 oa = o[0], ob = o[1];
+        const float u4 = abc_update<EXACT>(mb.y, mb.x, ob.y, l);
+        const float u3 = abc_update<EXACT>(mb.x, ma.w, u4, l);
+        const float u2 = abc_update<EXACT>(ma.w, ma.z, u3, l);
+        const float u1 = abc_update<EXACT>(ma.z, ma.y, u2, l);
+        o[0] = make_float4(oa.x, u1, u2, u3);
+        o[1] = make_float4(u4, ob.y, ob.z, ob.w);
+    }
+    {  // iz = n1-5 .. n1-2 from uo[n1-6]
+        const float h = bh[line];
+        const float4 ma = m[q - 2], mb = m[q - 1];
+        const float4 oa = o[q - 2], ob = o[q - 1];
+        const float v5 = abc_update<EXACT>(ma.z, ma.w, oa.z, h);
+        const float v4 = abc_update<EXACT>(ma.w, mb.x, v5, h);
+        const float v3 = abc_update<EXACT>(mb.x, mb.y, v4, h);
+        const float v2 = abc_update<EXACT>(mb.y, mb.z, v3, h);
+        o[q - 2] = make_float4(oa.x, oa.y, oa.z, v5);
+        o[q - 1] = make_float4(v4, v3, v2, ob.w);
+    }
+}
+
 // axis-2 faces: one thread per (i3, i1); coefficients [n3][n1]
 template <bool EXACT>
 __global__ void k_abc_axis2(float *uo, const float *__restrict__ um, const float *__restrict__ bl,
@@ -214,8 +250,14 @@ void launch_abconeB(int ndim, int nop, bool exact, int fsrf, float *uo, const fl
                     const Grid &g, cudaStream_t s) {
     const int T = 128;
     long long n = (long long)g.n2 * g.n3;
-    if (exact) k_abc_axis1<true><<<(n + T - 1) / T, T, 0, s>>>(uo, um, a.zl, a.zh, g, nop, !fsrf);
-    else k_abc_axis1<false><<<(n + T - 1) / T, T, 0, s>>>(uo, um, a.zl, a.zh, g, nop, !fsrf);
+    if (nop == 4 && g.n1 % 4 == 0 && g.n1 >= 16) {
+        if (exact) k_abc_axis1_v4<true><<<(n + T - 1) / T, T, 0, s>>>(uo, um, a.zl, a.zh, g, !fsrf);
+        else k_abc_axis1_v4<false><<<(n + T - 1) / T, T, 0, s>>>(uo, um, a.zl, a.zh, g, !fsrf);
+    } else if (exact) {
+        k_abc_axis1<true><<<(n + T - 1) / T, T, 0, s>>>(uo, um, a.zl, a.zh, g, nop, !fsrf);
+    } else {
+        k_abc_axis1<false><<<(n + T - 1) / T, T, 0, s>>>(uo, um, a.zl, a.zh, g, nop, !fsrf);
+    }
     n = (long long)g.n1 * g.n3;
     if (exact) k_abc_axis2<true><<<(n + T - 1) / T, T, 0, s>>>(uo, um, a.xl, a.xh, g, nop);
     else k_abc_axis2<false><<<(n + T - 1) / T, T, 0, s>>>(uo, um, a.xl, a.xh, g, nop);
@@ -339,10 +381,74 @@ __global__ void k_sponge_slab3(float *u, const float *__restrict__ w1, const flo
     u[i] = damp_cell<EXACT, 3>(u[i], i1, i2, i3, w1, w2, w3);
 }
 
+// The same three slabs with 16-byte accesses (n1 % 4 == 0): one thread per
+// float4, lanes outside the slab's axis-1 range are stored back unchanged
+// (no other thread of the launch touches them).
+template <bool EXACT, int NDIM>
+__device__ __forceinline__ void damp4(float4 &v, int i1, int lo, int hi, int i2, int i3, const float *w1,
+                                      const float *w2, const float *w3) {
+    float *e = &v.x;
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+        if (i1 + j >= lo && i1 + j < hi) e[j] = damp_cell<EXACT, NDIM>(e[j], i1 + j, i2, i3, w1, w2, w3);
+}
+
+template <bool EXACT, int NDIM>
+__global__ void k_sponge_slab1_v4(float *u, const float *__restrict__ w1, const float *__restrict__ w2,
+                                  const float *__restrict__ w3, Grid g, int W) {
+    // per line: chunks [0, c) cover axis-1 cells [0, W), chunks [q - c, q) cover [n1 - W, n1)
+    const int q = g.n1 / 4, c = (W + 3) / 4;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)g.n2 * g.n3 * 2 * c) return;
+    const int line = (int)(t / (2 * c)), k = (int)(t - (long long)line * 2 * c);
+    const int chunk = k < c ? k : q - 2 * c + k;
+    const int i2 = line % g.n2, i3 = line / g.n2, i1 = 4 * chunk;
+    float4 *p = reinterpret_cast<float4 *>(u + (long long)line * g.n1) + chunk;
+    float4 v = *p;
+    if (k < c) damp4<EXACT, NDIM>(v, i1, 0, W, i2, i3, w1, w2, w3);
+    else damp4<EXACT, NDIM>(v, i1, g.n1 - W, g.n1, i2, i3, w1, w2, w3);
+    *p = v;
+}
+
+// slab2 (NDIM 3: axis-2 bands; NDIM 2: the same) and slab3 (axis-3 bands)
+// over axis-1 cells [W, n1 - W), chunk-aligned
+template <bool EXACT, int NDIM, int SLAB>
+__global__ void k_sponge_slab23_v4(float *u, const float *__restrict__ w1, const float *__restrict__ w2,
+                                   const float *__restrict__ w3, Grid g, int W) {
+    const int c0 = W / 4, c1 = (g.n1 - W + 3) / 4;
+    const int chunk = c0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (chunk >= c1) return;
+    int i2, i3;
+    if (SLAB == 2) {
+        const int k = blockIdx.y;
+        i2 = k < W ? k : g.n2 - 2 * W + k;
+        i3 = blockIdx.z;
+    } else {
+        i2 = W + blockIdx.y;
+        const int k = blockIdx.z;
+        i3 = k < W ? k : g.n3 - 2 * W + k;
+    }
+    float4 *p = reinterpret_cast<float4 *>(u + ((long long)i3 * g.n2 + i2) * g.n1) + chunk;
+    float4 v = *p;
+    damp4<EXACT, NDIM>(v, 4 * chunk, W, g.n1 - W, i2, i3, w1, w2, w3);
+    *p = v;
+}
+
 template <bool EXACT, int NDIM>
 static void band_sponge_t(int W, float *u, const float *w1, const float *w2, const float *w3, const Grid &g,
                           cudaStream_t s) {
     const int T = 128;
+    if (g.n1 % 4 == 0 && g.n1 >= 2 * W + 8) {
+        const int c = (W + 3) / 4;
+        const long long n1tot = (long long)g.n2 * g.n3 * 2 * c;
+        k_sponge_slab1_v4<EXACT, NDIM><<<(unsigned)((n1tot + 255) / 256), 256, 0, s>>>(u, w1, w2, w3, g, W);
+        const int nch = (g.n1 - W + 3) / 4 - W / 4;
+        k_sponge_slab23_v4<EXACT, NDIM, 2><<<dim3((nch + 63) / 64, 2 * W, g.n3), 64, 0, s>>>(u, w1, w2, w3, g, W);
+        if (NDIM == 3 && g.n2 - 2 * W > 0)
+            k_sponge_slab23_v4<EXACT, 3, 3><<<dim3((nch + 63) / 64, g.n2 - 2 * W, 2 * W), 64, 0, s>>>(u, w1, w2, w3,
+                                                                                                   g, W);
+        return;
+    }
     const long long n1tot = (long long)g.n2 * g.n3 * 2 * W;
     k_sponge_slab1<EXACT, NDIM><<<(unsigned)((n1tot + 255) / 256), 256, 0, s>>>(u, w1, w2, w3, g, W);
     const int inner1 = g.n1 - 2 * W;

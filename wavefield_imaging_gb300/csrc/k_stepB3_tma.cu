@@ -46,6 +46,7 @@ struct Step3Params {
     float c0, cz[5], cx[5], cy[5];
     const float *w1, *w2, *w3;
     int damp_prev, sponge_new, shell;
+    int ilo[3], ihi[3];  // undamped interior per axis
     int L, ntz, ntx, nchunks;
     unsigned long long *counter;
     unsigned long long base;
@@ -81,7 +82,10 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
     if (__syncthreads_or(tid == 0 && *(volatile int *)p.err != 0)) return;
 
     const int nitems = p.ntz * p.ntx * p.nchunks;
-    unsigned long long gbase = 0;  // running stage sequence (slot and parity)
+    const long long plane = (long long)p.n1 * p.n2;
+    // ring position of the current item's first plane: slot and mbarrier parity
+    int slot0 = 0;
+    uint32_t ph0 = 0;
     for (;;) {
         if (tid == 0) s_item = (int)(atomicAdd(p.counter, 1ull) - p.base);
         __syncthreads();
@@ -93,8 +97,7 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
         const int S = (y1 - y0) + 2 * NOPQ;
 
         auto issue = [&](int s) {
-            const unsigned long long g = gbase + s;
-            const int slot = (int)(g % RING);
+            const int slot = (slot0 + s) % RING;
             const bool out = s >= 2 * NOPQ;
             mbar_expect_tx(&full[slot], BYTES_HALO + (out ? 2 * BYTES_TILE : 0));
             tma_load_3d(&st[slot].cur[0][0], &tm_cur, &full[slot], z0 - HALO, x0 - HALO, y0 - NOPQ + s);
@@ -122,7 +125,12 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
             zshell[i] = z < p.shell || z >= p.n1 - p.shell;
         }
         if (p.w2 && x < p.n2) wx = __ldg(p.w2 + x);
+        // the whole tile lies where the z and x sponge factors are exactly 1
+        const bool tile_undamped = z0 >= p.ilo[0] && z0 + TZ <= p.ihi[0] && x0 >= p.ilo[1] && x0 + TX <= p.ihi[1];
+        float *dst = p.nxt + ((long long)y0 * p.n2 + x) * p.n1 + zg;
 
+        int slot = slot0;  // ring slot and parity of plane s
+        uint32_t ph = ph0;
         float q[9][4];  // y queue: plane y0-4+s lives in q[s % 9]
 #pragma unroll 1
         for (int blk = 0; blk < S; blk += 9) {
@@ -130,9 +138,7 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
             for (int u = 0; u < 9; u++) {
                 const int s = blk + u;
                 if (s < S) {
-                    const unsigned long long g = gbase + s;
-                    const int slot = (int)(g % RING);
-                    const bool bad = !mbar_wait(&full[slot], (uint32_t)((g / RING) & 1), SPIN_LIMIT);
+                    const bool bad = !mbar_wait(&full[slot], ph, SPIN_LIMIT);
                     if (bad) atomicExch(p.err, 1);
                     const float4 cq = *reinterpret_cast<const float4 *>(&st[slot].cur[xi + HALO][4 * zq + HALO]);
                     q[u][0] = cq.x;
@@ -141,7 +147,7 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
                     q[u][3] = cq.w;
                     if (s >= 2 * NOPQ) {
                         const int y = y0 + s - 2 * NOPQ;
-                        const int hs = (int)((g - NOPQ) % RING);  // halo tile of plane y
+                        const int hs = slot >= NOPQ ? slot - NOPQ : slot + RING - NOPQ;  // halo tile of plane y
                         const float(*H)[HZ] = st[hs].cur;
                         float zw[12];
 #pragma unroll
@@ -166,58 +172,87 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
                                 const float zp = fadd<EXACT>(zw[4 + i - k], zw[4 + i + k]);
                                 const float xpair = fadd<EXACT>(xmv[i], xpv[i]);
                                 const float ypair = fadd<EXACT>(q[(jc + 9 - k) % 9][i], q[(jc + k) % 9][i]);
-                                float t = fadd<EXACT>(fmul<EXACT>(zp, p.cz[k]), fmul<EXACT>(xpair, p.cx[k]));
-                                t = fadd<EXACT>(t, fmul<EXACT>(ypair, p.cy[k]));
-                                lap[i] = fadd<EXACT>(lap[i], t);
+                                if constexpr (EXACT) {
+                                    // ts_kernel.c:292-300 order: (z*cz + x*cx) + y*cy, then into lap
+                                    float t = fadd<true>(fmul<true>(zp, p.cz[k]), fmul<true>(xpair, p.cx[k]));
+                                    t = fadd<true>(t, fmul<true>(ypair, p.cy[k]));
+                                    lap[i] = fadd<true>(lap[i], t);
+                                } else {
+                                    lap[i] = fmaf(zp, p.cz[k], lap[i]);
+                                    lap[i] = fmaf(xpair, p.cx[k], lap[i]);
+                                    lap[i] = fmaf(ypair, p.cy[k], lap[i]);
+                                }
                             }
                         }
                         const float4 pv = *reinterpret_cast<const float4 *>(&st[slot].prv[xi][4 * zq]);
                         const float4 vv = *reinterpret_cast<const float4 *>(&st[slot].vel[xi][4 * zq]);
                         const float prv4[4] = {pv.x, pv.y, pv.z, pv.w}, vel4[4] = {vv.x, vv.y, vv.z, vv.w};
-                        const float wy = p.w3 ? __ldg(p.w3 + y) : 1.f;
                         const bool yin = y >= NOPQ && y < p.n3 - NOPQ;
-                        const bool yshell = y < p.shell || y >= p.n3 - p.shell;
+                        // every sponge factor of this plane of the tile is 1: the
+                        // multiplies are identities and are skipped (CTA-uniform)
+                        const bool undamped = tile_undamped && y >= p.ilo[2] && y < p.ihi[2];
                         float out[4];
+                        if (undamped) {
 #pragma unroll
-                        for (int i = 0; i < 4; i++) {
-                            float pr = prv4[i];
-                            if (p.damp_prev) pr = damp3<EXACT>(pr, wz[i], wx, wy);
-                            float o = pr;
-                            if (zin[i] && xin && yin) {
-                                const float u0 = zw[4 + i];
-                                if constexpr (EXACT)
-                                    o = sum3_rn(__fmul_rn(vel4[i], lap[i]), __fadd_rn(u0, u0), -pr);
-                                else
-                                    o = fmaf(vel4[i], lap[i], 2.f * u0 - pr);
+                            for (int i = 0; i < 4; i++) {
+                                const float pr = prv4[i], u0 = zw[4 + i];
+                                float o = pr;
+                                if (zin[i] && xin && yin) {
+                                    if constexpr (EXACT)
+                                        o = sum3_rn(__fmul_rn(vel4[i], lap[i]), __fadd_rn(u0, u0), -pr);
+                                    else
+                                        o = fmaf(vel4[i], lap[i], 2.f * u0 - pr);
+                                }
+                                out[i] = o;
                             }
-                            if (p.sponge_new && !(zshell[i] || xshell || yshell)) o = damp3<EXACT>(o, wz[i], wx, wy);
-                            out[i] = o;
+                        } else {
+                            const float wy = p.w3 ? __ldg(p.w3 + y) : 1.f;
+                            const bool yshell = y < p.shell || y >= p.n3 - p.shell;
+#pragma unroll
+                            for (int i = 0; i < 4; i++) {
+                                float pr = prv4[i];
+                                if (p.damp_prev) pr = damp3<EXACT>(pr, wz[i], wx, wy);
+                                float o = pr;
+                                if (zin[i] && xin && yin) {
+                                    const float u0 = zw[4 + i];
+                                    if constexpr (EXACT)
+                                        o = sum3_rn(__fmul_rn(vel4[i], lap[i]), __fadd_rn(u0, u0), -pr);
+                                    else
+                                        o = fmaf(vel4[i], lap[i], 2.f * u0 - pr);
+                                }
+                                if (p.sponge_new && !(zshell[i] || xshell || yshell))
+                                    o = damp3<EXACT>(o, wz[i], wx, wy);
+                                out[i] = o;
+                            }
                         }
-                        if (col_ok) {
-                            float *dst = p.nxt + ((long long)y * p.n2 + x) * p.n1 + zg;
-                            *reinterpret_cast<float4 *>(dst) = make_float4(out[0], out[1], out[2], out[3]);
-                        }
+                        if (col_ok) *reinterpret_cast<float4 *>(dst) = make_float4(out[0], out[1], out[2], out[3]);
+                        dst += plane;
                     }
                     if (__syncthreads_or(bad)) {
                         // drain: wait (bounded) for every copy still in flight, then leave
                         if (tid == 0) {
                             const int issued = min(S, max(RING, s - NOPQ + RING));
                             for (int t = s; t < issued; t++) {
-                                const unsigned long long gt = gbase + t;
-                                mbar_wait(&full[gt % RING], (uint32_t)((gt / RING) & 1), SPIN_LIMIT);
+                                const int tt = slot0 + t;
+                                mbar_wait(&full[tt % RING], ph0 ^ (uint32_t)((tt / RING) & 1), SPIN_LIMIT);
                             }
                         }
                         __syncthreads();
                         return;
                     }
                     if (tid == 0 && s >= NOPQ && s - NOPQ + RING < S) issue(s - NOPQ + RING);
+                    if (++slot == RING) {
+                        slot = 0;
+                        ph ^= 1u;
+                    }
                 }
             }
         }
-        gbase += S;
+        const int t = slot0 + S;
+        ph0 ^= (uint32_t)((t / RING) & 1);
+        slot0 = t % RING;
     }
 }
-
 // cuTensorMapEncodeTiled, fetched from the driver at run time (no link-time libcuda dependency)
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
@@ -294,6 +329,10 @@ cudaError_t launch_stepB3_tma(bool exact, const CUtensorMap *maps, int icur, flo
     p.damp_prev = sp.damp_prev;
     p.sponge_new = sp.sponge_new;
     p.shell = sp.shell;
+    for (int a = 0; a < 3; a++) {
+        p.ilo[a] = sp.ilo[a];
+        p.ihi[a] = sp.ihi[a];
+    }
     p.L = sh.L;
     p.ntz = sh.ntz;
     p.ntx = sh.ntx;

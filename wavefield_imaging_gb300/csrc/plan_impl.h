@@ -30,6 +30,7 @@ struct awe_plan {
     float *den = nullptr;
     float *rfl = nullptr;
     float *w[3] = {nullptr, nullptr, nullptr};  // per-axis sponge factors
+    int wlo[3] = {0, 0, 0}, whi[3] = {0, 0, 0};  // undamped range of each factor table
     float *abc[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     float *damp = nullptr;
     std::vector<float> h_vel_raw;  // padded raw velocity (scheme GPU injection reflectivity, ABC tables)

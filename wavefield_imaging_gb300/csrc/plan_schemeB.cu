@@ -68,6 +68,7 @@ awe_status planB_init(awe_plan *p) {
                     t[i] = w[nb - i - 1];
                     t[len[a] - 1 - i] = w[nb - i - 1];
                 }
+            undamped_range(t, p->wlo[a], p->whi[a]);
             AWE_TRY(upload(p, &p->w[a], t.data(), t.size()));
         }
     }
@@ -282,6 +283,10 @@ awe_status planB_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, flo
     sp.damp_prev = sponge;
     sp.sponge_new = sponge && !p->sponge_deferred;
     sp.shell = shell;
+    for (int a = 0; a < 3; a++) {
+        sp.ilo[a] = sponge ? p->wlo[a] : 0;
+        sp.ihi[a] = sponge ? p->whi[a] : (a == 0 ? g.n1 : a == 1 ? g.n2 : g.n3);
+    }
     AbcB abc{p->abc[0], p->abc[1], p->abc[2], p->abc[3], p->abc[4], p->abc[5]};
     const float *pw1 = sponge ? p->w[0] : nullptr;
 
