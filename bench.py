@@ -341,7 +341,8 @@ def run_ours(args):
            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
            "config": {"workload": w["name"], "padded_cells": cells, "interior_cells": int(np.prod(w["n"])),
-                      "precision": args.precision, "l2": "no flush: every step streams 3 fields of 764 MB (> 129 MB L2)",
+                      "precision": args.precision,
+                      "l2": "no flush: every step streams 3 fields of %d MB (> 129 MB L2)" % (cells * 4 // 10**6),
                       "parallelism": "replicas" if world > 1 else "single", "seed": w["seed"]},
            "e2e": {"value": e2e_value, "unit": UNIT,
                    "h2d_bytes_per_step": int(vel.nbytes + wav.nbytes + sou.nbytes + rec.nbytes),
@@ -360,6 +361,121 @@ def run_ours(args):
     plan.close()
 
 
+GRAD_METRIC = "FWI gradients/s (misfit gradient, checkpointed fwd + adjoint)"
+
+
+def grad_workload(kind, nt, n):
+    if kind == "grad3d":
+        w = workload(nt, n)
+        w["name"] = ("3D misfit gradient d(0.5||d-dobs||^2)/d(1/v^2), %d^3 at 5 m (%d^3 padded), 8th order, nt=%d, "
+                     "dabc=y, 1 source, 128x128 receivers" % (n, n + 64, nt))
+        return w
+    # 2D: 512 x 512 at 5 m, nb=40, nt=4000, 512 receivers at z = 50 m, source at x = centre, z = 50 m
+    return dict(name="2D misfit gradient, %d^2 at 5 m (%d^2 padded, nb=40), 8th order, nt=%d, dabc=y, 1 source, "
+                     "512 receivers" % (n, n + 80, nt),
+                n=(n, n), d=(5.0, 5.0), o=(0.0, 0.0), nt=nt, dt=0.005, nb=40, fdorder=8, dabc=1, f0=5.0, seed=1)
+
+
+def smooth(vel, sigma_cells):
+    """Gaussian smoothing (FFT, periodic) of a model, for the starting model."""
+    out = vel.astype(np.float64)
+    for ax in range(vel.ndim):
+        k = np.fft.fftfreq(vel.shape[ax])
+        shape = [1] * vel.ndim
+        shape[ax] = -1
+        filt = np.exp(-0.5 * (2 * np.pi * k * sigma_cells) ** 2).reshape(shape)
+        out = np.real(np.fft.ifft(np.fft.fft(out, axis=ax) * filt, axis=ax))
+    return out.astype(np.float32)
+
+
+def run_grad(args):
+    """--workload grad3d | grad2d: time whole misfit gradients (forward with
+    checkpoints + segment recompute + adjoint) of the true-vs-smoothed model
+    problem.  One bench step = one gradient."""
+    import torch
+
+    import wavefield_imaging_gb300 as awe
+
+    dist, rank, world, local = dist_init()
+    torch.cuda.set_device(local)
+    nt = args.nt if args.nt != 3000 or args.workload == "grad3d" else 4000
+    w = grad_workload(args.workload, nt, args.n)
+    nd = len(w["n"])
+    if nd == 3:
+        vtrue = layered_model_3d(w)
+        sou, rec = geometry(w)
+    else:
+        w3 = dict(w, n=(w["n"][0], w["n"][1], 1))
+        vtrue = layered_model_3d(w3)[0]
+        nx = w["n"][1]
+        sou = np.array([[0.5 * (nx - 1) * 5.0, 50.0]], np.float32)
+        rec = np.stack([np.arange(nx) * 5.0, np.full(nx, 50.0)], 1).astype(np.float32)
+    v0 = smooth(vtrue, 100.0 / 5.0)
+    wav = ricker(w["nt"], w["dt"], w["f0"])
+    desc = awe.make_desc(nd, w["n"], w["d"], w["o"], w["nt"], w["dt"], nb=w["nb"], fdorder=w["fdorder"],
+                         dabc=w["dabc"], expl=1, precision=awe.FAST)
+    plan = awe.Plan(desc, device=local)
+    plan.set_geometry(sou, rec)
+    plan.set_model(vtrue)
+    dobs = plan.forward(wav)
+    plan.set_model(v0)
+    fmt = {"bf16": awe.CKPT_BF16, "fp16": awe.CKPT_FP16, "fp32": awe.CKPT_FP32}[args.ckpt]
+    d_wav = torch.from_numpy(wav).cuda()
+    d_dobs = torch.from_numpy(dobs).cuda()
+    ngrad = int(np.prod(w["n"]))
+    d_grad = torch.zeros(ngrad, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.Stream()
+
+    def step():
+        return plan.gradient_device(d_wav.data_ptr(), 1, d_dobs.data_ptr(), d_grad.data_ptr(), ckpt_format=fmt,
+                                    stream=stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        J = step()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(dist)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    launches = 0
+    for _ in range(args.steps):
+        J = step()
+        launches += plan.last_launch_count()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(dist)
+    clocks = sampler.stop()
+    ms = allmax(dist, ev0.elapsed_time(ev1))
+    # the forward alone, for the split
+    d_dat = torch.zeros((plan.nsmp, rec.shape[0]), dtype=torch.float32, device="cuda")
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    plan.forward_device(d_wav.data_ptr(), 1, d_dat.data_ptr(), 0, stream.cuda_stream)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    fwd_ms = f0.elapsed_time(f1)
+    if rank != 0:
+        return
+    cells = padded_cells(w)
+    g_s = ms / 1e3 / args.steps
+    out = {"metric": GRAD_METRIC, "value": args.steps * world / (ms / 1e3), "unit": "gradients/s",
+           "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32 fields, fp64 sums",
+           "data": "synthetic",
+           "config": {"workload": w["name"], "checkpoint": args.ckpt, "padded_cells": cells,
+                      "ckpt_every": int(np.ceil(np.sqrt(w["nt"]))), "start_model": "true model smoothed, 100 m",
+                      "device_bytes": plan.device_bytes(), "seed": w["seed"]},
+           "split": {"forward_ms": fwd_ms, "gradient_ms": ms / args.steps,
+                     "gradient_over_forward": (ms / args.steps) / fwd_ms,
+                     "cell_steps_per_s": cells * w["nt"] / g_s,
+                     "algorithmic_GBps": 48.0 * cells * w["nt"] / g_s / 1e9},
+           "misfit": J, "gpu_launches": int(launches), "clocks": clocks}
+    print(json.dumps(out))
+    plan.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -370,9 +486,14 @@ def main():
     ap.add_argument("--nt", type=int, default=3000, help="time steps (the workload is nt=3000)")
     ap.add_argument("--n", type=int, default=512, help="model edge (the workload is 512; smaller for profiling)")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--workload", default="fwd3d", choices=["fwd3d", "grad3d", "grad2d"],
+                    help="fwd3d: the headline forward workload; grad3d/grad2d: misfit gradients")
+    ap.add_argument("--ckpt", default="bf16", choices=["bf16", "fp16", "fp32"], help="checkpoint storage (grad*)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload != "fwd3d":
+        run_grad(args)
     else:
         run_ours(args)
 

@@ -159,6 +159,38 @@ long long awe_last_launch_count(const awe_plan *plan);
 awe_status awe_profile_enable(awe_plan *plan, int on);
 awe_status awe_profile_read(awe_plan *plan, double *step_kernel_ms, long long *step_launches);
 
+/* ---- Misfit gradient (no counterpart in the reference: its adj=y mode
+ * back-injects data for an image, MAWEFDcart2Dgpu.cu:386-396) ---- */
+/* Checkpoint storage: BF16 or FP16 with one FP32 scale (the level's max |v|)
+ * per stored level, or FP32.  The recomputed levels inherit the rounding:
+ * measured gradient error against an FP64 adjoint on the test cases ~1e-2
+ * (BF16), ~1e-3 (FP16), ~1e-7 (FP32). */
+typedef enum { AWE_CKPT_BF16 = 0, AWE_CKPT_FP32 = 1, AWE_CKPT_FP16 = 2 } awe_ckpt_format;
+
+typedef struct {
+    int ckpt_every;  /* forward steps between checkpoints; <= 0: ceil(sqrt(nt)) */
+    int ckpt_format; /* awe_ckpt_format */
+} awe_grad_opts;
+
+/* Gradient of J = 0.5 * sum over data rows of ||d - dobs||^2 with respect to
+ * m = 1/v^2 on the model grid, for the plan's model and geometry.  Scheme
+ * AWE_SCHEME_CPU (2D or 3D, any order, sponge and one-way ABC, free surface),
+ * no density, no hybrid ABC; the forward runs in AWE_FAST arithmetic.  The
+ * boundary coefficients (one-way ABC, sponge) are held at the plan's model.
+ * The forward pass stores both time levels every ckpt_every steps (BF16 or
+ * FP16 with one FP32 scale per level, or FP32); the adjoint sweep recomputes each
+ * segment once from its checkpoint.  Gradient and misfit sums are FP64.
+ * wav as awe_forward; dobs [nsmp][nr]; grad [n3][n2][n1]; misfit: J;
+ * dsyn (may be NULL): the synthetic data [nsmp][nr].  opts NULL = defaults
+ * (BF16, ceil(sqrt(nt))). */
+awe_status awe_gradient(awe_plan *plan, const float *wav, int ncs, const float *dobs, const awe_grad_opts *opts,
+                        double *grad, double *misfit, float *dsyn);
+
+/* The same on device buffers (d_grad double [n3][n2][n1]); misfit is a host
+ * pointer, written when the call returns (the call synchronizes `stream`). */
+awe_status awe_gradient_device(awe_plan *plan, const float *d_wav, int ncs, const float *d_dobs,
+                               const awe_grad_opts *opts, double *d_grad, double *misfit, float *d_dsyn, void *stream);
+
 /* 2D forward modelling without any device allocation.  No counterpart in
  * the reference (its programs cudaMalloc everything in main()).  For callers
  * that cannot call cudaMalloc - code inside a framework that owns the device

@@ -1,7 +1,8 @@
 """ctypes front end of the C oracle (awe_oracle.c) - test infrastructure only.
 
-``build()`` compiles liboracle.so (exact float restatement) and
-liboracle64.so (same scheme, FP64 wavefields) with gcc and, when the
+``build()`` compiles liboracle.so (exact float restatement),
+liboracle64.so (same scheme, FP64 wavefields) and liboracle_adj.so (FP64
+adjoint / misfit gradient, awe_adjoint.c) with gcc and, when the
 reference sources are present, the reference's own CPU programs into
 oracle/_ref/ (via oracle/ref/Makefile).
 """
@@ -30,6 +31,12 @@ def build(with_reference: bool = True) -> None:
             [os.path.getmtime(x) for x in srcs] + [os.path.getmtime(os.path.join(HERE, "awe_oracle.h"))]
         ):
             subprocess.check_call(["gcc", *CFLAGS, *extra, *srcs, "-o", out, "-lm"])
+    # FP64 adjoint of the CPU-program scheme (includes awe_oracle.c)
+    adj = os.path.join(HERE, "awe_adjoint.c")
+    out = os.path.join(BUILD, "liboracle_adj.so")
+    deps = [adj, os.path.join(HERE, "awe_oracle.c"), os.path.join(HERE, "awe_oracle.h")]
+    if not os.path.exists(out) or os.path.getmtime(out) < max(os.path.getmtime(x) for x in deps):
+        subprocess.check_call(["gcc", *CFLAGS, adj, "-o", out, "-lm"])
     if with_reference and os.path.isdir(REF_SRC):
         subprocess.check_call(
             ["make", "-s", "-C", os.path.join(HERE, "ref"), "REF=" + REF_SRC, "OUT=" + REF_OUT],
@@ -214,3 +221,65 @@ def gpu_scheme(kind: str, p: dict, vel, wav, sou, rec, rfl=None, use_reference_e
     if rc != 0:
         raise RuntimeError("GPU-scheme run returned %d" % rc)
     return dat, snaps
+
+
+_adj = None
+
+
+def _adj_lib():
+    global _adj
+    if _adj is None:
+        path = os.path.join(BUILD, "liboracle_adj.so")
+        if not os.path.exists(path):
+            build(with_reference=False)
+        L = C.CDLL(path)
+        fp = C.POINTER(C.c_float)
+        dp = C.POINTER(C.c_double)
+        L.orc_grad.argtypes = [C.POINTER(Par), C.c_int, C.c_int, fp, fp, C.c_int, fp, C.c_int, fp, fp, dp, dp, dp]
+        L.orc_grad.restype = C.c_int
+        L.orc_grad_m.argtypes = [C.POINTER(Par), C.c_int, C.c_int, dp, fp, C.c_int, fp, C.c_int, fp, fp, dp, dp, dp]
+        L.orc_grad_m.restype = C.c_int
+        L.orc_grad_ckpt.argtypes = [C.POINTER(Par), C.c_int, C.c_int, fp, fp, C.c_int, fp, C.c_int, fp, fp, C.c_int,
+                                    C.c_int, dp, dp, dp]
+        L.orc_grad_ckpt.restype = C.c_int
+        _adj = L
+    return _adj
+
+
+def misfit_gradient(p: dict, vel, wav, sou, rec, dobs, jdata: int = 1, m=None, ckpt_every: int = 0,
+                    ckpt_bits: int = 0):
+    """FP64 misfit J = 0.5 sum (d - dobs)^2 of the CPU-program scheme and its
+    gradient with respect to m = 1/v^2 (boundary coefficients held fixed).
+    The model is `vel` (float32 velocity, v^2 dt^2 formed in float as the
+    engine does) or, when `m` is given, slowness squared in float64 (for
+    finite differences free of float rounding; `vel` then only sets the shape).
+    ckpt_bits > 0 emulates checkpointed recompute from levels rounded to that
+    many significant bits every ckpt_every steps (8 = BF16).
+    Returns (grad [model shape] float64, J, dsyn [nsmp][nr] float64)."""
+    q = make_par(p)
+    ndim = len(p["n"])
+    vel = np.ascontiguousarray(vel, np.float32)
+    wav = np.ascontiguousarray(wav, np.float32)
+    sou = np.ascontiguousarray(sou, np.float32).reshape(-1, ndim)
+    rec = np.ascontiguousarray(rec, np.float32).reshape(-1, ndim)
+    ns, nr = sou.shape[0], rec.shape[0]
+    nsmp = (q.nt - 1) // jdata + 1
+    dobs = np.ascontiguousarray(dobs, np.float32).reshape(nsmp, nr)
+    grad = np.zeros(vel.shape, np.float64)
+    dsyn = np.zeros((nsmp, nr), np.float64)
+    J = C.c_double()
+    dp = C.POINTER(C.c_double)
+    if ckpt_bits:
+        rc = _adj_lib().orc_grad_ckpt(C.byref(q), ndim, jdata, _fp(vel), _fp(wav), ns, _fp(sou), nr, _fp(rec),
+                                      _fp(dobs), ckpt_every, ckpt_bits, grad.ctypes.data_as(dp), C.byref(J),
+                                      dsyn.ctypes.data_as(dp))
+    elif m is None:
+        rc = _adj_lib().orc_grad(C.byref(q), ndim, jdata, _fp(vel), _fp(wav), ns, _fp(sou), nr, _fp(rec), _fp(dobs),
+                                 grad.ctypes.data_as(dp), C.byref(J), dsyn.ctypes.data_as(dp))
+    else:
+        m = np.ascontiguousarray(m, np.float64).reshape(vel.shape)
+        rc = _adj_lib().orc_grad_m(C.byref(q), ndim, jdata, m.ctypes.data_as(dp), _fp(wav), ns, _fp(sou), nr,
+                                   _fp(rec), _fp(dobs), grad.ctypes.data_as(dp), C.byref(J), dsyn.ctypes.data_as(dp))
+    if rc != 0:
+        raise ValueError("orc_grad rejected the parameters")
+    return grad, J.value, dsyn

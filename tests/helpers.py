@@ -47,3 +47,46 @@ def rel_l2(a, b):
     b = np.asarray(b, np.float64).ravel()
     den = np.linalg.norm(b)
     return np.linalg.norm(a - b) / (den if den > 0 else 1.0)
+
+
+def ricker(nt, dt, f0=5.0):
+    t = np.arange(nt) * dt - 1.5 / f0
+    a = (np.pi * f0 * t) ** 2
+    return ((1 - 2 * a) * np.exp(-a)).astype(np.float32)
+
+
+def grad_case(nd, fsrf=0, dabc=1, nt=200, seed=0, n=None, nb=8, nrec=9):
+    """A small seeded gradient problem of the CPU-program scheme (8th order):
+    returns (par, vel, wav, sou, rec, vtrue) with vtrue a perturbed model for
+    the observed data."""
+    rng = np.random.default_rng(seed)
+    if n is None:
+        n = [48, 56] if nd == 2 else [24, 26, 22]
+    shape = tuple(n[::-1])
+    d = 5.0
+    vel = (150 + 30 * rng.random(shape)).astype(np.float32)
+    vtrue = (vel * (1 + 0.05 * rng.standard_normal(shape))).astype(np.float32)
+    par = dict(n=list(n), d=[d] * nd, o=[0.0] * nd, nb=nb, nt=nt, dt=0.005, fdorder=8, dabc=dabc, fsrf=fsrf, expl=1)
+    wav = ricker(nt, 0.005)
+    if nd == 2:
+        sou = np.array([[0.5 * (n[1] - 1) * d, 0.3 * (n[0] - 1) * d]], np.float32)
+        rec = np.stack([np.linspace(10, (n[1] - 2) * d, nrec), np.full(nrec, 0.6 * (n[0] - 1) * d)], 1)
+    else:
+        sou = np.array([[0.5 * (n[1] - 1) * d, 0.45 * (n[2] - 1) * d, 0.3 * (n[0] - 1) * d]], np.float32)
+        gx, gy = np.meshgrid(np.linspace(10, (n[1] - 2) * d, 4), np.linspace(10, (n[2] - 2) * d, 3), indexing="ij")
+        rec = np.stack([gx.ravel(), gy.ravel(), np.full(gx.size, 0.6 * (n[0] - 1) * d)], 1)
+    return par, vel, wav, sou, rec.astype(np.float32), vtrue
+
+
+def tapered_direction(shape, rng, margin=3):
+    """Random model direction, zero within `margin` cells of every face (so the
+    padding and the one-way ABC coefficients do not move)."""
+    dm = rng.standard_normal(shape)
+    for ax in range(len(shape)):
+        idx = [slice(None)] * len(shape)
+        for k in range(margin):
+            idx[ax] = k
+            dm[tuple(idx)] = 0
+            idx[ax] = -1 - k
+            dm[tuple(idx)] = 0
+    return dm

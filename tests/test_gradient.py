@@ -1,0 +1,130 @@
+"""The engine's misfit gradient (awe_gradient: hand-written adjoint step,
+checkpointed forward, FP64 accumulation) against the FP64 adjoint oracle and
+against finite differences through the torch.autograd harness."""
+import numpy as np
+import pytest
+
+from helpers import desc_from_par, grad_case, rel_l2, tapered_direction
+
+pytestmark = pytest.mark.gpu
+
+
+def _plan(par, vel, sou, rec):
+    import wavefield_imaging_gb300 as awe
+
+    p = awe.Plan(desc_from_par(par, precision=awe.FAST))
+    p.set_model(vel)
+    p.set_geometry(sou, rec)
+    return p
+
+
+def _observed(par, vtrue, wav, sou, rec):
+    from oracle import oracle
+
+    dobs, _ = oracle.cart_cpu(par, vtrue, wav, sou, rec)
+    return dobs
+
+
+@pytest.mark.parametrize("nd,fsrf", [(2, 0), (2, 1), (3, 0), (3, 1)])
+def test_gradient_matches_fp64_oracle(nd, fsrf):
+    import wavefield_imaging_gb300 as awe
+    from oracle import oracle
+
+    par, vel, wav, sou, rec, vtrue = grad_case(nd, fsrf=fsrf, nt=200 if nd == 2 else 110)
+    dobs = _observed(par, vtrue, wav, sou, rec)
+    gref, Jref, dref = oracle.misfit_gradient(par, vel, wav, sou, rec, dobs)
+    T = int(np.ceil(np.sqrt(par["nt"])))
+    with _plan(par, vel, sou, rec) as p:
+        g32, J32, d32 = p.gradient(wav, dobs, ckpt_format=awe.CKPT_FP32, return_dsyn=True)
+        gb, Jb = p.gradient(wav, dobs, ckpt_format=awe.CKPT_BF16)
+        gh, Jh = p.gradient(wav, dobs, ckpt_format=awe.CKPT_FP16)
+    assert rel_l2(d32, dref) <= 1e-5
+    assert abs(J32 - Jref) <= 1e-5 * abs(Jref)
+    assert Jb == J32 and Jh == J32  # the misfit comes from the forward pass, not the checkpoints
+    # FP32 checkpoints: only the FP32 arithmetic differs from the FP64 oracle
+    assert rel_l2(g32, gref) <= 1e-4
+    # 16-bit checkpoints: the recomputed segments start from levels rounded to
+    # 8 (BF16) or 11 (FP16) significant bits.  The oracle emulates the same
+    # rounding in FP64; the engine must match that, and the error it leaves
+    # against the exact gradient is the checkpoint format's, not the kernels'
+    for g16, bits, bound in ((gb, 8, 3e-2), (gh, 11, 4e-3)):
+        gq, _, _ = oracle.misfit_gradient(par, vel, wav, sou, rec, dobs, ckpt_every=T, ckpt_bits=bits)
+        assert rel_l2(g16, gq) <= 0.5 * rel_l2(gq, gref) + 1e-4
+        assert rel_l2(g16, gref) <= bound
+
+
+@pytest.mark.parametrize("every", [1, 7, 1000])
+def test_checkpoint_interval_does_not_change_fp32_gradient(every):
+    import wavefield_imaging_gb300 as awe
+
+    par, vel, wav, sou, rec, vtrue = grad_case(3, nt=60)
+    dobs = _observed(par, vtrue, wav, sou, rec)
+    with _plan(par, vel, sou, rec) as p:
+        ref, Jr = p.gradient(wav, dobs, ckpt_every=0, ckpt_format=awe.CKPT_FP32)
+        g, J = p.gradient(wav, dobs, ckpt_every=every, ckpt_format=awe.CKPT_FP32)
+    assert J == Jr
+    # recompute from FP32 checkpoints repeats the forward exactly; only the
+    # order of coincident receiver-corner atomics may differ
+    assert rel_l2(g, ref) <= 1e-6
+
+
+def test_gradient_with_decimated_data():
+    import wavefield_imaging_gb300 as awe
+    from oracle import oracle
+
+    par, vel, wav, sou, rec, vtrue = grad_case(2, nt=180)
+    par["jdata"] = 4
+    dobs = _observed(par, vtrue, wav, sou, rec)[::4]
+    gref, Jref, _ = oracle.misfit_gradient(par, vel, wav, sou, rec, dobs, jdata=4)
+    with _plan(par, vel, sou, rec) as p:
+        g, J = p.gradient(wav, dobs, ckpt_format=awe.CKPT_FP32)
+    assert abs(J - Jref) <= 1e-5 * abs(Jref)
+    assert rel_l2(g, gref) <= 1e-4
+
+
+@pytest.mark.parametrize("nd", [2, 3])
+def test_autograd_harness_against_finite_differences(nd):
+    """8 seeded directions, relative step 1e-3, through torch.autograd."""
+    torch = pytest.importorskip("torch")
+    import wavefield_imaging_gb300 as awe
+    from wavefield_imaging_gb300.autograd import misfit
+
+    par, vel, wav, sou, rec, vtrue = grad_case(nd, nt=200 if nd == 2 else 110)
+    dobs = _observed(par, vtrue, wav, sou, rec)
+    m0 = torch.tensor(1.0 / vel.astype(np.float64) ** 2, dtype=torch.float64, device="cuda")
+    with _plan(par, vel, sou, rec) as p:
+        m = m0.clone().requires_grad_(True)
+        J = misfit(m, p, wav, dobs, ckpt_format=awe.CKPT_FP32)
+        J.backward()
+        g = m.grad.detach().cpu().numpy()
+        rng = np.random.default_rng(2024)
+        errs = []
+        for _ in range(8):
+            dm = tapered_direction(vel.shape, rng) * m0.cpu().numpy()
+            h = 1e-3
+            Jp = float(misfit(m0 + h * torch.tensor(dm, device="cuda"), p, wav, dobs))
+            Jm = float(misfit(m0 - h * torch.tensor(dm, device="cuda"), p, wav, dobs))
+            fd = (Jp - Jm) / (2 * h)
+            an = float((g * dm).sum())
+            errs.append(abs(fd - an) / abs(an))
+    # FP32 forward: J carries ~1e-7 relative rounding, amplified by 1/h in the
+    # difference quotient
+    assert max(errs) <= 1e-2, errs
+
+
+def test_gradient_rejects_unsupported_plans():
+    import wavefield_imaging_gb300 as awe
+
+    par, vel, wav, sou, rec, vtrue = grad_case(2, nt=20)
+    dobs = np.zeros((20, rec.shape[0]), np.float32)
+    with awe.Plan(desc_from_par(par, precision=awe.EXACT)) as p:
+        p.set_model(vel)
+        p.set_geometry(sou, rec)
+        with pytest.raises(awe.AweError):
+            p.gradient(wav, dobs)
+    par_h = dict(par, hybrid=1)
+    with awe.Plan(desc_from_par(par_h, precision=awe.FAST)) as p:
+        p.set_model(vel)
+        p.set_geometry(sou, rec)
+        with pytest.raises(awe.AweError):
+            p.gradient(wav, dobs)

@@ -46,6 +46,7 @@ struct StepBParams {
     int sponge_new;             // apply the sponge to the new level in the step kernel
     int shell;                  // cells within `shell` of a face are stored raw (boundary pass follows)
     int ilo[3], ihi[3];         // per axis, every sponge factor in [ilo, ihi) is exactly 1
+    const float *prv;           // previous level when stepping out of place (null: read nxt in place)
 };
 
 // [lo, hi): the indices of a sponge factor table whose entries are exactly 1
@@ -110,6 +111,29 @@ void launch_injectA(bool exact, int ndim, float *u, const GeoPoint *pts, const f
 void launch_snapshot_transpose2(const float *u, float *dst, const Grid &g, int f1, int f2, int m1, int m2,
                                 cudaStream_t s);
 
+// ---- adjoint of the CPU-program scheme (k_adjoint.cu) ----
+struct AdjParams {
+    Grid g;
+    Coef k;
+    int nd, nop;
+    const float *w1, *w2, *w3;  // sponge axis factors; null = no sponge
+};
+void launch_adjB(const float *X, float *Y, const float *V, const float *vel, double *G, const AdjParams &p,
+                 cudaStream_t s);
+void launch_abc_adjB(int nop, int fsrf, float *mu, float *kap, const AbcB &a, const Grid &g, cudaStream_t s);
+void launch_kap_fold(float *mu, float *kap, const AdjParams &p, cudaStream_t s);
+void launch_rec_adj(float *mu, const GeoPoint *pts, int nr, const float *r, const AdjParams &p, const long long *off,
+                    cudaStream_t s);
+void launch_src_grad(double *G, const float *nu, const GeoPoint *pts, int ns, const float *wav, int it, int ncs,
+                     bool one_wavelet, int nd, const long long *off, cudaStream_t s);
+void launch_residual(const float *d, const float *dobs, float *r, int nrows, int nr, double *row_sum, cudaStream_t s);
+void launch_ckpt_store16(bool fp16, const float *u, long long n, unsigned int *amax, void *q, float *scale, int grid,
+                         cudaStream_t s);
+void launch_ckpt_load16(bool fp16, const void *q, long long n, const float *scale, float *u, int grid,
+                        cudaStream_t s);
+void launch_grad_fold(const double *G, const float *vel2, float dt, const Grid &g, int nb, const int *n, int nd,
+                      double *out, cudaStream_t s);
+
 // ---- host-side math (bit-identical to the reference's float evaluation) ----
 void fd_coefficients(int nop, int ndim, const float *dd, int optfd, Coef &k);
 void sponge_weights(int nb, std::vector<float> &w);   // fdutil.c sponge_make
@@ -140,5 +164,11 @@ Step3Launch stepB3_tma_shape(const Grid &g, int num_sms, int L);
 cudaError_t launch_stepB3_tma(bool exact, const CUtensorMap *maps, int icur, float *nxt, const StepBParams &sp,
                               const Step3Launch &sh, unsigned long long *counter, unsigned long long base, int *err,
                               cudaStream_t s);
+cudaError_t launch_stepB3_tma_with(bool exact, const CUtensorMap &cur, const CUtensorMap &prv, const CUtensorMap &vel,
+                                   float *nxt, const StepBParams &sp, const Step3Launch &sh,
+                                   unsigned long long *counter, unsigned long long base, int *err, cudaStream_t s);
+bool make_tmap_3d(CUtensorMap *m, const float *base, int n1, int n2, int n3, int b1, int b2);
+// tensor-map boxes of the TMA step: the current level's halo box and the tile box
+void stepB3_tma_boxes(int *halo1, int *halo2, int *tile1, int *tile2);
 
 }  // namespace awe

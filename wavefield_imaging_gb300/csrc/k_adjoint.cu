@@ -1,0 +1,374 @@
+// Adjoint of the CPU-program scheme's time step and the imaging-condition
+// gradient accumulator (no counterpart in the reference, which has only the
+// forward map of MAWEFDcart{2D,3D}cpu.c).
+//
+// Forward step k (V_k = level k after its own sponge; W = sponge factor, I =
+// cells at least nop from every face, vel2 = v^2 dt^2):
+//   N = I (2 V_k + vel2 L V_k - W V_{k-1}) + (1 - I) W V_{k-1} + S_k
+//   N' = ABC(N; um = V_k)  (3D, abcone3d_apply),  V_{k+1} = W N'
+//   d_k = R (W V_k)
+// Adjoint step k, with mu = W lambda_{k+1} held in the buffer that becomes nu_k:
+//   nu_k, kappa_k = ABC^T(mu)
+//   lambda_k = 2 I nu_k + L(I vel2 nu_k) + kappa_k + W (1 - 2 I) nu_{k+1} + W R^T r_k
+//   the new buffer holds mu_k = W lambda_k
+//   dJ/dvel2 += I nu_k L(V_k)  (+ nu_k wav w at the source corners), in FP64.
+// The stencil is symmetric, so L^T is the same stencil applied to I vel2 nu.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "awe_internal.h"
+
+namespace awe {
+
+__device__ __forceinline__ float wcell(const AdjParams &p, int i1, int i2, int i3) {
+    if (!p.w1) return 1.f;
+    float w = __ldg(p.w1 + i1) * __ldg(p.w2 + i2);
+    if (p.nd == 3) w *= __ldg(p.w3 + i3);
+    return w;
+}
+
+template <int NOP, int NDIM>
+__device__ __forceinline__ bool interior(const Grid &g, int i1, int i2, int i3) {
+    bool in = i1 >= NOP && i1 < g.n1 - NOP && i2 >= NOP && i2 < g.n2 - NOP;
+    if (NDIM == 3) in = in && i3 >= NOP && i3 < g.n3 - NOP;
+    return in;
+}
+
+// main adjoint step, one thread per cell.  X = nu_k (stencil), Y = nu_{k+1}
+// in / mu_k out (same cell only), V = V_k (stencil), G += I nu L(V) in FP64.
+template <int NOP, int NDIM>
+__global__ void __launch_bounds__(256) k_adjB(const float *__restrict__ X, float *__restrict__ Y,
+                                              const float *__restrict__ V, const float *__restrict__ vel,
+                                              double *__restrict__ G, const AdjParams p) {
+    const int i1 = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i2 = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i3 = (NDIM == 3) ? (int)blockIdx.z : 0;
+    const Grid g = p.g;
+    if (i1 >= g.n1 || i2 >= g.n2) return;
+    const long long s2 = g.n1, s3 = (long long)g.n1 * g.n2;
+    const long long i = i3 * s3 + i2 * s2 + i1;
+    const bool in = interior<NOP, NDIM>(g, i1, i2, i3);
+    const float x = X[i];
+    // L(I vel2 nu) at i: neighbours outside the interior (or the grid) contribute 0
+    auto f = [&](long long j, int j1, int j2, int j3) -> float {
+        return interior<NOP, NDIM>(g, j1, j2, j3) ? __ldg(vel + j) * __ldg(X + j) : 0.f;
+    };
+    float lt = in ? p.k.c0 * (__ldg(vel + i) * x) : 0.f;
+#pragma unroll
+    for (int k = 1; k <= NOP; k++) {
+        float t = f(i - k, i1 - k, i2, i3) + f(i + k, i1 + k, i2, i3);
+        lt = fmaf(t, p.k.c[0][k], lt);
+        t = f(i - k * s2, i1, i2 - k, i3) + f(i + k * s2, i1, i2 + k, i3);
+        lt = fmaf(t, p.k.c[1][k], lt);
+        if constexpr (NDIM == 3) {
+            t = f(i - k * s3, i1, i2, i3 - k) + f(i + k * s3, i1, i2, i3 + k);
+            lt = fmaf(t, p.k.c[2][k], lt);
+        }
+    }
+    const float w = wcell(p, i1, i2, i3);
+    const float lam = (in ? 2.f * x : 0.f) + lt + (in ? -w : w) * Y[i];
+    Y[i] = w * lam;
+    if (in) {
+        float lap = V[i] * p.k.c0;
+#pragma unroll
+        for (int k = 1; k <= NOP; k++) {
+            float t = fmaf(__ldg(V + i - k) + __ldg(V + i + k), p.k.c[0][k],
+                           (__ldg(V + i - k * s2) + __ldg(V + i + k * s2)) * p.k.c[1][k]);
+            if constexpr (NDIM == 3) t = fmaf(__ldg(V + i - k * s3) + __ldg(V + i + k * s3), p.k.c[2][k], t);
+            lap += t;
+        }
+        G[i] += (double)x * (double)lap;
+    }
+}
+
+template <int NDIM>
+static void adj_dispatch_nop(int nop, const float *X, float *Y, const float *V, const float *vel, double *G,
+                             const AdjParams &p, cudaStream_t s) {
+    dim3 block(64, 4, 1);
+    dim3 grid((p.g.n1 + 63) / 64, (p.g.n2 + 3) / 4, NDIM == 3 ? p.g.n3 : 1);
+    switch (nop) {
+#define CASE(N) \
+    case N: k_adjB<N, NDIM><<<grid, block, 0, s>>>(X, Y, V, vel, G, p); break;
+        CASE(1) CASE(2) CASE(3) CASE(4) CASE(5) CASE(6) CASE(7) CASE(8) CASE(9) CASE(10)
+#undef CASE
+        default: break;
+    }
+}
+
+void launch_adjB(const float *X, float *Y, const float *V, const float *vel, double *G, const AdjParams &p,
+                 cudaStream_t s) {
+    if (p.nd == 3) adj_dispatch_nop<3>(p.nop, X, Y, V, vel, G, p, s);
+    else adj_dispatch_nop<2>(p.nop, X, Y, V, vel, G, p, s);
+}
+
+// ---------------------------------------------------------------------------
+// Transpose of abcone3d_apply (fdutil.c:2085-2177).  The forward runs three
+// passes (axis-1, axis-2, axis-3 faces); each updates, per line and outward,
+// uo[i] = um[a] + (um[i] - uo[b]) * c with a = b = the inward neighbour.  The
+// transpose visits the passes and the updates in reverse order:
+//   t = mu[i]; mu[i] = 0; mu[b] -= c t; kap[a] += t; kap[i] += c t.
+template <int AXIS>
+__global__ void k_abc_adj(float *mu, float *kap, const float *__restrict__ bl, const float *__restrict__ bh, Grid g,
+                          int nop, int top) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long base, st;
+    int n;
+    if (AXIS == 1) {  // line (i3, i2), coefficients [n3][n2]
+        if (t >= (long long)g.n2 * g.n3) return;
+        base = t * g.n1;
+        st = 1;
+        n = g.n1;
+    } else if (AXIS == 2) {  // line (i3, i1), coefficients [n3][n1]
+        if (t >= (long long)g.n1 * g.n3) return;
+        base = (t / g.n1) * g.n1 * (long long)g.n2 + t % g.n1;
+        st = g.n1;
+        n = g.n2;
+    } else {  // line (i2, i1), coefficients [n2][n1]
+        if (t >= (long long)g.n1 * g.n2) return;
+        base = t;
+        st = (long long)g.n1 * g.n2;
+        n = g.n3;
+    }
+    const float cl = bl[t], ch = bh[t];
+    for (int jj = 0; jj < nop; jj++) {
+        const int iop = nop - 1 - jj;
+        long long i = base + (long long)(n - nop + iop - 1) * st, b = i - st;
+        float v = mu[i];
+        mu[i] = 0.f;
+        mu[b] -= ch * v;
+        kap[b] += v;
+        kap[i] += ch * v;
+        if (top) {
+            i = base + (long long)(nop - iop) * st;
+            b = i + st;
+            v = mu[i];
+            mu[i] = 0.f;
+            mu[b] -= cl * v;
+            kap[b] += v;
+            kap[i] += cl * v;
+        }
+    }
+}
+
+void launch_abc_adjB(int nop, int fsrf, float *mu, float *kap, const AbcB &a, const Grid &g, cudaStream_t s) {
+    const int T = 128;
+    long long n = (long long)g.n1 * g.n2;
+    k_abc_adj<3><<<(unsigned)((n + T - 1) / T), T, 0, s>>>(mu, kap, a.yl, a.yh, g, nop, 1);
+    n = (long long)g.n1 * g.n3;
+    k_abc_adj<2><<<(unsigned)((n + T - 1) / T), T, 0, s>>>(mu, kap, a.xl, a.xh, g, nop, 1);
+    n = (long long)g.n2 * g.n3;
+    k_abc_adj<1><<<(unsigned)((n + T - 1) / T), T, 0, s>>>(mu, kap, a.zl, a.zh, g, nop, !fsrf);
+}
+
+// mu += W kap on the faces the transpose ABC touched (the outer nop+2 cells of
+// every axis), clearing kap for the next step.  The three slabs are disjoint:
+// axis-1 ends of every line; axis-2 bands without them; axis-3 bands without both.
+__global__ void k_kap_fold(float *mu, float *kap, AdjParams p, int width) {
+    const Grid g = p.g;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int W = width;
+    const long long n_a = (long long)g.n2 * g.n3 * 2 * W;
+    const int in1 = g.n1 - 2 * W;
+    const long long n_b = (long long)in1 * 2 * W * g.n3;
+    const int in2 = g.n2 - 2 * W;
+    const long long n_c = (long long)in1 * in2 * 2 * W;
+    int i1, i2, i3;
+    if (t < n_a) {
+        const long long line = t / (2 * W);
+        const int k = (int)(t - line * 2 * W);
+        i1 = k < W ? k : g.n1 - 2 * W + k;
+        i2 = (int)(line % g.n2);
+        i3 = (int)(line / g.n2);
+    } else if (t < n_a + n_b) {
+        const long long u = t - n_a;
+        i1 = W + (int)(u % in1);
+        const long long r = u / in1;
+        const int k = (int)(r % (2 * W));
+        i2 = k < W ? k : g.n2 - 2 * W + k;
+        i3 = (int)(r / (2 * W));
+    } else if (t < n_a + n_b + n_c) {
+        const long long u = t - n_a - n_b;
+        i1 = W + (int)(u % in1);
+        const long long r = u / in1;
+        i2 = W + (int)(r % in2);
+        const int k = (int)(r / in2);
+        i3 = k < W ? k : g.n3 - 2 * W + k;
+    } else {
+        return;
+    }
+    const long long i = ((long long)i3 * g.n2 + i2) * g.n1 + i1;
+    const float kv = kap[i];
+    if (kv != 0.f) {
+        mu[i] += wcell(p, i1, i2, i3) * kv;
+        kap[i] = 0.f;
+    }
+}
+
+void launch_kap_fold(float *mu, float *kap, const AdjParams &p, cudaStream_t s) {
+    const Grid g = p.g;
+    const int W = p.nop + 2;
+    const long long n = (long long)g.n2 * g.n3 * 2 * W + (long long)(g.n1 - 2 * W) * 2 * W * g.n3 +
+                        (long long)(g.n1 - 2 * W) * (g.n2 - 2 * W) * 2 * W;
+    k_kap_fold<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(mu, kap, p, W);
+}
+
+// W R^T r: receiver residuals into mu (scaled by W twice: once from the
+// gather of W V, once from mu = W lambda).  Coincident corners add atomically.
+__global__ void k_rec_adj(float *mu, const GeoPoint *__restrict__ pts, int nr, const float *__restrict__ r,
+                          AdjParams p, const long long *__restrict__ off) {
+    const int ir = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ir >= nr) return;
+    const GeoPoint pt = pts[ir];
+    const float rv = r[ir];
+    const Grid g = p.g;
+    const int nc = p.nd == 3 ? 8 : 4;
+    for (int c = 0; c < nc; c++) {
+        const long long n = pt.base + off[c];
+        const int i1 = (int)(n % g.n1), i2 = (int)((n / g.n1) % g.n2), i3 = (int)(n / ((long long)g.n1 * g.n2));
+        const float w = wcell(p, i1, i2, i3);
+        atomicAdd(mu + n, w * (w * (pt.w[c] * rv)));
+    }
+}
+
+void launch_rec_adj(float *mu, const GeoPoint *pts, int nr, const float *r, const AdjParams &p, const long long *off,
+                    cudaStream_t s) {
+    if (nr > 0) k_rec_adj<<<(nr + 127) / 128, 128, 0, s>>>(mu, pts, nr, r, p, off);
+}
+
+// source term of the gradient: dJ/dvel2[node] += nu[node] * wav * w (one
+// thread, sources and corners in order)
+__global__ void k_src_grad(double *G, const float *__restrict__ nu, const GeoPoint *__restrict__ pts, int ns,
+                           const float *__restrict__ wav, int it, int ncs, int one_wavelet, int nc,
+                           const long long *__restrict__ off) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    for (int s = 0; s < ns; s++) {
+        const float dd = one_wavelet ? wav[(long long)it * ncs] : wav[(long long)it * ncs + s];
+        const GeoPoint pt = pts[s];
+        for (int c = 0; c < nc; c++) {
+            const long long n = pt.base + off[c];
+            G[n] += (double)nu[n] * (double)(dd * pt.w[c]);
+        }
+    }
+}
+
+void launch_src_grad(double *G, const float *nu, const GeoPoint *pts, int ns, const float *wav, int it, int ncs,
+                     bool one_wavelet, int nd, const long long *off, cudaStream_t s) {
+    if (ns > 0) k_src_grad<<<1, 1, 0, s>>>(G, nu, pts, ns, wav, it, ncs, one_wavelet, nd == 3 ? 8 : 4, off);
+}
+
+// ---------------------------------------------------------------------------
+// Residual and misfit: r = d - dobs per row; per-row sums of r^2 in FP64
+// (one block per row, fixed reduction order).
+__global__ void k_residual(const float *__restrict__ d, const float *__restrict__ dobs, float *__restrict__ r, int nr,
+                           double *__restrict__ row_sum) {
+    const int row = blockIdx.x;
+    __shared__ double part[256];
+    double acc = 0;
+    for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+        const long long j = (long long)row * nr + i;
+        const float v = d[j] - dobs[j];
+        r[j] = v;
+        acc += (double)v * (double)v;
+    }
+    part[threadIdx.x] = acc;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) part[threadIdx.x] += part[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) row_sum[row] = part[0];
+}
+
+void launch_residual(const float *d, const float *dobs, float *r, int nrows, int nr, double *row_sum, cudaStream_t s) {
+    if (nrows > 0) k_residual<<<nrows, 256, 0, s>>>(d, dobs, r, nr, row_sum);
+}
+
+// ---------------------------------------------------------------------------
+// Checkpoints: BF16 or FP16 with one FP32 scale per level (the level's
+// max |v|), or plain FP32 copies.
+__global__ void k_absmax(const float *__restrict__ u, long long n, unsigned int *out) {
+    float m = 0.f;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        m = fmaxf(m, fabsf(u[i]));
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));  // non-negative floats order as unsigned
+}
+
+__device__ __forceinline__ void to16(float x, __nv_bfloat16 &q) { q = __float2bfloat16_rn(x); }
+__device__ __forceinline__ void to16(float x, __half &q) { q = __float2half_rn(x); }
+__device__ __forceinline__ float from16(__nv_bfloat16 q) { return __bfloat162float(q); }
+__device__ __forceinline__ float from16(__half q) { return __half2float(q); }
+
+// q = round(u / scale) with scale = max |u| (1 for an all-zero level): the
+// values land in [-1, 1], inside FP16's normal range down to 6e-5 of the max
+template <typename Q>
+__global__ void k_quant16(const float *__restrict__ u, long long n, const unsigned int *__restrict__ amax,
+                          Q *__restrict__ q, float *__restrict__ scale_out) {
+    const float a = __uint_as_float(*amax);
+    const float scale = a > 0.f ? a : 1.f;
+    const float inv = 1.f / scale;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *scale_out = scale;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        to16(u[i] * inv, q[i]);
+}
+
+template <typename Q>
+__global__ void k_dequant16(const Q *__restrict__ q, long long n, const float *__restrict__ scale,
+                            float *__restrict__ u) {
+    const float sc = *scale;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        u[i] = from16(q[i]) * sc;
+}
+
+void launch_ckpt_store16(bool fp16, const float *u, long long n, unsigned int *amax, void *q, float *scale, int grid,
+                         cudaStream_t s) {
+    cudaMemsetAsync(amax, 0, sizeof(unsigned int), s);
+    k_absmax<<<grid, 256, 0, s>>>(u, n, amax);
+    if (fp16) k_quant16<__half><<<grid, 256, 0, s>>>(u, n, amax, (__half *)q, scale);
+    else k_quant16<__nv_bfloat16><<<grid, 256, 0, s>>>(u, n, amax, (__nv_bfloat16 *)q, scale);
+}
+
+void launch_ckpt_load16(bool fp16, const void *q, long long n, const float *scale, float *u, int grid,
+                        cudaStream_t s) {
+    if (fp16) k_dequant16<__half><<<grid, 256, 0, s>>>((const __half *)q, n, scale, u);
+    else k_dequant16<__nv_bfloat16><<<grid, 256, 0, s>>>((const __nv_bfloat16 *)q, n, scale, u);
+}
+
+// ---------------------------------------------------------------------------
+// dJ/dm on the model grid: dJ/dvel2 * (-vel2^2 / dt^2) per padded cell (vel2 =
+// v^2 dt^2, m = 1/v^2; zero where vel2 is zero), summed over the padded cells
+// that replicate each model cell (the transpose of the edge padding).
+__global__ void k_grad_fold(const double *__restrict__ G, const float *__restrict__ vel2, double inv_dt2, Grid g,
+                            int nb, int m1, int m2, int m3, int nd, double *__restrict__ out) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)m1 * m2 * m3) return;
+    const int j1 = (int)(t % m1), j2 = (int)((t / m1) % m2), j3 = (int)(t / ((long long)m1 * m2));
+    auto range = [&](int j, int m, int npad, int &lo, int &hi) {
+        lo = j == 0 ? 0 : j + nb;
+        hi = j == m - 1 ? npad - 1 : j + nb;
+    };
+    int a1, b1, a2, b2, a3 = 0, b3 = 0;
+    range(j1, m1, g.n1, a1, b1);
+    range(j2, m2, g.n2, a2, b2);
+    if (nd == 3) range(j3, m3, g.n3, a3, b3);
+    double acc = 0;
+    for (int i3 = a3; i3 <= b3; i3++)
+        for (int i2 = a2; i2 <= b2; i2++)
+            for (int i1 = a1; i1 <= b1; i1++) {
+                const long long i = ((long long)i3 * g.n2 + i2) * g.n1 + i1;
+                const double v2 = vel2[i];
+                acc += G[i] * (-v2 * v2 * inv_dt2);
+            }
+    out[t] = acc;
+}
+
+void launch_grad_fold(const double *G, const float *vel2, float dt, const Grid &g, int nb, const int *n, int nd,
+                      double *out, cudaStream_t s) {
+    const long long m = (long long)n[0] * n[1] * (nd == 3 ? n[2] : 1);
+    const double inv = 1.0 / ((double)dt * (double)dt);
+    k_grad_fold<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(G, vel2, inv, g, nb, n[0], n[1], nd == 3 ? n[2] : 1, nd,
+                                                          out);
+}
+
+}  // namespace awe

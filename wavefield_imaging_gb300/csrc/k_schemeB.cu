@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(256) k_stepB(const float *__restrict__ cur, fl
     const long long s2 = g.n1, s3 = (long long)g.n1 * g.n2;
     const long long i = i3 * s3 + i2 * s2 + i1;
 
-    float prv = nxt[i];
+    float prv = p.prv ? p.prv[i] : nxt[i];  // out of place when p.prv is set
     if (p.damp_prev) prv = damp_cell<EXACT, NDIM>(prv, i1, i2, i3, p.w1, p.w2, p.w3);
 
     bool interior = i1 >= NOP && i1 < g.n1 - NOP && i2 >= NOP && i2 < g.n2 - NOP;

@@ -282,6 +282,13 @@ bool make_tmap_3d(CUtensorMap *m, const float *base, int n1, int n2, int n3, int
     return r == CUDA_SUCCESS;
 }
 
+void stepB3_tma_boxes(int *halo1, int *halo2, int *tile1, int *tile2) {
+    *halo1 = s3::HZ;
+    *halo2 = s3::HX;
+    *tile1 = s3::TZ;
+    *tile2 = s3::TX;
+}
+
 bool stepB3_tma_eligible(int ndim, int nop, bool rho, const Grid &g) {
     return ndim == 3 && nop == 4 && !rho && g.n1 % 4 == 0 && g.n1 >= 16 && g.n2 >= 16 && g.n3 >= 9;
 }
@@ -313,6 +320,15 @@ Step3Launch stepB3_tma_shape(const Grid &g, int num_sms, int L) {
 cudaError_t launch_stepB3_tma(bool exact, const CUtensorMap *maps, int icur, float *nxt, const StepBParams &sp,
                               const Step3Launch &sh, unsigned long long *counter, unsigned long long base, int *err,
                               cudaStream_t s) {
+    return launch_stepB3_tma_with(exact, maps[icur], maps[2 + (1 - icur)], maps[4], nxt, sp, sh, counter, base, err,
+                                  s);
+}
+
+// one step with explicit maps: cur halo-box map, prv tile-box map (the buffer
+// the new level replaces, or another one when stepping out of place), vel
+cudaError_t launch_stepB3_tma_with(bool exact, const CUtensorMap &cur, const CUtensorMap &prv, const CUtensorMap &vel,
+                                   float *nxt, const StepBParams &sp, const Step3Launch &sh,
+                                   unsigned long long *counter, unsigned long long base, int *err, cudaStream_t s) {
     Step3Params p{};
     p.n1 = sp.g.n1;
     p.n2 = sp.g.n2;
@@ -341,7 +357,6 @@ cudaError_t launch_stepB3_tma(bool exact, const CUtensorMap *maps, int icur, flo
     p.base = base;
     p.err = err;
     p.nxt = nxt;
-    const CUtensorMap &cur = maps[icur], &prv = maps[2 + (1 - icur)], &vel = maps[4];
     if (exact) {
         cudaFuncSetAttribute(k_stepB3_o8<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem);
         k_stepB3_o8<true><<<sh.grid, s3::NTHREADS, sh.smem, s>>>(cur, prv, vel, p);

@@ -224,6 +224,7 @@ awe_status awe_plan_destroy(awe_plan *p) {
     if (!p) return AWE_OK;
     cudaSetDevice(p->device);
     if (p->stream) cudaStreamSynchronize(p->stream);
+    plan_gradient_free(p);
     for (auto &a : p->allocs) cudaFree(a.first);
     p->allocs.clear();
     if (p->h_pinned) cudaFreeHost(p->h_pinned);
@@ -380,6 +381,78 @@ awe_status awe_forward(awe_plan *p, const float *wav, int ncs, float *dat, float
     dev_free(p, d_dat);
     dev_free(p, d_wfl);
     if (st == AWE_OK) st = check_pipeline(p);
+    return st;
+}
+
+awe_status awe_gradient_device(awe_plan *p, const float *d_wav, int ncs, const float *d_dobs,
+                               const awe_grad_opts *opts, double *d_grad, double *misfit, float *d_dsyn,
+                               void *stream) {
+    if (!p || !d_wav || !d_dobs || !d_grad || !misfit) {
+        set_error("null plan, wavelet, data, gradient or misfit pointer");
+        return AWE_ERR_INVALID;
+    }
+    if (!p->model_set || !p->geom_set) {
+        set_error("awe_set_model and awe_set_geometry must precede awe_gradient");
+        return AWE_ERR_STATE;
+    }
+    if (ncs != 1 && ncs != p->ns) {
+        set_error("wavelet has %d components; need 1 or ns=%d", ncs, p->ns);
+        return AWE_ERR_INVALID;
+    }
+    awe_grad_opts o{0, AWE_CKPT_BF16};
+    if (opts) o = *opts;
+    CUDA_TRY(cudaSetDevice(p->device));
+    cudaStream_t s = stream ? (cudaStream_t)stream : p->stream;
+    awe_status st = plan_gradient(p, d_wav, ncs, d_dobs, o, d_grad, misfit, d_dsyn, s);
+    if (st != AWE_OK) return st;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error("kernel launch failed: %s", cudaGetErrorString(e));
+        return AWE_ERR_CUDA;
+    }
+    return check_pipeline(p);
+}
+
+awe_status awe_gradient(awe_plan *p, const float *wav, int ncs, const float *dobs, const awe_grad_opts *opts,
+                        double *grad, double *misfit, float *dsyn) {
+    if (!p || !wav || !dobs || !grad || !misfit) {
+        set_error("null plan, wavelet, data, gradient or misfit pointer");
+        return AWE_ERR_INVALID;
+    }
+    CUDA_TRY(cudaSetDevice(p->device));
+    const awe_desc &d = p->d;
+    const size_t wav_bytes = (size_t)d.nt * ncs * sizeof(float);
+    const size_t dat_bytes = (size_t)p->nsmp * p->nr * sizeof(float);
+    const size_t grad_bytes = (size_t)d.n[0] * d.n[1] * (d.ndim == 3 ? d.n[2] : 1) * sizeof(double);
+    float *d_wav = nullptr, *d_dobs = nullptr, *d_dsyn = nullptr;
+    double *d_grad = nullptr;
+    awe_status st = dev_alloc(p, (void **)&d_wav, wav_bytes);
+    if (st == AWE_OK) st = dev_alloc(p, (void **)&d_dobs, dat_bytes > 0 ? dat_bytes : 4);
+    if (st == AWE_OK && dsyn) st = dev_alloc(p, (void **)&d_dsyn, dat_bytes > 0 ? dat_bytes : 4);
+    if (st == AWE_OK) st = dev_alloc(p, (void **)&d_grad, grad_bytes);
+    if (st == AWE_OK) {
+        cudaError_t e = cudaMemcpyAsync(d_wav, wav, wav_bytes, cudaMemcpyHostToDevice, p->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d_dobs, dobs, dat_bytes, cudaMemcpyHostToDevice, p->stream);
+        if (e != cudaSuccess) {
+            set_error("input upload failed: %s", cudaGetErrorString(e));
+            st = AWE_ERR_CUDA;
+        }
+    }
+    if (st == AWE_OK) st = awe_gradient_device(p, d_wav, ncs, d_dobs, opts, d_grad, misfit, d_dsyn, nullptr);
+    if (st == AWE_OK) {
+        cudaError_t e = cudaMemcpyAsync(grad, d_grad, grad_bytes, cudaMemcpyDeviceToHost, p->stream);
+        if (e == cudaSuccess && dsyn) e = cudaMemcpyAsync(dsyn, d_dsyn, dat_bytes, cudaMemcpyDeviceToHost, p->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+        if (e != cudaSuccess) {
+            set_error("result download failed: %s", cudaGetErrorString(e));
+            st = AWE_ERR_CUDA;
+        }
+    }
+    cudaStreamSynchronize(p->stream);
+    dev_free(p, d_wav);
+    dev_free(p, d_dobs);
+    dev_free(p, d_dsyn);
+    dev_free(p, d_grad);
     return st;
 }
 

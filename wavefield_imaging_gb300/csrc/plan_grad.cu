@@ -1,0 +1,240 @@
+// Misfit gradient of the CPU-program scheme: forward pass with checkpoints,
+// then, segment by segment from the last, recompute of the forward levels
+// from the segment's checkpoint and the adjoint sweep over them.
+//
+// Memory (cells = padded grid): 2 forward levels + vel (the plan's), segment
+// levels (ckpt_every + 1) x 4 B, checkpoints 2 x ceil(nt / ckpt_every) x 2 B
+// (BF16, FP16) or 4 B, adjoint 2 x 4 B, ABC transpose scratch 4 B (3D), gradient 8 B.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <vector>
+
+#include "awe_internal.h"
+#include "plan_impl.h"
+
+namespace awe {
+
+#define CUDA_TRY(expr)                                                                            \
+    do {                                                                                          \
+        cudaError_t e_ = (expr);                                                                  \
+        if (e_ != cudaSuccess) {                                                                  \
+            set_error("%s failed: %s (%s:%d)", #expr, cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return AWE_ERR_CUDA;                                                                  \
+        }                                                                                         \
+    } while (0)
+#define AWE_TRY(expr)                \
+    do {                             \
+        awe_status s_ = (expr);      \
+        if (s_ != AWE_OK) return s_; \
+    } while (0)
+
+struct GradState {
+    int T = 0, nseg = 0, fmt = -1;
+    float *slots = nullptr;  // (T + 1) levels
+    void *ckpt = nullptr;    // 2 * nseg levels
+    float *scales = nullptr; // 2 * nseg (BF16)
+    unsigned int *amax = nullptr;
+    float *X = nullptr, *Y = nullptr, *kap = nullptr;
+    double *G = nullptr;
+    float *dat = nullptr, *r = nullptr;
+    double *row_sum = nullptr;
+    std::vector<CUtensorMap> halo_maps, tile_maps;  // per slot (TMA step kernel)
+};
+
+void plan_gradient_free(awe_plan *p) {
+    if (!p->grad) return;
+    GradState *st = p->grad;
+    for (void *ptr : {(void *)st->slots, st->ckpt, (void *)st->scales, (void *)st->amax, (void *)st->X, (void *)st->Y,
+                      (void *)st->kap, (void *)st->G, (void *)st->dat, (void *)st->r, (void *)st->row_sum})
+        if (ptr) dev_free(p, ptr);
+    delete st;
+    p->grad = nullptr;
+}
+
+static awe_status grad_alloc(awe_plan *p, int T, int fmt) {
+    if (p->grad && p->grad->T == T && p->grad->fmt == fmt) return AWE_OK;
+    plan_gradient_free(p);
+    GradState *st = new GradState();
+    p->grad = st;
+    const awe_desc &d = p->d;
+    const size_t cells = (size_t)p->g.cells();
+    st->T = T;
+    st->fmt = fmt;
+    st->nseg = (d.nt + T - 1) / T;
+    const size_t es = fmt == AWE_CKPT_FP32 ? 4 : 2;
+    AWE_TRY(dev_alloc(p, (void **)&st->slots, (size_t)(T + 1) * cells * sizeof(float)));
+    AWE_TRY(dev_alloc(p, &st->ckpt, (size_t)2 * st->nseg * cells * es));
+    AWE_TRY(dev_alloc(p, (void **)&st->scales, (size_t)2 * st->nseg * sizeof(float)));
+    AWE_TRY(dev_alloc(p, (void **)&st->amax, sizeof(unsigned int)));
+    AWE_TRY(dev_alloc(p, (void **)&st->X, cells * sizeof(float)));
+    AWE_TRY(dev_alloc(p, (void **)&st->Y, cells * sizeof(float)));
+    if (d.ndim == 3 && d.dabc) AWE_TRY(dev_alloc(p, (void **)&st->kap, cells * sizeof(float)));
+    AWE_TRY(dev_alloc(p, (void **)&st->G, cells * sizeof(double)));
+    const size_t nd = (size_t)p->nsmp * (p->nr > 0 ? p->nr : 1);
+    AWE_TRY(dev_alloc(p, (void **)&st->dat, nd * sizeof(float)));
+    AWE_TRY(dev_alloc(p, (void **)&st->r, nd * sizeof(float)));
+    AWE_TRY(dev_alloc(p, (void **)&st->row_sum, (size_t)p->nsmp * sizeof(double)));
+    if (p->use_tma) {
+        int h1, h2, t1, t2;
+        stepB3_tma_boxes(&h1, &h2, &t1, &t2);
+        st->halo_maps.resize(T + 1);
+        st->tile_maps.resize(T + 1);
+        for (int j = 0; j <= T; j++) {
+            const float *base = st->slots + (size_t)j * cells;
+            if (!make_tmap_3d(&st->halo_maps[j], base, p->g.n1, p->g.n2, p->g.n3, h1, h2) ||
+                !make_tmap_3d(&st->tile_maps[j], base, p->g.n1, p->g.n2, p->g.n3, t1, t2)) {
+                st->halo_maps.clear();
+                st->tile_maps.clear();
+                break;
+            }
+        }
+    }
+    return AWE_OK;
+}
+
+static int grid_for(long long n) {
+    long long b = (n + 255) / 256;
+    return (int)(b < 4096 ? (b > 0 ? b : 1) : 4096);
+}
+
+static awe_status ckpt_store(awe_plan *p, int idx, const float *u, cudaStream_t s) {
+    GradState *st = p->grad;
+    const long long cells = p->g.cells();
+    if (st->fmt != AWE_CKPT_FP32) {
+        void *q = (char *)st->ckpt + (size_t)idx * cells * 2;
+        launch_ckpt_store16(st->fmt == AWE_CKPT_FP16, u, cells, st->amax, q, st->scales + idx, grid_for(cells), s);
+    } else {
+        float *q = (float *)st->ckpt + (size_t)idx * cells;
+        CUDA_TRY(cudaMemcpyAsync(q, u, (size_t)cells * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    }
+    return AWE_OK;
+}
+
+static awe_status ckpt_load(awe_plan *p, int idx, float *u, cudaStream_t s) {
+    GradState *st = p->grad;
+    const long long cells = p->g.cells();
+    if (st->fmt != AWE_CKPT_FP32) {
+        const void *q = (const char *)st->ckpt + (size_t)idx * cells * 2;
+        launch_ckpt_load16(st->fmt == AWE_CKPT_FP16, q, cells, st->scales + idx, u, grid_for(cells), s);
+    } else {
+        const float *q = (const float *)st->ckpt + (size_t)idx * cells;
+        CUDA_TRY(cudaMemcpyAsync(u, q, (size_t)cells * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    }
+    return AWE_OK;
+}
+
+awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *d_dobs, const awe_grad_opts &o,
+                         double *d_grad, double *misfit, float *d_dsyn, cudaStream_t s) {
+    const awe_desc &d = p->d;
+    if (d.scheme != AWE_SCHEME_CPU || d.coords != AWE_CART) {
+        set_error("awe_gradient: only the cartesian CPU-program scheme has an adjoint");
+        return AWE_ERR_UNSUPPORTED;
+    }
+    if (p->den || d.hybrid) {
+        set_error("awe_gradient: variable density and the hybrid ABC have no adjoint here");
+        return AWE_ERR_UNSUPPORTED;
+    }
+    if (d.precision != AWE_FAST) {
+        set_error("awe_gradient: precision must be AWE_FAST");
+        return AWE_ERR_UNSUPPORTED;
+    }
+    const Grid &g = p->g;
+    const int W = p->nop + 2;
+    if (d.ndim == 3 && d.dabc && (g.n1 <= 2 * W || g.n2 <= 2 * W || g.n3 <= 2 * W)) {
+        set_error("awe_gradient: padded grid too small for the one-way ABC transpose");
+        return AWE_ERR_INVALID;
+    }
+    int T = o.ckpt_every > 0 ? o.ckpt_every : (int)std::ceil(std::sqrt((double)d.nt));
+    if (T > d.nt) T = d.nt;
+    if (T < 1) T = 1;
+    if (o.ckpt_format != AWE_CKPT_BF16 && o.ckpt_format != AWE_CKPT_FP32 && o.ckpt_format != AWE_CKPT_FP16) {
+        set_error("awe_gradient: unknown checkpoint format %d", o.ckpt_format);
+        return AWE_ERR_INVALID;
+    }
+    AWE_TRY(grad_alloc(p, T, o.ckpt_format));
+    GradState *st = p->grad;
+    const long long cells = g.cells();
+    const size_t bytes = (size_t)cells * sizeof(float);
+    float *dat = d_dsyn ? d_dsyn : st->dat;
+    long long launches = 0;
+
+    // 1. forward with checkpoints of both levels at the start of every segment
+    StepHook hook = [&](int it, const float *prev, const float *cur, cudaStream_t ss) -> awe_status {
+        if (it % T != 0) return AWE_OK;
+        const int seg = it / T;
+        AWE_TRY(ckpt_store(p, 2 * seg, prev, ss));
+        AWE_TRY(ckpt_store(p, 2 * seg + 1, cur, ss));
+        return AWE_OK;
+    };
+    AWE_TRY(planB_run_hooked(p, d_wav, ncs, dat, nullptr, s, &hook));
+    launches += p->launches;
+
+    // 2. residual and misfit (FP64 per row, summed in row order on the host)
+    launch_residual(dat, d_dobs, st->r, p->nsmp, p->nr, st->row_sum, s);
+    std::vector<double> rows(p->nsmp);
+    CUDA_TRY(cudaMemcpyAsync(rows.data(), st->row_sum, rows.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+
+    // 3. adjoint sweep
+    CUDA_TRY(cudaMemsetAsync(st->X, 0, bytes, s));
+    CUDA_TRY(cudaMemsetAsync(st->Y, 0, bytes, s));
+    CUDA_TRY(cudaMemsetAsync(st->G, 0, (size_t)cells * sizeof(double), s));
+    if (st->kap) CUDA_TRY(cudaMemsetAsync(st->kap, 0, bytes, s));
+    const StepBParams sp = stepB_params(p);
+    const bool sponge = d.dabc && !d.hybrid;
+    AdjParams ap{};
+    ap.g = g;
+    ap.k = p->k;
+    ap.nd = d.ndim;
+    ap.nop = p->nop;
+    ap.w1 = sponge ? p->w[0] : nullptr;
+    ap.w2 = sponge ? p->w[1] : nullptr;
+    ap.w3 = sponge ? p->w[2] : nullptr;
+    AbcB abc{p->abc[0], p->abc[1], p->abc[2], p->abc[3], p->abc[4], p->abc[5]};
+    const bool maps = !st->halo_maps.empty();
+    float *X = st->X, *Y = st->Y;
+    for (int seg = st->nseg - 1; seg >= 0; seg--) {
+        const int k0 = seg * T, k1 = std::min(k0 + T, d.nt);
+        float *slot0 = st->slots;
+        AWE_TRY(ckpt_load(p, 2 * seg, slot0, s));
+        AWE_TRY(ckpt_load(p, 2 * seg + 1, slot0 + cells, s));
+        for (int k = k0; k <= k1 - 2; k++) {
+            const int j = k - k0;
+            float *A = slot0 + (size_t)j * cells, *B = A + cells, *N = B + cells;
+            AWE_TRY(stepB_full(p, sp, A, B, N, k, d_wav, ncs, maps ? &st->halo_maps[j + 1] : nullptr,
+                               maps ? &st->tile_maps[j] : nullptr, s, launches));
+        }
+        for (int k = k1 - 1; k >= k0; k--) {
+            const float *Vk = slot0 + (size_t)(k - k0 + 1) * cells;
+            if (d.ndim == 3 && d.dabc) {
+                launch_abc_adjB(p->nop, d.fsrf, X, st->kap, abc, g, s);
+                launches += 3;
+            }
+            launch_adjB(X, Y, Vk, p->vel, st->G, ap, s);
+            launches++;
+            if (d.ndim == 3 && d.dabc) {
+                launch_kap_fold(Y, st->kap, ap, s);
+                launches++;
+            }
+            if (k % d.jdata == 0 && p->nr > 0) {
+                launch_rec_adj(Y, p->rec, p->nr, st->r + (size_t)(k / d.jdata) * p->nr, ap, p->corner_off, s);
+                launches++;
+            }
+            if (p->ns > 0) {
+                launch_src_grad(st->G, X, p->src, p->ns, d_wav, k, ncs, ncs == 1, d.ndim, p->corner_off, s);
+                launches++;
+            }
+            std::swap(X, Y);
+        }
+    }
+    launch_grad_fold(st->G, p->vel, d.dt, g, p->nbd, d.n, d.ndim, d_grad, s);
+    launches++;
+    CUDA_TRY(cudaStreamSynchronize(s));
+    double J = 0;
+    for (double v : rows) J += 0.5 * v;
+    *misfit = J;
+    p->launches = launches;
+    return AWE_OK;
+}
+
+}  // namespace awe

@@ -3,10 +3,15 @@
 
 #include <cuda_runtime.h>
 
+#include <functional>
 #include <utility>
 #include <vector>
 
 #include "awe_internal.h"
+
+namespace awe {
+struct GradState;
+}
 
 struct awe_plan {
     awe_desc d{};
@@ -67,6 +72,9 @@ struct awe_plan {
     unsigned long long sched_base = 0;
     int *d_err = nullptr;
 
+    // misfit gradient state (allocated by the first awe_gradient call)
+    awe::GradState *grad = nullptr;
+
     // optional per-launch timing of the step kernel
     bool profile = false;
     std::vector<cudaEvent_t> prof_ev;  // pairs (start, stop)
@@ -87,6 +95,18 @@ void prof_end(awe_plan *p, cudaStream_t s);
 awe_status planB_init(awe_plan *p);
 awe_status planB_model(awe_plan *p, const float *vel, const float *den);
 awe_status planB_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, float *d_wfl, cudaStream_t s);
+// called at the start of step it with the two levels (prev = V_{it-1} with its
+// second sponge pending, cur = V_it)
+typedef std::function<awe_status(int it, const float *prev, const float *cur, cudaStream_t s)> StepHook;
+awe_status planB_run_hooked(awe_plan *p, const float *d_wav, int ncs, float *d_dat, float *d_wfl, cudaStream_t s,
+                            const StepHook *hook);
+StepBParams stepB_params(const awe_plan *p);
+awe_status stepB_full(awe_plan *p, const StepBParams &sp, const float *prv, const float *cur, float *nxt, int it,
+                      const float *d_wav, int ncs, const CUtensorMap *cur_map, const CUtensorMap *prv_map,
+                      cudaStream_t s, long long &launches);
+awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *d_dobs, const awe_grad_opts &o,
+                         double *d_grad, double *misfit, float *d_dsyn, cudaStream_t s);
+void plan_gradient_free(awe_plan *p);
 
 awe_status planA_init(awe_plan *p);
 awe_status planA_model(awe_plan *p, const float *vel, const float *rfl);

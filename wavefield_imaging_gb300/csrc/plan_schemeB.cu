@@ -260,20 +260,10 @@ awe_status set_geometry_common(awe_plan *p, int ns, const float *sou, int nr, co
     return AWE_OK;
 }
 
-awe_status planB_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, float *d_wfl, cudaStream_t s) {
+StepBParams stepB_params(const awe_plan *p) {
     const awe_desc &d = p->d;
     const Grid &g = p->g;
-    const bool exact = d.precision == AWE_EXACT;
     const bool sponge = d.dabc && !d.hybrid;
-    const int shell = (d.ndim == 3 && sponge) ? p->nop + 2 : 0;
-    const size_t bytes = (size_t)g.cells() * sizeof(float);
-    long long launches = 0;
-
-    CUDA_TRY(cudaMemsetAsync(p->u[0], 0, bytes, s));
-    CUDA_TRY(cudaMemsetAsync(p->u[1], 0, bytes, s));
-    if (p->nsnap > 0 && !d_wfl && p->snap_cb && !p->d_snap_tmp)
-        AWE_TRY(dev_alloc(p, (void **)&p->d_snap_tmp, p->snap_elems * sizeof(float)));
-
     StepBParams sp{};
     sp.g = g;
     sp.k = p->k;
@@ -282,56 +272,97 @@ awe_status planB_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, flo
     sp.w3 = p->w[2];
     sp.damp_prev = sponge;
     sp.sponge_new = sponge && !p->sponge_deferred;
-    sp.shell = shell;
+    sp.shell = (d.ndim == 3 && sponge) ? p->nop + 2 : 0;
     for (int a = 0; a < 3; a++) {
         sp.ilo[a] = sponge ? p->wlo[a] : 0;
         sp.ihi[a] = sponge ? p->whi[a] : (a == 0 ? g.n1 : a == 1 ? g.n2 : g.n3);
     }
-    AbcB abc{p->abc[0], p->abc[1], p->abc[2], p->abc[3], p->abc[4], p->abc[5]};
+    sp.prv = nullptr;
+    return sp;
+}
+
+// One full time step it: the new level is written to `nxt`, which is the
+// buffer holding the previous level (in place, prv_map == null or the TMA
+// maps of that buffer) or a third buffer (out of place: `prv` names the
+// previous level, and for the TMA kernel `cur_map`/`prv_map` are given).
+awe_status stepB_full(awe_plan *p, const StepBParams &sp0, const float *prv, const float *cur, float *nxt, int it,
+                      const float *d_wav, int ncs, const CUtensorMap *cur_map, const CUtensorMap *prv_map,
+                      cudaStream_t s, long long &launches) {
+    const awe_desc &d = p->d;
+    const Grid &g = p->g;
+    const bool exact = d.precision == AWE_EXACT;
+    const bool sponge = d.dabc && !d.hybrid;
+    const int shell = sp0.shell;
+    StepBParams sp = sp0;
+    sp.prv = (prv != nxt) ? prv : nullptr;
+    prof_begin(p, s);
+    if (p->use_tma && cur_map && prv_map) {
+        cudaError_t e = launch_stepB3_tma_with(exact, *cur_map, *prv_map, p->tmaps[4], nxt, sp, p->tma_shape,
+                                               p->sched_counter, p->sched_base, p->d_err, s);
+        p->sched_base += (unsigned long long)p->tma_shape.items + p->tma_shape.grid;
+        if (e != cudaSuccess) {
+            set_error("TMA step launch failed: %s", cudaGetErrorString(e));
+            return AWE_ERR_CUDA;
+        }
+    } else {
+        launch_stepB(d.ndim, p->nop, exact, p->den != nullptr, cur, nxt, p->vel, p->den, sp, s);
+    }
+    prof_end(p, s);
+    launches++;
+    if (p->ns > 0) {
+        launch_injectB_off(d.ndim, exact, nxt, p->vel, p->src, p->ns, d_wav, it, ncs, ncs == 1, p->corner_off, s);
+        launches++;
+    }
+    if (d.dabc) {
+        AbcB abc{p->abc[0], p->abc[1], p->abc[2], p->abc[3], p->abc[4], p->abc[5]};
+        if (d.hybrid) {
+            launch_hybridB(d.ndim, p->nop, p->nbd, exact, d.fsrf, nxt, cur, abc, p->damp, g, s);
+            launches += d.ndim;
+        } else {
+            if (d.ndim == 3) {
+                launch_abconeB(3, p->nop, exact, d.fsrf, nxt, cur, abc, g, s);
+                launches += 3;
+            }
+            if (sponge && p->sponge_deferred) {
+                launch_band_sponge(d.ndim, std::max(p->nbd, shell), exact, nxt, p->w[0], p->w[1], p->w[2], g, s);
+                launches += d.ndim;  // one kernel per slab orientation
+            } else if (shell > 0) {
+                launch_band_sponge(d.ndim, shell, exact, nxt, p->w[0], p->w[1], p->w[2], g, s);
+                launches += d.ndim;
+            }
+        }
+    }
+    return AWE_OK;
+}
+
+awe_status planB_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, float *d_wfl, cudaStream_t s) {
+    return planB_run_hooked(p, d_wav, ncs, d_dat, d_wfl, s, nullptr);
+}
+
+awe_status planB_run_hooked(awe_plan *p, const float *d_wav, int ncs, float *d_dat, float *d_wfl, cudaStream_t s,
+                            const StepHook *hook) {
+    const awe_desc &d = p->d;
+    const Grid &g = p->g;
+    const bool exact = d.precision == AWE_EXACT;
+    const bool sponge = d.dabc && !d.hybrid;
+    const size_t bytes = (size_t)g.cells() * sizeof(float);
+    long long launches = 0;
+
+    CUDA_TRY(cudaMemsetAsync(p->u[0], 0, bytes, s));
+    CUDA_TRY(cudaMemsetAsync(p->u[1], 0, bytes, s));
+    if (p->nsnap > 0 && !d_wfl && p->snap_cb && !p->d_snap_tmp)
+        AWE_TRY(dev_alloc(p, (void **)&p->d_snap_tmp, p->snap_elems * sizeof(float)));
+
+    const StepBParams sp = stepB_params(p);
     const float *pw1 = sponge ? p->w[0] : nullptr;
 
     float *cur = p->u[1], *nxt = p->u[0];
     int icur = 1;
     int row = 0, isnap = 0;
     for (int it = 0; it < d.nt; it++) {
-        prof_begin(p, s);
-        if (p->use_tma) {
-            cudaError_t e = launch_stepB3_tma(exact, p->tmaps, icur, nxt, sp, p->tma_shape, p->sched_counter,
-                                              p->sched_base, p->d_err, s);
-            p->sched_base += (unsigned long long)p->tma_shape.items + p->tma_shape.grid;
-            if (e != cudaSuccess) {
-                set_error("TMA step launch failed: %s", cudaGetErrorString(e));
-                return AWE_ERR_CUDA;
-            }
-        } else {
-            launch_stepB(d.ndim, p->nop, exact, p->den != nullptr, cur, nxt, p->vel, p->den, sp, s);
-        }
-        prof_end(p, s);
-        launches++;
-        if (p->ns > 0) {
-            launch_injectB_off(d.ndim, exact, nxt, p->vel, p->src, p->ns, d_wav, it, ncs, ncs == 1, p->corner_off,
-                               s);
-            launches++;
-        }
-        if (d.dabc) {
-            if (d.hybrid) {
-                launch_hybridB(d.ndim, p->nop, p->nbd, exact, d.fsrf, nxt, cur, abc, p->damp, g, s);
-                launches += d.ndim;
-            } else {
-                if (d.ndim == 3) {
-                    launch_abconeB(3, p->nop, exact, d.fsrf, nxt, cur, abc, g, s);
-                    launches += 3;
-                }
-                if (p->sponge_deferred) {
-                    launch_band_sponge(d.ndim, std::max(p->nbd, shell), exact, nxt, p->w[0], p->w[1], p->w[2], g,
-                                       s);
-                    launches += d.ndim;  // one kernel per slab orientation
-                } else if (shell > 0) {
-                    launch_band_sponge(d.ndim, shell, exact, nxt, p->w[0], p->w[1], p->w[2], g, s);
-                    launches += d.ndim;
-                }
-            }
-        }
+        if (hook) AWE_TRY((*hook)(it, nxt, cur, s));
+        AWE_TRY(stepB_full(p, sp, nxt, cur, nxt, it, d_wav, ncs, &p->tmaps[icur], &p->tmaps[2 + (1 - icur)], s,
+                           launches));
         std::swap(cur, nxt);  // nxt now holds the time level `it` (sponge pending)
         icur ^= 1;
         if (p->nsnap > 0 && it % d.jsnap == 0) {

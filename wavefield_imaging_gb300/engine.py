@@ -45,6 +45,12 @@ class Info(C.Structure):
                 ("snap_elems", C.c_size_t), ("device_bytes", C.c_size_t), ("step_kernel", C.c_int)]
 
 
+class GradOpts(C.Structure):
+    _fields_ = [("ckpt_every", C.c_int), ("ckpt_format", C.c_int)]
+
+
+CKPT_BF16, CKPT_FP32, CKPT_FP16 = 0, 1, 2
+
 SNAP_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_float), C.c_size_t)
 
 _lib = None
@@ -75,9 +81,12 @@ def lib():
         L.awe_last_launch_count.restype = C.c_longlong
         L.awe_profile_enable.argtypes = [vp, C.c_int]
         L.awe_profile_read.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
+        dp = C.POINTER(C.c_double)
+        L.awe_gradient.argtypes = [vp, fp, C.c_int, fp, C.POINTER(GradOpts), dp, dp, fp]
+        L.awe_gradient_device.argtypes = [vp, vp, C.c_int, vp, C.POINTER(GradOpts), vp, dp, vp, vp]
         for name in ("awe_plan_create", "awe_plan_destroy", "awe_plan_info", "awe_set_model", "awe_set_geometry",
                      "awe_forward", "awe_forward_device", "awe_set_snapshot_callback", "awe_synchronize",
-                     "awe_profile_enable", "awe_profile_read"):
+                     "awe_profile_enable", "awe_profile_read", "awe_gradient", "awe_gradient_device"):
             getattr(L, name).restype = C.c_int
         _lib = L
     return _lib
@@ -156,6 +165,31 @@ class Plan:
         wfl = np.zeros((self.nsnap, self.snap_elems), np.float32) if snapshots and self.nsnap else None
         _check(lib().awe_forward(self._h, _fp(wav), ncs, _fp(dat), _fp(wfl)))
         return (dat, wfl) if snapshots else dat
+
+    def gradient(self, wav, dobs, ckpt_every: int = 0, ckpt_format: int = CKPT_BF16, return_dsyn: bool = False):
+        """Misfit J = 0.5 ||d - dobs||^2 and dJ/dm (m = 1/v^2) on the model
+        grid (float64, model shape).  Returns (grad, J[, dsyn])."""
+        wav = np.ascontiguousarray(wav, np.float32)
+        ncs = 1 if wav.ndim == 1 else wav.shape[1]
+        dobs = np.ascontiguousarray(dobs, np.float32).reshape(self.nsmp, self.nr)
+        n = list(self.desc.n)[: self.desc.ndim]
+        grad = np.zeros(n[::-1], np.float64)
+        dsyn = np.zeros((self.nsmp, self.nr), np.float32) if return_dsyn else None
+        J = C.c_double()
+        opts = GradOpts(ckpt_every, ckpt_format)
+        _check(lib().awe_gradient(self._h, _fp(wav), ncs, _fp(dobs), C.byref(opts),
+                                  grad.ctypes.data_as(C.POINTER(C.c_double)), C.byref(J), _fp(dsyn)))
+        return (grad, J.value, dsyn) if return_dsyn else (grad, J.value)
+
+    def gradient_device(self, d_wav: int, ncs: int, d_dobs: int, d_grad: int, ckpt_every: int = 0,
+                        ckpt_format: int = CKPT_BF16, d_dsyn: int = 0, stream: int = 0) -> float:
+        """Device-pointer variant; returns J (the call synchronizes)."""
+        J = C.c_double()
+        opts = GradOpts(ckpt_every, ckpt_format)
+        _check(lib().awe_gradient_device(self._h, C.c_void_p(d_wav), ncs, C.c_void_p(d_dobs), C.byref(opts),
+                                         C.c_void_p(d_grad), C.byref(J), C.c_void_p(d_dsyn or None),
+                                         C.c_void_p(stream or None)))
+        return J.value
 
     def forward_device(self, d_wav: int, ncs: int, d_dat: int, d_wfl: int = 0, stream: int = 0):
         """Device-resident run: arguments are raw device pointers (ints)."""
