@@ -476,6 +476,122 @@ def run_grad(args):
     plan.close()
 
 
+BATCH_METRIC = "batched 2D forward shots/s (uneven windows, one graph-replayed launch per step)"
+
+
+def batch_survey(nshots=256, nxm=6000, nz=512, seed=5):
+    """The c1-style survey: a seeded layered model 6000 columns wide, shots
+    every 20 m (4 columns) along a straight track, each on its own window of
+    nx in [300, 700] columns centred on the source, 128 receivers centred on
+    the source at z = 50 m, source at z = 50 m."""
+    rng = np.random.default_rng(seed)
+    w3 = dict(n=(nz, nxm, 1), d=(5.0, 5.0, 5.0), seed=seed)
+    vel = layered_model_3d(w3)[0]  # [nxm][nz]
+    shots = []
+    first = nxm // 2 - 2 * nshots
+    for i in range(nshots):
+        xs = first + 4 * i
+        nx = int(rng.integers(300, 701))
+        x0 = max(0, min(nxm - nx, xs - nx // 2))
+        sou = np.array([[xs * 5.0, 50.0]], np.float32)
+        rec = np.stack([(xs - 64 + np.arange(128)) * 5.0, np.full(128, 50.0)], 1).astype(np.float32)
+        shots.append((x0, nx, sou, rec))
+    return vel, shots
+
+
+def run_batch(args):
+    """--workload batch2d: all shots in one batched, graph-replayed forward
+    (autotuned tiles) against the same shots run one by one through the
+    single-shot path (each a plain launch sequence of its own)."""
+    import torch
+
+    import wavefield_imaging_gb300 as awe
+
+    dist, rank, world, local = dist_init()
+    torch.cuda.set_device(local)
+    nt = 4000 if args.nt == 3000 else args.nt
+    nshots, nz = args.shots, 512
+    vel, shots = batch_survey(nshots=nshots, nz=nz)
+    nxm = vel.shape[0]
+    wav = ricker(nt, 0.005, 5.0)
+    desc = awe.make_desc(2, (nz, nxm), (5.0, 5.0), (0.0, 0.0), nt, 0.005, nb=40, fdorder=8, dabc=1, expl=1,
+                         precision=awe.FAST)
+    batch = awe.Batch(desc, shots, device=local)
+    batch.set_model(vel)
+    tile, grid = batch.tune(steps=20)
+    d_wav = torch.from_numpy(wav).cuda()
+    d_dat = torch.zeros(batch.info.total_samples, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.Stream()
+
+    def step():
+        batch.forward_device(d_wav.data_ptr(), d_dat.data_ptr(), stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(dist)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = allmax(dist, e0.elapsed_time(e1)) / args.steps
+    cells = batch.info.cells
+
+    # plain loop: one single-shot plan per shot, run one after the other
+    plans = []
+    for (x0, nx, sou, rec) in shots:
+        dsc = awe.make_desc(2, (nz, nx), (5.0, 5.0), (0.0, x0 * 5.0), nt, 0.005, nb=40, fdorder=8, dabc=1, expl=1,
+                            precision=awe.FAST)
+        p = awe.Plan(dsc, device=local)
+        p.set_model(vel[x0:x0 + nx])
+        p.set_geometry(sou, rec)
+        plans.append(p)
+    d_pd = [torch.zeros((p.nsmp, 128), dtype=torch.float32, device="cuda") for p in plans]
+    for p, dd in zip(plans[:4], d_pd):
+        p.forward_device(d_wav.data_ptr(), 1, dd.data_ptr(), 0, stream.cuda_stream)
+    torch.cuda.synchronize()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    plain_launches = 0
+    for p, dd in zip(plans, d_pd):
+        p.forward_device(d_wav.data_ptr(), 1, dd.data_ptr(), 0, stream.cuda_stream)
+        plain_launches += p.last_launch_count()
+    p1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = p0.elapsed_time(p1)
+    # the batch's traces against the plain runs
+    dat = d_dat.cpu().numpy()
+    worst, off = 0.0, 0
+    for p, dd in zip(plans, d_pd):
+        a = dat[off:off + dd.numel()]
+        b_ = dd.cpu().numpy().ravel()
+        worst = max(worst, float(np.linalg.norm(a - b_) / max(np.linalg.norm(b_), 1e-30)))
+        off += dd.numel()
+    for p in plans:
+        p.close()
+    if rank != 0:
+        return
+    out = {"metric": BATCH_METRIC, "value": nshots * world / (ms / 1e3), "unit": "shots/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+           "config": {"workload": "%d shots, 20 m apart, windows nx in [300, 700] x nz 512 of a 6000-column model, "
+                                  "8th order, nt=%d, nb=40, dabc=y, 128 receivers per shot" % (nshots, nt),
+                      "padded_cells": cells, "tile": list(tile), "grid": grid,
+                      "work_items_per_launch": batch.info.work_items},
+           "cell_updates_per_s": cells * nt / (ms / 1e3),
+           "achieved_GBps": 16.0 * cells * nt / (ms / 1e3) / 1e9,
+           "plain": {"ms": plain_ms, "shots_per_s": nshots / (plain_ms / 1e3), "launches": plain_launches},
+           "speedup_vs_plain": plain_ms / ms, "max_rel_l2_vs_plain": worst,
+           "gpu_launches": nt * args.steps, "clocks": clocks}
+    print(json.dumps(out))
+    batch.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -486,12 +602,16 @@ def main():
     ap.add_argument("--nt", type=int, default=3000, help="time steps (the workload is nt=3000)")
     ap.add_argument("--n", type=int, default=512, help="model edge (the workload is 512; smaller for profiling)")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
-    ap.add_argument("--workload", default="fwd3d", choices=["fwd3d", "grad3d", "grad2d"],
-                    help="fwd3d: the headline forward workload; grad3d/grad2d: misfit gradients")
+    ap.add_argument("--workload", default="fwd3d", choices=["fwd3d", "grad3d", "grad2d", "batch2d"],
+                    help="fwd3d: the headline forward workload; grad3d/grad2d: misfit gradients; "
+                         "batch2d: the batched 2D survey")
+    ap.add_argument("--shots", type=int, default=256, help="batch2d: number of shots")
     ap.add_argument("--ckpt", default="bf16", choices=["bf16", "fp16", "fp32"], help="checkpoint storage (grad*)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch2d":
+        run_batch(args)
     elif args.workload != "fwd3d":
         run_grad(args)
     else:

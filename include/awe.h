@@ -191,6 +191,47 @@ awe_status awe_gradient(awe_plan *plan, const float *wav, int ncs, const float *
 awe_status awe_gradient_device(awe_plan *plan, const float *d_wav, int ncs, const float *d_dobs,
                                const awe_grad_opts *opts, double *d_grad, double *misfit, float *d_dsyn, void *stream);
 
+/* ---- Batched 2D forward: many shots along a track, each on its own window
+ * of one model.  Replaces a loop of sfAWEFDcart2Dcpu runs over cropped
+ * windows (the per-shot recipes of byrne_awe.py); the scheme is the CPU
+ * programs' (AWE_SCHEME_CPU, AWE_FAST, no hybrid ABC, no snapshots).  All
+ * shots advance together: one launch per time step covers every shot's
+ * tiles and receivers, and the nt launches run as one captured CUDA graph.
+ * Traces are exactly what per-shot awe_forward runs on the same windows
+ * return, within FP32 rounding of the fused update. ---- */
+typedef struct {
+    int x0, nx;       /* window: model columns [x0, x0 + nx) of axis 2 */
+    int ns, nr;       /* points of this shot */
+    const float *sou; /* [ns][2] (x, z) in model coordinates */
+    const float *rec; /* [nr][2] */
+} awe_shot;
+
+typedef struct awe_batch awe_batch;
+
+typedef struct {
+    int nshots, nsmp;
+    long long total_samples; /* sum over shots of nsmp * nr */
+    long long cells;         /* padded cells of all shots */
+    int tile_z, tile_x, grid;
+    int work_items;           /* (shot, tile) + (shot, receiver block) items per launch */
+    int launches_per_forward; /* = nt */
+} awe_batch_info_t;
+
+/* desc: the whole model (n[0] = nz, n[1] = model columns), nb, fdorder,
+ * dabc, fsrf, jdata, nt, dt; nz + 2 nb must be a multiple of 4. */
+awe_status awe_batch_create(const awe_desc *desc, int nshots, const awe_shot *shots, int device, awe_batch **out);
+awe_status awe_batch_destroy(awe_batch *batch);
+/* vel: host [n2][n1], the whole model; each shot takes its window. */
+awe_status awe_batch_set_model(awe_batch *batch, const float *vel);
+/* wav: [nt], one wavelet for every source.  dat: the shots' traces one
+ * after the other, shot s as [nsmp][nr_s]. */
+awe_status awe_batch_forward(awe_batch *batch, const float *wav, float *dat);
+awe_status awe_batch_forward_device(awe_batch *batch, const float *d_wav, float *d_dat, void *stream);
+/* Autotuner: times `steps` time steps of every tile shape and grid size on
+ * the current model and keeps the fastest (the next forward recaptures). */
+awe_status awe_batch_tune(awe_batch *batch, int steps, int *tile_out, int *grid_out);
+awe_status awe_batch_info(const awe_batch *batch, awe_batch_info_t *info);
+
 /* 2D forward modelling without any device allocation.  No counterpart in
  * the reference (its programs cudaMalloc everything in main()).  For callers
  * that cannot call cudaMalloc - code inside a framework that owns the device

@@ -134,6 +134,35 @@ void launch_ckpt_load16(bool fp16, const void *q, long long n, const float *scal
 void launch_grad_fold(const double *G, const float *vel2, float dt, const Grid &g, int nb, const int *n, int nd,
                       double *out, cudaStream_t s);
 
+// ---- batched 2D forward (k_batch2d.cu) ----
+struct BatchShot {
+    long long off;      // first cell of the shot's padded grid in the concatenated fields
+    int n2;             // padded columns
+    int wx_off;         // first entry of its axis-2 sponge table
+    int ns, src0;       // sources: count, first index in the point table
+    int nr, rec0;       // receivers
+    long long dat_off;  // first sample of its traces [nsmp][nr]
+};
+struct BatchStep {
+    const float *cur;
+    float *nxt;
+    const float *vel;
+    const float *wz, *wx;  // sponge tables (axis 1 common, axis 2 per shot)
+    int sponge;
+    int n1;  // padded rows (axis 1), common
+    float c0, cz[kMaxNop + 1], cx[kMaxNop + 1];
+    const GeoPoint *src, *rec;
+    const float *wav;  // one wavelet, [nt]
+    int it;
+    float *dat;
+    int row;  // trace row written by this step, -1: none
+};
+constexpr int kBatchNumTiles = 4;
+constexpr int kBatchRecBlock = 128;  // receivers per receiver item (<= threads of every tile shape)
+extern const int kBatchTiles[kBatchNumTiles][2];
+void launch_batch2d(int nop, int tile, const BatchShot *shots, const int4 *items, int nitems, int grid,
+                    const BatchStep &p, cudaStream_t s);
+
 // ---- host-side math (bit-identical to the reference's float evaluation) ----
 void fd_coefficients(int nop, int ndim, const float *dd, int optfd, Coef &k);
 void sponge_weights(int nb, std::vector<float> &w);   // fdutil.c sponge_make

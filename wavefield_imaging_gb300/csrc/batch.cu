@@ -1,0 +1,433 @@
+// Host side of the batched 2D forward (awe_batch_*): many shots along a
+// track, each on its own window of one model (the c1-style survey of
+// byrne_awe.py, one sfAWEFDcart2Dcpu run per window), advanced together.
+//
+// All shots' padded fields live in three concatenated arrays; every time step
+// is one launch of k_batch2d over the flat (shot, tile) + (shot, receiver
+// block) item list; the nt launches are captured once into a CUDA graph and
+// replayed.  The autotuner times each tile shape and grid size on a few steps
+// and keeps the fastest.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "awe_internal.h"
+
+using namespace awe;
+
+struct awe_batch {
+    awe_desc d{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int nop = 4, nb = 0, n1 = 0;  // padded rows
+    Coef k{};
+    std::vector<awe_shot> shots_in;
+    std::vector<BatchShot> shots;
+    std::vector<float> h_wz, h_wx;
+    std::vector<int4> items;
+    int ntile_items = 0;
+    long long cells = 0, ndat = 0;
+    int nsmp = 0;
+    std::vector<void *> allocs;
+    float *u[2] = {nullptr, nullptr}, *vel = nullptr, *wz = nullptr, *wx = nullptr, *wav = nullptr, *dat = nullptr;
+    BatchShot *d_shots = nullptr;
+    int4 *d_items = nullptr;
+    GeoPoint *src = nullptr, *rec = nullptr;
+    bool model_set = false;
+    int tile = 0, grid = 0, sms = 1;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long launches = 0;
+};
+
+#define CUDA_TRY(expr)                                                                            \
+    do {                                                                                          \
+        cudaError_t e_ = (expr);                                                                  \
+        if (e_ != cudaSuccess) {                                                                  \
+            set_error("%s failed: %s (%s:%d)", #expr, cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return AWE_ERR_CUDA;                                                                  \
+        }                                                                                         \
+    } while (0)
+
+static awe_status balloc(awe_batch *b, void **p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+    if (e != cudaSuccess) {
+        set_error("cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+        return AWE_ERR_NOMEM;
+    }
+    b->allocs.push_back(*p);
+    return AWE_OK;
+}
+
+static void drop_graph(awe_batch *b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+}
+
+static void build_items(awe_batch *b) {
+    const int TZ = kBatchTiles[b->tile][0], TX = kBatchTiles[b->tile][1];
+    b->items.clear();
+    for (int s = 0; s < (int)b->shots.size(); s++)
+        for (int x0 = 0; x0 < b->shots[s].n2; x0 += TX)
+            for (int z0 = 0; z0 < b->n1; z0 += TZ) b->items.push_back(make_int4(s, z0, x0, 0));
+    b->ntile_items = (int)b->items.size();
+    for (int s = 0; s < (int)b->shots.size(); s++)
+        for (int r = 0; r < b->shots[s].nr; r += kBatchRecBlock) b->items.push_back(make_int4(s, r, 0, 1));
+}
+
+static awe_status upload_items(awe_batch *b) {
+    if (b->d_items) {
+        cudaFree(b->d_items);
+        b->allocs.erase(std::find(b->allocs.begin(), b->allocs.end(), (void *)b->d_items));
+        b->d_items = nullptr;
+    }
+    awe_status st = balloc(b, (void **)&b->d_items, b->items.size() * sizeof(int4));
+    if (st != AWE_OK) return st;
+    CUDA_TRY(cudaMemcpy(b->d_items, b->items.data(), b->items.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    return AWE_OK;
+}
+
+static BatchStep step_params(const awe_batch *b, int it) {
+    BatchStep p{};
+    // level it lives in u[it & 1] (cur); the new level overwrites u[(it + 1) & 1]
+    p.cur = b->u[it & 1];
+    p.nxt = b->u[(it + 1) & 1];
+    p.vel = b->vel;
+    p.wz = b->wz;
+    p.wx = b->wx;
+    p.sponge = b->d.dabc ? 1 : 0;
+    p.n1 = b->n1;
+    p.c0 = b->k.c0;
+    for (int i = 0; i <= kMaxNop; i++) {
+        p.cz[i] = b->k.c[0][i];
+        p.cx[i] = b->k.c[1][i];
+    }
+    p.src = b->src;
+    p.rec = b->rec;
+    p.wav = b->wav;
+    p.it = it;
+    p.dat = b->dat;
+    p.row = (it % b->d.jdata == 0) ? it / b->d.jdata : -1;
+    return p;
+}
+
+static void launch_range(awe_batch *b, int it0, int it1, cudaStream_t s) {
+    for (int it = it0; it < it1; it++) {
+        const BatchStep p = step_params(b, it);
+        launch_batch2d(b->nop, b->tile, b->d_shots, b->d_items, (int)b->items.size(), b->grid, p, s);
+    }
+}
+
+static awe_status run_all(awe_batch *b, cudaStream_t s) {
+    const size_t bytes = (size_t)b->cells * sizeof(float);
+    CUDA_TRY(cudaMemsetAsync(b->u[0], 0, bytes, s));
+    CUDA_TRY(cudaMemsetAsync(b->u[1], 0, bytes, s));
+    if (!b->exec) {
+        // capture the nt step launches once; replays reuse the same buffers
+        cudaStream_t cs;
+        CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            launch_range(b, 0, b->d.nt, cs);
+            e = cudaStreamEndCapture(cs, &b->graph);
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+        cudaStreamDestroy(cs);
+        if (e != cudaSuccess) {
+            drop_graph(b);
+            set_error("CUDA graph capture of the batched time loop failed: %s", cudaGetErrorString(e));
+            return AWE_ERR_CUDA;
+        }
+    }
+    CUDA_TRY(cudaGraphLaunch(b->exec, s));
+    b->launches = b->d.nt;
+    return AWE_OK;
+}
+
+extern "C" {
+
+awe_status awe_batch_create(const awe_desc *desc, int nshots, const awe_shot *shots, int device, awe_batch **out) {
+    if (!desc || !shots || !out || nshots <= 0) {
+        set_error("null descriptor, shots or output, or no shots");
+        return AWE_ERR_INVALID;
+    }
+    *out = nullptr;
+    const awe_desc &d = *desc;
+    if (d.scheme != AWE_SCHEME_CPU || d.coords != AWE_CART || d.ndim != 2) {
+        set_error("awe_batch: 2D cartesian, scheme AWE_SCHEME_CPU only");
+        return AWE_ERR_UNSUPPORTED;
+    }
+    if (d.hybrid || d.precision != AWE_FAST || d.jsnap > 0) {
+        set_error("awe_batch: no hybrid ABC, no snapshots, AWE_FAST only");
+        return AWE_ERR_UNSUPPORTED;
+    }
+    const int fdorder = d.fdorder ? d.fdorder : 4;
+    if (fdorder < 2 || fdorder > 16 || fdorder % 2 || d.nt < 1 || d.dt <= 0 || d.n[0] < 1 || d.n[1] < 1 ||
+        d.jdata < 1) {
+        set_error("awe_batch: bad descriptor (fdorder 2..16 even, nt >= 1, dt > 0, jdata >= 1)");
+        return AWE_ERR_INVALID;
+    }
+    for (int s = 0; s < nshots; s++) {
+        const awe_shot &sh = shots[s];
+        if (sh.x0 < 0 || sh.nx < 1 || sh.x0 + sh.nx > d.n[1] || sh.ns < 0 || sh.nr < 0 ||
+            (sh.ns > 0 && !sh.sou) || (sh.nr > 0 && !sh.rec)) {
+            set_error("awe_batch: shot %d: window [%d, %d) outside the model's %d columns or bad points", s, sh.x0,
+                      sh.x0 + sh.nx, d.n[1]);
+            return AWE_ERR_INVALID;
+        }
+    }
+    if (cudaSetDevice(device) != cudaSuccess) {
+        set_error("no CUDA device %d", device);
+        return AWE_ERR_NODEVICE;
+    }
+    awe_batch *b = new awe_batch();
+    b->d = d;
+    b->d.fdorder = fdorder;
+    b->device = device;
+    b->nop = fdorder / 2;
+    int nb = d.nb;
+    if (nb < b->nop) nb = b->nop;  // MAWEFDcart2Dcpu.c:211
+    b->nb = nb;
+    b->n1 = d.n[0] + 2 * nb;
+    if (b->n1 % 4) {
+        delete b;
+        set_error("awe_batch: nz + 2 nb must be a multiple of 4 (16-byte rows)");
+        return AWE_ERR_UNSUPPORTED;
+    }
+    float dd[3] = {d.d[0], d.d[1], 1.f};
+    fd_coefficients(b->nop, 2, dd, d.optfd, b->k);
+    cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, device);
+    b->grid = 4 * std::max(b->sms, 1);
+    b->shots_in.assign(shots, shots + nshots);
+    cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+
+    // layout: shot s occupies (nx_s + 2 nb) columns of n1 floats
+    std::vector<float> w;
+    if (d.dabc) sponge_weights(nb, w);
+    auto table = [&](int n) {
+        std::vector<float> t(n, 1.f);
+        if (d.dabc)
+            for (int i = 0; i < nb && i < n; i++) t[i] = t[n - 1 - i] = w[nb - i - 1];
+        return t;
+    };
+    b->h_wz = table(b->n1);
+    long long off = 0, doff = 0;
+    b->nsmp = (d.nt - 1) / d.jdata + 1;
+    std::vector<GeoPoint> hs, hr;
+    for (int s = 0; s < nshots; s++) {
+        const awe_shot &in = shots[s];
+        BatchShot sh{};
+        sh.off = off;
+        sh.n2 = in.nx + 2 * nb;
+        sh.wx_off = (int)b->h_wx.size();
+        std::vector<float> tx = table(sh.n2);
+        b->h_wx.insert(b->h_wx.end(), tx.begin(), tx.end());
+        // the window's padded origin (fdutil_init on the cropped axes)
+        const float oz = d.o[0] - nb * d.d[0], ox = d.o[1] + in.x0 * d.d[1] - nb * d.d[1];
+        FdmAxes f{oz, ox, 0.f, d.d[0], d.d[1], 1.f, b->n1, sh.n2, 1};
+        auto point = [&](const float *xz) {
+            Lint l = lint_make(2, xz[0], 0.f, xz[1], f);
+            GeoPoint g{};
+            g.base = (long long)l.jx * b->n1 + l.jz;
+            for (int c = 0; c < 4; c++) g.w[c] = l.w[c];
+            return g;
+        };
+        sh.ns = in.ns;
+        sh.src0 = (int)hs.size();
+        for (int i = 0; i < in.ns; i++) hs.push_back(point(in.sou + 2 * i));
+        sh.nr = in.nr;
+        sh.rec0 = (int)hr.size();
+        for (int i = 0; i < in.nr; i++) hr.push_back(point(in.rec + 2 * i));
+        sh.dat_off = doff;
+        doff += (long long)b->nsmp * in.nr;
+        off += (long long)sh.n2 * b->n1;
+        b->shots.push_back(sh);
+    }
+    b->cells = off;
+    b->ndat = doff;
+    awe_status st = AWE_OK;
+    const size_t cb = (size_t)off * sizeof(float);
+    for (void **p : {(void **)&b->u[0], (void **)&b->u[1], (void **)&b->vel})
+        if (st == AWE_OK) st = balloc(b, p, cb);
+    if (st == AWE_OK) st = balloc(b, (void **)&b->wz, b->h_wz.size() * sizeof(float));
+    if (st == AWE_OK) st = balloc(b, (void **)&b->wx, b->h_wx.size() * sizeof(float));
+    if (st == AWE_OK) st = balloc(b, (void **)&b->wav, (size_t)d.nt * sizeof(float));
+    if (st == AWE_OK) st = balloc(b, (void **)&b->dat, (size_t)std::max(doff, 1LL) * sizeof(float));
+    if (st == AWE_OK) st = balloc(b, (void **)&b->d_shots, b->shots.size() * sizeof(BatchShot));
+    if (st == AWE_OK) st = balloc(b, (void **)&b->src, std::max<size_t>(hs.size(), 1) * sizeof(GeoPoint));
+    if (st == AWE_OK) st = balloc(b, (void **)&b->rec, std::max<size_t>(hr.size(), 1) * sizeof(GeoPoint));
+    if (st == AWE_OK) {
+        cudaMemcpy(b->wz, b->h_wz.data(), b->h_wz.size() * sizeof(float), cudaMemcpyHostToDevice);
+        cudaMemcpy(b->wx, b->h_wx.data(), b->h_wx.size() * sizeof(float), cudaMemcpyHostToDevice);
+        cudaMemcpy(b->d_shots, b->shots.data(), b->shots.size() * sizeof(BatchShot), cudaMemcpyHostToDevice);
+        if (!hs.empty()) cudaMemcpy(b->src, hs.data(), hs.size() * sizeof(GeoPoint), cudaMemcpyHostToDevice);
+        if (!hr.empty()) cudaMemcpy(b->rec, hr.data(), hr.size() * sizeof(GeoPoint), cudaMemcpyHostToDevice);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            set_error("batch upload failed: %s", cudaGetErrorString(e));
+            st = AWE_ERR_CUDA;
+        }
+    }
+    if (st == AWE_OK) {
+        build_items(b);
+        st = upload_items(b);
+    }
+    if (st != AWE_OK) {
+        awe_batch_destroy(b);
+        return st;
+    }
+    *out = b;
+    return AWE_OK;
+}
+
+awe_status awe_batch_destroy(awe_batch *b) {
+    if (!b) return AWE_OK;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    drop_graph(b);
+    for (void *p : b->allocs) cudaFree(p);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return AWE_OK;
+}
+
+awe_status awe_batch_set_model(awe_batch *b, const float *vel) {
+    if (!b || !vel) {
+        set_error("null batch or model");
+        return AWE_ERR_INVALID;
+    }
+    CUDA_TRY(cudaSetDevice(b->device));
+    const awe_desc &d = b->d;
+    const int nz = d.n[0];
+    std::vector<float> all((size_t)b->cells);
+    const float dt2 = d.dt * d.dt;
+    for (size_t s = 0; s < b->shots.size(); s++) {
+        const awe_shot &in = b->shots_in[s];
+        const BatchShot &sh = b->shots[s];
+        // window, padded by edge replication (expand2d, fdutil.c:435-458), then v^2 dt^2
+        const int n[2] = {nz, in.nx};
+        expand_model(2, vel + (size_t)in.x0 * nz, all.data() + sh.off, b->nb, n);
+        float *v = all.data() + sh.off;
+        for (long long i = 0; i < (long long)sh.n2 * b->n1; i++) v[i] *= v[i] * dt2;  // MAWEFDcart2Dcpu.c:290
+        if (d.fsrf)
+            for (int x = 0; x < sh.n2; x++)
+                for (int z = 0; z < b->nb + 1 && z < b->n1; z++) v[(size_t)x * b->n1 + z] = 0.f;  // :292-295
+    }
+    CUDA_TRY(cudaMemcpy(b->vel, all.data(), all.size() * sizeof(float), cudaMemcpyHostToDevice));
+    b->model_set = true;
+    return AWE_OK;
+}
+
+awe_status awe_batch_forward_device(awe_batch *b, const float *d_wav, float *d_dat, void *stream) {
+    if (!b || !d_wav || !d_dat) {
+        set_error("null batch, wavelet or data pointer");
+        return AWE_ERR_INVALID;
+    }
+    if (!b->model_set) {
+        set_error("awe_batch_set_model must precede awe_batch_forward");
+        return AWE_ERR_STATE;
+    }
+    CUDA_TRY(cudaSetDevice(b->device));
+    cudaStream_t s = stream ? (cudaStream_t)stream : b->stream;
+    CUDA_TRY(cudaMemcpyAsync(b->wav, d_wav, (size_t)b->d.nt * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    awe_status st = run_all(b, s);
+    if (st != AWE_OK) return st;
+    CUDA_TRY(cudaMemcpyAsync(d_dat, b->dat, (size_t)b->ndat * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    return AWE_OK;
+}
+
+awe_status awe_batch_forward(awe_batch *b, const float *wav, float *dat) {
+    if (!b || !wav || !dat) {
+        set_error("null batch, wavelet or data pointer");
+        return AWE_ERR_INVALID;
+    }
+    if (!b->model_set) {
+        set_error("awe_batch_set_model must precede awe_batch_forward");
+        return AWE_ERR_STATE;
+    }
+    CUDA_TRY(cudaSetDevice(b->device));
+    CUDA_TRY(cudaMemcpyAsync(b->wav, wav, (size_t)b->d.nt * sizeof(float), cudaMemcpyHostToDevice, b->stream));
+    awe_status st = run_all(b, b->stream);
+    if (st != AWE_OK) return st;
+    CUDA_TRY(cudaMemcpyAsync(dat, b->dat, (size_t)b->ndat * sizeof(float), cudaMemcpyDeviceToHost, b->stream));
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    return AWE_OK;
+}
+
+awe_status awe_batch_tune(awe_batch *b, int steps, int *tile_out, int *grid_out) {
+    if (!b || steps < 1) {
+        set_error("null batch or steps < 1");
+        return AWE_ERR_INVALID;
+    }
+    if (!b->model_set) {
+        set_error("awe_batch_set_model must precede awe_batch_tune");
+        return AWE_ERR_STATE;
+    }
+    CUDA_TRY(cudaSetDevice(b->device));
+    steps = std::min(steps, b->d.nt);
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int best_tile = b->tile, best_grid = b->grid;
+    const size_t bytes = (size_t)b->cells * sizeof(float);
+    for (int t = 0; t < kBatchNumTiles; t++) {
+        b->tile = t;
+        build_items(b);
+        awe_status st = upload_items(b);
+        if (st != AWE_OK) return st;
+        for (int mult : {2, 4, 8, 16}) {
+            b->grid = mult * b->sms;
+            cudaMemsetAsync(b->u[0], 0, bytes, b->stream);
+            cudaMemsetAsync(b->u[1], 0, bytes, b->stream);
+            launch_range(b, 0, 1, b->stream);  // warm
+            cudaEventRecord(e0, b->stream);
+            launch_range(b, 0, steps, b->stream);
+            cudaEventRecord(e1, b->stream);
+            CUDA_TRY(cudaEventSynchronize(e1));
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best) {
+                best = ms;
+                best_tile = t;
+                best_grid = b->grid;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->tile = best_tile;
+    b->grid = best_grid;
+    build_items(b);
+    awe_status st = upload_items(b);
+    if (st != AWE_OK) return st;
+    drop_graph(b);  // recaptured with the chosen shape on the next forward
+    CUDA_TRY(cudaGetLastError());
+    if (tile_out) *tile_out = best_tile;
+    if (grid_out) *grid_out = best_grid;
+    return AWE_OK;
+}
+
+awe_status awe_batch_info(const awe_batch *b, awe_batch_info_t *info) {
+    if (!b || !info) {
+        set_error("null argument");
+        return AWE_ERR_INVALID;
+    }
+    info->nshots = (int)b->shots.size();
+    info->nsmp = b->nsmp;
+    info->total_samples = b->ndat;
+    info->cells = b->cells;
+    info->tile_z = kBatchTiles[b->tile][0];
+    info->tile_x = kBatchTiles[b->tile][1];
+    info->grid = b->grid;
+    info->work_items = (int)b->items.size();
+    info->launches_per_forward = b->d.nt;
+    return AWE_OK;
+}
+
+}  // extern "C"

@@ -45,6 +45,17 @@ class Info(C.Structure):
                 ("snap_elems", C.c_size_t), ("device_bytes", C.c_size_t), ("step_kernel", C.c_int)]
 
 
+class Shot(C.Structure):
+    _fields_ = [("x0", C.c_int), ("nx", C.c_int), ("ns", C.c_int), ("nr", C.c_int),
+                ("sou", C.POINTER(C.c_float)), ("rec", C.POINTER(C.c_float))]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("nshots", C.c_int), ("nsmp", C.c_int), ("total_samples", C.c_longlong), ("cells", C.c_longlong),
+                ("tile_z", C.c_int), ("tile_x", C.c_int), ("grid", C.c_int), ("work_items", C.c_int),
+                ("launches_per_forward", C.c_int)]
+
+
 class GradOpts(C.Structure):
     _fields_ = [("ckpt_every", C.c_int), ("ckpt_format", C.c_int)]
 
@@ -81,6 +92,16 @@ def lib():
         L.awe_last_launch_count.restype = C.c_longlong
         L.awe_profile_enable.argtypes = [vp, C.c_int]
         L.awe_profile_read.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
+        L.awe_batch_create.argtypes = [C.POINTER(Desc), C.c_int, C.POINTER(Shot), C.c_int, C.POINTER(vp)]
+        L.awe_batch_destroy.argtypes = [vp]
+        L.awe_batch_set_model.argtypes = [vp, fp]
+        L.awe_batch_forward.argtypes = [vp, fp, fp]
+        L.awe_batch_forward_device.argtypes = [vp, vp, vp, vp]
+        L.awe_batch_tune.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.awe_batch_info.argtypes = [vp, C.POINTER(BatchInfo)]
+        for name in ("awe_batch_create", "awe_batch_destroy", "awe_batch_set_model", "awe_batch_forward",
+                     "awe_batch_forward_device", "awe_batch_tune", "awe_batch_info"):
+            getattr(L, name).restype = C.c_int
         dp = C.POINTER(C.c_double)
         L.awe_gradient.argtypes = [vp, fp, C.c_int, fp, C.POINTER(GradOpts), dp, dp, fp]
         L.awe_gradient_device.argtypes = [vp, vp, C.c_int, vp, C.POINTER(GradOpts), vp, dp, vp, vp]
@@ -241,3 +262,73 @@ class Plan:
 
     def __exit__(self, *a):
         self.close()
+
+
+class Batch:
+    """Many 2D shots, each on its own window [x0, x0 + nx) of one model,
+    advanced together (awe_batch_*).  shots: list of (x0, nx, sou [ns][2],
+    rec [nr][2]) with points in model coordinates."""
+
+    def __init__(self, desc: Desc, shots, device: int = 0):
+        self._keep = []
+        arr = (Shot * len(shots))()
+        self.nr = []
+        for i, (x0, nx, sou, rec) in enumerate(shots):
+            sou = np.ascontiguousarray(sou, np.float32).reshape(-1, 2)
+            rec = np.ascontiguousarray(rec, np.float32).reshape(-1, 2)
+            self._keep += [sou, rec]
+            arr[i] = Shot(int(x0), int(nx), sou.shape[0], rec.shape[0], _fp(sou), _fp(rec))
+            self.nr.append(rec.shape[0])
+        self._h = C.c_void_p()
+        _check(lib().awe_batch_create(C.byref(desc), len(shots), arr, device, C.byref(self._h)))
+        self.desc = desc
+        self.info = self._info()
+
+    def _info(self):
+        info = BatchInfo()
+        _check(lib().awe_batch_info(self._h, C.byref(info)))
+        return info
+
+    def set_model(self, vel):
+        vel = np.ascontiguousarray(vel, np.float32)
+        _check(lib().awe_batch_set_model(self._h, _fp(vel)))
+
+    def forward(self, wav):
+        """Returns a list of per-shot traces [nsmp][nr_s]."""
+        wav = np.ascontiguousarray(wav, np.float32).reshape(-1)
+        dat = np.zeros(self.info.total_samples, np.float32)
+        _check(lib().awe_batch_forward(self._h, _fp(wav), _fp(dat)))
+        out, off = [], 0
+        for nr in self.nr:
+            n = self.info.nsmp * nr
+            out.append(dat[off:off + n].reshape(self.info.nsmp, nr))
+            off += n
+        return out
+
+    def forward_device(self, d_wav: int, d_dat: int, stream: int = 0):
+        _check(lib().awe_batch_forward_device(self._h, C.c_void_p(d_wav), C.c_void_p(d_dat),
+                                              C.c_void_p(stream or None)))
+
+    def tune(self, steps: int = 20):
+        t, g = C.c_int(), C.c_int()
+        _check(lib().awe_batch_tune(self._h, steps, C.byref(t), C.byref(g)))
+        self.info = self._info()
+        return (self.info.tile_z, self.info.tile_x), g.value
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().awe_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
