@@ -592,6 +592,85 @@ def run_batch(args):
     batch.close()
 
 
+def run_batch_grad(args):
+    """--workload batchgrad2d: misfit gradient of the whole survey in one
+    batched, checkpointed fwd + adjoint run, against the plain per-shot loop
+    (awe_gradient shot after shot on the same GPU).  Value: shot gradients/s."""
+    import torch
+
+    import wavefield_imaging_gb300 as awe
+
+    dist, rank, world, local = dist_init()
+    torch.cuda.set_device(local)
+    nt = 4000 if args.nt == 3000 else args.nt
+    nshots, nz = args.shots, 512
+    vtrue, shots = batch_survey(nshots=nshots, nz=nz)
+    v0 = smooth(vtrue, 100.0 / 5.0)
+    nxm = vtrue.shape[0]
+    wav = ricker(nt, 0.005, 5.0)
+    fmt = {"bf16": awe.CKPT_BF16, "fp16": awe.CKPT_FP16, "fp32": awe.CKPT_FP32}[args.ckpt]
+    desc = awe.make_desc(2, (nz, nxm), (5.0, 5.0), (0.0, 0.0), nt, 0.005, nb=40, fdorder=8, dabc=1, expl=1,
+                         precision=awe.FAST)
+    batch = awe.Batch(desc, shots, device=local)
+    batch.set_model(vtrue)
+    batch.tune(steps=20)
+    dobs = batch.forward(wav)
+    batch.set_model(v0)
+    for _ in range(args.warmup):
+        batch.gradient(wav, dobs, ckpt_format=fmt)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        gb, Jb = batch.gradient(wav, dobs, ckpt_format=fmt)
+    t1 = time.perf_counter()
+    clocks = sampler.stop()
+    batch_s = allmax(dist, (t1 - t0) / args.steps)
+    info = batch.info
+    batch.close()
+    # plain: one plan per shot, awe_gradient one shot after the other
+    plans = []
+    for (x0, nx, sou, rec) in shots:
+        dsc = awe.make_desc(2, (nz, nx), (5.0, 5.0), (0.0, x0 * 5.0), nt, 0.005, nb=40, fdorder=8, dabc=1, expl=1,
+                            precision=awe.FAST)
+        p = awe.Plan(dsc, device=local)
+        p.set_model(v0[x0:x0 + nx])
+        p.set_geometry(sou, rec)
+        plans.append(p)
+    gp = np.zeros_like(gb)
+    plans[0].gradient(wav, dobs[0], ckpt_format=fmt)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    Jp = 0.0
+    for (x0, nx, _, _), p, d in zip(shots, plans, dobs):
+        g, J = p.gradient(wav, d, ckpt_format=fmt)
+        gp[x0:x0 + nx] += g
+        Jp += J
+    t1 = time.perf_counter()
+    plain_s = t1 - t0
+    for p in plans:
+        p.close()
+    if rank != 0:
+        return
+    out = {"metric": "batched FWI gradients/s (2D survey, checkpointed fwd + adjoint)",
+           "value": nshots * world / batch_s, "unit": "shot gradients/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * batch_s, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "fp32 fields, fp64 sums", "data": "synthetic",
+           "config": {"workload": "%d shots, windows nx in [300, 700] x nz 512 of a 6000-column model, 8th order, "
+                                  "nt=%d, nb=40, dabc=y; start model = true model smoothed 100 m" % (nshots, nt),
+                      "checkpoint": args.ckpt, "padded_cells": info.cells,
+                      "tile": [info.tile_z, info.tile_x], "grid": info.grid,
+                      "timing": "host wall clock around the synchronous gradient call (inputs from host)"},
+           "plain": {"s": plain_s, "shot_gradients_per_s": nshots / plain_s},
+           "speedup_vs_plain": plain_s / batch_s,
+           "rel_l2_batch_vs_plain": float(np.linalg.norm(gb - gp) / max(np.linalg.norm(gp), 1e-300)),
+           "misfit": {"batch": Jb, "plain": Jp},
+           "cell_steps_per_s": info.cells * nt / batch_s, "clocks": clocks}
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -602,7 +681,7 @@ def main():
     ap.add_argument("--nt", type=int, default=3000, help="time steps (the workload is nt=3000)")
     ap.add_argument("--n", type=int, default=512, help="model edge (the workload is 512; smaller for profiling)")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
-    ap.add_argument("--workload", default="fwd3d", choices=["fwd3d", "grad3d", "grad2d", "batch2d"],
+    ap.add_argument("--workload", default="fwd3d", choices=["fwd3d", "grad3d", "grad2d", "batch2d", "batchgrad2d"],
                     help="fwd3d: the headline forward workload; grad3d/grad2d: misfit gradients; "
                          "batch2d: the batched 2D survey")
     ap.add_argument("--shots", type=int, default=256, help="batch2d: number of shots")
@@ -612,6 +691,8 @@ def main():
         run_reference(args)
     elif args.workload == "batch2d":
         run_batch(args)
+    elif args.workload == "batchgrad2d":
+        run_batch_grad(args)
     elif args.workload != "fwd3d":
         run_grad(args)
     else:

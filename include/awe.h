@@ -231,6 +231,13 @@ awe_status awe_batch_forward_device(awe_batch *batch, const float *d_wav, float 
  * the current model and keeps the fastest (the next forward recaptures). */
 awe_status awe_batch_tune(awe_batch *batch, int steps, int *tile_out, int *grid_out);
 awe_status awe_batch_info(const awe_batch *batch, awe_batch_info_t *info);
+/* Misfit gradient of the whole batch: J = 0.5 sum over shots and samples of
+ * (d - dobs)^2, dJ/dm (m = 1/v^2) on the whole model [n2][n1] (each shot's
+ * window contributes), with the checkpointing of awe_gradient per shot (one
+ * FP32 scale per shot and stored level).  dobs laid out as awe_batch_forward's
+ * traces. */
+awe_status awe_batch_gradient(awe_batch *batch, const float *wav, const float *dobs, const awe_grad_opts *opts,
+                              double *grad, double *misfit);
 
 /* 2D forward modelling without any device allocation.  No counterpart in
  * the reference (its programs cudaMalloc everything in main()).  For callers

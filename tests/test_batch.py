@@ -76,3 +76,38 @@ def test_batch_rejects_bad_windows_without_a_device():
     with pytest.raises(awe.AweError) as e:
         awe.Batch(desc3, shots[:1])
     assert e.value.status == 4
+
+
+@pytest.mark.gpu
+def test_batch_gradient_is_the_sum_of_per_shot_gradients():
+    """The batch's misfit gradient against the FP64 oracle of every shot on
+    its window, summed onto the model columns."""
+    import wavefield_imaging_gb300 as awe
+    from oracle import oracle
+
+    nz, nxm, nt = 60, 220, 200
+    vel, shots = _survey(nshots=4, nz=nz, nxm=nxm, seed=9)
+    rng = np.random.default_rng(4)
+    vtrue = (vel * (1 + 0.05 * rng.standard_normal(vel.shape))).astype(np.float32)
+    wav = ricker(nt, 0.005)
+    gsum = np.zeros(vel.shape, np.float64)
+    Jsum = 0.0
+    dobs = []
+    for (x0, nx, sou, rec) in shots:
+        par = dict(n=[nz, nx], d=[5.0, 5.0], o=[0.0, x0 * 5.0], nb=10, nt=nt, dt=0.005, fdorder=8, dabc=1, expl=1)
+        d, _ = oracle.cart_cpu(par, vtrue[x0:x0 + nx], wav, sou, rec)
+        dobs.append(d)
+        g, J, _ = oracle.misfit_gradient(par, vel[x0:x0 + nx], wav, sou, rec, d)
+        gsum[x0:x0 + nx] += g
+        Jsum += J
+    with awe.Batch(_desc(nz, nxm, nt), shots) as b:
+        b.set_model(vel)
+        g32, J32 = b.gradient(wav, dobs, ckpt_format=awe.CKPT_FP32)
+        g16, J16 = b.gradient(wav, dobs, ckpt_format=awe.CKPT_BF16)
+        b.tune(steps=5)
+        g32b, _ = b.gradient(wav, dobs, ckpt_format=awe.CKPT_FP32)
+    assert abs(J32 - Jsum) <= 1e-5 * Jsum
+    assert J16 == J32
+    assert rel_l2(g32, gsum) <= 1e-4
+    assert rel_l2(g32b, gsum) <= 1e-4  # another tile shape after tuning
+    assert rel_l2(g16, gsum) <= 3e-2

@@ -155,8 +155,38 @@ struct BatchStep {
     const float *wav;  // one wavelet, [nt]
     int it;
     float *dat;
-    int row;  // trace row written by this step, -1: none
+    int row;            // trace row written by this step, -1: none
+    const float *prv;   // previous level when stepping out of place (null: in place in nxt)
 };
+struct BatchRecCorner {
+    long long node;  // cell of the shot's padded grid
+    int r;           // receiver index within the shot
+    float w;         // interpolation weight
+};
+struct BatchAdj {
+    const float *X;  // nu_k
+    float *Y;        // nu_{k+1} in, mu_k out
+    const float *V;  // forward level V_k
+    const float *vel;
+    double *G;  // dJ/dvel2, per shot, padded grids
+    const float *wz, *wx;
+    int sponge, n1;
+    float c0, cz[kMaxNop + 1], cx[kMaxNop + 1];
+    const GeoPoint *src;
+    const float *wav;
+    int it;
+    const int *rc_start;  // per work item: receiver corners [rc_start[w], rc_start[w + 1])
+    const BatchRecCorner *rc;
+    const float *res;  // residuals, laid out as the traces
+    int row;           // residual row of this step, -1: none
+};
+void launch_batch2d_adj(int nop, int tile, const BatchShot *shots, const int4 *items, int nitems, int grid,
+                        const BatchAdj &p, cudaStream_t s);
+void launch_batch_ckpt(bool store, int fmt, const BatchShot *shots, int nshots, float *u, void *q, float *scales,
+                       int n1, long long cells, cudaStream_t s);
+void launch_residual_flat(const float *d, const float *dobs, float *r, long long n, double *part, cudaStream_t s);
+void launch_batch_grad_fold(const BatchShot *shots, const int2 *win, int nshots, const double *G, const float *vel2,
+                            float dt, int n1, int nb, int nz, int nxm, double *out, cudaStream_t s);
 constexpr int kBatchNumTiles = 4;
 constexpr int kBatchRecBlock = 128;  // receivers per receiver item (<= threads of every tile shape)
 extern const int kBatchTiles[kBatchNumTiles][2];

@@ -41,6 +41,16 @@ struct awe_batch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     long long launches = 0;
+    std::vector<GeoPoint> h_rec;
+    // misfit gradient state
+    int gT = 0, gseg = 0, gfmt = -1;
+    float *slots = nullptr, *gX = nullptr, *gY = nullptr, *res = nullptr, *scales = nullptr, *dobs = nullptr;
+    void *ckpt = nullptr;
+    double *G = nullptr, *part = nullptr, *grad = nullptr;
+    int *rc_start = nullptr;
+    BatchRecCorner *rc = nullptr;
+    int2 *win = nullptr;
+    int rc_tile = -1;
 };
 
 #define CUDA_TRY(expr)                                                                            \
@@ -250,6 +260,7 @@ awe_status awe_batch_create(const awe_desc *desc, int nshots, const awe_shot *sh
     }
     b->cells = off;
     b->ndat = doff;
+    b->h_rec = hr;
     awe_status st = AWE_OK;
     const size_t cb = (size_t)off * sizeof(float);
     for (void **p : {(void **)&b->u[0], (void **)&b->u[1], (void **)&b->vel})
@@ -410,6 +421,211 @@ awe_status awe_batch_tune(awe_batch *b, int steps, int *tile_out, int *grid_out)
     CUDA_TRY(cudaGetLastError());
     if (tile_out) *tile_out = best_tile;
     if (grid_out) *grid_out = best_grid;
+    return AWE_OK;
+}
+
+// per-tile lists of receiver corners (cells the adjoint injects residuals into)
+static awe_status build_rec_corners(awe_batch *b) {
+    const int TZ = kBatchTiles[b->tile][0], TX = kBatchTiles[b->tile][1];
+    std::vector<std::vector<BatchRecCorner>> per(b->ntile_items);
+    // tile item index of (shot, z0, x0): items are laid out shot by shot, x-major
+    std::vector<int> first(b->shots.size());
+    int acc = 0;
+    const int ntz = (b->n1 + TZ - 1) / TZ;
+    for (size_t s = 0; s < b->shots.size(); s++) {
+        first[s] = acc;
+        acc += ((b->shots[s].n2 + TX - 1) / TX) * ntz;
+    }
+    for (size_t s = 0; s < b->shots.size(); s++) {
+        const BatchShot &sh = b->shots[s];
+        for (int r = 0; r < sh.nr; r++) {
+            const GeoPoint &g = b->h_rec[sh.rec0 + r];
+            for (int c = 0; c < 4; c++) {
+                const long long node = g.base + (c & 1) + (c >> 1) * (long long)b->n1;
+                const int z = (int)(node % b->n1), x = (int)(node / b->n1);
+                if (x < 0 || x >= sh.n2) continue;
+                const int item = first[s] + (x / TX) * ntz + z / TZ;
+                per[item].push_back(BatchRecCorner{node, r, g.w[c]});
+            }
+        }
+    }
+    std::vector<int> start(b->items.size() + 1, 0);
+    std::vector<BatchRecCorner> all;
+    for (size_t w = 0; w < b->items.size(); w++) {
+        start[w] = (int)all.size();
+        if ((int)w < b->ntile_items) all.insert(all.end(), per[w].begin(), per[w].end());
+    }
+    start[b->items.size()] = (int)all.size();
+    for (void *q : {(void *)b->rc_start, (void *)b->rc}) {
+        if (!q) continue;
+        cudaFree(q);
+        b->allocs.erase(std::find(b->allocs.begin(), b->allocs.end(), q));
+    }
+    b->rc_start = nullptr;
+    b->rc = nullptr;
+    awe_status st = balloc(b, (void **)&b->rc_start, start.size() * sizeof(int));
+    if (st == AWE_OK) st = balloc(b, (void **)&b->rc, std::max<size_t>(all.size(), 1) * sizeof(BatchRecCorner));
+    if (st != AWE_OK) return st;
+    CUDA_TRY(cudaMemcpy(b->rc_start, start.data(), start.size() * sizeof(int), cudaMemcpyHostToDevice));
+    if (!all.empty())
+        CUDA_TRY(cudaMemcpy(b->rc, all.data(), all.size() * sizeof(BatchRecCorner), cudaMemcpyHostToDevice));
+    b->rc_tile = b->tile;
+    return AWE_OK;
+}
+
+static awe_status grad_alloc(awe_batch *b, int T, int fmt) {
+    if (b->gT == T && b->gfmt == fmt) return AWE_OK;
+    for (void *q : {(void *)b->slots, b->ckpt, (void *)b->scales}) {
+        if (!q) continue;
+        cudaFree(q);
+        b->allocs.erase(std::find(b->allocs.begin(), b->allocs.end(), q));
+    }
+    b->slots = nullptr;
+    b->ckpt = nullptr;
+    b->scales = nullptr;
+    const int nseg = (b->d.nt + T - 1) / T;
+    const size_t es = fmt == AWE_CKPT_FP32 ? 4 : 2;
+    awe_status st = balloc(b, (void **)&b->slots, (size_t)(T + 1) * b->cells * sizeof(float));
+    if (st == AWE_OK) st = balloc(b, &b->ckpt, (size_t)2 * nseg * b->cells * es);
+    if (st == AWE_OK) st = balloc(b, (void **)&b->scales, (size_t)2 * nseg * b->shots.size() * sizeof(float));
+    if (st != AWE_OK) return st;
+    if (!b->gX) {
+        const size_t cb = (size_t)b->cells * sizeof(float);
+        const size_t nd = (size_t)std::max(b->ndat, 1LL);
+        for (void **q : {(void **)&b->gX, (void **)&b->gY})
+            if (st == AWE_OK) st = balloc(b, q, cb);
+        if (st == AWE_OK) st = balloc(b, (void **)&b->G, (size_t)b->cells * sizeof(double));
+        if (st == AWE_OK) st = balloc(b, (void **)&b->res, nd * sizeof(float));
+        if (st == AWE_OK) st = balloc(b, (void **)&b->dobs, nd * sizeof(float));
+        if (st == AWE_OK) st = balloc(b, (void **)&b->part, ((nd + 1023) / 1024) * sizeof(double));
+        if (st == AWE_OK) st = balloc(b, (void **)&b->grad, (size_t)b->d.n[0] * b->d.n[1] * sizeof(double));
+        if (st == AWE_OK) st = balloc(b, (void **)&b->win, b->shots.size() * sizeof(int2));
+        if (st != AWE_OK) return st;
+        std::vector<int2> w(b->shots.size());
+        for (size_t s = 0; s < w.size(); s++) w[s] = make_int2(b->shots_in[s].x0, b->shots_in[s].nx);
+        CUDA_TRY(cudaMemcpy(b->win, w.data(), w.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    }
+    b->gT = T;
+    b->gfmt = fmt;
+    b->gseg = nseg;
+    return AWE_OK;
+}
+
+static BatchAdj adj_params(const awe_batch *b, int it, const float *V) {
+    BatchAdj p{};
+    p.V = V;
+    p.vel = b->vel;
+    p.G = b->G;
+    p.wz = b->wz;
+    p.wx = b->wx;
+    p.sponge = b->d.dabc ? 1 : 0;
+    p.n1 = b->n1;
+    p.c0 = b->k.c0;
+    for (int i = 0; i <= kMaxNop; i++) {
+        p.cz[i] = b->k.c[0][i];
+        p.cx[i] = b->k.c[1][i];
+    }
+    p.src = b->src;
+    p.wav = b->wav;
+    p.it = it;
+    p.rc_start = b->rc_start;
+    p.rc = b->rc;
+    p.res = b->res;
+    p.row = (it % b->d.jdata == 0) ? it / b->d.jdata : -1;
+    return p;
+}
+
+// the whole gradient as one launch sequence on stream s (capturable)
+static awe_status grad_sequence(awe_batch *b, cudaStream_t s) {
+    const long long cells = b->cells;
+    const size_t cb = (size_t)cells * sizeof(float);
+    const int T = b->gT, ns = (int)b->shots.size(), nitems = (int)b->items.size();
+    const size_t es = b->gfmt == AWE_CKPT_FP32 ? 4 : 2;
+    auto ck = [&](int idx) { return (void *)((char *)b->ckpt + (size_t)idx * cells * es); };
+    auto sc = [&](int idx) { return b->scales + (size_t)idx * ns; };
+    // forward with checkpoints of both levels at every segment start
+    CUDA_TRY(cudaMemsetAsync(b->u[0], 0, cb, s));
+    CUDA_TRY(cudaMemsetAsync(b->u[1], 0, cb, s));
+    for (int it = 0; it < b->d.nt; it++) {
+        BatchStep p = step_params(b, it);
+        if (it % T == 0) {
+            const int seg = it / T;
+            launch_batch_ckpt(true, b->gfmt, b->d_shots, ns, p.nxt, ck(2 * seg), sc(2 * seg), b->n1, cells, s);
+            launch_batch_ckpt(true, b->gfmt, b->d_shots, ns, (float *)p.cur, ck(2 * seg + 1), sc(2 * seg + 1), b->n1,
+                              cells, s);
+        }
+        launch_batch2d(b->nop, b->tile, b->d_shots, b->d_items, nitems, b->grid, p, s);
+    }
+    launch_residual_flat(b->dat, b->dobs, b->res, b->ndat, b->part, s);
+    // adjoint sweep, last segment first
+    CUDA_TRY(cudaMemsetAsync(b->gX, 0, cb, s));
+    CUDA_TRY(cudaMemsetAsync(b->gY, 0, cb, s));
+    CUDA_TRY(cudaMemsetAsync(b->G, 0, (size_t)cells * sizeof(double), s));
+    float *X = b->gX, *Y = b->gY;
+    for (int seg = b->gseg - 1; seg >= 0; seg--) {
+        const int k0 = seg * T, k1 = std::min(k0 + T, b->d.nt);
+        launch_batch_ckpt(false, b->gfmt, b->d_shots, ns, b->slots, ck(2 * seg), sc(2 * seg), b->n1, cells, s);
+        launch_batch_ckpt(false, b->gfmt, b->d_shots, ns, b->slots + cells, ck(2 * seg + 1), sc(2 * seg + 1), b->n1,
+                          cells, s);
+        for (int k = k0; k <= k1 - 2; k++) {
+            const int j = k - k0;
+            BatchStep p = step_params(b, k);
+            p.prv = b->slots + (size_t)j * cells;
+            p.cur = b->slots + (size_t)(j + 1) * cells;
+            p.nxt = b->slots + (size_t)(j + 2) * cells;
+            p.row = -1;
+            launch_batch2d(b->nop, b->tile, b->d_shots, b->d_items, b->ntile_items, b->grid, p, s);
+        }
+        for (int k = k1 - 1; k >= k0; k--) {
+            BatchAdj p = adj_params(b, k, b->slots + (size_t)(k - k0 + 1) * cells);
+            p.X = X;
+            p.Y = Y;
+            launch_batch2d_adj(b->nop, b->tile, b->d_shots, b->d_items, b->ntile_items, b->grid, p, s);
+            std::swap(X, Y);
+        }
+    }
+    launch_batch_grad_fold(b->d_shots, b->win, ns, b->G, b->vel, b->d.dt, b->n1, b->nb, b->d.n[0], b->d.n[1],
+                           b->grad, s);
+    return AWE_OK;
+}
+
+awe_status awe_batch_gradient(awe_batch *b, const float *wav, const float *dobs, const awe_grad_opts *opts,
+                              double *grad, double *misfit) {
+    if (!b || !wav || !dobs || !grad || !misfit) {
+        set_error("null batch, wavelet, data, gradient or misfit pointer");
+        return AWE_ERR_INVALID;
+    }
+    if (!b->model_set) {
+        set_error("awe_batch_set_model must precede awe_batch_gradient");
+        return AWE_ERR_STATE;
+    }
+    awe_grad_opts o{0, AWE_CKPT_BF16};
+    if (opts) o = *opts;
+    if (o.ckpt_format != AWE_CKPT_BF16 && o.ckpt_format != AWE_CKPT_FP32 && o.ckpt_format != AWE_CKPT_FP16) {
+        set_error("awe_batch_gradient: unknown checkpoint format %d", o.ckpt_format);
+        return AWE_ERR_INVALID;
+    }
+    CUDA_TRY(cudaSetDevice(b->device));
+    int T = o.ckpt_every > 0 ? o.ckpt_every : (int)std::ceil(std::sqrt((double)b->d.nt));
+    T = std::max(1, std::min(T, b->d.nt));
+    awe_status st = grad_alloc(b, T, o.ckpt_format);
+    if (st == AWE_OK && b->rc_tile != b->tile) st = build_rec_corners(b);
+    if (st != AWE_OK) return st;
+    cudaStream_t s = b->stream;
+    CUDA_TRY(cudaMemcpyAsync(b->wav, wav, (size_t)b->d.nt * sizeof(float), cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(b->dobs, dobs, (size_t)b->ndat * sizeof(float), cudaMemcpyHostToDevice, s));
+    st = grad_sequence(b, s);
+    if (st != AWE_OK) return st;
+    const size_t nparts = (size_t)((b->ndat + 1023) / 1024);
+    std::vector<double> parts(nparts);
+    if (nparts) CUDA_TRY(cudaMemcpyAsync(parts.data(), b->part, nparts * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaMemcpyAsync(grad, b->grad, (size_t)b->d.n[0] * b->d.n[1] * sizeof(double), cudaMemcpyDeviceToHost,
+                             s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    CUDA_TRY(cudaGetLastError());
+    double J = 0;
+    for (double v : parts) J += 0.5 * v;
+    *misfit = J;
     return AWE_OK;
 }
 

@@ -10,6 +10,8 @@
 // engine's single-shot path).  Receiver items gather R (W V_k) from the
 // current level, which this launch does not write.  Shots share nz, the
 // spacing, the sponge width and the time axis; they differ in nx and offset.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "awe_internal.h"
@@ -58,7 +60,8 @@ __global__ void __launch_bounds__(TZ / 4 * TX) k_batch2d(const BatchShot *__rest
             if (x >= n2 || zb >= n1) continue;
             const float *row = &tile[xi + NOP][0];  // column SH holds z0
             const long long gi = sh.off + (long long)x * n1 + zb;
-            float4 pv = *reinterpret_cast<const float4 *>(nxt + gi);  // previous level (in place)
+            // previous level: in place in nxt, or p.prv when stepping out of place
+            float4 pv = *reinterpret_cast<const float4 *>((p.prv ? p.prv : nxt) + gi);
             const float4 vv = *reinterpret_cast<const float4 *>(vel + gi);
             const float wx = p.wx[sh.wx_off + x];
             float o[4];
@@ -148,6 +151,275 @@ void launch_batch2d(int nop, int tile, const BatchShot *shots, const int4 *items
         default: break;
     }
 #undef TILES
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint step of the batch (2D, sponge, no one-way ABC: the 2D CPU-program
+// scheme applies none without the hybrid option).  Per tile item, with
+// X = nu_k, Y = nu_{k+1} (overwritten by mu_k = W lambda_k), V = V_k:
+//   lambda = 2 I nu + L(I vel2 nu) + W (1 - 2 I) nu_{k+1} + W R^T r_k
+//   dJ/dvel2 += I nu L(V_k) + nu wav w (source corners), FP64 per shot.
+// The halo tiles of g = I vel2 nu and of V_k are staged in shared memory; the
+// receiver corners of the tile come from a per-tile list, so each cell is
+// written by the one thread that owns it.
+template <int NOP, int TZ, int TX>
+__global__ void __launch_bounds__(TZ / 4 * TX) k_batch2d_adj(const BatchShot *__restrict__ shots,
+                                                             const int4 *__restrict__ items, int nitems,
+                                                             const BatchAdj p) {
+    constexpr int NT = TZ / 4 * TX;
+    constexpr int SH = (NOP + 3) / 4 * 4;
+    constexpr int HX = TX + 2 * NOP;
+    constexpr int HZP = TZ + 2 * SH;
+    __shared__ __align__(16) float gt[HX][HZP];
+    __shared__ __align__(16) float vt[HX][HZP];
+    const int tid = threadIdx.x;
+    const int zq = tid % (TZ / 4), xi = tid / (TZ / 4);
+    const int n1 = p.n1;
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const int4 it = items[w];
+        if (it.w != 0) continue;  // receiver items belong to the forward
+        const BatchShot sh = shots[it.x];
+        const int n2 = sh.n2, z0 = it.y, x0 = it.z;
+        const float *X = p.X + sh.off, *V = p.V + sh.off, *vel = p.vel + sh.off;
+        __syncthreads();
+        constexpr int CH = HZP / 4;
+        for (int e = tid; e < HX * CH; e += NT) {
+            const int r = e / CH, q = e % CH;
+            const int x = x0 - NOP + r, z = z0 - SH + 4 * q;
+            float4 g = make_float4(0.f, 0.f, 0.f, 0.f), v = g;
+            if (x >= 0 && x < n2 && z >= 0 && z < n1) {  // n1 % 4 == 0: whole chunk inside
+                const long long j = (long long)x * n1 + z;
+                const float4 xv = *reinterpret_cast<const float4 *>(X + j);
+                const float4 vv = *reinterpret_cast<const float4 *>(vel + j);
+                v = *reinterpret_cast<const float4 *>(V + j);
+                const bool xin = x >= NOP && x < n2 - NOP;
+                g.x = (xin && z >= NOP && z < n1 - NOP) ? vv.x * xv.x : 0.f;
+                g.y = (xin && z + 1 >= NOP && z + 1 < n1 - NOP) ? vv.y * xv.y : 0.f;
+                g.z = (xin && z + 2 >= NOP && z + 2 < n1 - NOP) ? vv.z * xv.z : 0.f;
+                g.w = (xin && z + 3 >= NOP && z + 3 < n1 - NOP) ? vv.w * xv.w : 0.f;
+            }
+            *reinterpret_cast<float4 *>(&gt[r][4 * q]) = g;
+            *reinterpret_cast<float4 *>(&vt[r][4 * q]) = v;
+        }
+        __syncthreads();
+        const int x = x0 + xi, zb = z0 + 4 * zq;
+        if (x >= n2 || zb >= n1) continue;
+        const long long gi = sh.off + (long long)x * n1 + zb;
+        const float4 nv4 = *reinterpret_cast<const float4 *>(p.X + gi);
+        const float4 yv4 = *reinterpret_cast<const float4 *>(p.Y + gi);
+        const float nu[4] = {nv4.x, nv4.y, nv4.z, nv4.w}, yv[4] = {yv4.x, yv4.y, yv4.z, yv4.w};
+        const float wx = p.sponge ? p.wx[sh.wx_off + x] : 1.f;
+        const bool xin = x >= NOP && x < n2 - NOP;
+        float mu[4], wc[4];
+        double gacc[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int z = zb + i, tz = SH + 4 * zq + i;
+            const bool in = xin && z >= NOP && z < n1 - NOP;
+            wc[i] = p.sponge ? p.wz[z] * wx : 1.f;
+            float lt = gt[xi + NOP][tz] * p.c0;
+#pragma unroll
+            for (int k = 1; k <= NOP; k++) {
+                lt = fmaf(gt[xi + NOP][tz - k] + gt[xi + NOP][tz + k], p.cz[k], lt);
+                lt = fmaf(gt[xi + NOP - k][tz] + gt[xi + NOP + k][tz], p.cx[k], lt);
+            }
+            const float lam = (in ? 2.f * nu[i] : 0.f) + lt + (in ? -wc[i] : wc[i]) * yv[i];
+            mu[i] = wc[i] * lam;
+            gacc[i] = 0.0;
+            if (in) {
+                float lv = vt[xi + NOP][tz] * p.c0;
+#pragma unroll
+                for (int k = 1; k <= NOP; k++) {
+                    lv = fmaf(vt[xi + NOP][tz - k] + vt[xi + NOP][tz + k], p.cz[k], lv);
+                    lv = fmaf(vt[xi + NOP - k][tz] + vt[xi + NOP + k][tz], p.cx[k], lv);
+                }
+                gacc[i] = (double)nu[i] * (double)lv;
+            }
+        }
+        const long long cell0 = (long long)x * n1 + zb;
+        // receiver residuals (W R^T r, then the W of mu): corners listed per tile
+        if (p.row >= 0) {
+            const int a = p.rc_start[w], b = p.rc_start[w + 1];
+            for (int e = a; e < b; e++) {
+                const BatchRecCorner rc = p.rc[e];
+                const long long d = rc.node - cell0;
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+                    if (d == i) {
+                        const float r = p.res[sh.dat_off + (long long)p.row * sh.nr + rc.r];
+                        mu[i] += wc[i] * (wc[i] * (rc.w * r));
+                    }
+            }
+        }
+        // source term of the gradient
+        if (sh.ns > 0) {
+            const float dd = p.wav[p.it];
+            for (int s = 0; s < sh.ns; s++) {
+                const GeoPoint gp = p.src[sh.src0 + s];
+#pragma unroll
+                for (int cc = 0; cc < 4; cc++) {
+                    const long long d = gp.base + (cc & 1) + (cc >> 1) * (long long)n1 - cell0;
+#pragma unroll
+                    for (int i = 0; i < 4; i++)
+                        if (d == i) gacc[i] += (double)nu[i] * (double)(dd * gp.w[cc]);
+                }
+            }
+        }
+        *reinterpret_cast<float4 *>(p.Y + gi) = make_float4(mu[0], mu[1], mu[2], mu[3]);
+        double *G = p.G + gi;
+        const double2 g01 = *reinterpret_cast<const double2 *>(G), g23 = *reinterpret_cast<const double2 *>(G + 2);
+        *reinterpret_cast<double2 *>(G) = make_double2(g01.x + gacc[0], g01.y + gacc[1]);
+        *reinterpret_cast<double2 *>(G + 2) = make_double2(g23.x + gacc[2], g23.y + gacc[3]);
+    }
+}
+
+template <int NOP, int TZ, int TX>
+static void launch_adj_t(const BatchShot *shots, const int4 *items, int nitems, int grid, const BatchAdj &p,
+                         cudaStream_t s) {
+    k_batch2d_adj<NOP, TZ, TX><<<grid, TZ / 4 * TX, 0, s>>>(shots, items, nitems, p);
+}
+
+void launch_batch2d_adj(int nop, int tile, const BatchShot *shots, const int4 *items, int nitems, int grid,
+                        const BatchAdj &p, cudaStream_t s) {
+#define TILES(N)                                                                     \
+    case N:                                                                          \
+        if (tile == 0) launch_adj_t<N, 64, 16>(shots, items, nitems, grid, p, s);      \
+        else if (tile == 1) launch_adj_t<N, 128, 8>(shots, items, nitems, grid, p, s); \
+        else if (tile == 2) launch_adj_t<N, 32, 32>(shots, items, nitems, grid, p, s); \
+        else launch_adj_t<N, 64, 8>(shots, items, nitems, grid, p, s);                \
+        break;
+    switch (nop) {
+        TILES(1) TILES(2) TILES(3) TILES(4) TILES(5) TILES(6) TILES(7) TILES(8)
+        default: break;
+    }
+#undef TILES
+}
+
+// ---------------------------------------------------------------------------
+// Checkpoints of the batch: one block per shot, one FP32 scale per shot and
+// level (the shot's max |v|), 16-bit values (BF16 or FP16) or FP32 copies.
+template <typename Q>
+__device__ __forceinline__ void q_store(Q *q, long long i, float v);
+template <>
+__device__ __forceinline__ void q_store<__nv_bfloat16>(__nv_bfloat16 *q, long long i, float v) {
+    q[i] = __float2bfloat16_rn(v);
+}
+template <>
+__device__ __forceinline__ void q_store<__half>(__half *q, long long i, float v) {
+    q[i] = __float2half_rn(v);
+}
+__device__ __forceinline__ float q_load(const __nv_bfloat16 *q, long long i) { return __bfloat162float(q[i]); }
+__device__ __forceinline__ float q_load(const __half *q, long long i) { return __half2float(q[i]); }
+
+template <typename Q>
+__global__ void k_batch_ckpt_store(const BatchShot *__restrict__ shots, const float *__restrict__ u, Q *q,
+                                   float *scales, int n1) {
+    const BatchShot sh = shots[blockIdx.x];
+    const long long n = (long long)sh.n2 * n1;
+    const float *a = u + sh.off;
+    __shared__ float red[32];
+    float m = 0.f;
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) m = fmaxf(m, fabsf(a[i]));
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = threadIdx.x < (blockDim.x + 31) / 32 ? red[threadIdx.x] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0) red[0] = m;
+    }
+    __syncthreads();
+    const float scale = red[0] > 0.f ? red[0] : 1.f, inv = 1.f / scale;
+    if (threadIdx.x == 0) scales[blockIdx.x] = scale;
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) q_store<Q>(q, sh.off + i, a[i] * inv);
+}
+
+template <typename Q>
+__global__ void k_batch_ckpt_load(const BatchShot *__restrict__ shots, const Q *__restrict__ q,
+                                  const float *__restrict__ scales, float *u, int n1) {
+    const BatchShot sh = shots[blockIdx.x];
+    const long long n = (long long)sh.n2 * n1;
+    const float sc = scales[blockIdx.x];
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) u[sh.off + i] = q_load(q, sh.off + i) * sc;
+}
+
+void launch_batch_ckpt(bool store, int fmt, const BatchShot *shots, int nshots, float *u, void *q, float *scales,
+                       int n1, long long cells, cudaStream_t s) {
+    if (fmt == AWE_CKPT_FP32) {
+        if (store) cudaMemcpyAsync(q, u, (size_t)cells * sizeof(float), cudaMemcpyDeviceToDevice, s);
+        else cudaMemcpyAsync(u, q, (size_t)cells * sizeof(float), cudaMemcpyDeviceToDevice, s);
+        return;
+    }
+    if (fmt == AWE_CKPT_FP16) {
+        if (store) k_batch_ckpt_store<__half><<<nshots, 512, 0, s>>>(shots, u, (__half *)q, scales, n1);
+        else k_batch_ckpt_load<__half><<<nshots, 512, 0, s>>>(shots, (const __half *)q, scales, u, n1);
+    } else {
+        if (store) k_batch_ckpt_store<__nv_bfloat16><<<nshots, 512, 0, s>>>(shots, u, (__nv_bfloat16 *)q, scales, n1);
+        else k_batch_ckpt_load<__nv_bfloat16><<<nshots, 512, 0, s>>>(shots, (const __nv_bfloat16 *)q, scales, u, n1);
+    }
+}
+
+// residuals r = d - dobs over the concatenated traces; FP64 partial sums of
+// r^2 per block of 1024 samples (summed in order on the host)
+__global__ void k_residual_flat(const float *__restrict__ d, const float *__restrict__ dobs, float *__restrict__ r,
+                                long long n, double *__restrict__ part) {
+    __shared__ double red[256];
+    const long long b0 = (long long)blockIdx.x * 1024;
+    double acc = 0;
+    for (int j = threadIdx.x; j < 1024; j += 256) {
+        const long long i = b0 + j;
+        if (i < n) {
+            const float v = d[i] - dobs[i];
+            r[i] = v;
+            acc += (double)v * (double)v;
+        }
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+void launch_residual_flat(const float *d, const float *dobs, float *r, long long n, double *part, cudaStream_t s) {
+    const int blocks = (int)((n + 1023) / 1024);
+    if (blocks > 0) k_residual_flat<<<blocks, 256, 0, s>>>(d, dobs, r, n, part);
+}
+
+// model gradient: dJ/dvel2 * (-vel2^2 / dt^2), each shot's padded cells summed
+// onto the model cells they replicate (window columns x0 .. x0 + nx - 1)
+__global__ void k_batch_grad_fold(const BatchShot *__restrict__ shots, const int2 *__restrict__ win, int nshots,
+                                  const double *__restrict__ G, const float *__restrict__ vel2, double inv_dt2,
+                                  int n1, int nb, int nz, int nxm, double *__restrict__ out) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nz * nxm) return;
+    const int z = (int)(t % nz), xm = (int)(t / nz);
+    const int za = z == 0 ? 0 : z + nb, zbnd = z == nz - 1 ? n1 - 1 : z + nb;
+    double acc = 0;
+    for (int s = 0; s < nshots; s++) {
+        const int x0 = win[s].x, nx = win[s].y;
+        const int j = xm - x0;
+        if (j < 0 || j >= nx) continue;
+        const BatchShot sh = shots[s];
+        const int xa = j == 0 ? 0 : j + nb, xb = j == nx - 1 ? sh.n2 - 1 : j + nb;
+        for (int ix = xa; ix <= xb; ix++)
+            for (int iz = za; iz <= zbnd; iz++) {
+                const long long i = sh.off + (long long)ix * n1 + iz;
+                const double v2 = vel2[i];
+                acc += G[i] * (-v2 * v2 * inv_dt2);
+            }
+    }
+    out[t] = acc;
+}
+
+void launch_batch_grad_fold(const BatchShot *shots, const int2 *win, int nshots, const double *G, const float *vel2,
+                            float dt, int n1, int nb, int nz, int nxm, double *out, cudaStream_t s) {
+    const long long n = (long long)nz * nxm;
+    k_batch_grad_fold<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(shots, win, nshots, G, vel2,
+                                                                  1.0 / ((double)dt * (double)dt), n1, nb, nz, nxm,
+                                                                  out);
 }
 
 }  // namespace awe

@@ -99,8 +99,10 @@ def lib():
         L.awe_batch_forward_device.argtypes = [vp, vp, vp, vp]
         L.awe_batch_tune.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.awe_batch_info.argtypes = [vp, C.POINTER(BatchInfo)]
+        L.awe_batch_gradient.argtypes = [vp, fp, fp, C.POINTER(GradOpts), C.POINTER(C.c_double),
+                                         C.POINTER(C.c_double)]
         for name in ("awe_batch_create", "awe_batch_destroy", "awe_batch_set_model", "awe_batch_forward",
-                     "awe_batch_forward_device", "awe_batch_tune", "awe_batch_info"):
+                     "awe_batch_forward_device", "awe_batch_tune", "awe_batch_info", "awe_batch_gradient"):
             getattr(L, name).restype = C.c_int
         dp = C.POINTER(C.c_double)
         L.awe_gradient.argtypes = [vp, fp, C.c_int, fp, C.POINTER(GradOpts), dp, dp, fp]
@@ -308,6 +310,20 @@ class Batch:
     def forward_device(self, d_wav: int, d_dat: int, stream: int = 0):
         _check(lib().awe_batch_forward_device(self._h, C.c_void_p(d_wav), C.c_void_p(d_dat),
                                               C.c_void_p(stream or None)))
+
+    def gradient(self, wav, dobs, ckpt_every: int = 0, ckpt_format: int = CKPT_BF16):
+        """dobs: list of per-shot traces [nsmp][nr_s].  Returns (dJ/dm on the
+        whole model [n2][n1], float64; J)."""
+        wav = np.ascontiguousarray(wav, np.float32).reshape(-1)
+        flat = np.ascontiguousarray(np.concatenate([np.asarray(d, np.float32).ravel() for d in dobs]))
+        if flat.size != self.info.total_samples:
+            raise ValueError("dobs has %d samples, the batch %d" % (flat.size, self.info.total_samples))
+        grad = np.zeros((self.desc.n[1], self.desc.n[0]), np.float64)
+        J = C.c_double()
+        opts = GradOpts(ckpt_every, ckpt_format)
+        _check(lib().awe_batch_gradient(self._h, _fp(wav), _fp(flat), C.byref(opts),
+                                        grad.ctypes.data_as(C.POINTER(C.c_double)), C.byref(J)))
+        return grad, J.value
 
     def tune(self, steps: int = 20):
         t, g = C.c_int(), C.c_int()
