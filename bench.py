@@ -671,6 +671,93 @@ def run_batch_grad(args):
     print(json.dumps(out))
 
 
+def spher_workload(nt, nr=700, nang=512):
+    return dict(name="3D spherical shell (GPU-program scheme, metric terms), r in [3387.0, 3390.5] km at 5 m, "
+                     "theta and phi %d x 0.04/%d rad at the equator, nb=32, nt=%d, 1 source, 64x64 receivers"
+                     % (nang, nang, nt),
+                n=(nr, nang, nang), d=(0.005, 0.04 / nang, 0.04 / nang),
+                o=(3387.0, np.pi / 2 - 0.02, -0.02), nt=nt, dt=0.005, nb=32, f0=5.0, seed=11)
+
+
+def spher_model(w):
+    """Vacuum / ice (5 dust layers) / basalt as a function of depth below
+    r = 3389.5 km (surface at 200 m depth with 30 m random topography, basalt
+    below 1800 m), velocities in km/us.  Returns [nphi][ntheta][nr]."""
+    rng = np.random.default_rng(w["seed"])
+    nr, nth, nph = w["n"]
+    r = w["o"][0] + np.arange(nr) * w["d"][0]
+    depth = (3389.5 - r)[None, None, :]
+    topo = 0.2 + 0.03 * gaussian_field(rng, (nph, nth), 40.0)[:, :, None]
+    vel = np.full((nph, nth, nr), 0.168, np.float32)
+    for _ in range(5):
+        zd = rng.uniform(0.4, 1.6)
+        th = rng.uniform(0.010, 0.020)
+        vel[np.broadcast_to(np.abs(depth - (topo + zd - 0.2)) < 0.5 * th, vel.shape)] = 0.168 * rng.choice([0.95, 1.05])
+    vel[np.broadcast_to(depth < topo, vel.shape)] = 0.3
+    vel[np.broadcast_to(depth >= 1.8, vel.shape)] = 0.110
+    return vel
+
+
+def run_spher(args):
+    """--workload spher3d: one shot of the spherical-shell forward (scheme of
+    sfAWEFDspher3Dgpu) on the c4 grid."""
+    import torch
+
+    import wavefield_imaging_gb300 as awe
+
+    torch.cuda.set_device(0)
+    nt = args.nt
+    w = spher_workload(nt, nr=args.n + 188 if args.n != 512 else 700, nang=args.n)
+    vel = spher_model(w)
+    nr_, nth, nph = w["n"]
+    rs = 3389.5 - 0.2 + 0.05
+    th0, ph0 = w["o"][1] + 0.5 * (nth - 1) * w["d"][1], w["o"][2] + 0.5 * (nph - 1) * w["d"][2]
+    sou = np.array([[rs, ph0, th0]], np.float32)
+    gth = w["o"][1] + np.linspace(0.25, 0.75, 64) * (nth - 1) * w["d"][1]
+    gph = w["o"][2] + np.linspace(0.25, 0.75, 64) * (nph - 1) * w["d"][2]
+    P, T = np.meshgrid(gph, gth, indexing="ij")
+    rec = np.stack([np.full(P.size, rs), P.ravel(), T.ravel()], 1).astype(np.float32)
+    wav = ricker(nt, w["dt"], w["f0"])
+    desc = awe.make_desc(3, w["n"], w["d"], w["o"], nt, w["dt"], coords=awe.SPHER, scheme=awe.SCHEME_GPU,
+                         nb=w["nb"], expl=0, precision=awe.FAST)
+    plan = awe.Plan(desc)
+    plan.set_model(vel)
+    plan.set_geometry(sou, rec)
+    d_wav = torch.from_numpy(wav).cuda()
+    d_dat = torch.zeros((plan.nsmp, rec.shape[0]), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.Stream()
+    for _ in range(args.warmup):
+        plan.forward_device(d_wav.data_ptr(), 1, d_dat.data_ptr(), 0, stream.cuda_stream)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(0)
+    sampler.start()
+    plan.profile(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        plan.forward_device(d_wav.data_ptr(), 1, d_dat.data_ptr(), 0, stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    kern_ms, kern_n = plan.profile_read()
+    cells = int(np.prod([n + 2 * w["nb"] for n in w["n"]]))
+    peak, peak_kind = measured_peak()
+    avg = kern_ms / 1e3 / max(kern_n, 1)
+    out = {"metric": "cell-updates/s (3D spherical shell, GPU-program scheme)", "value": cells * nt / (ms / 1e3),
+           "unit": "cell-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+           "config": {"workload": w["name"], "padded_cells": cells},
+           "roofline": {"bound": "hbm", "kernel": "k_stepA<spherical>", "avg_launch_us": avg * 1e6,
+                        "achieved": BYTES_PER_CELL * cells / avg / 1e9, "peak": peak, "unit": "GB/s",
+                        "frac": BYTES_PER_CELL * cells / avg / 1e9 / peak, "peak_source": peak_kind,
+                        "kernel_share": kern_ms / args.steps / ms},
+           "gpu_launches": plan.last_launch_count() * args.steps, "clocks": clocks,
+           "trace_max_abs": float(d_dat.abs().max())}
+    print(json.dumps(out))
+    plan.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -681,7 +768,7 @@ def main():
     ap.add_argument("--nt", type=int, default=3000, help="time steps (the workload is nt=3000)")
     ap.add_argument("--n", type=int, default=512, help="model edge (the workload is 512; smaller for profiling)")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
-    ap.add_argument("--workload", default="fwd3d", choices=["fwd3d", "grad3d", "grad2d", "batch2d", "batchgrad2d"],
+    ap.add_argument("--workload", default="fwd3d", choices=["fwd3d", "grad3d", "grad2d", "batch2d", "batchgrad2d", "spher3d"],
                     help="fwd3d: the headline forward workload; grad3d/grad2d: misfit gradients; "
                          "batch2d: the batched 2D survey")
     ap.add_argument("--shots", type=int, default=256, help="batch2d: number of shots")
@@ -693,6 +780,8 @@ def main():
         run_batch(args)
     elif args.workload == "batchgrad2d":
         run_batch_grad(args)
+    elif args.workload == "spher3d":
+        run_spher(args)
     elif args.workload != "fwd3d":
         run_grad(args)
     else:

@@ -95,6 +95,7 @@ struct StepAParams {
     int shell, shell_axes;  // boundary shell width and the axes it spans (bit a = axis a+1)
     float dt2;
     float dd1, dd2, dd3, dd4, dd5;  // divisors of the Laplacian terms
+    float rd[5];                    // their reciprocals (AWE_FAST)
     float a0;                       // polar centre weight -2/dra^2
     const float *tr0, *tr1, *tr2, *tr3;  // per-radius tables
     const float *tt0, *tt1;              // per-(theta, r) tables (spherical)
@@ -223,9 +224,17 @@ Step3Launch stepB3_tma_shape(const Grid &g, int num_sms, int L);
 cudaError_t launch_stepB3_tma(bool exact, const CUtensorMap *maps, int icur, float *nxt, const StepBParams &sp,
                               const Step3Launch &sh, unsigned long long *counter, unsigned long long base, int *err,
                               cudaStream_t s);
+// lap_out (AWE_FAST only, may be null): also store L(cur) of interior cells
 cudaError_t launch_stepB3_tma_with(bool exact, const CUtensorMap &cur, const CUtensorMap &prv, const CUtensorMap &vel,
                                    float *nxt, const StepBParams &sp, const Step3Launch &sh,
-                                   unsigned long long *counter, unsigned long long base, int *err, cudaStream_t s);
+                                   unsigned long long *counter, unsigned long long base, int *err, cudaStream_t s,
+                                   float *lap_out);
+cudaError_t launch_stepB3_adj(const CUtensorMap &g_halo, const CUtensorMap &y_tile, const CUtensorMap &x_tile,
+                              float *Y, const float *lap_v, double *grad, const StepBParams &sp,
+                              const Step3Launch &sh, unsigned long long *counter, unsigned long long base, int *err,
+                              cudaStream_t s);
+// g = I vel2 nu (cells at least nop from every face), elementwise
+void launch_adj_g(const float *nu, const float *vel2, float *g, const Grid &gr, int nop, cudaStream_t s);
 bool make_tmap_3d(CUtensorMap *m, const float *base, int n1, int n2, int n3, int b1, int b2);
 // tensor-map boxes of the TMA step: the current level's halo box and the tile box
 void stepB3_tma_boxes(int *halo1, int *halo2, int *tile1, int *tile2);

@@ -102,6 +102,30 @@ void launch_adjB(const float *X, float *Y, const float *V, const float *vel, dou
     else adj_dispatch_nop<2>(p.nop, X, Y, V, vel, G, p, s);
 }
 
+// g = I vel2 nu, four cells per thread (n1 % 4 == 0)
+__global__ void k_adj_g(const float4 *__restrict__ nu, const float4 *__restrict__ vel2, float4 *__restrict__ g, Grid gr,
+                        int nop) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long n4 = (long long)gr.n1 * gr.n2 * gr.n3 / 4;
+    if (t >= n4) return;
+    const long long c = 4 * t;
+    const int i1 = (int)(c % gr.n1), i2 = (int)((c / gr.n1) % gr.n2), i3 = (int)(c / ((long long)gr.n1 * gr.n2));
+    const bool rest = i2 >= nop && i2 < gr.n2 - nop && (gr.n3 == 1 || (i3 >= nop && i3 < gr.n3 - nop));
+    const float4 a = nu[t], v = vel2[t];
+    float4 o;
+    o.x = (rest && i1 >= nop && i1 < gr.n1 - nop) ? v.x * a.x : 0.f;
+    o.y = (rest && i1 + 1 >= nop && i1 + 1 < gr.n1 - nop) ? v.y * a.y : 0.f;
+    o.z = (rest && i1 + 2 >= nop && i1 + 2 < gr.n1 - nop) ? v.z * a.z : 0.f;
+    o.w = (rest && i1 + 3 >= nop && i1 + 3 < gr.n1 - nop) ? v.w * a.w : 0.f;
+    g[t] = o;
+}
+
+void launch_adj_g(const float *nu, const float *vel2, float *g, const Grid &gr, int nop, cudaStream_t s) {
+    const long long n4 = gr.cells() / 4;
+    k_adj_g<<<(unsigned)((n4 + 255) / 256), 256, 0, s>>>((const float4 *)nu, (const float4 *)vel2, (float4 *)g, gr,
+                                                         nop);
+}
+
 // ---------------------------------------------------------------------------
 // Transpose of abcone3d_apply (fdutil.c:2085-2177).  The forward runs three
 // passes (axis-1, axis-2, axis-3 faces); each updates, per line and outward,

@@ -26,43 +26,59 @@ __global__ void __launch_bounds__(TZ / 4 * TX) k_batch2d(const BatchShot *__rest
     constexpr int SH = (NOP + 3) / 4 * 4;  // halo width along axis 1, rounded to 16 bytes
     constexpr int HX = TX + 2 * NOP;
     constexpr int HZP = TZ + 2 * SH;  // row pitch (floats), keeps rows 16-byte aligned
+    constexpr int CH = HZP / 4;       // 16-byte chunks per halo row
+    constexpr int NCH = (HX * CH + NT - 1) / NT;
     __shared__ __align__(16) float tile[HX][HZP];
     const int tid = threadIdx.x;
     const int zq = tid % (TZ / 4), xi = tid / (TZ / 4);
-    const float *cur = p.cur, *vel = p.vel;
-    float *nxt = p.nxt;
+    const int n1 = p.n1;
+    const float *prvb = p.prv ? p.prv : p.nxt;  // previous level: in place, or out of place
+    // registers of the next tile item: its halo chunks and this thread's
+    // previous-level and v^2 dt^2 strips (loaded while the current item computes)
+    float4 hb[NCH], pb = make_float4(0.f, 0.f, 0.f, 0.f), vb = pb;
+    auto fetch = [&](int w2) {
+        const int4 it = items[w2];
+        if (it.w != 0) return;
+        const BatchShot sh = shots[it.x];
+        const float *c = p.cur + sh.off;
+#pragma unroll
+        for (int j = 0; j < NCH; j++) {
+            const int e = tid + j * NT;
+            const int r = e / CH, q = e % CH;
+            const int x = it.z - NOP + r, z = it.y - SH + 4 * q;
+            hb[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+            // n1 % 4 == 0 and z % 4 == 0: a chunk is wholly inside or outside
+            if (e < HX * CH && x >= 0 && x < sh.n2 && z >= 0 && z < n1)
+                hb[j] = *reinterpret_cast<const float4 *>(c + (long long)x * n1 + z);
+        }
+        const int x = it.z + xi, zb = it.y + 4 * zq;
+        if (x < sh.n2 && zb < n1) {
+            const long long gi = sh.off + (long long)x * n1 + zb;
+            pb = *reinterpret_cast<const float4 *>(prvb + gi);
+            vb = *reinterpret_cast<const float4 *>(p.vel + gi);
+        }
+    };
+    if (blockIdx.x < nitems) fetch(blockIdx.x);
     for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
         const int4 it = items[w];
         const BatchShot sh = shots[it.x];
-        const int n1 = p.n1, n2 = sh.n2;
+        const int n2 = sh.n2;
         if (it.w == 0) {
             // ---- tile item: it.y = z0, it.z = x0
             const int z0 = it.y, x0 = it.z;
-            const float *c = cur + sh.off;
             __syncthreads();  // the previous item's readers are done with `tile`
-            // halo tile rows x0-NOP .. x0+TX+NOP-1, columns z0-NOP .. (16-byte chunks)
-            constexpr int CH = HZP / 4;
-            for (int e = tid; e < HX * CH; e += NT) {
-                const int r = e / CH, q = e % CH;
-                const int x = x0 - NOP + r, z = z0 - SH + 4 * q;
-                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (x >= 0 && x < n2 && z >= 0 && z + 3 < n1)
-                    v = *reinterpret_cast<const float4 *>(c + (long long)x * n1 + z);
-                else if (x >= 0 && x < n2) {
-                    float *pv = &v.x;
-                    for (int j = 0; j < 4; j++)
-                        if (z + j >= 0 && z + j < n1) pv[j] = c[(long long)x * n1 + z + j];
-                }
-                *reinterpret_cast<float4 *>(&tile[r][4 * q]) = v;
+#pragma unroll
+            for (int j = 0; j < NCH; j++) {
+                const int e = tid + j * NT;
+                if (e < HX * CH) *reinterpret_cast<float4 *>(&tile[e / CH][4 * (e % CH)]) = hb[j];
             }
+            const float4 pv = pb, vv = vb;
             __syncthreads();
+            if (w + (int)gridDim.x < nitems) fetch(w + gridDim.x);
             const int x = x0 + xi, zb = z0 + 4 * zq;
             if (x >= n2 || zb >= n1) continue;
             const float *row = &tile[xi + NOP][0];  // column SH holds z0
             const long long gi = sh.off + (long long)x * n1 + zb;
-            // previous level: in place in nxt, or p.prv when stepping out of place
-            float4 pv = *reinterpret_cast<const float4 *>((p.prv ? p.prv : nxt) + gi);
-            const float4 vv = *reinterpret_cast<const float4 *>(vel + gi);
             const float wx = p.wx[sh.wx_off + x];
             float o[4];
             const float pr4[4] = {pv.x, pv.y, pv.z, pv.w}, v4[4] = {vv.x, vv.y, vv.z, vv.w};
@@ -105,13 +121,15 @@ __global__ void __launch_bounds__(TZ / 4 * TX) k_batch2d(const BatchShot *__rest
 #pragma unroll
                 for (int i = 0; i < 4; i++) o[i] = (o[i] * p.wz[zb + i]) * wx;
             }
-            *reinterpret_cast<float4 *>(nxt + gi) = make_float4(o[0], o[1], o[2], o[3]);
-        } else if (p.row >= 0) {
+            *reinterpret_cast<float4 *>(p.nxt + gi) = make_float4(o[0], o[1], o[2], o[3]);
+        } else {
+            if (w + (int)gridDim.x < nitems) fetch(w + gridDim.x);
+            if (p.row < 0) continue;
             // ---- receiver item: it.y = first receiver of the block
             const int r = it.y + tid;
             if (tid >= kBatchRecBlock || r >= sh.nr) continue;
             const GeoPoint gp = p.rec[sh.rec0 + r];
-            const float *c = cur + sh.off;
+            const float *c = p.cur + sh.off;
             float acc = 0.f;
 #pragma unroll
             for (int cc = 0; cc < 4; cc++) {
@@ -170,43 +188,69 @@ __global__ void __launch_bounds__(TZ / 4 * TX) k_batch2d_adj(const BatchShot *__
     constexpr int SH = (NOP + 3) / 4 * 4;
     constexpr int HX = TX + 2 * NOP;
     constexpr int HZP = TZ + 2 * SH;
+    constexpr int CH = HZP / 4;
+    constexpr int NCH = (HX * CH + NT - 1) / NT;
     __shared__ __align__(16) float gt[HX][HZP];
     __shared__ __align__(16) float vt[HX][HZP];
     const int tid = threadIdx.x;
     const int zq = tid % (TZ / 4), xi = tid / (TZ / 4);
     const int n1 = p.n1;
-    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
-        const int4 it = items[w];
-        if (it.w != 0) continue;  // receiver items belong to the forward
+    // registers of the next item: g = I vel2 nu and V_k halo chunks, nu and
+    // nu_{k+1} strips of this thread (loaded while the current item computes)
+    float4 gb[NCH], vb[NCH], nb4 = make_float4(0.f, 0.f, 0.f, 0.f), yb4 = nb4;
+    auto fetch = [&](int w2) {
+        const int4 it = items[w2];
+        if (it.w != 0) return;
         const BatchShot sh = shots[it.x];
-        const int n2 = sh.n2, z0 = it.y, x0 = it.z;
         const float *X = p.X + sh.off, *V = p.V + sh.off, *vel = p.vel + sh.off;
-        __syncthreads();
-        constexpr int CH = HZP / 4;
-        for (int e = tid; e < HX * CH; e += NT) {
+#pragma unroll
+        for (int j = 0; j < NCH; j++) {
+            const int e = tid + j * NT;
             const int r = e / CH, q = e % CH;
-            const int x = x0 - NOP + r, z = z0 - SH + 4 * q;
+            const int x = it.z - NOP + r, z = it.y - SH + 4 * q;
             float4 g = make_float4(0.f, 0.f, 0.f, 0.f), v = g;
-            if (x >= 0 && x < n2 && z >= 0 && z < n1) {  // n1 % 4 == 0: whole chunk inside
-                const long long j = (long long)x * n1 + z;
-                const float4 xv = *reinterpret_cast<const float4 *>(X + j);
-                const float4 vv = *reinterpret_cast<const float4 *>(vel + j);
-                v = *reinterpret_cast<const float4 *>(V + j);
-                const bool xin = x >= NOP && x < n2 - NOP;
+            if (e < HX * CH && x >= 0 && x < sh.n2 && z >= 0 && z < n1) {  // n1 % 4 == 0
+                const long long jj = (long long)x * n1 + z;
+                const float4 xv = *reinterpret_cast<const float4 *>(X + jj);
+                const float4 vv = *reinterpret_cast<const float4 *>(vel + jj);
+                v = *reinterpret_cast<const float4 *>(V + jj);
+                const bool xin = x >= NOP && x < sh.n2 - NOP;
                 g.x = (xin && z >= NOP && z < n1 - NOP) ? vv.x * xv.x : 0.f;
                 g.y = (xin && z + 1 >= NOP && z + 1 < n1 - NOP) ? vv.y * xv.y : 0.f;
                 g.z = (xin && z + 2 >= NOP && z + 2 < n1 - NOP) ? vv.z * xv.z : 0.f;
                 g.w = (xin && z + 3 >= NOP && z + 3 < n1 - NOP) ? vv.w * xv.w : 0.f;
             }
-            *reinterpret_cast<float4 *>(&gt[r][4 * q]) = g;
-            *reinterpret_cast<float4 *>(&vt[r][4 * q]) = v;
+            gb[j] = g;
+            vb[j] = v;
         }
+        const int x = it.z + xi, zb = it.y + 4 * zq;
+        if (x < sh.n2 && zb < n1) {
+            const long long gi = sh.off + (long long)x * n1 + zb;
+            nb4 = *reinterpret_cast<const float4 *>(p.X + gi);
+            yb4 = *reinterpret_cast<const float4 *>(p.Y + gi);
+        }
+    };
+    if (blockIdx.x < nitems) fetch(blockIdx.x);
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const int4 it = items[w];
+        if (it.w != 0) continue;  // receiver items belong to the forward
+        const BatchShot sh = shots[it.x];
+        const int n2 = sh.n2, z0 = it.y, x0 = it.z;
         __syncthreads();
+#pragma unroll
+        for (int j = 0; j < NCH; j++) {
+            const int e = tid + j * NT;
+            if (e < HX * CH) {
+                *reinterpret_cast<float4 *>(&gt[e / CH][4 * (e % CH)]) = gb[j];
+                *reinterpret_cast<float4 *>(&vt[e / CH][4 * (e % CH)]) = vb[j];
+            }
+        }
+        const float4 nv4 = nb4, yv4 = yb4;
+        __syncthreads();
+        if (w + (int)gridDim.x < nitems) fetch(w + gridDim.x);
         const int x = x0 + xi, zb = z0 + 4 * zq;
         if (x >= n2 || zb >= n1) continue;
         const long long gi = sh.off + (long long)x * n1 + zb;
-        const float4 nv4 = *reinterpret_cast<const float4 *>(p.X + gi);
-        const float4 yv4 = *reinterpret_cast<const float4 *>(p.Y + gi);
         const float nu[4] = {nv4.x, nv4.y, nv4.z, nv4.w}, yv[4] = {yv4.x, yv4.y, yv4.z, yv4.w};
         const float wx = p.sponge ? p.wx[sh.wx_off + x] : 1.f;
         const bool xin = x >= NOP && x < n2 - NOP;

@@ -84,15 +84,16 @@ __device__ __forceinline__ float laplacian(const float *__restrict__ A, long lon
     auto d2 = [&](float m, float pl) {   // (p[+1] - 2 p) + p[-1]
         return fadd<EXACT>(fsub<EXACT>(pl, u2), m);
     };
-    auto div = [&](float a, float b) { return EXACT ? __fdiv_rn(a, b) : a / b; };
+    // AWE_EXACT divides as the reference; AWE_FAST multiplies by the reciprocal
+    auto div = [&](float a, float b, float rb) { return EXACT ? __fdiv_rn(a, b) : a * rb; };
     if constexpr (GEOM == 0) {  // cart 2D (x = axis 2, z = axis 1): pxx + pzz
-        const float pxx = div(d2(A[i - s2], A[i + s2]), p.dd2);
-        const float pzz = div(d2(A[i - 1], A[i + 1]), p.dd1);
+        const float pxx = div(d2(A[i - s2], A[i + s2]), p.dd2, p.rd[1]);
+        const float pzz = div(d2(A[i - 1], A[i + 1]), p.dd1, p.rd[0]);
         return fadd<EXACT>(pxx, pzz);
     } else if constexpr (GEOM == 1) {  // cart 3D: (pxx + pyy) + pzz
-        const float pxx = div(d2(A[i - s2], A[i + s2]), p.dd2);
-        const float pyy = div(d2(A[i - s3], A[i + s3]), p.dd3);
-        const float pzz = div(d2(A[i - 1], A[i + 1]), p.dd1);
+        const float pxx = div(d2(A[i - s2], A[i + s2]), p.dd2, p.rd[1]);
+        const float pyy = div(d2(A[i - s3], A[i + s3]), p.dd3, p.rd[2]);
+        const float pzz = div(d2(A[i - 1], A[i + 1]), p.dd1, p.rd[0]);
         return fadd<EXACT>(fadd<EXACT>(pxx, pyy), pzz);
     } else if constexpr (GEOM == 2) {  // polar (r = axis 1, theta = axis 2)
         const int ir = c[0];
@@ -104,11 +105,11 @@ __device__ __forceinline__ float laplacian(const float *__restrict__ A, long lon
         return fadd<EXACT>(compra, compth);
     } else {  // spherical (r = axis 1, theta = axis 2, phi = axis 3)
         const int ir = c[0];
-        const float pra = div(fsub<EXACT>(A[i + 1], A[i - 1]), p.dd1);        // / (2 dra)
-        const float ppra = div(d2(A[i - 1], A[i + 1]), p.dd2);                  // / dra^2
-        const float pth = div(fsub<EXACT>(A[i + s2], A[i - s2]), p.dd3);      // / (2 dth)
-        const float ppth = div(d2(A[i - s2], A[i + s2]), p.dd4);                // / dth^2
-        const float ppph = div(d2(A[i - s3], A[i + s3]), p.dd5);                // / dph^2
+        const float pra = div(fsub<EXACT>(A[i + 1], A[i - 1]), p.dd1, p.rd[0]);    // / (2 dra)
+        const float ppra = div(d2(A[i - 1], A[i + 1]), p.dd2, p.rd[1]);              // / dra^2
+        const float pth = div(fsub<EXACT>(A[i + s2], A[i - s2]), p.dd3, p.rd[2]);  // / (2 dth)
+        const float ppth = div(d2(A[i - s2], A[i + s2]), p.dd4, p.rd[3]);            // / dth^2
+        const float ppph = div(d2(A[i - s3], A[i + s3]), p.dd5, p.rd[4]);            // / dph^2
         const long long t = (long long)c[1] * p.g.n1 + ir;
         const float A2 = __ldg(p.tr0 + ir), Cr = __ldg(p.tr1 + ir), B = __ldg(p.tt0 + t), D = __ldg(p.tt1 + t);
         float lap = fadd<EXACT>(fmul<EXACT>(A2, pra), ppra);
@@ -149,9 +150,69 @@ __global__ void __launch_bounds__(256) k_stepA(const float *__restrict__ cur, fl
     nxt[i] = f;
 }
 
+// Spherical step, AWE_FAST: each thread owns one (r, theta) column and marches
+// along phi through a chunk of planes.  The phi neighbours stay in registers,
+// the per-radius and per-(theta, r) metric tables are read once per column,
+// and the r / theta neighbours come through L1 from the lanes and warps that
+// load the same plane.  Same formula and operation order as k_stepA<3>,
+// with fused multiply-adds and reciprocal multiplies.
+constexpr int kSphChunk = 16;
+
+__global__ void __launch_bounds__(256) k_stepA_sph_march(const float *__restrict__ cur, float *__restrict__ nxt,
+                                                         const float *__restrict__ vel, const StepAParams p) {
+    const int i1 = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i2 = blockIdx.y * blockDim.y + threadIdx.y;
+    const Grid g = p.g;
+    if (i1 >= g.n1 || i2 >= g.n2) return;
+    const int n[3] = {g.n1, g.n2, g.n3};
+    const long long s2 = g.n1, s3 = (long long)g.n1 * g.n2;
+    const int p0 = blockIdx.z * kSphChunk, p1 = min(p0 + kSphChunk, g.n3);
+    const bool in12 = i1 >= 4 && i1 < g.n1 - 4 && i2 >= 4 && i2 < g.n2 - 4;
+    const long long t = (long long)i2 * g.n1 + i1;
+    const float A2 = __ldg(p.tr0 + i1), Cr = __ldg(p.tr1 + i1), B = __ldg(p.tt0 + t), D = __ldg(p.tt1 + t);
+    const long long base = (long long)i2 * s2 + i1;
+    float um = p0 > 0 ? cur[base + (p0 - 1) * s3] : 0.f;
+    float uc = cur[base + p0 * s3];
+    for (int i3 = p0; i3 < p1; i3++) {
+        const long long i = base + i3 * s3;
+        const float up = i3 + 1 < g.n3 ? cur[i + s3] : 0.f;
+        const int c[3] = {i1, i2, i3};
+        const int si = sponge_index(c, n, p);
+        const float q = damp_a<false>(nxt[i], si, p.dtab, p.ftab);
+        float lap = 0.f;
+        if (in12 && i3 >= 4 && i3 < g.n3 - 4) {
+            const float u2 = uc + uc;
+            const float rm = cur[i - 1], rp = cur[i + 1], tm = cur[i - s2], tp = cur[i + s2];
+            const float pra = (rp - rm) * p.rd[0];
+            const float ppra = ((rp - u2) + rm) * p.rd[1];
+            const float pth = (tp - tm) * p.rd[2];
+            const float ppth = ((tp - u2) + tm) * p.rd[3];
+            const float ppph = ((up - u2) + um) * p.rd[4];
+            lap = fmaf(A2, pra, ppra);
+            lap = fmaf(B, pth, lap);
+            lap = fmaf(Cr, ppth, lap);
+            lap = fmaf(D, ppph, lap);
+        }
+        const float v = __ldg(vel + i);
+        float f = fmaf(p.dt2 * (v * v), lap, uc + uc) - q;
+        if (!in_shell(c, n, p)) {
+            if (p.mask && masked(c, n, p)) f = 0.f;
+            f = damp_a<false>(f, si, p.dtab, p.ftab);
+        }
+        nxt[i] = f;
+        um = uc;
+        uc = up;
+    }
+}
+
 template <bool EXACT>
 static void step_geom(int geom, const float *cur, float *nxt, const float *vel, const StepAParams &p, cudaStream_t s) {
     dim3 block(64, 4, 1), grid((p.g.n1 + 63) / 64, (p.g.n2 + 3) / 4, p.g.n3);
+    if (!EXACT && geom == 3) {
+        dim3 mg((p.g.n1 + 63) / 64, (p.g.n2 + 3) / 4, (p.g.n3 + kSphChunk - 1) / kSphChunk);
+        k_stepA_sph_march<<<mg, block, 0, s>>>(cur, nxt, vel, p);
+        return;
+    }
     switch (geom) {
         case 0: k_stepA<0, EXACT><<<grid, block, 0, s>>>(cur, nxt, vel, p); break;
         case 1: k_stepA<1, EXACT><<<grid, block, 0, s>>>(cur, nxt, vel, p); break;

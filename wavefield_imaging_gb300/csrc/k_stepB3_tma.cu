@@ -52,6 +52,12 @@ struct Step3Params {
     unsigned long long base;
     int *err;
     float *nxt;
+    // MODE 1: L(cur) of interior cells (0 elsewhere) stored here, laid out as the field
+    float *lap_out;
+    // MODE 2 (adjoint step): cur = I vel2 nu, prv = nu_{k+1} (overwritten by
+    // mu = W lambda), vel = nu_k; lap_v = L(V_k); grad += I nu L(V_k) (FP64)
+    const float *lap_v;
+    double *grad;
 };
 
 template <bool EXACT>
@@ -59,7 +65,9 @@ __device__ __forceinline__ float damp3(float v, float a, float b, float c) {
     return fmul<EXACT>(fmul<EXACT>(fmul<EXACT>(v, a), b), c);
 }
 
-template <bool EXACT>
+// MODE 0: forward step; 1: forward step that also stores L(cur); 2: adjoint
+// step of the misfit gradient (the tile loads are the same, the epilogue differs)
+template <bool EXACT, int MODE>
 __global__ void __launch_bounds__(s3::NTHREADS, 2)
     k_stepB3_o8(const __grid_constant__ CUtensorMap tm_cur, const __grid_constant__ CUtensorMap tm_prv,
                 const __grid_constant__ CUtensorMap tm_vel, const Step3Params p) {
@@ -192,7 +200,31 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
                         // multiplies are identities and are skipped (CTA-uniform)
                         const bool undamped = tile_undamped && y >= p.ilo[2] && y < p.ihi[2];
                         float out[4];
-                        if (undamped) {
+                        if constexpr (MODE == 2) {
+                            // lambda = 2 I nu + L(I vel2 nu) + W (1 - 2 I) nu_{k+1}; out = W lambda
+                            const float wy = (!undamped && p.w3) ? __ldg(p.w3 + y) : 1.f;
+                            const long long gi = ((long long)y * p.n2 + x) * p.n1 + zg;
+                            float4 lv = make_float4(0.f, 0.f, 0.f, 0.f);
+                            if (col_ok && xin && yin) lv = *reinterpret_cast<const float4 *>(p.lap_v + gi);
+                            const float lv4[4] = {lv.x, lv.y, lv.z, lv.w};
+                            double gacc[4];
+#pragma unroll
+                            for (int i = 0; i < 4; i++) {
+                                const bool in = zin[i] && xin && yin;
+                                const float w = undamped ? 1.f : (wz[i] * wx) * wy;
+                                const float nu = vel4[i];
+                                const float lam = (in ? 2.f * nu : 0.f) + lap[i] + (in ? -w : w) * prv4[i];
+                                out[i] = w * lam;
+                                gacc[i] = in ? (double)nu * (double)lv4[i] : 0.0;
+                            }
+                            if (col_ok && xin && yin) {
+                                double *G = p.grad + gi;
+                                const double2 a = *reinterpret_cast<const double2 *>(G);
+                                const double2 b = *reinterpret_cast<const double2 *>(G + 2);
+                                *reinterpret_cast<double2 *>(G) = make_double2(a.x + gacc[0], a.y + gacc[1]);
+                                *reinterpret_cast<double2 *>(G + 2) = make_double2(b.x + gacc[2], b.y + gacc[3]);
+                            }
+                        } else if (undamped) {
 #pragma unroll
                             for (int i = 0; i < 4; i++) {
                                 const float pr = prv4[i], u0 = zw[4 + i];
@@ -226,6 +258,15 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
                             }
                         }
                         if (col_ok) *reinterpret_cast<float4 *>(dst) = make_float4(out[0], out[1], out[2], out[3]);
+                        if constexpr (MODE == 1) {
+                            if (col_ok) {
+                                float lo[4];
+#pragma unroll
+                                for (int i = 0; i < 4; i++) lo[i] = (zin[i] && xin && yin) ? lap[i] : 0.f;
+                                *reinterpret_cast<float4 *>(p.lap_out + (dst - p.nxt)) =
+                                    make_float4(lo[0], lo[1], lo[2], lo[3]);
+                            }
+                        }
                         dst += plane;
                     }
                     if (__syncthreads_or(bad)) {
@@ -321,14 +362,11 @@ cudaError_t launch_stepB3_tma(bool exact, const CUtensorMap *maps, int icur, flo
                               const Step3Launch &sh, unsigned long long *counter, unsigned long long base, int *err,
                               cudaStream_t s) {
     return launch_stepB3_tma_with(exact, maps[icur], maps[2 + (1 - icur)], maps[4], nxt, sp, sh, counter, base, err,
-                                  s);
+                                  s, nullptr);
 }
 
-// one step with explicit maps: cur halo-box map, prv tile-box map (the buffer
-// the new level replaces, or another one when stepping out of place), vel
-cudaError_t launch_stepB3_tma_with(bool exact, const CUtensorMap &cur, const CUtensorMap &prv, const CUtensorMap &vel,
-                                   float *nxt, const StepBParams &sp, const Step3Launch &sh,
-                                   unsigned long long *counter, unsigned long long base, int *err, cudaStream_t s) {
+static Step3Params step3_params(const StepBParams &sp, const Step3Launch &sh, unsigned long long *counter,
+                                unsigned long long base, int *err, float *nxt) {
     Step3Params p{};
     p.n1 = sp.g.n1;
     p.n2 = sp.g.n2;
@@ -357,12 +395,67 @@ cudaError_t launch_stepB3_tma_with(bool exact, const CUtensorMap &cur, const CUt
     p.base = base;
     p.err = err;
     p.nxt = nxt;
+    return p;
+}
+
+// adjoint step (AWE_FAST): g_halo = halo-box map of I vel2 nu_k, y_tile = tile
+// map of nu_{k+1} (Y, overwritten by mu_k), x_tile = tile map of nu_k
+cudaError_t launch_stepB3_adj(const CUtensorMap &g_halo, const CUtensorMap &y_tile, const CUtensorMap &x_tile,
+                              float *Y, const float *lap_v, double *grad, const StepBParams &sp,
+                              const Step3Launch &sh, unsigned long long *counter, unsigned long long base, int *err,
+                              cudaStream_t s) {
+    Step3Params p = step3_params(sp, sh, counter, base, err, Y);
+    p.lap_v = lap_v;
+    p.grad = grad;
+    cudaFuncSetAttribute(k_stepB3_o8<false, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem);
+    k_stepB3_o8<false, 2><<<sh.grid, s3::NTHREADS, sh.smem, s>>>(g_halo, y_tile, x_tile, p);
+    return cudaGetLastError();
+}
+
+// one step with explicit maps: cur halo-box map, prv tile-box map (the buffer
+// the new level replaces, or another one when stepping out of place), vel
+cudaError_t launch_stepB3_tma_with(bool exact, const CUtensorMap &cur, const CUtensorMap &prv, const CUtensorMap &vel,
+                                   float *nxt, const StepBParams &sp, const Step3Launch &sh,
+                                   unsigned long long *counter, unsigned long long base, int *err, cudaStream_t s,
+                                   float *lap_out) {
+    Step3Params p{};
+    p.n1 = sp.g.n1;
+    p.n2 = sp.g.n2;
+    p.n3 = sp.g.n3;
+    p.c0 = sp.k.c0;
+    for (int k = 0; k <= 4; k++) {
+        p.cz[k] = sp.k.c[0][k];
+        p.cx[k] = sp.k.c[1][k];
+        p.cy[k] = sp.k.c[2][k];
+    }
+    p.w1 = sp.w1;
+    p.w2 = sp.w2;
+    p.w3 = sp.w3;
+    p.damp_prev = sp.damp_prev;
+    p.sponge_new = sp.sponge_new;
+    p.shell = sp.shell;
+    for (int a = 0; a < 3; a++) {
+        p.ilo[a] = sp.ilo[a];
+        p.ihi[a] = sp.ihi[a];
+    }
+    p.L = sh.L;
+    p.ntz = sh.ntz;
+    p.ntx = sh.ntx;
+    p.nchunks = sh.nchunks;
+    p.counter = counter;
+    p.base = base;
+    p.err = err;
+    p.nxt = nxt;
+    p.lap_out = lap_out;
     if (exact) {
-        cudaFuncSetAttribute(k_stepB3_o8<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem);
-        k_stepB3_o8<true><<<sh.grid, s3::NTHREADS, sh.smem, s>>>(cur, prv, vel, p);
+        cudaFuncSetAttribute(k_stepB3_o8<true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem);
+        k_stepB3_o8<true, 0><<<sh.grid, s3::NTHREADS, sh.smem, s>>>(cur, prv, vel, p);
+    } else if (lap_out) {
+        cudaFuncSetAttribute(k_stepB3_o8<false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem);
+        k_stepB3_o8<false, 1><<<sh.grid, s3::NTHREADS, sh.smem, s>>>(cur, prv, vel, p);
     } else {
-        cudaFuncSetAttribute(k_stepB3_o8<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem);
-        k_stepB3_o8<false><<<sh.grid, s3::NTHREADS, sh.smem, s>>>(cur, prv, vel, p);
+        cudaFuncSetAttribute(k_stepB3_o8<false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem);
+        k_stepB3_o8<false, 0><<<sh.grid, s3::NTHREADS, sh.smem, s>>>(cur, prv, vel, p);
     }
     return cudaGetLastError();
 }

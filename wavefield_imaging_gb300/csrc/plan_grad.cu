@@ -31,22 +31,28 @@ namespace awe {
 
 struct GradState {
     int T = 0, nseg = 0, fmt = -1;
-    float *slots = nullptr;  // (T + 1) levels
+    // generic path: (T + 1) segment levels V_k; TMA path: T slots of L(V_k)
+    float *slots = nullptr;
     void *ckpt = nullptr;    // 2 * nseg levels
-    float *scales = nullptr; // 2 * nseg (BF16)
+    float *scales = nullptr; // 2 * nseg (16-bit formats)
     unsigned int *amax = nullptr;
     float *X = nullptr, *Y = nullptr, *kap = nullptr;
     double *G = nullptr;
     float *dat = nullptr, *r = nullptr;
     double *row_sum = nullptr;
-    std::vector<CUtensorMap> halo_maps, tile_maps;  // per slot (TMA step kernel)
+    // TMA path (3D, 8th order): three rolling forward levels, I vel2 nu, and
+    // the tensor maps of every buffer the TMA kernels read
+    bool tma = false;
+    float *vr = nullptr, *gbuf = nullptr;
+    CUtensorMap vr_halo[3], vr_tile[3], g_halo, x_tile, y_tile;
 };
 
 void plan_gradient_free(awe_plan *p) {
     if (!p->grad) return;
     GradState *st = p->grad;
     for (void *ptr : {(void *)st->slots, st->ckpt, (void *)st->scales, (void *)st->amax, (void *)st->X, (void *)st->Y,
-                      (void *)st->kap, (void *)st->G, (void *)st->dat, (void *)st->r, (void *)st->row_sum})
+                      (void *)st->kap, (void *)st->G, (void *)st->dat, (void *)st->r, (void *)st->row_sum,
+                      (void *)st->vr, (void *)st->gbuf})
         if (ptr) dev_free(p, ptr);
     delete st;
     p->grad = nullptr;
@@ -63,7 +69,8 @@ static awe_status grad_alloc(awe_plan *p, int T, int fmt) {
     st->fmt = fmt;
     st->nseg = (d.nt + T - 1) / T;
     const size_t es = fmt == AWE_CKPT_FP32 ? 4 : 2;
-    AWE_TRY(dev_alloc(p, (void **)&st->slots, (size_t)(T + 1) * cells * sizeof(float)));
+    st->tma = p->use_tma && d.precision == AWE_FAST;
+    AWE_TRY(dev_alloc(p, (void **)&st->slots, (size_t)(st->tma ? T : T + 1) * cells * sizeof(float)));
     AWE_TRY(dev_alloc(p, &st->ckpt, (size_t)2 * st->nseg * cells * es));
     AWE_TRY(dev_alloc(p, (void **)&st->scales, (size_t)2 * st->nseg * sizeof(float)));
     AWE_TRY(dev_alloc(p, (void **)&st->amax, sizeof(unsigned int)));
@@ -75,19 +82,24 @@ static awe_status grad_alloc(awe_plan *p, int T, int fmt) {
     AWE_TRY(dev_alloc(p, (void **)&st->dat, nd * sizeof(float)));
     AWE_TRY(dev_alloc(p, (void **)&st->r, nd * sizeof(float)));
     AWE_TRY(dev_alloc(p, (void **)&st->row_sum, (size_t)p->nsmp * sizeof(double)));
-    if (p->use_tma) {
+    if (st->tma) {
+        AWE_TRY(dev_alloc(p, (void **)&st->vr, 3 * cells * sizeof(float)));
+        AWE_TRY(dev_alloc(p, (void **)&st->gbuf, cells * sizeof(float)));
         int h1, h2, t1, t2;
         stepB3_tma_boxes(&h1, &h2, &t1, &t2);
-        st->halo_maps.resize(T + 1);
-        st->tile_maps.resize(T + 1);
-        for (int j = 0; j <= T; j++) {
-            const float *base = st->slots + (size_t)j * cells;
-            if (!make_tmap_3d(&st->halo_maps[j], base, p->g.n1, p->g.n2, p->g.n3, h1, h2) ||
-                !make_tmap_3d(&st->tile_maps[j], base, p->g.n1, p->g.n2, p->g.n3, t1, t2)) {
-                st->halo_maps.clear();
-                st->tile_maps.clear();
-                break;
-            }
+        const Grid &g = p->g;
+        bool ok = true;
+        for (int j = 0; j < 3; j++) {
+            const float *b = st->vr + (size_t)j * cells;
+            ok = ok && make_tmap_3d(&st->vr_halo[j], b, g.n1, g.n2, g.n3, h1, h2) &&
+                 make_tmap_3d(&st->vr_tile[j], b, g.n1, g.n2, g.n3, t1, t2);
+        }
+        ok = ok && make_tmap_3d(&st->g_halo, st->gbuf, g.n1, g.n2, g.n3, h1, h2) &&
+             make_tmap_3d(&st->x_tile, st->X, g.n1, g.n2, g.n3, t1, t2) &&
+             make_tmap_3d(&st->y_tile, st->Y, g.n1, g.n2, g.n3, t1, t2);
+        if (!ok) {
+            set_error("awe_gradient: tensor map encoding failed");
+            return AWE_ERR_CUDA;
         }
     }
     return AWE_OK;
@@ -191,27 +203,52 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
     ap.w2 = sponge ? p->w[1] : nullptr;
     ap.w3 = sponge ? p->w[2] : nullptr;
     AbcB abc{p->abc[0], p->abc[1], p->abc[2], p->abc[3], p->abc[4], p->abc[5]};
-    const bool maps = !st->halo_maps.empty();
     float *X = st->X, *Y = st->Y;
+    const CUtensorMap *xmap = &st->x_tile, *ymap = &st->y_tile;
     for (int seg = st->nseg - 1; seg >= 0; seg--) {
         const int k0 = seg * T, k1 = std::min(k0 + T, d.nt);
         float *slot0 = st->slots;
-        AWE_TRY(ckpt_load(p, 2 * seg, slot0, s));
-        AWE_TRY(ckpt_load(p, 2 * seg + 1, slot0 + cells, s));
-        for (int k = k0; k <= k1 - 2; k++) {
-            const int j = k - k0;
-            float *A = slot0 + (size_t)j * cells, *B = A + cells, *N = B + cells;
-            AWE_TRY(stepB_full(p, sp, A, B, N, k, d_wav, ncs, maps ? &st->halo_maps[j + 1] : nullptr,
-                               maps ? &st->tile_maps[j] : nullptr, s, launches));
+        if (st->tma) {
+            // recompute with three rolling levels; the step kernel stores L(V_k) in slot k - k0
+            AWE_TRY(ckpt_load(p, 2 * seg, st->vr, s));
+            AWE_TRY(ckpt_load(p, 2 * seg + 1, st->vr + cells, s));
+            for (int k = k0; k < k1; k++) {
+                const int j = k - k0;
+                float *A = st->vr + (size_t)(j % 3) * cells, *B = st->vr + (size_t)((j + 1) % 3) * cells;
+                float *N = st->vr + (size_t)((j + 2) % 3) * cells;
+                AWE_TRY(stepB_full(p, sp, A, B, N, k, d_wav, ncs, &st->vr_halo[(j + 1) % 3], &st->vr_tile[j % 3], s,
+                                   launches, slot0 + (size_t)j * cells));
+            }
+        } else {
+            AWE_TRY(ckpt_load(p, 2 * seg, slot0, s));
+            AWE_TRY(ckpt_load(p, 2 * seg + 1, slot0 + cells, s));
+            for (int k = k0; k <= k1 - 2; k++) {
+                const int j = k - k0;
+                float *A = slot0 + (size_t)j * cells, *B = A + cells, *N = B + cells;
+                AWE_TRY(stepB_full(p, sp, A, B, N, k, d_wav, ncs, nullptr, nullptr, s, launches));
+            }
         }
         for (int k = k1 - 1; k >= k0; k--) {
-            const float *Vk = slot0 + (size_t)(k - k0 + 1) * cells;
             if (d.ndim == 3 && d.dabc) {
                 launch_abc_adjB(p->nop, d.fsrf, X, st->kap, abc, g, s);
                 launches += 3;
             }
-            launch_adjB(X, Y, Vk, p->vel, st->G, ap, s);
-            launches++;
+            if (st->tma) {
+                launch_adj_g(X, p->vel, st->gbuf, g, p->nop, s);
+                cudaError_t e = launch_stepB3_adj(st->g_halo, *ymap, *xmap, Y, slot0 + (size_t)(k - k0) * cells,
+                                                  st->G, sp, p->tma_shape, p->sched_counter, p->sched_base, p->d_err,
+                                                  s);
+                p->sched_base += (unsigned long long)p->tma_shape.items + p->tma_shape.grid;
+                if (e != cudaSuccess) {
+                    set_error("TMA adjoint launch failed: %s", cudaGetErrorString(e));
+                    return AWE_ERR_CUDA;
+                }
+                launches += 2;
+            } else {
+                const float *Vk = slot0 + (size_t)(k - k0 + 1) * cells;
+                launch_adjB(X, Y, Vk, p->vel, st->G, ap, s);
+                launches++;
+            }
             if (d.ndim == 3 && d.dabc) {
                 launch_kap_fold(Y, st->kap, ap, s);
                 launches++;
@@ -225,6 +262,7 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
                 launches++;
             }
             std::swap(X, Y);
+            std::swap(xmap, ymap);
         }
     }
     launch_grad_fold(st->G, p->vel, d.dt, g, p->nbd, d.n, d.ndim, d_grad, s);

@@ -101,9 +101,10 @@ typedef std::function<awe_status(int it, const float *prev, const float *cur, cu
 awe_status planB_run_hooked(awe_plan *p, const float *d_wav, int ncs, float *d_dat, float *d_wfl, cudaStream_t s,
                             const StepHook *hook);
 StepBParams stepB_params(const awe_plan *p);
+// lap_out: the TMA path also stores L(cur) of interior cells there (gradient recompute)
 awe_status stepB_full(awe_plan *p, const StepBParams &sp, const float *prv, const float *cur, float *nxt, int it,
                       const float *d_wav, int ncs, const CUtensorMap *cur_map, const CUtensorMap *prv_map,
-                      cudaStream_t s, long long &launches);
+                      cudaStream_t s, long long &launches, float *lap_out = nullptr);
 awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *d_dobs, const awe_grad_opts &o,
                          double *d_grad, double *misfit, float *d_dsyn, cudaStream_t s);
 void plan_gradient_free(awe_plan *p);

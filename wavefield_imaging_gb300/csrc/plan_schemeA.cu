@@ -169,6 +169,10 @@ awe_status planA_init(awe_plan *p) {
     AWE_TRY(dev_alloc(p, (void **)&p->corner_off, 8 * sizeof(long long)));
     if (pa.shell > 0) AWE_TRY(dev_alloc(p, (void **)&p->aux, cells * sizeof(float)));
 
+    // reciprocals of the Laplacian divisors (AWE_FAST multiplies; AWE_EXACT divides as the reference)
+    const float dvs[5] = {pa.dd1, pa.dd2, pa.dd3, pa.dd4, pa.dd5};
+    for (int j = 0; j < 5; j++) pa.rd[j] = dvs[j] != 0.f ? 1.f / dvs[j] : 0.f;
+
     // outputs: rows and snapshot windows as each program writes them
     const int jdata = d.jdata > 0 ? d.jdata : 1;
     p->nsmp = geom == 3 ? d.nt : d.nt / jdata;

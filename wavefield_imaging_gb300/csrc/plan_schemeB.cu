@@ -287,7 +287,7 @@ StepBParams stepB_params(const awe_plan *p) {
 // previous level, and for the TMA kernel `cur_map`/`prv_map` are given).
 awe_status stepB_full(awe_plan *p, const StepBParams &sp0, const float *prv, const float *cur, float *nxt, int it,
                       const float *d_wav, int ncs, const CUtensorMap *cur_map, const CUtensorMap *prv_map,
-                      cudaStream_t s, long long &launches) {
+                      cudaStream_t s, long long &launches, float *lap_out) {
     const awe_desc &d = p->d;
     const Grid &g = p->g;
     const bool exact = d.precision == AWE_EXACT;
@@ -298,7 +298,7 @@ awe_status stepB_full(awe_plan *p, const StepBParams &sp0, const float *prv, con
     prof_begin(p, s);
     if (p->use_tma && cur_map && prv_map) {
         cudaError_t e = launch_stepB3_tma_with(exact, *cur_map, *prv_map, p->tmaps[4], nxt, sp, p->tma_shape,
-                                               p->sched_counter, p->sched_base, p->d_err, s);
+                                               p->sched_counter, p->sched_base, p->d_err, s, lap_out);
         p->sched_base += (unsigned long long)p->tma_shape.items + p->tma_shape.grid;
         if (e != cudaSuccess) {
             set_error("TMA step launch failed: %s", cudaGetErrorString(e));
