@@ -61,12 +61,17 @@ struct AbcB {
     const float *xl, *xh;  // [n3][n1]
     const float *yl, *yh;  // [n2][n1]
 };
+// w1 != null (3D): lines at least `band` from the axis-2/3 faces also get the
+// sponge of their axis-1 ends in the axis-1 pass (when abc_zfused says the
+// fused form applies); launch_band_sponge(..., zfused = 1) then skips them
 void launch_abconeB(int ndim, int nop, bool exact, int fsrf, float *uo, const float *um, const AbcB &a,
-                    const Grid &g, cudaStream_t s);
+                    const Grid &g, cudaStream_t s, const float *w1 = nullptr, const float *w2 = nullptr,
+                    const float *w3 = nullptr, int band = 0);
+bool abc_zfused(int nop, const Grid &g, int band);
 void launch_hybridB(int ndim, int nop, int nbd, bool exact, int fsrf, float *uo, const float *um, const AbcB &a,
                     const float *damp, const Grid &g, cudaStream_t s);
 void launch_band_sponge(int ndim, int width, bool exact, float *u, const float *w1, const float *w2,
-                        const float *w3, const Grid &g, cudaStream_t s);
+                        const float *w3, const Grid &g, cudaStream_t s, int zfused = 0);
 
 // injection into the new level scaled by vel (v^2 dt^2): u += (dd*w)*vel.
 // off[c] = flat offset of corner c from the point's base index.

@@ -181,24 +181,47 @@ __global__ void k_abc_axis1(float *__restrict__ uo, const float *__restrict__ um
 // accesses: a face reads and writes inside the first (last) two float4 of
 // its line; the one sample of those float4s the face does not update is
 // stored back unchanged (no other thread of the launch touches the line).
+// With sponge tables given (w1 != null), lines at least `band` from the
+// axis-2 and axis-3 faces - which the later ABC passes neither read nor
+// write - also get the sponge of their axis-1 ends (the first and last
+// `band` <= 8 samples) here, as the band sponge would after the ABC.
+template <bool EXACT>
+__device__ __forceinline__ void damp_end(float4 &v, int i1, int lo, int hi, int i2, int i3, const float *w1,
+                                         const float *w2, const float *w3) {
+    float *e = &v.x;
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+        if (i1 + j >= lo && i1 + j < hi) e[j] = damp_cell<EXACT, 3>(e[j], i1 + j, i2, i3, w1, w2, w3);
+}
+
 template <bool EXACT>
 __global__ void k_abc_axis1_v4(float *__restrict__ uo, const float *__restrict__ um, const float *__restrict__ bl,
-                               const float *__restrict__ bh, Grid g, int top) {
+                               const float *__restrict__ bh, Grid g, int top, const float *__restrict__ w1,
+                               const float *__restrict__ w2, const float *__restrict__ w3, int band) {
     const int line = blockIdx.x * blockDim.x + threadIdx.x;
     if (line >= g.n2 * g.n3) return;
-    const int q = g.n1 / 4;
+    const int q = g.n1 / 4, i2 = line % g.n2, i3 = line / g.n2;
+    const bool sp = w1 && i2 >= band && i2 < g.n2 - band && i3 >= band && i3 < g.n3 - band;
     const float4 *m = reinterpret_cast<const float4 *>(um + (long long)line * g.n1);
     float4 *o = reinterpret_cast<float4 *>(uo + (long long)line * g.n1);
-    if (top) {  // iz = 4, 3, 2, 1 from uo[5]
-        const float l = bl[line];
-        const float4 ma = m[0], mb = m[1];
-        const float4 oa = o[0], ob = o[1];
-        const float u4 = abc_update<EXACT>(mb.y, mb.x, ob.y, l);
-        const float u3 = abc_update<EXACT>(mb.x, ma.w, u4, l);
-        const float u2 = abc_update<EXACT>(ma.w, ma.z, u3, l);
-        const float u1 = abc_update<EXACT>(ma.z, ma.y, u2, l);
-        o[0] = make_float4(oa.x, u1, u2, u3);
-        o[1] = make_float4(u4, ob.y, ob.z, ob.w);
+    if (top || sp) {  // iz = 4, 3, 2, 1 from uo[5]
+        float4 oa = o[0], ob = o[1];
+        if (top) {
+            const float l = bl[line];
+            const float4 ma = m[0], mb = m[1];
+            const float u4 = abc_update<EXACT>(mb.y, mb.x, ob.y, l);
+            const float u3 = abc_update<EXACT>(mb.x, ma.w, u4, l);
+            const float u2 = abc_update<EXACT>(ma.w, ma.z, u3, l);
+            const float u1 = abc_update<EXACT>(ma.z, ma.y, u2, l);
+            oa = make_float4(oa.x, u1, u2, u3);
+            ob = make_float4(u4, ob.y, ob.z, ob.w);
+        }
+        if (sp) {
+            damp_end<EXACT>(oa, 0, 0, band, i2, i3, w1, w2, w3);
+            damp_end<EXACT>(ob, 4, 0, band, i2, i3, w1, w2, w3);
+        }
+        o[0] = oa;
+        o[1] = ob;
     }
     {  // iz = n1-5 .. n1-2 from uo[n1-6]
         const float h = bh[line];
@@ -208,8 +231,13 @@ __global__ void k_abc_axis1_v4(float *__restrict__ uo, const float *__restrict__
         const float v4 = abc_update<EXACT>(ma.w, mb.x, v5, h);
         const float v3 = abc_update<EXACT>(mb.x, mb.y, v4, h);
         const float v2 = abc_update<EXACT>(mb.y, mb.z, v3, h);
-        o[q - 2] = make_float4(oa.x, oa.y, oa.z, v5);
-        o[q - 1] = make_float4(v4, v3, v2, ob.w);
+        float4 na = make_float4(oa.x, oa.y, oa.z, v5), nb = make_float4(v4, v3, v2, ob.w);
+        if (sp) {
+            damp_end<EXACT>(na, g.n1 - 8, g.n1 - band, g.n1, i2, i3, w1, w2, w3);
+            damp_end<EXACT>(nb, g.n1 - 4, g.n1 - band, g.n1, i2, i3, w1, w2, w3);
+        }
+        o[q - 2] = na;
+        o[q - 1] = nb;
     }
 }
 
@@ -246,13 +274,20 @@ __global__ void k_abc_axis3(float *uo, const float *__restrict__ um, const float
     }
 }
 
+bool abc_zfused(int nop, const Grid &g, int band) {
+    return nop == 4 && g.n1 % 4 == 0 && g.n1 >= 16 && band > 0 && band <= 8;
+}
+
 void launch_abconeB(int ndim, int nop, bool exact, int fsrf, float *uo, const float *um, const AbcB &a,
-                    const Grid &g, cudaStream_t s) {
+                    const Grid &g, cudaStream_t s, const float *w1, const float *w2, const float *w3, int band) {
     const int T = 128;
     long long n = (long long)g.n2 * g.n3;
     if (nop == 4 && g.n1 % 4 == 0 && g.n1 >= 16) {
-        if (exact) k_abc_axis1_v4<true><<<(n + T - 1) / T, T, 0, s>>>(uo, um, a.zl, a.zh, g, !fsrf);
-        else k_abc_axis1_v4<false><<<(n + T - 1) / T, T, 0, s>>>(uo, um, a.zl, a.zh, g, !fsrf);
+        if (!abc_zfused(nop, g, band)) w1 = nullptr;
+        if (exact)
+            k_abc_axis1_v4<true><<<(n + T - 1) / T, T, 0, s>>>(uo, um, a.zl, a.zh, g, !fsrf, w1, w2, w3, band);
+        else
+            k_abc_axis1_v4<false><<<(n + T - 1) / T, T, 0, s>>>(uo, um, a.zl, a.zh, g, !fsrf, w1, w2, w3, band);
     } else if (exact) {
         k_abc_axis1<true><<<(n + T - 1) / T, T, 0, s>>>(uo, um, a.zl, a.zh, g, nop, !fsrf);
     } else {
@@ -395,7 +430,7 @@ __device__ __forceinline__ void damp4(float4 &v, int i1, int lo, int hi, int i2,
 
 template <bool EXACT, int NDIM>
 __global__ void k_sponge_slab1_v4(float *u, const float *__restrict__ w1, const float *__restrict__ w2,
-                                  const float *__restrict__ w3, Grid g, int W) {
+                                  const float *__restrict__ w3, Grid g, int W, int zfused) {
     // per line: chunks [0, c) cover axis-1 cells [0, W), chunks [q - c, q) cover [n1 - W, n1)
     const int q = g.n1 / 4, c = (W + 3) / 4;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -403,6 +438,8 @@ __global__ void k_sponge_slab1_v4(float *u, const float *__restrict__ w1, const 
     const int line = (int)(t / (2 * c)), k = (int)(t - (long long)line * 2 * c);
     const int chunk = k < c ? k : q - 2 * c + k;
     const int i2 = line % g.n2, i3 = line / g.n2, i1 = 4 * chunk;
+    // lines away from the axis-2/3 bands were finished by the fused axis-1 ABC pass
+    if (zfused && i2 >= W && i2 < g.n2 - W && i3 >= W && i3 < g.n3 - W) return;
     float4 *p = reinterpret_cast<float4 *>(u + (long long)line * g.n1) + chunk;
     float4 v = *p;
     if (k < c) damp4<EXACT, NDIM>(v, i1, 0, W, i2, i3, w1, w2, w3);
@@ -436,12 +473,13 @@ __global__ void k_sponge_slab23_v4(float *u, const float *__restrict__ w1, const
 
 template <bool EXACT, int NDIM>
 static void band_sponge_t(int W, float *u, const float *w1, const float *w2, const float *w3, const Grid &g,
-                          cudaStream_t s) {
+                          cudaStream_t s, int zfused) {
     const int T = 128;
     if (g.n1 % 4 == 0 && g.n1 >= 2 * W + 8) {
         const int c = (W + 3) / 4;
         const long long n1tot = (long long)g.n2 * g.n3 * 2 * c;
-        k_sponge_slab1_v4<EXACT, NDIM><<<(unsigned)((n1tot + 255) / 256), 256, 0, s>>>(u, w1, w2, w3, g, W);
+        k_sponge_slab1_v4<EXACT, NDIM><<<(unsigned)((n1tot + 255) / 256), 256, 0, s>>>(u, w1, w2, w3, g, W,
+                                                                                       NDIM == 3 ? zfused : 0);
         const int nch = (g.n1 - W + 3) / 4 - W / 4;
         k_sponge_slab23_v4<EXACT, NDIM, 2><<<dim3((nch + 63) / 64, 2 * W, g.n3), 64, 0, s>>>(u, w1, w2, w3, g, W);
         if (NDIM == 3 && g.n2 - 2 * W > 0)
@@ -459,13 +497,13 @@ static void band_sponge_t(int W, float *u, const float *w1, const float *w2, con
 }
 
 void launch_band_sponge(int ndim, int width, bool exact, float *u, const float *w1, const float *w2, const float *w3,
-                        const Grid &g, cudaStream_t s) {
+                        const Grid &g, cudaStream_t s, int zfused) {
     if (ndim == 3) {
-        if (exact) band_sponge_t<true, 3>(width, u, w1, w2, w3, g, s);
-        else band_sponge_t<false, 3>(width, u, w1, w2, w3, g, s);
+        if (exact) band_sponge_t<true, 3>(width, u, w1, w2, w3, g, s, zfused);
+        else band_sponge_t<false, 3>(width, u, w1, w2, w3, g, s, zfused);
     } else {
-        if (exact) band_sponge_t<true, 2>(width, u, w1, w2, w3, g, s);
-        else band_sponge_t<false, 2>(width, u, w1, w2, w3, g, s);
+        if (exact) band_sponge_t<true, 2>(width, u, w1, w2, w3, g, s, 0);
+        else band_sponge_t<false, 2>(width, u, w1, w2, w3, g, s, 0);
     }
 }
 

@@ -135,6 +135,8 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
         if (p.w2 && x < p.n2) wx = __ldg(p.w2 + x);
         // the whole tile lies where the z and x sponge factors are exactly 1
         const bool tile_undamped = z0 >= p.ilo[0] && z0 + TZ <= p.ihi[0] && x0 >= p.ilo[1] && x0 + TX <= p.ihi[1];
+        // every column of the tile is at least NOPQ from the z and x faces
+        const bool tile_inner = z0 >= NOPQ && z0 + TZ <= p.n1 - NOPQ && x0 >= NOPQ && x0 + TX <= p.n2 - NOPQ;
         float *dst = p.nxt + ((long long)y0 * p.n2 + x) * p.n1 + zg;
 
         int slot = slot0;  // ring slot and parity of plane s
@@ -168,29 +170,59 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
                         }
                         const int jc = (u + 1 + 4) % 9;  // queue slot of plane y: ((s - 8) + 4) % 9
                         float lap[4];
+                        if constexpr (EXACT) {
 #pragma unroll
-                        for (int i = 0; i < 4; i++) lap[i] = fmul<EXACT>(zw[4 + i], p.c0);
+                            for (int i = 0; i < 4; i++) lap[i] = fmul<true>(zw[4 + i], p.c0);
 #pragma unroll
-                        for (int k = 1; k <= NOPQ; k++) {
-                            const float4 xm = *reinterpret_cast<const float4 *>(&H[xi + HALO - k][4 * zq + HALO]);
-                            const float4 xp = *reinterpret_cast<const float4 *>(&H[xi + HALO + k][4 * zq + HALO]);
-                            const float xmv[4] = {xm.x, xm.y, xm.z, xm.w}, xpv[4] = {xp.x, xp.y, xp.z, xp.w};
+                            for (int k = 1; k <= NOPQ; k++) {
+                                const float4 xm = *reinterpret_cast<const float4 *>(&H[xi + HALO - k][4 * zq + HALO]);
+                                const float4 xp = *reinterpret_cast<const float4 *>(&H[xi + HALO + k][4 * zq + HALO]);
+                                const float xmv[4] = {xm.x, xm.y, xm.z, xm.w}, xpv[4] = {xp.x, xp.y, xp.z, xp.w};
 #pragma unroll
-                            for (int i = 0; i < 4; i++) {
-                                const float zp = fadd<EXACT>(zw[4 + i - k], zw[4 + i + k]);
-                                const float xpair = fadd<EXACT>(xmv[i], xpv[i]);
-                                const float ypair = fadd<EXACT>(q[(jc + 9 - k) % 9][i], q[(jc + k) % 9][i]);
-                                if constexpr (EXACT) {
+                                for (int i = 0; i < 4; i++) {
+                                    const float zp = fadd<true>(zw[4 + i - k], zw[4 + i + k]);
+                                    const float xpair = fadd<true>(xmv[i], xpv[i]);
+                                    const float ypair = fadd<true>(q[(jc + 9 - k) % 9][i], q[(jc + k) % 9][i]);
                                     // ts_kernel.c:292-300 order: (z*cz + x*cx) + y*cy, then into lap
                                     float t = fadd<true>(fmul<true>(zp, p.cz[k]), fmul<true>(xpair, p.cx[k]));
                                     t = fadd<true>(t, fmul<true>(ypair, p.cy[k]));
                                     lap[i] = fadd<true>(lap[i], t);
-                                } else {
-                                    lap[i] = fmaf(zp, p.cz[k], lap[i]);
-                                    lap[i] = fmaf(xpair, p.cx[k], lap[i]);
-                                    lap[i] = fmaf(ypair, p.cy[k], lap[i]);
                                 }
                             }
+                        } else {
+                            // packed FP32x2 (add.f32x2 / fma.rn.f32x2): two cells per instruction
+                            float2 l01 = __fmul2_rn(make_float2(zw[4], zw[5]), make_float2(p.c0, p.c0));
+                            float2 l23 = __fmul2_rn(make_float2(zw[6], zw[7]), make_float2(p.c0, p.c0));
+#pragma unroll
+                            for (int k = 1; k <= NOPQ; k++) {
+                                const float4 xm = *reinterpret_cast<const float4 *>(&H[xi + HALO - k][4 * zq + HALO]);
+                                const float4 xp = *reinterpret_cast<const float4 *>(&H[xi + HALO + k][4 * zq + HALO]);
+                                float2 z01, z23;
+                                if (k % 2 == 0) {  // pairs aligned with the 16-byte loads
+                                    z01 = __fadd2_rn(make_float2(zw[4 - k], zw[5 - k]), make_float2(zw[4 + k], zw[5 + k]));
+                                    z23 = __fadd2_rn(make_float2(zw[6 - k], zw[7 - k]), make_float2(zw[6 + k], zw[7 + k]));
+                                } else {
+                                    z01 = make_float2(zw[4 - k] + zw[4 + k], zw[5 - k] + zw[5 + k]);
+                                    z23 = make_float2(zw[6 - k] + zw[6 + k], zw[7 - k] + zw[7 + k]);
+                                }
+                                const float2 x01 = __fadd2_rn(make_float2(xm.x, xm.y), make_float2(xp.x, xp.y));
+                                const float2 x23 = __fadd2_rn(make_float2(xm.z, xm.w), make_float2(xp.z, xp.w));
+                                const float *qa = q[(jc + 9 - k) % 9], *qb = q[(jc + k) % 9];
+                                const float2 y01 = __fadd2_rn(make_float2(qa[0], qa[1]), make_float2(qb[0], qb[1]));
+                                const float2 y23 = __fadd2_rn(make_float2(qa[2], qa[3]), make_float2(qb[2], qb[3]));
+                                const float2 cz = make_float2(p.cz[k], p.cz[k]), cx = make_float2(p.cx[k], p.cx[k]);
+                                const float2 cy = make_float2(p.cy[k], p.cy[k]);
+                                l01 = __ffma2_rn(z01, cz, l01);
+                                l23 = __ffma2_rn(z23, cz, l23);
+                                l01 = __ffma2_rn(x01, cx, l01);
+                                l23 = __ffma2_rn(x23, cx, l23);
+                                l01 = __ffma2_rn(y01, cy, l01);
+                                l23 = __ffma2_rn(y23, cy, l23);
+                            }
+                            lap[0] = l01.x;
+                            lap[1] = l01.y;
+                            lap[2] = l23.x;
+                            lap[3] = l23.y;
                         }
                         const float4 pv = *reinterpret_cast<const float4 *>(&st[slot].prv[xi][4 * zq]);
                         const float4 vv = *reinterpret_cast<const float4 *>(&st[slot].vel[xi][4 * zq]);
@@ -224,6 +256,17 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
                                 *reinterpret_cast<double2 *>(G) = make_double2(a.x + gacc[0], a.y + gacc[1]);
                                 *reinterpret_cast<double2 *>(G + 2) = make_double2(b.x + gacc[2], b.y + gacc[3]);
                             }
+                        } else if (!EXACT && undamped && tile_inner && yin) {
+                            // every cell of the strip is interior and undamped: packed update
+                            const float2 two = make_float2(2.f, 2.f);
+                            const float2 t01 = __ffma2_rn(two, make_float2(zw[4], zw[5]), make_float2(-pv.x, -pv.y));
+                            const float2 t23 = __ffma2_rn(two, make_float2(zw[6], zw[7]), make_float2(-pv.z, -pv.w));
+                            const float2 o01 = __ffma2_rn(make_float2(vv.x, vv.y), make_float2(lap[0], lap[1]), t01);
+                            const float2 o23 = __ffma2_rn(make_float2(vv.z, vv.w), make_float2(lap[2], lap[3]), t23);
+                            out[0] = o01.x;
+                            out[1] = o01.y;
+                            out[2] = o23.x;
+                            out[3] = o23.y;
                         } else if (undamped) {
 #pragma unroll
                             for (int i = 0; i < 4; i++) {

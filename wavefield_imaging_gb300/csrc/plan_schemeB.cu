@@ -319,15 +319,19 @@ awe_status stepB_full(awe_plan *p, const StepBParams &sp0, const float *prv, con
             launch_hybridB(d.ndim, p->nop, p->nbd, exact, d.fsrf, nxt, cur, abc, p->damp, g, s);
             launches += d.ndim;
         } else {
+            // the axis-1 ABC pass also applies the shell sponge to the axis-1 ends of
+            // lines the later passes leave alone (not when the sponge is deferred)
+            const bool zf = sponge && !p->sponge_deferred && shell > 0 && d.ndim == 3 && abc_zfused(p->nop, g, shell);
             if (d.ndim == 3) {
-                launch_abconeB(3, p->nop, exact, d.fsrf, nxt, cur, abc, g, s);
+                if (zf) launch_abconeB(3, p->nop, exact, d.fsrf, nxt, cur, abc, g, s, p->w[0], p->w[1], p->w[2], shell);
+                else launch_abconeB(3, p->nop, exact, d.fsrf, nxt, cur, abc, g, s);
                 launches += 3;
             }
             if (sponge && p->sponge_deferred) {
                 launch_band_sponge(d.ndim, std::max(p->nbd, shell), exact, nxt, p->w[0], p->w[1], p->w[2], g, s);
                 launches += d.ndim;  // one kernel per slab orientation
             } else if (shell > 0) {
-                launch_band_sponge(d.ndim, shell, exact, nxt, p->w[0], p->w[1], p->w[2], g, s);
+                launch_band_sponge(d.ndim, shell, exact, nxt, p->w[0], p->w[1], p->w[2], g, s, zf ? 1 : 0);
                 launches += d.ndim;
             }
         }
