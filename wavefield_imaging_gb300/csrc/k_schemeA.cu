@@ -205,12 +205,105 @@ __global__ void __launch_bounds__(256) k_stepA_sph_march(const float *__restrict
     }
 }
 
+// sponge_index for a 3D grid with the coordinates in registers (no indexed
+// arrays): the all-interior case first, then the priority walk
+__device__ __forceinline__ int sel3(int a, int v0, int v1, int v2) { return a == 0 ? v0 : (a == 1 ? v1 : v2); }
+
+__device__ __forceinline__ int sponge_index3(int c0, int c1, int c2, int n0, int n1, int n2, const StepAParams &p) {
+    const int nb = p.nb;
+    if (c0 >= nb && c0 <= n0 - nb && c1 >= nb && c1 <= n1 - nb && c2 >= nb && c2 <= n2 - nb) return 0;
+    const bool low = c0 < nb || c1 < nb || c2 < nb;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const int a = p.pri[k];
+        const int c = sel3(a, c0, c1, c2), n = sel3(a, n0, n1, n2);
+        if (low) {
+            if (c < nb) return nb - c;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const int a = p.pri[k];
+        const int c = sel3(a, c0, c1, c2), n = sel3(a, n0, n1, n2);
+        if (!low && c > n - nb) return c - (n - nb);
+    }
+    return 0;
+}
+
+// The same march with two consecutive radii per thread (n1 even): 8-byte
+// loads and packed FP32x2 arithmetic (fma.rn.f32x2 / add.f32x2 / mul.f32x2).
+__global__ void __launch_bounds__(256) k_stepA_sph_march2(const float *__restrict__ cur, float *__restrict__ nxt,
+                                                          const float *__restrict__ vel, const StepAParams p) {
+    const int i1 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int i2 = blockIdx.y * blockDim.y + threadIdx.y;
+    const Grid g = p.g;
+    if (i1 >= g.n1 || i2 >= g.n2) return;
+    const long long s2 = g.n1, s3 = (long long)g.n1 * g.n2;
+    const int p0 = blockIdx.z * kSphChunk, p1 = min(p0 + kSphChunk, g.n3);
+    const bool th_in = i2 >= 4 && i2 < g.n2 - 4;
+    const bool r0_in = i1 >= 4 && i1 < g.n1 - 4, r1_in = i1 + 1 >= 4 && i1 + 1 < g.n1 - 4;
+    const long long t = (long long)i2 * g.n1 + i1;
+    const float2 A2 = *reinterpret_cast<const float2 *>(p.tr0 + i1), Cr = *reinterpret_cast<const float2 *>(p.tr1 + i1);
+    const float2 B = *reinterpret_cast<const float2 *>(p.tt0 + t), D = *reinterpret_cast<const float2 *>(p.tt1 + t);
+    const float2 r0 = make_float2(p.rd[0], p.rd[0]), r1 = make_float2(p.rd[1], p.rd[1]);
+    const float2 r2 = make_float2(p.rd[2], p.rd[2]), r3 = make_float2(p.rd[3], p.rd[3]);
+    const float2 r4 = make_float2(p.rd[4], p.rd[4]), m1 = make_float2(-1.f, -1.f), m2 = make_float2(-2.f, -2.f);
+    const long long base = (long long)i2 * s2 + i1;
+    auto ld2 = [&](long long j) { return *reinterpret_cast<const float2 *>(cur + j); };
+    float2 um = p0 > 0 ? ld2(base + (p0 - 1) * s3) : make_float2(0.f, 0.f);
+    float2 uc = ld2(base + p0 * s3);
+    for (int i3 = p0; i3 < p1; i3++) {
+        const long long i = base + i3 * s3;
+        const float2 up = i3 + 1 < g.n3 ? ld2(i + s3) : make_float2(0.f, 0.f);
+        const float2 pv = *reinterpret_cast<const float2 *>(nxt + i);
+        const float2 vv = *reinterpret_cast<const float2 *>(vel + i);
+        float2 lap = make_float2(0.f, 0.f);
+        const bool ph_in = i3 >= 4 && i3 < g.n3 - 4;
+        if (th_in && ph_in && (r0_in || r1_in)) {
+            const float rm = i1 > 0 ? cur[i - 1] : 0.f, rp = i1 + 2 < g.n1 ? cur[i + 2] : 0.f;
+            const float2 mi = make_float2(rm, uc.x), pl = make_float2(uc.y, rp);  // r - 1 and r + 1 of both cells
+            const float2 tm = ld2(i - s2), tp = ld2(i + s2);
+            const float2 pra = __fmul2_rn(__ffma2_rn(mi, m1, pl), r0);
+            const float2 ppra = __fmul2_rn(__fadd2_rn(__ffma2_rn(uc, m2, pl), mi), r1);
+            const float2 pth = __fmul2_rn(__ffma2_rn(tm, m1, tp), r2);
+            const float2 ppth = __fmul2_rn(__fadd2_rn(__ffma2_rn(uc, m2, tp), tm), r3);
+            const float2 ppph = __fmul2_rn(__fadd2_rn(__ffma2_rn(uc, m2, up), um), r4);
+            lap = __ffma2_rn(A2, pra, ppra);
+            lap = __ffma2_rn(B, pth, lap);
+            lap = __ffma2_rn(Cr, ppth, lap);
+            lap = __ffma2_rn(D, ppph, lap);
+            if (!r0_in) lap.x = 0.f;
+            if (!r1_in) lap.y = 0.f;
+        }
+        const float2 a = __fmul2_rn(make_float2(p.dt2, p.dt2), __fmul2_rn(vv, vv));
+        const float2 f2 = __ffma2_rn(a, lap, __fadd2_rn(uc, uc));
+        float f[2] = {f2.x, f2.y};
+        const float pr[2] = {pv.x, pv.y};
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            const int si = sponge_index3(i1 + j, i2, i3, g.n1, g.n2, g.n3, p);
+            float v = f[j] - damp_a<false>(pr[j], si, p.dtab, p.ftab);
+            // the spherical program has no one-way boundary (no shell); free-surface mask
+            if (p.mask == 3 && (i1 + j > g.n1 - p.nb || (i1 + j < p.spill && (i2 >= 1 || i3 >= 1)))) v = 0.f;
+            f[j] = damp_a<false>(v, si, p.dtab, p.ftab);
+        }
+        *reinterpret_cast<float2 *>(nxt + i) = make_float2(f[0], f[1]);
+        um = uc;
+        uc = up;
+    }
+}
+
 template <bool EXACT>
 static void step_geom(int geom, const float *cur, float *nxt, const float *vel, const StepAParams &p, cudaStream_t s) {
     dim3 block(64, 4, 1), grid((p.g.n1 + 63) / 64, (p.g.n2 + 3) / 4, p.g.n3);
     if (!EXACT && geom == 3) {
-        dim3 mg((p.g.n1 + 63) / 64, (p.g.n2 + 3) / 4, (p.g.n3 + kSphChunk - 1) / kSphChunk);
-        k_stepA_sph_march<<<mg, block, 0, s>>>(cur, nxt, vel, p);
+        if (p.g.n1 % 2 == 0) {
+            dim3 b2(32, 8, 1), g2((p.g.n1 / 2 + 31) / 32, (p.g.n2 + 7) / 8, (p.g.n3 + kSphChunk - 1) / kSphChunk);
+            k_stepA_sph_march2<<<g2, b2, 0, s>>>(cur, nxt, vel, p);
+        } else {
+            dim3 mg((p.g.n1 + 63) / 64, (p.g.n2 + 3) / 4, (p.g.n3 + kSphChunk - 1) / kSphChunk);
+            k_stepA_sph_march<<<mg, block, 0, s>>>(cur, nxt, vel, p);
+        }
         return;
     }
     switch (geom) {
