@@ -510,7 +510,7 @@ def run_batch(args):
     dist, rank, world, local = dist_init()
     torch.cuda.set_device(local)
     nt = 4000 if args.nt == 3000 else args.nt
-    nshots, nz = args.shots, 512
+    nshots, nz = args.shots or 256, 512
     vel, shots = batch_survey(nshots=nshots, nz=nz)
     nxm = vel.shape[0]
     wav = ricker(nt, 0.005, 5.0)
@@ -603,7 +603,7 @@ def run_batch_grad(args):
     dist, rank, world, local = dist_init()
     torch.cuda.set_device(local)
     nt = 4000 if args.nt == 3000 else args.nt
-    nshots, nz = args.shots, 512
+    nshots, nz = args.shots or 256, 512
     vtrue, shots = batch_survey(nshots=nshots, nz=nz)
     v0 = smooth(vtrue, 100.0 / 5.0)
     nxm = vtrue.shape[0]
@@ -707,22 +707,32 @@ def run_spher(args):
 
     torch.cuda.set_device(0)
     nt = args.nt
+    nshots = args.shots or 1
     w = spher_workload(nt, nr=args.n + 188 if args.n != 512 else 700, nang=args.n)
     vel = spher_model(w)
     nr_, nth, nph = w["n"]
     rs = 3389.5 - 0.2 + 0.05
-    th0, ph0 = w["o"][1] + 0.5 * (nth - 1) * w["d"][1], w["o"][2] + 0.5 * (nph - 1) * w["d"][2]
-    sou = np.array([[rs, ph0, th0]], np.float32)
-    gth = w["o"][1] + np.linspace(0.25, 0.75, 64) * (nth - 1) * w["d"][1]
-    gph = w["o"][2] + np.linspace(0.25, 0.75, 64) * (nph - 1) * w["d"][2]
-    P, T = np.meshgrid(gph, gth, indexing="ij")
-    rec = np.stack([np.full(P.size, rs), P.ravel(), T.ravel()], 1).astype(np.float32)
+    th0 = w["o"][1] + 0.5 * (nth - 1) * w["d"][1]
+    # sources along the equator (a great circle) at 50 m altitude, 64 x 64 receivers around each
+    shots = []
+    for k in range(nshots):
+        ph_s = w["o"][2] + (0.5 if nshots == 1 else 0.3 + 0.4 * k / (nshots - 1)) * (nph - 1) * w["d"][2]
+        sou = np.array([[rs, ph_s, th0]], np.float32)
+        gth = th0 + np.linspace(-0.25, 0.25, 64) * (nth - 1) * w["d"][1]
+        gph = ph_s + np.linspace(-0.25, 0.25, 64) * (nph - 1) * w["d"][2]
+        P, T = np.meshgrid(gph, gth, indexing="ij")
+        rec = np.stack([np.full(P.size, rs), P.ravel(), T.ravel()], 1).astype(np.float32)
+        shots.append((sou, rec))
     wav = ricker(nt, w["dt"], w["f0"])
     desc = awe.make_desc(3, w["n"], w["d"], w["o"], nt, w["dt"], coords=awe.SPHER, scheme=awe.SCHEME_GPU,
                          nb=w["nb"], expl=0, precision=awe.FAST)
     plan = awe.Plan(desc)
     plan.set_model(vel)
-    plan.set_geometry(sou, rec)
+    if nshots == 1:
+        plan.set_geometry(*shots[0])
+    else:
+        plan.set_shots(shots)
+    rec = np.concatenate([r for _, r in shots])
     d_wav = torch.from_numpy(wav).cuda()
     d_dat = torch.zeros((plan.nsmp, rec.shape[0]), dtype=torch.float32, device="cuda")
     stream = torch.cuda.Stream()
@@ -741,14 +751,30 @@ def run_spher(args):
     clocks = sampler.stop()
     ms = e0.elapsed_time(e1) / args.steps
     kern_ms, kern_n = plan.profile_read()
-    cells = int(np.prod([n + 2 * w["nb"] for n in w["n"]]))
+    cells = nshots * int(np.prod([n + 2 * w["nb"] for n in w["n"]]))
     peak, peak_kind = measured_peak()
     avg = kern_ms / 1e3 / max(kern_n, 1)
+    plain = None
+    if nshots > 1:  # the same shots one after the other through the single-shot path
+        single = awe.Plan(desc)
+        single.set_model(vel)
+        d1 = torch.zeros((single.nsmp, 4096), dtype=torch.float32, device="cuda")
+        q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        q0.record(stream)
+        for sou, r in shots:
+            single.set_geometry(sou, r)
+            single.forward_device(d_wav.data_ptr(), 1, d1.data_ptr(), 0, stream.cuda_stream)
+        q1.record(stream)
+        torch.cuda.synchronize()
+        plain = {"ms": q0.elapsed_time(q1), "speedup_batched_vs_plain": q0.elapsed_time(q1) / ms}
+        single.close()
     out = {"metric": "cell-updates/s (3D spherical shell, GPU-program scheme)", "value": cells * nt / (ms / 1e3),
            "unit": "cell-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
-           "config": {"workload": w["name"], "padded_cells": cells},
-           "roofline": {"bound": "hbm", "kernel": "k_stepA<spherical>", "avg_launch_us": avg * 1e6,
+           "config": {"workload": w["name"] + (", %d shots in one launch per step" % nshots if nshots > 1 else ""),
+                      "padded_cells": cells, "shots": nshots},
+           "plain_sequential": plain,
+           "roofline": {"bound": "hbm", "kernel": "k_stepA_sph_march2", "avg_launch_us": avg * 1e6,
                         "achieved": BYTES_PER_CELL * cells / avg / 1e9, "peak": peak, "unit": "GB/s",
                         "frac": BYTES_PER_CELL * cells / avg / 1e9 / peak, "peak_source": peak_kind,
                         "kernel_share": kern_ms / args.steps / ms},
@@ -771,7 +797,8 @@ def main():
     ap.add_argument("--workload", default="fwd3d", choices=["fwd3d", "grad3d", "grad2d", "batch2d", "batchgrad2d", "spher3d"],
                     help="fwd3d: the headline forward workload; grad3d/grad2d: misfit gradients; "
                          "batch2d: the batched 2D survey")
-    ap.add_argument("--shots", type=int, default=256, help="batch2d: number of shots")
+    ap.add_argument("--shots", type=int, default=0,
+                    help="shots: batch2d/batchgrad2d (default 256), spher3d (default 1; 16 on the survey track)")
     ap.add_argument("--ckpt", default="bf16", choices=["bf16", "fp16", "fp32"], help="checkpoint storage (grad*)")
     args = ap.parse_args()
     if args.impl == "reference":

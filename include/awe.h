@@ -132,6 +132,17 @@ awe_status awe_set_model(awe_plan *plan, const float *vel, const float *den, con
  * [spherical: (r, phi, theta)]. */
 awe_status awe_set_geometry(awe_plan *plan, int ns, const float *sou, int nr, const float *rec);
 
+/* Several shots on the plan's grid and model, advanced together (one launch
+ * of the step kernel covers every shot's field): the 16-shot track of the
+ * spherical-shell survey.  Shot s has ns[s] sources and nr[s] receivers;
+ * sou and rec hold all shots' points one shot after the other, in
+ * awe_set_geometry's order.  The traces of awe_forward become [nsmp][sum nr]
+ * (receivers of shot 0, then of shot 1, ...), every source injecting the same
+ * wavelet into its own shot.  Spherical 3D, AWE_SCHEME_GPU, AWE_FAST, no
+ * snapshots (nshots = 1 is awe_set_geometry).  Replaces running
+ * sfAWEFDspher3Dgpu once per source position. */
+awe_status awe_set_shots(awe_plan *plan, int nshots, const int *ns, const float *sou, const int *nr, const float *rec);
+
 /* Host-buffer forward modelling: wav [nt][ncs] (ncs = 1 or ns); dat
  * [nsmp][nr]; wfl (may be NULL) [nsnap][snap_elems].  Snapshots also go to
  * the callback when one is set. */

@@ -108,6 +108,8 @@ struct StepAParams {
     const float *ftab;                   // the same rounded to float (FAST mode)
     float b2lo, b2hi;                    // 2D one-way coefficients at the last sample
     const float *tb[6];                  // cart 3D one-way coefficient tables
+    int nshot;                           // shots advanced together (spherical 3D, AWE_FAST), fields back to back
+    long long shot_cells;                // cells of one shot's field
 };
 void launch_stepA(int geom, bool exact, const float *cur, float *nxt, const float *vel, const StepAParams &p,
                   cudaStream_t s);

@@ -234,12 +234,18 @@ __device__ __forceinline__ int sponge_index3(int c0, int c1, int c2, int n0, int
 // loads and packed FP32x2 arithmetic (fma.rn.f32x2 / add.f32x2 / mul.f32x2).
 __global__ void __launch_bounds__(256) k_stepA_sph_march2(const float *__restrict__ cur, float *__restrict__ nxt,
                                                           const float *__restrict__ vel, const StepAParams p) {
+    // (the shot offset below is applied to cur and nxt, never to the shared model)
     const int i1 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int i2 = blockIdx.y * blockDim.y + threadIdx.y;
     const Grid g = p.g;
     if (i1 >= g.n1 || i2 >= g.n2) return;
     const long long s2 = g.n1, s3 = (long long)g.n1 * g.n2;
-    const int p0 = blockIdx.z * kSphChunk, p1 = min(p0 + kSphChunk, g.n3);
+    // blockIdx.z enumerates (shot, phi chunk); shots' fields lie back to back
+    const int nchunk = (g.n3 + kSphChunk - 1) / kSphChunk;
+    const int shot = blockIdx.z / nchunk;
+    cur += shot * p.shot_cells;
+    nxt += shot * p.shot_cells;
+    const int p0 = (blockIdx.z % nchunk) * kSphChunk, p1 = min(p0 + kSphChunk, g.n3);
     const bool th_in = i2 >= 4 && i2 < g.n2 - 4;
     const bool r0_in = i1 >= 4 && i1 < g.n1 - 4, r1_in = i1 + 1 >= 4 && i1 + 1 < g.n1 - 4;
     const long long t = (long long)i2 * g.n1 + i1;
@@ -298,7 +304,8 @@ static void step_geom(int geom, const float *cur, float *nxt, const float *vel, 
     dim3 block(64, 4, 1), grid((p.g.n1 + 63) / 64, (p.g.n2 + 3) / 4, p.g.n3);
     if (!EXACT && geom == 3) {
         if (p.g.n1 % 2 == 0) {
-            dim3 b2(32, 8, 1), g2((p.g.n1 / 2 + 31) / 32, (p.g.n2 + 7) / 8, (p.g.n3 + kSphChunk - 1) / kSphChunk);
+            const int nchunk = (p.g.n3 + kSphChunk - 1) / kSphChunk;
+            dim3 b2(32, 8, 1), g2((p.g.n1 / 2 + 31) / 32, (p.g.n2 + 7) / 8, nchunk * (p.nshot > 0 ? p.nshot : 1));
             k_stepA_sph_march2<<<g2, b2, 0, s>>>(cur, nxt, vel, p);
         } else {
             dim3 mg((p.g.n1 + 63) / 64, (p.g.n2 + 3) / 4, (p.g.n3 + kSphChunk - 1) / kSphChunk);

@@ -60,7 +60,6 @@ awe_status deliver_snapshot(awe_plan *p, const float *d_frame, int isnap, int it
     const size_t bytes = p->snap_elems * sizeof(float);
     if (p->h_pinned_bytes < bytes) {
         if (p->h_pinned) cudaFreeHost(p->h_pinned);
-    for (cudaEvent_t e : p->prof_ev) cudaEventDestroy(e);
         p->h_pinned = nullptr;
         p->h_pinned_bytes = 0;
         if (cudaMallocHost((void **)&p->h_pinned, bytes) != cudaSuccess) {
@@ -271,6 +270,55 @@ awe_status awe_set_geometry(awe_plan *p, int ns, const float *sou, int nr, const
     awe_status st = set_geometry_common(p, ns, sou, nr, rec);
     if (st == AWE_OK) p->geom_set = true;
     return st;
+}
+
+awe_status awe_set_shots(awe_plan *p, int nshots, const int *ns, const float *sou, const int *nr, const float *rec) {
+    if (!p || nshots < 1 || !ns || !nr) {
+        set_error("bad shot arguments");
+        return AWE_ERR_INVALID;
+    }
+    const awe_desc &d = p->d;
+    if (nshots > 1 && !(d.scheme == AWE_SCHEME_GPU && d.coords == AWE_SPHER && d.ndim == 3 &&
+                        d.precision == AWE_FAST && d.jsnap == 0)) {
+        set_error("awe_set_shots: several shots need the spherical 3D GPU-program scheme, AWE_FAST, no snapshots");
+        return AWE_ERR_UNSUPPORTED;
+    }
+    int NS = 0, NR = 0;
+    for (int s = 0; s < nshots; s++) {
+        if (ns[s] < 0 || nr[s] < 0) {
+            set_error("negative point count for shot %d", s);
+            return AWE_ERR_INVALID;
+        }
+        NS += ns[s];
+        NR += nr[s];
+    }
+    if ((NS > 0 && !sou) || (NR > 0 && !rec)) {
+        set_error("null source or receiver coordinates");
+        return AWE_ERR_INVALID;
+    }
+    CUDA_TRY(cudaSetDevice(p->device));
+    awe_status st = set_geometry_common(p, NS, sou, NR, rec);
+    if (st != AWE_OK) return st;
+    // points of shot s address field s
+    const long long cells = p->g.cells();
+    int a = 0, b = 0;
+    for (int s = 0; s < nshots; s++) {
+        for (int i = 0; i < ns[s]; i++) p->h_src[a++].base += s * cells;
+        for (int i = 0; i < nr[s]; i++) p->h_rec[b++].base += s * cells;
+    }
+    if (NS) CUDA_TRY(cudaMemcpy(p->src, p->h_src.data(), NS * sizeof(GeoPoint), cudaMemcpyHostToDevice));
+    if (NR) CUDA_TRY(cudaMemcpy(p->rec, p->h_rec.data(), NR * sizeof(GeoPoint), cudaMemcpyHostToDevice));
+    if (nshots != p->pa.nshot) {
+        for (int k = 0; k < 2; k++) {
+            dev_free(p, p->u[k]);
+            p->u[k] = nullptr;
+            st = dev_alloc(p, (void **)&p->u[k], (size_t)nshots * cells * sizeof(float));
+            if (st != AWE_OK) return st;
+        }
+        p->pa.nshot = nshots;
+    }
+    p->geom_set = true;
+    return AWE_OK;
 }
 
 awe_status awe_set_snapshot_callback(awe_plan *p, awe_snap_fn fn, void *user) {

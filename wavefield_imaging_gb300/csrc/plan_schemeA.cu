@@ -169,6 +169,8 @@ awe_status planA_init(awe_plan *p) {
     AWE_TRY(dev_alloc(p, (void **)&p->corner_off, 8 * sizeof(long long)));
     if (pa.shell > 0) AWE_TRY(dev_alloc(p, (void **)&p->aux, cells * sizeof(float)));
 
+    pa.nshot = 1;
+    pa.shot_cells = g.cells();
     // reciprocals of the Laplacian divisors (AWE_FAST multiplies; AWE_EXACT divides as the reference)
     const float dvs[5] = {pa.dd1, pa.dd2, pa.dd3, pa.dd4, pa.dd5};
     for (int j = 0; j < 5; j++) pa.rd[j] = dvs[j] != 0.f ? 1.f / dvs[j] : 0.f;
@@ -322,7 +324,7 @@ awe_status planA_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, flo
     const Grid &g = p->g;
     const StepAParams &pa = p->pa;
     const bool exact = d.precision == AWE_EXACT;
-    const size_t bytes = (size_t)g.cells() * sizeof(float);
+    const size_t bytes = (size_t)g.cells() * sizeof(float) * (pa.nshot > 0 ? pa.nshot : 1);
     bool scaled = false;
     AWE_TRY(prepare_injection(p, scaled));
     CUDA_TRY(cudaMemsetAsync(p->u[0], 0, bytes, s));

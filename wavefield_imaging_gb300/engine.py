@@ -104,6 +104,9 @@ def lib():
         for name in ("awe_batch_create", "awe_batch_destroy", "awe_batch_set_model", "awe_batch_forward",
                      "awe_batch_forward_device", "awe_batch_tune", "awe_batch_info", "awe_batch_gradient"):
             getattr(L, name).restype = C.c_int
+        ip = C.POINTER(C.c_int)
+        L.awe_set_shots.argtypes = [vp, C.c_int, ip, fp, ip, fp]
+        L.awe_set_shots.restype = C.c_int
         dp = C.POINTER(C.c_double)
         L.awe_gradient.argtypes = [vp, fp, C.c_int, fp, C.POINTER(GradOpts), dp, dp, fp]
         L.awe_gradient_device.argtypes = [vp, vp, C.c_int, vp, C.POINTER(GradOpts), vp, dp, vp, vp]
@@ -178,6 +181,17 @@ class Plan:
         rec = np.ascontiguousarray(rec, np.float32).reshape(-1, nd)
         self.ns, self.nr = sou.shape[0], rec.shape[0]
         _check(lib().awe_set_geometry(self._h, self.ns, _fp(sou), self.nr, _fp(rec)))
+
+    def set_shots(self, shots):
+        """shots: list of (sou [ns][3], rec [nr][3]) advanced together (spherical 3D)."""
+        nd = self.desc.ndim
+        sou = [np.ascontiguousarray(s_, np.float32).reshape(-1, nd) for s_, _ in shots]
+        rec = [np.ascontiguousarray(r_, np.float32).reshape(-1, nd) for _, r_ in shots]
+        ns = (C.c_int * len(shots))(*[a.shape[0] for a in sou])
+        nr = (C.c_int * len(shots))(*[a.shape[0] for a in rec])
+        S, R = np.ascontiguousarray(np.concatenate(sou)), np.ascontiguousarray(np.concatenate(rec))
+        self.ns, self.nr = S.shape[0], R.shape[0]
+        _check(lib().awe_set_shots(self._h, len(shots), ns, _fp(S), nr, _fp(R)))
 
     def forward(self, wav, snapshots: bool = False):
         """wav: [nt] or [nt][ncs].  Returns dat [nsmp][nr] (and snaps
