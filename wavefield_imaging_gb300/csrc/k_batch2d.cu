@@ -77,29 +77,48 @@ __global__ void __launch_bounds__(TZ / 4 * TX) k_batch2d(const BatchShot *__rest
             if (w + (int)gridDim.x < nitems) fetch(w + gridDim.x);
             const int x = x0 + xi, zb = z0 + 4 * zq;
             if (x >= n2 || zb >= n1) continue;
-            const float *row = &tile[xi + NOP][0];  // column SH holds z0
             const long long gi = sh.off + (long long)x * n1 + zb;
             const float wx = p.wx[sh.wx_off + x];
             float o[4];
             const float pr4[4] = {pv.x, pv.y, pv.z, pv.w}, v4[4] = {vv.x, vv.y, vv.z, vv.w};
             const bool xin = x >= NOP && x < n2 - NOP;
+            // 16-byte shared loads (conflict-free): the z window of the strip and
+            // the x neighbours' strips; packed FP32x2 arithmetic, two cells at a time
+            const int tz0 = SH + 4 * zq;  // tile column of zb
+            constexpr int NZW = 4 + 2 * SH;
+            float zw[NZW];
+#pragma unroll
+            for (int j = 0; j < NZW / 4; j++) {
+                const float4 t = *reinterpret_cast<const float4 *>(&tile[xi + NOP][tz0 - SH + 4 * j]);
+                zw[4 * j] = t.x;
+                zw[4 * j + 1] = t.y;
+                zw[4 * j + 2] = t.z;
+                zw[4 * j + 3] = t.w;
+            }
+            float2 l01 = __fmul2_rn(make_float2(zw[SH], zw[SH + 1]), make_float2(p.c0, p.c0));
+            float2 l23 = __fmul2_rn(make_float2(zw[SH + 2], zw[SH + 3]), make_float2(p.c0, p.c0));
+#pragma unroll
+            for (int k = 1; k <= NOP; k++) {
+                const float4 xm = *reinterpret_cast<const float4 *>(&tile[xi + NOP - k][tz0]);
+                const float4 xp = *reinterpret_cast<const float4 *>(&tile[xi + NOP + k][tz0]);
+                const float2 z01 = make_float2(zw[SH - k] + zw[SH + k], zw[SH + 1 - k] + zw[SH + 1 + k]);
+                const float2 z23 = make_float2(zw[SH + 2 - k] + zw[SH + 2 + k], zw[SH + 3 - k] + zw[SH + 3 + k]);
+                const float2 x01 = __fadd2_rn(make_float2(xm.x, xm.y), make_float2(xp.x, xp.y));
+                const float2 x23 = __fadd2_rn(make_float2(xm.z, xm.w), make_float2(xp.z, xp.w));
+                const float2 cz = make_float2(p.cz[k], p.cz[k]), cx = make_float2(p.cx[k], p.cx[k]);
+                l01 = __ffma2_rn(z01, cz, l01);
+                l23 = __ffma2_rn(z23, cz, l23);
+                l01 = __ffma2_rn(x01, cx, l01);
+                l23 = __ffma2_rn(x23, cx, l23);
+            }
+            const float lap[4] = {l01.x, l01.y, l23.x, l23.y};
 #pragma unroll
             for (int i = 0; i < 4; i++) {
-                const int z = zb + i, tz = SH + 4 * zq + i;
-                const float wz = p.wz[z];
+                const int z = zb + i;
                 float pr = pr4[i];
-                if (p.sponge) pr = (pr * wz) * wx;
+                if (p.sponge) pr = (pr * p.wz[z]) * wx;
                 float out = pr;
-                if (xin && z >= NOP && z < n1 - NOP) {
-                    const float u = row[tz];
-                    float lap = u * p.c0;
-#pragma unroll
-                    for (int k = 1; k <= NOP; k++) {
-                        lap = fmaf(row[tz - k] + row[tz + k], p.cz[k], lap);
-                        lap = fmaf(tile[xi + NOP - k][tz] + tile[xi + NOP + k][tz], p.cx[k], lap);
-                    }
-                    out = fmaf(v4[i], lap, 2.f * u - pr);
-                }
+                if (xin && z >= NOP && z < n1 - NOP) out = fmaf(v4[i], lap[i], 2.f * zw[SH + i] - pr);
                 o[i] = out;
             }
             // source corners of this shot that fall in this 4-cell strip
@@ -256,29 +275,45 @@ __global__ void __launch_bounds__(TZ / 4 * TX) k_batch2d_adj(const BatchShot *__
         const bool xin = x >= NOP && x < n2 - NOP;
         float mu[4], wc[4];
         double gacc[4];
+        // 16-byte shared loads of both stencils' z windows and x neighbours, packed FP32x2
+        const int tz0 = SH + 4 * zq;
+        constexpr int NZW = 4 + 2 * SH;
+        float gz[NZW], vz[NZW];
+#pragma unroll
+        for (int j = 0; j < NZW / 4; j++) {
+            const float4 a = *reinterpret_cast<const float4 *>(&gt[xi + NOP][tz0 - SH + 4 * j]);
+            const float4 b = *reinterpret_cast<const float4 *>(&vt[xi + NOP][tz0 - SH + 4 * j]);
+            gz[4 * j] = a.x, gz[4 * j + 1] = a.y, gz[4 * j + 2] = a.z, gz[4 * j + 3] = a.w;
+            vz[4 * j] = b.x, vz[4 * j + 1] = b.y, vz[4 * j + 2] = b.z, vz[4 * j + 3] = b.w;
+        }
+        const float2 c0 = make_float2(p.c0, p.c0);
+        float2 g01 = __fmul2_rn(make_float2(gz[SH], gz[SH + 1]), c0), g23 = __fmul2_rn(make_float2(gz[SH + 2], gz[SH + 3]), c0);
+        float2 v01 = __fmul2_rn(make_float2(vz[SH], vz[SH + 1]), c0), v23 = __fmul2_rn(make_float2(vz[SH + 2], vz[SH + 3]), c0);
+#pragma unroll
+        for (int k = 1; k <= NOP; k++) {
+            const float2 cz = make_float2(p.cz[k], p.cz[k]), cx = make_float2(p.cx[k], p.cx[k]);
+            const float4 gm = *reinterpret_cast<const float4 *>(&gt[xi + NOP - k][tz0]);
+            const float4 gp = *reinterpret_cast<const float4 *>(&gt[xi + NOP + k][tz0]);
+            const float4 vm = *reinterpret_cast<const float4 *>(&vt[xi + NOP - k][tz0]);
+            const float4 vp = *reinterpret_cast<const float4 *>(&vt[xi + NOP + k][tz0]);
+            g01 = __ffma2_rn(make_float2(gz[SH - k] + gz[SH + k], gz[SH + 1 - k] + gz[SH + 1 + k]), cz, g01);
+            g23 = __ffma2_rn(make_float2(gz[SH + 2 - k] + gz[SH + 2 + k], gz[SH + 3 - k] + gz[SH + 3 + k]), cz, g23);
+            g01 = __ffma2_rn(__fadd2_rn(make_float2(gm.x, gm.y), make_float2(gp.x, gp.y)), cx, g01);
+            g23 = __ffma2_rn(__fadd2_rn(make_float2(gm.z, gm.w), make_float2(gp.z, gp.w)), cx, g23);
+            v01 = __ffma2_rn(make_float2(vz[SH - k] + vz[SH + k], vz[SH + 1 - k] + vz[SH + 1 + k]), cz, v01);
+            v23 = __ffma2_rn(make_float2(vz[SH + 2 - k] + vz[SH + 2 + k], vz[SH + 3 - k] + vz[SH + 3 + k]), cz, v23);
+            v01 = __ffma2_rn(__fadd2_rn(make_float2(vm.x, vm.y), make_float2(vp.x, vp.y)), cx, v01);
+            v23 = __ffma2_rn(__fadd2_rn(make_float2(vm.z, vm.w), make_float2(vp.z, vp.w)), cx, v23);
+        }
+        const float lt4[4] = {g01.x, g01.y, g23.x, g23.y}, lv4[4] = {v01.x, v01.y, v23.x, v23.y};
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-            const int z = zb + i, tz = SH + 4 * zq + i;
+            const int z = zb + i;
             const bool in = xin && z >= NOP && z < n1 - NOP;
             wc[i] = p.sponge ? p.wz[z] * wx : 1.f;
-            float lt = gt[xi + NOP][tz] * p.c0;
-#pragma unroll
-            for (int k = 1; k <= NOP; k++) {
-                lt = fmaf(gt[xi + NOP][tz - k] + gt[xi + NOP][tz + k], p.cz[k], lt);
-                lt = fmaf(gt[xi + NOP - k][tz] + gt[xi + NOP + k][tz], p.cx[k], lt);
-            }
-            const float lam = (in ? 2.f * nu[i] : 0.f) + lt + (in ? -wc[i] : wc[i]) * yv[i];
+            const float lam = (in ? 2.f * nu[i] : 0.f) + lt4[i] + (in ? -wc[i] : wc[i]) * yv[i];
             mu[i] = wc[i] * lam;
-            gacc[i] = 0.0;
-            if (in) {
-                float lv = vt[xi + NOP][tz] * p.c0;
-#pragma unroll
-                for (int k = 1; k <= NOP; k++) {
-                    lv = fmaf(vt[xi + NOP][tz - k] + vt[xi + NOP][tz + k], p.cz[k], lv);
-                    lv = fmaf(vt[xi + NOP - k][tz] + vt[xi + NOP + k][tz], p.cx[k], lv);
-                }
-                gacc[i] = (double)nu[i] * (double)lv;
-            }
+            gacc[i] = in ? (double)nu[i] * (double)lv4[i] : 0.0;
         }
         const long long cell0 = (long long)x * n1 + zb;
         // receiver residuals (W R^T r, then the W of mu): corners listed per tile
@@ -311,9 +346,9 @@ __global__ void __launch_bounds__(TZ / 4 * TX) k_batch2d_adj(const BatchShot *__
         }
         *reinterpret_cast<float4 *>(p.Y + gi) = make_float4(mu[0], mu[1], mu[2], mu[3]);
         double *G = p.G + gi;
-        const double2 g01 = *reinterpret_cast<const double2 *>(G), g23 = *reinterpret_cast<const double2 *>(G + 2);
-        *reinterpret_cast<double2 *>(G) = make_double2(g01.x + gacc[0], g01.y + gacc[1]);
-        *reinterpret_cast<double2 *>(G + 2) = make_double2(g23.x + gacc[2], g23.y + gacc[3]);
+        const double2 G01 = *reinterpret_cast<const double2 *>(G), G23 = *reinterpret_cast<const double2 *>(G + 2);
+        *reinterpret_cast<double2 *>(G) = make_double2(G01.x + gacc[0], G01.y + gacc[1]);
+        *reinterpret_cast<double2 *>(G + 2) = make_double2(G23.x + gacc[2], G23.y + gacc[3]);
     }
 }
 
