@@ -72,6 +72,10 @@ typedef struct {
     int jdata, jsnap, bnds, fsrf, expl, refl;
 } orc_gpar;
 
+/* The spherical 3D case with FP64 wavefields and arithmetic; dat [nt][nr] double. */
+int orc_gpu_spher3d_fp64(const orc_gpar *p, const float *vel, const float *wav, int ns, const float *sou, int nr,
+                         const float *rec, double *dat);
+
 int orc_gpu_forward(int kind, const orc_gpar *p, const float *vel, const float *rfl, const float *wav, int ns,
                     const float *sou, int nr, const float *rec, float *dat, float *snaps);
 

@@ -691,6 +691,95 @@ static int gpu_spher3d(const orc_gpar *P, const float *vel_in, const float *wav,
     return 0;
 }
 
+/* The spherical scheme above with FP64 wavefields and arithmetic (inputs,
+ * geometry and sponge table as above; trig in double), to state the FP32
+ * error of the spherical configuration.  No snapshots. */
+int orc_gpu_spher3d_fp64(const orc_gpar *P, const float *vel_in, const float *wav, int ns, const float *sou, int nr,
+                         const float *rec, double *dat) {
+    const int nra = P->n1, nth = P->n2, nph = P->n3, nt = P->nt;
+    const double dra = P->d1, dth = P->d2, dph = P->d3, dt = P->dt;
+    const int nb = P->nb < NOPA ? NOPA : P->nb;
+    const int nrapad = nra + 2 * nb, nthpad = nth + 2 * nb, nphpad = nph + 2 * nb;
+    const float orpad = P->o1 - nb * P->d1, othpad = P->o2 - nb * P->d2, ophpad = P->o3 - nb * P->d3;
+    const size_t st = nrapad, sp = (size_t)nrapad * nthpad, npad = sp * nphpad;
+    float *v = malloc(npad * 4);
+    double *po = calloc(npad, 8), *ppo = calloc(npad, 8), *fpo = calloc(npad, 8);
+    pad_clamp(vel_in, v, nb, nra, nth, nph);
+    double tab[4096];
+    for (int i = 1; i <= nb; i++) tab[i] = sponge_damp(i, nb);
+    glint *cs = malloc((ns ? ns : 1) * sizeof(glint)), *cr = malloc((nr ? nr : 1) * sizeof(glint));
+    for (int i = 0; i < ns; i++)
+        glint_make(3, sou[3 * i], sou[3 * i + 1], sou[3 * i + 2], othpad, orpad, ophpad, P->d2, P->d1, P->d3, nthpad,
+                   nrapad, nphpad, &cs[i]);
+    for (int i = 0; i < nr; i++)
+        glint_make(3, rec[3 * i], rec[3 * i + 1], rec[3 * i + 2], othpad, orpad, ophpad, P->d2, P->d1, P->d3, nthpad,
+                   nrapad, nphpad, &cr[i]);
+    size_t off[8];
+    for (int k = 0; k < 8; k++) off[k] = ((k & 1) ? st : 0) + ((k & 2) ? 1 : 0) + ((k & 4) ? sp : 0);
+#define CS(iph, ith, ira) ((size_t)(iph) * sp + (size_t)(ith) * st + (ira))
+    for (int it = 0; it < nt; it++) {
+        const double wa = wav[it];
+        for (int s = 0; s < ns; s++) {
+            const glint *c = &cs[s];
+            size_t b = CS(c->jy, c->jz, c->jx);
+            double r = 1.0;
+            if (P->expl) r = refl3(v, npad, (long long)b, st, sp);
+            for (int k = 0; k < 8; k++) po[b + off[k]] += wa * c->w[k] * r;
+        }
+        for (int iph = 0; iph < nphpad; iph++)
+            for (int ith = 0; ith < nthpad; ith++)
+                for (int ira = 0; ira < nrapad; ira++) {
+                    size_t c = CS(iph, ith, ira);
+                    const double ra = dra * ira + orpad, th = dth * ith + othpad, vv = v[c];
+                    double lap = 0.;
+                    if (ira >= NOPA && ira < nrapad - NOPA && iph >= NOPA && iph < nphpad - NOPA && ith >= NOPA &&
+                        ith < nthpad - NOPA) {
+                        const double pra = (po[c + 1] - po[c - 1]) / (2 * dra);
+                        const double ppra = (po[c + 1] - 2 * po[c] + po[c - 1]) / (dra * dra);
+                        const double pth = (po[c + st] - po[c - st]) / (2 * dth);
+                        const double ppth = (po[c + st] - 2 * po[c] + po[c - st]) / (dth * dth);
+                        const double ppph = (po[c + sp] - 2 * po[c] + po[c - sp]) / (dph * dph);
+                        lap = (2 / ra) * pra + ppra + (cos(th) / (ra * ra * sin(th))) * pth + (1 / (ra * ra)) * ppth +
+                              (1 / (ra * ra * sin(th) * sin(th))) * ppph;
+                    }
+                    fpo[c] = (dt * dt) * (vv * vv) * lap + 2 * po[c] - ppo[c];
+                }
+        double *t = ppo;
+        ppo = po;
+        po = fpo;
+        fpo = t;
+        for (int iph = 0; iph < nphpad; iph++)
+            for (int ith = 0; ith < nthpad; ith++)
+                for (int ira = 0; ira < nrapad; ira++) {
+                    int i = sponge_i(ira, nrapad, iph, nphpad, ith, nthpad, nb);
+                    size_t c = CS(iph, ith, ira);
+                    if (i) {
+                        po[c] *= tab[i];
+                        ppo[c] *= tab[i];
+                    }
+                    if (P->fsrf && ira > nrapad - nb) po[c] = 0;
+                }
+        if (P->fsrf)
+            for (size_t line = 0; line + 1 < (size_t)nthpad * nphpad; line++)
+                for (int k = 0; k < 8 * ((nrapad + 7) / 8) - nrapad; k++) po[(line + 1) * nrapad + k] = 0;
+        for (int r = 0; r < nr; r++) {
+            const glint *c = &cr[r];
+            size_t b = CS(c->jy, c->jz, c->jx);
+            double acc = 0;
+            for (int k = 0; k < 8; k++) acc += po[b + off[k]] * c->w[k];
+            dat[(size_t)it * nr + r] = acc;
+        }
+    }
+#undef CS
+    free(v);
+    free(po);
+    free(ppo);
+    free(fpo);
+    free(cs);
+    free(cr);
+    return 0;
+}
+
 int orc_gpu_forward(int kind, const orc_gpar *P, const float *vel, const float *rfl, const float *wav, int ns,
                     const float *sou, int nr, const float *rec, float *dat, float *snaps) {
     switch (kind) {

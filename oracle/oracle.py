@@ -87,6 +87,9 @@ def lib(fp64: bool = False):
         L.orc_cart_padded.argtypes = [C.POINTER(Par)] + [C.POINTER(C.c_int)] * 4
         L.orc_gpu_forward.argtypes = [C.c_int, C.POINTER(GPar), fp, fp, fp, C.c_int, fp, C.c_int, fp, fp, fp]
         L.orc_gpu_forward.restype = C.c_int
+        L.orc_gpu_spher3d_fp64.argtypes = [C.POINTER(GPar), fp, fp, C.c_int, fp, C.c_int, fp,
+                                           C.POINTER(C.c_double)]
+        L.orc_gpu_spher3d_fp64.restype = C.c_int
         L.orc_cart3d_cpu_steps.argtypes = [C.c_int] * 6
         L.orc_cart3d_cpu_steps.restype = C.c_double
         _libs[name] = L
@@ -283,3 +286,26 @@ def misfit_gradient(p: dict, vel, wav, sou, rec, dobs, jdata: int = 1, m=None, c
     if rc != 0:
         raise ValueError("orc_grad rejected the parameters")
     return grad, J.value, dsyn
+
+
+def spher3d_fp64(p: dict, vel, wav, sou, rec):
+    """Traces [nt][nr] (float64) of the spherical GPU-program scheme with FP64
+    wavefields; p as for gpu_scheme."""
+    q = GPar()
+    q.n1, q.n2, q.n3 = p["n"]
+    q.d1, q.d2, q.d3 = p["d"]
+    q.o1, q.o2, q.o3 = p["o"]
+    q.nb, q.nt, q.dt = p["nb"], p["nt"], p["dt"]
+    q.jdata, q.jsnap, q.bnds = 1, 0, 0
+    q.fsrf, q.expl, q.refl = int(p.get("fsrf", 0)), int(p.get("expl", 0)), 0
+    vel = np.ascontiguousarray(vel, np.float32)
+    wav = np.ascontiguousarray(wav, np.float32)
+    sou = np.ascontiguousarray(sou, np.float32).reshape(-1, 3)
+    rec = np.ascontiguousarray(rec, np.float32).reshape(-1, 3)
+    dat = np.zeros((q.nt, rec.shape[0]), np.float64)
+    rc = lib().orc_gpu_spher3d_fp64(C.byref(q), _fp(vel), _fp(wav), sou.shape[0], _fp(sou), rec.shape[0], _fp(rec),
+                                    dat.ctypes.data_as(C.POINTER(C.c_double)))
+    if rc != 0:
+        raise ValueError("orc_gpu_spher3d_fp64 failed")
+    return dat
+

@@ -1,0 +1,96 @@
+"""FP32 error of each configuration against an FP64 CPU run of the same
+scheme (the engine's AWE_FAST traces against liboracle64 / the FP64
+spherical restatement).  Sizes: the 2D configuration in full (512^2, nt=4000);
+the 3D and spherical ones on reduced grids a CPU finishes in seconds.  The
+errors are printed (pytest -s) and bounded."""
+import numpy as np
+import pytest
+
+from helpers import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _report(name, err):
+    print("\nFP64_ERROR %s rel_l2=%.3e" % (name, err))
+
+
+def test_2d_full_config_against_fp64():
+    import bench
+    import wavefield_imaging_gb300 as awe
+    from oracle import oracle
+
+    nz = nx = 512
+    nt = 4000
+    w3 = dict(n=(nz, nx, 1), d=(5.0, 5.0, 5.0), seed=1)
+    vel = bench.layered_model_3d(w3)[0]
+    wav = bench.ricker(nt, 0.005, 5.0)
+    sou = np.array([[0.5 * (nx - 1) * 5.0, 50.0]], np.float32)
+    rec = np.stack([np.arange(nx) * 5.0, np.full(nx, 50.0)], 1).astype(np.float32)
+    par = dict(n=[nz, nx], d=[5.0, 5.0], o=[0.0, 0.0], nb=40, nt=nt, dt=0.005, fdorder=8, dabc=1, expl=1,
+               nthreads=0)
+    desc = awe.make_desc(2, (nz, nx), (5.0, 5.0), (0.0, 0.0), nt, 0.005, nb=40, fdorder=8, dabc=1, expl=1,
+                         precision=awe.FAST)
+    with awe.Plan(desc) as p:
+        p.set_model(vel)
+        p.set_geometry(sou, rec)
+        dat = p.forward(wav)
+    ref, _ = oracle.cart_cpu(par, vel, wav, sou, rec, fp64=True)
+    err = rel_l2(dat, ref)
+    _report("2D 512^2 nt=4000 8th order (c0/c1/c2 grid)", err)
+    assert err <= 1e-3
+
+
+def test_3d_reduced_config_against_fp64():
+    import bench
+    import wavefield_imaging_gb300 as awe
+    from oracle import oracle
+
+    w = bench.workload(300, 96)
+    w["nb"] = 16
+    vel = bench.layered_model_3d(w)
+    sou, rec = bench.geometry(w)
+    rec = rec[::64]
+    wav = bench.ricker(w["nt"], w["dt"], w["f0"])
+    par = dict(n=list(w["n"]), d=list(w["d"]), o=list(w["o"]), nb=16, nt=w["nt"], dt=w["dt"], fdorder=8, dabc=1,
+               expl=1)
+    desc = awe.make_desc(3, w["n"], w["d"], w["o"], w["nt"], w["dt"], nb=16, fdorder=8, dabc=1, expl=1,
+                         precision=awe.FAST)
+    with awe.Plan(desc) as p:
+        assert p.step_kernel == "tma3d"
+        p.set_model(vel)
+        p.set_geometry(sou, rec)
+        dat = p.forward(wav)
+    ref, _ = oracle.cart_cpu(par, vel, wav, sou, rec, fp64=True)
+    err = rel_l2(dat, ref)
+    _report("3D 96^3 nt=300 8th order, TMA kernel (c3 scheme)", err)
+    assert err <= 1e-3
+
+
+def test_spherical_reduced_config_against_fp64():
+    import bench
+    import wavefield_imaging_gb300 as awe
+    from oracle import oracle
+
+    w = bench.spher_workload(300, nr=120, nang=48)
+    w["nb"] = 10
+    w["d"] = (0.005, 0.04 / 512, 0.04 / 512)
+    vel = bench.spher_model(w)
+    nr_, nth, nph = w["n"]
+    rs = 3387.0 + 0.6 * nr_ * 0.005
+    th0 = w["o"][1] + 0.5 * (nth - 1) * w["d"][1]
+    ph0 = w["o"][2] + 0.5 * (nph - 1) * w["d"][2]
+    sou = np.array([[rs, ph0, th0]], np.float32)
+    rec = np.array([[rs + 0.02, ph0 + k * w["d"][2], th0] for k in range(-12, 13, 3)], np.float32)
+    wav = bench.ricker(w["nt"], w["dt"], w["f0"])
+    par = dict(n=list(w["n"]), d=list(w["d"]), o=list(w["o"]), nb=10, nt=w["nt"], dt=w["dt"])
+    desc = awe.make_desc(3, w["n"], w["d"], w["o"], w["nt"], w["dt"], coords=awe.SPHER, scheme=awe.SCHEME_GPU,
+                         nb=10, precision=awe.FAST)
+    with awe.Plan(desc) as p:
+        p.set_model(vel)
+        p.set_geometry(sou, rec)
+        dat = p.forward(wav)
+    ref = oracle.spher3d_fp64(par, vel, wav, sou, rec)
+    err = rel_l2(dat, ref)
+    _report("spherical shell 120x48x48 nt=300 (c4 scheme)", err)
+    assert err <= 1e-3

@@ -31,6 +31,14 @@ using namespace awe;
 
 namespace awe {
 
+void plan_graph_drop(awe_plan *p) {
+    if (p->gexec) cudaGraphExecDestroy(p->gexec);
+    p->gexec = nullptr;
+    p->g_wav = nullptr;
+    p->g_dat = nullptr;
+    p->g_ncs = 0;
+}
+
 awe_status dev_alloc(awe_plan *p, void **ptr, size_t bytes) {
     if (bytes == 0) bytes = 16;
     cudaError_t e = cudaMalloc(ptr, bytes);
@@ -223,6 +231,7 @@ awe_status awe_plan_destroy(awe_plan *p) {
     if (!p) return AWE_OK;
     cudaSetDevice(p->device);
     if (p->stream) cudaStreamSynchronize(p->stream);
+    plan_graph_drop(p);
     plan_gradient_free(p);
     for (auto &a : p->allocs) cudaFree(a.first);
     p->allocs.clear();
@@ -255,6 +264,7 @@ awe_status awe_set_model(awe_plan *p, const float *vel, const float *den, const 
         set_error("null plan or velocity");
         return AWE_ERR_INVALID;
     }
+    plan_graph_drop(p);  // the captured time loop baked in the old state
     CUDA_TRY(cudaSetDevice(p->device));
     awe_status st = (p->d.scheme == AWE_SCHEME_CPU) ? planB_model(p, vel, den) : planA_model(p, vel, rfl);
     if (st == AWE_OK) p->model_set = true;
@@ -266,6 +276,7 @@ awe_status awe_set_geometry(awe_plan *p, int ns, const float *sou, int nr, const
         set_error("bad geometry arguments");
         return AWE_ERR_INVALID;
     }
+    plan_graph_drop(p);  // the captured time loop baked in the old state
     CUDA_TRY(cudaSetDevice(p->device));
     awe_status st = set_geometry_common(p, ns, sou, nr, rec);
     if (st == AWE_OK) p->geom_set = true;
@@ -277,6 +288,7 @@ awe_status awe_set_shots(awe_plan *p, int nshots, const int *ns, const float *so
         set_error("bad shot arguments");
         return AWE_ERR_INVALID;
     }
+    plan_graph_drop(p);  // the captured time loop baked in the old state
     const awe_desc &d = p->d;
     if (nshots > 1 && !(d.scheme == AWE_SCHEME_GPU && d.coords == AWE_SPHER && d.ndim == 3 &&
                         d.precision == AWE_FAST && d.jsnap == 0)) {
@@ -326,6 +338,7 @@ awe_status awe_set_snapshot_callback(awe_plan *p, awe_snap_fn fn, void *user) {
         set_error("null plan");
         return AWE_ERR_INVALID;
     }
+    plan_graph_drop(p);  // the captured time loop baked in the old state
     p->snap_cb = fn;
     p->snap_user = user;
     return AWE_OK;
@@ -342,6 +355,7 @@ long long awe_last_launch_count(const awe_plan *p) { return p ? p->launches : -1
 
 awe_status awe_profile_enable(awe_plan *p, int on) {
     if (!p) return AWE_ERR_INVALID;
+    plan_graph_drop(p);  // profiled runs bracket kernels with host-side events: no graph
     p->profile = on != 0;
     p->prof_n = 0;
     return AWE_OK;
@@ -378,8 +392,42 @@ awe_status awe_forward_device(awe_plan *p, const float *d_wav, int ncs, float *d
     }
     CUDA_TRY(cudaSetDevice(p->device));
     cudaStream_t s = stream ? (cudaStream_t)stream : p->stream;
-    awe_status st = (p->d.scheme == AWE_SCHEME_CPU) ? planB_run(p, d_wav, ncs, d_dat, d_wfl, s)
-                                                     : planA_run(p, d_wav, ncs, d_dat, d_wfl, s);
+    // the CPU-program scheme's loop is pure stream work without snapshots and
+    // profiling: capture it once as a CUDA graph and replay it (one launch per
+    // run instead of several per time step - what matters for small 2D grids)
+    const bool graph = p->d.scheme == AWE_SCHEME_CPU && !(p->nsnap > 0 && (d_wfl || p->snap_cb)) && !p->profile;
+    awe_status st = AWE_OK;
+    if (graph) {
+        if (!p->gexec || p->g_wav != d_wav || p->g_dat != d_dat || p->g_ncs != ncs) {
+            plan_graph_drop(p);
+            cudaStream_t cs;
+            CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+            cudaGraph_t gr = nullptr;
+            cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                st = planB_run(p, d_wav, ncs, d_dat, nullptr, cs);
+                e = cudaStreamEndCapture(cs, &gr);
+            }
+            if (st == AWE_OK && e == cudaSuccess) e = cudaGraphInstantiate(&p->gexec, gr, 0);
+            if (gr) cudaGraphDestroy(gr);
+            cudaStreamDestroy(cs);
+            if (st != AWE_OK) return st;
+            if (e != cudaSuccess) {
+                plan_graph_drop(p);
+                set_error("CUDA graph capture of the time loop failed: %s", cudaGetErrorString(e));
+                return AWE_ERR_CUDA;
+            }
+            p->g_wav = d_wav;
+            p->g_dat = d_dat;
+            p->g_ncs = ncs;
+            p->g_launches = p->launches;
+        }
+        CUDA_TRY(cudaGraphLaunch(p->gexec, s));
+        p->launches = p->g_launches;
+    } else {
+        st = (p->d.scheme == AWE_SCHEME_CPU) ? planB_run(p, d_wav, ncs, d_dat, d_wfl, s)
+                                             : planA_run(p, d_wav, ncs, d_dat, d_wfl, s);
+    }
     if (st != AWE_OK) return st;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -401,9 +449,20 @@ awe_status awe_forward(awe_plan *p, const float *wav, int ncs, float *dat, float
     CUDA_TRY(cudaSetDevice(p->device));
     const size_t wav_bytes = (size_t)p->d.nt * ncs * sizeof(float);
     const size_t dat_bytes = (size_t)p->nsmp * p->nr * sizeof(float);
-    float *d_wav = nullptr, *d_dat = nullptr, *d_wfl = nullptr;
-    awe_status st = dev_alloc(p, (void **)&d_wav, wav_bytes);
-    if (st == AWE_OK) st = dev_alloc(p, (void **)&d_dat, dat_bytes);
+    // staging buffers kept across calls (stable pointers keep the captured time loop valid)
+    awe_status st = AWE_OK;
+    auto stage = [&](float **buf, size_t &have, size_t need) {
+        if (have >= need && *buf) return AWE_OK;
+        dev_free(p, *buf);
+        *buf = nullptr;
+        have = 0;
+        awe_status r = dev_alloc(p, (void **)buf, need);
+        if (r == AWE_OK) have = need;
+        return r;
+    };
+    st = stage(&p->stage_wav, p->stage_wav_bytes, wav_bytes);
+    if (st == AWE_OK) st = stage(&p->stage_dat, p->stage_dat_bytes, dat_bytes);
+    float *d_wav = p->stage_wav, *d_dat = p->stage_dat, *d_wfl = nullptr;
     if (st == AWE_OK && wfl && p->nsnap > 0) st = dev_alloc(p, (void **)&d_wfl, p->nsnap * p->snap_elems * sizeof(float));
     if (st == AWE_OK) {
         cudaError_t e = cudaMemcpyAsync(d_wav, wav, wav_bytes, cudaMemcpyHostToDevice, p->stream);
@@ -425,8 +484,6 @@ awe_status awe_forward(awe_plan *p, const float *wav, int ncs, float *dat, float
         }
     }
     cudaStreamSynchronize(p->stream);
-    dev_free(p, d_wav);
-    dev_free(p, d_dat);
     dev_free(p, d_wfl);
     if (st == AWE_OK) st = check_pipeline(p);
     return st;

@@ -72,6 +72,16 @@ struct awe_plan {
     unsigned long long sched_base = 0;
     int *d_err = nullptr;
 
+    // the forward time loop captured as a CUDA graph (CPU-program scheme, no
+    // snapshots, no profiling), replayed while its device pointers stay the same
+    cudaGraphExec_t gexec = nullptr;
+    const float *g_wav = nullptr;
+    float *g_dat = nullptr;
+    int g_ncs = 0;
+    long long g_launches = 0;
+    float *stage_wav = nullptr, *stage_dat = nullptr;  // awe_forward's device staging buffers
+    size_t stage_wav_bytes = 0, stage_dat_bytes = 0;
+
     // misfit gradient state (allocated by the first awe_gradient call)
     awe::GradState *grad = nullptr;
 
@@ -83,6 +93,8 @@ struct awe_plan {
 
 namespace awe {
 awe_status dev_alloc(awe_plan *p, void **ptr, size_t bytes);
+// forget the captured time loop (the model, geometry or buffers it baked in changed)
+void plan_graph_drop(awe_plan *p);
 void dev_free(awe_plan *p, void *ptr);
 awe_status deliver_snapshot(awe_plan *p, const float *d_frame, int isnap, int it, cudaStream_t s);
 

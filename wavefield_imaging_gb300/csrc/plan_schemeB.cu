@@ -354,6 +354,10 @@ awe_status planB_run_hooked(awe_plan *p, const float *d_wav, int ncs, float *d_d
 
     CUDA_TRY(cudaMemsetAsync(p->u[0], 0, bytes, s));
     CUDA_TRY(cudaMemsetAsync(p->u[1], 0, bytes, s));
+    if (p->use_tma) {  // the TMA kernel's work counter restarts with every run (graph replays included)
+        CUDA_TRY(cudaMemsetAsync(p->sched_counter, 0, sizeof(unsigned long long), s));
+        p->sched_base = 0;
+    }
     if (p->nsnap > 0 && !d_wfl && p->snap_cb && !p->d_snap_tmp)
         AWE_TRY(dev_alloc(p, (void **)&p->d_snap_tmp, p->snap_elems * sizeof(float)));
 
