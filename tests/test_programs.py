@@ -106,9 +106,11 @@ def _run_bare(bindir, name, args):
                           timeout=60)
 
 
-@pytest.mark.parametrize("arg,msg", [("adj=y", "adj=y"), ("sinc=y", "sinc=y"), ("nqz=10", "snapshot windows")])
-def test_unsupported_options_stop_with_an_error(bindir, arg, msg):
-    r = _run_bare(bindir, "sfAWEFDcart2Dcpu", [arg])
+@pytest.mark.parametrize("name,arg,msg", [("sfAWEFDcart2Dgpu", "adj=y", "adj=y"),
+                                          ("sfAWEFDcart2Dcpu", "sinc=y", "sinc=y"),
+                                          ("sfAWEFDcart2Dcpu", "nqz=10", "snapshot windows")])
+def test_unsupported_options_stop_with_an_error(bindir, name, arg, msg):
+    r = _run_bare(bindir, name, [arg])
     assert r.returncode == 1
     assert msg in r.stderr.decode()
 
@@ -124,3 +126,32 @@ def test_every_program_name_is_installed(bindir):
         assert os.access(os.path.join(bindir, name), os.X_OK), name
     r = _run_bare(bindir, "awe_prog", [])
     assert r.returncode == 1
+
+
+@pytest.mark.gpu
+def test_cpu_program_adjoint_back_injection_image(bindir, tmp_path):
+    """adj=y: the traces on standard input go back into the model at the
+    receivers, reversed in time; the image is the wavefield at step nt-kt.
+    Checked bit for bit (precision=exact) against the oracle run with the same
+    back-injection (sources at the receivers, reversed traces, snapshot at
+    nt-kt)."""
+    from oracle import oracle
+
+    par, a = load_golden(golden_paths("c2d_o8_sponge.npz")[0])
+    nt, kt = par["nt"], 40
+    data = a["dat"]  # [nt][nr] traces of the golden run, used as the recorded data
+    nd = len(par["n"])
+    rsf.write(str(tmp_path / "vel.rsf"), a["vel"], [(n, o, d) for n, o, d in zip(par["n"], par["o"], par["d"])])
+    rsf.write(str(tmp_path / "sou.rsf"), a["sou"], [(nd, 0.0, 1.0), (a["sou"].shape[0], 0.0, 1.0)])
+    rsf.write(str(tmp_path / "rec.rsf"), a["rec"], [(nd, 0.0, 1.0), (a["rec"].shape[0], 0.0, 1.0)])
+    rsf.write(str(tmp_path / "wav.rsf"), data, [(data.shape[1], 0.0, 1.0), (nt, 0.0, par["dt"])])
+    args = ["vel=" + str(tmp_path / "vel.rsf"), "sou=" + str(tmp_path / "sou.rsf"), "rec=" + str(tmp_path / "rec.rsf"),
+            "adj=y", "kt=%d" % kt, "expl=n", "fdorder=8", "dabc=y", "nb=%d" % par["nb"], "precision=exact"]
+    out = run_program(bindir, "sfAWEFDcart2Dcpu", tmp_path, args)
+    img, hdr = rsf.read(str(out))
+    assert (int(hdr["n1"]), int(hdr["n2"])) == (par["n"][0], par["n"][1])
+    steps = nt - kt + 1
+    back = np.ascontiguousarray(data[::-1][:steps])
+    p2 = dict(par, nt=steps, jsnap=nt - kt, expl=0, bnds=0)
+    _, snaps = oracle.cart_cpu(p2, a["vel"], back, a["rec"], a["rec"][:1])
+    np.testing.assert_array_equal(img.ravel(), snaps[-1].ravel())

@@ -29,6 +29,12 @@ using namespace awe;
         }                                                                                         \
     } while (0)
 
+#define AWE_TRY_SNAP(expr)           \
+    do {                             \
+        awe_status s_ = (expr);      \
+        if (s_ != AWE_OK) return s_; \
+    } while (0)
+
 namespace awe {
 
 void plan_graph_drop(awe_plan *p) {
@@ -62,25 +68,47 @@ void dev_free(awe_plan *p, void *ptr) {
     cudaFree(ptr);
 }
 
-// Copy one snapshot frame to the host and hand it to the callback.
+// Snapshot frames stream to the callback through two pinned host buffers:
+// frame k is copied (cudaMemcpyAsync, event) while the host hands frame k-1,
+// whose copy finished long before, to the callback - the host never waits on
+// the GPU for the frame it just queued, and the GPU never waits on the
+// callback (disk writes overlap the following time steps).
+static awe_status snap_deliver_pending(awe_plan *p) {
+    if (p->snap_pending < 0) return AWE_OK;
+    const int b = p->snap_pending_isnap & 1;
+    CUDA_TRY(cudaEventSynchronize(p->snap_ev[b]));
+    p->snap_cb(p->snap_user, p->snap_pending_isnap, p->snap_pending_it, p->snap_host[b], p->snap_elems);
+    p->snap_pending = -1;
+    return AWE_OK;
+}
+
 awe_status deliver_snapshot(awe_plan *p, const float *d_frame, int isnap, int it, cudaStream_t s) {
     if (!p->snap_cb) return AWE_OK;
     const size_t bytes = p->snap_elems * sizeof(float);
-    if (p->h_pinned_bytes < bytes) {
-        if (p->h_pinned) cudaFreeHost(p->h_pinned);
-        p->h_pinned = nullptr;
-        p->h_pinned_bytes = 0;
-        if (cudaMallocHost((void **)&p->h_pinned, bytes) != cudaSuccess) {
-            set_error("pinned snapshot buffer (%zu bytes) failed", bytes);
-            return AWE_ERR_NOMEM;
+    if (p->snap_host_bytes < bytes) {
+        AWE_TRY_SNAP(snap_deliver_pending(p));
+        for (int b = 0; b < 2; b++) {
+            if (p->snap_host[b]) cudaFreeHost(p->snap_host[b]);
+            p->snap_host[b] = nullptr;
+            if (cudaMallocHost((void **)&p->snap_host[b], bytes) != cudaSuccess) {
+                set_error("pinned snapshot buffers (2 x %zu bytes) failed", bytes);
+                return AWE_ERR_NOMEM;
+            }
+            if (!p->snap_ev[b]) CUDA_TRY(cudaEventCreateWithFlags(&p->snap_ev[b], cudaEventDisableTiming));
         }
-        p->h_pinned_bytes = bytes;
+        p->snap_host_bytes = bytes;
     }
-    CUDA_TRY(cudaMemcpyAsync(p->h_pinned, d_frame, bytes, cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(cudaStreamSynchronize(s));
-    p->snap_cb(p->snap_user, isnap, it, p->h_pinned, p->snap_elems);
+    const int b = isnap & 1;
+    CUDA_TRY(cudaMemcpyAsync(p->snap_host[b], d_frame, bytes, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaEventRecord(p->snap_ev[b], s));
+    AWE_TRY_SNAP(snap_deliver_pending(p));
+    p->snap_pending = 1;
+    p->snap_pending_isnap = isnap;
+    p->snap_pending_it = it;
     return AWE_OK;
 }
+
+awe_status flush_snapshots(awe_plan *p) { return p->snap_cb ? snap_deliver_pending(p) : AWE_OK; }
 
 void prof_begin(awe_plan *p, cudaStream_t s) {
     if (!p->profile) return;
@@ -235,7 +263,10 @@ awe_status awe_plan_destroy(awe_plan *p) {
     plan_gradient_free(p);
     for (auto &a : p->allocs) cudaFree(a.first);
     p->allocs.clear();
-    if (p->h_pinned) cudaFreeHost(p->h_pinned);
+    for (int b = 0; b < 2; b++) {
+        if (p->snap_host[b]) cudaFreeHost(p->snap_host[b]);
+        if (p->snap_ev[b]) cudaEventDestroy(p->snap_ev[b]);
+    }
     for (cudaEvent_t e : p->prof_ev) cudaEventDestroy(e);
     if (p->stream) cudaStreamDestroy(p->stream);
     delete p;

@@ -59,8 +59,10 @@ struct awe_plan {
     bool model_set = false, geom_set = false;
     awe_snap_fn snap_cb = nullptr;
     void *snap_user = nullptr;
-    float *h_pinned = nullptr;
-    size_t h_pinned_bytes = 0;
+    float *snap_host[2] = {nullptr, nullptr};  // pinned frame buffers (double-buffered delivery)
+    size_t snap_host_bytes = 0;
+    cudaEvent_t snap_ev[2] = {nullptr, nullptr};
+    int snap_pending = -1, snap_pending_isnap = 0, snap_pending_it = 0;
     float *d_snap_tmp = nullptr;
     long long launches = 0;
 
@@ -97,6 +99,8 @@ awe_status dev_alloc(awe_plan *p, void **ptr, size_t bytes);
 void plan_graph_drop(awe_plan *p);
 void dev_free(awe_plan *p, void *ptr);
 awe_status deliver_snapshot(awe_plan *p, const float *d_frame, int isnap, int it, cudaStream_t s);
+// hand the last queued frame to the callback (end of a run)
+awe_status flush_snapshots(awe_plan *p);
 
 awe_status set_geometry_common(awe_plan *p, int ns, const float *sou, int nr, const float *rec);
 

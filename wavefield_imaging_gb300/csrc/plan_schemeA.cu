@@ -332,6 +332,7 @@ awe_status planA_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, flo
     CUDA_TRY(cudaMemsetAsync(d_dat, 0, (size_t)p->nsmp * p->nr * sizeof(float), s));
     if (p->nsnap > 0 && !d_wfl && p->snap_cb && !p->d_snap_tmp)
         AWE_TRY(dev_alloc(p, (void **)&p->d_snap_tmp, p->snap_elems * sizeof(float)));
+    p->snap_pending = -1;  // a frame left queued by a failed run is not delivered
 
     const int jdata = d.jdata > 0 ? d.jdata : 1;
     long long launches = 0;
@@ -383,7 +384,7 @@ awe_status planA_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, flo
         }
     }
     p->launches = launches;
-    return AWE_OK;
+    return flush_snapshots(p);
 }
 
 }  // namespace awe

@@ -360,6 +360,7 @@ awe_status planB_run_hooked(awe_plan *p, const float *d_wav, int ncs, float *d_d
     }
     if (p->nsnap > 0 && !d_wfl && p->snap_cb && !p->d_snap_tmp)
         AWE_TRY(dev_alloc(p, (void **)&p->d_snap_tmp, p->snap_elems * sizeof(float)));
+    p->snap_pending = -1;  // a frame left queued by a failed run is not delivered
 
     const StepBParams sp = stepB_params(p);
     const float *pw1 = sponge ? p->w[0] : nullptr;
@@ -391,7 +392,7 @@ awe_status planB_run_hooked(awe_plan *p, const float *d_wav, int ncs, float *d_d
         }
     }
     p->launches = launches;
-    return AWE_OK;
+    return flush_snapshots(p);
 }
 
 }  // namespace awe

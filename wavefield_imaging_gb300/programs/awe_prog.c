@@ -13,8 +13,16 @@
  * Parameters and defaults are those of each program's main() (cited below).
  * Extra parameter: precision=exact|fast (default fast; exact reproduces the
  * reference's float/double evaluation bit for bit).
- * Not provided: adj=y back-injection, sinc=y injection and the snapshot
- * windows nq*=/oq*=/dq*= of the cpu programs (they stop with an error).
+ * adj=y (cpu programs, expl=n): the data on standard input ([nt][nr]) are
+ * injected backwards in time at the receivers (MAWEFDcart2Dcpu.c:304-315)
+ * and the wavefield at step nt-kt, cut to the model, is written to standard
+ * output as the image (:353-369); the reference writes its traces to the same
+ * file before the image and leaves the image axes unset without snap=y,
+ * here the output holds the image alone.
+ * Not provided: adj=y for the gpu programs (their back-injection indexes the
+ * source weight tables with receiver indices, MAWEFDcart2Dgpu.cu:391-394),
+ * sinc=y injection and the snapshot windows nq*=/oq*=/dq*= of the cpu
+ * programs (they stop with an error).
  * Header differences: sfAWEFDspher3Dgpu's data and wavefield headers hold
  * the rows and frames actually written (the reference declares nt/jdata rows
  * and one frame more than it writes).
@@ -33,11 +41,16 @@ static void die(const char *what, const char *msg) {
 }
 
 static rsf_file *g_wfl = NULL;
+static float *g_image = NULL;  /* adj=y: the last frame */
 
 static void write_frame(void *user, int isnap, int it, const float *frame, size_t n) {
     (void)user;
     (void)isnap;
     (void)it;
+    if (g_image) {
+        memcpy(g_image, frame, n * sizeof(float));
+        return;
+    }
     if (rsf_write(g_wfl, frame, n) != n) die("wfl", "short write");
 }
 
@@ -74,7 +87,8 @@ int main(int argc, char **argv) {
     rsf_get_bool("adj", &adj);
     rsf_get_bool("verb", &verb);
     rsf_get_bool("sinc", &sinc);
-    if (adj) die(prog, "adj=y (back-injection imaging) is not provided");
+    if (adj && scheme != AWE_SCHEME_CPU) die(prog, "adj=y (back-injection imaging) is provided for the cpu programs");
+    if (adj && expl) die(prog, "adj=y needs expl=n (one trace per receiver)");
     if (sinc) die(prog, "sinc=y injection is not provided");
     {
         static const char *win[] = {"nqz", "nqx", "nqy", "oqz", "oqx", "oqy", "dqz", "dqx", "dqy"};
@@ -172,7 +186,42 @@ int main(int argc, char **argv) {
      * value per source per step (expl=n) or one for all (expl=y) */
     int wcs = 1;
     if (scheme == AWE_SCHEME_CPU && !expl) wcs = ns;
-    if (wcs > ncs && nwav < (size_t)nt * wcs) die(prog, "wavelet has fewer components than sources");
+    if (!adj && wcs > ncs && nwav < (size_t)nt * wcs) die(prog, "wavelet has fewer components than sources");
+
+    if (adj) {
+        /* back-injection: sources at the receivers, traces reversed in time, the
+         * image is the snapshot of step nt-kt (window = the model) */
+        int kt = 0;
+        rsf_get_int("kt", &kt);
+        if (kt < 0 || kt >= nt) die(prog, "kt must be in [0, nt)");
+        if (ncs != nr) die(prog, "adj=y: standard input must hold one trace per receiver (n1 = nr)");
+        const int steps = nt - kt + 1;
+        float *bw = malloc(sizeof(float) * (size_t)steps * nr);
+        for (int it = 0; it < steps; it++)
+            memcpy(bw + (size_t)it * nr, wav + (size_t)(nt - 1 - it) * nr, sizeof(float) * nr);
+        d.nt = steps;
+        d.jsnap = nt - kt > 0 ? nt - kt : 1;
+        d.bnds = 0;
+        d.jdata = 1;
+        awe_plan *plan = NULL;
+        if (awe_plan_create(&d, gpu, &plan) != AWE_OK) die(prog, awe_last_error());
+        if (awe_set_model(plan, vel, den, NULL) != AWE_OK) die(prog, awe_last_error());
+        if (awe_set_geometry(plan, nr, rec, 0, NULL) != AWE_OK) die(prog, awe_last_error());
+        awe_info info;
+        awe_plan_info(plan, &info);
+        g_image = calloc(info.snap_elems, sizeof(float));
+        awe_set_snapshot_callback(plan, write_frame, NULL);
+        float *dat1 = malloc(sizeof(float) * ((size_t)info.nsmp + 1));
+        if (awe_forward(plan, bw, nr, dat1, NULL) != AWE_OK) die(prog, awe_last_error());
+        rsf_file *Fimg = rsf_output("out");
+        if (!Fimg) die(prog, rsf_error());
+        const char *lab[3] = {"z", "x", "y"};
+        for (int a = 0; a < ndim; a++) rsf_set_axis(Fimg, a + 1, d.n[a], d.o[a], d.d[a], lab[a]);
+        if (rsf_write(Fimg, g_image, info.snap_elems) != info.snap_elems) die(prog, "short write (image)");
+        rsf_close(Fimg);
+        awe_plan_destroy(plan);
+        return 0;
+    }
 
     awe_plan *plan = NULL;
     if (awe_plan_create(&d, gpu, &plan) != AWE_OK) die(prog, awe_last_error());
