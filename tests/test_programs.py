@@ -155,3 +155,58 @@ def test_cpu_program_adjoint_back_injection_image(bindir, tmp_path):
     p2 = dict(par, nt=steps, jsnap=nt - kt, expl=0, bnds=0)
     _, snaps = oracle.cart_cpu(p2, a["vel"], back, a["rec"], a["rec"][:1])
     np.testing.assert_array_equal(img.ravel(), snaps[-1].ravel())
+
+
+@pytest.mark.gpu
+def test_cpu_program_adjoint_expl_snapshots(bindir, tmp_path):
+    """sfAWEFDcart2Dcpu adj=y expl=y snap=y bnds=y: the one-component wavelet,
+    reversed in time, goes in at the sources; the padded frames of the steps
+    it % jsnap == 0 up to the image step go to wfl and the image is the model
+    window of step nt-kt (here not a multiple of jsnap, so the engine delivers
+    every frame).  Bit for bit against the oracle."""
+    from oracle import oracle
+
+    par, a = load_golden(golden_paths("c2d_o8_sponge.npz")[0])
+    nt, kt, jsnap = par["nt"], 37, 11
+    args = write_inputs(tmp_path, par, a)
+    args += ["adj=y", "kt=%d" % kt, "expl=y", "snap=y", "bnds=y", "jsnap=%d" % jsnap, "fdorder=8", "dabc=y",
+             "nb=%d" % par["nb"], "precision=exact"]
+    out = run_program(bindir, "sfAWEFDcart2Dcpu", tmp_path, args)
+    img, hdr = rsf.read(str(out))
+    wfl, whdr = rsf.read(str(tmp_path / "wfl.rsf"))
+    img_it = nt - kt
+    assert img_it % jsnap != 0
+    steps = img_it + 1
+    back = np.ascontiguousarray(a["wav"][::-1][:steps])
+    _, frames = oracle.cart_cpu(dict(par, nt=steps, jsnap=jsnap, expl=1, bnds=1), a["vel"], back, a["sou"],
+                                a["rec"][:1])
+    assert int(whdr["n3"]) == frames.shape[0] == img_it // jsnap + 1
+    np.testing.assert_array_equal(wfl.ravel(), frames.ravel())
+    _, last = oracle.cart_cpu(dict(par, nt=steps, jsnap=img_it, expl=1, bnds=0), a["vel"], back, a["sou"],
+                              a["rec"][:1])
+    assert (int(hdr["n1"]), int(hdr["n2"])) == (par["n"][0], par["n"][1])
+    np.testing.assert_array_equal(img.ravel(), last[-1].ravel())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fixture", ["c3d_o8_sponge.npz", "c3d_o4_free_den.npz"])
+def test_cpu3d_program_adjoint_is_reversed_forward(bindir, tmp_path, fixture):
+    """sfAWEFDcart3Dcpu adj=y injects the wavelet reversed in time at the
+    sources and otherwise runs as forward (traces on standard output): the
+    outputs equal those of adj=n on the reversed wavelet, bit for bit."""
+    par, a = load_golden(golden_paths(fixture)[0])
+    common = ["expl=%s" % yn(par["expl"]), "fdorder=%d" % par["fdorder"], "dabc=%s" % yn(par["dabc"]),
+              "free=%s" % yn(par["fsrf"]), "nb=%d" % par["nb"], "precision=exact"]
+    fwd_dir, adj_dir = tmp_path / "fwd", tmp_path / "adj"
+    fwd_dir.mkdir()
+    adj_dir.mkdir()
+    args = write_inputs(adj_dir, par, a) + common
+    adj_out = run_program(bindir, "sfAWEFDcart3Dcpu", adj_dir, args + ["adj=y"])
+    rev = dict(a, wav=np.ascontiguousarray(a["wav"][::-1]))
+    args = write_inputs(fwd_dir, par, rev) + common
+    fwd_out = run_program(bindir, "sfAWEFDcart3Dcpu", fwd_dir, args)
+    d_adj, h_adj = rsf.read(str(adj_out))
+    d_fwd, h_fwd = rsf.read(str(fwd_out))
+    assert int(h_adj["n2"]) == par["nt"]
+    np.testing.assert_array_equal(d_adj, d_fwd)
+    assert np.abs(d_adj).max() > 0

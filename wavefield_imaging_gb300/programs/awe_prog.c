@@ -13,19 +13,24 @@
  * Parameters and defaults are those of each program's main() (cited below).
  * Extra parameter: precision=exact|fast (default fast; exact reproduces the
  * reference's float/double evaluation bit for bit).
- * adj=y (cpu programs, expl=n): the data on standard input ([nt][nr]) are
- * injected backwards in time at the receivers (MAWEFDcart2Dcpu.c:304-315)
- * and the wavefield at step nt-kt, cut to the model, is written to standard
- * output as the image (:353-369); the reference writes its traces to the same
- * file before the image and leaves the image axes unset without snap=y,
- * here the output holds the image alone.
+ * adj=y (backward injection, cpu programs):
+ *   sfAWEFDcart2Dcpu (MAWEFDcart2Dcpu.c:304-316, :353-369): expl=n injects
+ *   the traces on standard input ([nt][nr]) at the receivers, expl=y the
+ *   one-component wavelet at the sources, both reversed in time; the run
+ *   stops after step nt-kt, whose wavefield (model window) is written to
+ *   standard output as the image (axes z, x); no traces are written.
+ *   kt=0 (the reference's default) never reaches the image step there and
+ *   writes no image, so kt must be in [1, nt] here.
+ *   sfAWEFDcart3Dcpu (MAWEFDcart3Dcpu.c:304-316): the wavelet reversed in
+ *   time is injected at the sources; traces and snapshots as in a forward run.
  * Not provided: adj=y for the gpu programs (their back-injection indexes the
  * source weight tables with receiver indices, MAWEFDcart2Dgpu.cu:391-394),
  * sinc=y injection and the snapshot windows nq*=/oq*=/dq*= of the cpu
  * programs (they stop with an error).
  * Header differences: sfAWEFDspher3Dgpu's data and wavefield headers hold
  * the rows and frames actually written (the reference declares nt/jdata rows
- * and one frame more than it writes).
+ * and one frame more than it writes), and so does sfAWEFDcart2Dcpu adj=y
+ * snap=y (the reference declares the frames of all nt steps).
  * Errors print to stderr and exit 1, as sf_error. */
 #include <libgen.h>
 #include <stdio.h>
@@ -41,15 +46,29 @@ static void die(const char *what, const char *msg) {
 }
 
 static rsf_file *g_wfl = NULL;
-static float *g_image = NULL;  /* adj=y: the last frame */
+
+/* 2D adj=y: the image is the frame of step img_it, cut from the padded
+ * frame when bnds=y; snapshot frames go to wfl every wfl_j steps (0: none) */
+static struct {
+    int img_it, wfl_j;
+    float *image;
+    int cut, nb, n1, n2, n1pad;
+} g_adj = {-1, 0, NULL, 0, 0, 0, 0, 0};
 
 static void write_frame(void *user, int isnap, int it, const float *frame, size_t n) {
     (void)user;
     (void)isnap;
-    (void)it;
-    if (g_image) {
-        memcpy(g_image, frame, n * sizeof(float));
-        return;
+    if (g_adj.img_it >= 0) {
+        if (it == g_adj.img_it) {
+            if (!g_adj.cut) {
+                memcpy(g_adj.image, frame, n * sizeof(float));
+            } else {
+                for (int i2 = 0; i2 < g_adj.n2; i2++)
+                    memcpy(g_adj.image + (size_t)i2 * g_adj.n1,
+                           frame + (size_t)(g_adj.nb + i2) * g_adj.n1pad + g_adj.nb, sizeof(float) * g_adj.n1);
+            }
+        }
+        if (g_adj.wfl_j == 0 || it % g_adj.wfl_j != 0) return;
     }
     if (rsf_write(g_wfl, frame, n) != n) die("wfl", "short write");
 }
@@ -88,7 +107,6 @@ int main(int argc, char **argv) {
     rsf_get_bool("verb", &verb);
     rsf_get_bool("sinc", &sinc);
     if (adj && scheme != AWE_SCHEME_CPU) die(prog, "adj=y (back-injection imaging) is provided for the cpu programs");
-    if (adj && expl) die(prog, "adj=y needs expl=n (one trace per receiver)");
     if (sinc) die(prog, "sinc=y injection is not provided");
     {
         static const char *win[] = {"nqz", "nqx", "nqy", "oqz", "oqx", "oqy", "dqz", "dqx", "dqy"};
@@ -188,53 +206,72 @@ int main(int argc, char **argv) {
     if (scheme == AWE_SCHEME_CPU && !expl) wcs = ns;
     if (!adj && wcs > ncs && nwav < (size_t)nt * wcs) die(prog, "wavelet has fewer components than sources");
 
+    /* adj=y: the injected series reversed in time.  The reference seeks to
+     * row nt-1-it of the input with the row length it reads: nr traces for
+     * the 2D program with expl=n, else the forward row length (ns, or 1 with
+     * expl=y). */
+    const int img2d = adj && ndim == 2;
+    const int user_jsnap = d.jsnap;
     if (adj) {
-        /* back-injection: sources at the receivers, traces reversed in time, the
-         * image is the snapshot of step nt-kt (window = the model) */
-        int kt = 0;
-        rsf_get_int("kt", &kt);
-        if (kt < 0 || kt >= nt) die(prog, "kt must be in [0, nt)");
-        if (ncs != nr) die(prog, "adj=y: standard input must hold one trace per receiver (n1 = nr)");
-        const int steps = nt - kt + 1;
-        float *bw = malloc(sizeof(float) * (size_t)steps * nr);
-        for (int it = 0; it < steps; it++)
-            memcpy(bw + (size_t)it * nr, wav + (size_t)(nt - 1 - it) * nr, sizeof(float) * nr);
-        d.nt = steps;
-        d.jsnap = nt - kt > 0 ? nt - kt : 1;
-        d.bnds = 0;
+        if (img2d) {
+            int kt = 0;
+            rsf_get_int("kt", &kt);
+            if (kt < 1 || kt > nt)
+                die(prog, "adj=y: kt must be in [1, nt] (the image is the wavefield of step nt-kt; "
+                          "the reference writes none for kt=0)");
+            g_adj.img_it = nt - kt;
+            d.nt = g_adj.img_it + 1;
+        }
+        const int row = img2d && !expl ? nr : wcs;
+        if (nwav < (size_t)nt * row) die(prog, "adj=y: standard input holds fewer than nt rows");
+        float *bw = malloc(sizeof(float) * (size_t)d.nt * row);
+        for (int it = 0; it < d.nt; it++)
+            memcpy(bw + (size_t)it * row, wav + (size_t)(nt - 1 - it) * row, sizeof(float) * row);
+        free(wav);
+        wav = bw;
+        wcs = row;
+    }
+    if (img2d) {
+        /* frames: the image step, plus the snapshots of snap=y; every step
+         * when the two do not share a period */
+        g_adj.wfl_j = user_jsnap;
+        if (user_jsnap > 0)
+            d.jsnap = g_adj.img_it % user_jsnap == 0 ? user_jsnap : 1;
+        else
+            d.jsnap = g_adj.img_it > 0 ? g_adj.img_it : 1;
         d.jdata = 1;
-        awe_plan *plan = NULL;
-        if (awe_plan_create(&d, gpu, &plan) != AWE_OK) die(prog, awe_last_error());
-        if (awe_set_model(plan, vel, den, NULL) != AWE_OK) die(prog, awe_last_error());
-        if (awe_set_geometry(plan, nr, rec, 0, NULL) != AWE_OK) die(prog, awe_last_error());
-        awe_info info;
-        awe_plan_info(plan, &info);
-        g_image = calloc(info.snap_elems, sizeof(float));
-        awe_set_snapshot_callback(plan, write_frame, NULL);
-        float *dat1 = malloc(sizeof(float) * ((size_t)info.nsmp + 1));
-        if (awe_forward(plan, bw, nr, dat1, NULL) != AWE_OK) die(prog, awe_last_error());
-        rsf_file *Fimg = rsf_output("out");
-        if (!Fimg) die(prog, rsf_error());
-        const char *lab[3] = {"z", "x", "y"};
-        for (int a = 0; a < ndim; a++) rsf_set_axis(Fimg, a + 1, d.n[a], d.o[a], d.d[a], lab[a]);
-        if (rsf_write(Fimg, g_image, info.snap_elems) != info.snap_elems) die(prog, "short write (image)");
-        rsf_close(Fimg);
-        awe_plan_destroy(plan);
-        return 0;
     }
 
     awe_plan *plan = NULL;
     if (awe_plan_create(&d, gpu, &plan) != AWE_OK) die(prog, awe_last_error());
     if (awe_set_model(plan, vel, den, scheme == AWE_SCHEME_GPU ? rfl : NULL) != AWE_OK) die(prog, awe_last_error());
-    if (awe_set_geometry(plan, ns, sou, nr, rec) != AWE_OK) die(prog, awe_last_error());
+    if (img2d) { /* injection at the receivers (expl=n) or the sources (expl=y); no traces */
+        if (awe_set_geometry(plan, expl ? ns : nr, expl ? sou : rec, 0, NULL) != AWE_OK) die(prog, awe_last_error());
+    } else if (awe_set_geometry(plan, ns, sou, nr, rec) != AWE_OK) {
+        die(prog, awe_last_error());
+    }
     awe_info info;
     awe_plan_info(plan, &info);
+    if (img2d) {
+        g_adj.image = calloc((size_t)d.n[0] * d.n[1], sizeof(float));
+        g_adj.cut = bnds;
+        g_adj.nb = info.nbpad;
+        g_adj.n1 = d.n[0];
+        g_adj.n2 = d.n[1];
+        g_adj.n1pad = info.npad[0];
+        if (user_jsnap == 0) awe_set_snapshot_callback(plan, write_frame, NULL);
+    }
 
     rsf_file *Fdat = rsf_output("out");
     if (!Fdat) die(prog, rsf_error());
-    rsf_set_axis(Fdat, 1, nr, rsf_o(Frec, 2), rsf_d(Frec, 2), "r");
-    rsf_set_axis(Fdat, 2, info.nsmp, ot, dt * d.jdata, "t");
-    if (d.jsnap > 0) {
+    if (img2d) { /* MAWEFDcart2Dcpu.c:362-363: the model axes */
+        rsf_set_axis(Fdat, 1, d.n[0], d.o[0], d.d[0], "z");
+        rsf_set_axis(Fdat, 2, d.n[1], d.o[1], d.d[1], "x");
+    } else {
+        rsf_set_axis(Fdat, 1, nr, rsf_o(Frec, 2), rsf_d(Frec, 2), "r");
+        rsf_set_axis(Fdat, 2, info.nsmp, ot, dt * d.jdata, "t");
+    }
+    if (img2d ? user_jsnap > 0 : d.jsnap > 0) {
         g_wfl = rsf_output("wfl");
         if (!g_wfl) die(prog, rsf_error());
         /* snapshot axes as each program writes them: bnds=y keeps the
@@ -251,14 +288,22 @@ int main(int argc, char **argv) {
             for (int a = 0; a < ndim; a++)
                 rsf_set_axis(g_wfl, a + 1, bnds ? info.npad[a] : d.n[a], o[a], d.d[a], lab[spher][a]);
         }
-        rsf_set_axis(g_wfl, ndim + 1, info.nsnap, ot, dt * d.jsnap, "t");
+        if (img2d)
+            rsf_set_axis(g_wfl, ndim + 1, g_adj.img_it / user_jsnap + 1, ot, dt * user_jsnap, "t");
+        else
+            rsf_set_axis(g_wfl, ndim + 1, info.nsnap, ot, dt * d.jsnap, "t");
         awe_set_snapshot_callback(plan, write_frame, NULL);
     }
     float *dat = malloc(sizeof(float) * (size_t)info.nsmp * (nr > 0 ? nr : 1));
     if (verb) fprintf(stderr, "%s: %d steps on a %d x %d x %d padded grid\n", prog, nt, info.npad[0], info.npad[1],
                       info.npad[2]);
     if (awe_forward(plan, wav, wcs, dat, NULL) != AWE_OK) die(prog, awe_last_error());
-    if (rsf_write(Fdat, dat, (size_t)info.nsmp * nr) != (size_t)info.nsmp * nr) die(prog, "short write (dat)");
+    if (img2d) {
+        const size_t nimg = (size_t)d.n[0] * d.n[1];
+        if (rsf_write(Fdat, g_adj.image, nimg) != nimg) die(prog, "short write (image)");
+    } else if (rsf_write(Fdat, dat, (size_t)info.nsmp * nr) != (size_t)info.nsmp * nr) {
+        die(prog, "short write (dat)");
+    }
     awe_plan_destroy(plan);
     rsf_close(Fdat);
     if (g_wfl) rsf_close(g_wfl);
@@ -275,5 +320,6 @@ int main(int argc, char **argv) {
     free(den);
     free(wav);
     free(dat);
+    free(g_adj.image);
     return 0;
 }
