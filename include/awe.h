@@ -143,6 +143,30 @@ awe_status awe_set_geometry(awe_plan *plan, int ns, const float *sou, int nr, co
  * sfAWEFDspher3Dgpu once per source position. */
 awe_status awe_set_shots(awe_plan *plan, int nshots, const int *ns, const float *sou, const int *nr, const float *rec);
 
+/* How a moving geometry's table entry is chosen for point k at step it. */
+typedef enum {
+    /* entry min(it, rows-1)*n + k: one row of positions per time step (the
+     * last row holds after the table ends) - an orbit sampled every step */
+    AWE_MOVE_PER_STEP = 0,
+    /* entry k*(it+1), as sfDYNAWEFDcart2Dgpu indexes its tables
+     * (dyn_cart_kernels.cu:133 inject_sources_2D_dyn, :326 extract_2D_dyn);
+     * that program also applies the free surface only with free=y
+     * (MDYNAWEFDcart2Dgpu.cu:393-396), which this mode follows.  Cartesian
+     * 2D, AWE_SCHEME_GPU only. */
+    AWE_MOVE_DYN = 1
+} awe_move_mode;
+
+/* Sources and receivers that move during the run (replaces
+ * MDYNAWEFDcart2Dgpu.cu:296-344): sou holds ns*nst points and rec nr*nrt
+ * points (awe_set_geometry's coordinate order, entry e at e*ndim); at each
+ * step ns sources inject and nr receivers record, each from the entry that
+ * `mode` selects.  Every entry a run can select must exist (AWE_MOVE_DYN:
+ * (n-1)*nt < n*rows).  AWE_SCHEME_GPU plans need expl = 0 (unscaled
+ * injection); the misfit gradient is not available on a moving geometry.
+ * awe_set_geometry / awe_set_shots return the plan to fixed points. */
+awe_status awe_set_moving_geometry(awe_plan *plan, int ns, int nst, const float *sou, int nr, int nrt,
+                                   const float *rec, int mode);
+
 /* Host-buffer forward modelling: wav [nt][ncs] (ncs = 1 or ns); dat
  * [nsmp][nr]; wfl (may be NULL) [nsnap][snap_elems].  Snapshots also go to
  * the callback when one is set. */

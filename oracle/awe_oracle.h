@@ -78,6 +78,11 @@ int orc_gpu_spher3d_fp64(const orc_gpar *p, const float *vel, const float *wav, 
 
 int orc_gpu_forward(int kind, const orc_gpar *p, const float *vel, const float *rfl, const float *wav, int ns,
                     const float *sou, int nr, const float *rec, float *dat, float *snaps);
+/* sfAWEFDcart2Dgpu's scheme on a moving geometry (expl = refl = 0): sou
+ * ns*nst points, rec nr*nrt points; move 0 = one row per step (last row
+ * held), 1 = MDYNAWEFDcart2Dgpu (entry k*(it+1), free surface only with fsrf) */
+int orc_gpu_cart2d_moving(const orc_gpar *p, const float *vel, const float *wav, int ns, int nst, const float *sou,
+                          int nr, int nrt, const float *rec, int move, float *dat, float *snaps);
 
 /* Time nsteps of the 3D scheme-B update on a padded grid (for the CPU
  * baseline): returns wall seconds.  Fields are allocated internally. */

@@ -145,9 +145,24 @@ static float refl3(const float *v, size_t n, long long s, long long rs, long lon
 int orc_gpu_snap_frames(int nt, int jsnap) { return jsnap > 0 ? (nt - 1) / jsnap + 1 : 0; }
 
 /* ------------------------------------------------------------------ */
-/* MAWEFDcart2Dgpu.cu:362-492.  vel/rfl [nx][nz]; sou/rec (x,z); dat [nt/jdata][nr] */
-static int gpu_cart2d(const orc_gpar *P, const float *vel_in, const float *rfl_in, const float *wav, int ns,
-                      const float *sou, int nr, const float *rec, float *dat, float *snaps) {
+/* table entry of point k at step it for a moving geometry (move < 0: fixed
+ * points, entry k).  move 0: one row of n positions per step, the last row
+ * held; move 1: k*(it+1), the index of MDYNAWEFDcart2Dgpu's kernels
+ * (dyn_cart_kernels.cu:133 inject_sources_2D_dyn, :326 extract_2D_dyn). */
+static size_t move_entry(int move, int k, int it, int n, int rows) {
+    if (move == 0) return (size_t)(it < rows ? it : rows - 1) * n + k;
+    if (move == 1) return (size_t)k * (it + 1);
+    return (size_t)k;
+}
+
+/* MAWEFDcart2Dgpu.cu:362-492.  vel/rfl [nx][nz]; sou/rec (x,z); dat [nt/jdata][nr].
+ * With a moving geometry (move >= 0) sou holds ns*nst and rec nr*nrt
+ * points; move 1 is MDYNAWEFDcart2Dgpu.cu:362-432, whose loop is this one
+ * with unscaled injection and the free surface only with free=y
+ * (MDYNAWEFDcart2Dgpu.cu:393-396). */
+static int gpu_cart2d_move(const orc_gpar *P, const float *vel_in, const float *rfl_in, const float *wav, int ns,
+                           int nst, const float *sou, int nr, int nrt, const float *rec, int move, float *dat,
+                           float *snaps) {
     const int nz = P->n1, nx = P->n2, nt = P->nt;
     const float dz = P->d1, dx = P->d2, dt = P->dt;
     const int nb = P->nb < NOPA ? NOPA : P->nb;
@@ -166,11 +181,13 @@ static int gpu_cart2d(const orc_gpar *P, const float *vel_in, const float *rfl_i
     float dq = v[(size_t)NOPA * nxpad + nxpad - 1] * (dt / dz), bzl = (1 - dq) / (1 + dq);
     dq = v[(size_t)(nzpad - NOPA - 1) * nxpad + nxpad - 1] * (dt / dz);
     float bzh = (1 - dq) / (1 + dq);
-    glint *cs = malloc((ns ? ns : 1) * sizeof(glint)), *cr = malloc((nr ? nr : 1) * sizeof(glint));
-    for (int i = 0; i < ns; i++)
+    const size_t nsrc = (size_t)ns * (move >= 0 ? nst : 1), nrec = (size_t)nr * (move >= 0 ? nrt : 1);
+    glint *cs = malloc((nsrc ? nsrc : 1) * sizeof(glint)), *cr = malloc((nrec ? nrec : 1) * sizeof(glint));
+    for (size_t i = 0; i < nsrc; i++)
         glint_make(2, sou[2 * i], 0, sou[2 * i + 1], ozpad, oxpad, 0, dz, dx, 1, nzpad, nxpad, 1, &cs[i]);
-    for (int i = 0; i < nr; i++)
+    for (size_t i = 0; i < nrec; i++)
         glint_make(2, rec[2 * i], 0, rec[2 * i + 1], ozpad, oxpad, 0, dz, dx, 1, nzpad, nxpad, 1, &cr[i]);
+    const int fsurf = move != 1 || P->fsrf;
     const int jdata = P->jdata > 0 ? P->jdata : 1, nsmp = nt / jdata;
     const int fz = (int)(floor)((P->o1 - ozpad) / dz), fx = (int)(floor)((P->o2 - oxpad) / dx);
     size_t isnap = 0;
@@ -178,7 +195,7 @@ static int gpu_cart2d(const orc_gpar *P, const float *vel_in, const float *rfl_i
     for (int it = 0; it < nt; it++) {
         const float wa = wav[it];
         for (int s = 0; s < ns; s++) { /* inject into po, kernel order of corners */
-            const glint *c = &cs[s];
+            const glint *c = &cs[move_entry(move, s, it, ns, nst)];
             float r = 1.f;
             int mode = P->expl ? (P->refl ? 2 : 1) : 0;
             size_t k00 = C2(c->jx, c->jz), k01 = C2(c->jx, c->jz + 1), k10 = C2(c->jx + 1, c->jz),
@@ -246,12 +263,13 @@ static int gpu_cart2d(const orc_gpar *P, const float *vel_in, const float *rfl_i
                 int i = sponge_i(ix, nxpad, iz, nzpad, -1, 0, nb);
                 po[C2(ix, iz)] = damp_apply(po[C2(ix, iz)], i, tab);
                 ppo[C2(ix, iz)] = damp_apply(ppo[C2(ix, iz)], i, tab);
-                if (ix > nxpad - nb) po[C2(ix, iz)] = 0;
+                if (fsurf && ix > nxpad - nb) po[C2(ix, iz)] = 0;
             }
         /* freeSurf_2D's threads past nxpad (grid rounded up to 8) zero the
          * first samples of the next row (row = z in the kernel's x-fastest view) */
-        for (int iz = 0; iz + 1 < nzpad; iz++)
-            for (int k = 0; k < 8 * ((nxpad + 7) / 8) - nxpad; k++) po[C2(k, iz + 1)] = 0;
+        if (fsurf)
+            for (int iz = 0; iz + 1 < nzpad; iz++)
+                for (int k = 0; k < 8 * ((nxpad + 7) / 8) - nxpad; k++) po[C2(k, iz + 1)] = 0;
         if (snaps && P->jsnap > 0 && it % P->jsnap == 0) {
             if (P->bnds) {
                 memcpy(snaps + isnap * npad, po, npad * 4);
@@ -264,7 +282,7 @@ static int gpu_cart2d(const orc_gpar *P, const float *vel_in, const float *rfl_i
         }
         if (it < nsmp)
             for (int r = 0; r < nr; r++) {
-                const glint *c = &cr[r];
+                const glint *c = &cr[move_entry(move, r, it, nr, nrt)];
                 dat[(size_t)it * nr + r] = po[C2(c->jx, c->jz)] * c->w[0] + po[C2(c->jx, c->jz + 1)] * c->w[1] +
                                            po[C2(c->jx + 1, c->jz)] * c->w[2] +
                                            po[C2(c->jx + 1, c->jz + 1)] * c->w[3];
@@ -783,10 +801,16 @@ int orc_gpu_spher3d_fp64(const orc_gpar *P, const float *vel_in, const float *wa
 int orc_gpu_forward(int kind, const orc_gpar *P, const float *vel, const float *rfl, const float *wav, int ns,
                     const float *sou, int nr, const float *rec, float *dat, float *snaps) {
     switch (kind) {
-        case 0: return gpu_cart2d(P, vel, rfl, wav, ns, sou, nr, rec, dat, snaps);
+        case 0: return gpu_cart2d_move(P, vel, rfl, wav, ns, 1, sou, nr, 1, rec, -1, dat, snaps);
         case 1: return gpu_cart3d(P, vel, wav, ns, sou, nr, rec, dat, snaps);
         case 2: return gpu_polar2d(P, vel, wav, ns, sou, nr, rec, dat, snaps);
         case 3: return gpu_spher3d(P, vel, wav, ns, sou, nr, rec, dat, snaps);
     }
     return 1;
+}
+
+int orc_gpu_cart2d_moving(const orc_gpar *P, const float *vel, const float *wav, int ns, int nst, const float *sou,
+                          int nr, int nrt, const float *rec, int move, float *dat, float *snaps) {
+    if (move != 0 && move != 1) return 1;
+    return gpu_cart2d_move(P, vel, NULL, wav, ns, nst, sou, nr, nrt, rec, move, dat, snaps);
 }

@@ -226,6 +226,39 @@ def gpu_scheme(kind: str, p: dict, vel, wav, sou, rec, rfl=None, use_reference_e
     return dat, snaps
 
 
+def gpu_cart2d_moving(p: dict, vel, wav, sou, nst: int, rec, nrt: int, move: int,
+                      use_reference_emulation: bool = False):
+    """sfAWEFDcart2Dgpu's scheme with moving sources and receivers: sou holds
+    ns*nst (x, z) points and rec nr*nrt; move 0 = row min(it, rows-1) per
+    step, 1 = sfDYNAWEFDcart2Dgpu (entry k*(it+1), free surface only with
+    fsrf).  use_reference_emulation=True runs MDYNAWEFDcart2Dgpu's own
+    kernels through the host emulation (move 1 only).  Returns (dat, snaps)."""
+    q = make_gpar(p)
+    vel = np.ascontiguousarray(vel, np.float32)
+    wav = np.ascontiguousarray(wav, np.float32).ravel()
+    sou = np.ascontiguousarray(sou, np.float32).reshape(-1, 2)
+    rec = np.ascontiguousarray(rec, np.float32).reshape(-1, 2)
+    ns, nr = sou.shape[0] // nst, rec.shape[0] // nrt
+    assert ns * nst == sou.shape[0] and nr * nrt == rec.shape[0]
+    rows, frames, elems = gpu_shapes("cart2d", p, nr)
+    dat = np.zeros((rows, nr), np.float32)
+    snaps = np.zeros((frames, elems), np.float32) if frames else None
+    if use_reference_emulation:
+        if move != 1:
+            raise ValueError("the reference emulation covers sfDYNAWEFDcart2Dgpu (move=1) only")
+        L = C.CDLL(os.path.join(REF_OUT, "libgpuref.so"))
+        fp = C.POINTER(C.c_float)
+        fn = L.gpuref_dyncart2d
+        fn.argtypes = [C.POINTER(GPar), fp, fp, C.c_int, C.c_int, fp, C.c_int, C.c_int, fp, fp, fp]
+        rc = fn(C.byref(q), _fp(vel), _fp(wav), ns, nst, _fp(sou), nr, nrt, _fp(rec), _fp(dat), _fp(snaps))
+    else:
+        rc = lib().orc_gpu_cart2d_moving(C.byref(q), _fp(vel), _fp(wav), ns, nst, _fp(sou), nr, nrt, _fp(rec), move,
+                                         _fp(dat), _fp(snaps))
+    if rc != 0:
+        raise RuntimeError("moving-geometry run returned %d" % rc)
+    return dat, snaps
+
+
 _adj = None
 
 

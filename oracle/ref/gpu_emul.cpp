@@ -4,9 +4,10 @@
 // The reference's kernel files (CODE/cart_kernels.cu, CODE/spher_kernels.cu)
 // are compiled unchanged as C++ host code: __global__ functions become plain
 // functions and every launch runs the grid's threads one after another.  The
-// per-step sequences of the four programs' main() (MAWEFDcart2Dgpu.cu:362-492,
+// per-step sequences of the programs' main() (MAWEFDcart2Dgpu.cu:362-492,
 // MAWEFDcart3Dgpu.cu:380-466, MAWEFDspher2Dgpu.cu:341-419,
-// MAWEFDspher3Dgpu.cu:449-566) are restated below around those kernels, with
+// MAWEFDspher3Dgpu.cu:449-566, and MDYNAWEFDcart2Dgpu.cu:362-432 over
+// CODE/dyn_cart_kernels.cu) are restated below around those kernels, with
 // the reference's own fdutil.c (lint2d_make, lint3d_make, fdutil_init,
 // cut2d, cut3d, cut3d_sph) for geometry and windows.
 //
@@ -58,6 +59,12 @@ namespace ref_cart {
 #undef NOP
 namespace ref_spher {
 #include "spher_kernels.cu"
+}
+#undef INDEX2D
+#undef INDEX3D
+#undef NOP
+namespace ref_dyn {
+#include "dyn_cart_kernels.cu"
 }
 #undef INDEX2D
 #undef INDEX3D
@@ -516,6 +523,97 @@ int gpuref_spher3d(const gpuref_par *P, const float *vel, const float *wav, int 
             isnap++;
         }
     }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// sfDYNAWEFDcart2Dgpu (MDYNAWEFDcart2Dgpu.cu:296-432): vel [nx][nz]; sou
+// ns*nst and rec nr*nrt (x, z) points; the kernels of dyn_cart_kernels.cu
+// pick entry k*(it+1) of each table.  Traces of every step go to row it
+// (the program's buffer holds nt/jdata rows: jdata must be 1).
+int gpuref_dyncart2d(const gpuref_par *P, const float *vel, const float *wav, int ns, int nst, const float *sou,
+                     int nr, int nrt, const float *rec, float *dat, float *snaps) {
+    using namespace ref_dyn;
+    const int nz = P->n1, nx = P->n2, nt = P->nt;
+    const float dz = P->d1, dx = P->d2, dt = P->dt;
+    if (P->jdata != 1) return 2;
+    int nb = P->nb < NOP ? NOP : P->nb;
+    sf_axis az = sf_maxa(nz, P->o1, dz), ax = sf_maxa(nx, P->o2, dx);
+    fdm2d fdm = fdutil_init(false, P->fsrf, az, ax, nb, 1);
+    const int nxpad = fdm->nxpad, nzpad = fdm->nzpad;
+    std::vector<float> h_vel((size_t)nxpad * nzpad);
+    std::vector<float> tt1(vel, vel + (size_t)nx * nz);
+    expand_cpu_2d(tt1.data(), h_vel.data(), fdm->nb, nz, nzpad, nx, nxpad);
+    std::vector<float> bzl(nxpad), bzh(nxpad), bxl(nzpad), bxh(nzpad);
+    for (int ix = 0; ix < nxpad; ix++) {  // MDYNAWEFDcart2Dgpu.cu:275-289
+        float d = h_vel[NOP * nxpad + ix] * (dt / dz);
+        bzl[ix] = (1 - d) / (1 + d);
+        d = h_vel[(nzpad - NOP - 1) * nxpad + ix] * (dt / dz);
+        bzh[ix] = (1 - d) / (1 + d);
+    }
+    for (int iz = 0; iz < nzpad; iz++) {
+        float d = h_vel[iz * nxpad + NOP] * (dt / dx);
+        bxl[iz] = (1 - d) / (1 + d);
+        d = h_vel[iz * nxpad + nxpad - NOP - 1] * (dt / dx);
+        bxh[iz] = (1 - d) / (1 + d);
+    }
+    const int nse = ns * nst, nre = nr * nrt;
+    pt2d *ss = (pt2d *)calloc(nse > 0 ? nse : 1, sizeof(pt2d)), *rr = (pt2d *)calloc(nre > 0 ? nre : 1, sizeof(pt2d));
+    for (int i = 0; i < nse; i++) {
+        ss[i].x = sou[2 * i];
+        ss[i].z = sou[2 * i + 1];
+    }
+    for (int i = 0; i < nre; i++) {
+        rr[i].x = rec[2 * i];
+        rr[i].z = rec[2 * i + 1];
+    }
+    lint2d cs = lint2d_make(nse, ss, fdm), cr = lint2d_make(nre, rr, fdm);
+    const size_t npad = (size_t)nxpad * nzpad;
+    std::vector<float> ppo(npad + kSlack, 0.f), po(npad + kSlack, 0.f), fpo(npad + kSlack, 0.f);
+    float **pz = sf_floatalloc2(nzpad, nxpad), **oslice = sf_floatalloc2(nz, nx);
+    std::vector<float> dd((size_t)nt * nr + nr, 0.f);
+    const dim3 g2((unsigned)ceil(nxpad / 8.0f), (unsigned)ceil(nzpad / 8.0f)), b2(8, 8);
+    float *pww = const_cast<float *>(wav);
+    size_t isnap = 0;
+    for (int it = 0; it < nt; it++) {
+        if (ns > 0) {
+            dim3 gS(MIN(ns, (int)ceil(ns / 1024.0f)), 1), bS(MIN(ns, 1024), 1);
+            launch(gS, bS, [&] {
+                inject_sources_2D_dyn(po.data(), pww, cs->w00, cs->w01, cs->w10, cs->w11, cs->jx, cs->jz, it, ns,
+                                      nxpad, nzpad);
+            });
+        }
+        launch(g2, b2, [&] { solve_2D(fpo.data(), po.data(), ppo.data(), h_vel.data(), dx, dz, dt, nxpad, nzpad); });
+        launch(g2, b2, [&] { shift_2D(fpo.data(), po.data(), ppo.data(), nxpad, nzpad); });
+        launch_ordered(
+            g2, b2,
+            [&] {
+                onewayBC_2D(po.data(), ppo.data(), bzl.data(), bzh.data(), bxl.data(), bxh.data(), nxpad, nzpad);
+            },
+            [&](long long, long long y, long long) { return facedist(y, nzpad); });
+        launch(g2, b2, [&] { spongeKernel_2D(po.data(), nxpad, nzpad, nb); });
+        launch(g2, b2, [&] { spongeKernel_2D(ppo.data(), nxpad, nzpad, nb); });
+        if (P->fsrf) launch(g2, b2, [&] { freeSurf_2D(po.data(), nxpad, nzpad, nb); });
+        if (snaps && P->jsnap > 0 && it % P->jsnap == 0) {
+            for (int x = 0; x < nxpad; x++)
+                for (int z = 0; z < nzpad; z++) pz[x][z] = po[(size_t)z * nxpad + x];
+            if (P->bnds) {
+                memcpy(snaps + isnap * npad, pz[0], npad * sizeof(float));
+            } else {
+                cut2d(pz, oslice, fdm, az, ax);
+                memcpy(snaps + isnap * (size_t)nz * nx, oslice[0], (size_t)nz * nx * sizeof(float));
+            }
+            isnap++;
+        }
+        if (nr > 0) {
+            dim3 gR(MIN(nr, (int)ceil(nr / 1024.0f)), 1), bR(MIN(nr, 1024), 1);
+            launch(gR, bR, [&] {
+                extract_2D_dyn(dd.data(), it, nr, nxpad, nzpad, po.data(), cr->jx, cr->jz, cr->w00, cr->w01,
+                               cr->w10, cr->w11);
+            });
+        }
+    }
+    memcpy(dat, dd.data(), (size_t)nt * nr * sizeof(float));
     return 0;
 }
 

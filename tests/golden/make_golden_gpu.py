@@ -6,7 +6,7 @@ per-step sequence of each program's main() (oracle/ref/gpu_emul.cpp).  This
 script runs that emulation on small seeded cases and stores inputs and
 outputs as tests/golden/A_<case>.npz.  Needs the reference checkout:
 
-    python tests/golden/make_golden_gpu.py
+    python tests/golden/make_golden_gpu.py [case names]
 """
 from __future__ import annotations
 
@@ -115,9 +115,53 @@ def make_inputs(case):
     return par, vel, wav, sou, rec, rfl
 
 
-def main():
+# sfDYNAWEFDcart2Dgpu: sources and receivers read from tables of ns*nst and
+# nr*nrt points (entry k*(it+1) at step it), unscaled injection
+DYN_CASES = [
+    dict(name="A_dyncart2d_move", n=(40, 44), d=(5.0, 5.0), o=(0.0, 0.0), nb=8, nt=220, dt=0.005, ns=3, nr=5,
+         jsnap=70, bnds=0, fsrf=0, seed=41),
+    dict(name="A_dyncart2d_free_bnds", n=(36, 40), d=(5.0, 5.0), o=(0.0, 0.0), nb=6, nt=180, dt=0.005, ns=2, nr=4,
+         jsnap=60, bnds=1, fsrf=1, seed=42),
+]
+
+
+def make_dyn_inputs(case):
+    """Tables with nst = nrt = nt rows: every entry k*(it+1), k < n, it < nt,
+    exists ((n-1)*nt < n*nt).  Entry e sits on a track crossing the model."""
+    rng = np.random.default_rng(case["seed"])
+    n, d, o, nt = case["n"], case["d"], case["o"], case["nt"]
+    vel = layered_cart(rng, n, d[0])
+    ext = [(n[a] - 1) * d[a] for a in range(2)]
+    ns, nr = case["ns"], case["nr"]
+
+    def track(count, depth, phase):
+        e = np.arange(count)
+        u = 0.15 + 0.7 * np.mod(e * 0.618034 + phase, 1.0)
+        return np.stack([o[1] + u * ext[1], o[0] + depth * ext[0] + 0.3 * d[0] * np.sin(e * 0.05)], 1)
+
+    sou = track(ns * nt, 0.42, 0.1).astype(np.float32)
+    rec = track(nr * nt, 0.3, 0.55).astype(np.float32)
+    wav = ricker(nt, case["dt"], 5.0, 0.3)
+    par = dict(kind="dyncart2d", n=list(n), d=[float(x) for x in d], o=[float(x) for x in o], nb=case["nb"], nt=nt,
+               dt=case["dt"], jdata=1, jsnap=case["jsnap"], bnds=case["bnds"], fsrf=case["fsrf"], expl=0, refl=0,
+               ns=ns, nst=nt, nr=nr, nrt=nt)
+    return par, vel, wav, sou, rec
+
+
+def main(only=None):
     oracle.build(with_reference=True)
+    for case in DYN_CASES:
+        if only and case["name"] not in only:
+            continue
+        par, vel, wav, sou, rec = make_dyn_inputs(case)
+        dat, snaps = oracle.gpu_cart2d_moving(par, vel, wav, sou, par["nst"], rec, par["nrt"], 1,
+                                              use_reference_emulation=True)
+        out = dict(par=np.array(json.dumps(par)), vel=vel, wav=wav, sou=sou, rec=rec, dat=dat, snaps=snaps)
+        np.savez_compressed(os.path.join(HERE, case["name"] + ".npz"), **out)
+        print("%-28s dat %s max|dat| %.3e snaps %s" % (case["name"], dat.shape, np.abs(dat).max(), snaps.shape))
     for case in CASES:
+        if only and case["name"] not in only:
+            continue
         par, vel, wav, sou, rec, rfl = make_inputs(case)
         dat, snaps = oracle.gpu_scheme(par["kind"], par, vel, wav, sou, rec, rfl=rfl, use_reference_emulation=True)
         out = dict(par=np.array(json.dumps(par)), vel=vel, wav=wav, sou=sou, rec=rec, dat=dat)
@@ -131,4 +175,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:] or None)

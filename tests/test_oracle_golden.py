@@ -55,7 +55,10 @@ def test_gpu_scheme_oracle_matches_reference_kernels_bit_exact(path):
     """Fixtures from the reference's own CUDA kernel files run through the host
     emulation of the GPU programs (tests/golden/make_golden_gpu.py)."""
     par, a = load(path)
-    dat, snaps = oracle.gpu_scheme(par["kind"], par, a["vel"], a["wav"], a["sou"], a["rec"], rfl=a.get("rfl"))
+    if par["kind"] == "dyncart2d":  # sfDYNAWEFDcart2Dgpu: moving-geometry tables
+        dat, snaps = oracle.gpu_cart2d_moving(par, a["vel"], a["wav"], a["sou"], par["nst"], a["rec"], par["nrt"], 1)
+    else:
+        dat, snaps = oracle.gpu_scheme(par["kind"], par, a["vel"], a["wav"], a["sou"], a["rec"], rfl=a.get("rfl"))
     assert np.array_equal(dat, a["dat"])
     if "snaps" in a:
         assert np.array_equal(snaps, a["snaps"])
@@ -63,4 +66,22 @@ def test_gpu_scheme_oracle_matches_reference_kernels_bit_exact(path):
 
 def test_gpu_scheme_golden_set_covers_programs():
     kinds = {load(p)[0]["kind"] for p in GOLDEN_A}
-    assert kinds == {"cart2d", "cart3d", "polar2d", "spher3d"}
+    assert kinds == {"cart2d", "cart3d", "polar2d", "spher3d", "dyncart2d"}
+
+
+def test_moving_geometry_oracle_modes():
+    """The per-step mode with every row equal is the fixed geometry, and the
+    sfDYNAWEFDcart2Dgpu mode with one point (entry 0 at every step) too,
+    except for its free surface, which needs free=y."""
+    par, a = load(os.path.join(os.path.dirname(__file__), "golden", "A_cart2d_const.npz"))
+    ref, rsn = oracle.gpu_scheme("cart2d", par, a["vel"], a["wav"], a["sou"], a["rec"])
+    sou_t = np.tile(a["sou"], (7, 1))
+    rec_t = np.tile(a["rec"], (7, 1))
+    dat, snaps = oracle.gpu_cart2d_moving(par, a["vel"], a["wav"], sou_t, 7, rec_t, 7, 0)
+    assert np.array_equal(dat, ref) and np.array_equal(snaps, rsn)
+    one = dict(par, fsrf=1)
+    d1, _ = oracle.gpu_cart2d_moving(one, a["vel"], a["wav"], a["sou"][:1], 1, a["rec"][:1], 1, 1)
+    r1, _ = oracle.gpu_scheme("cart2d", par, a["vel"], a["wav"], a["sou"][:1], a["rec"][:1])
+    assert np.array_equal(d1, r1)
+    d0, _ = oracle.gpu_cart2d_moving(par, a["vel"], a["wav"], a["sou"][:1], 1, a["rec"][:1], 1, 1)
+    assert not np.array_equal(d0, r1)

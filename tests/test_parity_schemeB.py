@@ -55,3 +55,37 @@ def test_graph_replay_equals_direct_launches():
     np.testing.assert_array_equal(g2, g1)
     np.testing.assert_array_equal(d1, g1)
     np.testing.assert_array_equal(g3, g1[:, ::-1])
+
+
+@pytest.mark.parametrize("precision", [1, 0], ids=["exact", "fast"])
+def test_moving_geometry_per_step_equals_fixed_points(precision):
+    """AWE_MOVE_PER_STEP on the CPU-program scheme (8th order, sponge, one
+    wavelet per source): a moving receiver's sample at step it is the fixed
+    receiver at that step's position, and one source that jumps between three
+    positions equals a fixed run with a source at each position whose wavelet
+    is zero outside its steps - bit for bit, in both precisions."""
+    import wavefield_imaging_gb300 as awe
+
+    par, a = load_golden(golden_paths("c2d_o8_sponge.npz")[0])
+    nt = 150
+    par = dict(par, nt=nt, expl=0, jsnap=0)
+    wav = np.ascontiguousarray(a["wav"][:nt])
+    pos = np.array([[110.0, 60.0], [150.5, 75.2], [200.0, 100.0]], np.float32)
+    which = np.arange(nt) * 3 // nt  # source position of each step
+    rx = (20.0 + 1.3 * np.arange(nt)).astype(np.float32)
+    rec_moving = np.stack([np.stack([rx, np.full(nt, 40.3, np.float32)], 1),
+                           np.tile(np.array([[250.0, 70.1]], np.float32), (nt, 1))], 1).reshape(-1, 2)
+    with awe.Plan(desc_from_par(par, precision=precision)) as p:
+        p.set_model(a["vel"])
+        p.set_moving_geometry(pos[which], nt, rec_moving, nt, awe.MOVE_PER_STEP)
+        dat = p.forward(wav)
+        rec_fixed = np.concatenate([np.stack([rx, np.full(nt, 40.3, np.float32)], 1),
+                                    np.array([[250.0, 70.1]], np.float32)])
+        p.set_geometry(pos, rec_fixed)
+        w3 = np.zeros((nt, 3), np.float32)
+        w3[np.arange(nt), which] = wav
+        ref = p.forward(w3)
+    assert dat.shape == (nt, 2)
+    np.testing.assert_array_equal(dat[:, 0], ref[np.arange(nt), np.arange(nt)])
+    np.testing.assert_array_equal(dat[:, 1], ref[:, nt])
+    assert np.abs(dat).max() > 0

@@ -17,7 +17,7 @@ from wavefield_imaging_gb300 import rsf
 from wavefield_imaging_gb300 import build as awe_build
 
 PROGRAM_OF_KIND = {"cart2d": "sfAWEFDcart2Dgpu", "cart3d": "sfAWEFDcart3Dgpu", "polar2d": "sfAWEFDspher2Dgpu",
-                   "spher3d": "sfAWEFDspher3Dgpu"}
+                   "spher3d": "sfAWEFDspher3Dgpu", "dyncart2d": "sfDYNAWEFDcart2Dgpu"}
 
 
 @pytest.fixture(scope="module")
@@ -36,8 +36,12 @@ def write_inputs(tmp, par, a):
     wav = a["wav"]
     ncs = 1 if wav.ndim == 1 else wav.shape[1]
     rsf.write(str(tmp / "wav.rsf"), wav.reshape(par["nt"], ncs), [(ncs, 0.0, 1.0), (par["nt"], 0.0, par["dt"])])
-    rsf.write(str(tmp / "sou.rsf"), a["sou"], [(nd, 0.0, 1.0), (a["sou"].shape[0], 0.0, 1.0)])
-    rsf.write(str(tmp / "rec.rsf"), a["rec"], [(nd, 0.0, 1.0), (a["rec"].shape[0], 0.0, 1.0)])
+    if par.get("kind") == "dyncart2d":  # position tables: n2 points per step, n3 rows
+        rsf.write(str(tmp / "sou.rsf"), a["sou"], [(nd, 0.0, 1.0), (par["ns"], 0.0, 1.0), (par["nst"], 0.0, 1.0)])
+        rsf.write(str(tmp / "rec.rsf"), a["rec"], [(nd, 0.0, 1.0), (par["nr"], 0.0, 1.0), (par["nrt"], 0.0, 1.0)])
+    else:
+        rsf.write(str(tmp / "sou.rsf"), a["sou"], [(nd, 0.0, 1.0), (a["sou"].shape[0], 0.0, 1.0)])
+        rsf.write(str(tmp / "rec.rsf"), a["rec"], [(nd, 0.0, 1.0), (a["rec"].shape[0], 0.0, 1.0)])
     args = ["vel=" + str(tmp / "vel.rsf"), "sou=" + str(tmp / "sou.rsf"), "rec=" + str(tmp / "rec.rsf")]
     for key in ("den", "rfl"):
         if key in a:
@@ -72,7 +76,7 @@ def test_gpu_program_matches_reference_outputs(bindir, tmp_path, path):
     out = run_program(bindir, PROGRAM_OF_KIND[par["kind"]], tmp_path, args)
     dat, hdr = rsf.read(str(out))
     np.testing.assert_array_equal(dat.reshape(a["dat"].shape), a["dat"])
-    assert int(hdr["n1"]) == a["rec"].shape[0]
+    assert int(hdr["n1"]) == a["dat"].shape[1]
     if "snaps" in a:
         wfl, _ = rsf.read(str(tmp_path / "wfl.rsf"))
         np.testing.assert_array_equal(wfl.ravel(), a["snaps"].ravel())
@@ -107,6 +111,7 @@ def _run_bare(bindir, name, args):
 
 
 @pytest.mark.parametrize("name,arg,msg", [("sfAWEFDcart2Dgpu", "adj=y", "adj=y"),
+                                          ("sfDYNAWEFDcart2Dgpu", "jdata=2", "jdata must be 1"),
                                           ("sfAWEFDcart2Dcpu", "sinc=y", "sinc=y"),
                                           ("sfAWEFDcart2Dcpu", "nqz=10", "snapshot windows")])
 def test_unsupported_options_stop_with_an_error(bindir, name, arg, msg):

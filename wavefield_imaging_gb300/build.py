@@ -82,7 +82,7 @@ def build(verbose: bool = False) -> str:
 PROGS = os.path.join(PKG, "programs")
 BIN = os.path.join(OUT, "bin")
 PROGRAM_NAMES = ["sfAWEFDcart2Dgpu", "sfAWEFDcart3Dgpu", "sfAWEFDspher2Dgpu", "sfAWEFDspher3Dgpu",
-                 "sfAWEFDcart2Dcpu", "sfAWEFDcart3Dcpu"]
+                 "sfAWEFDcart2Dcpu", "sfAWEFDcart3Dcpu", "sfDYNAWEFDcart2Dgpu"]
 
 
 def build_programs() -> str:

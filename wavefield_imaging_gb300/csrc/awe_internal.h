@@ -75,14 +75,16 @@ void launch_band_sponge(int ndim, int width, bool exact, float *u, const float *
 
 // injection into the new level scaled by vel (v^2 dt^2): u += (dd*w)*vel.
 // off[c] = flat offset of corner c from the point's base index.
+// stride: distance between consecutive points in pts (moving geometries)
 void launch_injectB_off(int ndim, bool exact, float *u, const float *vel, const GeoPoint *pts, int ns,
-                        const float *wav, int it, int ncs, bool one_wavelet, const long long *off, cudaStream_t s);
+                        const float *wav, int it, int ncs, bool one_wavelet, const long long *off, cudaStream_t s,
+                        int stride = 1);
 
 // receiver gather; when w1 != null the sponge factors are applied to each node
 // value first (the field carries a pending sponge)
 void launch_extract_off(int ndim, bool exact, const float *u, const GeoPoint *pts, int nr, float *dat_row,
                         const float *w1, const float *w2, const float *w3, const Grid &g, const long long *off,
-                        cudaStream_t s);
+                        cudaStream_t s, int stride = 1);
 
 // copy a window (or the whole padded grid) of u into dst, applying pending sponge
 void launch_snapshot(int ndim, const float *u, float *dst, const Grid &g, int f1, int f2, int f3, int m1, int m2,
@@ -115,7 +117,7 @@ void launch_stepA(int geom, bool exact, const float *cur, float *nxt, const floa
                   cudaStream_t s);
 void launch_bcA(bool exact, const float *um, float *uo, float *aux, const StepAParams &p, cudaStream_t s);
 void launch_injectA(bool exact, int ndim, float *u, const GeoPoint *pts, const float *scale, int ns, const float *wav,
-                    int it, bool scaled, const long long *off, cudaStream_t s);
+                    int it, bool scaled, const long long *off, cudaStream_t s, int stride = 1);
 void launch_snapshot_transpose2(const float *u, float *dst, const Grid &g, int f1, int f2, int m1, int m2,
                                 cudaStream_t s);
 

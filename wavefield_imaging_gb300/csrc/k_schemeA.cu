@@ -433,11 +433,11 @@ void launch_bcA(bool exact, const float *um, float *uo, float *aux, const StepAP
 template <bool EXACT>
 __global__ void k_injectA(float *u, const GeoPoint *__restrict__ pts, const float *__restrict__ scale, int ns,
                           const float *__restrict__ wav, int it, int ncorner, int scaled,
-                          const long long *__restrict__ off) {
+                          const long long *__restrict__ off, int stride) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     const float wa = wav[it];
     for (int s = 0; s < ns; s++) {
-        const GeoPoint pt = pts[s];
+        const GeoPoint pt = pts[(long long)s * stride];
         for (int c = 0; c < ncorner; c++) {
             const long long n = pt.base + off[c];
             float a = fmul<EXACT>(wa, pt.w[c]);
@@ -448,11 +448,11 @@ __global__ void k_injectA(float *u, const GeoPoint *__restrict__ pts, const floa
 }
 
 void launch_injectA(bool exact, int ndim, float *u, const GeoPoint *pts, const float *scale, int ns, const float *wav,
-                    int it, bool scaled, const long long *off, cudaStream_t s) {
+                    int it, bool scaled, const long long *off, cudaStream_t s, int stride) {
     if (ns <= 0) return;
     const int nc = ndim == 3 ? 8 : 4;
-    if (exact) k_injectA<true><<<1, 32, 0, s>>>(u, pts, scale, ns, wav, it, nc, scaled, off);
-    else k_injectA<false><<<1, 32, 0, s>>>(u, pts, scale, ns, wav, it, nc, scaled, off);
+    if (exact) k_injectA<true><<<1, 32, 0, s>>>(u, pts, scale, ns, wav, it, nc, scaled, off, stride);
+    else k_injectA<false><<<1, 32, 0, s>>>(u, pts, scale, ns, wav, it, nc, scaled, off, stride);
 }
 
 // polar snapshots are theta-fastest ([r][theta]) as sfAWEFDspher2Dgpu writes them

@@ -514,11 +514,11 @@ void launch_band_sponge(int ndim, int width, bool exact, float *u, const float *
 template <bool EXACT>
 __global__ void k_injectB(float *u, const float *__restrict__ vel, const GeoPoint *__restrict__ pts, int ns,
                           const float *__restrict__ wav, int it, int ncs, int one_wavelet, int ncorner,
-                          const long long *__restrict__ off) {
+                          const long long *__restrict__ off, int stride) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     for (int s = 0; s < ns; s++) {
         const float dd = one_wavelet ? wav[(long long)it * ncs] : wav[(long long)it * ncs + s];
-        const GeoPoint pt = pts[s];
+        const GeoPoint pt = pts[(long long)s * stride];
         for (int c = 0; c < ncorner; c++) {
             const long long n = pt.base + off[c];
             u[n] = fadd<EXACT>(u[n], fmul<EXACT>(fmul<EXACT>(dd, pt.w[c]), vel[n]));
@@ -532,10 +532,10 @@ __global__ void k_injectB(float *u, const float *__restrict__ vel, const GeoPoin
 template <bool EXACT, int NDIM>
 __global__ void k_extract(const float *__restrict__ u, const GeoPoint *__restrict__ pts, int nr, float *dat,
                           const float *__restrict__ w1, const float *__restrict__ w2, const float *__restrict__ w3,
-                          Grid g, const long long *__restrict__ off) {
+                          Grid g, const long long *__restrict__ off, int stride) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nr) return;
-    const GeoPoint pt = pts[r];
+    const GeoPoint pt = pts[(long long)r * stride];
     constexpr int NC = NDIM == 3 ? 8 : 4;
     float acc = 0.f;
 #pragma unroll
@@ -554,24 +554,25 @@ __global__ void k_extract(const float *__restrict__ u, const GeoPoint *__restric
 }
 
 void launch_injectB_off(int ndim, bool exact, float *u, const float *vel, const GeoPoint *pts, int ns,
-                        const float *wav, int it, int ncs, bool one_wavelet, const long long *off, cudaStream_t s) {
+                        const float *wav, int it, int ncs, bool one_wavelet, const long long *off, cudaStream_t s,
+                        int stride) {
     if (ns <= 0) return;
     const int nc = ndim == 3 ? 8 : 4;
-    if (exact) k_injectB<true><<<1, 32, 0, s>>>(u, vel, pts, ns, wav, it, ncs, one_wavelet, nc, off);
-    else k_injectB<false><<<1, 32, 0, s>>>(u, vel, pts, ns, wav, it, ncs, one_wavelet, nc, off);
+    if (exact) k_injectB<true><<<1, 32, 0, s>>>(u, vel, pts, ns, wav, it, ncs, one_wavelet, nc, off, stride);
+    else k_injectB<false><<<1, 32, 0, s>>>(u, vel, pts, ns, wav, it, ncs, one_wavelet, nc, off, stride);
 }
 
 void launch_extract_off(int ndim, bool exact, const float *u, const GeoPoint *pts, int nr, float *dat_row,
                         const float *w1, const float *w2, const float *w3, const Grid &g, const long long *off,
-                        cudaStream_t s) {
+                        cudaStream_t s, int stride) {
     if (nr <= 0) return;
     const int T = 128, B = (nr + T - 1) / T;
     if (ndim == 3) {
-        if (exact) k_extract<true, 3><<<B, T, 0, s>>>(u, pts, nr, dat_row, w1, w2, w3, g, off);
-        else k_extract<false, 3><<<B, T, 0, s>>>(u, pts, nr, dat_row, w1, w2, w3, g, off);
+        if (exact) k_extract<true, 3><<<B, T, 0, s>>>(u, pts, nr, dat_row, w1, w2, w3, g, off, stride);
+        else k_extract<false, 3><<<B, T, 0, s>>>(u, pts, nr, dat_row, w1, w2, w3, g, off, stride);
     } else {
-        if (exact) k_extract<true, 2><<<B, T, 0, s>>>(u, pts, nr, dat_row, w1, w2, w3, g, off);
-        else k_extract<false, 2><<<B, T, 0, s>>>(u, pts, nr, dat_row, w1, w2, w3, g, off);
+        if (exact) k_extract<true, 2><<<B, T, 0, s>>>(u, pts, nr, dat_row, w1, w2, w3, g, off, stride);
+        else k_extract<false, 2><<<B, T, 0, s>>>(u, pts, nr, dat_row, w1, w2, w3, g, off, stride);
     }
 }
 

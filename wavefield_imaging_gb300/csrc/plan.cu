@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <climits>
 #include <cstring>
 #include <vector>
 
@@ -36,6 +37,16 @@ using namespace awe;
     } while (0)
 
 namespace awe {
+
+// Fixed (mode < 0) or moving points.  sfDYNAWEFDcart2Dgpu applies the free
+// surface only with free=y (MDYNAWEFDcart2Dgpu.cu:393-396) where
+// sfAWEFDcart2Dgpu applies it always (MAWEFDcart2Dgpu.cu:424).
+static void set_move_mode(awe_plan *p, int mode, int src_rows, int rec_rows) {
+    p->move_mode = mode;
+    p->src_rows = src_rows;
+    p->rec_rows = rec_rows;
+    if (p->d.scheme == AWE_SCHEME_GPU && p->pa.geom == 0) p->pa.mask = (mode == AWE_MOVE_DYN && !p->d.fsrf) ? 0 : 1;
+}
 
 void plan_graph_drop(awe_plan *p) {
     if (p->gexec) cudaGraphExecDestroy(p->gexec);
@@ -309,9 +320,54 @@ awe_status awe_set_geometry(awe_plan *p, int ns, const float *sou, int nr, const
     }
     plan_graph_drop(p);  // the captured time loop baked in the old state
     CUDA_TRY(cudaSetDevice(p->device));
+    set_move_mode(p, -1, 1, 1);
     awe_status st = set_geometry_common(p, ns, sou, nr, rec);
     if (st == AWE_OK) p->geom_set = true;
     return st;
+}
+
+awe_status awe_set_moving_geometry(awe_plan *p, int ns, int nst, const float *sou, int nr, int nrt,
+                                   const float *rec, int mode) {
+    if (!p || ns < 0 || nr < 0 || nst < 1 || nrt < 1 || (ns > 0 && !sou) || (nr > 0 && !rec)) {
+        set_error("bad moving-geometry arguments (ns, nr >= 0; nst, nrt >= 1; coordinates for every entry)");
+        return AWE_ERR_INVALID;
+    }
+    const awe_desc &d = p->d;
+    if (mode != AWE_MOVE_PER_STEP && mode != AWE_MOVE_DYN) {
+        set_error("unknown moving-geometry mode %d", mode);
+        return AWE_ERR_INVALID;
+    }
+    if (mode == AWE_MOVE_DYN && !(d.scheme == AWE_SCHEME_GPU && d.coords == AWE_CART && d.ndim == 2)) {
+        set_error("AWE_MOVE_DYN follows sfDYNAWEFDcart2Dgpu: cartesian 2D, AWE_SCHEME_GPU");
+        return AWE_ERR_UNSUPPORTED;
+    }
+    if (d.scheme == AWE_SCHEME_GPU && (d.expl || d.refl)) {
+        set_error("moving geometry on the GPU-program scheme needs expl = 0 (unscaled injection)");
+        return AWE_ERR_UNSUPPORTED;
+    }
+    if (mode == AWE_MOVE_DYN) {
+        // the entries the run selects: k*(it+1) for k < n, it < nt
+        const long long last_s = (long long)(ns > 0 ? ns - 1 : 0) * d.nt, last_r = (long long)(nr > 0 ? nr - 1 : 0) * d.nt;
+        if ((ns > 0 && last_s >= (long long)ns * nst) || (nr > 0 && last_r >= (long long)nr * nrt)) {
+            set_error("AWE_MOVE_DYN reads entry (n-1)*nt of each table: need (ns-1)*nt < ns*nst and "
+                      "(nr-1)*nt < nr*nrt (ns=%d nst=%d nr=%d nrt=%d nt=%d)",
+                      ns, nst, nr, nrt, d.nt);
+            return AWE_ERR_INVALID;
+        }
+    }
+    if ((long long)ns * nst > INT_MAX || (long long)nr * nrt > INT_MAX) {
+        set_error("moving-geometry tables too large");
+        return AWE_ERR_INVALID;
+    }
+    plan_graph_drop(p);  // the captured time loop baked in the old state
+    CUDA_TRY(cudaSetDevice(p->device));
+    awe_status st = set_geometry_common(p, ns * nst, sou, nr * nrt, rec);
+    if (st != AWE_OK) return st;
+    p->ns = ns;
+    p->nr = nr;
+    set_move_mode(p, mode, nst, nrt);
+    p->geom_set = true;
+    return AWE_OK;
 }
 
 awe_status awe_set_shots(awe_plan *p, int nshots, const int *ns, const float *sou, const int *nr, const float *rec) {
@@ -340,6 +396,7 @@ awe_status awe_set_shots(awe_plan *p, int nshots, const int *ns, const float *so
         return AWE_ERR_INVALID;
     }
     CUDA_TRY(cudaSetDevice(p->device));
+    set_move_mode(p, -1, 1, 1);
     awe_status st = set_geometry_common(p, NS, sou, NR, rec);
     if (st != AWE_OK) return st;
     // points of shot s address field s
@@ -530,6 +587,10 @@ awe_status awe_gradient_device(awe_plan *p, const float *d_wav, int ncs, const f
     if (!p->model_set || !p->geom_set) {
         set_error("awe_set_model and awe_set_geometry must precede awe_gradient");
         return AWE_ERR_STATE;
+    }
+    if (p->move_mode >= 0) {
+        set_error("awe_gradient: the misfit gradient needs fixed sources and receivers (awe_set_geometry)");
+        return AWE_ERR_UNSUPPORTED;
     }
     if (ncs != 1 && ncs != p->ns) {
         set_error("wavelet has %d components; need 1 or ns=%d", ncs, p->ns);

@@ -48,6 +48,9 @@ struct awe_plan {
     std::vector<awe::GeoPoint> h_src, h_rec;
     std::vector<awe::Lint> h_src_lint;  // source corner indices in the reference's fdm axes
     bool sponge_deferred = false;  // a source node lies in the sponge band outside the boundary shell
+    // moving geometry (awe_set_moving_geometry): src/rec hold ns*src_rows and
+    // nr*rec_rows entries; move_mode < 0 = fixed points
+    int move_mode = -1, src_rows = 1, rec_rows = 1;
 
     // scheme-GPU specific
     float *aux = nullptr;              // boundary values (phase 1 -> phase 2)
@@ -103,6 +106,18 @@ awe_status deliver_snapshot(awe_plan *p, const float *d_frame, int isnap, int it
 awe_status flush_snapshots(awe_plan *p);
 
 awe_status set_geometry_common(awe_plan *p, int ns, const float *sou, int nr, const float *rec);
+
+// The n points of a table active at step it: the first one and the stride
+// between consecutive points (fixed points: the table itself, stride 1).
+struct PointsAt {
+    const GeoPoint *pts;
+    int stride;
+};
+inline PointsAt points_at(const awe_plan *p, const GeoPoint *tab, int n, int rows, int it) {
+    if (p->move_mode == AWE_MOVE_PER_STEP) return {tab + (size_t)(it < rows ? it : rows - 1) * n, 1};
+    if (p->move_mode == AWE_MOVE_DYN) return {tab, it + 1};
+    return {tab, 1};
+}
 
 // bracket one step-kernel launch with events when profiling is on
 void prof_begin(awe_plan *p, cudaStream_t s);

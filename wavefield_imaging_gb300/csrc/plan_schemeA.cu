@@ -340,7 +340,9 @@ awe_status planA_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, flo
     int itr = 0, isnap = 0;
     for (int it = 0; it < d.nt; it++) {
         if (p->ns > 0) {
-            launch_injectA(exact, d.ndim, cur, p->src, p->inj_scale, p->ns, d_wav, it, scaled, p->corner_off, s);
+            const PointsAt ps = points_at(p, p->src, p->ns, p->src_rows, it);
+            launch_injectA(exact, d.ndim, cur, ps.pts, p->inj_scale, p->ns, d_wav, it, scaled, p->corner_off, s,
+                           ps.stride);
             launches++;
         }
         prof_begin(p, s);
@@ -364,8 +366,9 @@ awe_status planA_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, flo
             row = it;
         }
         if (row >= 0 && p->nr > 0) {
-            launch_extract_off(d.ndim, exact, cur, p->rec, p->nr, d_dat + (size_t)row * p->nr, nullptr, nullptr,
-                               nullptr, g, p->corner_off, s);
+            const PointsAt pr = points_at(p, p->rec, p->nr, p->rec_rows, it);
+            launch_extract_off(d.ndim, exact, cur, pr.pts, p->nr, d_dat + (size_t)row * p->nr, nullptr, nullptr,
+                               nullptr, g, p->corner_off, s, pr.stride);
             launches++;
         }
         if (p->nsnap > 0 && it % d.jsnap == 0) {

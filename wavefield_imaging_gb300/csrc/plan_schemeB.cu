@@ -310,7 +310,9 @@ awe_status stepB_full(awe_plan *p, const StepBParams &sp0, const float *prv, con
     prof_end(p, s);
     launches++;
     if (p->ns > 0) {
-        launch_injectB_off(d.ndim, exact, nxt, p->vel, p->src, p->ns, d_wav, it, ncs, ncs == 1, p->corner_off, s);
+        const PointsAt ps = points_at(p, p->src, p->ns, p->src_rows, it);
+        launch_injectB_off(d.ndim, exact, nxt, p->vel, ps.pts, p->ns, d_wav, it, ncs, ncs == 1, p->corner_off, s,
+                           ps.stride);
         launches++;
     }
     if (d.dabc) {
@@ -385,8 +387,9 @@ awe_status planB_run_hooked(awe_plan *p, const float *d_wav, int ncs, float *d_d
             isnap++;
         }
         if (it % d.jdata == 0) {
-            launch_extract_off(d.ndim, exact, nxt, p->rec, p->nr, d_dat + (size_t)row * p->nr, pw1, p->w[1],
-                               p->w[2], g, p->corner_off, s);
+            const PointsAt pr = points_at(p, p->rec, p->nr, p->rec_rows, it);
+            launch_extract_off(d.ndim, exact, nxt, pr.pts, p->nr, d_dat + (size_t)row * p->nr, pw1, p->w[1],
+                               p->w[2], g, p->corner_off, s, pr.stride);
             launches += p->nr > 0;
             row++;
         }

@@ -61,6 +61,8 @@ class GradOpts(C.Structure):
 
 
 CKPT_BF16, CKPT_FP32, CKPT_FP16 = 0, 1, 2
+# awe_move_mode: one row of positions per step / sfDYNAWEFDcart2Dgpu's entry k*(it+1)
+MOVE_PER_STEP, MOVE_DYN = 0, 1
 
 SNAP_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_float), C.c_size_t)
 
@@ -107,6 +109,8 @@ def lib():
         ip = C.POINTER(C.c_int)
         L.awe_set_shots.argtypes = [vp, C.c_int, ip, fp, ip, fp]
         L.awe_set_shots.restype = C.c_int
+        L.awe_set_moving_geometry.argtypes = [vp, C.c_int, C.c_int, fp, C.c_int, C.c_int, fp, C.c_int]
+        L.awe_set_moving_geometry.restype = C.c_int
         dp = C.POINTER(C.c_double)
         L.awe_gradient.argtypes = [vp, fp, C.c_int, fp, C.POINTER(GradOpts), dp, dp, fp]
         L.awe_gradient_device.argtypes = [vp, vp, C.c_int, vp, C.POINTER(GradOpts), vp, dp, vp, vp]
@@ -181,6 +185,18 @@ class Plan:
         rec = np.ascontiguousarray(rec, np.float32).reshape(-1, nd)
         self.ns, self.nr = sou.shape[0], rec.shape[0]
         _check(lib().awe_set_geometry(self._h, self.ns, _fp(sou), self.nr, _fp(rec)))
+
+    def set_moving_geometry(self, sou, nst: int, rec, nrt: int, mode: int = MOVE_PER_STEP):
+        """sou: ns*nst points, rec: nr*nrt points (awe_set_geometry's
+        coordinate order); at each step ns sources and nr receivers use the
+        entries `mode` selects (awe_set_moving_geometry)."""
+        nd = self.desc.ndim
+        sou = np.ascontiguousarray(sou, np.float32).reshape(-1, nd)
+        rec = np.ascontiguousarray(rec, np.float32).reshape(-1, nd)
+        if sou.shape[0] % nst or rec.shape[0] % nrt:
+            raise ValueError("tables must hold ns*nst and nr*nrt points")
+        self.ns, self.nr = sou.shape[0] // nst, rec.shape[0] // nrt
+        _check(lib().awe_set_moving_geometry(self._h, self.ns, nst, _fp(sou), self.nr, nrt, _fp(rec), mode))
 
     def set_shots(self, shots):
         """shots: list of (sou [ns][3], rec [nr][3]) advanced together (spherical 3D)."""

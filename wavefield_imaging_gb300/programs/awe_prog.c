@@ -5,6 +5,8 @@
  *   sfAWEFDspher3Dgpu (CODE/MAWEFDspher3Dgpu.cu)
  *   sfAWEFDcart2Dcpu  (CODE/MAWEFDcart2Dcpu.c, run on the GPU)
  *   sfAWEFDcart3Dcpu  (CODE/MAWEFDcart3Dcpu.c, run on the GPU)
+ *   sfDYNAWEFDcart2Dgpu (CODE/MDYNAWEFDcart2Dgpu.cu: moving sources and
+ *     receivers, sou/rec n2 = points per step, n3 = table rows)
  * on the engine's C-ABI (include/awe.h).  One source; the program name picks
  * the geometry and the scheme.  Usage as the reference:
  *
@@ -81,6 +83,8 @@ int main(int argc, char **argv) {
     const int spher = strstr(prog, "spher") != NULL;
     const int ndim = strstr(prog, "3D") != NULL ? 3 : 2;
     const int cart2d = !spher && ndim == 2;
+    const int dyn = strstr(prog, "DYNAWEFD") != NULL;
+    if (dyn && !(cart2d && strstr(prog, "gpu"))) die(prog, "the moving-geometry program is sfDYNAWEFDcart2Dgpu");
     const int scheme = strstr(prog, "cpu") != NULL ? AWE_SCHEME_CPU : AWE_SCHEME_GPU;
     if (scheme == AWE_SCHEME_CPU && spher) die(prog, "the spherical cpu programs are not provided");
     if (!strstr(prog, "AWEFD")) die(prog, "run as sfAWEFD{cart,spher}{2D,3D}gpu or sfAWEFDcart{2D,3D}cpu");
@@ -91,6 +95,9 @@ int main(int argc, char **argv) {
     int fsrf = 0, dabc = 0, snap, bnds, expl, refl = 0, adj = 0, verb = 0, sinc = 0;
     if (scheme == AWE_SCHEME_CPU) {
         snap = bnds = expl = 0;
+    } else if (dyn) { /* MDYNAWEFDcart2Dgpu.cu:71-74: no expl/refl (unscaled injection) */
+        snap = 1;
+        bnds = expl = 0;
     } else {
         snap = cart2d || (spher && ndim == 2);
         bnds = cart2d;
@@ -101,13 +108,18 @@ int main(int argc, char **argv) {
     rsf_get_bool("dabc", &dabc);
     rsf_get_bool("snap", &snap);
     rsf_get_bool("bnds", &bnds);
-    rsf_get_bool("expl", &expl);
-    if (cart2d && scheme == AWE_SCHEME_GPU) rsf_get_bool("refl", &refl);
+    if (!dyn) rsf_get_bool("expl", &expl);
+    if (cart2d && scheme == AWE_SCHEME_GPU && !dyn) rsf_get_bool("refl", &refl);
     rsf_get_bool("adj", &adj);
     rsf_get_bool("verb", &verb);
     rsf_get_bool("sinc", &sinc);
     if (adj && scheme != AWE_SCHEME_CPU) die(prog, "adj=y (back-injection imaging) is provided for the cpu programs");
     if (sinc) die(prog, "sinc=y injection is not provided");
+    if (dyn) {
+        int jd = 1;
+        rsf_get_int("jdata", &jd);
+        if (jd != 1) die(prog, "jdata must be 1 (the reference writes every step into a buffer of nt/jdata rows)");
+    }
     {
         static const char *win[] = {"nqz", "nqx", "nqy", "oqz", "oqx", "oqy", "dqz", "dqx", "dqy"};
         for (int i = 0; i < 9; i++)
@@ -172,20 +184,27 @@ int main(int argc, char **argv) {
     /* points: n1 coordinates, count = n2 (* n3 for the programs that read it:
      * MAWEFDcart2Dgpu.cu:120, MAWEFDcart3Dgpu.cu:105, MAWEFDspher2Dgpu.cu:104) */
     const int ncoord = ndim;
-    const int use_n3 = scheme == AWE_SCHEME_GPU && !(spher && ndim == 3);
+    const int use_n3 = scheme == AWE_SCHEME_GPU && !(spher && ndim == 3) && !dyn;
     const int ns = rsf_n(Fsou, 2) * (use_n3 ? rsf_n(Fsou, 3) : 1);
     const int nr = rsf_n(Frec, 2) * (use_n3 ? rsf_n(Frec, 3) : 1);
+    /* sfDYNAWEFDcart2Dgpu: n3 = rows of the position tables
+     * (MDYNAWEFDcart2Dgpu.cu:103-111), ns*nst and nr*nrt points read */
+    const int nst = dyn ? rsf_n(Fsou, 3) : 1, nrt = dyn ? rsf_n(Frec, 3) : 1;
+    const size_t nse = (size_t)ns * nst, nre = (size_t)nr * nrt;
     if (rsf_n(Fsou, 1) < ncoord || rsf_n(Frec, 1) < ncoord) die(prog, "sou/rec need one coordinate per axis on n1");
-    float *sou = malloc(sizeof(float) * (size_t)ns * ncoord), *rec = malloc(sizeof(float) * (size_t)nr * ncoord);
-    float tmp[4];
-    for (int i = 0; i < ns; i++) {
-        if (rsf_read(Fsou, tmp, (size_t)rsf_n(Fsou, 1)) != (size_t)rsf_n(Fsou, 1)) die(prog, "short read (sou)");
-        memcpy(sou + (size_t)i * ncoord, tmp, sizeof(float) * ncoord);
+    float *sou = malloc(sizeof(float) * (nse > 0 ? nse : 1) * ncoord);
+    float *rec = malloc(sizeof(float) * (nre > 0 ? nre : 1) * ncoord);
+    const size_t n1s = (size_t)rsf_n(Fsou, 1), n1r = (size_t)rsf_n(Frec, 1);
+    float *tmp = malloc(sizeof(float) * (n1s > n1r ? n1s : n1r));
+    for (size_t i = 0; i < nse; i++) {
+        if (rsf_read(Fsou, tmp, n1s) != n1s) die(prog, "short read (sou)");
+        memcpy(sou + i * ncoord, tmp, sizeof(float) * ncoord);
     }
-    for (int i = 0; i < nr; i++) {
-        if (rsf_read(Frec, tmp, (size_t)rsf_n(Frec, 1)) != (size_t)rsf_n(Frec, 1)) die(prog, "short read (rec)");
-        memcpy(rec + (size_t)i * ncoord, tmp, sizeof(float) * ncoord);
+    for (size_t i = 0; i < nre; i++) {
+        if (rsf_read(Frec, tmp, n1r) != n1r) die(prog, "short read (rec)");
+        memcpy(rec + i * ncoord, tmp, sizeof(float) * ncoord);
     }
+    free(tmp);
     const size_t nmodel = (size_t)d.n[0] * d.n[1] * d.n[2];
     float *vel = malloc(sizeof(float) * nmodel), *rfl = NULL, *den = NULL;
     if (rsf_read(Fvel, vel, nmodel) != nmodel) die(prog, "short read (vel)");
@@ -247,6 +266,9 @@ int main(int argc, char **argv) {
     if (awe_set_model(plan, vel, den, scheme == AWE_SCHEME_GPU ? rfl : NULL) != AWE_OK) die(prog, awe_last_error());
     if (img2d) { /* injection at the receivers (expl=n) or the sources (expl=y); no traces */
         if (awe_set_geometry(plan, expl ? ns : nr, expl ? sou : rec, 0, NULL) != AWE_OK) die(prog, awe_last_error());
+    } else if (dyn) {
+        if (awe_set_moving_geometry(plan, ns, nst, sou, nr, nrt, rec, AWE_MOVE_DYN) != AWE_OK)
+            die(prog, awe_last_error());
     } else if (awe_set_geometry(plan, ns, sou, nr, rec) != AWE_OK) {
         die(prog, awe_last_error());
     }
