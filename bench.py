@@ -419,7 +419,7 @@ def run_grad(args):
     plan.set_model(vtrue)
     dobs = plan.forward(wav)
     plan.set_model(v0)
-    fmt = {"bf16": awe.CKPT_BF16, "fp16": awe.CKPT_FP16, "fp32": awe.CKPT_FP32}[args.ckpt]
+    fmt = {"bfp16": awe.CKPT_BFP16, "bf16": awe.CKPT_BF16, "fp16": awe.CKPT_FP16, "fp32": awe.CKPT_FP32}[args.ckpt]
     d_wav = torch.from_numpy(wav).cuda()
     d_dobs = torch.from_numpy(dobs).cuda()
     ngrad = int(np.prod(w["n"]))
@@ -608,7 +608,7 @@ def run_batch_grad(args):
     v0 = smooth(vtrue, 100.0 / 5.0)
     nxm = vtrue.shape[0]
     wav = ricker(nt, 0.005, 5.0)
-    fmt = {"bf16": awe.CKPT_BF16, "fp16": awe.CKPT_FP16, "fp32": awe.CKPT_FP32}[args.ckpt]
+    fmt = {"bfp16": awe.CKPT_BFP16, "bf16": awe.CKPT_BF16, "fp16": awe.CKPT_FP16, "fp32": awe.CKPT_FP32}[args.ckpt]
     desc = awe.make_desc(2, (nz, nxm), (5.0, 5.0), (0.0, 0.0), nt, 0.005, nb=40, fdorder=8, dabc=1, expl=1,
                          precision=awe.FAST)
     batch = awe.Batch(desc, shots, device=local)
@@ -858,7 +858,8 @@ def main():
                          "batch2d: the batched 2D survey")
     ap.add_argument("--shots", type=int, default=0,
                     help="shots: batch2d/batchgrad2d (default 256), spher3d (default 1; 16 on the survey track)")
-    ap.add_argument("--ckpt", default="bf16", choices=["bf16", "fp16", "fp32"], help="checkpoint storage (grad*)")
+    ap.add_argument("--ckpt", default="bfp16", choices=["bfp16", "bf16", "fp16", "fp32"],
+                    help="checkpoint storage (grad*): bfp16 = 16-bit block floating point")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -197,10 +197,13 @@ awe_status awe_profile_read(awe_plan *plan, double *step_kernel_ms, long long *s
 /* ---- Misfit gradient (no counterpart in the reference: its adj=y mode
  * back-injects data for an image, MAWEFDcart2Dgpu.cu:386-396) ---- */
 /* Checkpoint storage: BF16 or FP16 with one FP32 scale (the level's max |v|)
- * per stored level, or FP32.  The recomputed levels inherit the rounding:
+ * per stored level, FP32 copies, or block floating point (BFP16: 16-bit
+ * integers with one FP32 scale per 64 consecutive cells, 2.06 bytes per
+ * cell, error at most 1/65534 of the block's largest value; the default when
+ * no options are given).  The recomputed levels inherit the rounding:
  * measured gradient error against an FP64 adjoint on the test cases ~1e-2
- * (BF16), ~1e-3 (FP16), ~1e-7 (FP32). */
-typedef enum { AWE_CKPT_BF16 = 0, AWE_CKPT_FP32 = 1, AWE_CKPT_FP16 = 2 } awe_ckpt_format;
+ * (BF16), ~1e-3 (FP16), ~1e-4 (BFP16), ~1e-7 (FP32). */
+typedef enum { AWE_CKPT_BF16 = 0, AWE_CKPT_FP32 = 1, AWE_CKPT_FP16 = 2, AWE_CKPT_BFP16 = 3 } awe_ckpt_format;
 
 typedef struct {
     int ckpt_every;  /* forward steps between checkpoints; <= 0: ceil(sqrt(nt)) */

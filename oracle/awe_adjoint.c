@@ -167,6 +167,27 @@ static double quantize(double x, double scale, int bits) {
     return ldexp(nearbyint(t), e - bits) * scale;
 }
 
+/* Block floating point as the engine's AWE_CKPT_BFP16 checkpoints store a
+ * level (k_bfp_store): the level rounded to float, then per block of 64
+ * consecutive cells s = max|v| / 32767, q = round(v * (1/s)) (half to even,
+ * clamped to +-32767), v' = q * s, all in float; blocks with max|v| <= 1e-30
+ * are stored as zeros. */
+static void quantize_bfp16(double *u, size_t n) {
+    for (size_t b = 0; b < n; b += 64) {
+        const size_t e = b + 64 < n ? b + 64 : n;
+        float m = 0.f;
+        for (size_t i = b; i < e; i++) m = fabsf((float)u[i]) > m ? fabsf((float)u[i]) : m;
+        const float sc = m > 1e-30f ? m / 32767.f : 0.f;
+        const float inv = m > 1e-30f ? 1.f / sc : 0.f;
+        for (size_t i = b; i < e; i++) {
+            const float t = (float)u[i] * inv;
+            float q = nearbyintf(t);
+            q = q > 32767.f ? 32767.f : (q < -32767.f ? -32767.f : q);
+            u[i] = (double)(q * sc);
+        }
+    }
+}
+
 /* The model is either velocity in float (vel_in: vel2 = v * (v * dt^2) in
  * float, as the engine) or slowness squared in double (m_in: vel2 = dt^2 / m
  * in double, so that finite differences of J are free of float rounding). */
@@ -324,12 +345,17 @@ static int grad_impl(const orc_par *p, int ndim, int jdata, const float *vel_in,
 
     /* checkpointed recompute: every ckpt_every steps the two levels V[k0-1],
      * V[k0] are rounded to ckpt_bits significant bits (one scale, the level's
-     * max |v|, per level) and the segment's later levels recomputed from them */
-    if (ckpt_bits > 0 && ckpt_every > 0)  /* last segment first: each restart reads levels of the exact forward */
+     * max |v|, per level; ckpt_bits < 0: block floating point) and the
+     * segment's later levels recomputed from them */
+    if (ckpt_bits != 0 && ckpt_every > 0)  /* last segment first: each restart reads levels of the exact forward */
         for (int k0 = ((nt - 1) / ckpt_every) * ckpt_every; k0 >= 0; k0 -= ckpt_every) {
             for (int lv = k0 - 1; lv <= k0; lv++) {
                 if (lv < 0) continue;
                 double *u = V + (size_t)lv * np, amax = 0;
+                if (ckpt_bits < 0) {
+                    quantize_bfp16(u, np);
+                    continue;
+                }
                 for (size_t i = 0; i < np; i++) amax = fabs(u[i]) > amax ? fabs(u[i]) : amax;
                 for (size_t i = 0; i < np; i++) u[i] = quantize(u[i], amax, ckpt_bits);
             }
@@ -430,7 +456,8 @@ int orc_grad_m(const orc_par *p, int ndim, int jdata, const double *m, const flo
 
 /* As orc_grad, with the adjoint sweep reading levels recomputed from
  * checkpoints rounded to `bits` significant bits every `every` steps (8: the
- * engine's BF16 checkpoints, 11: FP16 with its subnormal range, 24: FP32). */
+ * engine's BF16 checkpoints, 11: FP16 with its subnormal range, 24: FP32,
+ * -1: the block floating point of AWE_CKPT_BFP16). */
 int orc_grad_ckpt(const orc_par *p, int ndim, int jdata, const float *vel_in, const float *wav, int ns,
                   const float *sou, int nr, const float *rec, const float *dobs, int every, int bits, double *grad,
                   double *misfit, double *dsyn) {

@@ -290,7 +290,8 @@ def misfit_gradient(p: dict, vel, wav, sou, rec, dobs, jdata: int = 1, m=None, c
     engine does) or, when `m` is given, slowness squared in float64 (for
     finite differences free of float rounding; `vel` then only sets the shape).
     ckpt_bits > 0 emulates checkpointed recompute from levels rounded to that
-    many significant bits every ckpt_every steps (8 = BF16).
+    many significant bits every ckpt_every steps (8 = BF16); ckpt_bits = -1
+    emulates the block floating point checkpoints (AWE_CKPT_BFP16).
     Returns (grad [model shape] float64, J, dsyn [nsmp][nr] float64)."""
     q = make_par(p)
     ndim = len(p["n"])

@@ -104,6 +104,7 @@ def test_batch_gradient_is_the_sum_of_per_shot_gradients():
         b.set_model(vel)
         g32, J32 = b.gradient(wav, dobs, ckpt_format=awe.CKPT_FP32)
         g16, J16 = b.gradient(wav, dobs, ckpt_format=awe.CKPT_BF16)
+        gbf, Jbf = b.gradient(wav, dobs, ckpt_format=awe.CKPT_BFP16)
         b.tune(steps=5)
         g32b, _ = b.gradient(wav, dobs, ckpt_format=awe.CKPT_FP32)
     assert abs(J32 - Jsum) <= 1e-5 * Jsum
@@ -111,3 +112,4 @@ def test_batch_gradient_is_the_sum_of_per_shot_gradients():
     assert rel_l2(g32, gsum) <= 1e-4
     assert rel_l2(g32b, gsum) <= 1e-4  # another tile shape after tuning
     assert rel_l2(g16, gsum) <= 3e-2
+    assert Jbf == J32 and rel_l2(gbf, gsum) <= 1e-3  # block floating point checkpoints

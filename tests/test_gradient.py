@@ -38,16 +38,19 @@ def test_gradient_matches_fp64_oracle(nd, fsrf):
         g32, J32, d32 = p.gradient(wav, dobs, ckpt_format=awe.CKPT_FP32, return_dsyn=True)
         gb, Jb = p.gradient(wav, dobs, ckpt_format=awe.CKPT_BF16)
         gh, Jh = p.gradient(wav, dobs, ckpt_format=awe.CKPT_FP16)
+        gf, Jf = p.gradient(wav, dobs, ckpt_format=awe.CKPT_BFP16)
     assert rel_l2(d32, dref) <= 1e-5
     assert abs(J32 - Jref) <= 1e-5 * abs(Jref)
-    assert Jb == J32 and Jh == J32  # the misfit comes from the forward pass, not the checkpoints
+    assert Jb == J32 and Jh == J32 and Jf == J32  # the misfit comes from the forward pass, not the checkpoints
     # FP32 checkpoints: only the FP32 arithmetic differs from the FP64 oracle
     assert rel_l2(g32, gref) <= 1e-4
     # 16-bit checkpoints: the recomputed segments start from levels rounded to
-    # 8 (BF16) or 11 (FP16) significant bits.  The oracle emulates the same
-    # rounding in FP64; the engine must match that, and the error it leaves
-    # against the exact gradient is the checkpoint format's, not the kernels'
-    for g16, bits, bound in ((gb, 8, 3e-2), (gh, 11, 4e-3)):
+    # 8 (BF16) or 11 (FP16) significant bits, or to 16-bit integers with a
+    # scale per 64 cells (BFP16, emulated as ckpt_bits=-1).  The oracle
+    # emulates the same rounding in FP64; the engine must match that, and the
+    # error it leaves against the exact gradient is the checkpoint format's,
+    # not the kernels'.  BFP16 meets the 1e-3 gradient bound at 2 bytes/cell.
+    for g16, bits, bound in ((gb, 8, 3e-2), (gh, 11, 4e-3), (gf, -1, 1e-3)):
         gq, _, _ = oracle.misfit_gradient(par, vel, wav, sou, rec, dobs, ckpt_every=T, ckpt_bits=bits)
         assert rel_l2(g16, gq) <= 0.5 * rel_l2(gq, gref) + 1e-4
         assert rel_l2(g16, gref) <= bound

@@ -11,7 +11,7 @@ from __future__ import annotations
 
 import torch
 
-from .engine import CKPT_BF16
+from .engine import CKPT_BFP16
 
 
 class MisfitFunction(torch.autograd.Function):
@@ -29,6 +29,6 @@ class MisfitFunction(torch.autograd.Function):
         return gJ * g, None, None, None, None, None
 
 
-def misfit(m, plan, wav, dobs, ckpt_every: int = 0, ckpt_format: int = CKPT_BF16):
+def misfit(m, plan, wav, dobs, ckpt_every: int = 0, ckpt_format: int = CKPT_BFP16):
     """0.5 ||d(m) - dobs||^2 as a differentiable scalar of m = 1/v^2."""
     return MisfitFunction.apply(m, plan, wav, dobs, ckpt_every, ckpt_format)

@@ -141,6 +141,11 @@ void launch_ckpt_store16(bool fp16, const float *u, long long n, unsigned int *a
                          cudaStream_t s);
 void launch_ckpt_load16(bool fp16, const void *q, long long n, const float *scale, float *u, int grid,
                         cudaStream_t s);
+// block floating point checkpoints: kBfpBlock consecutive cells share one FP32 scale
+constexpr int kBfpBlock = 64;
+constexpr float kBfpTiny = 1e-30f;  // blocks with max |v| <= this are stored as zero
+void launch_ckpt_store_bfp(const float *u, long long n, short *q, float *scale, int grid, cudaStream_t s);
+void launch_ckpt_load_bfp(const short *q, const float *scale, long long n, float *u, int grid, cudaStream_t s);
 void launch_grad_fold(const double *G, const float *vel2, float dt, const Grid &g, int nb, const int *n, int nd,
                       double *out, cudaStream_t s);
 

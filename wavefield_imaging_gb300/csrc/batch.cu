@@ -44,6 +44,7 @@ struct awe_batch {
     std::vector<GeoPoint> h_rec;
     // misfit gradient state
     int gT = 0, gseg = 0, gfmt = -1;
+    long long gscale_per = 0;  // checkpoint scales per level: one per shot, or per 64-cell block (BFP16)
     float *slots = nullptr, *gX = nullptr, *gY = nullptr, *res = nullptr, *scales = nullptr, *dobs = nullptr;
     void *ckpt = nullptr;
     double *G = nullptr, *part = nullptr, *grad = nullptr;
@@ -487,7 +488,8 @@ static awe_status grad_alloc(awe_batch *b, int T, int fmt) {
     const size_t es = fmt == AWE_CKPT_FP32 ? 4 : 2;
     awe_status st = balloc(b, (void **)&b->slots, (size_t)(T + 1) * b->cells * sizeof(float));
     if (st == AWE_OK) st = balloc(b, &b->ckpt, (size_t)2 * nseg * b->cells * es);
-    if (st == AWE_OK) st = balloc(b, (void **)&b->scales, (size_t)2 * nseg * b->shots.size() * sizeof(float));
+    b->gscale_per = fmt == AWE_CKPT_BFP16 ? (b->cells + kBfpBlock - 1) / kBfpBlock : (long long)b->shots.size();
+    if (st == AWE_OK) st = balloc(b, (void **)&b->scales, (size_t)2 * nseg * b->gscale_per * sizeof(float));
     if (st != AWE_OK) return st;
     if (!b->gX) {
         const size_t cb = (size_t)b->cells * sizeof(float);
@@ -542,7 +544,7 @@ static awe_status grad_sequence(awe_batch *b, cudaStream_t s) {
     const int T = b->gT, ns = (int)b->shots.size(), nitems = (int)b->items.size();
     const size_t es = b->gfmt == AWE_CKPT_FP32 ? 4 : 2;
     auto ck = [&](int idx) { return (void *)((char *)b->ckpt + (size_t)idx * cells * es); };
-    auto sc = [&](int idx) { return b->scales + (size_t)idx * ns; };
+    auto sc = [&](int idx) { return b->scales + (size_t)idx * b->gscale_per; };
     // forward with checkpoints of both levels at every segment start
     CUDA_TRY(cudaMemsetAsync(b->u[0], 0, cb, s));
     CUDA_TRY(cudaMemsetAsync(b->u[1], 0, cb, s));
@@ -599,9 +601,10 @@ awe_status awe_batch_gradient(awe_batch *b, const float *wav, const float *dobs,
         set_error("awe_batch_set_model must precede awe_batch_gradient");
         return AWE_ERR_STATE;
     }
-    awe_grad_opts o{0, AWE_CKPT_BF16};
+    awe_grad_opts o{0, AWE_CKPT_BFP16};
     if (opts) o = *opts;
-    if (o.ckpt_format != AWE_CKPT_BF16 && o.ckpt_format != AWE_CKPT_FP32 && o.ckpt_format != AWE_CKPT_FP16) {
+    if (o.ckpt_format != AWE_CKPT_BF16 && o.ckpt_format != AWE_CKPT_FP32 && o.ckpt_format != AWE_CKPT_FP16 &&
+        o.ckpt_format != AWE_CKPT_BFP16) {
         set_error("awe_batch_gradient: unknown checkpoint format %d", o.ckpt_format);
         return AWE_ERR_INVALID;
     }

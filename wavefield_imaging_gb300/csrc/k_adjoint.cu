@@ -359,6 +359,49 @@ void launch_ckpt_load16(bool fp16, const void *q, long long n, const float *scal
     else k_dequant16<__nv_bfloat16><<<grid, 256, 0, s>>>((const __nv_bfloat16 *)q, n, scale, u);
 }
 
+// Block floating point: each block of 64 consecutive cells keeps 16-bit
+// integers q = round(v / s) and one FP32 scale s = max|v| / 32767 of the
+// block, so the error is at most s/2 - relative to the block's largest value
+// 2^-16, against BF16's 2^-9 per value.  One warp per block: lane l holds
+// cells l and l + 32 (coalesced 128-byte loads, 64-byte stores); the
+// division and the reciprocal are IEEE round-to-nearest so a host
+// restatement gets the same integers.  Unlike the per-level formats no
+// separate max pass over the level is needed.
+__global__ void k_bfp_store(const float *__restrict__ u, long long n, short *__restrict__ q,
+                            float *__restrict__ scale) {
+    const int lane = threadIdx.x & 31;
+    const long long nblk = (n + kBfpBlock - 1) / kBfpBlock;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long b = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); b < nblk; b += warps) {
+        const long long i0 = b * kBfpBlock + lane, i1 = i0 + 32;
+        const float v0 = i0 < n ? u[i0] : 0.f, v1 = i1 < n ? u[i1] : 0.f;
+        float m = fmaxf(fabsf(v0), fabsf(v1));
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        // blocks at or below kBfpTiny store zeros (keeps s and 1/s normal floats)
+        const float sc = m > kBfpTiny ? __fdiv_rn(m, 32767.f) : 0.f;
+        const float inv = m > kBfpTiny ? __frcp_rn(sc) : 0.f;
+        const int a0 = max(-32767, min(32767, __float2int_rn(__fmul_rn(v0, inv))));
+        const int a1 = max(-32767, min(32767, __float2int_rn(__fmul_rn(v1, inv))));
+        if (i0 < n) q[i0] = (short)a0;
+        if (i1 < n) q[i1] = (short)a1;
+        if (lane == 0) scale[b] = sc;
+    }
+}
+
+__global__ void k_bfp_load(const short *__restrict__ q, const float *__restrict__ scale, long long n,
+                           float *__restrict__ u) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        u[i] = __fmul_rn(__int2float_rn(q[i]), scale[i / kBfpBlock]);
+}
+
+void launch_ckpt_store_bfp(const float *u, long long n, short *q, float *scale, int grid, cudaStream_t s) {
+    k_bfp_store<<<grid, 256, 0, s>>>(u, n, q, scale);
+}
+
+void launch_ckpt_load_bfp(const short *q, const float *scale, long long n, float *u, int grid, cudaStream_t s) {
+    k_bfp_load<<<grid, 256, 0, s>>>(q, scale, n, u);
+}
+
 // ---------------------------------------------------------------------------
 // dJ/dm on the model grid: dJ/dvel2 * (-vel2^2 / dt^2) per padded cell (vel2 =
 // v^2 dt^2, m = 1/v^2; zero where vel2 is zero), summed over the padded cells

@@ -429,6 +429,12 @@ void launch_batch_ckpt(bool store, int fmt, const BatchShot *shots, int nshots, 
         else cudaMemcpyAsync(u, q, (size_t)cells * sizeof(float), cudaMemcpyDeviceToDevice, s);
         return;
     }
+    if (fmt == AWE_CKPT_BFP16) {  // blocks of 64 cells over the concatenated fields, scales per block
+        const int grid = (int)((cells + 255) / 256 < 4096 ? (cells + 255) / 256 : 4096);
+        if (store) launch_ckpt_store_bfp(u, cells, (short *)q, scales, grid, s);
+        else launch_ckpt_load_bfp((const short *)q, scales, cells, u, grid, s);
+        return;
+    }
     if (fmt == AWE_CKPT_FP16) {
         if (store) k_batch_ckpt_store<__half><<<nshots, 512, 0, s>>>(shots, u, (__half *)q, scales, n1);
         else k_batch_ckpt_load<__half><<<nshots, 512, 0, s>>>(shots, (const __half *)q, scales, u, n1);

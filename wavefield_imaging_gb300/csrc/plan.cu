@@ -596,7 +596,7 @@ awe_status awe_gradient_device(awe_plan *p, const float *d_wav, int ncs, const f
         set_error("wavelet has %d components; need 1 or ns=%d", ncs, p->ns);
         return AWE_ERR_INVALID;
     }
-    awe_grad_opts o{0, AWE_CKPT_BF16};
+    awe_grad_opts o{0, AWE_CKPT_BFP16};
     if (opts) o = *opts;
     CUDA_TRY(cudaSetDevice(p->device));
     cudaStream_t s = stream ? (cudaStream_t)stream : p->stream;

@@ -34,7 +34,8 @@ struct GradState {
     // generic path: (T + 1) segment levels V_k; TMA path: T slots of L(V_k)
     float *slots = nullptr;
     void *ckpt = nullptr;    // 2 * nseg levels
-    float *scales = nullptr; // 2 * nseg (16-bit formats)
+    float *scales = nullptr; // 2 * nseg (BF16/FP16), 2 * nseg * blocks (block floating point)
+    long long nblk = 0;      // scale blocks per level (block floating point)
     unsigned int *amax = nullptr;
     float *X = nullptr, *Y = nullptr, *kap = nullptr;
     double *G = nullptr;
@@ -72,7 +73,8 @@ static awe_status grad_alloc(awe_plan *p, int T, int fmt) {
     st->tma = p->use_tma && d.precision == AWE_FAST;
     AWE_TRY(dev_alloc(p, (void **)&st->slots, (size_t)(st->tma ? T : T + 1) * cells * sizeof(float)));
     AWE_TRY(dev_alloc(p, &st->ckpt, (size_t)2 * st->nseg * cells * es));
-    AWE_TRY(dev_alloc(p, (void **)&st->scales, (size_t)2 * st->nseg * sizeof(float)));
+    st->nblk = fmt == AWE_CKPT_BFP16 ? ((long long)cells + kBfpBlock - 1) / kBfpBlock : 1;
+    AWE_TRY(dev_alloc(p, (void **)&st->scales, (size_t)2 * st->nseg * st->nblk * sizeof(float)));
     AWE_TRY(dev_alloc(p, (void **)&st->amax, sizeof(unsigned int)));
     AWE_TRY(dev_alloc(p, (void **)&st->X, cells * sizeof(float)));
     AWE_TRY(dev_alloc(p, (void **)&st->Y, cells * sizeof(float)));
@@ -113,7 +115,10 @@ static int grid_for(long long n) {
 static awe_status ckpt_store(awe_plan *p, int idx, const float *u, cudaStream_t s) {
     GradState *st = p->grad;
     const long long cells = p->g.cells();
-    if (st->fmt != AWE_CKPT_FP32) {
+    if (st->fmt == AWE_CKPT_BFP16) {
+        short *q = (short *)st->ckpt + (size_t)idx * cells;
+        launch_ckpt_store_bfp(u, cells, q, st->scales + (size_t)idx * st->nblk, grid_for(cells), s);
+    } else if (st->fmt != AWE_CKPT_FP32) {
         void *q = (char *)st->ckpt + (size_t)idx * cells * 2;
         launch_ckpt_store16(st->fmt == AWE_CKPT_FP16, u, cells, st->amax, q, st->scales + idx, grid_for(cells), s);
     } else {
@@ -126,7 +131,10 @@ static awe_status ckpt_store(awe_plan *p, int idx, const float *u, cudaStream_t 
 static awe_status ckpt_load(awe_plan *p, int idx, float *u, cudaStream_t s) {
     GradState *st = p->grad;
     const long long cells = p->g.cells();
-    if (st->fmt != AWE_CKPT_FP32) {
+    if (st->fmt == AWE_CKPT_BFP16) {
+        const short *q = (const short *)st->ckpt + (size_t)idx * cells;
+        launch_ckpt_load_bfp(q, st->scales + (size_t)idx * st->nblk, cells, u, grid_for(cells), s);
+    } else if (st->fmt != AWE_CKPT_FP32) {
         const void *q = (const char *)st->ckpt + (size_t)idx * cells * 2;
         launch_ckpt_load16(st->fmt == AWE_CKPT_FP16, q, cells, st->scales + idx, u, grid_for(cells), s);
     } else {
@@ -160,7 +168,8 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
     int T = o.ckpt_every > 0 ? o.ckpt_every : (int)std::ceil(std::sqrt((double)d.nt));
     if (T > d.nt) T = d.nt;
     if (T < 1) T = 1;
-    if (o.ckpt_format != AWE_CKPT_BF16 && o.ckpt_format != AWE_CKPT_FP32 && o.ckpt_format != AWE_CKPT_FP16) {
+    if (o.ckpt_format != AWE_CKPT_BF16 && o.ckpt_format != AWE_CKPT_FP32 && o.ckpt_format != AWE_CKPT_FP16 &&
+        o.ckpt_format != AWE_CKPT_BFP16) {
         set_error("awe_gradient: unknown checkpoint format %d", o.ckpt_format);
         return AWE_ERR_INVALID;
     }

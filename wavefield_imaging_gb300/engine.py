@@ -60,7 +60,7 @@ class GradOpts(C.Structure):
     _fields_ = [("ckpt_every", C.c_int), ("ckpt_format", C.c_int)]
 
 
-CKPT_BF16, CKPT_FP32, CKPT_FP16 = 0, 1, 2
+CKPT_BF16, CKPT_FP32, CKPT_FP16, CKPT_BFP16 = 0, 1, 2, 3
 # awe_move_mode: one row of positions per step / sfDYNAWEFDcart2Dgpu's entry k*(it+1)
 MOVE_PER_STEP, MOVE_DYN = 0, 1
 
@@ -219,7 +219,7 @@ class Plan:
         _check(lib().awe_forward(self._h, _fp(wav), ncs, _fp(dat), _fp(wfl)))
         return (dat, wfl) if snapshots else dat
 
-    def gradient(self, wav, dobs, ckpt_every: int = 0, ckpt_format: int = CKPT_BF16, return_dsyn: bool = False):
+    def gradient(self, wav, dobs, ckpt_every: int = 0, ckpt_format: int = CKPT_BFP16, return_dsyn: bool = False):
         """Misfit J = 0.5 ||d - dobs||^2 and dJ/dm (m = 1/v^2) on the model
         grid (float64, model shape).  Returns (grad, J[, dsyn])."""
         wav = np.ascontiguousarray(wav, np.float32)
@@ -235,7 +235,7 @@ class Plan:
         return (grad, J.value, dsyn) if return_dsyn else (grad, J.value)
 
     def gradient_device(self, d_wav: int, ncs: int, d_dobs: int, d_grad: int, ckpt_every: int = 0,
-                        ckpt_format: int = CKPT_BF16, d_dsyn: int = 0, stream: int = 0) -> float:
+                        ckpt_format: int = CKPT_BFP16, d_dsyn: int = 0, stream: int = 0) -> float:
         """Device-pointer variant; returns J (the call synchronizes)."""
         J = C.c_double()
         opts = GradOpts(ckpt_every, ckpt_format)
@@ -341,7 +341,7 @@ class Batch:
         _check(lib().awe_batch_forward_device(self._h, C.c_void_p(d_wav), C.c_void_p(d_dat),
                                               C.c_void_p(stream or None)))
 
-    def gradient(self, wav, dobs, ckpt_every: int = 0, ckpt_format: int = CKPT_BF16):
+    def gradient(self, wav, dobs, ckpt_every: int = 0, ckpt_format: int = CKPT_BFP16):
         """dobs: list of per-shot traces [nsmp][nr_s].  Returns (dJ/dm on the
         whole model [n2][n1], float64; J)."""
         wav = np.ascontiguousarray(wav, np.float32).reshape(-1)
