@@ -215,12 +215,12 @@ typedef struct {
  * AWE_SCHEME_CPU (2D or 3D, any order, sponge and one-way ABC, free surface),
  * no density, no hybrid ABC; the forward runs in AWE_FAST arithmetic.  The
  * boundary coefficients (one-way ABC, sponge) are held at the plan's model.
- * The forward pass stores both time levels every ckpt_every steps (BF16 or
- * FP16 with one FP32 scale per level, or FP32); the adjoint sweep recomputes each
- * segment once from its checkpoint.  Gradient and misfit sums are FP64.
+ * The forward pass stores both time levels every ckpt_every steps (in
+ * opts->ckpt_format); the adjoint sweep recomputes each segment once from
+ * its checkpoint.  Gradient and misfit sums are FP64.
  * wav as awe_forward; dobs [nsmp][nr]; grad [n3][n2][n1]; misfit: J;
  * dsyn (may be NULL): the synthetic data [nsmp][nr].  opts NULL = defaults
- * (BF16, ceil(sqrt(nt))). */
+ * (BFP16, ceil(sqrt(nt))). */
 awe_status awe_gradient(awe_plan *plan, const float *wav, int ncs, const float *dobs, const awe_grad_opts *opts,
                         double *grad, double *misfit, float *dsyn);
 
@@ -228,6 +228,29 @@ awe_status awe_gradient(awe_plan *plan, const float *wav, int ncs, const float *
  * pointer, written when the call returns (the call synchronizes `stream`). */
 awe_status awe_gradient_device(awe_plan *plan, const float *d_wav, int ncs, const float *d_dobs,
                                const awe_grad_opts *opts, double *d_grad, double *misfit, float *d_dsyn, void *stream);
+
+/* ---- Reverse-time migration on the exact adjoint (replaces the reference
+ * recipes that image by correlating a source wavefield with a receiver
+ * wavefield, cicmig / awertm2d in byrne_awe.py:428-476, :628-652, and the
+ * programs' adj=y back-injection image, MAWEFDcart2Dcpu.c:353-369).  The
+ * receiver wavefield is the discrete adjoint of the plan's forward driven by
+ * the recorded data; the source wavefield is recomputed from checkpoints as
+ * in awe_gradient, so no wavefield is ever written out. */
+typedef enum {
+    /* image(x) = sum over steps k of nu_k(x) V_k(x): zero-lag cross-correlation
+     * of the adjoint (receiver) and forward (source) wavefields, model cells */
+    AWE_IMAGE_XCORR = 0,
+    /* the Born adjoint of the data: awe_gradient's formula with the residual
+     * replaced by the data (dJ/dm for zero synthetics, sign flipped) */
+    AWE_IMAGE_BORN = 1
+} awe_image_condition;
+
+/* Same plans, options and arguments as awe_gradient; data [nsmp][nr] are
+ * the recorded traces; image [n3][n2][n1] in FP64. */
+awe_status awe_rtm(awe_plan *plan, const float *wav, int ncs, const float *data, const awe_grad_opts *opts,
+                   int condition, double *image);
+awe_status awe_rtm_device(awe_plan *plan, const float *d_wav, int ncs, const float *d_data, const awe_grad_opts *opts,
+                          int condition, double *d_image, void *stream);
 
 /* ---- Batched 2D forward: many shots along a track, each on its own window
  * of one model.  Replaces a loop of sfAWEFDcart2Dcpu runs over cropped

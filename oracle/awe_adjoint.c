@@ -193,7 +193,7 @@ static void quantize_bfp16(double *u, size_t n) {
  * in double, so that finite differences of J are free of float rounding). */
 static int grad_impl(const orc_par *p, int ndim, int jdata, const float *vel_in, const double *m_in, const float *wav,
                      int ns, const float *sou, int nr, const float *rec, const float *dobs, double *grad,
-                     double *misfit, double *dsyn, int ckpt_every, int ckpt_bits) {
+                     double *misfit, double *dsyn, int ckpt_every, int ckpt_bits, int image) {
     if (p->hybrid || jdata < 1) return 1;
     g_t g;
     g.nd = ndim;
@@ -336,7 +336,7 @@ static int grad_impl(const orc_par *p, int ndim, int jdata, const float *vel_in,
                 }
                 const size_t row = (size_t)(k / jdata) * nr + ir;
                 if (dsyn) dsyn[row] = v;
-                r[row] = v - dobs[row];
+                r[row] = image < 0 ? v - dobs[row] : (double)dobs[row]; /* an image back-propagates the data */
             }
     }
     double J = 0;
@@ -381,7 +381,7 @@ static int grad_impl(const orc_par *p, int ndim, int jdata, const float *vel_in,
                     const size_t i = iy * sy + ix * sx + iz;
                     lam[i] = (I[i] ? 2 * nu[i] : 0) + lapT_at(&g, f, iz, ix, iy) + kap[i] +
                              W[i] * (I[i] ? -1.0 : 1.0) * nun[i];
-                    if (I[i]) gv[i] += nu[i] * lap_at(&g, Vk, i);
+                    if (I[i]) gv[i] += nu[i] * (image == 0 ? Vk[i] : lap_at(&g, Vk, i));
                 }
         if (k % jdata == 0)
             for (int ir = 0; ir < nr; ir++)
@@ -389,7 +389,7 @@ static int grad_impl(const orc_par *p, int ndim, int jdata, const float *vel_in,
                     const size_t n = BASE(&cr[ir]) + off[c];
                     lam[n] += W[n] * cr[ir].w[c] * r[(size_t)(k / jdata) * nr + ir];
                 }
-        for (int s = 0; s < ns; s++)
+        for (int s = 0; s < ns && image != 0; s++)
             for (int c = 0; c < nc; c++) {
                 const size_t n = BASE(&cs[s]) + off[c];
                 gv[n] += nu[n] * WAVE(k, s) * cs[s].w[c];
@@ -403,7 +403,14 @@ static int grad_impl(const orc_par *p, int ndim, int jdata, const float *vel_in,
     /* d vel2 / d m = -vel2 v^2, then the adjoint of the edge-replicating padding */
     const int m1 = p->n1, m2 = p->n2, m3 = ndim == 3 ? p->n3 : 1;
     memset(grad, 0, (size_t)m1 * m2 * m3 * sizeof(double));
-    for (int iy = 0; iy < ny; iy++)
+    for (int iy = 0; iy < ny && image == 0; iy++) /* cross-correlation image: the model window */
+        for (int ix = 0; ix < nx; ix++)
+            for (int iz = 0; iz < nz; iz++) {
+                const int jz = iz - nbd, jx = ix - nbd, jy = ndim == 3 ? iy - nbd : 0;
+                if (jz >= 0 && jz < m1 && jx >= 0 && jx < m2 && jy >= 0 && jy < m3)
+                    grad[((size_t)jy * m2 + jx) * m1 + jz] = gv[iy * sy + ix * sx + iz];
+            }
+    for (int iy = 0; iy < ny && image != 0; iy++)
         for (int ix = 0; ix < nx; ix++)
             for (int iz = 0; iz < nz; iz++) {
                 const size_t i = iy * sy + ix * sx + iz;
@@ -446,12 +453,12 @@ static int grad_impl(const orc_par *p, int ndim, int jdata, const float *vel_in,
 
 int orc_grad(const orc_par *p, int ndim, int jdata, const float *vel_in, const float *wav, int ns, const float *sou,
              int nr, const float *rec, const float *dobs, double *grad, double *misfit, double *dsyn) {
-    return grad_impl(p, ndim, jdata, vel_in, NULL, wav, ns, sou, nr, rec, dobs, grad, misfit, dsyn, 0, 0);
+    return grad_impl(p, ndim, jdata, vel_in, NULL, wav, ns, sou, nr, rec, dobs, grad, misfit, dsyn, 0, 0, -1);
 }
 
 int orc_grad_m(const orc_par *p, int ndim, int jdata, const double *m, const float *wav, int ns, const float *sou,
                int nr, const float *rec, const float *dobs, double *grad, double *misfit, double *dsyn) {
-    return grad_impl(p, ndim, jdata, NULL, m, wav, ns, sou, nr, rec, dobs, grad, misfit, dsyn, 0, 0);
+    return grad_impl(p, ndim, jdata, NULL, m, wav, ns, sou, nr, rec, dobs, grad, misfit, dsyn, 0, 0, -1);
 }
 
 /* As orc_grad, with the adjoint sweep reading levels recomputed from
@@ -461,5 +468,17 @@ int orc_grad_m(const orc_par *p, int ndim, int jdata, const double *m, const flo
 int orc_grad_ckpt(const orc_par *p, int ndim, int jdata, const float *vel_in, const float *wav, int ns,
                   const float *sou, int nr, const float *rec, const float *dobs, int every, int bits, double *grad,
                   double *misfit, double *dsyn) {
-    return grad_impl(p, ndim, jdata, vel_in, NULL, wav, ns, sou, nr, rec, dobs, grad, misfit, dsyn, every, bits);
+    return grad_impl(p, ndim, jdata, vel_in, NULL, wav, ns, sou, nr, rec, dobs, grad, misfit, dsyn, every, bits, -1);
+}
+
+/* Reverse-time migration images on the same FP64 adjoint (the engine's
+ * awe_rtm): the residual is the data themselves; condition 0 = zero-lag
+ * cross-correlation sum_k I nu_k V_k on the model window, 1 = the Born
+ * adjoint (the gradient formula with the data as residual). */
+int orc_image(const orc_par *p, int ndim, int jdata, const float *vel_in, const float *wav, int ns, const float *sou,
+              int nr, const float *rec, const float *data, int condition, double *image) {
+    double unused = 0;
+    if (condition != 0 && condition != 1) return 1;
+    return grad_impl(p, ndim, jdata, vel_in, NULL, wav, ns, sou, nr, rec, data, image, &unused, NULL, 0, 0,
+                     condition);
 }

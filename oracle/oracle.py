@@ -278,6 +278,8 @@ def _adj_lib():
         L.orc_grad_ckpt.argtypes = [C.POINTER(Par), C.c_int, C.c_int, fp, fp, C.c_int, fp, C.c_int, fp, fp, C.c_int,
                                     C.c_int, dp, dp, dp]
         L.orc_grad_ckpt.restype = C.c_int
+        L.orc_image.argtypes = [C.POINTER(Par), C.c_int, C.c_int, fp, fp, C.c_int, fp, C.c_int, fp, fp, C.c_int, dp]
+        L.orc_image.restype = C.c_int
         _adj = L
     return _adj
 
@@ -320,6 +322,28 @@ def misfit_gradient(p: dict, vel, wav, sou, rec, dobs, jdata: int = 1, m=None, c
     if rc != 0:
         raise ValueError("orc_grad rejected the parameters")
     return grad, J.value, dsyn
+
+
+def rtm_image(p: dict, vel, wav, sou, rec, data, condition: int, jdata: int = 1):
+    """FP64 reverse-time migration image of the CPU-program scheme on the
+    exact adjoint driven by `data` [nsmp][nr]: condition 0 = zero-lag
+    cross-correlation of the adjoint and forward wavefields (model window),
+    1 = the Born adjoint (the gradient formula with the data as residual).
+    Returns the image (model shape, float64)."""
+    q = make_par(p)
+    ndim = len(p["n"])
+    vel = np.ascontiguousarray(vel, np.float32)
+    wav = np.ascontiguousarray(wav, np.float32)
+    sou = np.ascontiguousarray(sou, np.float32).reshape(-1, ndim)
+    rec = np.ascontiguousarray(rec, np.float32).reshape(-1, ndim)
+    nsmp = (q.nt - 1) // jdata + 1
+    data = np.ascontiguousarray(data, np.float32).reshape(nsmp, rec.shape[0])
+    img = np.zeros(vel.shape, np.float64)
+    rc = _adj_lib().orc_image(C.byref(q), ndim, jdata, _fp(vel), _fp(wav), sou.shape[0], _fp(sou), rec.shape[0],
+                              _fp(rec), _fp(data), condition, img.ctypes.data_as(C.POINTER(C.c_double)))
+    if rc != 0:
+        raise ValueError("orc_image rejected the parameters")
+    return img
 
 
 def spher3d_fp64(p: dict, vel, wav, sou, rec):

@@ -69,3 +69,19 @@ def test_checkpoint_rounding_emulation_converges():
             for b in (8, 11, 24)]
     assert errs[0] > errs[1] > errs[2]
     assert errs[2] < 1e-6
+
+
+def test_oracle_born_image_is_linear_in_the_data():
+    """The FP64 Born image (the gradient formula with the data as residual)
+    satisfies grad(dobs) = born(dsyn) - born(dobs); the cross-correlation
+    image is nonzero and finite."""
+    from oracle import oracle
+
+    par, vel, wav, sou, rec, vtrue = grad_case(2, nt=120)
+    dobs, _ = oracle.cart_cpu(par, vtrue, wav, sou, rec)
+    g, _, dsyn = oracle.misfit_gradient(par, vel, wav, sou, rec, dobs)
+    b_syn = oracle.rtm_image(par, vel, wav, sou, rec, dsyn.astype(np.float32), 1)
+    b_obs = oracle.rtm_image(par, vel, wav, sou, rec, dobs, 1)
+    assert np.linalg.norm(g - (b_syn - b_obs)) <= 1e-6 * np.linalg.norm(g)
+    x = oracle.rtm_image(par, vel, wav, sou, rec, dobs, 0)
+    assert np.isfinite(x).all() and np.abs(x).max() > 0

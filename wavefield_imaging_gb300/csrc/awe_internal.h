@@ -127,6 +127,7 @@ struct AdjParams {
     Coef k;
     int nd, nop;
     const float *w1, *w2, *w3;  // sponge axis factors; null = no sponge
+    int xcorr;                  // imaging condition: G += I nu V (cross-correlation) instead of I nu L(V)
 };
 void launch_adjB(const float *X, float *Y, const float *V, const float *vel, double *G, const AdjParams &p,
                  cudaStream_t s);
@@ -146,6 +147,8 @@ constexpr int kBfpBlock = 64;
 constexpr float kBfpTiny = 1e-30f;  // blocks with max |v| <= this are stored as zero
 void launch_ckpt_store_bfp(const float *u, long long n, short *q, float *scale, int grid, cudaStream_t s);
 void launch_ckpt_load_bfp(const short *q, const float *scale, long long n, float *u, int grid, cudaStream_t s);
+// image on the model grid: the padded grid's model window of G
+void launch_image_cut(const double *G, const Grid &g, int nb, const int *n, int nd, double *out, cudaStream_t s);
 void launch_grad_fold(const double *G, const float *vel2, float dt, const Grid &g, int nb, const int *n, int nd,
                       double *out, cudaStream_t s);
 

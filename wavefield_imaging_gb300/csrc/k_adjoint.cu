@@ -36,7 +36,8 @@ __device__ __forceinline__ bool interior(const Grid &g, int i1, int i2, int i3) 
 }
 
 // main adjoint step, one thread per cell.  X = nu_k (stencil), Y = nu_{k+1}
-// in / mu_k out (same cell only), V = V_k (stencil), G += I nu L(V) in FP64.
+// in / mu_k out (same cell only), V = V_k (stencil), G += I nu L(V) in FP64
+// (p.xcorr: G += I nu V, the cross-correlation imaging condition).
 template <int NOP, int NDIM>
 __global__ void __launch_bounds__(256) k_adjB(const float *__restrict__ X, float *__restrict__ Y,
                                               const float *__restrict__ V, const float *__restrict__ vel,
@@ -69,7 +70,9 @@ __global__ void __launch_bounds__(256) k_adjB(const float *__restrict__ X, float
     const float w = wcell(p, i1, i2, i3);
     const float lam = (in ? 2.f * x : 0.f) + lt + (in ? -w : w) * Y[i];
     Y[i] = w * lam;
-    if (in) {
+    if (in && p.xcorr) {
+        G[i] += (double)x * (double)V[i];
+    } else if (in) {
         float lap = V[i] * p.k.c0;
 #pragma unroll
         for (int k = 1; k <= NOP; k++) {
@@ -428,6 +431,19 @@ __global__ void k_grad_fold(const double *__restrict__ G, const float *__restric
                 acc += G[i] * (-v2 * v2 * inv_dt2);
             }
     out[t] = acc;
+}
+
+__global__ void k_image_cut(const double *__restrict__ G, Grid g, int nb, int m1, int m2, int m3, int nd,
+                            double *__restrict__ out) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)m1 * m2 * m3) return;
+    const int j1 = (int)(t % m1), j2 = (int)((t / m1) % m2), j3 = (int)(t / ((long long)m1 * m2));
+    out[t] = G[((long long)(nd == 3 ? j3 + nb : 0) * g.n2 + j2 + nb) * g.n1 + j1 + nb];
+}
+
+void launch_image_cut(const double *G, const Grid &g, int nb, const int *n, int nd, double *out, cudaStream_t s) {
+    const long long m = (long long)n[0] * n[1] * (nd == 3 ? n[2] : 1);
+    k_image_cut<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(G, g, nb, n[0], n[1], nd == 3 ? n[2] : 1, nd, out);
 }
 
 void launch_grad_fold(const double *G, const float *vel2, float dt, const Grid &g, int nb, const int *n, int nd,

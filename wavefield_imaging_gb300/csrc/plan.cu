@@ -577,9 +577,29 @@ awe_status awe_forward(awe_plan *p, const float *wav, int ncs, float *dat, float
     return st;
 }
 
+static awe_status gradient_or_image(awe_plan *p, const float *d_wav, int ncs, const float *d_dobs,
+                                    const awe_grad_opts *opts, double *d_grad, double *misfit, float *d_dsyn,
+                                    void *stream, int image);
+
+awe_status awe_rtm_device(awe_plan *p, const float *d_wav, int ncs, const float *d_data, const awe_grad_opts *opts,
+                          int condition, double *d_image, void *stream) {
+    if (condition != AWE_IMAGE_XCORR && condition != AWE_IMAGE_BORN) {
+        set_error("awe_rtm: unknown imaging condition %d", condition);
+        return AWE_ERR_INVALID;
+    }
+    double unused = 0;
+    return gradient_or_image(p, d_wav, ncs, d_data, opts, d_image, &unused, nullptr, stream, condition);
+}
+
 awe_status awe_gradient_device(awe_plan *p, const float *d_wav, int ncs, const float *d_dobs,
                                const awe_grad_opts *opts, double *d_grad, double *misfit, float *d_dsyn,
                                void *stream) {
+    return gradient_or_image(p, d_wav, ncs, d_dobs, opts, d_grad, misfit, d_dsyn, stream, -1);
+}
+
+static awe_status gradient_or_image(awe_plan *p, const float *d_wav, int ncs, const float *d_dobs,
+                                    const awe_grad_opts *opts, double *d_grad, double *misfit, float *d_dsyn,
+                                    void *stream, int image) {
     if (!p || !d_wav || !d_dobs || !d_grad || !misfit) {
         set_error("null plan, wavelet, data, gradient or misfit pointer");
         return AWE_ERR_INVALID;
@@ -600,7 +620,7 @@ awe_status awe_gradient_device(awe_plan *p, const float *d_wav, int ncs, const f
     if (opts) o = *opts;
     CUDA_TRY(cudaSetDevice(p->device));
     cudaStream_t s = stream ? (cudaStream_t)stream : p->stream;
-    awe_status st = plan_gradient(p, d_wav, ncs, d_dobs, o, d_grad, misfit, d_dsyn, s);
+    awe_status st = plan_gradient(p, d_wav, ncs, d_dobs, o, d_grad, misfit, d_dsyn, s, image);
     if (st != AWE_OK) return st;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -610,8 +630,28 @@ awe_status awe_gradient_device(awe_plan *p, const float *d_wav, int ncs, const f
     return check_pipeline(p);
 }
 
+static awe_status gradient_or_image_host(awe_plan *p, const float *wav, int ncs, const float *dobs,
+                                         const awe_grad_opts *opts, double *grad, double *misfit, float *dsyn,
+                                         int image);
+
 awe_status awe_gradient(awe_plan *p, const float *wav, int ncs, const float *dobs, const awe_grad_opts *opts,
                         double *grad, double *misfit, float *dsyn) {
+    return gradient_or_image_host(p, wav, ncs, dobs, opts, grad, misfit, dsyn, -1);
+}
+
+awe_status awe_rtm(awe_plan *p, const float *wav, int ncs, const float *data, const awe_grad_opts *opts,
+                   int condition, double *image) {
+    if (condition != AWE_IMAGE_XCORR && condition != AWE_IMAGE_BORN) {
+        set_error("awe_rtm: unknown imaging condition %d", condition);
+        return AWE_ERR_INVALID;
+    }
+    double unused = 0;
+    return gradient_or_image_host(p, wav, ncs, data, opts, image, &unused, nullptr, condition);
+}
+
+static awe_status gradient_or_image_host(awe_plan *p, const float *wav, int ncs, const float *dobs,
+                                         const awe_grad_opts *opts, double *grad, double *misfit, float *dsyn,
+                                         int image) {
     if (!p || !wav || !dobs || !grad || !misfit) {
         set_error("null plan, wavelet, data, gradient or misfit pointer");
         return AWE_ERR_INVALID;
@@ -635,7 +675,7 @@ awe_status awe_gradient(awe_plan *p, const float *wav, int ncs, const float *dob
             st = AWE_ERR_CUDA;
         }
     }
-    if (st == AWE_OK) st = awe_gradient_device(p, d_wav, ncs, d_dobs, opts, d_grad, misfit, d_dsyn, nullptr);
+    if (st == AWE_OK) st = gradient_or_image(p, d_wav, ncs, d_dobs, opts, d_grad, misfit, d_dsyn, nullptr, image);
     if (st == AWE_OK) {
         cudaError_t e = cudaMemcpyAsync(grad, d_grad, grad_bytes, cudaMemcpyDeviceToHost, p->stream);
         if (e == cudaSuccess && dsyn) e = cudaMemcpyAsync(dsyn, d_dsyn, dat_bytes, cudaMemcpyDeviceToHost, p->stream);

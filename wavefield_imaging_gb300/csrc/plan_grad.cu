@@ -145,7 +145,7 @@ static awe_status ckpt_load(awe_plan *p, int idx, float *u, cudaStream_t s) {
 }
 
 awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *d_dobs, const awe_grad_opts &o,
-                         double *d_grad, double *misfit, float *d_dsyn, cudaStream_t s) {
+                         double *d_grad, double *misfit, float *d_dsyn, cudaStream_t s, int image) {
     const awe_desc &d = p->d;
     if (d.scheme != AWE_SCHEME_CPU || d.coords != AWE_CART) {
         set_error("awe_gradient: only the cartesian CPU-program scheme has an adjoint");
@@ -191,10 +191,17 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
     AWE_TRY(planB_run_hooked(p, d_wav, ncs, dat, nullptr, s, &hook));
     launches += p->launches;
 
-    // 2. residual and misfit (FP64 per row, summed in row order on the host)
-    launch_residual(dat, d_dobs, st->r, p->nsmp, p->nr, st->row_sum, s);
-    std::vector<double> rows(p->nsmp);
-    CUDA_TRY(cudaMemcpyAsync(rows.data(), st->row_sum, rows.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+    // 2. residual and misfit (FP64 per row, summed in row order on the host);
+    // an image back-propagates the recorded data themselves
+    std::vector<double> rows;
+    if (image < 0) {
+        launch_residual(dat, d_dobs, st->r, p->nsmp, p->nr, st->row_sum, s);
+        rows.resize(p->nsmp);
+        CUDA_TRY(cudaMemcpyAsync(rows.data(), st->row_sum, rows.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+    } else {
+        CUDA_TRY(cudaMemcpyAsync(st->r, d_dobs, (size_t)p->nsmp * p->nr * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    }
+    const bool xcorr = image == AWE_IMAGE_XCORR;
 
     // 3. adjoint sweep
     CUDA_TRY(cudaMemsetAsync(st->X, 0, bytes, s));
@@ -211,6 +218,7 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
     ap.w1 = sponge ? p->w[0] : nullptr;
     ap.w2 = sponge ? p->w[1] : nullptr;
     ap.w3 = sponge ? p->w[2] : nullptr;
+    ap.xcorr = xcorr;
     AbcB abc{p->abc[0], p->abc[1], p->abc[2], p->abc[3], p->abc[4], p->abc[5]};
     float *X = st->X, *Y = st->Y;
     const CUtensorMap *xmap = &st->x_tile, *ymap = &st->y_tile;
@@ -225,8 +233,10 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
                 const int j = k - k0;
                 float *A = st->vr + (size_t)(j % 3) * cells, *B = st->vr + (size_t)((j + 1) % 3) * cells;
                 float *N = st->vr + (size_t)((j + 2) % 3) * cells;
+                // the slot gets L(V_k) for the gradient, V_k itself for the cross-correlation image
                 AWE_TRY(stepB_full(p, sp, A, B, N, k, d_wav, ncs, &st->vr_halo[(j + 1) % 3], &st->vr_tile[j % 3], s,
-                                   launches, slot0 + (size_t)j * cells));
+                                   launches, xcorr ? nullptr : slot0 + (size_t)j * cells));
+                if (xcorr) CUDA_TRY(cudaMemcpyAsync(slot0 + (size_t)j * cells, B, bytes, cudaMemcpyDeviceToDevice, s));
             }
         } else {
             AWE_TRY(ckpt_load(p, 2 * seg, slot0, s));
@@ -266,7 +276,7 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
                 launch_rec_adj(Y, p->rec, p->nr, st->r + (size_t)(k / d.jdata) * p->nr, ap, p->corner_off, s);
                 launches++;
             }
-            if (p->ns > 0) {
+            if (p->ns > 0 && !xcorr) {
                 launch_src_grad(st->G, X, p->src, p->ns, d_wav, k, ncs, ncs == 1, d.ndim, p->corner_off, s);
                 launches++;
             }
@@ -274,7 +284,8 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
             std::swap(xmap, ymap);
         }
     }
-    launch_grad_fold(st->G, p->vel, d.dt, g, p->nbd, d.n, d.ndim, d_grad, s);
+    if (xcorr) launch_image_cut(st->G, g, p->nbd, d.n, d.ndim, d_grad, s);
+    else launch_grad_fold(st->G, p->vel, d.dt, g, p->nbd, d.n, d.ndim, d_grad, s);
     launches++;
     CUDA_TRY(cudaStreamSynchronize(s));
     double J = 0;

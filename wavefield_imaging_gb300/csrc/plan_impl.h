@@ -136,8 +136,9 @@ StepBParams stepB_params(const awe_plan *p);
 awe_status stepB_full(awe_plan *p, const StepBParams &sp, const float *prv, const float *cur, float *nxt, int it,
                       const float *d_wav, int ncs, const CUtensorMap *cur_map, const CUtensorMap *prv_map,
                       cudaStream_t s, long long &launches, float *lap_out = nullptr);
+// image < 0: misfit gradient; else awe_image_condition (the residual is the data)
 awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *d_dobs, const awe_grad_opts &o,
-                         double *d_grad, double *misfit, float *d_dsyn, cudaStream_t s);
+                         double *d_grad, double *misfit, float *d_dsyn, cudaStream_t s, int image = -1);
 void plan_gradient_free(awe_plan *p);
 
 awe_status planA_init(awe_plan *p);

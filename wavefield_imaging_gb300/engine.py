@@ -63,6 +63,8 @@ class GradOpts(C.Structure):
 CKPT_BF16, CKPT_FP32, CKPT_FP16, CKPT_BFP16 = 0, 1, 2, 3
 # awe_move_mode: one row of positions per step / sfDYNAWEFDcart2Dgpu's entry k*(it+1)
 MOVE_PER_STEP, MOVE_DYN = 0, 1
+# awe_image_condition: zero-lag cross-correlation / Born adjoint
+IMAGE_XCORR, IMAGE_BORN = 0, 1
 
 SNAP_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_float), C.c_size_t)
 
@@ -111,6 +113,10 @@ def lib():
         L.awe_set_shots.restype = C.c_int
         L.awe_set_moving_geometry.argtypes = [vp, C.c_int, C.c_int, fp, C.c_int, C.c_int, fp, C.c_int]
         L.awe_set_moving_geometry.restype = C.c_int
+        L.awe_rtm.argtypes = [vp, fp, C.c_int, fp, C.POINTER(GradOpts), C.c_int, C.POINTER(C.c_double)]
+        L.awe_rtm.restype = C.c_int
+        L.awe_rtm_device.argtypes = [vp, vp, C.c_int, vp, C.POINTER(GradOpts), C.c_int, vp, vp]
+        L.awe_rtm_device.restype = C.c_int
         dp = C.POINTER(C.c_double)
         L.awe_gradient.argtypes = [vp, fp, C.c_int, fp, C.POINTER(GradOpts), dp, dp, fp]
         L.awe_gradient_device.argtypes = [vp, vp, C.c_int, vp, C.POINTER(GradOpts), vp, dp, vp, vp]
@@ -233,6 +239,18 @@ class Plan:
         _check(lib().awe_gradient(self._h, _fp(wav), ncs, _fp(dobs), C.byref(opts),
                                   grad.ctypes.data_as(C.POINTER(C.c_double)), C.byref(J), _fp(dsyn)))
         return (grad, J.value, dsyn) if return_dsyn else (grad, J.value)
+
+    def rtm(self, wav, data, condition: int = IMAGE_XCORR, ckpt_every: int = 0, ckpt_format: int = CKPT_BFP16):
+        """Reverse-time migration image of the recorded traces `data`
+        [nsmp][nr] on the exact adjoint (awe_rtm): model shape, float64."""
+        wav = np.ascontiguousarray(wav, np.float32)
+        ncs = 1 if wav.ndim == 1 else wav.shape[1]
+        data = np.ascontiguousarray(data, np.float32).reshape(self.nsmp, self.nr)
+        img = np.zeros(list(self.desc.n)[: self.desc.ndim][::-1], np.float64)
+        opts = GradOpts(ckpt_every, ckpt_format)
+        _check(lib().awe_rtm(self._h, _fp(wav), ncs, _fp(data), C.byref(opts), condition,
+                             img.ctypes.data_as(C.POINTER(C.c_double))))
+        return img
 
     def gradient_device(self, d_wav: int, ncs: int, d_dobs: int, d_grad: int, ckpt_every: int = 0,
                         ckpt_format: int = CKPT_BFP16, d_dsyn: int = 0, stream: int = 0) -> float:
