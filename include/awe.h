@@ -252,6 +252,42 @@ awe_status awe_rtm(awe_plan *plan, const float *wav, int ncs, const float *data,
 awe_status awe_rtm_device(awe_plan *plan, const float *d_wav, int ncs, const float *d_data, const awe_grad_opts *opts,
                           int condition, double *d_image, void *stream);
 
+/* ---- Point-cloud windowing and merging (CODE/Mbycloudwin3d.c,
+ * CODE/Mbycloudmerge3d.c with CODE/hash.c): the selection of the ground
+ * points an orbit stretch illuminates, which cuts a survey into the windows
+ * that are modelled, and the fold-normalised sum of the windows' data back
+ * onto the full cloud.  A cloud point is AWE_CLOUD_NCO floats: x, y, z, the
+ * surface normal, and three more carried along.  Host buffers; device
+ * memory is allocated for the call. ---- */
+#define AWE_CLOUD_NCO 9
+
+/* Keeps, in input order, the ground points [ng][9] whose aperture cone
+ * (half-angle apt degrees about the normal, both sides) contains at least
+ * one orbit point (x, y, z of orbit [no][9]); the test is the reference's
+ * isInCone in the same float operations.  Writes *nw and index [nw] (input
+ * positions; capacity ng), win [nw][9] when win is not NULL (capacity
+ * ng*9), and for nf > 0 the data columns: data [nf][ng] -> win_data
+ * [nf][nw], ncomp floats per sample (2: complex, as the reference's data;
+ * 1: real).  Replaces Mbycloudwin3d.c:108-246 (fast=y). */
+awe_status awe_cloud_window(int device, const float *ground, long long ng, const float *orbit, long long no,
+                            float apt, long long nf, int ncomp, const float *data, long long *nw, long long *index,
+                            float *win, float *win_data);
+
+/* Sums windows' data onto the full cloud all [na][9]: window c holds
+ * nwp[c] points (win_pts: the windows' [nwp[c]][9] one after the other) and
+ * the data [nf][nwp[c]] (win_data: the windows' blocks one after the other,
+ * ncomp floats per sample).  Each window point goes to the full-cloud point
+ * that the reference's hash lookup finds (within ddMIN/10, ddMIN the
+ * smallest spacing of consecutive full-cloud points; table of
+ * hashscale*na slots, default 2), windows added in order; with norm, each
+ * full-cloud sample is divided by the number of windows that held the point
+ * (at least 1).  out [nf][na] (ncomp floats per sample).  A window point
+ * without a match is an error (the reference indexes out of its array).
+ * Replaces Mbycloudmerge3d.c:119-300. */
+awe_status awe_cloud_merge(int device, const float *all, long long na, int nwin, const long long *nwp,
+                           const float *win_pts, const float *win_data, long long nf, int ncomp, int norm,
+                           float hashscale, float *out);
+
 /* ---- Batched 2D forward: many shots along a track, each on its own window
  * of one model.  Replaces a loop of sfAWEFDcart2Dcpu runs over cropped
  * windows (the per-shot recipes of byrne_awe.py); the scheme is the CPU

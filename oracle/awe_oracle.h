@@ -91,4 +91,11 @@ double orc_cart3d_cpu_steps(int n1pad, int n2pad, int n3pad, int fdorder, int ns
 #ifdef __cplusplus
 }
 #endif
+/* point-cloud tools (oracle/awe_cloud.c): Mbycloudwin3d (fast=y) and
+ * Mbycloudmerge3d; ncomp floats per data sample (2 = complex) */
+int orc_cloud_window(const float *g, long long ng, const float *o, long long no, float apt, long long nf, int ncomp,
+                     const float *data, long long *nw, long long *index, float *win, float *win_data);
+int orc_cloud_merge(const float *all, long long na, int nwin, const long long *nwp, const float *win_pts,
+                    const float *win_data, long long nf, int ncomp, int norm, float hashscale, float *out);
+
 #endif

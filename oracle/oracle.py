@@ -24,7 +24,7 @@ CFLAGS = ["-std=gnu99", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-share
 
 def build(with_reference: bool = True) -> None:
     os.makedirs(BUILD, exist_ok=True)
-    srcs = [os.path.join(HERE, "awe_oracle.c"), os.path.join(HERE, "awe_oracle_gpu.c")]
+    srcs = [os.path.join(HERE, "awe_oracle.c"), os.path.join(HERE, "awe_oracle_gpu.c"), os.path.join(HERE, "awe_cloud.c")]
     for name, extra in (("liboracle.so", []), ("liboracle64.so", ["-DAWE_REAL_DOUBLE"])):
         out = os.path.join(BUILD, name)
         if not os.path.exists(out) or os.path.getmtime(out) < max(
@@ -257,6 +257,57 @@ def gpu_cart2d_moving(p: dict, vel, wav, sou, nst: int, rec, nrt: int, move: int
     if rc != 0:
         raise RuntimeError("moving-geometry run returned %d" % rc)
     return dat, snaps
+
+
+def cloud_window(ground, orbit, apt: float, data=None):
+    """Mbycloudwin3d (fast=y): ground [ng][9], orbit [no][9], aperture in
+    degrees, data [nf][ng] complex64 or float32 (optional).  Returns (index,
+    window points [nw][9], window data [nf][nw] or None)."""
+    g = np.ascontiguousarray(ground, np.float32).reshape(-1, 9)
+    o = np.ascontiguousarray(orbit, np.float32).reshape(-1, 9)
+    ng = g.shape[0]
+    nf, ncomp, dflat = 0, 2, None
+    if data is not None:
+        ncomp = 2 if np.iscomplexobj(data) else 1
+        d = np.ascontiguousarray(data, np.complex64 if ncomp == 2 else np.float32)
+        nf = d.shape[0]
+        dflat = d.view(np.float32).reshape(-1)
+    index = np.zeros(max(ng, 1), np.int64)
+    win = np.zeros((max(ng, 1), 9), np.float32)
+    wd = np.zeros(max(nf * ng * ncomp, 1), np.float32)
+    nw = C.c_longlong()
+    L = lib()
+    lp = C.POINTER(C.c_longlong)
+    rc = L.orc_cloud_window(_fp(g), C.c_longlong(ng), _fp(o), C.c_longlong(o.shape[0]), C.c_float(apt),
+                            C.c_longlong(nf), ncomp, _fp(dflat), C.byref(nw), index.ctypes.data_as(lp), _fp(win),
+                            _fp(wd))
+    if rc != 0:
+        raise RuntimeError("orc_cloud_window returned %d" % rc)
+    n = nw.value
+    wdat = None
+    if data is not None:
+        wdat = wd[: nf * n * ncomp].view(np.complex64 if ncomp == 2 else np.float32).reshape(nf, n)
+    return index[:n].copy(), win[:n].copy(), wdat
+
+
+def cloud_merge(all_pts, windows, norm: bool = True, hashscale: float = 2.0):
+    """Mbycloudmerge3d: all_pts [na][9]; windows: list of (points [nw][9],
+    data [nf][nw]) with one dtype (complex64 or float32).  Returns [nf][na]."""
+    a = np.ascontiguousarray(all_pts, np.float32).reshape(-1, 9)
+    na = a.shape[0]
+    ncomp = 2 if np.iscomplexobj(windows[0][1]) else 1
+    dt = np.complex64 if ncomp == 2 else np.float32
+    nf = windows[0][1].shape[0]
+    nwp = np.array([w[0].reshape(-1, 9).shape[0] for w in windows], np.int64)
+    pts = np.ascontiguousarray(np.concatenate([np.asarray(w[0], np.float32).reshape(-1, 9) for w in windows]))
+    dat = np.ascontiguousarray(np.concatenate([np.asarray(w[1], dt).reshape(-1) for w in windows])).view(np.float32)
+    out = np.zeros(nf * na * ncomp, np.float32)
+    lp = C.POINTER(C.c_longlong)
+    rc = lib().orc_cloud_merge(_fp(a), C.c_longlong(na), len(windows), nwp.ctypes.data_as(lp), _fp(pts), _fp(dat),
+                               C.c_longlong(nf), ncomp, int(norm), C.c_float(hashscale), _fp(out))
+    if rc != 0:
+        raise RuntimeError("orc_cloud_merge returned %d" % rc)
+    return out.view(dt).reshape(nf, na)
 
 
 _adj = None

@@ -44,7 +44,7 @@ def header_for(src_path, module):
 def main():
     ref_dir, out_dir = sys.argv[1], sys.argv[2]
     os.makedirs(out_dir, exist_ok=True)
-    for module in ("fdutil", "ts_kernel", "omputil"):
+    for module in ("fdutil", "ts_kernel", "omputil", "hash"):
         src = os.path.join(ref_dir, module + ".c")
         hdr = header_for(src, module)
         if module == "ts_kernel":

@@ -2,11 +2,13 @@
  *
  * Files: an RSF header is a text file of key=value pairs; the samples live in
  * a separate binary file named by the header's in="..." entry
- * (data_format=native_float, esize=4).  Output headers are written at the
+ * (data_format=native_float, esize=4, or native_complex, esize=8).  Output headers are written at the
  * first sample write and rewritten at exit, so axes set late are kept.
  * The tags "in" and "out" are standard input and output; for "out" the binary
  * file is <path of stdout>@.  Any other tag names a file on the command line
- * (tag=path).
+ * (tag=path); an input tag with no such parameter is itself the file name
+ * (as sf_input treats it).  Outputs start with the keys of the standard
+ * input's header, as Madagascar's do.
  *
  * Test infrastructure for the oracle's checker; not product code. */
 #define _GNU_SOURCE
@@ -33,11 +35,13 @@ struct sf_File {
     char keys[MAXKEYS][32];
     char vals[MAXKEYS][256];
     int header_written;
+    sf_datatype type;
 };
 
 static int g_argc = 0;
 static char **g_argv = NULL;
 static struct sf_File *g_outputs[16];
+static struct sf_File *g_in = NULL; /* standard input, whose header outputs inherit */
 static int g_nout = 0;
 
 static const char *arg_value(const char *key) {
@@ -53,7 +57,8 @@ static void write_header(struct sf_File *f) {
     FILE *h = fopen(f->hdr_path, "w");
     if (!h) sf_error("cannot write header %s", f->hdr_path);
     for (int i = 0; i < f->nkeys; i++) fprintf(h, "%s=%s\n", f->keys[i], f->vals[i]);
-    fprintf(h, "data_format=\"native_float\"\nesize=4\nin=\"%s\"\n", f->bin_path);
+    if (f->type == SF_COMPLEX) fprintf(h, "data_format=\"native_complex\"\nesize=8\nin=\"%s\"\n", f->bin_path);
+    else fprintf(h, "data_format=\"native_float\"\nesize=4\nin=\"%s\"\n", f->bin_path);
     fclose(h);
     f->header_written = 1;
 }
@@ -147,13 +152,16 @@ sf_file sf_input(const char *tag) {
         snprintf(f->hdr_path, sizeof f->hdr_path, "stdin");
     } else {
         const char *p = arg_value(tag);
-        if (!p) sf_error("missing %s= argument", tag);
+        if (!p) p = tag; /* a file name given as such */
         snprintf(f->hdr_path, sizeof f->hdr_path, "%s", p);
         h = fopen(p, "r");
         if (!h) sf_error("cannot open %s", p);
     }
     parse_header(f, h);
     if (h != stdin) fclose(h);
+    const char *fmt = get_key(f, "data_format");
+    f->type = (fmt && strstr(fmt, "complex")) ? SF_COMPLEX : SF_FLOAT;
+    if (strcmp(tag, "in") == 0) g_in = f;
     const char *in = get_key(f, "in");
     if (!in) sf_error("header %s has no in=", f->hdr_path);
     snprintf(f->bin_path, sizeof f->bin_path, "%s", in);
@@ -165,6 +173,13 @@ sf_file sf_input(const char *tag) {
 sf_file sf_output(const char *tag) {
     struct sf_File *f = calloc(1, sizeof *f);
     f->output = 1;
+    f->type = SF_FLOAT;
+    if (g_in) { /* an output starts as a copy of the standard input's header */
+        for (int i = 0; i < g_in->nkeys; i++)
+            if (strcmp(g_in->keys[i], "in") && strcmp(g_in->keys[i], "data_format") && strcmp(g_in->keys[i], "esize"))
+                set_key(f, g_in->keys[i], g_in->vals[i]);
+        f->type = g_in->type;
+    }
     if (strcmp(tag, "out") == 0) {
         ssize_t l = readlink("/proc/self/fd/1", f->hdr_path, sizeof f->hdr_path - 1);
         if (l <= 0) sf_error("cannot resolve stdout path");
@@ -237,6 +252,33 @@ void sf_floatwrite(float *arr, size_t n, sf_file f) {
         write_header(f);
     }
     if (fwrite(arr, sizeof(float), n, f->bin) != n) sf_error("short write to %s", f->bin_path);
+}
+
+void sf_settype(sf_file f, sf_datatype t) { f->type = t; }
+sf_datatype sf_gettype(sf_file f) { return f->type; }
+
+void sf_fileclose(sf_file f) {
+    if (!f->output && f->bin) { /* outputs keep their stream: headers are rewritten at exit */
+        fclose(f->bin);
+        f->bin = NULL;
+    }
+}
+
+sf_complex *sf_complexalloc(size_t n) { return (sf_complex *)sf_alloc(n, sizeof(sf_complex)); }
+bool *sf_boolalloc(size_t n) { return (bool *)sf_alloc(n, sizeof(bool)); }
+off_t *sf_largeintalloc(size_t n) { return (off_t *)sf_alloc(n, sizeof(off_t)); }
+
+void sf_complexread(sf_complex *arr, size_t n, sf_file f) {
+    if (fread(arr, sizeof(sf_complex), n, f->bin) != n) sf_error("short read from %s", f->bin_path);
+}
+
+void sf_complexwrite(sf_complex *arr, size_t n, sf_file f) {
+    if (!f->bin) {
+        f->bin = fopen(f->bin_path, "wb");
+        if (!f->bin) sf_error("cannot open %s", f->bin_path);
+        write_header(f);
+    }
+    if (fwrite(arr, sizeof(sf_complex), n, f->bin) != n) sf_error("short write to %s", f->bin_path);
 }
 
 void sf_seek(sf_file f, off_t offset, int whence) {

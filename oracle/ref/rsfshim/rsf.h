@@ -15,7 +15,16 @@
 #include <stdlib.h>
 #include <string.h>
 #include <math.h>
+#include <float.h>
+#include <unistd.h>
 #include <sys/types.h>
+#ifndef __cplusplus
+#include <complex.h>
+typedef float _Complex sf_complex;
+#endif
+
+/* sample types (the subset the programs use) */
+typedef enum { SF_UCHAR, SF_CHAR, SF_INT, SF_FLOAT, SF_COMPLEX } sf_datatype;
 
 #define SF_PI (3.14159265358979323846264338328)
 #define SF_MAX(a, b) ((a) < (b) ? (b) : (a))
@@ -63,6 +72,16 @@ void sf_setunit(sf_axis a, const char *unit);
 
 void sf_floatread(float *arr, size_t n, sf_file f);
 void sf_floatwrite(float *arr, size_t n, sf_file f);
+void sf_settype(sf_file f, sf_datatype t);
+sf_datatype sf_gettype(sf_file f);
+void sf_fileclose(sf_file f);
+bool *sf_boolalloc(size_t n);
+off_t *sf_largeintalloc(size_t n);
+#ifndef __cplusplus
+sf_complex *sf_complexalloc(size_t n);
+void sf_complexread(sf_complex *arr, size_t n, sf_file f);
+void sf_complexwrite(sf_complex *arr, size_t n, sf_file f);
+#endif
 void sf_seek(sf_file f, off_t offset, int whence);
 
 void *sf_alloc(size_t n, size_t size);

@@ -7,8 +7,8 @@ in include/awe.h, built into wavefield_imaging_gb300/_build/libawe.so.
 """
 from .engine import (  # noqa: F401
     CART, CKPT_BF16, CKPT_BFP16, CKPT_FP16, CKPT_FP32, EXACT, FAST, IMAGE_BORN, IMAGE_XCORR, MOVE_DYN, MOVE_PER_STEP, SCHEME_CPU, SCHEME_GPU, SPHER, AweError,
-    Batch, Desc, Plan, lib, make_desc,
+    Batch, Desc, Plan, cloud_merge, cloud_window, lib, make_desc,
 )
 
-__all__ = ["Plan", "Batch", "Desc", "make_desc", "AweError", "lib", "CART", "SPHER", "SCHEME_CPU", "SCHEME_GPU", "FAST",
+__all__ = ["Plan", "Batch", "cloud_window", "cloud_merge", "Desc", "make_desc", "AweError", "lib", "CART", "SPHER", "SCHEME_CPU", "SCHEME_GPU", "FAST",
            "EXACT", "CKPT_BF16", "CKPT_BFP16", "CKPT_FP16", "CKPT_FP32", "MOVE_PER_STEP", "MOVE_DYN", "IMAGE_XCORR", "IMAGE_BORN"]

@@ -85,24 +85,30 @@ PROGRAM_NAMES = ["sfAWEFDcart2Dgpu", "sfAWEFDcart3Dgpu", "sfAWEFDspher2Dgpu", "s
                  "sfAWEFDcart2Dcpu", "sfAWEFDcart3Dcpu", "sfDYNAWEFDcart2Dgpu"]
 
 
+CLOUD_PROGRAM_NAMES = ["sfbycloudwin3d", "sfbycloudmerge3d"]
+
+
 def build_programs() -> str:
-    """Link the drop-in RSF programs (one binary, one name per program) against libawe.so."""
+    """Link the drop-in RSF programs (one binary per family, one name per
+    program) against libawe.so."""
     os.makedirs(BIN, exist_ok=True)
-    exe = os.path.join(BIN, "awe_prog")
-    srcs = [os.path.join(PROGS, "awe_prog.c"), os.path.join(PROGS, "rsfio.c")]
-    deps = srcs + [os.path.join(PROGS, "rsfio.h"), os.path.join(ROOT, "include", "awe.h"), LIB]
-    if not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(x) for x in deps):
-        cmd = ["gcc", "-O2", "-std=c11", "-D_GNU_SOURCE", "-Wall", "-I" + os.path.join(ROOT, "include"), "-I" + PROGS,
-               *srcs, "-o", exe, "-L" + OUT, "-lawe", "-Wl,-rpath,$ORIGIN/.."]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError("program link failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
-    for name in PROGRAM_NAMES:
-        link = os.path.join(BIN, name)
-        if not os.path.islink(link):
-            if os.path.exists(link):
-                os.remove(link)
-            os.symlink("awe_prog", link)
+    for exe_name, main_src, names in (("awe_prog", "awe_prog.c", PROGRAM_NAMES),
+                                      ("cloud_prog", "cloud_prog.c", CLOUD_PROGRAM_NAMES)):
+        exe = os.path.join(BIN, exe_name)
+        srcs = [os.path.join(PROGS, main_src), os.path.join(PROGS, "rsfio.c")]
+        deps = srcs + [os.path.join(PROGS, "rsfio.h"), os.path.join(ROOT, "include", "awe.h"), LIB]
+        if not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(x) for x in deps):
+            cmd = ["gcc", "-O2", "-std=c11", "-D_GNU_SOURCE", "-Wall", "-I" + os.path.join(ROOT, "include"),
+                   "-I" + PROGS, *srcs, "-o", exe, "-L" + OUT, "-lawe", "-Wl,-rpath,$ORIGIN/.."]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError("program link failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+        for name in names:
+            link = os.path.join(BIN, name)
+            if not os.path.islink(link):
+                if os.path.exists(link):
+                    os.remove(link)
+                os.symlink(exe_name, link)
     return BIN
 
 

@@ -115,6 +115,12 @@ def lib():
         L.awe_set_moving_geometry.restype = C.c_int
         L.awe_rtm.argtypes = [vp, fp, C.c_int, fp, C.POINTER(GradOpts), C.c_int, C.POINTER(C.c_double)]
         L.awe_rtm.restype = C.c_int
+        lp = C.POINTER(C.c_longlong)
+        ll = C.c_longlong
+        L.awe_cloud_window.argtypes = [C.c_int, fp, ll, fp, ll, C.c_float, ll, C.c_int, fp, lp, lp, fp, fp]
+        L.awe_cloud_window.restype = C.c_int
+        L.awe_cloud_merge.argtypes = [C.c_int, fp, ll, C.c_int, lp, fp, fp, ll, C.c_int, C.c_int, C.c_float, fp]
+        L.awe_cloud_merge.restype = C.c_int
         L.awe_rtm_device.argtypes = [vp, vp, C.c_int, vp, C.POINTER(GradOpts), C.c_int, vp, vp]
         L.awe_rtm_device.restype = C.c_int
         dp = C.POINTER(C.c_double)
@@ -396,3 +402,48 @@ class Batch:
     def __exit__(self, *a):
         self.close()
 
+
+
+def cloud_window(ground, orbit, apt: float, data=None, device: int = 0):
+    """Ground points [ng][9] whose aperture cone (apt degrees about the normal)
+    holds an orbit point (orbit [no][9]), in input order (awe_cloud_window).
+    data [nf][ng] (complex64 or float32) is optional.  Returns (index [nw],
+    points [nw][9], data [nf][nw] or None)."""
+    g = np.ascontiguousarray(ground, np.float32).reshape(-1, 9)
+    o = np.ascontiguousarray(orbit, np.float32).reshape(-1, 9)
+    ng = g.shape[0]
+    nf, ncomp, dflat = 0, 2, None
+    if data is not None:
+        ncomp = 2 if np.iscomplexobj(data) else 1
+        d = np.ascontiguousarray(data, np.complex64 if ncomp == 2 else np.float32)
+        nf = d.shape[0]
+        dflat = d.view(np.float32).reshape(-1)
+    index = np.zeros(max(ng, 1), np.int64)
+    win = np.zeros((max(ng, 1), 9), np.float32)
+    wd = np.zeros(max(nf * ng * ncomp, 1), np.float32)
+    nw = C.c_longlong()
+    _check(lib().awe_cloud_window(device, _fp(g), ng, _fp(o), o.shape[0], apt, nf, ncomp, _fp(dflat), C.byref(nw),
+                                  index.ctypes.data_as(C.POINTER(C.c_longlong)), _fp(win), _fp(wd)))
+    n = nw.value
+    wdat = None
+    if data is not None:
+        wdat = wd[: nf * n * ncomp].view(np.complex64 if ncomp == 2 else np.float32).reshape(nf, n).copy()
+    return index[:n].copy(), win[:n].copy(), wdat
+
+
+def cloud_merge(all_pts, windows, norm: bool = True, hashscale: float = 2.0, device: int = 0):
+    """Sum windows [(points [nw][9], data [nf][nw]), ...] onto the full cloud
+    all_pts [na][9], fold-normalised with norm (awe_cloud_merge).  Returns
+    [nf][na] in the windows' dtype (complex64 or float32)."""
+    a = np.ascontiguousarray(all_pts, np.float32).reshape(-1, 9)
+    na = a.shape[0]
+    ncomp = 2 if np.iscomplexobj(windows[0][1]) else 1
+    dt = np.complex64 if ncomp == 2 else np.float32
+    nf = np.asarray(windows[0][1]).shape[0]
+    nwp = np.array([np.asarray(w[0]).reshape(-1, 9).shape[0] for w in windows], np.int64)
+    pts = np.ascontiguousarray(np.concatenate([np.asarray(w[0], np.float32).reshape(-1, 9) for w in windows]))
+    dat = np.ascontiguousarray(np.concatenate([np.asarray(w[1], dt).reshape(-1) for w in windows])).view(np.float32)
+    out = np.zeros(max(nf * na * ncomp, 1), np.float32)
+    _check(lib().awe_cloud_merge(device, _fp(a), na, len(windows), nwp.ctypes.data_as(C.POINTER(C.c_longlong)),
+                                 _fp(pts), _fp(dat), nf, ncomp, int(norm), hashscale, _fp(out)))
+    return out[: nf * na * ncomp].view(dt).reshape(nf, na)

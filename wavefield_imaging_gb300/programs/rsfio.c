@@ -23,6 +23,7 @@ struct rsf_file {
     float o[NAX], d[NAX];
     char label[NAX][32];
     int own_hdr;
+    int cplx; /* native_complex samples */
 };
 
 static int g_argc;
@@ -124,14 +125,14 @@ static rsf_file *new_file(void) {
     return f;
 }
 
-rsf_file *rsf_input(const char *tag) {
+static rsf_file *open_input(const char *tag, const char *path) {
     rsf_file *f = new_file();
     FILE *h;
-    if (strcmp(tag, "in") == 0) {
+    if (!path && strcmp(tag, "in") == 0) {
         h = stdin;
         snprintf(f->hdr_path, sizeof f->hdr_path, "stdin");
     } else {
-        const char *path = arg(tag);
+        if (!path) path = arg(tag);
         if (!path) {
             set_err("missing %s= argument", tag);
             free(f);
@@ -165,8 +166,9 @@ rsf_file *rsf_input(const char *tag) {
     char in_path[4096] = "", fmt[64] = "native_float";
     parse(f, text, in_path, sizeof in_path, fmt, sizeof fmt);
     free(text);
-    if (strcmp(fmt, "native_float") != 0) {
-        set_err("%s: only data_format=native_float is supported (got %s)", f->hdr_path, fmt);
+    f->cplx = strcmp(fmt, "native_complex") == 0;
+    if (strcmp(fmt, "native_float") != 0 && !f->cplx) {
+        set_err("%s: only data_format=native_float or native_complex is supported (got %s)", f->hdr_path, fmt);
         free(f);
         return NULL;
     }
@@ -189,6 +191,11 @@ rsf_file *rsf_input(const char *tag) {
     }
     return f;
 }
+
+rsf_file *rsf_input(const char *tag) { return open_input(tag, NULL); }
+rsf_file *rsf_input_path(const char *path) { return open_input(path, path); }
+int rsf_is_complex(const rsf_file *f) { return f->cplx; }
+void rsf_set_complex(rsf_file *f, int on) { f->cplx = on != 0; }
 
 rsf_file *rsf_output(const char *tag) {
     rsf_file *f = new_file();
@@ -255,7 +262,8 @@ static int write_header(rsf_file *f) {
         if (f->label[a][0]) fprintf(h, " label%d=\"%s\"", a + 1, f->label[a]);
         fputc('\n', h);
     }
-    fprintf(h, "data_format=\"native_float\" esize=4\n");
+    if (f->cplx) fprintf(h, "data_format=\"native_complex\" esize=8\n");
+    else fprintf(h, "data_format=\"native_float\" esize=4\n");
     if (f->inline_data) {
         fprintf(h, "in=\"stdin\"\n");
         fputc(0x0c, h);
