@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(256) k_adjB(const float *__restrict__ X, float
     const float lam = (in ? 2.f * x : 0.f) + lt + (in ? -w : w) * Y[i];
     Y[i] = w * lam;
     if (in && p.xcorr) {
-        G[i] += (double)x * (double)V[i];
+        G[i] += (double)__fmul_rn(x, V[i]);  // FP32 product, FP64 sum
     } else if (in) {
         float lap = V[i] * p.k.c0;
 #pragma unroll
@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(256) k_adjB(const float *__restrict__ X, float
             if constexpr (NDIM == 3) t = fmaf(__ldg(V + i - k * s3) + __ldg(V + i + k * s3), p.k.c[2][k], t);
             lap += t;
         }
-        G[i] += (double)x * (double)lap;
+        G[i] += (double)__fmul_rn(x, lap);
     }
 }
 
@@ -178,6 +178,51 @@ __global__ void k_abc_adj(float *mu, float *kap, const float *__restrict__ bl, c
     }
 }
 
+// Axis-1 faces with nop = 4 and n1 % 4 == 0 (the layout of k_abc_axis1_v4):
+// one thread per line keeps the eight cells at each end of mu and kap in
+// registers (two float4 each) and runs the transposed recurrence there,
+// instead of the dependent global read-modify-writes of k_abc_adj<1>.
+__device__ __forceinline__ void abc_adj_cell(float &mi, float &mb, float &kb, float &ki, float c) {
+    const float v = mi;
+    mi = 0.f;
+    mb -= c * v;
+    kb += v;
+    ki += c * v;
+}
+
+__global__ void k_abc_adj1_v4(float *__restrict__ mu, float *__restrict__ kap, const float *__restrict__ bl,
+                              const float *__restrict__ bh, Grid g, int top) {
+    const long long line = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (line >= (long long)g.n2 * g.n3) return;
+    const int q = g.n1 / 4;
+    float4 *M = reinterpret_cast<float4 *>(mu + line * g.n1);
+    float4 *K = reinterpret_cast<float4 *>(kap + line * g.n1);
+    {  // i = n1-2, n1-3, n1-4, n1-5 (the forward's last update first), b = i - 1
+        const float h = bh[line];
+        float4 ma = M[q - 2], mb = M[q - 1], ka = K[q - 2], kb = K[q - 1];
+        abc_adj_cell(mb.z, mb.y, kb.y, kb.z, h);
+        abc_adj_cell(mb.y, mb.x, kb.x, kb.y, h);
+        abc_adj_cell(mb.x, ma.w, ka.w, kb.x, h);
+        abc_adj_cell(ma.w, ma.z, ka.z, ka.w, h);
+        M[q - 2] = ma;
+        M[q - 1] = mb;
+        K[q - 2] = ka;
+        K[q - 1] = kb;
+    }
+    if (top) {  // i = 1, 2, 3, 4, b = i + 1
+        const float l = bl[line];
+        float4 ma = M[0], mb = M[1], ka = K[0], kb = K[1];
+        abc_adj_cell(ma.y, ma.z, ka.z, ka.y, l);
+        abc_adj_cell(ma.z, ma.w, ka.w, ka.z, l);
+        abc_adj_cell(ma.w, mb.x, kb.x, ka.w, l);
+        abc_adj_cell(mb.x, mb.y, kb.y, kb.x, l);
+        M[0] = ma;
+        M[1] = mb;
+        K[0] = ka;
+        K[1] = kb;
+    }
+}
+
 void launch_abc_adjB(int nop, int fsrf, float *mu, float *kap, const AbcB &a, const Grid &g, cudaStream_t s) {
     const int T = 128;
     long long n = (long long)g.n1 * g.n2;
@@ -185,7 +230,10 @@ void launch_abc_adjB(int nop, int fsrf, float *mu, float *kap, const AbcB &a, co
     n = (long long)g.n1 * g.n3;
     k_abc_adj<2><<<(unsigned)((n + T - 1) / T), T, 0, s>>>(mu, kap, a.xl, a.xh, g, nop, 1);
     n = (long long)g.n2 * g.n3;
-    k_abc_adj<1><<<(unsigned)((n + T - 1) / T), T, 0, s>>>(mu, kap, a.zl, a.zh, g, nop, !fsrf);
+    if (nop == 4 && g.n1 % 4 == 0 && g.n1 >= 16)
+        k_abc_adj1_v4<<<(unsigned)((n + T - 1) / T), T, 0, s>>>(mu, kap, a.zl, a.zh, g, !fsrf);
+    else
+        k_abc_adj<1><<<(unsigned)((n + T - 1) / T), T, 0, s>>>(mu, kap, a.zl, a.zh, g, nop, !fsrf);
 }
 
 // mu += W kap on the faces the transpose ABC touched (the outer nop+2 cells of
@@ -409,15 +457,26 @@ void launch_ckpt_load_bfp(const short *q, const float *scale, long long n, float
 // dJ/dm on the model grid: dJ/dvel2 * (-vel2^2 / dt^2) per padded cell (vel2 =
 // v^2 dt^2, m = 1/v^2; zero where vel2 is zero), summed over the padded cells
 // that replicate each model cell (the transpose of the edge padding).
+// padded cells that replicate model index j along one axis
+__device__ __forceinline__ void fold_range(int j, int m, int npad, int nb, int &lo, int &hi) {
+    lo = j == 0 ? 0 : j + nb;
+    hi = j == m - 1 ? npad - 1 : j + nb;
+}
+
+__device__ __forceinline__ int edge_axes(int j1, int j2, int j3, int m1, int m2, int m3, int nd) {
+    return (j1 == 0 || j1 == m1 - 1) + (j2 == 0 || j2 == m2 - 1) + (nd == 3 && (j3 == 0 || j3 == m3 - 1));
+}
+
+// skip_big: model cells on two or more edge axes (the model's edges and
+// corners, whose replicas span (nb+1)^2 or (nb+1)^3 padded cells) are left
+// to k_grad_fold_big
 __global__ void k_grad_fold(const double *__restrict__ G, const float *__restrict__ vel2, double inv_dt2, Grid g,
-                            int nb, int m1, int m2, int m3, int nd, double *__restrict__ out) {
+                            int nb, int m1, int m2, int m3, int nd, double *__restrict__ out, int skip_big) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)m1 * m2 * m3) return;
     const int j1 = (int)(t % m1), j2 = (int)((t / m1) % m2), j3 = (int)(t / ((long long)m1 * m2));
-    auto range = [&](int j, int m, int npad, int &lo, int &hi) {
-        lo = j == 0 ? 0 : j + nb;
-        hi = j == m - 1 ? npad - 1 : j + nb;
-    };
+    if (skip_big && edge_axes(j1, j2, j3, m1, m2, m3, nd) >= 2) return;
+    auto range = [&](int j, int m, int npad, int &lo, int &hi) { fold_range(j, m, npad, nb, lo, hi); };
     int a1, b1, a2, b2, a3 = 0, b3 = 0;
     range(j1, m1, g.n1, a1, b1);
     range(j2, m2, g.n2, a2, b2);
@@ -446,12 +505,68 @@ void launch_image_cut(const double *G, const Grid &g, int nb, const int *n, int 
     k_image_cut<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(G, g, nb, n[0], n[1], nd == 3 ? n[2] : 1, nd, out);
 }
 
+// The model's edge and corner cells, one block each: 2D the 4 corners; 3D
+// the 4 edges along each axis (corners counted with the axis-1 edges).
+__global__ void __launch_bounds__(256) k_grad_fold_big(const double *__restrict__ G, const float *__restrict__ vel2,
+                                                       double inv_dt2, Grid g, int nb, int m1, int m2, int m3, int nd,
+                                                       double *__restrict__ out) {
+    long long b = blockIdx.x;
+    int j1, j2, j3 = 0;
+    if (nd == 2) {
+        j1 = (b & 1) ? m1 - 1 : 0;
+        j2 = (b & 2) ? m2 - 1 : 0;
+    } else if (b < 4LL * m1) {
+        const int e = (int)(b / m1);
+        j1 = (int)(b % m1);
+        j2 = (e & 1) ? m2 - 1 : 0;
+        j3 = (e & 2) ? m3 - 1 : 0;
+    } else if ((b -= 4LL * m1) < 4LL * (m2 - 2)) {
+        const int e = (int)(b / (m2 - 2));
+        j2 = 1 + (int)(b % (m2 - 2));
+        j1 = (e & 1) ? m1 - 1 : 0;
+        j3 = (e & 2) ? m3 - 1 : 0;
+    } else {
+        b -= 4LL * (m2 - 2);
+        const int e = (int)(b / (m3 - 2));
+        j3 = 1 + (int)(b % (m3 - 2));
+        j1 = (e & 1) ? m1 - 1 : 0;
+        j2 = (e & 2) ? m2 - 1 : 0;
+    }
+    int a1, b1, a2, b2, a3 = 0, b3 = 0;
+    fold_range(j1, m1, g.n1, nb, a1, b1);
+    fold_range(j2, m2, g.n2, nb, a2, b2);
+    if (nd == 3) fold_range(j3, m3, g.n3, nb, a3, b3);
+    const long long w1 = b1 - a1 + 1, w2 = b2 - a2 + 1, vol = w1 * w2 * (b3 - a3 + 1);
+    double acc = 0;
+    for (long long k = threadIdx.x; k < vol; k += blockDim.x) {
+        const long long i1 = a1 + k % w1, i2 = a2 + (k / w1) % w2, i3 = a3 + k / (w1 * w2);
+        const long long i = (i3 * g.n2 + i2) * g.n1 + i1;
+        const double v2 = vel2[i];
+        acc += G[i] * (-v2 * v2 * inv_dt2);
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    __shared__ double part[8];
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += part[w];
+        out[((long long)j3 * m2 + j2) * m1 + j1] = t;
+    }
+}
+
 void launch_grad_fold(const double *G, const float *vel2, float dt, const Grid &g, int nb, const int *n, int nd,
                       double *out, cudaStream_t s) {
-    const long long m = (long long)n[0] * n[1] * (nd == 3 ? n[2] : 1);
+    const int m1 = n[0], m2 = n[1], m3 = nd == 3 ? n[2] : 1;
+    const long long m = (long long)m1 * m2 * m3;
     const double inv = 1.0 / ((double)dt * (double)dt);
-    k_grad_fold<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(G, vel2, inv, g, nb, n[0], n[1], nd == 3 ? n[2] : 1, nd,
-                                                          out);
+    // edges and corners go to one block each when every model axis has an interior
+    const bool split = m1 >= 3 && m2 >= 3 && (nd == 2 || m3 >= 3);
+    k_grad_fold<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(G, vel2, inv, g, nb, m1, m2, m3, nd, out, split ? 1 : 0);
+    if (split) {
+        const long long nbig = nd == 2 ? 4 : 4LL * (m1 + m2 - 2 + m3 - 2);
+        k_grad_fold_big<<<(unsigned)nbig, 256, 0, s>>>(G, vel2, inv, g, nb, m1, m2, m3, nd, out);
+    }
 }
 
 }  // namespace awe

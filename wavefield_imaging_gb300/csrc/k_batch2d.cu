@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(TZ / 4 * TX) k_batch2d_adj(const BatchShot *__
             wc[i] = p.sponge ? p.wz[z] * wx : 1.f;
             const float lam = (in ? 2.f * nu[i] : 0.f) + lt4[i] + (in ? -wc[i] : wc[i]) * yv[i];
             mu[i] = wc[i] * lam;
-            gacc[i] = in ? (double)nu[i] * (double)lv4[i] : 0.0;
+            gacc[i] = (double)(in ? __fmul_rn(nu[i], lv4[i]) : 0.f);  // FP32 product, FP64 sum
         }
         const long long cell0 = (long long)x * n1 + zb;
         // receiver residuals (W R^T r, then the W of mu): corners listed per tile

@@ -148,6 +148,24 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
             for (int u = 0; u < 9; u++) {
                 const int s = blk + u;
                 if (s < S) {
+                    // adjoint: the plane's L(V) and gradient loads go out before the
+                    // ring wait and the stencil, so their latency overlaps both
+                    float4 lvp = make_float4(0.f, 0.f, 0.f, 0.f);
+                    double2 gp0 = make_double2(0.0, 0.0), gp1 = make_double2(0.0, 0.0);
+                    bool gok = false;
+                    long long gip = 0;
+                    if constexpr (MODE == 2) {
+                        if (s >= 2 * NOPQ) {
+                            const int yp = y0 + s - 2 * NOPQ;
+                            gok = col_ok && xin && yp >= NOPQ && yp < p.n3 - NOPQ;
+                            gip = ((long long)yp * p.n2 + x) * p.n1 + zg;
+                            if (gok) {
+                                lvp = __ldcs(reinterpret_cast<const float4 *>(p.lap_v + gip));
+                                gp0 = __ldcs(reinterpret_cast<const double2 *>(p.grad + gip));
+                                gp1 = __ldcs(reinterpret_cast<const double2 *>(p.grad + gip + 2));
+                            }
+                        }
+                    }
                     const bool bad = !mbar_wait(&full[slot], ph, SPIN_LIMIT);
                     if (bad) atomicExch(p.err, 1);
                     const float4 cq = *reinterpret_cast<const float4 *>(&st[slot].cur[xi + HALO][4 * zq + HALO]);
@@ -235,10 +253,7 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
                         if constexpr (MODE == 2) {
                             // lambda = 2 I nu + L(I vel2 nu) + W (1 - 2 I) nu_{k+1}; out = W lambda
                             const float wy = (!undamped && p.w3) ? __ldg(p.w3 + y) : 1.f;
-                            const long long gi = ((long long)y * p.n2 + x) * p.n1 + zg;
-                            float4 lv = make_float4(0.f, 0.f, 0.f, 0.f);
-                            if (col_ok && xin && yin) lv = *reinterpret_cast<const float4 *>(p.lap_v + gi);
-                            const float lv4[4] = {lv.x, lv.y, lv.z, lv.w};
+                            const float lv4[4] = {lvp.x, lvp.y, lvp.z, lvp.w};
                             double gacc[4];
 #pragma unroll
                             for (int i = 0; i < 4; i++) {
@@ -247,14 +262,15 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
                                 const float nu = vel4[i];
                                 const float lam = (in ? 2.f * nu : 0.f) + lap[i] + (in ? -w : w) * prv4[i];
                                 out[i] = w * lam;
-                                gacc[i] = in ? (double)nu * (double)lv4[i] : 0.0;
+                                // product in FP32 (the fields are FP32), accumulated in FP64:
+                                // one conversion and one FP64 add per cell
+                                gacc[i] = (double)(in ? __fmul_rn(nu, lv4[i]) : 0.f);
                             }
-                            if (col_ok && xin && yin) {
-                                double *G = p.grad + gi;
-                                const double2 a = *reinterpret_cast<const double2 *>(G);
-                                const double2 b = *reinterpret_cast<const double2 *>(G + 2);
-                                *reinterpret_cast<double2 *>(G) = make_double2(a.x + gacc[0], a.y + gacc[1]);
-                                *reinterpret_cast<double2 *>(G + 2) = make_double2(b.x + gacc[2], b.y + gacc[3]);
+                            if (gok) {
+                                double *G = p.grad + gip;
+                                __stcs(reinterpret_cast<double2 *>(G), make_double2(gp0.x + gacc[0], gp0.y + gacc[1]));
+                                __stcs(reinterpret_cast<double2 *>(G + 2),
+                                       make_double2(gp1.x + gacc[2], gp1.y + gacc[3]));
                             }
                         } else if (!EXACT && undamped && tile_inner && yin) {
                             // every cell of the strip is interior and undamped: packed update
