@@ -309,8 +309,8 @@ typedef struct {
     int nshots, nsmp;
     long long total_samples; /* sum over shots of nsmp * nr */
     long long cells;         /* padded cells of all shots */
-    int tile_z, tile_x, grid;
-    int work_items;           /* (shot, tile) + (shot, receiver block) items per launch */
+    int tile_z, tile_x, grid; /* forward kernel: tile, or (n1, columns per item) of the column march */
+    int work_items;           /* (shot, tile or column chunk) + (shot, receiver block) items per launch */
     int launches_per_forward; /* = nt */
 } awe_batch_info_t;
 
@@ -324,10 +324,19 @@ awe_status awe_batch_set_model(awe_batch *batch, const float *vel);
  * after the other, shot s as [nsmp][nr_s]. */
 awe_status awe_batch_forward(awe_batch *batch, const float *wav, float *dat);
 awe_status awe_batch_forward_device(awe_batch *batch, const float *d_wav, float *d_dat, void *stream);
-/* Autotuner: times `steps` time steps of every tile shape and grid size on
- * the current model and keeps the fastest (the next forward recaptures). */
+/* Autotuner: times `steps` time steps of every tile shape and grid size,
+ * and of the column-march kernel (8th order: whole columns streamed by bulk
+ * copies, chunks of 16/32/64 columns) on the current model and keeps the
+ * fastest for the forward (the next forward recaptures); the gradient keeps
+ * the fastest tile shape.  tile_out: the tile index, or 4 for the column
+ * march; grid_out: the forward's grid. */
 awe_status awe_batch_tune(awe_batch *batch, int steps, int *tile_out, int *grid_out);
 awe_status awe_batch_info(const awe_batch *batch, awe_batch_info_t *info);
+/* Picks the forward kernel without timing: kernel 0-3 = the tile shapes,
+ * 4 = the column march with `chunk` columns per item (8th order only);
+ * grid <= 0 = the default (4 CTAs per SM for tiles, every resident CTA for
+ * the column march). */
+awe_status awe_batch_select(awe_batch *batch, int kernel, int chunk, int grid);
 /* Misfit gradient of the whole batch: J = 0.5 sum over shots and samples of
  * (d - dobs)^2, dJ/dm (m = 1/v^2) on the whole model [n2][n1] (each shot's
  * window contributes), with the checkpointing of awe_gradient per shot (one

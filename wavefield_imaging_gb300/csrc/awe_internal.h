@@ -205,6 +205,12 @@ void launch_batch_ckpt(bool store, int fmt, const BatchShot *shots, int nshots, 
 void launch_residual_flat(const float *d, const float *dobs, float *r, long long n, double *part, cudaStream_t s);
 void launch_batch_grad_fold(const BatchShot *shots, const int2 *win, int nshots, const double *G, const float *vel2,
                             float dt, int n1, int nb, int nz, int nxm, double *out, cudaStream_t s);
+// column-march forward (k_batch2d_col.cu): 8th order, n1 % 4 == 0, n1 <= 2048;
+// returns the threads per CTA (0 if the shape is not covered) and the dynamic shared memory
+int batch2d_col_shape(int nop, int n1, size_t *smem);
+int batch2d_col_ctas_per_sm(int n1);
+void launch_batch2d_col(const BatchShot *shots, const int4 *items, int nitems, int grid, int L, const BatchStep &p,
+                        int *err, cudaStream_t s);
 constexpr int kBatchNumTiles = 4;
 constexpr int kBatchRecBlock = 128;  // receivers per receiver item (<= threads of every tile shape)
 extern const int kBatchTiles[kBatchNumTiles][2];

@@ -52,6 +52,11 @@ struct awe_batch {
     BatchRecCorner *rc = nullptr;
     int2 *win = nullptr;
     int rc_tile = -1;
+    // column-march forward (k_batch2d_col): chunk length (0 = the tile kernels), its items and grid
+    int colL = 0, col_grid = 0;
+    std::vector<int4> col_items;
+    int4 *d_col_items = nullptr;
+    int *d_err = nullptr;  // set by a bulk-copy wait that timed out
 };
 
 #define CUDA_TRY(expr)                                                                            \
@@ -103,6 +108,26 @@ static awe_status upload_items(awe_batch *b) {
     return AWE_OK;
 }
 
+// column items (shot, x0) for chunks of L columns, then the receiver items
+static awe_status build_col_items(awe_batch *b, int L) {
+    b->col_items.clear();
+    for (int s = 0; s < (int)b->shots.size(); s++)
+        for (int x0 = 0; x0 < b->shots[s].n2; x0 += L) b->col_items.push_back(make_int4(s, 0, x0, 0));
+    for (int s = 0; s < (int)b->shots.size(); s++)
+        for (int r = 0; r < b->shots[s].nr; r += kBatchRecBlock) b->col_items.push_back(make_int4(s, r, 0, 1));
+    if (b->d_col_items) {
+        cudaFree(b->d_col_items);
+        b->allocs.erase(std::find(b->allocs.begin(), b->allocs.end(), (void *)b->d_col_items));
+        b->d_col_items = nullptr;
+    }
+    awe_status st = balloc(b, (void **)&b->d_col_items, b->col_items.size() * sizeof(int4));
+    if (st != AWE_OK) return st;
+    CUDA_TRY(cudaMemcpy(b->d_col_items, b->col_items.data(), b->col_items.size() * sizeof(int4),
+                        cudaMemcpyHostToDevice));
+    b->colL = L;
+    return AWE_OK;
+}
+
 static BatchStep step_params(const awe_batch *b, int it) {
     BatchStep p{};
     // level it lives in u[it & 1] (cur); the new level overwrites u[(it + 1) & 1]
@@ -130,7 +155,11 @@ static BatchStep step_params(const awe_batch *b, int it) {
 static void launch_range(awe_batch *b, int it0, int it1, cudaStream_t s) {
     for (int it = it0; it < it1; it++) {
         const BatchStep p = step_params(b, it);
-        launch_batch2d(b->nop, b->tile, b->d_shots, b->d_items, (int)b->items.size(), b->grid, p, s);
+        if (b->colL > 0)
+            launch_batch2d_col(b->d_shots, b->d_col_items, (int)b->col_items.size(), b->col_grid, b->colL, p,
+                               b->d_err, s);
+        else
+            launch_batch2d(b->nop, b->tile, b->d_shots, b->d_items, (int)b->items.size(), b->grid, p, s);
     }
 }
 
@@ -138,6 +167,7 @@ static awe_status run_all(awe_batch *b, cudaStream_t s) {
     const size_t bytes = (size_t)b->cells * sizeof(float);
     CUDA_TRY(cudaMemsetAsync(b->u[0], 0, bytes, s));
     CUDA_TRY(cudaMemsetAsync(b->u[1], 0, bytes, s));
+    CUDA_TRY(cudaMemsetAsync(b->d_err, 0, sizeof(int), s));
     if (!b->exec) {
         // capture the nt step launches once; replays reuse the same buffers
         cudaStream_t cs;
@@ -273,6 +303,8 @@ awe_status awe_batch_create(const awe_desc *desc, int nshots, const awe_shot *sh
     if (st == AWE_OK) st = balloc(b, (void **)&b->d_shots, b->shots.size() * sizeof(BatchShot));
     if (st == AWE_OK) st = balloc(b, (void **)&b->src, std::max<size_t>(hs.size(), 1) * sizeof(GeoPoint));
     if (st == AWE_OK) st = balloc(b, (void **)&b->rec, std::max<size_t>(hr.size(), 1) * sizeof(GeoPoint));
+    if (st == AWE_OK) st = balloc(b, (void **)&b->d_err, sizeof(int));
+    if (st == AWE_OK && cudaMemset(b->d_err, 0, sizeof(int)) != cudaSuccess) st = AWE_ERR_CUDA;
     if (st == AWE_OK) {
         cudaMemcpy(b->wz, b->h_wz.data(), b->h_wz.size() * sizeof(float), cudaMemcpyHostToDevice);
         cudaMemcpy(b->wx, b->h_wx.data(), b->h_wx.size() * sizeof(float), cudaMemcpyHostToDevice);
@@ -368,6 +400,12 @@ awe_status awe_batch_forward(awe_batch *b, const float *wav, float *dat) {
     if (st != AWE_OK) return st;
     CUDA_TRY(cudaMemcpyAsync(dat, b->dat, (size_t)b->ndat * sizeof(float), cudaMemcpyDeviceToHost, b->stream));
     CUDA_TRY(cudaStreamSynchronize(b->stream));
+    int bad = 0;
+    CUDA_TRY(cudaMemcpy(&bad, b->d_err, sizeof bad, cudaMemcpyDeviceToHost));
+    if (bad) {
+        set_error("awe_batch_forward: a bulk-copy wait of the column kernel timed out; results are invalid");
+        return AWE_ERR_CUDA;
+    }
     return AWE_OK;
 }
 
@@ -411,17 +449,54 @@ awe_status awe_batch_tune(awe_batch *b, int steps, int *tile_out, int *grid_out)
             }
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    // the column-march kernel: chunk lengths x (1, 2) persistent waves
     b->tile = best_tile;
     b->grid = best_grid;
+    int best_col = 0, best_col_grid = 0;
+    const int cpsm = batch2d_col_shape(b->nop, b->n1, nullptr) ? batch2d_col_ctas_per_sm(b->n1) : 0;
+    for (int L : {16, 32, 64}) {
+        if (cpsm <= 0) break;
+        awe_status st = build_col_items(b, L);
+        if (st != AWE_OK) return st;
+        for (int mult : {1, 2}) {
+            b->col_grid = mult * cpsm * b->sms;
+            cudaMemsetAsync(b->u[0], 0, bytes, b->stream);
+            cudaMemsetAsync(b->u[1], 0, bytes, b->stream);
+            launch_range(b, 0, 1, b->stream);  // warm
+            cudaEventRecord(e0, b->stream);
+            launch_range(b, 0, steps, b->stream);
+            cudaEventRecord(e1, b->stream);
+            CUDA_TRY(cudaEventSynchronize(e1));
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best) {
+                best = ms;
+                best_col = L;
+                best_col_grid = b->col_grid;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->colL = 0;
+    if (best_col > 0) {
+        awe_status st = build_col_items(b, best_col);
+        if (st != AWE_OK) return st;
+        b->col_grid = best_col_grid;
+    }
+    int bad = 0;
+    CUDA_TRY(cudaMemcpy(&bad, b->d_err, sizeof bad, cudaMemcpyDeviceToHost));
+    if (bad) {
+        set_error("awe_batch_tune: a bulk-copy wait of the column kernel timed out");
+        return AWE_ERR_CUDA;
+    }
     build_items(b);
     awe_status st = upload_items(b);
     if (st != AWE_OK) return st;
     drop_graph(b);  // recaptured with the chosen shape on the next forward
     CUDA_TRY(cudaGetLastError());
-    if (tile_out) *tile_out = best_tile;
-    if (grid_out) *grid_out = best_grid;
+    if (tile_out) *tile_out = b->colL > 0 ? kBatchNumTiles : best_tile;
+    if (grid_out) *grid_out = b->colL > 0 ? b->col_grid : best_grid;
     return AWE_OK;
 }
 
@@ -632,6 +707,35 @@ awe_status awe_batch_gradient(awe_batch *b, const float *wav, const float *dobs,
     return AWE_OK;
 }
 
+awe_status awe_batch_select(awe_batch *b, int kernel, int chunk, int grid) {
+    if (!b || kernel < 0 || kernel > kBatchNumTiles) {
+        set_error("awe_batch_select: kernel must be 0-%d", kBatchNumTiles);
+        return AWE_ERR_INVALID;
+    }
+    CUDA_TRY(cudaSetDevice(b->device));
+    drop_graph(b);
+    if (kernel < kBatchNumTiles) {
+        b->tile = kernel;
+        b->grid = grid > 0 ? grid : 4 * std::max(b->sms, 1);
+        b->colL = 0;
+        build_items(b);
+        return upload_items(b);
+    }
+    if (chunk < 1 || !batch2d_col_shape(b->nop, b->n1, nullptr)) {
+        set_error("awe_batch_select: the column march needs 8th order, nz + 2 nb <= 2048 and chunk >= 1");
+        return AWE_ERR_UNSUPPORTED;
+    }
+    const int cpsm = batch2d_col_ctas_per_sm(b->n1);
+    if (cpsm < 1) {
+        set_error("awe_batch_select: the column march does not fit on this device");
+        return AWE_ERR_UNSUPPORTED;
+    }
+    awe_status st = build_col_items(b, chunk);
+    if (st != AWE_OK) return st;
+    b->col_grid = grid > 0 ? grid : cpsm * b->sms;
+    return AWE_OK;
+}
+
 awe_status awe_batch_info(const awe_batch *b, awe_batch_info_t *info) {
     if (!b || !info) {
         set_error("null argument");
@@ -641,10 +745,17 @@ awe_status awe_batch_info(const awe_batch *b, awe_batch_info_t *info) {
     info->nsmp = b->nsmp;
     info->total_samples = b->ndat;
     info->cells = b->cells;
-    info->tile_z = kBatchTiles[b->tile][0];
-    info->tile_x = kBatchTiles[b->tile][1];
-    info->grid = b->grid;
-    info->work_items = (int)b->items.size();
+    if (b->colL > 0) {  // column march: whole columns, chunks of colL
+        info->tile_z = b->n1;
+        info->tile_x = b->colL;
+        info->grid = b->col_grid;
+        info->work_items = (int)b->col_items.size();
+    } else {
+        info->tile_z = kBatchTiles[b->tile][0];
+        info->tile_x = kBatchTiles[b->tile][1];
+        info->grid = b->grid;
+        info->work_items = (int)b->items.size();
+    }
     info->launches_per_forward = b->d.nt;
     return AWE_OK;
 }

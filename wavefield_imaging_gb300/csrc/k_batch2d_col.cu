@@ -1,0 +1,250 @@
+// Batched 2D forward, column march (8th order): the same step as k_batch2d
+// (V_{k+1} = W (N + S) of the CPU-program scheme on every shot's window),
+// laid out for HBM streaming.
+//
+// A work item is one shot and a chunk of L consecutive columns (x).  A CTA
+// of n1/4 threads (four z cells each) marches along x: for every column it
+// needs, one thread issues 1D bulk copies (cp.async.bulk, mbarrier
+// completion) of the current level's column and, for output columns, of the
+// previous level's and v^2 dt^2's columns into a ring of CRING shared-memory
+// slots, CRING - 4 columns ahead of the one being computed.  The x
+// neighbours of a cell come from a 9-column register queue, the z
+// neighbours from the centre column in shared memory (zero-padded ends).
+// Each plane is copied once per item (the chunk's 8 halo columns are read
+// twice), so DRAM traffic is about (1 + 8/L) x 4 + 12 bytes per cell.
+// Receiver items gather from the current level as in k_batch2d.
+//
+// Every mbarrier wait is bounded; a CTA that gives up sets *err, waits
+// (bounded) for its copies in flight and returns.
+#include <cuda_runtime.h>
+
+#include "awe_internal.h"
+#include "tma.cuh"
+
+namespace awe {
+namespace {
+
+constexpr int CNOP = 4, QL = 2 * CNOP + 1, CRING = 8;
+constexpr long long CSPIN = 1ll << 22;
+constexpr int kColMaxN1 = 2048;  // ring of 8 slots of 3 columns: 197 KB of shared memory at 2048
+
+__host__ __device__ inline int col_pitch(int n1) { return n1 + 8; }           // cur column: 4 zeros each end
+__host__ __device__ inline int col_slot(int n1) { return col_pitch(n1) + 2 * n1; }  // + prv + vel columns
+
+__global__ void __launch_bounds__(512) k_batch2d_col(const BatchShot *__restrict__ shots,
+                                                      const int4 *__restrict__ items, int nitems, const BatchStep p,
+                                                      int L, int *err) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int n1 = p.n1;
+    const int CP = col_pitch(n1), SLOT = col_slot(n1);
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw);
+    float *ring = reinterpret_cast<float *>(smem_raw + 128);
+    const int tid = threadIdx.x;
+    const int zb = 4 * tid;
+    const bool active = zb < n1;
+    if (tid == 0) {
+        for (int i = 0; i < CRING; i++) mbar_init(&full[i], 1);
+        fence_mbar_init();
+    }
+    for (int i = tid; i < CRING * 8; i += blockDim.x) {  // zero ends of every cur column
+        const int sl = i / 8, k = i % 8;
+        ring[sl * SLOT + (k < 4 ? k : CP - 8 + k)] = 0.f;
+    }
+    __syncthreads();
+    const float *prvb = p.prv ? p.prv : p.nxt;
+    float wz[4];
+    bool zin[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int z = zb + i;
+        wz[i] = (p.sponge && z < n1) ? __ldg(p.wz + z) : 1.f;
+        zin[i] = z >= CNOP && z < n1 - CNOP;
+    }
+    int slot0 = 0;
+    uint32_t ph0 = 0;
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const int4 it = items[w];
+        const BatchShot sh = shots[it.x];
+        if (it.w != 0) {  // receiver item: it.y = first receiver of the block
+            if (p.row < 0) continue;
+            const float *c = p.cur + sh.off;
+            const int rend = min(it.y + kBatchRecBlock, sh.nr);
+            for (int r = it.y + tid; r < rend; r += blockDim.x) {
+                const GeoPoint gp = p.rec[sh.rec0 + r];
+                float acc = 0.f;
+#pragma unroll
+                for (int cc = 0; cc < 4; cc++) {
+                    const long long n = gp.base + (cc & 1) + (cc >> 1) * (long long)n1;
+                    float v = c[n];
+                    if (p.sponge) {
+                        const int z = (int)(n % n1), xx = (int)(n / n1);
+                        v = (v * p.wz[z]) * p.wx[sh.wx_off + xx];
+                    }
+                    acc = fmaf(v, gp.w[cc], acc);
+                }
+                p.dat[sh.dat_off + (long long)p.row * sh.nr + r] = acc;
+            }
+            continue;
+        }
+        // ---- column item: it.z = first output column
+        const int x0 = it.z, x1 = min(x0 + L, sh.n2);
+        const int S = (x1 - x0) + 2 * CNOP;
+        const float *cbase = p.cur + sh.off;
+        const uint32_t cb = (uint32_t)n1 * 4u;
+        auto issue = [&](int s) {
+            const int sx = (slot0 + s) % CRING;
+            float *sl = ring + sx * SLOT;
+            const int xc = x0 - CNOP + s;
+            const bool cin = xc >= 0 && xc < sh.n2;
+            const bool out = s >= 2 * CNOP;
+            mbar_expect_tx(&full[sx], (cin ? cb : 0u) + (out ? 2u * cb : 0u));
+            if (cin) bulk_load_1d(sl + 4, cbase + (long long)xc * n1, cb, &full[sx]);
+            if (out) {
+                const long long go = sh.off + (long long)(x0 + s - 2 * CNOP) * n1;
+                bulk_load_1d(sl + CP, prvb + go, cb, &full[sx]);
+                bulk_load_1d(sl + CP + n1, p.vel + go, cb, &full[sx]);
+            }
+        };
+        if (tid == 0)
+            for (int s = 0; s < CRING && s < S; s++) issue(s);
+
+        int slot = slot0;
+        uint32_t ph = ph0;
+        float q[QL][4];
+#pragma unroll 1
+        for (int blk = 0; blk < S; blk += QL) {
+#pragma unroll
+            for (int u = 0; u < QL; u++) {
+                const int s = blk + u;
+                if (s < S) {
+                    const bool bad = !mbar_wait(&full[slot], ph, CSPIN);
+                    if (bad) atomicExch(err, 1);
+                    const float *sl = ring + slot * SLOT;
+                    const int xc = x0 - CNOP + s;
+                    if (active) {
+                        float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+                        if (xc >= 0 && xc < sh.n2) c = *reinterpret_cast<const float4 *>(sl + 4 + zb);
+                        q[u][0] = c.x;
+                        q[u][1] = c.y;
+                        q[u][2] = c.z;
+                        q[u][3] = c.w;
+                    }
+                    if (s >= 2 * CNOP && active) {
+                        const int x = x0 + s - 2 * CNOP;
+                        const int hs = (slot + CRING - CNOP) % CRING;  // slot of the centre column
+                        const float *H = ring + hs * SLOT;             // padded: H[4 + z] = column[z]
+                        float zw[12];
+#pragma unroll
+                        for (int v = 0; v < 3; v++) {
+                            const float4 t = *reinterpret_cast<const float4 *>(H + zb + 4 * v);
+                            zw[4 * v] = t.x;
+                            zw[4 * v + 1] = t.y;
+                            zw[4 * v + 2] = t.z;
+                            zw[4 * v + 3] = t.w;
+                        }
+                        const int jc = (u + 1 + CNOP) % QL;  // queue slot of the centre column
+                        float2 l01 = __fmul2_rn(make_float2(zw[4], zw[5]), make_float2(p.c0, p.c0));
+                        float2 l23 = __fmul2_rn(make_float2(zw[6], zw[7]), make_float2(p.c0, p.c0));
+#pragma unroll
+                        for (int k = 1; k <= CNOP; k++) {
+                            const float2 z01 = make_float2(zw[4 - k] + zw[4 + k], zw[5 - k] + zw[5 + k]);
+                            const float2 z23 = make_float2(zw[6 - k] + zw[6 + k], zw[7 - k] + zw[7 + k]);
+                            const float *qa = q[(jc + QL - k) % QL], *qb = q[(jc + k) % QL];
+                            const float2 x01 = __fadd2_rn(make_float2(qa[0], qa[1]), make_float2(qb[0], qb[1]));
+                            const float2 x23 = __fadd2_rn(make_float2(qa[2], qa[3]), make_float2(qb[2], qb[3]));
+                            const float2 cz = make_float2(p.cz[k], p.cz[k]), cx = make_float2(p.cx[k], p.cx[k]);
+                            l01 = __ffma2_rn(z01, cz, l01);
+                            l23 = __ffma2_rn(z23, cz, l23);
+                            l01 = __ffma2_rn(x01, cx, l01);
+                            l23 = __ffma2_rn(x23, cx, l23);
+                        }
+                        const float lap[4] = {l01.x, l01.y, l23.x, l23.y};
+                        const float4 pv = *reinterpret_cast<const float4 *>(sl + CP + zb);
+                        const float4 vv = *reinterpret_cast<const float4 *>(sl + CP + n1 + zb);
+                        const float pr4[4] = {pv.x, pv.y, pv.z, pv.w}, v4[4] = {vv.x, vv.y, vv.z, vv.w};
+                        const float wx = p.sponge ? __ldg(p.wx + sh.wx_off + x) : 1.f;
+                        const bool xin = x >= CNOP && x < sh.n2 - CNOP;
+                        float o[4];
+#pragma unroll
+                        for (int i = 0; i < 4; i++) {
+                            float pr = pr4[i];
+                            if (p.sponge) pr = (pr * wz[i]) * wx;
+                            float out = pr;
+                            if (xin && zin[i]) out = fmaf(v4[i], lap[i], 2.f * zw[4 + i] - pr);
+                            o[i] = out;
+                        }
+                        if (sh.ns > 0) {  // source corners of this shot in this 4-cell strip
+                            const float dd = p.wav[p.it];
+                            for (int sidx = 0; sidx < sh.ns; sidx++) {
+                                const GeoPoint gp = p.src[sh.src0 + sidx];
+#pragma unroll
+                                for (int cc = 0; cc < 4; cc++) {
+                                    const long long n = gp.base + (cc & 1) + (cc >> 1) * (long long)n1;
+                                    const long long d = n - ((long long)x * n1 + zb);
+#pragma unroll
+                                    for (int i = 0; i < 4; i++)
+                                        if (d == i) o[i] = o[i] + (dd * gp.w[cc]) * v4[i];
+                                }
+                            }
+                        }
+                        if (p.sponge) {
+#pragma unroll
+                            for (int i = 0; i < 4; i++) o[i] = (o[i] * wz[i]) * wx;
+                        }
+                        *reinterpret_cast<float4 *>(p.nxt + sh.off + (long long)x * n1 + zb) =
+                            make_float4(o[0], o[1], o[2], o[3]);
+                    }
+                    if (__syncthreads_or(bad)) {
+                        // drain: wait (bounded) for every copy still in flight, then leave
+                        if (tid == 0) {
+                            const int issued = min(S, max(CRING, s - CNOP + CRING));
+                            for (int t = s; t < issued; t++) {
+                                const int tt = slot0 + t;
+                                mbar_wait(&full[tt % CRING], ph0 ^ (uint32_t)((tt / CRING) & 1), CSPIN);
+                            }
+                        }
+                        __syncthreads();
+                        return;
+                    }
+                    if (tid == 0 && s >= CNOP && s - CNOP + CRING < S) issue(s - CNOP + CRING);
+                    if (++slot == CRING) {
+                        slot = 0;
+                        ph ^= 1u;
+                    }
+                }
+            }
+        }
+        const int t = slot0 + S;
+        ph0 ^= (uint32_t)((t / CRING) & 1);
+        slot0 = t % CRING;
+    }
+}
+
+}  // namespace
+
+int batch2d_col_shape(int nop, int n1, size_t *smem) {
+    if (nop != CNOP || n1 % 4 != 0 || n1 < 16 || n1 > kColMaxN1) return 0;
+    if (smem) *smem = 128 + (size_t)CRING * col_slot(n1) * sizeof(float);
+    return ((n1 / 4 + 31) / 32) * 32;
+}
+
+int batch2d_col_ctas_per_sm(int n1) {
+    size_t smem = 0;
+    const int threads = batch2d_col_shape(CNOP, n1, &smem);
+    if (!threads) return 0;
+    if (cudaFuncSetAttribute(k_batch2d_col, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return 0;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch2d_col, threads, smem) != cudaSuccess) return 0;
+    return nb;
+}
+
+void launch_batch2d_col(const BatchShot *shots, const int4 *items, int nitems, int grid, int L, const BatchStep &p,
+                        int *err, cudaStream_t s) {
+    size_t smem = 0;
+    const int threads = batch2d_col_shape(CNOP, p.n1, &smem);
+    if (!threads || grid < 1) return;
+    k_batch2d_col<<<grid, threads, smem, s>>>(shots, items, nitems, p, L, err);
+}
+
+}  // namespace awe

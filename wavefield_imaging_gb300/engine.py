@@ -102,6 +102,8 @@ def lib():
         L.awe_batch_forward.argtypes = [vp, fp, fp]
         L.awe_batch_forward_device.argtypes = [vp, vp, vp, vp]
         L.awe_batch_tune.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.awe_batch_select.argtypes = [vp, C.c_int, C.c_int, C.c_int]
+        L.awe_batch_select.restype = C.c_int
         L.awe_batch_info.argtypes = [vp, C.POINTER(BatchInfo)]
         L.awe_batch_gradient.argtypes = [vp, fp, fp, C.POINTER(GradOpts), C.POINTER(C.c_double),
                                          C.POINTER(C.c_double)]
@@ -378,6 +380,12 @@ class Batch:
         _check(lib().awe_batch_gradient(self._h, _fp(wav), _fp(flat), C.byref(opts),
                                         grad.ctypes.data_as(C.POINTER(C.c_double)), C.byref(J)))
         return grad, J.value
+
+    def select(self, kernel: int, chunk: int = 32, grid: int = 0):
+        """Forward kernel without timing (awe_batch_select): 0-3 tile shapes,
+        4 = the column march with `chunk` columns per item."""
+        _check(lib().awe_batch_select(self._h, kernel, chunk, grid))
+        self.info = self._info()
 
     def tune(self, steps: int = 20):
         t, g = C.c_int(), C.c_int()
