@@ -53,7 +53,7 @@ struct awe_batch {
     int2 *win = nullptr;
     int rc_tile = -1;
     // column-march forward (k_batch2d_col): chunk length (0 = the tile kernels), its items and grid
-    int colL = 0, col_grid = 0;
+    int colL = 0, col_grid = 0, ncol_items = 0;
     std::vector<int4> col_items;
     int4 *d_col_items = nullptr;
     int *d_err = nullptr;  // set by a bulk-copy wait that timed out
@@ -113,6 +113,7 @@ static awe_status build_col_items(awe_batch *b, int L) {
     b->col_items.clear();
     for (int s = 0; s < (int)b->shots.size(); s++)
         for (int x0 = 0; x0 < b->shots[s].n2; x0 += L) b->col_items.push_back(make_int4(s, 0, x0, 0));
+    b->ncol_items = (int)b->col_items.size();
     for (int s = 0; s < (int)b->shots.size(); s++)
         for (int r = 0; r < b->shots[s].nr; r += kBatchRecBlock) b->col_items.push_back(make_int4(s, r, 0, 1));
     if (b->d_col_items) {
@@ -150,6 +151,17 @@ static BatchStep step_params(const awe_batch *b, int it) {
     p.dat = b->dat;
     p.row = (it % b->d.jdata == 0) ? it / b->d.jdata : -1;
     return p;
+}
+
+// one forward step with the chosen kernel; without receivers: the column or
+// tile items alone (the gradient's recompute)
+static void launch_fwd(awe_batch *b, const BatchStep &p, cudaStream_t s, bool receivers) {
+    if (b->colL > 0)
+        launch_batch2d_col(b->d_shots, b->d_col_items, receivers ? (int)b->col_items.size() : b->ncol_items,
+                           b->col_grid, b->colL, p, b->d_err, s);
+    else
+        launch_batch2d(b->nop, b->tile, b->d_shots, b->d_items, receivers ? (int)b->items.size() : b->ntile_items,
+                       b->grid, p, s);
 }
 
 static void launch_range(awe_batch *b, int it0, int it1, cudaStream_t s) {
@@ -616,11 +628,12 @@ static BatchAdj adj_params(const awe_batch *b, int it, const float *V) {
 static awe_status grad_sequence(awe_batch *b, cudaStream_t s) {
     const long long cells = b->cells;
     const size_t cb = (size_t)cells * sizeof(float);
-    const int T = b->gT, ns = (int)b->shots.size(), nitems = (int)b->items.size();
+    const int T = b->gT, ns = (int)b->shots.size();
     const size_t es = b->gfmt == AWE_CKPT_FP32 ? 4 : 2;
     auto ck = [&](int idx) { return (void *)((char *)b->ckpt + (size_t)idx * cells * es); };
     auto sc = [&](int idx) { return b->scales + (size_t)idx * b->gscale_per; };
     // forward with checkpoints of both levels at every segment start
+    CUDA_TRY(cudaMemsetAsync(b->d_err, 0, sizeof(int), s));
     CUDA_TRY(cudaMemsetAsync(b->u[0], 0, cb, s));
     CUDA_TRY(cudaMemsetAsync(b->u[1], 0, cb, s));
     for (int it = 0; it < b->d.nt; it++) {
@@ -631,7 +644,7 @@ static awe_status grad_sequence(awe_batch *b, cudaStream_t s) {
             launch_batch_ckpt(true, b->gfmt, b->d_shots, ns, (float *)p.cur, ck(2 * seg + 1), sc(2 * seg + 1), b->n1,
                               cells, s);
         }
-        launch_batch2d(b->nop, b->tile, b->d_shots, b->d_items, nitems, b->grid, p, s);
+        launch_fwd(b, p, s, true);
     }
     launch_residual_flat(b->dat, b->dobs, b->res, b->ndat, b->part, s);
     // adjoint sweep, last segment first
@@ -651,7 +664,7 @@ static awe_status grad_sequence(awe_batch *b, cudaStream_t s) {
             p.cur = b->slots + (size_t)(j + 1) * cells;
             p.nxt = b->slots + (size_t)(j + 2) * cells;
             p.row = -1;
-            launch_batch2d(b->nop, b->tile, b->d_shots, b->d_items, b->ntile_items, b->grid, p, s);
+            launch_fwd(b, p, s, false);
         }
         for (int k = k1 - 1; k >= k0; k--) {
             BatchAdj p = adj_params(b, k, b->slots + (size_t)(k - k0 + 1) * cells);
@@ -701,6 +714,12 @@ awe_status awe_batch_gradient(awe_batch *b, const float *wav, const float *dobs,
                              s));
     CUDA_TRY(cudaStreamSynchronize(s));
     CUDA_TRY(cudaGetLastError());
+    int bad = 0;
+    CUDA_TRY(cudaMemcpy(&bad, b->d_err, sizeof bad, cudaMemcpyDeviceToHost));
+    if (bad) {
+        set_error("awe_batch_gradient: a bulk-copy wait of the column kernel timed out; results are invalid");
+        return AWE_ERR_CUDA;
+    }
     double J = 0;
     for (double v : parts) J += 0.5 * v;
     *misfit = J;
