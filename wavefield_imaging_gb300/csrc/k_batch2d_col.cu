@@ -54,11 +54,13 @@ __global__ void __launch_bounds__(512) k_batch2d_col(const BatchShot *__restrict
     const float *prvb = p.prv ? p.prv : p.nxt;
     float wz[4];
     bool zin[4];
+    bool zone = true;  // this thread's four z factors are all 1 (the multiplies are identities)
 #pragma unroll
     for (int i = 0; i < 4; i++) {
         const int z = zb + i;
         wz[i] = (p.sponge && z < n1) ? __ldg(p.wz + z) : 1.f;
         zin[i] = z >= CNOP && z < n1 - CNOP;
+        zone = zone && wz[i] == 1.f;
     }
     int slot0 = 0;
     uint32_t ph0 = 0;
@@ -91,6 +93,11 @@ __global__ void __launch_bounds__(512) k_batch2d_col(const BatchShot *__restrict
         const int S = (x1 - x0) + 2 * CNOP;
         const float *cbase = p.cur + sh.off;
         const uint32_t cb = (uint32_t)n1 * 4u;
+        // columns of the shot's first sources (a source's corners lie within
+        // two columns of its base index); more than 4 sources: every column is checked
+        int scol[4] = {-2, -2, -2, -2};
+        const bool few = sh.ns <= 4;
+        for (int k = 0; k < sh.ns && k < 4; k++) scol[k] = (int)(p.src[sh.src0 + k].base / n1);
         auto issue = [&](int s) {
             const int sx = (slot0 + s) % CRING;
             float *sl = ring + sx * SLOT;
@@ -163,17 +170,21 @@ __global__ void __launch_bounds__(512) k_batch2d_col(const BatchShot *__restrict
                         const float4 vv = *reinterpret_cast<const float4 *>(sl + CP + n1 + zb);
                         const float pr4[4] = {pv.x, pv.y, pv.z, pv.w}, v4[4] = {vv.x, vv.y, vv.z, vv.w};
                         const float wx = p.sponge ? __ldg(p.wx + sh.wx_off + x) : 1.f;
+                        const bool damp = p.sponge && !(zone && wx == 1.f);  // else multiplies by 1 skipped
                         const bool xin = x >= CNOP && x < sh.n2 - CNOP;
                         float o[4];
 #pragma unroll
                         for (int i = 0; i < 4; i++) {
                             float pr = pr4[i];
-                            if (p.sponge) pr = (pr * wz[i]) * wx;
+                            if (damp) pr = (pr * wz[i]) * wx;
                             float out = pr;
                             if (xin && zin[i]) out = fmaf(v4[i], lap[i], 2.f * zw[4 + i] - pr);
                             o[i] = out;
                         }
-                        if (sh.ns > 0) {  // source corners of this shot in this 4-cell strip
+                        bool near = !few;
+#pragma unroll
+                        for (int k = 0; k < 4; k++) near = near || (unsigned)(x - scol[k]) <= 2u;
+                        if (sh.ns > 0 && near) {  // source corners of this shot in this 4-cell strip
                             const float dd = p.wav[p.it];
                             for (int sidx = 0; sidx < sh.ns; sidx++) {
                                 const GeoPoint gp = p.src[sh.src0 + sidx];
@@ -187,7 +198,7 @@ __global__ void __launch_bounds__(512) k_batch2d_col(const BatchShot *__restrict
                                 }
                             }
                         }
-                        if (p.sponge) {
+                        if (damp) {
 #pragma unroll
                             for (int i = 0; i < 4; i++) o[i] = (o[i] * wz[i]) * wx;
                         }
