@@ -270,6 +270,11 @@ __global__ void __launch_bounds__(TZ / 4 * TX) k_batch2d_adj(const BatchShot *__
         const int x = x0 + xi, zb = z0 + 4 * zq;
         if (x >= n2 || zb >= n1) continue;
         const long long gi = sh.off + (long long)x * n1 + zb;
+        // the FP64 gradient of this strip, loaded before the stencils so the
+        // load latency overlaps them
+        double *G = p.G + gi;
+        const double2 G01 = __ldcs(reinterpret_cast<const double2 *>(G));
+        const double2 G23 = __ldcs(reinterpret_cast<const double2 *>(G + 2));
         const float nu[4] = {nv4.x, nv4.y, nv4.z, nv4.w}, yv[4] = {yv4.x, yv4.y, yv4.z, yv4.w};
         const float wx = p.sponge ? p.wx[sh.wx_off + x] : 1.f;
         const bool xin = x >= NOP && x < n2 - NOP;
@@ -330,10 +335,12 @@ __global__ void __launch_bounds__(TZ / 4 * TX) k_batch2d_adj(const BatchShot *__
                     }
             }
         }
-        // source term of the gradient
+        // source term of the gradient (corners lie within n1 + 1 of the base index)
         if (sh.ns > 0) {
             const float dd = p.wav[p.it];
             for (int s = 0; s < sh.ns; s++) {
+                const long long b0 = p.src[sh.src0 + s].base - cell0;
+                if (b0 < -(long long)n1 - 1 || b0 > 3) continue;
                 const GeoPoint gp = p.src[sh.src0 + s];
 #pragma unroll
                 for (int cc = 0; cc < 4; cc++) {
@@ -345,10 +352,8 @@ __global__ void __launch_bounds__(TZ / 4 * TX) k_batch2d_adj(const BatchShot *__
             }
         }
         *reinterpret_cast<float4 *>(p.Y + gi) = make_float4(mu[0], mu[1], mu[2], mu[3]);
-        double *G = p.G + gi;
-        const double2 G01 = *reinterpret_cast<const double2 *>(G), G23 = *reinterpret_cast<const double2 *>(G + 2);
-        *reinterpret_cast<double2 *>(G) = make_double2(G01.x + gacc[0], G01.y + gacc[1]);
-        *reinterpret_cast<double2 *>(G + 2) = make_double2(G23.x + gacc[2], G23.y + gacc[3]);
+        __stcs(reinterpret_cast<double2 *>(G), make_double2(G01.x + gacc[0], G01.y + gacc[1]));
+        __stcs(reinterpret_cast<double2 *>(G + 2), make_double2(G23.x + gacc[2], G23.y + gacc[3]));
     }
 }
 
