@@ -47,6 +47,16 @@ struct StepBParams {
     int shell;                  // cells within `shell` of a face are stored raw (boundary pass follows)
     int ilo[3], ihi[3];         // per axis, every sponge factor in [ilo, ihi) is exactly 1
     const float *prv;           // previous level when stepping out of place (null: read nxt in place)
+    // 2D only, fused point work: sources added to the new level after its
+    // update (k_injectB's arithmetic and order) ...
+    const GeoPoint *inj;
+    int inj_n, inj_stride, inj_ncs, inj_one, inj_it;
+    const float *inj_wav;
+    // ... and receivers gathered from `cur` (the level this launch reads,
+    // pending sponge applied) by extra blocks after the cell blocks
+    const GeoPoint *ext;
+    int ext_n, ext_stride;
+    float *ext_row;
 };
 
 // [lo, hi): the indices of a sponge factor table whose entries are exactly 1

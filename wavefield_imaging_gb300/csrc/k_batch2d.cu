@@ -125,6 +125,9 @@ __global__ void __launch_bounds__(TZ / 4 * TX) k_batch2d(const BatchShot *__rest
             if (sh.ns > 0) {
                 const float dd = p.wav[p.it];
                 for (int s = 0; s < sh.ns; s++) {
+                    // corners lie within n1 + 1 of the base index
+                    const long long b0 = p.src[sh.src0 + s].base - ((long long)x * n1 + zb);
+                    if (b0 < -(long long)n1 - 1 || b0 > 3) continue;
                     const GeoPoint gp = p.src[sh.src0 + s];
 #pragma unroll
                     for (int cc = 0; cc < 4; cc++) {

@@ -34,12 +34,32 @@ template <int NOP, int NDIM, bool EXACT, bool RHO>
 __global__ void __launch_bounds__(256) k_stepB(const float *__restrict__ cur, float *__restrict__ nxt,
                                                const float *__restrict__ vel, const float *__restrict__ rho,
                                                const StepBParams p) {
+    const Grid g = p.g;
+    const long long s2 = g.n1, s3 = (long long)g.n1 * g.n2;
+    if (NDIM == 2 && p.ext_n > 0) {
+        const int rows = (g.n2 + (int)blockDim.y - 1) / (int)blockDim.y;  // blocks of cells
+        if ((int)blockIdx.y >= rows) {  // receiver gather of `cur`, lint2d_extract's order
+            const int r = (((int)blockIdx.y - rows) * (int)gridDim.x + (int)blockIdx.x) * (int)(blockDim.x * blockDim.y) +
+                          (int)(threadIdx.y * blockDim.x + threadIdx.x);
+            if (r >= p.ext_n) return;
+            const GeoPoint pt = p.ext[(long long)r * p.ext_stride];
+            float acc = 0.f;
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const long long n = pt.base + (c & 1) + (c >> 1) * s2;
+                float v = __ldg(cur + n);
+                if (p.damp_prev) v = damp_cell<EXACT, 2>(v, (int)(n % s2), (int)(n / s2), 0, p.w1, p.w2, p.w3);
+                const float t = fmul<EXACT>(v, pt.w[c]);
+                acc = (c == 0) ? t : fadd<EXACT>(acc, t);
+            }
+            p.ext_row[r] = acc;
+            return;
+        }
+    }
     const int i1 = blockIdx.x * blockDim.x + threadIdx.x;
     const int i2 = blockIdx.y * blockDim.y + threadIdx.y;
     const int i3 = (NDIM == 3) ? (int)blockIdx.z : 0;
-    const Grid g = p.g;
     if (i1 >= g.n1 || i2 >= g.n2) return;
-    const long long s2 = g.n1, s3 = (long long)g.n1 * g.n2;
     const long long i = i3 * s3 + i2 * s2 + i1;
 
     float prv = p.prv ? p.prv[i] : nxt[i];  // out of place when p.prv is set
@@ -100,6 +120,19 @@ __global__ void __launch_bounds__(256) k_stepB(const float *__restrict__ cur, fl
         }
         if (!raw) out = damp_cell<EXACT, NDIM>(out, i1, i2, i3, p.w1, p.w2, p.w3);
     }
+    if (NDIM == 2 && p.inj_n > 0) {  // lint2d_inject_with_vv, sources and corners in order
+        for (int sidx = 0; sidx < p.inj_n; sidx++) {
+            const long long b0 = p.inj[(long long)sidx * p.inj_stride].base - i;
+            if (b0 < -(s2 + 1) || b0 > 0) continue;  // corners are base + {0, 1, s2, s2 + 1}
+            const GeoPoint pt = p.inj[(long long)sidx * p.inj_stride];
+            const float dd = p.inj_one ? p.inj_wav[(long long)p.inj_it * p.inj_ncs]
+                                       : p.inj_wav[(long long)p.inj_it * p.inj_ncs + sidx];
+#pragma unroll
+            for (int c = 0; c < 4; c++)
+                if (pt.base + (c & 1) + (c >> 1) * s2 == i)
+                    out = fadd<EXACT>(out, fmul<EXACT>(fmul<EXACT>(dd, pt.w[c]), __ldg(vel + i)));
+        }
+    }
     nxt[i] = out;
 }
 
@@ -108,6 +141,8 @@ static void dispatch_rho(bool rho, const float *cur, float *nxt, const float *ve
                          const StepBParams &p, cudaStream_t s) {
     dim3 block(64, 4, 1);
     dim3 grid((p.g.n1 + 63) / 64, (p.g.n2 + 3) / 4, NDIM == 3 ? p.g.n3 : 1);
+    if (NDIM == 2 && p.ext_n > 0)  // extra rows of blocks gather the receivers
+        grid.y += (unsigned)((p.ext_n + grid.x * 256 - 1) / (grid.x * 256));
     if (rho)
         k_stepB<NOP, NDIM, EXACT, true><<<grid, block, 0, s>>>(cur, nxt, vel, den, p);
     else

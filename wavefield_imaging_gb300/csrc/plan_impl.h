@@ -133,9 +133,14 @@ awe_status planB_run_hooked(awe_plan *p, const float *d_wav, int ncs, float *d_d
                             const StepHook *hook);
 StepBParams stepB_params(const awe_plan *p);
 // lap_out: the TMA path also stores L(cur) of interior cells there (gradient recompute)
+// ext_*: 2D, the receivers of `cur` (pending sponge applied) gathered into
+// ext_row by the same launch
 awe_status stepB_full(awe_plan *p, const StepBParams &sp, const float *prv, const float *cur, float *nxt, int it,
                       const float *d_wav, int ncs, const CUtensorMap *cur_map, const CUtensorMap *prv_map,
-                      cudaStream_t s, long long &launches, float *lap_out = nullptr);
+                      cudaStream_t s, long long &launches, float *lap_out = nullptr, const GeoPoint *ext_pts = nullptr,
+                      int ext_n = 0, int ext_stride = 1, float *ext_row = nullptr);
+// 2D steps add the sources in the step kernel (one launch per step) up to this many sources
+constexpr int kFusedSources = 8;
 // image < 0: misfit gradient; else awe_image_condition (the residual is the data)
 awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *d_dobs, const awe_grad_opts &o,
                          double *d_grad, double *misfit, float *d_dsyn, cudaStream_t s, int image = -1);

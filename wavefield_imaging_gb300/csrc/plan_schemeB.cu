@@ -287,7 +287,8 @@ StepBParams stepB_params(const awe_plan *p) {
 // previous level, and for the TMA kernel `cur_map`/`prv_map` are given).
 awe_status stepB_full(awe_plan *p, const StepBParams &sp0, const float *prv, const float *cur, float *nxt, int it,
                       const float *d_wav, int ncs, const CUtensorMap *cur_map, const CUtensorMap *prv_map,
-                      cudaStream_t s, long long &launches, float *lap_out) {
+                      cudaStream_t s, long long &launches, float *lap_out, const GeoPoint *ext_pts, int ext_n,
+                      int ext_stride, float *ext_row) {
     const awe_desc &d = p->d;
     const Grid &g = p->g;
     const bool exact = d.precision == AWE_EXACT;
@@ -295,6 +296,24 @@ awe_status stepB_full(awe_plan *p, const StepBParams &sp0, const float *prv, con
     const int shell = sp0.shell;
     StepBParams sp = sp0;
     sp.prv = (prv != nxt) ? prv : nullptr;
+    // 2D: sources (few) and receivers ride in the step kernel's launch
+    const bool fuse_src = d.ndim == 2 && p->ns > 0 && p->ns <= kFusedSources;
+    if (fuse_src) {
+        const PointsAt ps = points_at(p, p->src, p->ns, p->src_rows, it);
+        sp.inj = ps.pts;
+        sp.inj_n = p->ns;
+        sp.inj_stride = ps.stride;
+        sp.inj_wav = d_wav;
+        sp.inj_it = it;
+        sp.inj_ncs = ncs;
+        sp.inj_one = ncs == 1;
+    }
+    if (d.ndim == 2 && ext_n > 0) {
+        sp.ext = ext_pts;
+        sp.ext_n = ext_n;
+        sp.ext_stride = ext_stride;
+        sp.ext_row = ext_row;
+    }
     prof_begin(p, s);
     if (p->use_tma && cur_map && prv_map) {
         cudaError_t e = launch_stepB3_tma_with(exact, *cur_map, *prv_map, p->tmaps[4], nxt, sp, p->tma_shape,
@@ -309,7 +328,7 @@ awe_status stepB_full(awe_plan *p, const StepBParams &sp0, const float *prv, con
     }
     prof_end(p, s);
     launches++;
-    if (p->ns > 0) {
+    if (p->ns > 0 && !fuse_src) {
         const PointsAt ps = points_at(p, p->src, p->ns, p->src_rows, it);
         launch_injectB_off(d.ndim, exact, nxt, p->vel, ps.pts, p->ns, d_wav, it, ncs, ncs == 1, p->corner_off, s,
                            ps.stride);
@@ -370,10 +389,17 @@ awe_status planB_run_hooked(awe_plan *p, const float *d_wav, int ncs, float *d_d
     float *cur = p->u[1], *nxt = p->u[0];
     int icur = 1;
     int row = 0, isnap = 0;
+    // 2D: the traces of step it (the level the step reads, pending sponge
+    // applied, as the reference extracts after its swap) are gathered by the
+    // step's own launch
+    const bool fuse_rec = d.ndim == 2 && p->nr > 0;
     for (int it = 0; it < d.nt; it++) {
         if (hook) AWE_TRY((*hook)(it, nxt, cur, s));
+        const bool ext = fuse_rec && it % d.jdata == 0;
+        const PointsAt pe = points_at(p, p->rec, p->nr, p->rec_rows, it);
         AWE_TRY(stepB_full(p, sp, nxt, cur, nxt, it, d_wav, ncs, &p->tmaps[icur], &p->tmaps[2 + (1 - icur)], s,
-                           launches));
+                           launches, nullptr, pe.pts, ext ? p->nr : 0, pe.stride,
+                           ext ? d_dat + (size_t)row * p->nr : nullptr));
         std::swap(cur, nxt);  // nxt now holds the time level `it` (sponge pending)
         icur ^= 1;
         if (p->nsnap > 0 && it % d.jsnap == 0) {
@@ -387,10 +413,12 @@ awe_status planB_run_hooked(awe_plan *p, const float *d_wav, int ncs, float *d_d
             isnap++;
         }
         if (it % d.jdata == 0) {
-            const PointsAt pr = points_at(p, p->rec, p->nr, p->rec_rows, it);
-            launch_extract_off(d.ndim, exact, nxt, pr.pts, p->nr, d_dat + (size_t)row * p->nr, pw1, p->w[1],
-                               p->w[2], g, p->corner_off, s, pr.stride);
-            launches += p->nr > 0;
+            if (!fuse_rec) {
+                const PointsAt pr = points_at(p, p->rec, p->nr, p->rec_rows, it);
+                launch_extract_off(d.ndim, exact, nxt, pr.pts, p->nr, d_dat + (size_t)row * p->nr, pw1, p->w[1],
+                                   p->w[2], g, p->corner_off, s, pr.stride);
+                launches += p->nr > 0;
+            }
             row++;
         }
     }
