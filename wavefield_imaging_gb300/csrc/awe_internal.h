@@ -191,6 +191,12 @@ struct BatchRecCorner {
     int r;           // receiver index within the shot
     float w;         // interpolation weight
 };
+// a receiver corner of a column item: column and row in the shot's padded grid
+struct BatchColCorner {
+    int x, z;
+    int r;    // receiver index within the shot
+    float w;  // interpolation weight
+};
 struct BatchAdj {
     const float *X;  // nu_k
     float *Y;        // nu_{k+1} in, mu_k out
@@ -221,6 +227,12 @@ int batch2d_col_shape(int nop, int n1, size_t *smem);
 int batch2d_col_ctas_per_sm(int n1);
 void launch_batch2d_col(const BatchShot *shots, const int4 *items, int nitems, int grid, int L, const BatchStep &p,
                         int *err, cudaStream_t s);
+// adjoint step as a column march (same arithmetic as k_batch2d_adj): per
+// item the receiver corners [cstart[w], cstart[w+1]) sorted by column
+int batch2d_col_adj_ctas_per_sm(int n1);
+void launch_batch2d_col_adj(const BatchShot *shots, const int4 *items, int nitems, int grid, int L,
+                            const BatchAdj &p, const int *cstart, const BatchColCorner *crc, int *err,
+                            cudaStream_t s);
 constexpr int kBatchNumTiles = 4;
 constexpr int kBatchRecBlock = 128;  // receivers per receiver item (<= threads of every tile shape)
 extern const int kBatchTiles[kBatchNumTiles][2];

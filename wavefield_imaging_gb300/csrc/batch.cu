@@ -57,6 +57,10 @@ struct awe_batch {
     std::vector<int4> col_items;
     int4 *d_col_items = nullptr;
     int *d_err = nullptr;  // set by a bulk-copy wait that timed out
+    // column-march adjoint: receiver corners of each column item, by column
+    int *col_cstart = nullptr;
+    BatchColCorner *col_rc = nullptr;
+    int col_rc_L = -1, col_adj_grid = 0;
 };
 
 #define CUDA_TRY(expr)                                                                            \
@@ -552,11 +556,11 @@ static awe_status build_rec_corners(awe_batch *b) {
     b->rc_start = nullptr;
     b->rc = nullptr;
     awe_status st = balloc(b, (void **)&b->rc_start, start.size() * sizeof(int));
-    if (st == AWE_OK) st = balloc(b, (void **)&b->rc, std::max<size_t>(all.size(), 1) * sizeof(BatchRecCorner));
+    if (st == AWE_OK) st = balloc(b, (void **)&b->rc, std::max<size_t>(all.size(), 1) * sizeof(BatchColCorner));
     if (st != AWE_OK) return st;
     CUDA_TRY(cudaMemcpy(b->rc_start, start.data(), start.size() * sizeof(int), cudaMemcpyHostToDevice));
     if (!all.empty())
-        CUDA_TRY(cudaMemcpy(b->rc, all.data(), all.size() * sizeof(BatchRecCorner), cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemcpy(b->rc, all.data(), all.size() * sizeof(BatchColCorner), cudaMemcpyHostToDevice));
     b->rc_tile = b->tile;
     return AWE_OK;
 }
@@ -597,6 +601,56 @@ static awe_status grad_alloc(awe_batch *b, int T, int fmt) {
     b->gT = T;
     b->gfmt = fmt;
     b->gseg = nseg;
+    return AWE_OK;
+}
+
+// receiver corners of every column item (chunk colL), sorted by column; the
+// corners of one cell keep the (receiver, corner) order of the tile lists
+static awe_status build_col_rec_corners(awe_batch *b) {
+    std::vector<int> start(b->ncol_items + 1, 0);
+    std::vector<BatchColCorner> all;
+    std::vector<int> first(b->shots.size());
+    int acc = 0;
+    for (size_t s = 0; s < b->shots.size(); s++) {
+        first[s] = acc;
+        acc += (b->shots[s].n2 + b->colL - 1) / b->colL;
+    }
+    std::vector<std::vector<BatchColCorner>> per(b->ncol_items);
+    for (size_t s = 0; s < b->shots.size(); s++) {
+        const BatchShot &sh = b->shots[s];
+        for (int r = 0; r < sh.nr; r++) {
+            const GeoPoint &g = b->h_rec[sh.rec0 + r];
+            for (int c = 0; c < 4; c++) {
+                const long long node = g.base + (c & 1) + (c >> 1) * (long long)b->n1;
+                const int x = (int)(node / b->n1), z = (int)(node % b->n1);
+                if (x < 0 || x >= sh.n2) continue;
+                per[first[s] + x / b->colL].push_back(BatchColCorner{x, z, r, g.w[c]});
+            }
+        }
+    }
+    for (int w = 0; w < b->ncol_items; w++) {
+        std::stable_sort(per[w].begin(), per[w].end(),
+                         [](const BatchColCorner &a, const BatchColCorner &c) { return a.x < c.x; });
+        start[w] = (int)all.size();
+        all.insert(all.end(), per[w].begin(), per[w].end());
+    }
+    start[b->ncol_items] = (int)all.size();
+    for (void *q : {(void *)b->col_cstart, (void *)b->col_rc}) {
+        if (!q) continue;
+        cudaFree(q);
+        b->allocs.erase(std::find(b->allocs.begin(), b->allocs.end(), q));
+    }
+    b->col_cstart = nullptr;
+    b->col_rc = nullptr;
+    awe_status st = balloc(b, (void **)&b->col_cstart, start.size() * sizeof(int));
+    if (st == AWE_OK) st = balloc(b, (void **)&b->col_rc, std::max<size_t>(all.size(), 1) * sizeof(BatchColCorner));
+    if (st != AWE_OK) return st;
+    CUDA_TRY(cudaMemcpy(b->col_cstart, start.data(), start.size() * sizeof(int), cudaMemcpyHostToDevice));
+    if (!all.empty())
+        CUDA_TRY(cudaMemcpy(b->col_rc, all.data(), all.size() * sizeof(BatchColCorner), cudaMemcpyHostToDevice));
+    b->col_rc_L = b->colL;
+    const int cpsm = batch2d_col_adj_ctas_per_sm(b->n1);
+    b->col_adj_grid = cpsm > 0 ? cpsm * b->sms : 0;
     return AWE_OK;
 }
 
@@ -670,7 +724,11 @@ static awe_status grad_sequence(awe_batch *b, cudaStream_t s) {
             BatchAdj p = adj_params(b, k, b->slots + (size_t)(k - k0 + 1) * cells);
             p.X = X;
             p.Y = Y;
-            launch_batch2d_adj(b->nop, b->tile, b->d_shots, b->d_items, b->ntile_items, b->grid, p, s);
+            if (b->colL > 0 && b->col_adj_grid > 0)
+                launch_batch2d_col_adj(b->d_shots, b->d_col_items, b->ncol_items, b->col_adj_grid, b->colL, p,
+                                       b->col_cstart, b->col_rc, b->d_err, s);
+            else
+                launch_batch2d_adj(b->nop, b->tile, b->d_shots, b->d_items, b->ntile_items, b->grid, p, s);
             std::swap(X, Y);
         }
     }
@@ -701,6 +759,7 @@ awe_status awe_batch_gradient(awe_batch *b, const float *wav, const float *dobs,
     T = std::max(1, std::min(T, b->d.nt));
     awe_status st = grad_alloc(b, T, o.ckpt_format);
     if (st == AWE_OK && b->rc_tile != b->tile) st = build_rec_corners(b);
+    if (st == AWE_OK && b->colL > 0 && b->col_rc_L != b->colL) st = build_col_rec_corners(b);
     if (st != AWE_OK) return st;
     cudaStream_t s = b->stream;
     CUDA_TRY(cudaMemcpyAsync(b->wav, wav, (size_t)b->d.nt * sizeof(float), cudaMemcpyHostToDevice, s));

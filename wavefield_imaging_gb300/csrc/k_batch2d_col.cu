@@ -231,7 +231,270 @@ __global__ void __launch_bounds__(512) k_batch2d_col(const BatchShot *__restrict
     }
 }
 
+// ---------------------------------------------------------------------------
+// Adjoint step of the batch as a column march (the arithmetic of
+// k_batch2d_adj in the same order).  Two z cells per thread (twice the warps
+// of the forward's four-cell layout, half the queue registers).  Per plane
+// (column xc): X = nu_k, v^2dt^2 and V_k columns by bulk copy; the thread
+// forms g = I vel2 nu for its cells and writes it to the slot's g column
+// (zero-padded) for the z window, and keeps g and V in 9-column register
+// queues for the x neighbours.  For the output column (the centre) the
+// thread's nu_{k+1} (Y) and FP64 gradient strips are loaded before the ring
+// wait; mu_k = W lambda goes back to Y and the gradient strip is updated and
+// stored.  Receiver corners of the item are listed by column; sources are
+// tested only near their columns.
+constexpr int ARING = 8;
+constexpr int kAdjMaxN1 = 1024;  // 512 threads of two cells
+constexpr int YG_AHEAD = 3;      // output columns whose nu_{k+1} / gradient strips are in flight
+constexpr int YG_DEPTH = YG_AHEAD + 1;
+
+__host__ __device__ inline int adj_slot(int n1) { return 2 * n1 + 2 * (n1 + 8); }
+// slot layout (floats): X [n1] | vel [n1] | V [4 | n1 | 4] | g [4 | n1 | 4]; after the
+// ring, YG_DEPTH slots of the output columns' FP64 gradient [n1] and nu_{k+1} [n1]
+__host__ __device__ inline int adj_off_v(int n1) { return 2 * n1; }
+__host__ __device__ inline int adj_off_g(int n1) { return 2 * n1 + (n1 + 8); }
+
+__global__ void __maxnreg__(96) k_batch2d_col_adj(const BatchShot *__restrict__ shots,
+                                                         const int4 *__restrict__ items, int nitems,
+                                                         const BatchAdj p, int L, const int *__restrict__ cstart,
+                                                         const BatchColCorner *__restrict__ crc, int *err) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int n1 = p.n1;
+    const int SLOT = adj_slot(n1), OV = adj_off_v(n1), OG = adj_off_g(n1);
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw);
+    float *ring = reinterpret_cast<float *>(smem_raw + 128);
+    double *gring = reinterpret_cast<double *>(ring + ARING * SLOT);
+    float *yring = reinterpret_cast<float *>(gring + YG_DEPTH * n1);
+    const int tid = threadIdx.x;
+    const int zb = 2 * tid;
+    const bool active = zb < n1;
+    if (tid == 0) {
+        for (int i = 0; i < ARING; i++) mbar_init(&full[i], 1);
+        fence_mbar_init();
+    }
+    for (int i = tid; i < ARING * 16; i += blockDim.x) {  // zero ends of every V and g column
+        const int sl = i / 16, k = i % 16, base = (k < 8) ? OV : OG, kk = k % 8;
+        ring[sl * SLOT + base + (kk < 4 ? kk : n1 + kk)] = 0.f;
+    }
+    __syncthreads();
+    bool zin[2];
+    float wz[2];
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+        zin[i] = zb + i >= CNOP && zb + i < n1 - CNOP;
+        wz[i] = (p.sponge && zb + i < n1) ? __ldg(p.wz + zb + i) : 1.f;
+    }
+    int slot0 = 0;
+    uint32_t ph0 = 0;
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const int4 it = items[w];
+        if (it.w != 0) continue;  // receiver items belong to the forward
+        const BatchShot sh = shots[it.x];
+        const int x0 = it.z, x1 = min(x0 + L, sh.n2);
+        const int S = (x1 - x0) + 2 * CNOP;
+        const uint32_t cb = (uint32_t)n1 * 4u;
+        auto issue = [&](int s) {
+            const int sx = (slot0 + s) % ARING;
+            float *sl = ring + sx * SLOT;
+            const int xc = x0 - CNOP + s;
+            const bool cin = xc >= 0 && xc < sh.n2;
+            mbar_expect_tx(&full[sx], cin ? 3u * cb : 0u);
+            if (cin) {
+                const long long gc = sh.off + (long long)xc * n1;
+                bulk_load_1d(sl, p.X + gc, cb, &full[sx]);
+                bulk_load_1d(sl + n1, p.vel + gc, cb, &full[sx]);
+                bulk_load_1d(sl + OV + 4, p.V + gc, cb, &full[sx]);
+            }
+        };
+        if (tid == 0)
+            for (int s = 0; s < ARING && s < S; s++) issue(s);
+        int e = cstart[w];
+        const int eend = cstart[w + 1];
+        int scol[4] = {-8, -8, -8, -8};
+        const bool few = sh.ns <= 4;
+        for (int k = 0; k < sh.ns && k < 4; k++) scol[k] = (int)(p.src[sh.src0 + k].base / n1);
+        // this thread's strips of output column t (t >= 2 CNOP), one commit group per column
+        auto issue_yg = [&](int t) {
+            if (active && t >= 2 * CNOP && t < S) {
+                const long long gi = sh.off + (long long)(x0 + t - 2 * CNOP) * n1 + zb;
+                const int q = (t % YG_DEPTH) * n1 + zb;
+                cp_async_16(gring + q, p.G + gi);
+                cp_async_8(yring + q, p.Y + gi);
+            }
+            cp_async_commit();
+        };
+        for (int t = 0; t < YG_AHEAD; t++) issue_yg(t);
+
+        int slot = slot0;
+        uint32_t ph = ph0;
+        float gq[QL][2], vq[QL][2];
+#pragma unroll 1
+        for (int blk = 0; blk < S; blk += QL) {
+#pragma unroll
+            for (int u = 0; u < QL; u++) {
+                const int s = blk + u;
+                if (s < S) {
+                    const bool outp = s >= 2 * CNOP && active;
+                    const int x = x0 + s - 2 * CNOP;
+                    const long long gi = sh.off + (long long)x * n1 + zb;
+                    const float wx = (p.sponge && outp) ? __ldg(p.wx + sh.wx_off + x) : 1.f;
+                    issue_yg(s + YG_AHEAD);
+                    cp_async_wait<YG_AHEAD>();  // column s's strips are in (own copies only)
+                    const bool bad = !mbar_wait(&full[slot], ph, CSPIN);
+                    if (bad) atomicExch(err, 1);
+                    float *sl = ring + slot * SLOT;
+                    const int xc = x0 - CNOP + s;
+                    if (active) {
+                        float2 gv = make_float2(0.f, 0.f), vv = gv;
+                        if (xc >= 0 && xc < sh.n2) {
+                            const float2 xv = *reinterpret_cast<const float2 *>(sl + zb);
+                            const float2 wv = *reinterpret_cast<const float2 *>(sl + n1 + zb);
+                            vv = *reinterpret_cast<const float2 *>(sl + OV + 4 + zb);
+                            const bool xin = xc >= CNOP && xc < sh.n2 - CNOP;
+                            gv.x = (xin && zin[0]) ? wv.x * xv.x : 0.f;
+                            gv.y = (xin && zin[1]) ? wv.y * xv.y : 0.f;
+                        }
+                        // this column's g, for its z window when it is the centre (after barriers)
+                        *reinterpret_cast<float2 *>(sl + OG + 4 + zb) = gv;
+                        gq[u][0] = gv.x, gq[u][1] = gv.y;
+                        vq[u][0] = vv.x, vq[u][1] = vv.y;
+                    }
+                    if (outp) {
+                        const float *H = ring + ((slot + ARING - CNOP) % ARING) * SLOT;  // centre column's slot
+                        float gz[10], vz[10];  // z = zb - 4 .. zb + 5
+#pragma unroll
+                        for (int v = 0; v < 5; v++) {
+                            const float2 a = *reinterpret_cast<const float2 *>(H + OG + zb + 2 * v);
+                            const float2 c = *reinterpret_cast<const float2 *>(H + OV + zb + 2 * v);
+                            gz[2 * v] = a.x, gz[2 * v + 1] = a.y;
+                            vz[2 * v] = c.x, vz[2 * v + 1] = c.y;
+                        }
+                        const int jc = (u + 1 + CNOP) % QL;
+                        const float2 c0 = make_float2(p.c0, p.c0);
+                        float2 g01 = __fmul2_rn(make_float2(gz[4], gz[5]), c0);
+                        float2 v01 = __fmul2_rn(make_float2(vz[4], vz[5]), c0);
+#pragma unroll
+                        for (int k = 1; k <= CNOP; k++) {
+                            const float2 cz = make_float2(p.cz[k], p.cz[k]), cx = make_float2(p.cx[k], p.cx[k]);
+                            const float *ga = gq[(jc + QL - k) % QL], *gb = gq[(jc + k) % QL];
+                            const float *va = vq[(jc + QL - k) % QL], *vb = vq[(jc + k) % QL];
+                            const float2 gs = (k % 2 == 0)
+                                                  ? __fadd2_rn(make_float2(gz[4 - k], gz[5 - k]), make_float2(gz[4 + k], gz[5 + k]))
+                                                  : make_float2(gz[4 - k] + gz[4 + k], gz[5 - k] + gz[5 + k]);
+                            const float2 vs = (k % 2 == 0)
+                                                  ? __fadd2_rn(make_float2(vz[4 - k], vz[5 - k]), make_float2(vz[4 + k], vz[5 + k]))
+                                                  : make_float2(vz[4 - k] + vz[4 + k], vz[5 - k] + vz[5 + k]);
+                            g01 = __ffma2_rn(gs, cz, g01);
+                            g01 = __ffma2_rn(__fadd2_rn(make_float2(ga[0], ga[1]), make_float2(gb[0], gb[1])), cx, g01);
+                            v01 = __ffma2_rn(vs, cz, v01);
+                            v01 = __ffma2_rn(__fadd2_rn(make_float2(va[0], va[1]), make_float2(vb[0], vb[1])), cx, v01);
+                        }
+                        const float lt[2] = {g01.x, g01.y}, lv[2] = {v01.x, v01.y};
+                        const float2 nv2 = *reinterpret_cast<const float2 *>(H + zb);  // nu_k of the centre
+                        const int q = (s % YG_DEPTH) * n1 + zb;
+                        const float2 yv2 = *reinterpret_cast<const float2 *>(yring + q);
+                        const double2 G01 = *reinterpret_cast<const double2 *>(gring + q);
+                        const float nu[2] = {nv2.x, nv2.y}, yv[2] = {yv2.x, yv2.y};
+                        const bool xin = x >= CNOP && x < sh.n2 - CNOP;
+                        float mu[2], wc[2];
+                        double gacc[2];
+#pragma unroll
+                        for (int i = 0; i < 2; i++) {
+                            const bool in = xin && zin[i];
+                            wc[i] = p.sponge ? wz[i] * wx : 1.f;
+                            const float lam = (in ? 2.f * nu[i] : 0.f) + lt[i] + (in ? -wc[i] : wc[i]) * yv[i];
+                            mu[i] = wc[i] * lam;
+                            gacc[i] = (double)(in ? __fmul_rn(nu[i], lv[i]) : 0.f);  // FP32 product, FP64 sum
+                        }
+                        if (p.row >= 0) {  // receiver residuals of this column (corners in list order)
+                            for (int ee = e; ee < eend; ee++) {
+                                const BatchColCorner rc = crc[ee];
+                                if (rc.x != x) break;
+                                const int d = rc.z - zb;
+#pragma unroll
+                                for (int i = 0; i < 2; i++)
+                                    if (d == i) {
+                                        const float r = p.res[sh.dat_off + (long long)p.row * sh.nr + rc.r];
+                                        mu[i] += wc[i] * (wc[i] * (rc.w * r));
+                                    }
+                            }
+                        }
+                        bool near = !few;
+#pragma unroll
+                        for (int k = 0; k < 4; k++) near = near || (unsigned)(x - scol[k]) <= 2u;
+                        if (sh.ns > 0 && near) {  // source term of the gradient
+                            const float dd = p.wav[p.it];
+                            const long long cell0 = (long long)x * n1 + zb;
+                            for (int sidx = 0; sidx < sh.ns; sidx++) {
+                                const GeoPoint gp = p.src[sh.src0 + sidx];
+#pragma unroll
+                                for (int cc = 0; cc < 4; cc++) {
+                                    const long long d = gp.base + (cc & 1) + (cc >> 1) * (long long)n1 - cell0;
+#pragma unroll
+                                    for (int i = 0; i < 2; i++)
+                                        if (d == i) gacc[i] += (double)nu[i] * (double)(dd * gp.w[cc]);
+                                }
+                            }
+                        }
+                        *reinterpret_cast<float2 *>(p.Y + gi) = make_float2(mu[0], mu[1]);
+                        __stcs(reinterpret_cast<double2 *>(p.G + gi), make_double2(G01.x + gacc[0], G01.y + gacc[1]));
+                    }
+                    if (s >= 2 * CNOP) {  // the corners of this output column are done
+                        while (e < eend && crc[e].x == x) e++;
+                    }
+                    if (__syncthreads_or(bad)) {
+                        cp_async_wait<0>();
+                        if (tid == 0) {
+                            const int issued = min(S, max(ARING, s - CNOP + ARING));
+                            for (int t = s; t < issued; t++) {
+                                const int tt = slot0 + t;
+                                mbar_wait(&full[tt % ARING], ph0 ^ (uint32_t)((tt / ARING) & 1), CSPIN);
+                            }
+                        }
+                        __syncthreads();
+                        return;
+                    }
+                    if (tid == 0 && s >= CNOP && s - CNOP + ARING < S) issue(s - CNOP + ARING);
+                    if (++slot == ARING) {
+                        slot = 0;
+                        ph ^= 1u;
+                    }
+                }
+            }
+        }
+        const int t = slot0 + S;
+        ph0 ^= (uint32_t)((t / ARING) & 1);
+        slot0 = t % ARING;
+    }
+}
+
 }  // namespace
+
+size_t batch2d_col_adj_smem(int n1) {
+    return 128 + (size_t)ARING * adj_slot(n1) * sizeof(float) + (size_t)YG_DEPTH * n1 * (sizeof(double) + sizeof(float));
+}
+
+static int adj_threads(int n1) { return ((n1 / 2 + 31) / 32) * 32; }
+
+int batch2d_col_adj_ctas_per_sm(int n1) {
+    if (!batch2d_col_shape(CNOP, n1, nullptr) || n1 > kAdjMaxN1) return 0;
+    const size_t smem = batch2d_col_adj_smem(n1);
+    if (cudaFuncSetAttribute(k_batch2d_col_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+        return 0;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch2d_col_adj, adj_threads(n1), smem) != cudaSuccess)
+        return 0;
+    return nb;
+}
+
+void launch_batch2d_col_adj(const BatchShot *shots, const int4 *items, int nitems, int grid, int L,
+                            const BatchAdj &p, const int *cstart, const BatchColCorner *crc, int *err,
+                            cudaStream_t s) {
+    if (p.n1 > kAdjMaxN1 || grid < 1) return;
+    k_batch2d_col_adj<<<grid, adj_threads(p.n1), batch2d_col_adj_smem(p.n1), s>>>(shots, items, nitems, p, L, cstart,
+                                                                                    crc, err);
+}
 
 int batch2d_col_shape(int nop, int n1, size_t *smem) {
     if (nop != CNOP || n1 % 4 != 0 || n1 < 16 || n1 > kColMaxN1) return 0;
