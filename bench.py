@@ -462,7 +462,7 @@ def run_grad(args):
     g_s = ms / 1e3 / args.steps
     out = {"metric": GRAD_METRIC, "value": args.steps * world / (ms / 1e3), "unit": "gradients/s",
            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32 fields, fp64 sums",
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32 fields, compensated fp32 sums",
            "data": "synthetic",
            "config": {"workload": w["name"], "checkpoint": args.ckpt, "padded_cells": cells,
                       "ckpt_every": int(np.ceil(np.sqrt(w["nt"]))), "start_model": "true model smoothed, 100 m",
@@ -657,7 +657,7 @@ def run_batch_grad(args):
     out = {"metric": "batched FWI gradients/s (2D survey, checkpointed fwd + adjoint)",
            "value": nshots * world / batch_s, "unit": "shot gradients/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": 1e3 * batch_s, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "fp32 fields, fp64 sums", "data": "synthetic",
+           "vs_baseline": None, "dtype": "fp32 fields, compensated fp32 sums", "data": "synthetic",
            "config": {"workload": "%d shots, windows nx in [300, 700] x nz 512 of a 6000-column model, 8th order, "
                                   "nt=%d, nb=40, dabc=y; start model = true model smoothed 100 m" % (nshots, nt),
                       "checkpoint": args.ckpt, "padded_cells": info.cells,

@@ -217,7 +217,9 @@ typedef struct {
  * boundary coefficients (one-way ABC, sponge) are held at the plan's model.
  * The forward pass stores both time levels every ckpt_every steps (in
  * opts->ckpt_format); the adjoint sweep recomputes each segment once from
- * its checkpoint.  Gradient and misfit sums are FP64.
+ * its checkpoint.  The gradient is summed over time steps per padded cell as
+ * a compensated (Kahan) FP32 pair and folded onto the model in FP64; the
+ * misfit sum is FP64.
  * wav as awe_forward; dobs [nsmp][nr]; grad [n3][n2][n1]; misfit: J;
  * dsyn (may be NULL): the synthetic data [nsmp][nr].  opts NULL = defaults
  * (BFP16, ceil(sqrt(nt))). */

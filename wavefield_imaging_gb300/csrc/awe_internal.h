@@ -139,13 +139,13 @@ struct AdjParams {
     const float *w1, *w2, *w3;  // sponge axis factors; null = no sponge
     int xcorr;                  // imaging condition: G += I nu V (cross-correlation) instead of I nu L(V)
 };
-void launch_adjB(const float *X, float *Y, const float *V, const float *vel, double *G, const AdjParams &p,
+void launch_adjB(const float *X, float *Y, const float *V, const float *vel, float2 *G, const AdjParams &p,
                  cudaStream_t s);
 void launch_abc_adjB(int nop, int fsrf, float *mu, float *kap, const AbcB &a, const Grid &g, cudaStream_t s);
 void launch_kap_fold(float *mu, float *kap, const AdjParams &p, cudaStream_t s);
 void launch_rec_adj(float *mu, const GeoPoint *pts, int nr, const float *r, const AdjParams &p, const long long *off,
                     cudaStream_t s);
-void launch_src_grad(double *G, const float *nu, const GeoPoint *pts, int ns, const float *wav, int it, int ncs,
+void launch_src_grad(float2 *G, const float *nu, const GeoPoint *pts, int ns, const float *wav, int it, int ncs,
                      bool one_wavelet, int nd, const long long *off, cudaStream_t s);
 void launch_residual(const float *d, const float *dobs, float *r, int nrows, int nr, double *row_sum, cudaStream_t s);
 void launch_ckpt_store16(bool fp16, const float *u, long long n, unsigned int *amax, void *q, float *scale, int grid,
@@ -158,8 +158,8 @@ constexpr float kBfpTiny = 1e-30f;  // blocks with max |v| <= this are stored as
 void launch_ckpt_store_bfp(const float *u, long long n, short *q, float *scale, int grid, cudaStream_t s);
 void launch_ckpt_load_bfp(const short *q, const float *scale, long long n, float *u, int grid, cudaStream_t s);
 // image on the model grid: the padded grid's model window of G
-void launch_image_cut(const double *G, const Grid &g, int nb, const int *n, int nd, double *out, cudaStream_t s);
-void launch_grad_fold(const double *G, const float *vel2, float dt, const Grid &g, int nb, const int *n, int nd,
+void launch_image_cut(const float2 *G, const Grid &g, int nb, const int *n, int nd, double *out, cudaStream_t s);
+void launch_grad_fold(const float2 *G, const float *vel2, float dt, const Grid &g, int nb, const int *n, int nd,
                       double *out, cudaStream_t s);
 
 // ---- batched 2D forward (k_batch2d.cu) ----
@@ -202,7 +202,7 @@ struct BatchAdj {
     float *Y;        // nu_{k+1} in, mu_k out
     const float *V;  // forward level V_k
     const float *vel;
-    double *G;  // dJ/dvel2, per shot, padded grids
+    float2 *G;  // dJ/dvel2 accumulators (compensated pairs), per shot, padded grids
     const float *wz, *wx;
     int sponge, n1;
     float c0, cz[kMaxNop + 1], cx[kMaxNop + 1];
@@ -219,7 +219,7 @@ void launch_batch2d_adj(int nop, int tile, const BatchShot *shots, const int4 *i
 void launch_batch_ckpt(bool store, int fmt, const BatchShot *shots, int nshots, float *u, void *q, float *scales,
                        int n1, long long cells, cudaStream_t s);
 void launch_residual_flat(const float *d, const float *dobs, float *r, long long n, double *part, cudaStream_t s);
-void launch_batch_grad_fold(const BatchShot *shots, const int2 *win, int nshots, const double *G, const float *vel2,
+void launch_batch_grad_fold(const BatchShot *shots, const int2 *win, int nshots, const float2 *G, const float *vel2,
                             float dt, int n1, int nb, int nz, int nxm, double *out, cudaStream_t s);
 // column-march forward (k_batch2d_col.cu): 8th order, n1 % 4 == 0, n1 <= 2048;
 // returns the threads per CTA (0 if the shape is not covered) and the dynamic shared memory
@@ -275,7 +275,7 @@ cudaError_t launch_stepB3_tma_with(bool exact, const CUtensorMap &cur, const CUt
                                    unsigned long long *counter, unsigned long long base, int *err, cudaStream_t s,
                                    float *lap_out);
 cudaError_t launch_stepB3_adj(const CUtensorMap &g_halo, const CUtensorMap &y_tile, const CUtensorMap &x_tile,
-                              float *Y, const float *lap_v, double *grad, const StepBParams &sp,
+                              float *Y, const float *lap_v, float2 *grad, const StepBParams &sp,
                               const Step3Launch &sh, unsigned long long *counter, unsigned long long base, int *err,
                               cudaStream_t s);
 // g = I vel2 nu (cells at least nop from every face), elementwise

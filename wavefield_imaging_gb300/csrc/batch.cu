@@ -47,7 +47,8 @@ struct awe_batch {
     long long gscale_per = 0;  // checkpoint scales per level: one per shot, or per 64-cell block (BFP16)
     float *slots = nullptr, *gX = nullptr, *gY = nullptr, *res = nullptr, *scales = nullptr, *dobs = nullptr;
     void *ckpt = nullptr;
-    double *G = nullptr, *part = nullptr, *grad = nullptr;
+    float2 *G = nullptr;  // gradient accumulators (compensated pairs)
+    double *part = nullptr, *grad = nullptr;
     int *rc_start = nullptr;
     BatchRecCorner *rc = nullptr;
     int2 *win = nullptr;
@@ -587,7 +588,7 @@ static awe_status grad_alloc(awe_batch *b, int T, int fmt) {
         const size_t nd = (size_t)std::max(b->ndat, 1LL);
         for (void **q : {(void **)&b->gX, (void **)&b->gY})
             if (st == AWE_OK) st = balloc(b, q, cb);
-        if (st == AWE_OK) st = balloc(b, (void **)&b->G, (size_t)b->cells * sizeof(double));
+        if (st == AWE_OK) st = balloc(b, (void **)&b->G, (size_t)b->cells * sizeof(float2));
         if (st == AWE_OK) st = balloc(b, (void **)&b->res, nd * sizeof(float));
         if (st == AWE_OK) st = balloc(b, (void **)&b->dobs, nd * sizeof(float));
         if (st == AWE_OK) st = balloc(b, (void **)&b->part, ((nd + 1023) / 1024) * sizeof(double));
@@ -704,7 +705,7 @@ static awe_status grad_sequence(awe_batch *b, cudaStream_t s) {
     // adjoint sweep, last segment first
     CUDA_TRY(cudaMemsetAsync(b->gX, 0, cb, s));
     CUDA_TRY(cudaMemsetAsync(b->gY, 0, cb, s));
-    CUDA_TRY(cudaMemsetAsync(b->G, 0, (size_t)cells * sizeof(double), s));
+    CUDA_TRY(cudaMemsetAsync(b->G, 0, (size_t)cells * sizeof(float2), s));
     float *X = b->gX, *Y = b->gY;
     for (int seg = b->gseg - 1; seg >= 0; seg--) {
         const int k0 = seg * T, k1 = std::min(k0 + T, b->d.nt);

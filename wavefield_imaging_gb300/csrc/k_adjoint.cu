@@ -11,13 +11,15 @@
 //   nu_k, kappa_k = ABC^T(mu)
 //   lambda_k = 2 I nu_k + L(I vel2 nu_k) + kappa_k + W (1 - 2 I) nu_{k+1} + W R^T r_k
 //   the new buffer holds mu_k = W lambda_k
-//   dJ/dvel2 += I nu_k L(V_k)  (+ nu_k wav w at the source corners), in FP64.
+//   dJ/dvel2 += I nu_k L(V_k)  (+ nu_k wav w at the source corners), summed per
+//   cell as a compensated FP32 pair (gsum.cuh) and folded in FP64.
 // The stencil is symmetric, so L^T is the same stencil applied to I vel2 nu.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "awe_internal.h"
+#include "gsum.cuh"
 
 namespace awe {
 
@@ -36,12 +38,12 @@ __device__ __forceinline__ bool interior(const Grid &g, int i1, int i2, int i3) 
 }
 
 // main adjoint step, one thread per cell.  X = nu_k (stencil), Y = nu_{k+1}
-// in / mu_k out (same cell only), V = V_k (stencil), G += I nu L(V) in FP64
+// in / mu_k out (same cell only), V = V_k (stencil), G += I nu L(V) (compensated)
 // (p.xcorr: G += I nu V, the cross-correlation imaging condition).
 template <int NOP, int NDIM>
 __global__ void __launch_bounds__(256) k_adjB(const float *__restrict__ X, float *__restrict__ Y,
                                               const float *__restrict__ V, const float *__restrict__ vel,
-                                              double *__restrict__ G, const AdjParams p) {
+                                              float2 *__restrict__ G, const AdjParams p) {
     const int i1 = blockIdx.x * blockDim.x + threadIdx.x;
     const int i2 = blockIdx.y * blockDim.y + threadIdx.y;
     const int i3 = (NDIM == 3) ? (int)blockIdx.z : 0;
@@ -71,7 +73,7 @@ __global__ void __launch_bounds__(256) k_adjB(const float *__restrict__ X, float
     const float lam = (in ? 2.f * x : 0.f) + lt + (in ? -w : w) * Y[i];
     Y[i] = w * lam;
     if (in && p.xcorr) {
-        G[i] += (double)__fmul_rn(x, V[i]);  // FP32 product, FP64 sum
+        G[i] = gsum_add(G[i], __fmul_rn(x, V[i]));  // FP32 product, compensated sum
     } else if (in) {
         float lap = V[i] * p.k.c0;
 #pragma unroll
@@ -81,12 +83,12 @@ __global__ void __launch_bounds__(256) k_adjB(const float *__restrict__ X, float
             if constexpr (NDIM == 3) t = fmaf(__ldg(V + i - k * s3) + __ldg(V + i + k * s3), p.k.c[2][k], t);
             lap += t;
         }
-        G[i] += (double)__fmul_rn(x, lap);
+        G[i] = gsum_add(G[i], __fmul_rn(x, lap));
     }
 }
 
 template <int NDIM>
-static void adj_dispatch_nop(int nop, const float *X, float *Y, const float *V, const float *vel, double *G,
+static void adj_dispatch_nop(int nop, const float *X, float *Y, const float *V, const float *vel, float2 *G,
                              const AdjParams &p, cudaStream_t s) {
     dim3 block(64, 4, 1);
     dim3 grid((p.g.n1 + 63) / 64, (p.g.n2 + 3) / 4, NDIM == 3 ? p.g.n3 : 1);
@@ -99,7 +101,7 @@ static void adj_dispatch_nop(int nop, const float *X, float *Y, const float *V, 
     }
 }
 
-void launch_adjB(const float *X, float *Y, const float *V, const float *vel, double *G, const AdjParams &p,
+void launch_adjB(const float *X, float *Y, const float *V, const float *vel, float2 *G, const AdjParams &p,
                  cudaStream_t s) {
     if (p.nd == 3) adj_dispatch_nop<3>(p.nop, X, Y, V, vel, G, p, s);
     else adj_dispatch_nop<2>(p.nop, X, Y, V, vel, G, p, s);
@@ -313,7 +315,7 @@ void launch_rec_adj(float *mu, const GeoPoint *pts, int nr, const float *r, cons
 
 // source term of the gradient: dJ/dvel2[node] += nu[node] * wav * w (one
 // thread, sources and corners in order)
-__global__ void k_src_grad(double *G, const float *__restrict__ nu, const GeoPoint *__restrict__ pts, int ns,
+__global__ void k_src_grad(float2 *G, const float *__restrict__ nu, const GeoPoint *__restrict__ pts, int ns,
                            const float *__restrict__ wav, int it, int ncs, int one_wavelet, int nc,
                            const long long *__restrict__ off) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
@@ -322,12 +324,12 @@ __global__ void k_src_grad(double *G, const float *__restrict__ nu, const GeoPoi
         const GeoPoint pt = pts[s];
         for (int c = 0; c < nc; c++) {
             const long long n = pt.base + off[c];
-            G[n] += (double)nu[n] * (double)(dd * pt.w[c]);
+            G[n] = gsum_add_prod(G[n], nu[n], dd * pt.w[c]);
         }
     }
 }
 
-void launch_src_grad(double *G, const float *nu, const GeoPoint *pts, int ns, const float *wav, int it, int ncs,
+void launch_src_grad(float2 *G, const float *nu, const GeoPoint *pts, int ns, const float *wav, int it, int ncs,
                      bool one_wavelet, int nd, const long long *off, cudaStream_t s) {
     if (ns > 0) k_src_grad<<<1, 1, 0, s>>>(G, nu, pts, ns, wav, it, ncs, one_wavelet, nd == 3 ? 8 : 4, off);
 }
@@ -470,7 +472,7 @@ __device__ __forceinline__ int edge_axes(int j1, int j2, int j3, int m1, int m2,
 // skip_big: model cells on two or more edge axes (the model's edges and
 // corners, whose replicas span (nb+1)^2 or (nb+1)^3 padded cells) are left
 // to k_grad_fold_big
-__global__ void k_grad_fold(const double *__restrict__ G, const float *__restrict__ vel2, double inv_dt2, Grid g,
+__global__ void k_grad_fold(const float2 *__restrict__ G, const float *__restrict__ vel2, double inv_dt2, Grid g,
                             int nb, int m1, int m2, int m3, int nd, double *__restrict__ out, int skip_big) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)m1 * m2 * m3) return;
@@ -487,27 +489,27 @@ __global__ void k_grad_fold(const double *__restrict__ G, const float *__restric
             for (int i1 = a1; i1 <= b1; i1++) {
                 const long long i = ((long long)i3 * g.n2 + i2) * g.n1 + i1;
                 const double v2 = vel2[i];
-                acc += G[i] * (-v2 * v2 * inv_dt2);
+                acc += gsum_value(G[i]) * (-v2 * v2 * inv_dt2);
             }
     out[t] = acc;
 }
 
-__global__ void k_image_cut(const double *__restrict__ G, Grid g, int nb, int m1, int m2, int m3, int nd,
+__global__ void k_image_cut(const float2 *__restrict__ G, Grid g, int nb, int m1, int m2, int m3, int nd,
                             double *__restrict__ out) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)m1 * m2 * m3) return;
     const int j1 = (int)(t % m1), j2 = (int)((t / m1) % m2), j3 = (int)(t / ((long long)m1 * m2));
-    out[t] = G[((long long)(nd == 3 ? j3 + nb : 0) * g.n2 + j2 + nb) * g.n1 + j1 + nb];
+    out[t] = gsum_value(G[((long long)(nd == 3 ? j3 + nb : 0) * g.n2 + j2 + nb) * g.n1 + j1 + nb]);
 }
 
-void launch_image_cut(const double *G, const Grid &g, int nb, const int *n, int nd, double *out, cudaStream_t s) {
+void launch_image_cut(const float2 *G, const Grid &g, int nb, const int *n, int nd, double *out, cudaStream_t s) {
     const long long m = (long long)n[0] * n[1] * (nd == 3 ? n[2] : 1);
     k_image_cut<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(G, g, nb, n[0], n[1], nd == 3 ? n[2] : 1, nd, out);
 }
 
 // The model's edge and corner cells, one block each: 2D the 4 corners; 3D
 // the 4 edges along each axis (corners counted with the axis-1 edges).
-__global__ void __launch_bounds__(256) k_grad_fold_big(const double *__restrict__ G, const float *__restrict__ vel2,
+__global__ void __launch_bounds__(256) k_grad_fold_big(const float2 *__restrict__ G, const float *__restrict__ vel2,
                                                        double inv_dt2, Grid g, int nb, int m1, int m2, int m3, int nd,
                                                        double *__restrict__ out) {
     long long b = blockIdx.x;
@@ -542,7 +544,7 @@ __global__ void __launch_bounds__(256) k_grad_fold_big(const double *__restrict_
         const long long i1 = a1 + k % w1, i2 = a2 + (k / w1) % w2, i3 = a3 + k / (w1 * w2);
         const long long i = (i3 * g.n2 + i2) * g.n1 + i1;
         const double v2 = vel2[i];
-        acc += G[i] * (-v2 * v2 * inv_dt2);
+        acc += gsum_value(G[i]) * (-v2 * v2 * inv_dt2);
     }
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     __shared__ double part[8];
@@ -555,7 +557,7 @@ __global__ void __launch_bounds__(256) k_grad_fold_big(const double *__restrict_
     }
 }
 
-void launch_grad_fold(const double *G, const float *vel2, float dt, const Grid &g, int nb, const int *n, int nd,
+void launch_grad_fold(const float2 *G, const float *vel2, float dt, const Grid &g, int nb, const int *n, int nd,
                       double *out, cudaStream_t s) {
     const int m1 = n[0], m2 = n[1], m3 = nd == 3 ? n[2] : 1;
     const long long m = (long long)m1 * m2 * m3;

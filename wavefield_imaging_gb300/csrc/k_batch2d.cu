@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include "awe_internal.h"
+#include "gsum.cuh"
 
 namespace awe {
 
@@ -273,16 +274,17 @@ __global__ void __launch_bounds__(TZ / 4 * TX) k_batch2d_adj(const BatchShot *__
         const int x = x0 + xi, zb = z0 + 4 * zq;
         if (x >= n2 || zb >= n1) continue;
         const long long gi = sh.off + (long long)x * n1 + zb;
-        // the FP64 gradient of this strip, loaded before the stencils so the
-        // load latency overlaps them
-        double *G = p.G + gi;
-        const double2 G01 = __ldcs(reinterpret_cast<const double2 *>(G));
-        const double2 G23 = __ldcs(reinterpret_cast<const double2 *>(G + 2));
+        // the gradient accumulators of this strip, loaded before the stencils
+        // so the load latency overlaps them
+        float2 *G = p.G + gi;
+        const float4 G01 = __ldcs(reinterpret_cast<const float4 *>(G));
+        const float4 G23 = __ldcs(reinterpret_cast<const float4 *>(G + 2));
         const float nu[4] = {nv4.x, nv4.y, nv4.z, nv4.w}, yv[4] = {yv4.x, yv4.y, yv4.z, yv4.w};
         const float wx = p.sponge ? p.wx[sh.wx_off + x] : 1.f;
         const bool xin = x >= NOP && x < n2 - NOP;
         float mu[4], wc[4];
-        double gacc[4];
+        float2 ga[4] = {make_float2(G01.x, G01.y), make_float2(G01.z, G01.w), make_float2(G23.x, G23.y),
+                        make_float2(G23.z, G23.w)};
         // 16-byte shared loads of both stencils' z windows and x neighbours, packed FP32x2
         const int tz0 = SH + 4 * zq;
         constexpr int NZW = 4 + 2 * SH;
@@ -321,7 +323,7 @@ __global__ void __launch_bounds__(TZ / 4 * TX) k_batch2d_adj(const BatchShot *__
             wc[i] = p.sponge ? p.wz[z] * wx : 1.f;
             const float lam = (in ? 2.f * nu[i] : 0.f) + lt4[i] + (in ? -wc[i] : wc[i]) * yv[i];
             mu[i] = wc[i] * lam;
-            gacc[i] = (double)(in ? __fmul_rn(nu[i], lv4[i]) : 0.f);  // FP32 product, FP64 sum
+            if (in) ga[i] = gsum_add(ga[i], __fmul_rn(nu[i], lv4[i]));  // FP32 product, compensated sum
         }
         const long long cell0 = (long long)x * n1 + zb;
         // receiver residuals (W R^T r, then the W of mu): corners listed per tile
@@ -350,13 +352,13 @@ __global__ void __launch_bounds__(TZ / 4 * TX) k_batch2d_adj(const BatchShot *__
                     const long long d = gp.base + (cc & 1) + (cc >> 1) * (long long)n1 - cell0;
 #pragma unroll
                     for (int i = 0; i < 4; i++)
-                        if (d == i) gacc[i] += (double)nu[i] * (double)(dd * gp.w[cc]);
+                        if (d == i) ga[i] = gsum_add_prod(ga[i], nu[i], dd * gp.w[cc]);
                 }
             }
         }
         *reinterpret_cast<float4 *>(p.Y + gi) = make_float4(mu[0], mu[1], mu[2], mu[3]);
-        __stcs(reinterpret_cast<double2 *>(G), make_double2(G01.x + gacc[0], G01.y + gacc[1]));
-        __stcs(reinterpret_cast<double2 *>(G + 2), make_double2(G23.x + gacc[2], G23.y + gacc[3]));
+        __stcs(reinterpret_cast<float4 *>(G), make_float4(ga[0].x, ga[0].y, ga[1].x, ga[1].y));
+        __stcs(reinterpret_cast<float4 *>(G + 2), make_float4(ga[2].x, ga[2].y, ga[3].x, ga[3].y));
     }
 }
 
@@ -484,7 +486,7 @@ void launch_residual_flat(const float *d, const float *dobs, float *r, long long
 // model gradient: dJ/dvel2 * (-vel2^2 / dt^2), each shot's padded cells summed
 // onto the model cells they replicate (window columns x0 .. x0 + nx - 1)
 __global__ void k_batch_grad_fold(const BatchShot *__restrict__ shots, const int2 *__restrict__ win, int nshots,
-                                  const double *__restrict__ G, const float *__restrict__ vel2, double inv_dt2,
+                                  const float2 *__restrict__ G, const float *__restrict__ vel2, double inv_dt2,
                                   int n1, int nb, int nz, int nxm, double *__restrict__ out) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)nz * nxm) return;
@@ -501,13 +503,13 @@ __global__ void k_batch_grad_fold(const BatchShot *__restrict__ shots, const int
             for (int iz = za; iz <= zbnd; iz++) {
                 const long long i = sh.off + (long long)ix * n1 + iz;
                 const double v2 = vel2[i];
-                acc += G[i] * (-v2 * v2 * inv_dt2);
+                acc += gsum_value(G[i]) * (-v2 * v2 * inv_dt2);
             }
     }
     out[t] = acc;
 }
 
-void launch_batch_grad_fold(const BatchShot *shots, const int2 *win, int nshots, const double *G, const float *vel2,
+void launch_batch_grad_fold(const BatchShot *shots, const int2 *win, int nshots, const float2 *G, const float *vel2,
                             float dt, int n1, int nb, int nz, int nxm, double *out, cudaStream_t s) {
     const long long n = (long long)nz * nxm;
     k_batch_grad_fold<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(shots, win, nshots, G, vel2,

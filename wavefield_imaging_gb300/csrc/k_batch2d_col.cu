@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include "awe_internal.h"
+#include "gsum.cuh"
 #include "tma.cuh"
 
 namespace awe {
@@ -239,7 +240,7 @@ __global__ void __launch_bounds__(512) k_batch2d_col(const BatchShot *__restrict
 // forms g = I vel2 nu for its cells and writes it to the slot's g column
 // (zero-padded) for the z window, and keeps g and V in 9-column register
 // queues for the x neighbours.  For the output column (the centre) the
-// thread's nu_{k+1} (Y) and FP64 gradient strips are loaded before the ring
+// thread's nu_{k+1} (Y) and gradient-accumulator strips are loaded before the ring
 // wait; mu_k = W lambda goes back to Y and the gradient strip is updated and
 // stored.  Receiver corners of the item are listed by column; sources are
 // tested only near their columns.
@@ -250,7 +251,7 @@ constexpr int YG_DEPTH = YG_AHEAD + 1;
 
 __host__ __device__ inline int adj_slot(int n1) { return 2 * n1 + 2 * (n1 + 8); }
 // slot layout (floats): X [n1] | vel [n1] | V [4 | n1 | 4] | g [4 | n1 | 4]; after the
-// ring, YG_DEPTH slots of the output columns' FP64 gradient [n1] and nu_{k+1} [n1]
+// ring, YG_DEPTH slots of the output columns' gradient accumulators [n1] and nu_{k+1} [n1]
 __host__ __device__ inline int adj_off_v(int n1) { return 2 * n1; }
 __host__ __device__ inline int adj_off_g(int n1) { return 2 * n1 + (n1 + 8); }
 
@@ -263,7 +264,7 @@ __global__ void __maxnreg__(96) k_batch2d_col_adj(const BatchShot *__restrict__ 
     const int SLOT = adj_slot(n1), OV = adj_off_v(n1), OG = adj_off_g(n1);
     uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw);
     float *ring = reinterpret_cast<float *>(smem_raw + 128);
-    double *gring = reinterpret_cast<double *>(ring + ARING * SLOT);
+    float2 *gring = reinterpret_cast<float2 *>(ring + ARING * SLOT);
     float *yring = reinterpret_cast<float *>(gring + YG_DEPTH * n1);
     const int tid = threadIdx.x;
     const int zb = 2 * tid;
@@ -393,18 +394,18 @@ __global__ void __maxnreg__(96) k_batch2d_col_adj(const BatchShot *__restrict__ 
                         const float2 nv2 = *reinterpret_cast<const float2 *>(H + zb);  // nu_k of the centre
                         const int q = (s % YG_DEPTH) * n1 + zb;
                         const float2 yv2 = *reinterpret_cast<const float2 *>(yring + q);
-                        const double2 G01 = *reinterpret_cast<const double2 *>(gring + q);
+                        const float4 G01 = *reinterpret_cast<const float4 *>(gring + q);
                         const float nu[2] = {nv2.x, nv2.y}, yv[2] = {yv2.x, yv2.y};
                         const bool xin = x >= CNOP && x < sh.n2 - CNOP;
                         float mu[2], wc[2];
-                        double gacc[2];
+                        float2 ga[2] = {make_float2(G01.x, G01.y), make_float2(G01.z, G01.w)};
 #pragma unroll
                         for (int i = 0; i < 2; i++) {
                             const bool in = xin && zin[i];
                             wc[i] = p.sponge ? wz[i] * wx : 1.f;
                             const float lam = (in ? 2.f * nu[i] : 0.f) + lt[i] + (in ? -wc[i] : wc[i]) * yv[i];
                             mu[i] = wc[i] * lam;
-                            gacc[i] = (double)(in ? __fmul_rn(nu[i], lv[i]) : 0.f);  // FP32 product, FP64 sum
+                            if (in) ga[i] = gsum_add(ga[i], __fmul_rn(nu[i], lv[i]));  // FP32 product, compensated sum
                         }
                         if (p.row >= 0) {  // receiver residuals of this column (corners in list order)
                             for (int ee = e; ee < eend; ee++) {
@@ -432,12 +433,12 @@ __global__ void __maxnreg__(96) k_batch2d_col_adj(const BatchShot *__restrict__ 
                                     const long long d = gp.base + (cc & 1) + (cc >> 1) * (long long)n1 - cell0;
 #pragma unroll
                                     for (int i = 0; i < 2; i++)
-                                        if (d == i) gacc[i] += (double)nu[i] * (double)(dd * gp.w[cc]);
+                                        if (d == i) ga[i] = gsum_add_prod(ga[i], nu[i], dd * gp.w[cc]);
                                 }
                             }
                         }
                         *reinterpret_cast<float2 *>(p.Y + gi) = make_float2(mu[0], mu[1]);
-                        __stcs(reinterpret_cast<double2 *>(p.G + gi), make_double2(G01.x + gacc[0], G01.y + gacc[1]));
+                        __stcs(reinterpret_cast<float4 *>(p.G + gi), make_float4(ga[0].x, ga[0].y, ga[1].x, ga[1].y));
                     }
                     if (s >= 2 * CNOP) {  // the corners of this output column are done
                         while (e < eend && crc[e].x == x) e++;
@@ -471,7 +472,7 @@ __global__ void __maxnreg__(96) k_batch2d_col_adj(const BatchShot *__restrict__ 
 }  // namespace
 
 size_t batch2d_col_adj_smem(int n1) {
-    return 128 + (size_t)ARING * adj_slot(n1) * sizeof(float) + (size_t)YG_DEPTH * n1 * (sizeof(double) + sizeof(float));
+    return 128 + (size_t)ARING * adj_slot(n1) * sizeof(float) + (size_t)YG_DEPTH * n1 * (sizeof(float2) + sizeof(float));
 }
 
 static int adj_threads(int n1) { return ((n1 / 2 + 31) / 32) * 32; }

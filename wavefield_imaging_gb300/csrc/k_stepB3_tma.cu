@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include "awe_internal.h"
+#include "gsum.cuh"
 #include "fp_exact.cuh"
 #include "tma.cuh"
 
@@ -57,7 +58,7 @@ struct Step3Params {
     // MODE 2 (adjoint step): cur = I vel2 nu, prv = nu_{k+1} (overwritten by
     // mu = W lambda), vel = nu_k; lap_v = L(V_k); grad += I nu L(V_k) (FP64)
     const float *lap_v;
-    double *grad;
+    float2 *grad;  // gradient accumulators (compensated pairs)
 };
 
 template <bool EXACT>
@@ -151,7 +152,7 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
                     // adjoint: the plane's L(V) and gradient loads go out before the
                     // ring wait and the stencil, so their latency overlaps both
                     float4 lvp = make_float4(0.f, 0.f, 0.f, 0.f);
-                    double2 gp0 = make_double2(0.0, 0.0), gp1 = make_double2(0.0, 0.0);
+                    float4 gp0 = make_float4(0.f, 0.f, 0.f, 0.f), gp1 = gp0;
                     bool gok = false;
                     long long gip = 0;
                     if constexpr (MODE == 2) {
@@ -161,8 +162,8 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
                             gip = ((long long)yp * p.n2 + x) * p.n1 + zg;
                             if (gok) {
                                 lvp = __ldcs(reinterpret_cast<const float4 *>(p.lap_v + gip));
-                                gp0 = __ldcs(reinterpret_cast<const double2 *>(p.grad + gip));
-                                gp1 = __ldcs(reinterpret_cast<const double2 *>(p.grad + gip + 2));
+                                gp0 = __ldcs(reinterpret_cast<const float4 *>(p.grad + gip));
+                                gp1 = __ldcs(reinterpret_cast<const float4 *>(p.grad + gip + 2));
                             }
                         }
                     }
@@ -254,7 +255,8 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
                             // lambda = 2 I nu + L(I vel2 nu) + W (1 - 2 I) nu_{k+1}; out = W lambda
                             const float wy = (!undamped && p.w3) ? __ldg(p.w3 + y) : 1.f;
                             const float lv4[4] = {lvp.x, lvp.y, lvp.z, lvp.w};
-                            double gacc[4];
+                            float2 ga[4] = {make_float2(gp0.x, gp0.y), make_float2(gp0.z, gp0.w),
+                                            make_float2(gp1.x, gp1.y), make_float2(gp1.z, gp1.w)};
 #pragma unroll
                             for (int i = 0; i < 4; i++) {
                                 const bool in = zin[i] && xin && yin;
@@ -262,15 +264,13 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
                                 const float nu = vel4[i];
                                 const float lam = (in ? 2.f * nu : 0.f) + lap[i] + (in ? -w : w) * prv4[i];
                                 out[i] = w * lam;
-                                // product in FP32 (the fields are FP32), accumulated in FP64:
-                                // one conversion and one FP64 add per cell
-                                gacc[i] = (double)(in ? __fmul_rn(nu, lv4[i]) : 0.f);
+                                // product in FP32 (the fields are FP32), compensated FP32 sum
+                                if (in) ga[i] = gsum_add(ga[i], __fmul_rn(nu, lv4[i]));
                             }
                             if (gok) {
-                                double *G = p.grad + gip;
-                                __stcs(reinterpret_cast<double2 *>(G), make_double2(gp0.x + gacc[0], gp0.y + gacc[1]));
-                                __stcs(reinterpret_cast<double2 *>(G + 2),
-                                       make_double2(gp1.x + gacc[2], gp1.y + gacc[3]));
+                                float2 *G = p.grad + gip;
+                                __stcs(reinterpret_cast<float4 *>(G), make_float4(ga[0].x, ga[0].y, ga[1].x, ga[1].y));
+                                __stcs(reinterpret_cast<float4 *>(G + 2), make_float4(ga[2].x, ga[2].y, ga[3].x, ga[3].y));
                             }
                         } else if (!EXACT && undamped && tile_inner && yin) {
                             // every cell of the strip is interior and undamped: packed update
@@ -460,7 +460,7 @@ static Step3Params step3_params(const StepBParams &sp, const Step3Launch &sh, un
 // adjoint step (AWE_FAST): g_halo = halo-box map of I vel2 nu_k, y_tile = tile
 // map of nu_{k+1} (Y, overwritten by mu_k), x_tile = tile map of nu_k
 cudaError_t launch_stepB3_adj(const CUtensorMap &g_halo, const CUtensorMap &y_tile, const CUtensorMap &x_tile,
-                              float *Y, const float *lap_v, double *grad, const StepBParams &sp,
+                              float *Y, const float *lap_v, float2 *grad, const StepBParams &sp,
                               const Step3Launch &sh, unsigned long long *counter, unsigned long long base, int *err,
                               cudaStream_t s) {
     Step3Params p = step3_params(sp, sh, counter, base, err, Y);

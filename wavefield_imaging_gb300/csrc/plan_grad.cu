@@ -38,7 +38,7 @@ struct GradState {
     long long nblk = 0;      // scale blocks per level (block floating point)
     unsigned int *amax = nullptr;
     float *X = nullptr, *Y = nullptr, *kap = nullptr;
-    double *G = nullptr;
+    float2 *G = nullptr;  // gradient / image accumulators (compensated pairs)
     float *dat = nullptr, *r = nullptr;
     double *row_sum = nullptr;
     // TMA path (3D, 8th order): three rolling forward levels, I vel2 nu, and
@@ -79,7 +79,7 @@ static awe_status grad_alloc(awe_plan *p, int T, int fmt) {
     AWE_TRY(dev_alloc(p, (void **)&st->X, cells * sizeof(float)));
     AWE_TRY(dev_alloc(p, (void **)&st->Y, cells * sizeof(float)));
     if (d.ndim == 3 && d.dabc) AWE_TRY(dev_alloc(p, (void **)&st->kap, cells * sizeof(float)));
-    AWE_TRY(dev_alloc(p, (void **)&st->G, cells * sizeof(double)));
+    AWE_TRY(dev_alloc(p, (void **)&st->G, cells * sizeof(float2)));
     const size_t nd = (size_t)p->nsmp * (p->nr > 0 ? p->nr : 1);
     AWE_TRY(dev_alloc(p, (void **)&st->dat, nd * sizeof(float)));
     AWE_TRY(dev_alloc(p, (void **)&st->r, nd * sizeof(float)));
@@ -206,7 +206,7 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
     // 3. adjoint sweep
     CUDA_TRY(cudaMemsetAsync(st->X, 0, bytes, s));
     CUDA_TRY(cudaMemsetAsync(st->Y, 0, bytes, s));
-    CUDA_TRY(cudaMemsetAsync(st->G, 0, (size_t)cells * sizeof(double), s));
+    CUDA_TRY(cudaMemsetAsync(st->G, 0, (size_t)cells * sizeof(float2), s));
     if (st->kap) CUDA_TRY(cudaMemsetAsync(st->kap, 0, bytes, s));
     const StepBParams sp = stepB_params(p);
     const bool sponge = d.dabc && !d.hybrid;
