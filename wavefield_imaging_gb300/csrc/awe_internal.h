@@ -186,14 +186,13 @@ struct BatchStep {
     int row;            // trace row written by this step, -1: none
     const float *prv;   // previous level when stepping out of place (null: in place in nxt)
 };
-struct BatchRecCorner {
-    long long node;  // cell of the shot's padded grid
-    int r;           // receiver index within the shot
-    float w;         // interpolation weight
+// a padded cell that receivers inject adjoint residuals into, with its
+// receiver corners [e0, e1) in (receiver, corner) order
+struct BatchRecCell {
+    long long gi;  // cell of the concatenated padded grids
+    int shot, x, z, e0, e1, pad;
 };
-// a receiver corner of a column item: column and row in the shot's padded grid
-struct BatchColCorner {
-    int x, z;
+struct BatchRecW {
     int r;    // receiver index within the shot
     float w;  // interpolation weight
 };
@@ -209,8 +208,6 @@ struct BatchAdj {
     const GeoPoint *src;
     const float *wav;
     int it;
-    const int *rc_start;  // per work item: receiver corners [rc_start[w], rc_start[w + 1])
-    const BatchRecCorner *rc;
     const float *res;  // residuals, laid out as the traces
     int row;           // residual row of this step, -1: none
 };
@@ -227,12 +224,14 @@ int batch2d_col_shape(int nop, int n1, size_t *smem);
 int batch2d_col_ctas_per_sm(int n1);
 void launch_batch2d_col(const BatchShot *shots, const int4 *items, int nitems, int grid, int L, const BatchStep &p,
                         int *err, cudaStream_t s);
-// adjoint step as a column march (same arithmetic as k_batch2d_adj): per
-// item the receiver corners [cstart[w], cstart[w+1]) sorted by column
+// adjoint step as a column march (same arithmetic as k_batch2d_adj)
 int batch2d_col_adj_ctas_per_sm(int n1);
 void launch_batch2d_col_adj(const BatchShot *shots, const int4 *items, int nitems, int grid, int L,
-                            const BatchAdj &p, const int *cstart, const BatchColCorner *crc, int *err,
-                            cudaStream_t s);
+                            const BatchAdj &p, int *err, cudaStream_t s);
+// the adjoint step's receiver term W R^T r on mu (p.Y), after either adjoint
+// kernel: one thread per receiver cell, its corners in order
+void launch_batch_rec_adj(const BatchRecCell *cells, int ncells, const BatchRecW *ws, const BatchShot *shots,
+                          const BatchAdj &p, cudaStream_t s);
 constexpr int kBatchNumTiles = 4;
 constexpr int kBatchRecBlock = 128;  // receivers per receiver item (<= threads of every tile shape)
 extern const int kBatchTiles[kBatchNumTiles][2];

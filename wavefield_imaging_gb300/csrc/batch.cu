@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <vector>
 
 #include "awe_internal.h"
@@ -49,19 +50,17 @@ struct awe_batch {
     void *ckpt = nullptr;
     float2 *G = nullptr;  // gradient accumulators (compensated pairs)
     double *part = nullptr, *grad = nullptr;
-    int *rc_start = nullptr;
-    BatchRecCorner *rc = nullptr;
+    // receiver cells of the adjoint's residual term (-1: not built yet)
+    BatchRecCell *rec_cells = nullptr;
+    BatchRecW *rec_ws = nullptr;
+    int nrec_cells = -1;
     int2 *win = nullptr;
-    int rc_tile = -1;
     // column-march forward (k_batch2d_col): chunk length (0 = the tile kernels), its items and grid
     int colL = 0, col_grid = 0, ncol_items = 0;
     std::vector<int4> col_items;
     int4 *d_col_items = nullptr;
     int *d_err = nullptr;  // set by a bulk-copy wait that timed out
-    // column-march adjoint: receiver corners of each column item, by column
-    int *col_cstart = nullptr;
-    BatchColCorner *col_rc = nullptr;
-    int col_rc_L = -1, col_adj_grid = 0;
+    int col_adj_grid = 0;  // column-march adjoint's grid (0: the tile adjoint)
 };
 
 #define CUDA_TRY(expr)                                                                            \
@@ -517,52 +516,44 @@ awe_status awe_batch_tune(awe_batch *b, int steps, int *tile_out, int *grid_out)
     return AWE_OK;
 }
 
-// per-tile lists of receiver corners (cells the adjoint injects residuals into)
-static awe_status build_rec_corners(awe_batch *b) {
-    const int TZ = kBatchTiles[b->tile][0], TX = kBatchTiles[b->tile][1];
-    std::vector<std::vector<BatchRecCorner>> per(b->ntile_items);
-    // tile item index of (shot, z0, x0): items are laid out shot by shot, x-major
-    std::vector<int> first(b->shots.size());
-    int acc = 0;
-    const int ntz = (b->n1 + TZ - 1) / TZ;
-    for (size_t s = 0; s < b->shots.size(); s++) {
-        first[s] = acc;
-        acc += ((b->shots[s].n2 + TX - 1) / TX) * ntz;
-    }
+// receiver cells of every shot (cells the adjoint injects residuals into),
+// each with its corners in (receiver, corner) order
+static awe_status build_rec_cells(awe_batch *b) {
+    std::vector<BatchRecCell> cells;
+    std::vector<BatchRecW> ws;
     for (size_t s = 0; s < b->shots.size(); s++) {
         const BatchShot &sh = b->shots[s];
+        std::map<long long, std::vector<BatchRecW>> per;
         for (int r = 0; r < sh.nr; r++) {
             const GeoPoint &g = b->h_rec[sh.rec0 + r];
             for (int c = 0; c < 4; c++) {
                 const long long node = g.base + (c & 1) + (c >> 1) * (long long)b->n1;
-                const int z = (int)(node % b->n1), x = (int)(node / b->n1);
-                if (x < 0 || x >= sh.n2) continue;
-                const int item = first[s] + (x / TX) * ntz + z / TZ;
-                per[item].push_back(BatchRecCorner{node, r, g.w[c]});
+                if (node < 0 || node >= (long long)sh.n2 * b->n1) continue;
+                per[node].push_back(BatchRecW{r, g.w[c]});
             }
         }
+        for (const auto &kv : per) {
+            const int e0 = (int)ws.size();
+            ws.insert(ws.end(), kv.second.begin(), kv.second.end());
+            cells.push_back(BatchRecCell{sh.off + kv.first, (int)s, (int)(kv.first / b->n1), (int)(kv.first % b->n1),
+                                         e0, (int)ws.size(), 0});
+        }
     }
-    std::vector<int> start(b->items.size() + 1, 0);
-    std::vector<BatchRecCorner> all;
-    for (size_t w = 0; w < b->items.size(); w++) {
-        start[w] = (int)all.size();
-        if ((int)w < b->ntile_items) all.insert(all.end(), per[w].begin(), per[w].end());
-    }
-    start[b->items.size()] = (int)all.size();
-    for (void *q : {(void *)b->rc_start, (void *)b->rc}) {
+    for (void *q : {(void *)b->rec_cells, (void *)b->rec_ws}) {
         if (!q) continue;
         cudaFree(q);
         b->allocs.erase(std::find(b->allocs.begin(), b->allocs.end(), q));
     }
-    b->rc_start = nullptr;
-    b->rc = nullptr;
-    awe_status st = balloc(b, (void **)&b->rc_start, start.size() * sizeof(int));
-    if (st == AWE_OK) st = balloc(b, (void **)&b->rc, std::max<size_t>(all.size(), 1) * sizeof(BatchColCorner));
+    b->rec_cells = nullptr;
+    b->rec_ws = nullptr;
+    awe_status st = balloc(b, (void **)&b->rec_cells, std::max<size_t>(cells.size(), 1) * sizeof(BatchRecCell));
+    if (st == AWE_OK) st = balloc(b, (void **)&b->rec_ws, std::max<size_t>(ws.size(), 1) * sizeof(BatchRecW));
     if (st != AWE_OK) return st;
-    CUDA_TRY(cudaMemcpy(b->rc_start, start.data(), start.size() * sizeof(int), cudaMemcpyHostToDevice));
-    if (!all.empty())
-        CUDA_TRY(cudaMemcpy(b->rc, all.data(), all.size() * sizeof(BatchColCorner), cudaMemcpyHostToDevice));
-    b->rc_tile = b->tile;
+    if (!cells.empty()) {
+        CUDA_TRY(cudaMemcpy(b->rec_cells, cells.data(), cells.size() * sizeof(BatchRecCell), cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemcpy(b->rec_ws, ws.data(), ws.size() * sizeof(BatchRecW), cudaMemcpyHostToDevice));
+    }
+    b->nrec_cells = (int)cells.size();
     return AWE_OK;
 }
 
@@ -605,56 +596,6 @@ static awe_status grad_alloc(awe_batch *b, int T, int fmt) {
     return AWE_OK;
 }
 
-// receiver corners of every column item (chunk colL), sorted by column; the
-// corners of one cell keep the (receiver, corner) order of the tile lists
-static awe_status build_col_rec_corners(awe_batch *b) {
-    std::vector<int> start(b->ncol_items + 1, 0);
-    std::vector<BatchColCorner> all;
-    std::vector<int> first(b->shots.size());
-    int acc = 0;
-    for (size_t s = 0; s < b->shots.size(); s++) {
-        first[s] = acc;
-        acc += (b->shots[s].n2 + b->colL - 1) / b->colL;
-    }
-    std::vector<std::vector<BatchColCorner>> per(b->ncol_items);
-    for (size_t s = 0; s < b->shots.size(); s++) {
-        const BatchShot &sh = b->shots[s];
-        for (int r = 0; r < sh.nr; r++) {
-            const GeoPoint &g = b->h_rec[sh.rec0 + r];
-            for (int c = 0; c < 4; c++) {
-                const long long node = g.base + (c & 1) + (c >> 1) * (long long)b->n1;
-                const int x = (int)(node / b->n1), z = (int)(node % b->n1);
-                if (x < 0 || x >= sh.n2) continue;
-                per[first[s] + x / b->colL].push_back(BatchColCorner{x, z, r, g.w[c]});
-            }
-        }
-    }
-    for (int w = 0; w < b->ncol_items; w++) {
-        std::stable_sort(per[w].begin(), per[w].end(),
-                         [](const BatchColCorner &a, const BatchColCorner &c) { return a.x < c.x; });
-        start[w] = (int)all.size();
-        all.insert(all.end(), per[w].begin(), per[w].end());
-    }
-    start[b->ncol_items] = (int)all.size();
-    for (void *q : {(void *)b->col_cstart, (void *)b->col_rc}) {
-        if (!q) continue;
-        cudaFree(q);
-        b->allocs.erase(std::find(b->allocs.begin(), b->allocs.end(), q));
-    }
-    b->col_cstart = nullptr;
-    b->col_rc = nullptr;
-    awe_status st = balloc(b, (void **)&b->col_cstart, start.size() * sizeof(int));
-    if (st == AWE_OK) st = balloc(b, (void **)&b->col_rc, std::max<size_t>(all.size(), 1) * sizeof(BatchColCorner));
-    if (st != AWE_OK) return st;
-    CUDA_TRY(cudaMemcpy(b->col_cstart, start.data(), start.size() * sizeof(int), cudaMemcpyHostToDevice));
-    if (!all.empty())
-        CUDA_TRY(cudaMemcpy(b->col_rc, all.data(), all.size() * sizeof(BatchColCorner), cudaMemcpyHostToDevice));
-    b->col_rc_L = b->colL;
-    const int cpsm = batch2d_col_adj_ctas_per_sm(b->n1);
-    b->col_adj_grid = cpsm > 0 ? cpsm * b->sms : 0;
-    return AWE_OK;
-}
-
 static BatchAdj adj_params(const awe_batch *b, int it, const float *V) {
     BatchAdj p{};
     p.V = V;
@@ -672,8 +613,6 @@ static BatchAdj adj_params(const awe_batch *b, int it, const float *V) {
     p.src = b->src;
     p.wav = b->wav;
     p.it = it;
-    p.rc_start = b->rc_start;
-    p.rc = b->rc;
     p.res = b->res;
     p.row = (it % b->d.jdata == 0) ? it / b->d.jdata : -1;
     return p;
@@ -727,9 +666,10 @@ static awe_status grad_sequence(awe_batch *b, cudaStream_t s) {
             p.Y = Y;
             if (b->colL > 0 && b->col_adj_grid > 0)
                 launch_batch2d_col_adj(b->d_shots, b->d_col_items, b->ncol_items, b->col_adj_grid, b->colL, p,
-                                       b->col_cstart, b->col_rc, b->d_err, s);
+                                       b->d_err, s);
             else
                 launch_batch2d_adj(b->nop, b->tile, b->d_shots, b->d_items, b->ntile_items, b->grid, p, s);
+            launch_batch_rec_adj(b->rec_cells, b->nrec_cells, b->rec_ws, b->d_shots, p, s);
             std::swap(X, Y);
         }
     }
@@ -759,8 +699,11 @@ awe_status awe_batch_gradient(awe_batch *b, const float *wav, const float *dobs,
     int T = o.ckpt_every > 0 ? o.ckpt_every : (int)std::ceil(std::sqrt((double)b->d.nt));
     T = std::max(1, std::min(T, b->d.nt));
     awe_status st = grad_alloc(b, T, o.ckpt_format);
-    if (st == AWE_OK && b->rc_tile != b->tile) st = build_rec_corners(b);
-    if (st == AWE_OK && b->colL > 0 && b->col_rc_L != b->colL) st = build_col_rec_corners(b);
+    if (st == AWE_OK && b->nrec_cells < 0) st = build_rec_cells(b);
+    if (st == AWE_OK) {
+        const int cpsm = b->colL > 0 ? batch2d_col_adj_ctas_per_sm(b->n1) : 0;
+        b->col_adj_grid = cpsm > 0 ? cpsm * b->sms : 0;
+    }
     if (st != AWE_OK) return st;
     cudaStream_t s = b->stream;
     CUDA_TRY(cudaMemcpyAsync(b->wav, wav, (size_t)b->d.nt * sizeof(float), cudaMemcpyHostToDevice, s));

@@ -326,20 +326,6 @@ __global__ void __launch_bounds__(TZ / 4 * TX) k_batch2d_adj(const BatchShot *__
             if (in) ga[i] = gsum_add(ga[i], __fmul_rn(nu[i], lv4[i]));  // FP32 product, compensated sum
         }
         const long long cell0 = (long long)x * n1 + zb;
-        // receiver residuals (W R^T r, then the W of mu): corners listed per tile
-        if (p.row >= 0) {
-            const int a = p.rc_start[w], b = p.rc_start[w + 1];
-            for (int e = a; e < b; e++) {
-                const BatchRecCorner rc = p.rc[e];
-                const long long d = rc.node - cell0;
-#pragma unroll
-                for (int i = 0; i < 4; i++)
-                    if (d == i) {
-                        const float r = p.res[sh.dat_off + (long long)p.row * sh.nr + rc.r];
-                        mu[i] += wc[i] * (wc[i] * (rc.w * r));
-                    }
-            }
-        }
         // source term of the gradient (corners lie within n1 + 1 of the base index)
         if (sh.ns > 0) {
             const float dd = p.wav[p.it];
@@ -481,6 +467,26 @@ __global__ void k_residual_flat(const float *__restrict__ d, const float *__rest
 void launch_residual_flat(const float *d, const float *dobs, float *r, long long n, double *part, cudaStream_t s) {
     const int blocks = (int)((n + 1023) / 1024);
     if (blocks > 0) k_residual_flat<<<blocks, 256, 0, s>>>(d, dobs, r, n, part);
+}
+
+// receiver residuals of the adjoint step on mu = W lambda (W R^T r, then the
+// W of mu): mu += W (W (w r)) per corner, in (receiver, corner) order
+__global__ void k_batch_rec_adj(const BatchRecCell *__restrict__ cells, int ncells, const BatchRecW *__restrict__ ws,
+                                const BatchShot *__restrict__ shots, const BatchAdj p) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ncells) return;
+    const BatchRecCell c = cells[t];
+    const BatchShot sh = shots[c.shot];
+    const float wc = p.sponge ? p.wz[c.z] * p.wx[sh.wx_off + c.x] : 1.f;
+    const float *res = p.res + sh.dat_off + (long long)p.row * sh.nr;
+    float mu = p.Y[c.gi];
+    for (int e = c.e0; e < c.e1; e++) mu = __fmaf_rn(wc, __fmul_rn(wc, __fmul_rn(ws[e].w, res[ws[e].r])), mu);
+    p.Y[c.gi] = mu;
+}
+
+void launch_batch_rec_adj(const BatchRecCell *cells, int ncells, const BatchRecW *ws, const BatchShot *shots,
+                          const BatchAdj &p, cudaStream_t s) {
+    if (ncells > 0 && p.row >= 0) k_batch_rec_adj<<<(ncells + 127) / 128, 128, 0, s>>>(cells, ncells, ws, shots, p);
 }
 
 // model gradient: dJ/dvel2 * (-vel2^2 / dt^2), each shot's padded cells summed

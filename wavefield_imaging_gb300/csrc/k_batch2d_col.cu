@@ -242,8 +242,8 @@ __global__ void __launch_bounds__(512) k_batch2d_col(const BatchShot *__restrict
 // queues for the x neighbours.  For the output column (the centre) the
 // thread's nu_{k+1} (Y) and gradient-accumulator strips are loaded before the ring
 // wait; mu_k = W lambda goes back to Y and the gradient strip is updated and
-// stored.  Receiver corners of the item are listed by column; sources are
-// tested only near their columns.
+// stored (the receiver term follows in k_batch_rec_adj); sources are tested
+// only near their columns.
 constexpr int ARING = 8;
 constexpr int kAdjMaxN1 = 1024;  // 512 threads of two cells
 constexpr int YG_AHEAD = 3;      // output columns whose nu_{k+1} / gradient strips are in flight
@@ -257,8 +257,7 @@ __host__ __device__ inline int adj_off_g(int n1) { return 2 * n1 + (n1 + 8); }
 
 __global__ void __maxnreg__(96) k_batch2d_col_adj(const BatchShot *__restrict__ shots,
                                                          const int4 *__restrict__ items, int nitems,
-                                                         const BatchAdj p, int L, const int *__restrict__ cstart,
-                                                         const BatchColCorner *__restrict__ crc, int *err) {
+                                                         const BatchAdj p, int L, int *err) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int n1 = p.n1;
     const int SLOT = adj_slot(n1), OV = adj_off_v(n1), OG = adj_off_g(n1);
@@ -309,8 +308,6 @@ __global__ void __maxnreg__(96) k_batch2d_col_adj(const BatchShot *__restrict__ 
         };
         if (tid == 0)
             for (int s = 0; s < ARING && s < S; s++) issue(s);
-        int e = cstart[w];
-        const int eend = cstart[w + 1];
         int scol[4] = {-8, -8, -8, -8};
         const bool few = sh.ns <= 4;
         for (int k = 0; k < sh.ns && k < 4; k++) scol[k] = (int)(p.src[sh.src0 + k].base / n1);
@@ -407,19 +404,6 @@ __global__ void __maxnreg__(96) k_batch2d_col_adj(const BatchShot *__restrict__ 
                             mu[i] = wc[i] * lam;
                             if (in) ga[i] = gsum_add(ga[i], __fmul_rn(nu[i], lv[i]));  // FP32 product, compensated sum
                         }
-                        if (p.row >= 0) {  // receiver residuals of this column (corners in list order)
-                            for (int ee = e; ee < eend; ee++) {
-                                const BatchColCorner rc = crc[ee];
-                                if (rc.x != x) break;
-                                const int d = rc.z - zb;
-#pragma unroll
-                                for (int i = 0; i < 2; i++)
-                                    if (d == i) {
-                                        const float r = p.res[sh.dat_off + (long long)p.row * sh.nr + rc.r];
-                                        mu[i] += wc[i] * (wc[i] * (rc.w * r));
-                                    }
-                            }
-                        }
                         bool near = !few;
 #pragma unroll
                         for (int k = 0; k < 4; k++) near = near || (unsigned)(x - scol[k]) <= 2u;
@@ -439,9 +423,6 @@ __global__ void __maxnreg__(96) k_batch2d_col_adj(const BatchShot *__restrict__ 
                         }
                         *reinterpret_cast<float2 *>(p.Y + gi) = make_float2(mu[0], mu[1]);
                         __stcs(reinterpret_cast<float4 *>(p.G + gi), make_float4(ga[0].x, ga[0].y, ga[1].x, ga[1].y));
-                    }
-                    if (s >= 2 * CNOP) {  // the corners of this output column are done
-                        while (e < eend && crc[e].x == x) e++;
                     }
                     if (__syncthreads_or(bad)) {
                         cp_async_wait<0>();
@@ -490,11 +471,10 @@ int batch2d_col_adj_ctas_per_sm(int n1) {
 }
 
 void launch_batch2d_col_adj(const BatchShot *shots, const int4 *items, int nitems, int grid, int L,
-                            const BatchAdj &p, const int *cstart, const BatchColCorner *crc, int *err,
+                            const BatchAdj &p, int *err,
                             cudaStream_t s) {
     if (p.n1 > kAdjMaxN1 || grid < 1) return;
-    k_batch2d_col_adj<<<grid, adj_threads(p.n1), batch2d_col_adj_smem(p.n1), s>>>(shots, items, nitems, p, L, cstart,
-                                                                                    crc, err);
+    k_batch2d_col_adj<<<grid, adj_threads(p.n1), batch2d_col_adj_smem(p.n1), s>>>(shots, items, nitems, p, L, err);
 }
 
 int batch2d_col_shape(int nop, int n1, size_t *smem) {
