@@ -157,7 +157,7 @@ static void fstep(const fctx *c, const double *A, const double *B, double *Vn, d
 /* round x / scale to `bits` significant bits (round half to even), times
  * scale.  bits == 11 follows IEEE half precision below its normal range
  * (|x / scale| < 2^-14: a fixed spacing of 2^-24, gradual underflow) */
-static double quantize(double x, double scale, int bits) {
+double orc_quantize(double x, double scale, int bits) {
     if (x == 0 || scale == 0) return x;
     const double y = x / scale;
     if (bits == 11 && fabs(y) < ldexp(1.0, -14)) return ldexp(nearbyint(ldexp(y, 24)), -24) * scale;
@@ -172,7 +172,7 @@ static double quantize(double x, double scale, int bits) {
  * consecutive cells s = max|v| / 32767, q = round(v * (1/s)) (half to even,
  * clamped to +-32767), v' = q * s, all in float; blocks with max|v| <= 1e-30
  * are stored as zeros. */
-static void quantize_bfp16(double *u, size_t n) {
+void orc_quantize_bfp16(double *u, size_t n) {
     for (size_t b = 0; b < n; b += 64) {
         const size_t e = b + 64 < n ? b + 64 : n;
         float m = 0.f;
@@ -353,11 +353,11 @@ static int grad_impl(const orc_par *p, int ndim, int jdata, const float *vel_in,
                 if (lv < 0) continue;
                 double *u = V + (size_t)lv * np, amax = 0;
                 if (ckpt_bits < 0) {
-                    quantize_bfp16(u, np);
+                    orc_quantize_bfp16(u, np);
                     continue;
                 }
                 for (size_t i = 0; i < np; i++) amax = fabs(u[i]) > amax ? fabs(u[i]) : amax;
-                for (size_t i = 0; i < np; i++) u[i] = quantize(u[i], amax, ckpt_bits);
+                for (size_t i = 0; i < np; i++) u[i] = orc_quantize(u[i], amax, ckpt_bits);
             }
             for (int k = k0; k < k0 + ckpt_every - 1 && k < nt - 1; k++) {
                 const double *B = V + (size_t)k * np, *A = k > 0 ? V + (size_t)(k - 1) * np : zero;

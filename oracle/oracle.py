@@ -32,11 +32,12 @@ def build(with_reference: bool = True) -> None:
         ):
             subprocess.check_call(["gcc", *CFLAGS, *extra, *srcs, "-o", out, "-lm"])
     # FP64 adjoint of the CPU-program scheme (includes awe_oracle.c)
-    adj = os.path.join(HERE, "awe_adjoint.c")
+    # and of the spherical GPU-program scheme (awe_adjoint_sph.c, includes awe_oracle_gpu.c)
+    adj = [os.path.join(HERE, "awe_adjoint.c"), os.path.join(HERE, "awe_adjoint_sph.c")]
     out = os.path.join(BUILD, "liboracle_adj.so")
-    deps = [adj, os.path.join(HERE, "awe_oracle.c"), os.path.join(HERE, "awe_oracle.h")]
+    deps = adj + [os.path.join(HERE, x) for x in ("awe_oracle.c", "awe_oracle_gpu.c", "awe_oracle.h")]
     if not os.path.exists(out) or os.path.getmtime(out) < max(os.path.getmtime(x) for x in deps):
-        subprocess.check_call(["gcc", *CFLAGS, adj, "-o", out, "-lm"])
+        subprocess.check_call(["gcc", *CFLAGS, *adj, "-o", out, "-lm"])
     if with_reference and os.path.isdir(REF_SRC):
         subprocess.check_call(
             ["make", "-s", "-C", os.path.join(HERE, "ref"), "REF=" + REF_SRC, "OUT=" + REF_OUT],
@@ -331,6 +332,9 @@ def _adj_lib():
         L.orc_grad_ckpt.restype = C.c_int
         L.orc_image.argtypes = [C.POINTER(Par), C.c_int, C.c_int, fp, fp, C.c_int, fp, C.c_int, fp, fp, C.c_int, dp]
         L.orc_image.restype = C.c_int
+        L.orc_gpu_spher3d_grad.argtypes = [C.POINTER(GPar), fp, dp, fp, C.c_int, fp, C.c_int, fp, fp, C.c_int,
+                                           C.c_int, dp, dp, dp]
+        L.orc_gpu_spher3d_grad.restype = C.c_int
         _adj = L
     return _adj
 
@@ -395,6 +399,48 @@ def rtm_image(p: dict, vel, wav, sou, rec, data, condition: int, jdata: int = 1)
     if rc != 0:
         raise ValueError("orc_image rejected the parameters")
     return img
+
+
+def _gpar_spher(p: dict) -> GPar:
+    q = GPar()
+    q.n1, q.n2, q.n3 = p["n"]
+    q.d1, q.d2, q.d3 = p["d"]
+    q.o1, q.o2, q.o3 = p["o"]
+    q.nb, q.nt, q.dt = p["nb"], p["nt"], p["dt"]
+    q.jdata, q.jsnap, q.bnds = 1, 0, 0
+    q.fsrf, q.expl, q.refl = int(p.get("fsrf", 0)), int(p.get("expl", 0)), 0
+    return q
+
+
+def spher3d_gradient(p: dict, vel, wav, sou, rec, dobs, m=None, ckpt_every: int = 0, ckpt_bits: int = 0):
+    """FP64 misfit J = 0.5 sum (d - dobs)^2 of the spherical GPU-program
+    scheme and its gradient with respect to m = 1/v^2 (the discrete adjoint
+    of that scheme, awe_adjoint_sph.c).  The model is `vel` (float32) or,
+    when `m` is given, slowness squared in float64.  ckpt_bits != 0 emulates
+    checkpointed recompute every ckpt_every steps from levels rounded as the
+    engine's checkpoint format (8 BF16, 11 FP16, -1 block floating point).
+    Returns (grad [nph][nth][nr] float64, J, dsyn [nt][nrec] float64)."""
+    q = _gpar_spher(p)
+    vel = np.ascontiguousarray(vel, np.float32)
+    wav = np.ascontiguousarray(wav, np.float32)
+    sou = np.ascontiguousarray(sou, np.float32).reshape(-1, 3)
+    rec = np.ascontiguousarray(rec, np.float32).reshape(-1, 3)
+    nr = rec.shape[0]
+    dobs = np.ascontiguousarray(dobs, np.float32).reshape(q.nt, nr)
+    grad = np.zeros(vel.shape, np.float64)
+    dsyn = np.zeros((q.nt, nr), np.float64)
+    J = C.c_double()
+    dp = C.POINTER(C.c_double)
+    mp = None
+    if m is not None:
+        m = np.ascontiguousarray(m, np.float64).reshape(vel.shape)
+        mp = m.ctypes.data_as(dp)
+    rc = _adj_lib().orc_gpu_spher3d_grad(C.byref(q), _fp(vel), mp, _fp(wav), sou.shape[0], _fp(sou), nr, _fp(rec),
+                                         _fp(dobs), ckpt_every, ckpt_bits, grad.ctypes.data_as(dp), C.byref(J),
+                                         dsyn.ctypes.data_as(dp))
+    if rc != 0:
+        raise ValueError("orc_gpu_spher3d_grad rejected the parameters")
+    return grad, J.value, dsyn
 
 
 def spher3d_fp64(p: dict, vel, wav, sou, rec):

@@ -90,3 +90,34 @@ def tapered_direction(shape, rng, margin=3):
             idx[ax] = -1 - k
             dm[tuple(idx)] = 0
     return dm
+
+
+def spher_grad_case(fsrf=0, nt=150, seed=3, n=(45, 20, 20), nb=8):
+    """A small seeded gradient problem of the spherical GPU-program scheme:
+    the c4 spacing (5 m in r, 0.04/512 rad in theta and phi) on a (r, theta,
+    phi) = n grid near r = 3388 km, ice over basalt with 2 % noise, one
+    source and 7 receivers above it, close to the free surface.  Returns
+    (par, vel, wav, sou, rec, vtrue); models are [nphi][ntheta][nr]."""
+    rng = np.random.default_rng(seed)
+    d = (0.005, 0.04 / 512, 0.04 / 512)
+    o = (3388.0, np.pi / 2 - 10 * d[1], -10 * d[2])
+    r = o[0] + np.arange(n[0]) * d[0]
+    vel = np.full((n[2], n[1], n[0]), 0.168, np.float32)
+    vel[:, :, r > o[0] + 0.15] = 0.110
+    vel *= (1 + 0.02 * rng.standard_normal(vel.shape)).astype(np.float32)
+    vtrue = vel.copy()
+    vtrue[:, :, 20:30] *= np.float32(1.05)
+    par = dict(n=list(n), d=list(d), o=list(o), nb=nb, nt=nt, dt=0.005, fsrf=fsrf, expl=0)
+    th0, ph0 = o[1] + 9.5 * d[1], o[2] + 9.5 * d[2]
+    sou = np.array([[o[0] + 0.17, ph0, th0]], np.float32)
+    rec = np.array([[o[0] + 0.12 + 0.012 * k, ph0 + (k - 3) * d[2], th0 + (k % 3 - 1) * d[1]] for k in range(7)],
+                   np.float32)
+    return par, vel, ricker(nt, 0.005), sou, rec, vtrue
+
+
+def spher_desc(par, precision=0):
+    import wavefield_imaging_gb300 as awe
+
+    return awe.make_desc(3, par["n"], par["d"], par["o"], par["nt"], par["dt"], coords=awe.SPHER,
+                         scheme=awe.SCHEME_GPU, nb=par["nb"], fsrf=par.get("fsrf", 0), expl=par.get("expl", 0),
+                         precision=precision)

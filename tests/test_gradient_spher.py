@@ -1,0 +1,112 @@
+"""Misfit gradient of the spherical GPU-program scheme (sfAWEFDspher3Dgpu's
+step, the c4 configuration's scheme) on the engine's discrete adjoint,
+against the FP64 adjoint oracle (oracle/awe_adjoint_sph.c), which is pinned
+by finite differences of its own FP64 misfit."""
+import numpy as np
+import pytest
+
+from helpers import rel_l2, spher_desc, spher_grad_case
+
+
+def _dobs(par, vtrue, wav, sou, rec):
+    from oracle import oracle
+
+    _, _, d = oracle.spher3d_gradient(par, vtrue, wav, sou, rec, np.zeros((par["nt"], rec.shape[0])))
+    return d.astype(np.float32)
+
+
+@pytest.mark.parametrize("fsrf", [0, 1])
+def test_oracle_gradient_matches_finite_differences(fsrf):
+    """Centred differences of the FP64 misfit in m = 1/v^2 (double model
+    path), Richardson-extrapolated over steps 1e-3 and 5e-4, along 3 seeded
+    directions."""
+    from oracle import oracle
+
+    par, vel, wav, sou, rec, vtrue = spher_grad_case(fsrf=fsrf)
+    dobs = _dobs(par, vtrue, wav, sou, rec)
+    m = 1.0 / vel.astype(np.float64) ** 2
+    g, J, _ = oracle.spher3d_gradient(par, vel, wav, sou, rec, dobs, m=m)
+    assert J > 0
+    rng = np.random.default_rng(5)
+    for _ in range(3):
+        dm = rng.standard_normal(m.shape) * m
+        fd = []
+        for h in (1e-3, 5e-4):
+            jp = oracle.spher3d_gradient(par, vel, wav, sou, rec, dobs, m=m + h * dm)[1]
+            jm = oracle.spher3d_gradient(par, vel, wav, sou, rec, dobs, m=m - h * dm)[1]
+            fd.append((jp - jm) / (2 * h))
+        rich = (4 * fd[1] - fd[0]) / 3
+        assert abs(float(np.sum(g * dm)) - rich) <= 1e-7 * abs(rich)
+
+
+def test_oracle_checkpoint_emulation_fp32_is_exact():
+    """Rounding the checkpoints to 24 bits (FP32) changes the FP64 oracle
+    gradient by no more than float rounding of the restart levels."""
+    from oracle import oracle
+
+    par, vel, wav, sou, rec, vtrue = spher_grad_case()
+    dobs = _dobs(par, vtrue, wav, sou, rec)
+    g, J, _ = oracle.spher3d_gradient(par, vel, wav, sou, rec, dobs)
+    g24, J24, _ = oracle.spher3d_gradient(par, vel, wav, sou, rec, dobs, ckpt_every=13, ckpt_bits=24)
+    assert J24 == J
+    assert rel_l2(g24, g) <= 1e-6
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fsrf", [0, 1])
+def test_gradient_matches_fp64_oracle(fsrf):
+    import wavefield_imaging_gb300 as awe
+    from oracle import oracle
+
+    par, vel, wav, sou, rec, vtrue = spher_grad_case(fsrf=fsrf)
+    dobs = _dobs(par, vtrue, wav, sou, rec)
+    gref, Jref, dref = oracle.spher3d_gradient(par, vel, wav, sou, rec, dobs)
+    T = int(np.ceil(np.sqrt(par["nt"])))
+    with awe.Plan(spher_desc(par)) as p:
+        p.set_model(vel)
+        p.set_geometry(sou, rec)
+        g32, J32, d32 = p.gradient(wav, dobs, ckpt_format=awe.CKPT_FP32, return_dsyn=True)
+        gf, Jf = p.gradient(wav, dobs, ckpt_format=awe.CKPT_BFP16)
+        gb, Jb = p.gradient(wav, dobs, ckpt_format=awe.CKPT_BF16)
+    assert rel_l2(d32, dref) <= 1e-5
+    # the residual is a small difference of close trace sets (the true model
+    # differs by 5 % in one layer), so the FP32 trace error weighs more in J
+    assert abs(J32 - Jref) <= 2e-4 * abs(Jref)
+    assert Jf == J32 and Jb == J32  # the misfit comes from the forward pass
+    assert rel_l2(g32, gref) <= 1e-4
+    # 16-bit checkpoints: the oracle emulates the same rounding in FP64
+    for g16, bits, bound in ((gf, -1, 1e-3), (gb, 8, 3e-2)):
+        gq, _, _ = oracle.spher3d_gradient(par, vel, wav, sou, rec, dobs, ckpt_every=T, ckpt_bits=bits)
+        assert rel_l2(g16, gq) <= 0.5 * rel_l2(gq, gref) + 1e-4
+        assert rel_l2(g16, gref) <= bound
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("every", [1, 7, 1000])
+def test_checkpoint_interval_does_not_change_fp32_gradient(every):
+    import wavefield_imaging_gb300 as awe
+
+    par, vel, wav, sou, rec, vtrue = spher_grad_case(nt=60)
+    dobs = _dobs(par, vtrue, wav, sou, rec)
+    with awe.Plan(spher_desc(par)) as p:
+        p.set_model(vel)
+        p.set_geometry(sou, rec)
+        ref, Jr = p.gradient(wav, dobs, ckpt_every=0, ckpt_format=awe.CKPT_FP32)
+        g, J = p.gradient(wav, dobs, ckpt_every=every, ckpt_format=awe.CKPT_FP32)
+    assert J == Jr
+    # the recompute repeats the forward exactly; only the order of coincident
+    # receiver-corner atomics may differ
+    assert rel_l2(g, ref) <= 1e-6
+
+
+@pytest.mark.gpu
+def test_reflectivity_injection_is_refused():
+    import wavefield_imaging_gb300 as awe
+
+    par, vel, wav, sou, rec, vtrue = spher_grad_case(nt=20)
+    par["expl"] = 1
+    with awe.Plan(spher_desc(par)) as p:
+        p.set_model(vel)
+        p.set_geometry(sou, rec)
+        with pytest.raises(awe.AweError):
+            p.gradient(wav, np.zeros((par["nt"], rec.shape[0]), np.float32))

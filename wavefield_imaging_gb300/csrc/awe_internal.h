@@ -123,9 +123,19 @@ struct StepAParams {
     int nshot;                           // shots advanced together (spherical 3D, AWE_FAST), fields back to back
     long long shot_cells;                // cells of one shot's field
 };
+// out of place (the spherical AWE_FAST march kernels): prv the previous level, out the new one
+bool stepA_out_of_place(int geom, bool exact);
+void launch_stepA_oop(int geom, bool exact, const float *cur, const float *prv, float *out, const float *vel,
+                      const StepAParams &p, cudaStream_t s);
 void launch_stepA(int geom, bool exact, const float *cur, float *nxt, const float *vel, const StepAParams &p,
                   cudaStream_t s);
 void launch_bcA(bool exact, const float *um, float *uo, float *aux, const StepAParams &p, cudaStream_t s);
+// adjoint of the spherical step (AWE_FAST): Y <- W M (L^T(I c X) + 2 X - W Y),
+// G += X L(A) on the interior (A null: none); receivers z += W M (w r)
+void launch_adjA_sph(const float *X, float *Y, const float *A, const float *vel, float2 *G, const StepAParams &p,
+                     cudaStream_t s);
+void launch_rec_adjA(float *z, const GeoPoint *pts, int nr, const float *r, const StepAParams &p, const long long *off,
+                     cudaStream_t s);
 void launch_injectA(bool exact, int ndim, float *u, const GeoPoint *pts, const float *scale, int ns, const float *wav,
                     int it, bool scaled, const long long *off, cudaStream_t s, int stride = 1);
 void launch_snapshot_transpose2(const float *u, float *dst, const Grid &g, int f1, int f2, int m1, int m2,
@@ -159,8 +169,9 @@ void launch_ckpt_store_bfp(const float *u, long long n, short *q, float *scale, 
 void launch_ckpt_load_bfp(const short *q, const float *scale, long long n, float *u, int grid, cudaStream_t s);
 // image on the model grid: the padded grid's model window of G
 void launch_image_cut(const float2 *G, const Grid &g, int nb, const int *n, int nd, double *out, cudaStream_t s);
+// vel2: v^2 dt^2 per padded cell, or the velocity itself (raw_v: c = dt^2 v^2)
 void launch_grad_fold(const float2 *G, const float *vel2, float dt, const Grid &g, int nb, const int *n, int nd,
-                      double *out, cudaStream_t s);
+                      double *out, cudaStream_t s, bool raw_v = false);
 
 // ---- batched 2D forward (k_batch2d.cu) ----
 struct BatchShot {

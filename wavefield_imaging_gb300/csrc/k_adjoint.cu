@@ -472,8 +472,15 @@ __device__ __forceinline__ int edge_axes(int j1, int j2, int j3, int m1, int m2,
 // skip_big: model cells on two or more edge axes (the model's edges and
 // corners, whose replicas span (nb+1)^2 or (nb+1)^3 padded cells) are left
 // to k_grad_fold_big
+// vel2 holds c = v^2 dt^2 per padded cell, or (cscale > 0) the velocity v with c = cscale v^2
+__device__ __forceinline__ double fold_c(const float *vel2, long long i, double cscale) {
+    const double v = vel2[i];
+    return cscale > 0 ? cscale * v * v : v;
+}
+
 __global__ void k_grad_fold(const float2 *__restrict__ G, const float *__restrict__ vel2, double inv_dt2, Grid g,
-                            int nb, int m1, int m2, int m3, int nd, double *__restrict__ out, int skip_big) {
+                            int nb, int m1, int m2, int m3, int nd, double *__restrict__ out, int skip_big,
+                            double cscale) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)m1 * m2 * m3) return;
     const int j1 = (int)(t % m1), j2 = (int)((t / m1) % m2), j3 = (int)(t / ((long long)m1 * m2));
@@ -488,7 +495,7 @@ __global__ void k_grad_fold(const float2 *__restrict__ G, const float *__restric
         for (int i2 = a2; i2 <= b2; i2++)
             for (int i1 = a1; i1 <= b1; i1++) {
                 const long long i = ((long long)i3 * g.n2 + i2) * g.n1 + i1;
-                const double v2 = vel2[i];
+                const double v2 = fold_c(vel2, i, cscale);
                 acc += gsum_value(G[i]) * (-v2 * v2 * inv_dt2);
             }
     out[t] = acc;
@@ -511,7 +518,7 @@ void launch_image_cut(const float2 *G, const Grid &g, int nb, const int *n, int 
 // the 4 edges along each axis (corners counted with the axis-1 edges).
 __global__ void __launch_bounds__(256) k_grad_fold_big(const float2 *__restrict__ G, const float *__restrict__ vel2,
                                                        double inv_dt2, Grid g, int nb, int m1, int m2, int m3, int nd,
-                                                       double *__restrict__ out) {
+                                                       double *__restrict__ out, double cscale) {
     long long b = blockIdx.x;
     int j1, j2, j3 = 0;
     if (nd == 2) {
@@ -543,7 +550,7 @@ __global__ void __launch_bounds__(256) k_grad_fold_big(const float2 *__restrict_
     for (long long k = threadIdx.x; k < vol; k += blockDim.x) {
         const long long i1 = a1 + k % w1, i2 = a2 + (k / w1) % w2, i3 = a3 + k / (w1 * w2);
         const long long i = (i3 * g.n2 + i2) * g.n1 + i1;
-        const double v2 = vel2[i];
+        const double v2 = fold_c(vel2, i, cscale);
         acc += gsum_value(G[i]) * (-v2 * v2 * inv_dt2);
     }
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -558,16 +565,18 @@ __global__ void __launch_bounds__(256) k_grad_fold_big(const float2 *__restrict_
 }
 
 void launch_grad_fold(const float2 *G, const float *vel2, float dt, const Grid &g, int nb, const int *n, int nd,
-                      double *out, cudaStream_t s) {
+                      double *out, cudaStream_t s, bool raw_v) {
+    const double cscale = raw_v ? (double)dt * (double)dt : 0.0;
     const int m1 = n[0], m2 = n[1], m3 = nd == 3 ? n[2] : 1;
     const long long m = (long long)m1 * m2 * m3;
     const double inv = 1.0 / ((double)dt * (double)dt);
     // edges and corners go to one block each when every model axis has an interior
     const bool split = m1 >= 3 && m2 >= 3 && (nd == 2 || m3 >= 3);
-    k_grad_fold<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(G, vel2, inv, g, nb, m1, m2, m3, nd, out, split ? 1 : 0);
+    k_grad_fold<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(G, vel2, inv, g, nb, m1, m2, m3, nd, out, split ? 1 : 0,
+                                                            cscale);
     if (split) {
         const long long nbig = nd == 2 ? 4 : 4LL * (m1 + m2 - 2 + m3 - 2);
-        k_grad_fold_big<<<(unsigned)nbig, 256, 0, s>>>(G, vel2, inv, g, nb, m1, m2, m3, nd, out);
+        k_grad_fold_big<<<(unsigned)nbig, 256, 0, s>>>(G, vel2, inv, g, nb, m1, m2, m3, nd, out, cscale);
     }
 }
 

@@ -18,6 +18,7 @@
 
 #include "awe_internal.h"
 #include "fp_exact.cuh"
+#include "gsum.cuh"
 
 namespace awe {
 
@@ -158,7 +159,8 @@ __global__ void __launch_bounds__(256) k_stepA(const float *__restrict__ cur, fl
 // with fused multiply-adds and reciprocal multiplies.
 constexpr int kSphChunk = 16;
 
-__global__ void __launch_bounds__(256) k_stepA_sph_march(const float *__restrict__ cur, float *__restrict__ nxt,
+// prv: the previous level (the same buffer as nxt for the in-place step)
+__global__ void __launch_bounds__(256) k_stepA_sph_march(const float *__restrict__ cur, const float *prv, float *nxt,
                                                          const float *__restrict__ vel, const StepAParams p) {
     const int i1 = blockIdx.x * blockDim.x + threadIdx.x;
     const int i2 = blockIdx.y * blockDim.y + threadIdx.y;
@@ -178,7 +180,7 @@ __global__ void __launch_bounds__(256) k_stepA_sph_march(const float *__restrict
         const float up = i3 + 1 < g.n3 ? cur[i + s3] : 0.f;
         const int c[3] = {i1, i2, i3};
         const int si = sponge_index(c, n, p);
-        const float q = damp_a<false>(nxt[i], si, p.dtab, p.ftab);
+        const float q = damp_a<false>(prv[i], si, p.dtab, p.ftab);
         float lap = 0.f;
         if (in12 && i3 >= 4 && i3 < g.n3 - 4) {
             const float u2 = uc + uc;
@@ -232,7 +234,7 @@ __device__ __forceinline__ int sponge_index3(int c0, int c1, int c2, int n0, int
 
 // The same march with two consecutive radii per thread (n1 even): 8-byte
 // loads and packed FP32x2 arithmetic (fma.rn.f32x2 / add.f32x2 / mul.f32x2).
-__global__ void __launch_bounds__(256) k_stepA_sph_march2(const float *__restrict__ cur, float *__restrict__ nxt,
+__global__ void __launch_bounds__(256) k_stepA_sph_march2(const float *__restrict__ cur, const float *prv, float *nxt,
                                                           const float *__restrict__ vel, const StepAParams p) {
     // (the shot offset below is applied to cur and nxt, never to the shared model)
     const int i1 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
@@ -244,6 +246,7 @@ __global__ void __launch_bounds__(256) k_stepA_sph_march2(const float *__restric
     const int nchunk = (g.n3 + kSphChunk - 1) / kSphChunk;
     const int shot = blockIdx.z / nchunk;
     cur += shot * p.shot_cells;
+    prv += shot * p.shot_cells;
     nxt += shot * p.shot_cells;
     const int p0 = (blockIdx.z % nchunk) * kSphChunk, p1 = min(p0 + kSphChunk, g.n3);
     const bool th_in = i2 >= 4 && i2 < g.n2 - 4;
@@ -261,7 +264,7 @@ __global__ void __launch_bounds__(256) k_stepA_sph_march2(const float *__restric
     for (int i3 = p0; i3 < p1; i3++) {
         const long long i = base + i3 * s3;
         const float2 up = i3 + 1 < g.n3 ? ld2(i + s3) : make_float2(0.f, 0.f);
-        const float2 pv = *reinterpret_cast<const float2 *>(nxt + i);
+        const float2 pv = *reinterpret_cast<const float2 *>(prv + i);
         const float2 vv = *reinterpret_cast<const float2 *>(vel + i);
         float2 lap = make_float2(0.f, 0.f);
         const bool ph_in = i3 >= 4 && i3 < g.n3 - 4;
@@ -300,16 +303,17 @@ __global__ void __launch_bounds__(256) k_stepA_sph_march2(const float *__restric
 }
 
 template <bool EXACT>
-static void step_geom(int geom, const float *cur, float *nxt, const float *vel, const StepAParams &p, cudaStream_t s) {
+static void step_geom(int geom, const float *cur, const float *prv, float *nxt, const float *vel, const StepAParams &p,
+                      cudaStream_t s) {
     dim3 block(64, 4, 1), grid((p.g.n1 + 63) / 64, (p.g.n2 + 3) / 4, p.g.n3);
     if (!EXACT && geom == 3) {
         if (p.g.n1 % 2 == 0) {
             const int nchunk = (p.g.n3 + kSphChunk - 1) / kSphChunk;
             dim3 b2(32, 8, 1), g2((p.g.n1 / 2 + 31) / 32, (p.g.n2 + 7) / 8, nchunk * (p.nshot > 0 ? p.nshot : 1));
-            k_stepA_sph_march2<<<g2, b2, 0, s>>>(cur, nxt, vel, p);
+            k_stepA_sph_march2<<<g2, b2, 0, s>>>(cur, prv, nxt, vel, p);
         } else {
             dim3 mg((p.g.n1 + 63) / 64, (p.g.n2 + 3) / 4, (p.g.n3 + kSphChunk - 1) / kSphChunk);
-            k_stepA_sph_march<<<mg, block, 0, s>>>(cur, nxt, vel, p);
+            k_stepA_sph_march<<<mg, block, 0, s>>>(cur, prv, nxt, vel, p);
         }
         return;
     }
@@ -323,8 +327,15 @@ static void step_geom(int geom, const float *cur, float *nxt, const float *vel, 
 
 void launch_stepA(int geom, bool exact, const float *cur, float *nxt, const float *vel, const StepAParams &p,
                   cudaStream_t s) {
-    if (exact) step_geom<true>(geom, cur, nxt, vel, p, s);
-    else step_geom<false>(geom, cur, nxt, vel, p, s);
+    if (exact) step_geom<true>(geom, cur, nxt, nxt, vel, p, s);
+    else step_geom<false>(geom, cur, nxt, nxt, vel, p, s);
+}
+
+bool stepA_out_of_place(int geom, bool exact) { return geom == 3 && !exact; }
+
+void launch_stepA_oop(int geom, bool exact, const float *cur, const float *prv, float *out, const float *vel,
+                      const StepAParams &p, cudaStream_t s) {
+    if (stepA_out_of_place(geom, exact)) step_geom<false>(geom, cur, prv, out, vel, p, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -468,6 +479,125 @@ void launch_snapshot_transpose2(const float *u, float *dst, const Grid &g, int f
                                 cudaStream_t s) {
     const long long n = (long long)m1 * m2;
     k_snapshot_transpose2<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(u, dst, g, f1, f2, m1, m2);
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint of the spherical step (AWE_FAST).  The forward map of one step is
+//   U_{k+1} = W M (c L A_k + 2 A_k - W A_{k-1}),   c = dt^2 v^2,
+// A_k the current level after the injection, L the metric Laplacian on the
+// interior (zero in the 4-cell ring), W the sponge factor, M the free-surface
+// mask.  Its transpose, with X = z_{j+1} and Y = z_{j+2}:
+//   Y <- z_j = W M (L^T (I c X) + 2 X - W Y)
+//   G += X L(A_j) on the interior (A == nullptr: no gradient term).
+// L is not symmetric: each neighbour n of the cell contributes I c X at n
+// times the weight of this cell in n's stencil, so the r neighbours use their
+// own 2/r and the theta neighbours their own cos/(r^2 sin).  One thread per
+// (r, theta) column marching a chunk of phi; the phi neighbours of I c X and
+// of A stay in registers.
+__global__ void __launch_bounds__(256) k_adjA_sph(const float *__restrict__ X, float *__restrict__ Y,
+                                                  const float *__restrict__ A, const float *__restrict__ vel,
+                                                  float2 *__restrict__ G, const StepAParams p) {
+    const int i1 = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i2 = blockIdx.y * blockDim.y + threadIdx.y;
+    const Grid g = p.g;
+    if (i1 >= g.n1 || i2 >= g.n2) return;
+    const long long s2 = g.n1, s3 = (long long)g.n1 * g.n2;
+    const int p0 = blockIdx.z * kSphChunk, p1 = min(p0 + kSphChunk, g.n3);
+    auto rin = [&](int r) { return r >= 4 && r < g.n1 - 4; };
+    auto tin = [&](int t) { return t >= 4 && t < g.n2 - 4; };
+    auto pin = [&](int f) { return f >= 4 && f < g.n3 - 4; };
+    const bool c_in = rin(i1) && tin(i2);
+    const bool rm_in = rin(i1 - 1) && tin(i2), rp_in = rin(i1 + 1) && tin(i2);
+    const bool tm_in = rin(i1) && tin(i2 - 1), tp_in = rin(i1) && tin(i2 + 1);
+    const long long t = (long long)i2 * g.n1 + i1;
+    const float rd0 = p.rd[0], rd1 = p.rd[1], rd2 = p.rd[2], rd3 = p.rd[3], rd4 = p.rd[4];
+    const float A2 = __ldg(p.tr0 + i1), Cr = __ldg(p.tr1 + i1), B = __ldg(p.tt0 + t), D = __ldg(p.tt1 + t);
+    // this cell's weight in each neighbour's stencil (0 where the neighbour has no stencil)
+    const float w_rm = rm_in ? fmaf(__ldg(p.tr0 + i1 - 1), rd0, rd1) : 0.f;
+    const float w_rp = rp_in ? fmaf(-__ldg(p.tr0 + i1 + 1), rd0, rd1) : 0.f;
+    const float w_tm = tm_in ? fmaf(__ldg(p.tt0 + t - s2), rd2, Cr * rd3) : 0.f;
+    const float w_tp = tp_in ? fmaf(-__ldg(p.tt0 + t + s2), rd2, Cr * rd3) : 0.f;
+    const float w_c = -2.f * (rd1 + Cr * rd3 + D * rd4), w_ph = D * rd4;
+    const float dt2 = p.dt2;
+    auto ycx = [&](long long j) {  // c X at cell j
+        const float v = __ldg(vel + j);
+        return (dt2 * (v * v)) * X[j];
+    };
+    const long long base = (long long)i2 * s2 + i1;
+    // phi - 1 and phi of I c X and A for the column
+    float ym = (p0 > 0 && c_in && pin(p0 - 1)) ? ycx(base + (p0 - 1) * s3) : 0.f;
+    float yc = (c_in && pin(p0)) ? ycx(base + p0 * s3) : 0.f;
+    float am = 0.f, ac = 0.f;
+    if (A) {
+        am = p0 > 0 ? A[base + (p0 - 1) * s3] : 0.f;
+        ac = A[base + p0 * s3];
+    }
+    for (int i3 = p0; i3 < p1; i3++) {
+        const long long i = base + i3 * s3;
+        const bool ph = pin(i3);
+        const float yp = (i3 + 1 < g.n3 && c_in && pin(i3 + 1)) ? ycx(i + s3) : 0.f;
+        const float ap = (A && i3 + 1 < g.n3) ? A[i + s3] : 0.f;
+        float lt = w_ph * (ym + yp);
+        if (ph) {
+            lt = fmaf(w_c, yc, lt);
+            if (rm_in) lt = fmaf(w_rm, ycx(i - 1), lt);
+            if (rp_in) lt = fmaf(w_rp, ycx(i + 1), lt);
+            if (tm_in) lt = fmaf(w_tm, ycx(i - s2), lt);
+            if (tp_in) lt = fmaf(w_tp, ycx(i + s2), lt);
+        }
+        const float xc = X[i];
+        const int si = sponge_index3(i1, i2, i3, g.n1, g.n2, g.n3, p);
+        const float yv = Y[i];
+        float mu = fmaf(-damp_a<false>(1.f, si, p.dtab, p.ftab), yv, fmaf(2.f, xc, lt));
+        if (p.mask == 3 && (i1 > g.n1 - p.nb || (i1 < p.spill && (i2 >= 1 || i3 >= 1)))) mu = 0.f;
+        Y[i] = damp_a<false>(mu, si, p.dtab, p.ftab);
+        if (A && c_in && ph) {  // the forward's Laplacian of A at this cell
+            const float u2 = ac + ac;
+            const float rm = A[i - 1], rp = A[i + 1], tm = A[i - s2], tp = A[i + s2];
+            const float pra = (rp - rm) * rd0;
+            const float ppra = ((rp - u2) + rm) * rd1;
+            const float pth = (tp - tm) * rd2;
+            const float ppth = ((tp - u2) + tm) * rd3;
+            const float ppph = ((ap - u2) + am) * rd4;
+            float lap = fmaf(A2, pra, ppra);
+            lap = fmaf(B, pth, lap);
+            lap = fmaf(Cr, ppth, lap);
+            lap = fmaf(D, ppph, lap);
+            G[i] = gsum_add(G[i], __fmul_rn(xc, lap));
+        }
+        ym = yc;
+        yc = yp;
+        am = ac;
+        ac = ap;
+    }
+}
+
+void launch_adjA_sph(const float *X, float *Y, const float *A, const float *vel, float2 *G, const StepAParams &p,
+                     cudaStream_t s) {
+    dim3 block(64, 4, 1), grid((p.g.n1 + 63) / 64, (p.g.n2 + 3) / 4, (p.g.n3 + kSphChunk - 1) / kSphChunk);
+    k_adjA_sph<<<grid, block, 0, s>>>(X, Y, A, vel, G, p);
+}
+
+// receiver term of the spherical adjoint: z += W M (w r) at every corner
+__global__ void k_rec_adjA(float *z, const GeoPoint *__restrict__ pts, int nr, const float *__restrict__ r,
+                           const StepAParams p, const long long *__restrict__ off) {
+    const int ir = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ir >= nr) return;
+    const GeoPoint pt = pts[ir];
+    const float rv = r[ir];
+    const Grid g = p.g;
+    for (int k = 0; k < 8; k++) {
+        const long long j = pt.base + off[k];
+        const int c0 = (int)(j % g.n1), c1 = (int)((j / g.n1) % g.n2), c2 = (int)(j / ((long long)g.n1 * g.n2));
+        if (p.mask == 3 && (c0 > g.n1 - p.nb || (c0 < p.spill && (c1 >= 1 || c2 >= 1)))) continue;
+        const int si = sponge_index3(c0, c1, c2, g.n1, g.n2, g.n3, p);
+        atomicAdd(z + j, damp_a<false>(pt.w[k] * rv, si, p.dtab, p.ftab));
+    }
+}
+
+void launch_rec_adjA(float *z, const GeoPoint *pts, int nr, const float *r, const StepAParams &p, const long long *off,
+                     cudaStream_t s) {
+    if (nr > 0) k_rec_adjA<<<(nr + 127) / 128, 128, 0, s>>>(z, pts, nr, r, p, off);
 }
 
 }  // namespace awe

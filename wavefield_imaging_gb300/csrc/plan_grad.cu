@@ -78,7 +78,7 @@ static awe_status grad_alloc(awe_plan *p, int T, int fmt) {
     AWE_TRY(dev_alloc(p, (void **)&st->amax, sizeof(unsigned int)));
     AWE_TRY(dev_alloc(p, (void **)&st->X, cells * sizeof(float)));
     AWE_TRY(dev_alloc(p, (void **)&st->Y, cells * sizeof(float)));
-    if (d.ndim == 3 && d.dabc) AWE_TRY(dev_alloc(p, (void **)&st->kap, cells * sizeof(float)));
+    if (d.ndim == 3 && d.dabc && d.scheme == AWE_SCHEME_CPU) AWE_TRY(dev_alloc(p, (void **)&st->kap, cells * sizeof(float)));
     AWE_TRY(dev_alloc(p, (void **)&st->G, cells * sizeof(float2)));
     const size_t nd = (size_t)p->nsmp * (p->nr > 0 ? p->nr : 1);
     AWE_TRY(dev_alloc(p, (void **)&st->dat, nd * sizeof(float)));
@@ -144,12 +144,112 @@ static awe_status ckpt_load(awe_plan *p, int idx, float *u, cudaStream_t s) {
     return AWE_OK;
 }
 
+// Spherical GPU-program scheme (sfAWEFDspher3Dgpu's step, AWE_FAST).  Forward
+// with the two levels stored at the start of every segment's first iteration
+// (the previous level, sponge pending, and the current one before its
+// injection); per segment, last first, the levels after injection A_k are
+// recomputed out of place into slots 1..T (slot 0: A_{k0-1}); the adjoint
+// sweep j = nt .. 0 keeps z_{j+1} and z_{j+2} in two buffers:
+//   z_j = W M (L^T(I c z_{j+1}) + 2 z_{j+1} - W z_{j+2}) + W M R^T r_{j-1},
+//   dJ/dc += z_{j+1} L(A_j),  c = dt^2 v^2, folded to dJ/dm = dJ/dc (-c^2/dt^2).
+static awe_status plan_gradient_spher(awe_plan *p, const float *d_wav, int ncs, const float *d_dobs, int T, int fmt,
+                                      double *d_grad, double *misfit, float *d_dsyn, cudaStream_t s) {
+    const awe_desc &d = p->d;
+    const StepAParams &pa = p->pa;
+    if (d.expl) {
+        set_error("awe_gradient: the reflectivity-scaled injection (expl=y) depends on the model; use expl=n");
+        return AWE_ERR_UNSUPPORTED;
+    }
+    if (p->move_mode >= 0 || pa.nshot > 1) {
+        set_error("awe_gradient: one shot on a fixed geometry");
+        return AWE_ERR_UNSUPPORTED;
+    }
+    AWE_TRY(grad_alloc(p, T, fmt));
+    GradState *st = p->grad;
+    const Grid &g = p->g;
+    const long long cells = g.cells();
+    const size_t bytes = (size_t)cells * sizeof(float);
+    float *dat = d_dsyn ? d_dsyn : st->dat;
+    long long launches = 0;
+
+    StepHook hook = [&](int it, const float *prev, const float *cur, cudaStream_t ss) -> awe_status {
+        if (it % T != 0) return AWE_OK;
+        const int seg = it / T;
+        AWE_TRY(ckpt_store(p, 2 * seg, prev, ss));
+        AWE_TRY(ckpt_store(p, 2 * seg + 1, cur, ss));
+        return AWE_OK;
+    };
+    AWE_TRY(planA_run(p, d_wav, ncs, dat, nullptr, s, &hook));
+    launches += p->launches;
+    launch_residual(dat, d_dobs, st->r, p->nsmp, p->nr, st->row_sum, s);
+    std::vector<double> rows(p->nsmp);
+    CUDA_TRY(cudaMemcpyAsync(rows.data(), st->row_sum, rows.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+
+    CUDA_TRY(cudaMemsetAsync(st->X, 0, bytes, s));
+    CUDA_TRY(cudaMemsetAsync(st->Y, 0, bytes, s));
+    CUDA_TRY(cudaMemsetAsync(st->G, 0, (size_t)cells * sizeof(float2), s));
+    float *X = st->X, *Y = st->Y;
+    // j = nt: z_nt = W M R^T r_{nt-1}
+    launch_rec_adjA(Y, p->rec, p->nr, st->r + (size_t)(d.nt - 1) * p->nr, pa, p->corner_off, s);
+    std::swap(X, Y);
+    launches++;
+    for (int seg = st->nseg - 1; seg >= 0; seg--) {
+        const int k0 = seg * T, k1 = std::min(k0 + T, d.nt);
+        float *slot = st->slots;  // slot[k - k0 + 1] = A_k
+        AWE_TRY(ckpt_load(p, 2 * seg, slot, s));
+        AWE_TRY(ckpt_load(p, 2 * seg + 1, slot + cells, s));
+        for (int k = k0; k < k1; k++) {
+            float *cur = slot + (size_t)(k - k0 + 1) * cells;
+            launch_injectA(false, 3, cur, p->src, nullptr, p->ns, d_wav, k, false, p->corner_off, s);
+            if (k + 1 < k1) launch_stepA_oop(pa.geom, false, cur, cur - cells, cur + cells, p->vel, pa, s);
+            launches += (p->ns > 0) + (k + 1 < k1);
+        }
+        for (int j = k1 - 1; j >= k0; j--) {
+            launch_adjA_sph(X, Y, slot + (size_t)(j - k0 + 1) * cells, p->vel, st->G, pa, s);
+            launches++;
+            if (j >= 1) {
+                launch_rec_adjA(Y, p->rec, p->nr, st->r + (size_t)(j - 1) * p->nr, pa, p->corner_off, s);
+                launches++;
+            }
+            std::swap(X, Y);
+        }
+    }
+    launch_grad_fold(st->G, p->vel, d.dt, g, p->nbd, d.n, d.ndim, d_grad, s, true);
+    launches++;
+    CUDA_TRY(cudaStreamSynchronize(s));
+    double J = 0;
+    for (double v : rows) J += 0.5 * v;
+    *misfit = J;
+    p->launches = launches;
+    return AWE_OK;
+}
+
 awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *d_dobs, const awe_grad_opts &o,
                          double *d_grad, double *misfit, float *d_dsyn, cudaStream_t s, int image) {
     const awe_desc &d = p->d;
-    if (d.scheme != AWE_SCHEME_CPU || d.coords != AWE_CART) {
-        set_error("awe_gradient: only the cartesian CPU-program scheme has an adjoint");
+    const bool spher = d.scheme == AWE_SCHEME_GPU && d.coords == AWE_SPHER && d.ndim == 3;
+    if ((d.scheme != AWE_SCHEME_CPU || d.coords != AWE_CART) && !spher) {
+        set_error("awe_gradient: the adjoint covers the cartesian CPU-program scheme and the spherical 3D "
+                  "GPU-program scheme");
         return AWE_ERR_UNSUPPORTED;
+    }
+    if (spher) {
+        if (image >= 0) {
+            set_error("awe_rtm: the spherical scheme has the gradient only");
+            return AWE_ERR_UNSUPPORTED;
+        }
+        if (d.precision != AWE_FAST) {
+            set_error("awe_gradient: precision must be AWE_FAST");
+            return AWE_ERR_UNSUPPORTED;
+        }
+        int T = o.ckpt_every > 0 ? o.ckpt_every : (int)std::ceil(std::sqrt((double)d.nt));
+        T = std::max(1, std::min(T, d.nt));
+        if (o.ckpt_format != AWE_CKPT_BF16 && o.ckpt_format != AWE_CKPT_FP32 && o.ckpt_format != AWE_CKPT_FP16 &&
+            o.ckpt_format != AWE_CKPT_BFP16) {
+            set_error("awe_gradient: unknown checkpoint format %d", o.ckpt_format);
+            return AWE_ERR_INVALID;
+        }
+        return plan_gradient_spher(p, d_wav, ncs, d_dobs, T, o.ckpt_format, d_grad, misfit, d_dsyn, s);
     }
     if (p->den || d.hybrid) {
         set_error("awe_gradient: variable density and the hybrid ABC have no adjoint here");

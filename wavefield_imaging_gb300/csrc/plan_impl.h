@@ -148,5 +148,6 @@ void plan_gradient_free(awe_plan *p);
 
 awe_status planA_init(awe_plan *p);
 awe_status planA_model(awe_plan *p, const float *vel, const float *rfl);
-awe_status planA_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, float *d_wfl, cudaStream_t s);
+awe_status planA_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, float *d_wfl, cudaStream_t s,
+                     const StepHook *hook = nullptr);
 }  // namespace awe

@@ -318,7 +318,11 @@ static awe_status prepare_injection(awe_plan *p, bool &scaled) {
     return AWE_OK;
 }
 
-awe_status planA_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, float *d_wfl, cudaStream_t s) {
+// hook (may be null): called at the start of every iteration, before the
+// injection, with prev = the previous level (sponge pending) and cur = the
+// current level
+awe_status planA_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, float *d_wfl, cudaStream_t s,
+                     const StepHook *hook) {
     (void)ncs;
     const awe_desc &d = p->d;
     const Grid &g = p->g;
@@ -339,6 +343,7 @@ awe_status planA_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, flo
     float *cur = p->u[1], *nxt = p->u[0];
     int itr = 0, isnap = 0;
     for (int it = 0; it < d.nt; it++) {
+        if (hook) AWE_TRY((*hook)(it, nxt, cur, s));
         if (p->ns > 0) {
             const PointsAt ps = points_at(p, p->src, p->ns, p->src_rows, it);
             launch_injectA(exact, d.ndim, cur, ps.pts, p->inj_scale, p->ns, d_wav, it, scaled, p->corner_off, s,
