@@ -698,6 +698,98 @@ def spher_model(w):
     return vel
 
 
+def spher_shots(w, nshots):
+    """Sources along the equator (a great circle) at 50 m altitude above the
+    mean surface, 64 x 64 receivers around each: [(sou, rec)] in (r, phi, theta)."""
+    nr_, nth, nph = w["n"]
+    rs = 3389.5 - 0.2 + 0.05
+    th0 = w["o"][1] + 0.5 * (nth - 1) * w["d"][1]
+    shots = []
+    for k in range(nshots):
+        ph_s = w["o"][2] + (0.5 if nshots == 1 else 0.3 + 0.4 * k / (nshots - 1)) * (nph - 1) * w["d"][2]
+        sou = np.array([[rs, ph_s, th0]], np.float32)
+        gth = th0 + np.linspace(-0.25, 0.25, 64) * (nth - 1) * w["d"][1]
+        gph = ph_s + np.linspace(-0.25, 0.25, 64) * (nph - 1) * w["d"][2]
+        P, T = np.meshgrid(gph, gth, indexing="ij")
+        rec = np.stack([np.full(P.size, rs), P.ravel(), T.ravel()], 1).astype(np.float32)
+        shots.append((sou, rec))
+    return shots
+
+
+def run_sphergrad(args):
+    """--workload sphergrad3d: misfit gradient of one shot of the spherical
+    shell (c4 grid and scheme): forward with checkpoints, segment recompute,
+    adjoint of the spherical step.  Start model: the true model smoothed
+    along r (100 m).  One bench step = one gradient; the forward alone is
+    timed beside it."""
+    import torch
+    from scipy.ndimage import gaussian_filter1d
+
+    import wavefield_imaging_gb300 as awe
+
+    torch.cuda.set_device(0)
+    nt = args.nt
+    w = spher_workload(nt, nr=args.n + 188 if args.n != 512 else 700, nang=args.n)
+    vtrue = spher_model(w)
+    v0 = gaussian_filter1d(vtrue, 100.0 / 5.0, axis=2, mode="nearest").astype(np.float32)
+    sou, rec = spher_shots(w, 1)[0]
+    wav = ricker(nt, w["dt"], w["f0"])
+    desc = awe.make_desc(3, w["n"], w["d"], w["o"], nt, w["dt"], coords=awe.SPHER, scheme=awe.SCHEME_GPU,
+                         nb=w["nb"], expl=0, precision=awe.FAST)
+    plan = awe.Plan(desc)
+    plan.set_geometry(sou, rec)
+    plan.set_model(vtrue)
+    dobs = plan.forward(wav)
+    plan.set_model(v0)
+    fmt = {"bfp16": awe.CKPT_BFP16, "bf16": awe.CKPT_BF16, "fp16": awe.CKPT_FP16, "fp32": awe.CKPT_FP32}[args.ckpt]
+    d_wav = torch.from_numpy(wav).cuda()
+    d_dobs = torch.from_numpy(dobs).cuda()
+    d_grad = torch.zeros(int(np.prod(w["n"])), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.Stream()
+
+    def step():
+        return plan.gradient_device(d_wav.data_ptr(), 1, d_dobs.data_ptr(), d_grad.data_ptr(), ckpt_format=fmt,
+                                    stream=stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        J = step()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(0)
+    sampler.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    launches = 0
+    for _ in range(args.steps):
+        J = step()
+        launches += plan.last_launch_count()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    d_dat = torch.zeros((plan.nsmp, rec.shape[0]), dtype=torch.float32, device="cuda")
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    plan.forward_device(d_wav.data_ptr(), 1, d_dat.data_ptr(), 0, stream.cuda_stream)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    fwd_ms = f0.elapsed_time(f1)
+    cells = int(np.prod([n + 2 * w["nb"] for n in w["n"]]))
+    g = d_grad.cpu().numpy()
+    out = {"metric": "FWI gradients/s (spherical shell, checkpointed fwd + adjoint)", "value": 1e3 / ms,
+           "unit": "gradients/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "fp32 fields, compensated fp32 sums", "data": "synthetic",
+           "config": {"workload": w["name"] + ", 1 shot, start model smoothed 100 m along r", "checkpoint": args.ckpt,
+                      "padded_cells": cells, "ckpt_every": int(np.ceil(np.sqrt(nt))),
+                      "device_bytes": plan.device_bytes()},
+           "split": {"forward_ms": fwd_ms, "gradient_ms": ms, "gradient_over_forward": ms / fwd_ms,
+                     "cell_steps_per_s": cells * nt / (ms / 1e3)},
+           "misfit": J, "grad_finite": bool(np.isfinite(g).all()), "grad_max_abs": float(np.abs(g).max()),
+           "gpu_launches": int(launches), "clocks": clocks}
+    print(json.dumps(out))
+    plan.close()
+
+
 def run_spher(args):
     """--workload spher3d: one shot of the spherical-shell forward (scheme of
     sfAWEFDspher3Dgpu) on the c4 grid."""
@@ -710,19 +802,7 @@ def run_spher(args):
     nshots = args.shots or 1
     w = spher_workload(nt, nr=args.n + 188 if args.n != 512 else 700, nang=args.n)
     vel = spher_model(w)
-    nr_, nth, nph = w["n"]
-    rs = 3389.5 - 0.2 + 0.05
-    th0 = w["o"][1] + 0.5 * (nth - 1) * w["d"][1]
-    # sources along the equator (a great circle) at 50 m altitude, 64 x 64 receivers around each
-    shots = []
-    for k in range(nshots):
-        ph_s = w["o"][2] + (0.5 if nshots == 1 else 0.3 + 0.4 * k / (nshots - 1)) * (nph - 1) * w["d"][2]
-        sou = np.array([[rs, ph_s, th0]], np.float32)
-        gth = th0 + np.linspace(-0.25, 0.25, 64) * (nth - 1) * w["d"][1]
-        gph = ph_s + np.linspace(-0.25, 0.25, 64) * (nph - 1) * w["d"][2]
-        P, T = np.meshgrid(gph, gth, indexing="ij")
-        rec = np.stack([np.full(P.size, rs), P.ravel(), T.ravel()], 1).astype(np.float32)
-        shots.append((sou, rec))
+    shots = spher_shots(w, nshots)
     wav = ricker(nt, w["dt"], w["f0"])
     desc = awe.make_desc(3, w["n"], w["d"], w["o"], nt, w["dt"], coords=awe.SPHER, scheme=awe.SCHEME_GPU,
                          nb=w["nb"], expl=0, precision=awe.FAST)
@@ -853,7 +933,7 @@ def main():
     ap.add_argument("--nt", type=int, default=3000, help="time steps (the workload is nt=3000)")
     ap.add_argument("--n", type=int, default=512, help="model edge (the workload is 512; smaller for profiling)")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
-    ap.add_argument("--workload", default="fwd3d", choices=["fwd3d", "fwd2d", "grad3d", "grad2d", "batch2d", "batchgrad2d", "spher3d"],
+    ap.add_argument("--workload", default="fwd3d", choices=["fwd3d", "fwd2d", "grad3d", "grad2d", "batch2d", "batchgrad2d", "spher3d", "sphergrad3d"],
                     help="fwd3d: the headline forward workload; grad3d/grad2d: misfit gradients; "
                          "batch2d: the batched 2D survey")
     ap.add_argument("--shots", type=int, default=0,
@@ -867,6 +947,8 @@ def main():
         run_batch(args)
     elif args.workload == "batchgrad2d":
         run_batch_grad(args)
+    elif args.workload == "sphergrad3d":
+        run_sphergrad(args)
     elif args.workload == "spher3d":
         run_spher(args)
     elif args.workload == "fwd2d":
