@@ -53,12 +53,14 @@ def test_oracle_checkpoint_emulation_fp32_is_exact():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("fsrf", [0, 1])
-def test_gradient_matches_fp64_oracle(fsrf):
+@pytest.mark.parametrize("fsrf,nr", [(0, 45), (1, 45), (0, 46), (1, 46)])
+def test_gradient_matches_fp64_oracle(fsrf, nr):
+    """nr = 45: odd padded radius count (one radius per thread); 46: even
+    (two radii per thread, packed arithmetic)."""
     import wavefield_imaging_gb300 as awe
     from oracle import oracle
 
-    par, vel, wav, sou, rec, vtrue = spher_grad_case(fsrf=fsrf)
+    par, vel, wav, sou, rec, vtrue = spher_grad_case(fsrf=fsrf, n=(nr, 20, 20))
     dobs = _dobs(par, vtrue, wav, sou, rec)
     gref, Jref, dref = oracle.spher3d_gradient(par, vel, wav, sou, rec, dobs)
     T = int(np.ceil(np.sqrt(par["nt"])))

@@ -572,9 +572,133 @@ __global__ void __launch_bounds__(256) k_adjA_sph(const float *__restrict__ X, f
     }
 }
 
+// The same adjoint with two consecutive radii per thread (n1 even): 8-byte
+// loads and packed FP32x2 arithmetic; the r neighbours outside the pair come
+// from scalar loads, those inside it from the thread's own cells.
+__global__ void __launch_bounds__(256) k_adjA_sph2(const float *__restrict__ X, float *__restrict__ Y,
+                                                   const float *__restrict__ A, const float *__restrict__ vel,
+                                                   float2 *__restrict__ G, const StepAParams p) {
+    const int i1 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int i2 = blockIdx.y * blockDim.y + threadIdx.y;
+    const Grid g = p.g;
+    if (i1 >= g.n1 || i2 >= g.n2) return;
+    const long long s2 = g.n1, s3 = (long long)g.n1 * g.n2;
+    const int p0 = blockIdx.z * kSphChunk, p1 = min(p0 + kSphChunk, g.n3);
+    auto rin = [&](int r) { return r >= 4 && r < g.n1 - 4; };
+    auto pin = [&](int f) { return f >= 4 && f < g.n3 - 4; };
+    const bool t_in = i2 >= 4 && i2 < g.n2 - 4;
+    const bool tm_ok = i2 - 1 >= 4 && i2 - 1 < g.n2 - 4, tp_ok = i2 + 1 >= 4 && i2 + 1 < g.n2 - 4;
+    const bool r0 = rin(i1), r1 = rin(i1 + 1);
+    const bool c0 = r0 && t_in, c1 = r1 && t_in;
+    const long long t = (long long)i2 * g.n1 + i1;
+    const float rd0 = p.rd[0], rd1 = p.rd[1], rd2 = p.rd[2], rd3 = p.rd[3], rd4 = p.rd[4];
+    const float2 A2 = *reinterpret_cast<const float2 *>(p.tr0 + i1), Cr = *reinterpret_cast<const float2 *>(p.tr1 + i1);
+    const float2 B = *reinterpret_cast<const float2 *>(p.tt0 + t), D = *reinterpret_cast<const float2 *>(p.tt1 + t);
+    // weights of the two cells in their neighbours' stencils (0: no stencil there)
+    // r - 1: cell 0's neighbour i1 - 1 (outside the pair), cell 1's is cell 0
+    const float wrm0 = (rin(i1 - 1) && t_in) ? fmaf(__ldg(p.tr0 + i1 - 1), rd0, rd1) : 0.f;
+    const float wrm1 = c0 ? fmaf(A2.x, rd0, rd1) : 0.f;
+    // r + 1: cell 0's neighbour is cell 1, cell 1's is i1 + 2 (outside)
+    const float wrp0 = c1 ? fmaf(-A2.y, rd0, rd1) : 0.f;
+    const float wrp1 = (rin(i1 + 2) && t_in) ? fmaf(-__ldg(p.tr0 + i1 + 2), rd0, rd1) : 0.f;
+    float2 wtm = make_float2(0.f, 0.f), wtp = wtm;
+    if (tm_ok) {
+        const float2 Bm = *reinterpret_cast<const float2 *>(p.tt0 + t - s2);
+        wtm = make_float2(r0 ? fmaf(Bm.x, rd2, Cr.x * rd3) : 0.f, r1 ? fmaf(Bm.y, rd2, Cr.y * rd3) : 0.f);
+    }
+    if (tp_ok) {
+        const float2 Bp = *reinterpret_cast<const float2 *>(p.tt0 + t + s2);
+        wtp = make_float2(r0 ? fmaf(-Bp.x, rd2, Cr.x * rd3) : 0.f, r1 ? fmaf(-Bp.y, rd2, Cr.y * rd3) : 0.f);
+    }
+    const float2 wc = make_float2(-2.f * (rd1 + Cr.x * rd3 + D.x * rd4), -2.f * (rd1 + Cr.y * rd3 + D.y * rd4));
+    const float2 wph = make_float2(D.x * rd4, D.y * rd4);
+    const float dt2 = p.dt2;
+    const float2 dt22 = make_float2(dt2, dt2);
+    auto ld2 = [](const float *b, long long j) { return *reinterpret_cast<const float2 *>(b + j); };
+    auto ycx2 = [&](long long j) {  // c X at cells j, j + 1
+        const float2 v = ld2(vel, j);
+        return __fmul2_rn(__fmul2_rn(dt22, __fmul2_rn(v, v)), ld2(X, j));
+    };
+    auto ycx1 = [&](long long j) {
+        const float v = __ldg(vel + j);
+        return (dt2 * (v * v)) * X[j];
+    };
+    auto own = [&](float2 y, int f) {  // I c X of the own cells at plane f
+        const bool ph = f >= 0 && f < g.n3 && pin(f);
+        return make_float2(c0 && ph ? y.x : 0.f, c1 && ph ? y.y : 0.f);
+    };
+    const long long base = (long long)i2 * s2 + i1;
+    float2 ym = p0 > 0 ? own(ycx2(base + (p0 - 1) * s3), p0 - 1) : make_float2(0.f, 0.f);
+    float2 yc = own(ycx2(base + p0 * s3), p0);
+    float2 am = make_float2(0.f, 0.f), ac = am;
+    if (A) {
+        am = p0 > 0 ? ld2(A, base + (p0 - 1) * s3) : am;
+        ac = ld2(A, base + p0 * s3);
+    }
+    const float2 r0v = make_float2(rd0, rd0), r1v = make_float2(rd1, rd1), r2v = make_float2(rd2, rd2);
+    const float2 r3v = make_float2(rd3, rd3), r4v = make_float2(rd4, rd4), m1 = make_float2(-1.f, -1.f),
+                 m2 = make_float2(-2.f, -2.f);
+    for (int i3 = p0; i3 < p1; i3++) {
+        const long long i = base + i3 * s3;
+        const bool ph = pin(i3);
+        const float2 yp = i3 + 1 < g.n3 ? own(ycx2(i + s3), i3 + 1) : make_float2(0.f, 0.f);
+        const float2 ap = (A && i3 + 1 < g.n3) ? ld2(A, i + s3) : make_float2(0.f, 0.f);
+        float2 lt = __fmul2_rn(wph, __fadd2_rn(ym, yp));
+        if (ph) {
+            lt = __ffma2_rn(wc, yc, lt);
+            const float yrm = wrm0 != 0.f ? ycx1(i - 1) : 0.f, yrp = wrp1 != 0.f ? ycx1(i + 2) : 0.f;
+            lt = __ffma2_rn(make_float2(wrm0, wrm1), make_float2(yrm, yc.x), lt);
+            lt = __ffma2_rn(make_float2(wrp0, wrp1), make_float2(yc.y, yrp), lt);
+            if (tm_ok) lt = __ffma2_rn(wtm, ycx2(i - s2), lt);
+            if (tp_ok) lt = __ffma2_rn(wtp, ycx2(i + s2), lt);
+        }
+        const float2 xc = ld2(X, i), yv = ld2(Y, i);
+        const float2 mu2 = __ffma2_rn(make_float2(2.f, 2.f), xc, lt);
+        float out[2] = {mu2.x, mu2.y};
+        const float yy[2] = {yv.x, yv.y};
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            const int si = sponge_index3(i1 + j, i2, i3, g.n1, g.n2, g.n3, p);
+            float m = fmaf(-damp_a<false>(1.f, si, p.dtab, p.ftab), yy[j], out[j]);
+            if (p.mask == 3 && (i1 + j > g.n1 - p.nb || (i1 + j < p.spill && (i2 >= 1 || i3 >= 1)))) m = 0.f;
+            out[j] = damp_a<false>(m, si, p.dtab, p.ftab);
+        }
+        *reinterpret_cast<float2 *>(Y + i) = make_float2(out[0], out[1]);
+        if (A && (c0 || c1) && ph) {  // the forward's Laplacian of A at the two cells
+            const float rm = A[i - 1], rp = A[i + 2];
+            const float2 mi = make_float2(rm, ac.x), pl = make_float2(ac.y, rp);
+            const float2 tm = ld2(A, i - s2), tp = ld2(A, i + s2);
+            const float2 pra = __fmul2_rn(__ffma2_rn(mi, m1, pl), r0v);
+            const float2 ppra = __fmul2_rn(__fadd2_rn(__ffma2_rn(ac, m2, pl), mi), r1v);
+            const float2 pth = __fmul2_rn(__ffma2_rn(tm, m1, tp), r2v);
+            const float2 ppth = __fmul2_rn(__fadd2_rn(__ffma2_rn(ac, m2, tp), tm), r3v);
+            const float2 ppph = __fmul2_rn(__fadd2_rn(__ffma2_rn(ac, m2, ap), am), r4v);
+            float2 lap = __ffma2_rn(A2, pra, ppra);
+            lap = __ffma2_rn(B, pth, lap);
+            lap = __ffma2_rn(Cr, ppth, lap);
+            lap = __ffma2_rn(D, ppph, lap);
+            const float4 gq = *reinterpret_cast<const float4 *>(G + i);
+            float2 g0 = make_float2(gq.x, gq.y), g1 = make_float2(gq.z, gq.w);
+            if (c0) g0 = gsum_add(g0, __fmul_rn(xc.x, lap.x));
+            if (c1) g1 = gsum_add(g1, __fmul_rn(xc.y, lap.y));
+            *reinterpret_cast<float4 *>(G + i) = make_float4(g0.x, g0.y, g1.x, g1.y);
+        }
+        ym = yc;
+        yc = yp;
+        am = ac;
+        ac = ap;
+    }
+}
+
 void launch_adjA_sph(const float *X, float *Y, const float *A, const float *vel, float2 *G, const StepAParams &p,
                      cudaStream_t s) {
-    dim3 block(64, 4, 1), grid((p.g.n1 + 63) / 64, (p.g.n2 + 3) / 4, (p.g.n3 + kSphChunk - 1) / kSphChunk);
+    const int nchunk = (p.g.n3 + kSphChunk - 1) / kSphChunk;
+    if (p.g.n1 % 2 == 0) {
+        dim3 b2(32, 8, 1), g2((p.g.n1 / 2 + 31) / 32, (p.g.n2 + 7) / 8, nchunk);
+        k_adjA_sph2<<<g2, b2, 0, s>>>(X, Y, A, vel, G, p);
+        return;
+    }
+    dim3 block(64, 4, 1), grid((p.g.n1 + 63) / 64, (p.g.n2 + 3) / 4, nchunk);
     k_adjA_sph<<<grid, block, 0, s>>>(X, Y, A, vel, G, p);
 }
 
