@@ -213,7 +213,9 @@ typedef struct {
 /* Gradient of J = 0.5 * sum over data rows of ||d - dobs||^2 with respect to
  * m = 1/v^2 on the model grid, for the plan's model and geometry.  Scheme
  * AWE_SCHEME_CPU (2D or 3D, any order, sponge and one-way ABC, free surface),
- * no density, no hybrid ABC; the forward runs in AWE_FAST arithmetic.  The
+ * no density, no hybrid ABC; or the spherical 3D AWE_SCHEME_GPU scheme of
+ * sfAWEFDspher3Dgpu (sponge, free surface; expl=n, one shot, fixed points).
+ * The forward runs in AWE_FAST arithmetic.  The
  * boundary coefficients (one-way ABC, sponge) are held at the plan's model.
  * The forward pass stores both time levels every ckpt_every steps (in
  * opts->ckpt_format); the adjoint sweep recomputes each segment once from
