@@ -148,6 +148,14 @@ struct AdjParams {
     int nd, nop;
     const float *w1, *w2, *w3;  // sponge axis factors; null = no sponge
     int xcorr;                  // imaging condition: G += I nu V (cross-correlation) instead of I nu L(V)
+    // point terms fused into the step (null: none), per padded cell i the
+    // entries [start[i], start[i + 1]) as (point index, weight bits):
+    // receivers mu += W (W (w r[point])) with r = rrow; sources G += nu (wav w)
+    const int *rc_start, *sc_start;
+    const int2 *rc_ent, *sc_ent;
+    const float *rrow;     // this step's residual row (null: no receiver term this step)
+    const float *wav;      // wavelet (null: no source term)
+    int it, ncs, one_wavelet;
 };
 void launch_adjB(const float *X, float *Y, const float *V, const float *vel, float2 *G, const AdjParams &p,
                  cudaStream_t s);

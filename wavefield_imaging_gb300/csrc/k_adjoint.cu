@@ -71,7 +71,14 @@ __global__ void __launch_bounds__(256) k_adjB(const float *__restrict__ X, float
     }
     const float w = wcell(p, i1, i2, i3);
     const float lam = (in ? 2.f * x : 0.f) + lt + (in ? -w : w) * Y[i];
-    Y[i] = w * lam;
+    float mu = w * lam;
+    if (p.rrow) {  // receiver residuals at this cell, in (receiver, corner) order
+        for (int e = p.rc_start[i], e1 = p.rc_start[i + 1]; e < e1; e++) {
+            const int2 en = p.rc_ent[e];
+            mu = __fadd_rn(mu, __fmul_rn(w, __fmul_rn(w, __fmul_rn(__int_as_float(en.y), p.rrow[en.x]))));
+        }
+    }
+    Y[i] = mu;
     if (in && p.xcorr) {
         G[i] = gsum_add(G[i], __fmul_rn(x, V[i]));  // FP32 product, compensated sum
     } else if (in) {
@@ -84,6 +91,13 @@ __global__ void __launch_bounds__(256) k_adjB(const float *__restrict__ X, float
             lap += t;
         }
         G[i] = gsum_add(G[i], __fmul_rn(x, lap));
+    }
+    if (p.wav && !p.xcorr) {  // source term, in (source, corner) order
+        for (int e = p.sc_start[i], e1 = p.sc_start[i + 1]; e < e1; e++) {
+            const int2 en = p.sc_ent[e];
+            const float dd = p.one_wavelet ? p.wav[(long long)p.it * p.ncs] : p.wav[(long long)p.it * p.ncs + en.x];
+            G[i] = gsum_add_prod(G[i], x, dd * __int_as_float(en.y));
+        }
     }
 }
 

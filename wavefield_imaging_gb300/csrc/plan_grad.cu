@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "awe_internal.h"
@@ -46,6 +47,10 @@ struct GradState {
     bool tma = false;
     float *vr = nullptr, *gbuf = nullptr;
     CUtensorMap vr_halo[3], vr_tile[3], g_halo, x_tile, y_tile;
+    // receiver / source corners by padded cell for the fused adjoint step
+    int *rc_start = nullptr, *sc_start = nullptr;
+    int2 *rc_ent = nullptr, *sc_ent = nullptr;
+    size_t rc_cap = 0, sc_cap = 0;
 };
 
 void plan_gradient_free(awe_plan *p) {
@@ -53,7 +58,8 @@ void plan_gradient_free(awe_plan *p) {
     GradState *st = p->grad;
     for (void *ptr : {(void *)st->slots, st->ckpt, (void *)st->scales, (void *)st->amax, (void *)st->X, (void *)st->Y,
                       (void *)st->kap, (void *)st->G, (void *)st->dat, (void *)st->r, (void *)st->row_sum,
-                      (void *)st->vr, (void *)st->gbuf})
+                      (void *)st->vr, (void *)st->gbuf, (void *)st->rc_start, (void *)st->sc_start,
+                      (void *)st->rc_ent, (void *)st->sc_ent})
         if (ptr) dev_free(p, ptr);
     delete st;
     p->grad = nullptr;
@@ -104,6 +110,44 @@ static awe_status grad_alloc(awe_plan *p, int T, int fmt) {
             return AWE_ERR_CUDA;
         }
     }
+    return AWE_OK;
+}
+
+static int float_bits(float f) {
+    int i;
+    std::memcpy(&i, &f, sizeof i);
+    return i;
+}
+
+// corners of `pts` grouped by padded cell (counting sort, each cell's
+// entries in (point, corner) order) into start[cells + 1] and ent
+static awe_status build_cell_lists(awe_plan *p, const std::vector<GeoPoint> &pts, int nc, int **start, int2 **ent,
+                                   size_t *cap, cudaStream_t s) {
+    const long long cells = p->g.cells();
+    std::vector<int> cnt((size_t)cells + 1, 0);
+    for (const GeoPoint &pt : pts)
+        for (int c = 0; c < nc; c++) {
+            const long long n = pt.base + p->h_corner_off[c];
+            if (n >= 0 && n < cells) cnt[(size_t)n + 1]++;
+        }
+    for (long long i = 0; i < cells; i++) cnt[(size_t)i + 1] += cnt[(size_t)i];
+    std::vector<int2> e(std::max<size_t>((size_t)cnt[(size_t)cells], 1));
+    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+    for (size_t k = 0; k < pts.size(); k++)
+        for (int c = 0; c < nc; c++) {
+            const long long n = pts[k].base + p->h_corner_off[c];
+            if (n >= 0 && n < cells) e[(size_t)fill[(size_t)n]++] = make_int2((int)k, float_bits(pts[k].w[c]));
+        }
+    if (!*start) AWE_TRY(dev_alloc(p, (void **)start, ((size_t)cells + 1) * sizeof(int)));
+    if (*cap < e.size()) {
+        if (*ent) dev_free(p, *ent);
+        *ent = nullptr;
+        AWE_TRY(dev_alloc(p, (void **)ent, e.size() * sizeof(int2)));
+        *cap = e.size();
+    }
+    CUDA_TRY(cudaMemcpyAsync(*start, cnt.data(), cnt.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(*ent, e.data(), e.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors go out of scope
     return AWE_OK;
 }
 
@@ -320,6 +364,21 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
     ap.w3 = sponge ? p->w[2] : nullptr;
     ap.xcorr = xcorr;
     AbcB abc{p->abc[0], p->abc[1], p->abc[2], p->abc[3], p->abc[4], p->abc[5]};
+    // receivers and sources in the adjoint step itself (one launch per step)
+    // where the grid is small enough for per-cell lists and no ABC transpose
+    // follows the step
+    const bool fuse_pts = !st->tma && !st->kap && cells <= (1LL << 24);
+    if (fuse_pts) {
+        const int nc = d.ndim == 3 ? 8 : 4;
+        AWE_TRY(build_cell_lists(p, p->h_rec, nc, &st->rc_start, &st->rc_ent, &st->rc_cap, s));
+        AWE_TRY(build_cell_lists(p, p->h_src, nc, &st->sc_start, &st->sc_ent, &st->sc_cap, s));
+        ap.rc_start = st->rc_start;
+        ap.rc_ent = st->rc_ent;
+        ap.sc_start = st->sc_start;
+        ap.sc_ent = st->sc_ent;
+        ap.ncs = ncs;
+        ap.one_wavelet = ncs == 1;
+    }
     float *X = st->X, *Y = st->Y;
     const CUtensorMap *xmap = &st->x_tile, *ymap = &st->y_tile;
     for (int seg = st->nseg - 1; seg >= 0; seg--) {
@@ -365,6 +424,11 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
                 launches += 2;
             } else {
                 const float *Vk = slot0 + (size_t)(k - k0 + 1) * cells;
+                if (fuse_pts) {
+                    ap.rrow = (k % d.jdata == 0 && p->nr > 0) ? st->r + (size_t)(k / d.jdata) * p->nr : nullptr;
+                    ap.wav = (p->ns > 0 && !xcorr) ? d_wav : nullptr;
+                    ap.it = k;
+                }
                 launch_adjB(X, Y, Vk, p->vel, st->G, ap, s);
                 launches++;
             }
@@ -372,11 +436,11 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
                 launch_kap_fold(Y, st->kap, ap, s);
                 launches++;
             }
-            if (k % d.jdata == 0 && p->nr > 0) {
+            if (k % d.jdata == 0 && p->nr > 0 && !fuse_pts) {
                 launch_rec_adj(Y, p->rec, p->nr, st->r + (size_t)(k / d.jdata) * p->nr, ap, p->corner_off, s);
                 launches++;
             }
-            if (p->ns > 0 && !xcorr) {
+            if (p->ns > 0 && !xcorr && !fuse_pts) {
                 launch_src_grad(st->G, X, p->src, p->ns, d_wav, k, ncs, ncs == 1, d.ndim, p->corner_off, s);
                 launches++;
             }
