@@ -49,6 +49,7 @@ static void set_move_mode(awe_plan *p, int mode, int src_rows, int rec_rows) {
 }
 
 void plan_graph_drop(awe_plan *p) {
+    plan_gradient_graph_drop(p);
     if (p->gexec) cudaGraphExecDestroy(p->gexec);
     p->gexec = nullptr;
     p->g_wav = nullptr;
@@ -661,12 +662,24 @@ static awe_status gradient_or_image_host(awe_plan *p, const float *wav, int ncs,
     const size_t wav_bytes = (size_t)d.nt * ncs * sizeof(float);
     const size_t dat_bytes = (size_t)p->nsmp * p->nr * sizeof(float);
     const size_t grad_bytes = (size_t)d.n[0] * d.n[1] * (d.ndim == 3 ? d.n[2] : 1) * sizeof(double);
-    float *d_wav = nullptr, *d_dobs = nullptr, *d_dsyn = nullptr;
-    double *d_grad = nullptr;
-    awe_status st = dev_alloc(p, (void **)&d_wav, wav_bytes);
-    if (st == AWE_OK) st = dev_alloc(p, (void **)&d_dobs, dat_bytes > 0 ? dat_bytes : 4);
-    if (st == AWE_OK && dsyn) st = dev_alloc(p, (void **)&d_dsyn, dat_bytes > 0 ? dat_bytes : 4);
-    if (st == AWE_OK) st = dev_alloc(p, (void **)&d_grad, grad_bytes);
+    // staging buffers kept across calls (stable pointers keep a captured gradient valid)
+    auto stage = [&](void **buf, size_t &have, size_t need) {
+        if (need == 0) need = 16;
+        if (have >= need && *buf) return AWE_OK;
+        dev_free(p, *buf);
+        *buf = nullptr;
+        have = 0;
+        awe_status r = dev_alloc(p, buf, need);
+        if (r == AWE_OK) have = need;
+        return r;
+    };
+    awe_status st = stage((void **)&p->stage_wav, p->stage_wav_bytes, wav_bytes);
+    if (st == AWE_OK) st = stage((void **)&p->stage_dat, p->stage_dat_bytes, dat_bytes);
+    if (st == AWE_OK && dsyn) st = stage((void **)&p->stage_dsyn, p->stage_dsyn_bytes, dat_bytes);
+    if (st == AWE_OK) st = stage((void **)&p->stage_grad, p->stage_grad_bytes, grad_bytes);
+    if (st != AWE_OK) return st;
+    float *d_wav = p->stage_wav, *d_dobs = p->stage_dat, *d_dsyn = dsyn ? p->stage_dsyn : nullptr;
+    double *d_grad = p->stage_grad;
     if (st == AWE_OK) {
         cudaError_t e = cudaMemcpyAsync(d_wav, wav, wav_bytes, cudaMemcpyHostToDevice, p->stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(d_dobs, dobs, dat_bytes, cudaMemcpyHostToDevice, p->stream);
@@ -686,10 +699,6 @@ static awe_status gradient_or_image_host(awe_plan *p, const float *wav, int ncs,
         }
     }
     cudaStreamSynchronize(p->stream);
-    dev_free(p, d_wav);
-    dev_free(p, d_dobs);
-    dev_free(p, d_dsyn);
-    dev_free(p, d_grad);
     return st;
 }
 

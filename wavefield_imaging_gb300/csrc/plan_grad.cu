@@ -51,11 +51,29 @@ struct GradState {
     int *rc_start = nullptr, *sc_start = nullptr;
     int2 *rc_ent = nullptr, *sc_ent = nullptr;
     size_t rc_cap = 0, sc_cap = 0;
+    bool lists_ok = false;  // cleared when the geometry changes
+    // misfit rows (pinned, written by the stream) and the captured gradient
+    double *h_rows = nullptr;
+    size_t h_rows_n = 0;
+    cudaGraphExec_t gexec = nullptr;
+    const void *g_key[4] = {nullptr, nullptr, nullptr, nullptr};
+    int g_ncs = 0, g_image = -2;
+    long long g_launches = 0;
 };
+
+void plan_gradient_graph_drop(awe_plan *p) {
+    if (!p->grad) return;
+    GradState *st = p->grad;
+    if (st->gexec) cudaGraphExecDestroy(st->gexec);
+    st->gexec = nullptr;
+    st->lists_ok = false;
+}
 
 void plan_gradient_free(awe_plan *p) {
     if (!p->grad) return;
+    plan_gradient_graph_drop(p);
     GradState *st = p->grad;
+    if (st->h_rows) cudaFreeHost(st->h_rows);
     for (void *ptr : {(void *)st->slots, st->ckpt, (void *)st->scales, (void *)st->amax, (void *)st->X, (void *)st->Y,
                       (void *)st->kap, (void *)st->G, (void *)st->dat, (void *)st->r, (void *)st->row_sum,
                       (void *)st->vr, (void *)st->gbuf, (void *)st->rc_start, (void *)st->sc_start,
@@ -322,36 +340,14 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
     const long long cells = g.cells();
     const size_t bytes = (size_t)cells * sizeof(float);
     float *dat = d_dsyn ? d_dsyn : st->dat;
-    long long launches = 0;
-
-    // 1. forward with checkpoints of both levels at the start of every segment
-    StepHook hook = [&](int it, const float *prev, const float *cur, cudaStream_t ss) -> awe_status {
-        if (it % T != 0) return AWE_OK;
-        const int seg = it / T;
-        AWE_TRY(ckpt_store(p, 2 * seg, prev, ss));
-        AWE_TRY(ckpt_store(p, 2 * seg + 1, cur, ss));
-        return AWE_OK;
-    };
-    AWE_TRY(planB_run_hooked(p, d_wav, ncs, dat, nullptr, s, &hook));
-    launches += p->launches;
-
-    // 2. residual and misfit (FP64 per row, summed in row order on the host);
-    // an image back-propagates the recorded data themselves
-    std::vector<double> rows;
-    if (image < 0) {
-        launch_residual(dat, d_dobs, st->r, p->nsmp, p->nr, st->row_sum, s);
-        rows.resize(p->nsmp);
-        CUDA_TRY(cudaMemcpyAsync(rows.data(), st->row_sum, rows.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
-    } else {
-        CUDA_TRY(cudaMemcpyAsync(st->r, d_dobs, (size_t)p->nsmp * p->nr * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    if (st->h_rows_n < (size_t)p->nsmp) {
+        if (st->h_rows) cudaFreeHost(st->h_rows);
+        st->h_rows = nullptr;
+        st->h_rows_n = 0;
+        CUDA_TRY(cudaMallocHost((void **)&st->h_rows, (size_t)p->nsmp * sizeof(double)));
+        st->h_rows_n = (size_t)p->nsmp;
     }
     const bool xcorr = image == AWE_IMAGE_XCORR;
-
-    // 3. adjoint sweep
-    CUDA_TRY(cudaMemsetAsync(st->X, 0, bytes, s));
-    CUDA_TRY(cudaMemsetAsync(st->Y, 0, bytes, s));
-    CUDA_TRY(cudaMemsetAsync(st->G, 0, (size_t)cells * sizeof(float2), s));
-    if (st->kap) CUDA_TRY(cudaMemsetAsync(st->kap, 0, bytes, s));
     const StepBParams sp = stepB_params(p);
     const bool sponge = d.dabc && !d.hybrid;
     AdjParams ap{};
@@ -369,9 +365,12 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
     // follows the step
     const bool fuse_pts = !st->tma && !st->kap && cells <= (1LL << 24);
     if (fuse_pts) {
-        const int nc = d.ndim == 3 ? 8 : 4;
-        AWE_TRY(build_cell_lists(p, p->h_rec, nc, &st->rc_start, &st->rc_ent, &st->rc_cap, s));
-        AWE_TRY(build_cell_lists(p, p->h_src, nc, &st->sc_start, &st->sc_ent, &st->sc_cap, s));
+        if (!st->lists_ok) {
+            const int nc = d.ndim == 3 ? 8 : 4;
+            AWE_TRY(build_cell_lists(p, p->h_rec, nc, &st->rc_start, &st->rc_ent, &st->rc_cap, s));
+            AWE_TRY(build_cell_lists(p, p->h_src, nc, &st->sc_start, &st->sc_ent, &st->sc_cap, s));
+            st->lists_ok = true;
+        }
         ap.rc_start = st->rc_start;
         ap.rc_ent = st->rc_ent;
         ap.sc_start = st->sc_start;
@@ -379,6 +378,36 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
         ap.ncs = ncs;
         ap.one_wavelet = ncs == 1;
     }
+
+    // the whole gradient as stream work on `s`
+    auto seq = [&](cudaStream_t s, long long &launches) -> awe_status {
+
+    // 1. forward with checkpoints of both levels at the start of every segment
+    StepHook hook = [&](int it, const float *prev, const float *cur, cudaStream_t ss) -> awe_status {
+        if (it % T != 0) return AWE_OK;
+        const int seg = it / T;
+        AWE_TRY(ckpt_store(p, 2 * seg, prev, ss));
+        AWE_TRY(ckpt_store(p, 2 * seg + 1, cur, ss));
+        return AWE_OK;
+    };
+    AWE_TRY(planB_run_hooked(p, d_wav, ncs, dat, nullptr, s, &hook));
+    launches += p->launches;
+
+    // 2. residual and misfit (FP64 per row, summed in row order on the host);
+    // an image back-propagates the recorded data themselves
+    if (image < 0) {
+        launch_residual(dat, d_dobs, st->r, p->nsmp, p->nr, st->row_sum, s);
+        CUDA_TRY(cudaMemcpyAsync(st->h_rows, st->row_sum, (size_t)p->nsmp * sizeof(double), cudaMemcpyDeviceToHost,
+                                 s));
+    } else {
+        CUDA_TRY(cudaMemcpyAsync(st->r, d_dobs, (size_t)p->nsmp * p->nr * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    }
+
+    // 3. adjoint sweep
+    CUDA_TRY(cudaMemsetAsync(st->X, 0, bytes, s));
+    CUDA_TRY(cudaMemsetAsync(st->Y, 0, bytes, s));
+    CUDA_TRY(cudaMemsetAsync(st->G, 0, (size_t)cells * sizeof(float2), s));
+    if (st->kap) CUDA_TRY(cudaMemsetAsync(st->kap, 0, bytes, s));
     float *X = st->X, *Y = st->Y;
     const CUtensorMap *xmap = &st->x_tile, *ymap = &st->y_tile;
     for (int seg = st->nseg - 1; seg >= 0; seg--) {
@@ -451,9 +480,53 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
     if (xcorr) launch_image_cut(st->G, g, p->nbd, d.n, d.ndim, d_grad, s);
     else launch_grad_fold(st->G, p->vel, d.dt, g, p->nbd, d.n, d.ndim, d_grad, s);
     launches++;
+    return AWE_OK;
+    };  // seq
+
+    // Without the TMA path (whose work-counter bases are host state) and
+    // without snapshot delivery or profiling, the sequence is captured once as
+    // a CUDA graph and replayed while its buffers and settings stay the same
+    // (what matters for launch-bound 2D grids).
+    const bool graph = !st->tma && !p->snap_cb && !p->profile;
+    long long launches = 0;
+    if (graph) {
+        const void *key[4] = {d_wav, d_dobs, d_grad, dat};
+        bool same = st->gexec && st->g_ncs == ncs && st->g_image == image;
+        for (int q = 0; q < 4; q++) same = same && st->g_key[q] == key[q];
+        if (!same) {
+            if (st->gexec) cudaGraphExecDestroy(st->gexec);
+            st->gexec = nullptr;
+            cudaStream_t cs;
+            CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+            cudaGraph_t gr = nullptr;
+            awe_status rs = AWE_OK;
+            cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                rs = seq(cs, launches);
+                e = cudaStreamEndCapture(cs, &gr);
+            }
+            if (rs == AWE_OK && e == cudaSuccess) e = cudaGraphInstantiate(&st->gexec, gr, 0);
+            if (gr) cudaGraphDestroy(gr);
+            cudaStreamDestroy(cs);
+            if (rs != AWE_OK) return rs;
+            if (e != cudaSuccess) {
+                st->gexec = nullptr;
+                set_error("CUDA graph capture of the gradient failed: %s", cudaGetErrorString(e));
+                return AWE_ERR_CUDA;
+            }
+            for (int q = 0; q < 4; q++) st->g_key[q] = key[q];
+            st->g_ncs = ncs;
+            st->g_image = image;
+            st->g_launches = launches;
+        }
+        CUDA_TRY(cudaGraphLaunch(st->gexec, s));
+        launches = st->g_launches;
+    } else {
+        AWE_TRY(seq(s, launches));
+    }
     CUDA_TRY(cudaStreamSynchronize(s));
     double J = 0;
-    for (double v : rows) J += 0.5 * v;
+    for (int q = 0; image < 0 && q < p->nsmp; q++) J += 0.5 * st->h_rows[q];
     *misfit = J;
     p->launches = launches;
     return AWE_OK;

@@ -86,6 +86,9 @@ struct awe_plan {
     long long g_launches = 0;
     float *stage_wav = nullptr, *stage_dat = nullptr;  // awe_forward's device staging buffers
     size_t stage_wav_bytes = 0, stage_dat_bytes = 0;
+    float *stage_dsyn = nullptr;  // awe_gradient / awe_rtm staging (with stage_wav, stage_dat)
+    double *stage_grad = nullptr;
+    size_t stage_dsyn_bytes = 0, stage_grad_bytes = 0;
 
     // misfit gradient state (allocated by the first awe_gradient call)
     awe::GradState *grad = nullptr;
@@ -145,6 +148,8 @@ constexpr int kFusedSources = 8;
 awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *d_dobs, const awe_grad_opts &o,
                          double *d_grad, double *misfit, float *d_dsyn, cudaStream_t s, int image = -1);
 void plan_gradient_free(awe_plan *p);
+// drops the gradient's captured graph and its per-cell point lists
+void plan_gradient_graph_drop(awe_plan *p);
 
 awe_status planA_init(awe_plan *p);
 awe_status planA_model(awe_plan *p, const float *vel, const float *rfl);
