@@ -56,8 +56,11 @@ struct GradState {
     double *h_rows = nullptr;
     size_t h_rows_n = 0;
     cudaGraphExec_t gexec = nullptr;
+    // settings of the captured graph, or of the last direct run (captured when
+    // a second call repeats them: a one-off call pays no capture)
     const void *g_key[4] = {nullptr, nullptr, nullptr, nullptr};
     int g_ncs = 0, g_image = -2;
+    bool g_seen = false;
     long long g_launches = 0;
 };
 
@@ -66,6 +69,7 @@ void plan_gradient_graph_drop(awe_plan *p) {
     GradState *st = p->grad;
     if (st->gexec) cudaGraphExecDestroy(st->gexec);
     st->gexec = nullptr;
+    st->g_seen = false;
     st->lists_ok = false;
 }
 
@@ -489,13 +493,19 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
     // (what matters for launch-bound 2D grids).
     const bool graph = !st->tma && !p->snap_cb && !p->profile;
     long long launches = 0;
-    if (graph) {
-        const void *key[4] = {d_wav, d_dobs, d_grad, dat};
-        bool same = st->gexec && st->g_ncs == ncs && st->g_image == image;
-        for (int q = 0; q < 4; q++) same = same && st->g_key[q] == key[q];
-        if (!same) {
-            if (st->gexec) cudaGraphExecDestroy(st->gexec);
-            st->gexec = nullptr;
+    const void *key[4] = {d_wav, d_dobs, d_grad, dat};
+    bool same = st->g_ncs == ncs && st->g_image == image;
+    for (int q = 0; q < 4; q++) same = same && st->g_key[q] == key[q];
+    if (graph && !(same && (st->gexec || st->g_seen))) {  // new settings: run directly and remember them
+        if (st->gexec) cudaGraphExecDestroy(st->gexec);
+        st->gexec = nullptr;
+        for (int q = 0; q < 4; q++) st->g_key[q] = key[q];
+        st->g_ncs = ncs;
+        st->g_image = image;
+        st->g_seen = true;
+        AWE_TRY(seq(s, launches));
+    } else if (graph && (st->gexec || st->g_seen)) {  // repeated settings: capture once, then replay
+        if (!st->gexec) {
             cudaStream_t cs;
             CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
             cudaGraph_t gr = nullptr;
@@ -514,9 +524,6 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
                 set_error("CUDA graph capture of the gradient failed: %s", cudaGetErrorString(e));
                 return AWE_ERR_CUDA;
             }
-            for (int q = 0; q < 4; q++) st->g_key[q] = key[q];
-            st->g_ncs = ncs;
-            st->g_image = image;
             st->g_launches = launches;
         }
         CUDA_TRY(cudaGraphLaunch(st->gexec, s));
