@@ -32,6 +32,54 @@ constexpr int kColMaxN1 = 2048;  // ring of 8 slots of 3 columns: 197 KB of shar
 __host__ __device__ inline int col_pitch(int n1) { return n1 + 8; }           // cur column: 4 zeros each end
 __host__ __device__ inline int col_slot(int n1) { return col_pitch(n1) + 2 * n1; }  // + prv + vel columns
 
+// Rarely taken parts of the column loops, kept out of line so the nine
+// unrolled copies of the loop body stay small.
+
+// forward: the shot's source terms on a 4-cell strip (cells cell0 .. cell0 + 3)
+__device__ __noinline__ float4 col_sources_fwd(float4 o, float4 v4, const GeoPoint *src, int ns, float dd, int n1,
+                                               long long cell0) {
+    float r[4] = {o.x, o.y, o.z, o.w};
+    const float v[4] = {v4.x, v4.y, v4.z, v4.w};
+    for (int sidx = 0; sidx < ns; sidx++) {
+        const GeoPoint gp = src[sidx];
+#pragma unroll
+        for (int cc = 0; cc < 4; cc++) {
+            const long long d = gp.base + (cc & 1) + (cc >> 1) * (long long)n1 - cell0;
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+                if (d == i) r[i] = r[i] + (dd * gp.w[cc]) * v[i];
+        }
+    }
+    return make_float4(r[0], r[1], r[2], r[3]);
+}
+
+// adjoint: the shot's source terms of the gradient on a 2-cell strip
+__device__ __noinline__ float4 col_sources_adj(float4 ga, float2 nu, const GeoPoint *src, int ns, float dd, int n1,
+                                               long long cell0) {
+    float2 g[2] = {make_float2(ga.x, ga.y), make_float2(ga.z, ga.w)};
+    const float v[2] = {nu.x, nu.y};
+    for (int sidx = 0; sidx < ns; sidx++) {
+        const GeoPoint gp = src[sidx];
+#pragma unroll
+        for (int cc = 0; cc < 4; cc++) {
+            const long long d = gp.base + (cc & 1) + (cc >> 1) * (long long)n1 - cell0;
+#pragma unroll
+            for (int i = 0; i < 2; i++)
+                if (d == i) g[i] = gsum_add_prod(g[i], v[i], dd * gp.w[cc]);
+        }
+    }
+    return make_float4(g[0].x, g[0].y, g[1].x, g[1].y);
+}
+
+// tid 0 after a timed-out wait: waits (bounded) for every copy still in
+// flight of the item (columns s .. issued - 1)
+__device__ __noinline__ void col_drain(uint64_t *full, int ring, int slot0, uint32_t ph0, int s, int issued) {
+    for (int t = s; t < issued; t++) {
+        const int tt = slot0 + t;
+        mbar_wait(&full[tt % ring], ph0 ^ (uint32_t)((tt / ring) & 1), CSPIN);
+    }
+}
+
 __global__ void __launch_bounds__(512) k_batch2d_col(const BatchShot *__restrict__ shots,
                                                       const int4 *__restrict__ items, int nitems, const BatchStep p,
                                                       int L, int *err) {
@@ -186,18 +234,10 @@ __global__ void __launch_bounds__(512) k_batch2d_col(const BatchShot *__restrict
 #pragma unroll
                         for (int k = 0; k < 4; k++) near = near || (unsigned)(x - scol[k]) <= 2u;
                         if (sh.ns > 0 && near) {  // source corners of this shot in this 4-cell strip
-                            const float dd = p.wav[p.it];
-                            for (int sidx = 0; sidx < sh.ns; sidx++) {
-                                const GeoPoint gp = p.src[sh.src0 + sidx];
-#pragma unroll
-                                for (int cc = 0; cc < 4; cc++) {
-                                    const long long n = gp.base + (cc & 1) + (cc >> 1) * (long long)n1;
-                                    const long long d = n - ((long long)x * n1 + zb);
-#pragma unroll
-                                    for (int i = 0; i < 4; i++)
-                                        if (d == i) o[i] = o[i] + (dd * gp.w[cc]) * v4[i];
-                                }
-                            }
+                            const float4 r = col_sources_fwd(make_float4(o[0], o[1], o[2], o[3]), vv,
+                                                             p.src + sh.src0, sh.ns, p.wav[p.it], n1,
+                                                             (long long)x * n1 + zb);
+                            o[0] = r.x, o[1] = r.y, o[2] = r.z, o[3] = r.w;
                         }
                         if (damp) {
 #pragma unroll
@@ -208,13 +248,7 @@ __global__ void __launch_bounds__(512) k_batch2d_col(const BatchShot *__restrict
                     }
                     if (__syncthreads_or(bad)) {
                         // drain: wait (bounded) for every copy still in flight, then leave
-                        if (tid == 0) {
-                            const int issued = min(S, max(CRING, s - CNOP + CRING));
-                            for (int t = s; t < issued; t++) {
-                                const int tt = slot0 + t;
-                                mbar_wait(&full[tt % CRING], ph0 ^ (uint32_t)((tt / CRING) & 1), CSPIN);
-                            }
-                        }
+                        if (tid == 0) col_drain(full, CRING, slot0, ph0, s, min(S, max(CRING, s - CNOP + CRING)));
                         __syncthreads();
                         return;
                     }
@@ -408,31 +442,18 @@ __global__ void __maxnreg__(96) k_batch2d_col_adj(const BatchShot *__restrict__ 
 #pragma unroll
                         for (int k = 0; k < 4; k++) near = near || (unsigned)(x - scol[k]) <= 2u;
                         if (sh.ns > 0 && near) {  // source term of the gradient
-                            const float dd = p.wav[p.it];
-                            const long long cell0 = (long long)x * n1 + zb;
-                            for (int sidx = 0; sidx < sh.ns; sidx++) {
-                                const GeoPoint gp = p.src[sh.src0 + sidx];
-#pragma unroll
-                                for (int cc = 0; cc < 4; cc++) {
-                                    const long long d = gp.base + (cc & 1) + (cc >> 1) * (long long)n1 - cell0;
-#pragma unroll
-                                    for (int i = 0; i < 2; i++)
-                                        if (d == i) ga[i] = gsum_add_prod(ga[i], nu[i], dd * gp.w[cc]);
-                                }
-                            }
+                            const float4 r = col_sources_adj(make_float4(ga[0].x, ga[0].y, ga[1].x, ga[1].y), nv2,
+                                                             p.src + sh.src0, sh.ns, p.wav[p.it], n1,
+                                                             (long long)x * n1 + zb);
+                            ga[0] = make_float2(r.x, r.y);
+                            ga[1] = make_float2(r.z, r.w);
                         }
                         *reinterpret_cast<float2 *>(p.Y + gi) = make_float2(mu[0], mu[1]);
                         __stcs(reinterpret_cast<float4 *>(p.G + gi), make_float4(ga[0].x, ga[0].y, ga[1].x, ga[1].y));
                     }
                     if (__syncthreads_or(bad)) {
                         cp_async_wait<0>();
-                        if (tid == 0) {
-                            const int issued = min(S, max(ARING, s - CNOP + ARING));
-                            for (int t = s; t < issued; t++) {
-                                const int tt = slot0 + t;
-                                mbar_wait(&full[tt % ARING], ph0 ^ (uint32_t)((tt / ARING) & 1), CSPIN);
-                            }
-                        }
+                        if (tid == 0) col_drain(full, ARING, slot0, ph0, s, min(S, max(ARING, s - CNOP + ARING)));
                         __syncthreads();
                         return;
                     }
