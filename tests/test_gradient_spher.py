@@ -112,3 +112,34 @@ def test_reflectivity_injection_is_refused():
         p.set_geometry(sou, rec)
         with pytest.raises(awe.AweError):
             p.gradient(wav, np.zeros((par["nt"], rec.shape[0]), np.float32))
+
+
+@pytest.mark.gpu
+def test_several_shots_sum_the_single_shot_gradients():
+    """awe_set_shots (the c4 track's layout): the gradient of three shots
+    is the sum of the three single-shot gradients, the misfit the sum of
+    theirs, the synthetic data each shot's own columns; awe_set_geometry
+    afterwards goes back to one shot."""
+    import wavefield_imaging_gb300 as awe
+
+    par, vel, wav, sou, rec, vtrue = spher_grad_case(n=(46, 20, 20), nt=80)
+    d = par["d"]
+    shots = [(sou + np.array([[0.0, k * 3 * d[2], 0.0]], np.float32), rec[: 7 - k]) for k in range(3)]
+    dobs = [_dobs(par, vtrue, wav, s_, r_) for s_, r_ in shots]
+    with awe.Plan(spher_desc(par)) as p:
+        p.set_model(vel)
+        gsum, Jsum, dsyn = np.zeros_like(vel, np.float64), 0.0, []
+        for (s_, r_), d_ in zip(shots, dobs):
+            p.set_geometry(s_, r_)
+            g, J, ds = p.gradient(wav, d_, ckpt_format=awe.CKPT_FP32, return_dsyn=True)
+            gsum += g
+            Jsum += J
+            dsyn.append(ds)
+        p.set_shots(shots)
+        gm, Jm, dsm = p.gradient(wav, np.concatenate(dobs, axis=1), ckpt_format=awe.CKPT_FP32, return_dsyn=True)
+        p.set_geometry(*shots[1])
+        d1 = p.forward(wav)
+    assert rel_l2(gm, gsum) <= 1e-6  # coincident receiver corners add by atomics
+    assert abs(Jm - Jsum) <= 1e-9 * Jsum
+    np.testing.assert_array_equal(dsm, np.concatenate(dsyn, axis=1))
+    np.testing.assert_array_equal(d1, dsyn[1])

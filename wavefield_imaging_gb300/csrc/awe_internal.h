@@ -176,6 +176,7 @@ constexpr float kBfpTiny = 1e-30f;  // blocks with max |v| <= this are stored as
 void launch_ckpt_store_bfp(const float *u, long long n, short *q, float *scale, int grid, cudaStream_t s);
 void launch_ckpt_load_bfp(const short *q, const float *scale, long long n, float *u, int grid, cudaStream_t s);
 // image on the model grid: the padded grid's model window of G
+void launch_add_f64(double *dst, const double *src, long long n, cudaStream_t s);
 void launch_image_cut(const float2 *G, const Grid &g, int nb, const int *n, int nd, double *out, cudaStream_t s);
 // vel2: v^2 dt^2 per padded cell, or the velocity itself (raw_v: c = dt^2 v^2)
 void launch_grad_fold(const float2 *G, const float *vel2, float dt, const Grid &g, int nb, const int *n, int nd,

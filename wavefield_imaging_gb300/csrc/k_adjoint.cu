@@ -18,6 +18,8 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "awe_internal.h"
 #include "gsum.cuh"
 
@@ -521,6 +523,16 @@ __global__ void k_image_cut(const float2 *__restrict__ G, Grid g, int nb, int m1
     if (t >= (long long)m1 * m2 * m3) return;
     const int j1 = (int)(t % m1), j2 = (int)((t / m1) % m2), j3 = (int)(t / ((long long)m1 * m2));
     out[t] = gsum_value(G[((long long)(nd == 3 ? j3 + nb : 0) * g.n2 + j2 + nb) * g.n1 + j1 + nb]);
+}
+
+// dst += src (gradients of several shots)
+__global__ void k_add_f64(double *__restrict__ dst, const double *__restrict__ src, long long n) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] += src[i];
+}
+
+void launch_add_f64(double *dst, const double *src, long long n, cudaStream_t s) {
+    if (n > 0) k_add_f64<<<(unsigned)std::min<long long>((n + 255) / 256, 4096), 256, 0, s>>>(dst, src, n);
 }
 
 void launch_image_cut(const float2 *G, const Grid &g, int nb, const int *n, int nd, double *out, cudaStream_t s) {

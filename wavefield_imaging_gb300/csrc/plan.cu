@@ -314,6 +314,22 @@ awe_status awe_set_model(awe_plan *p, const float *vel, const float *den, const 
     return st;
 }
 
+// back to one shot after awe_set_shots: one field per time level
+static awe_status single_shot(awe_plan *p, int ns, int nr) {
+    p->shot_ns.assign(1, ns);
+    p->shot_nr.assign(1, nr);
+    if (p->pa.nshot <= 1) return AWE_OK;
+    const size_t bytes = (size_t)p->g.cells() * sizeof(float);
+    for (int k = 0; k < 2; k++) {
+        dev_free(p, p->u[k]);
+        p->u[k] = nullptr;
+        const awe_status st = dev_alloc(p, (void **)&p->u[k], bytes);
+        if (st != AWE_OK) return st;
+    }
+    p->pa.nshot = 1;
+    return AWE_OK;
+}
+
 awe_status awe_set_geometry(awe_plan *p, int ns, const float *sou, int nr, const float *rec) {
     if (!p || ns < 0 || nr < 0 || (ns > 0 && !sou) || (nr > 0 && !rec)) {
         set_error("bad geometry arguments");
@@ -323,6 +339,7 @@ awe_status awe_set_geometry(awe_plan *p, int ns, const float *sou, int nr, const
     CUDA_TRY(cudaSetDevice(p->device));
     set_move_mode(p, -1, 1, 1);
     awe_status st = set_geometry_common(p, ns, sou, nr, rec);
+    if (st == AWE_OK) st = single_shot(p, ns, nr);
     if (st == AWE_OK) p->geom_set = true;
     return st;
 }
@@ -367,6 +384,8 @@ awe_status awe_set_moving_geometry(awe_plan *p, int ns, int nst, const float *so
     p->ns = ns;
     p->nr = nr;
     set_move_mode(p, mode, nst, nrt);
+    st = single_shot(p, ns, nr);
+    if (st != AWE_OK) return st;
     p->geom_set = true;
     return AWE_OK;
 }
@@ -409,6 +428,8 @@ awe_status awe_set_shots(awe_plan *p, int nshots, const int *ns, const float *so
     }
     if (NS) CUDA_TRY(cudaMemcpy(p->src, p->h_src.data(), NS * sizeof(GeoPoint), cudaMemcpyHostToDevice));
     if (NR) CUDA_TRY(cudaMemcpy(p->rec, p->h_rec.data(), NR * sizeof(GeoPoint), cudaMemcpyHostToDevice));
+    p->shot_ns.assign(ns, ns + nshots);
+    p->shot_nr.assign(nr, nr + nshots);
     if (nshots != p->pa.nshot) {
         for (int k = 0; k < 2; k++) {
             dev_free(p, p->u[k]);

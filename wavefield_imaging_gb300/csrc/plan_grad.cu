@@ -52,6 +52,7 @@ struct GradState {
     int2 *rc_ent = nullptr, *sc_ent = nullptr;
     size_t rc_cap = 0, sc_cap = 0;
     bool lists_ok = false;  // cleared when the geometry changes
+    size_t nd_cap = 0;      // trace samples dat and r hold
     // misfit rows (pinned, written by the stream) and the captured gradient
     double *h_rows = nullptr;
     size_t h_rows_n = 0;
@@ -88,7 +89,8 @@ void plan_gradient_free(awe_plan *p) {
 }
 
 static awe_status grad_alloc(awe_plan *p, int T, int fmt) {
-    if (p->grad && p->grad->T == T && p->grad->fmt == fmt) return AWE_OK;
+    const size_t nd = (size_t)p->nsmp * (p->nr > 0 ? p->nr : 1);
+    if (p->grad && p->grad->T == T && p->grad->fmt == fmt && p->grad->nd_cap >= nd) return AWE_OK;
     plan_gradient_free(p);
     GradState *st = new GradState();
     p->grad = st;
@@ -108,7 +110,7 @@ static awe_status grad_alloc(awe_plan *p, int T, int fmt) {
     AWE_TRY(dev_alloc(p, (void **)&st->Y, cells * sizeof(float)));
     if (d.ndim == 3 && d.dabc && d.scheme == AWE_SCHEME_CPU) AWE_TRY(dev_alloc(p, (void **)&st->kap, cells * sizeof(float)));
     AWE_TRY(dev_alloc(p, (void **)&st->G, cells * sizeof(float2)));
-    const size_t nd = (size_t)p->nsmp * (p->nr > 0 ? p->nr : 1);
+    st->nd_cap = nd;
     AWE_TRY(dev_alloc(p, (void **)&st->dat, nd * sizeof(float)));
     AWE_TRY(dev_alloc(p, (void **)&st->r, nd * sizeof(float)));
     AWE_TRY(dev_alloc(p, (void **)&st->row_sum, (size_t)p->nsmp * sizeof(double)));
@@ -218,18 +220,10 @@ static awe_status ckpt_load(awe_plan *p, int idx, float *u, cudaStream_t s) {
 // sweep j = nt .. 0 keeps z_{j+1} and z_{j+2} in two buffers:
 //   z_j = W M (L^T(I c z_{j+1}) + 2 z_{j+1} - W z_{j+2}) + W M R^T r_{j-1},
 //   dJ/dc += z_{j+1} L(A_j),  c = dt^2 v^2, folded to dJ/dm = dJ/dc (-c^2/dt^2).
-static awe_status plan_gradient_spher(awe_plan *p, const float *d_wav, int ncs, const float *d_dobs, int T, int fmt,
-                                      double *d_grad, double *misfit, float *d_dsyn, cudaStream_t s) {
+static awe_status gradient_spher_one(awe_plan *p, const float *d_wav, int ncs, const float *d_dobs, int T, int fmt,
+                                     double *d_grad, double *misfit, float *d_dsyn, cudaStream_t s) {
     const awe_desc &d = p->d;
     const StepAParams &pa = p->pa;
-    if (d.expl) {
-        set_error("awe_gradient: the reflectivity-scaled injection (expl=y) depends on the model; use expl=n");
-        return AWE_ERR_UNSUPPORTED;
-    }
-    if (p->move_mode >= 0 || pa.nshot > 1) {
-        set_error("awe_gradient: one shot on a fixed geometry");
-        return AWE_ERR_UNSUPPORTED;
-    }
     AWE_TRY(grad_alloc(p, T, fmt));
     GradState *st = p->grad;
     const Grid &g = p->g;
@@ -288,6 +282,101 @@ static awe_status plan_gradient_spher(awe_plan *p, const float *d_wav, int ncs, 
     *misfit = J;
     p->launches = launches;
     return AWE_OK;
+}
+
+// Several shots (awe_set_shots: points of shot s address field s): one shot
+// after the other on the single-shot machinery, with the shot's points
+// (bases moved back to field 0) and its columns of the data; gradients and
+// misfits summed.
+static awe_status plan_gradient_spher(awe_plan *p, const float *d_wav, int ncs, const float *d_dobs, int T, int fmt,
+                                      double *d_grad, double *misfit, float *d_dsyn, cudaStream_t s) {
+    const awe_desc &d = p->d;
+    if (d.expl) {
+        set_error("awe_gradient: the reflectivity-scaled injection (expl=y) depends on the model; use expl=n");
+        return AWE_ERR_UNSUPPORTED;
+    }
+    if (p->move_mode >= 0) {
+        set_error("awe_gradient: fixed sources and receivers only");
+        return AWE_ERR_UNSUPPORTED;
+    }
+    const int nshot = p->pa.nshot > 1 ? p->pa.nshot : 1;
+    if (nshot == 1) return gradient_spher_one(p, d_wav, ncs, d_dobs, T, fmt, d_grad, misfit, d_dsyn, s);
+    const long long cells = p->g.cells();
+    const int NS = p->ns, NR = p->nr;
+    int max_nr = 1;
+    for (int v : p->shot_nr) max_nr = std::max(max_nr, v);
+    std::vector<GeoPoint> pts(p->h_src);
+    pts.insert(pts.end(), p->h_rec.begin(), p->h_rec.end());
+    {
+        int a = 0;
+        for (int q = 0; q < nshot; q++)
+            for (int i = 0; i < p->shot_ns[q]; i++) pts[a++].base -= q * cells;
+        for (int q = 0; q < nshot; q++)
+            for (int i = 0; i < p->shot_nr[q]; i++) pts[a++].base -= q * cells;
+    }
+    const size_t mcells = (size_t)d.n[0] * d.n[1] * d.n[2];
+    GeoPoint *d_pts = nullptr;
+    float *dobs_s = nullptr, *dsyn_s = nullptr;
+    double *grad_s = nullptr;
+    GeoPoint *src0 = p->src, *rec0 = p->rec;
+    auto cleanup = [&]() {
+        p->src = src0;
+        p->rec = rec0;
+        p->ns = NS;
+        p->nr = NR;
+        p->pa.nshot = nshot;
+        dev_free(p, d_pts);
+        dev_free(p, dobs_s);
+        dev_free(p, dsyn_s);
+        dev_free(p, grad_s);
+    };
+    awe_status st = dev_alloc(p, (void **)&d_pts, std::max<size_t>(pts.size(), 1) * sizeof(GeoPoint));
+    if (st == AWE_OK) st = dev_alloc(p, (void **)&dobs_s, (size_t)p->nsmp * max_nr * sizeof(float));
+    if (st == AWE_OK && d_dsyn) st = dev_alloc(p, (void **)&dsyn_s, (size_t)p->nsmp * max_nr * sizeof(float));
+    if (st == AWE_OK) st = dev_alloc(p, (void **)&grad_s, mcells * sizeof(double));
+    if (st == AWE_OK && !pts.empty() &&
+        cudaMemcpyAsync(d_pts, pts.data(), pts.size() * sizeof(GeoPoint), cudaMemcpyHostToDevice, s) != cudaSuccess) {
+        set_error("awe_gradient: point upload failed");
+        st = AWE_ERR_CUDA;
+    }
+    if (st == AWE_OK && cudaMemsetAsync(d_grad, 0, mcells * sizeof(double), s) != cudaSuccess) st = AWE_ERR_CUDA;
+    p->pa.nshot = 1;
+    p->nr = max_nr;  // sizes the gradient's trace buffers for every shot
+    if (st == AWE_OK) st = grad_alloc(p, T, fmt);
+    double J = 0;
+    int s0 = 0, r0 = 0;
+    for (int q = 0; q < nshot && st == AWE_OK; q++) {
+        const int ns = p->shot_ns[q], nr = p->shot_nr[q];
+        p->src = d_pts + s0;
+        p->ns = ns;
+        p->rec = d_pts + NS + r0;
+        p->nr = nr;
+        if (nr > 0 && cudaMemcpy2DAsync(dobs_s, (size_t)nr * sizeof(float), d_dobs + r0, (size_t)NR * sizeof(float),
+                                        (size_t)nr * sizeof(float), p->nsmp, cudaMemcpyDeviceToDevice,
+                                        s) != cudaSuccess) {
+            set_error("awe_gradient: data gather failed");
+            st = AWE_ERR_CUDA;
+            break;
+        }
+        double Jq = 0;
+        st = gradient_spher_one(p, d_wav, ncs, dobs_s, T, fmt, grad_s, &Jq, dsyn_s, s);
+        if (st != AWE_OK) break;
+        launch_add_f64(d_grad, grad_s, (long long)mcells, s);
+        if (d_dsyn && nr > 0 &&
+            cudaMemcpy2DAsync(d_dsyn + r0, (size_t)NR * sizeof(float), dsyn_s, (size_t)nr * sizeof(float),
+                              (size_t)nr * sizeof(float), p->nsmp, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+            set_error("awe_gradient: data scatter failed");
+            st = AWE_ERR_CUDA;
+            break;
+        }
+        J += Jq;
+        s0 += ns;
+        r0 += nr;
+    }
+    if (st == AWE_OK && cudaStreamSynchronize(s) != cudaSuccess) st = AWE_ERR_CUDA;
+    cleanup();
+    *misfit = J;
+    return st;
 }
 
 awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *d_dobs, const awe_grad_opts &o,

@@ -42,6 +42,7 @@ struct awe_plan {
 
     // geometry
     int ns = 0, nr = 0;
+    std::vector<int> shot_ns, shot_nr;  // points per shot (awe_set_shots; one shot: {ns}, {nr})
     awe::GeoPoint *src = nullptr, *rec = nullptr;
     long long *corner_off = nullptr;  // device [8]
     long long h_corner_off[8] = {0};
