@@ -344,6 +344,7 @@ static awe_status plan_gradient_spher(awe_plan *p, const float *d_wav, int ncs, 
     p->nr = max_nr;  // sizes the gradient's trace buffers for every shot
     if (st == AWE_OK) st = grad_alloc(p, T, fmt);
     double J = 0;
+    long long launches = 0;
     int s0 = 0, r0 = 0;
     for (int q = 0; q < nshot && st == AWE_OK; q++) {
         const int ns = p->shot_ns[q], nr = p->shot_nr[q];
@@ -370,12 +371,14 @@ static awe_status plan_gradient_spher(awe_plan *p, const float *d_wav, int ncs, 
             break;
         }
         J += Jq;
+        launches += p->launches + 1;
         s0 += ns;
         r0 += nr;
     }
     if (st == AWE_OK && cudaStreamSynchronize(s) != cudaSuccess) st = AWE_ERR_CUDA;
     cleanup();
     *misfit = J;
+    p->launches = launches;
     return st;
 }
 
