@@ -169,13 +169,15 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes per step-kernel launch from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "k_stepB_3d_o8_c3.txt")
+def profiled_traffic(cells):
+    """DRAM bytes per step-kernel launch: the committed ncu capture's bytes
+    per cell (profiles/k_stepB3_o8_tma_n320.md, 384^3 padded) times the
+    launch's cells, or None without it."""
+    path = os.path.join(ROOT, "profiles", "k_stepB3_o8_tma_n320.md")
     try:
         for line in open(path):
-            if line.startswith("dram_bytes_per_launch_full:"):
-                return float(line.split(":", 1)[1].split()[0])
+            if line.strip().startswith("dram_bytes_per_cell:"):
+                return float(line.split(":", 1)[1].split()[0]) * cells
     except Exception:
         pass
     return None
@@ -336,7 +338,7 @@ def run_ours(args):
     peak, peak_kind = measured_peak()
     avg_kernel_s = (kern_ms / 1e3) / max(kern_n, 1)
     achieved = BYTES_PER_CELL * cells / avg_kernel_s / 1e9
-    traffic = profiled_traffic()
+    traffic = profiled_traffic(cells) if args.precision == "fast" else None
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
@@ -349,6 +351,9 @@ def run_ours(args):
                    "d2h_bytes_per_step": int(plan.nsmp * nr * 4)},
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak, "traffic": traffic,
+                        "traffic_source": ("ncu DRAM bytes per cell of a 384^3-padded launch of the same kernel "
+                                           "(profiles/k_stepB3_o8_tma_n320.md) x this launch's cells"
+                                           if traffic else None),
                         "kernel": ("k_stepB3_o8 (TMA-staged, 3D 8th order)" if plan.step_kernel == "tma3d"
                                    else "k_stepB (one thread per cell, 3D 8th order)"),
                         "peak_source": peak_kind, "avg_launch_us": avg_kernel_s * 1e6,
