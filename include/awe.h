@@ -214,7 +214,10 @@ typedef struct {
  * m = 1/v^2 on the model grid, for the plan's model and geometry.  Scheme
  * AWE_SCHEME_CPU (2D or 3D, any order, sponge and one-way ABC, free surface),
  * no density, no hybrid ABC; or the spherical 3D AWE_SCHEME_GPU scheme of
- * sfAWEFDspher3Dgpu (sponge, free surface; expl=n, one shot, fixed points).
+ * sfAWEFDspher3Dgpu (sponge, free surface; expl=n, fixed points; the shots
+ * of awe_set_shots run one after the other on one set of checkpoint
+ * buffers, dobs holding every shot's receivers as awe_forward writes them,
+ * gradients and misfits summed).
  * The forward runs in AWE_FAST arithmetic.  The
  * boundary coefficients (one-way ABC, sponge) are held at the plan's model.
  * The forward pass stores both time levels every ckpt_every steps (in
