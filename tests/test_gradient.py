@@ -158,3 +158,20 @@ def test_repeated_gradient_replays_the_captured_graph(nd):
             else:
                 assert rel_l2(g, g0) <= 1e-6
     assert again[0][1] != runs[0][1]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nd", [2, 3])
+def test_empty_point_sets(nd):
+    """No receivers: zero misfit and gradient; no sources: zero wavefield,
+    so a zero gradient while the misfit is the data's energy."""
+    import wavefield_imaging_gb300 as awe
+
+    par, vel, wav, sou, rec, vtrue = grad_case(nd, nt=40)
+    with _plan(par, vel, sou, np.zeros((0, nd), np.float32)) as p:
+        g, J = p.gradient(wav, np.zeros((40, 0), np.float32), ckpt_format=awe.CKPT_FP32)
+        assert J == 0.0 and not g.any()
+    with _plan(par, vel, np.zeros((0, nd), np.float32), rec) as p:
+        dobs = np.ones((40, rec.shape[0]), np.float32)
+        g, J = p.gradient(wav, dobs, ckpt_format=awe.CKPT_FP32)
+        assert J == pytest.approx(0.5 * dobs.size) and not g.any()

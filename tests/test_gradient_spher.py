@@ -143,3 +143,21 @@ def test_several_shots_sum_the_single_shot_gradients():
     assert abs(Jm - Jsum) <= 1e-9 * Jsum
     np.testing.assert_array_equal(dsm, np.concatenate(dsyn, axis=1))
     np.testing.assert_array_equal(d1, dsyn[1])
+
+
+@pytest.mark.gpu
+def test_empty_point_sets():
+    """No receivers: zero misfit and gradient; no sources: zero wavefield,
+    so a zero gradient while the misfit is the data's energy."""
+    import wavefield_imaging_gb300 as awe
+
+    par, vel, wav, sou, rec, vtrue = spher_grad_case(n=(46, 20, 20), nt=40)
+    with awe.Plan(spher_desc(par)) as p:
+        p.set_model(vel)
+        p.set_geometry(sou, np.zeros((0, 3), np.float32))
+        g, J = p.gradient(wav, np.zeros((par["nt"], 0), np.float32), ckpt_format=awe.CKPT_FP32)
+        assert J == 0.0 and not g.any()
+        p.set_geometry(np.zeros((0, 3), np.float32), rec)
+        dobs = np.ones((par["nt"], rec.shape[0]), np.float32)
+        g, J = p.gradient(wav, dobs, ckpt_format=awe.CKPT_FP32)
+        assert J == pytest.approx(0.5 * dobs.size) and not g.any()
