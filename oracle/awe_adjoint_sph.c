@@ -20,6 +20,11 @@
  * by the transpose of the edge-replicating padding.  With expl = 1 the
  * injection's reflectivity scale (piecewise constant in v) is held fixed.
  *
+ * Images (the engine's awe_rtm): image = 0 sums z_{j+1} A_j (zero-lag
+ * cross-correlation) and returns the model window of the padded sum; image =
+ * 1 is the gradient formula with the data themselves as the residual (Born
+ * adjoint); image < 0 is the misfit gradient.
+ *
  * Checkpoint emulation: every `every` steps the two levels the engine stores
  * at the start of an iteration (A_{k0-1} and U_{k0}) are rounded as the
  * engine's checkpoint format does (bits 8 / 11 / 24 with one scale per level,
@@ -83,9 +88,9 @@ static void s_lapT_add(const sgrid *g, const double *y, double *out) {
             }
 }
 
-int orc_gpu_spher3d_grad(const orc_gpar *P, const float *vel_in, const double *m_in, const float *wav, int ns,
-                         const float *sou, int nr, const float *rec, const float *dobs, int every, int bits,
-                         double *grad, double *misfit, double *dsyn) {
+static int spher_impl(const orc_gpar *P, const float *vel_in, const double *m_in, const float *wav, int ns,
+                      const float *sou, int nr, const float *rec, const float *dobs, int every, int bits,
+                      double *grad, double *misfit, double *dsyn, int image) {
     const int nra = P->n1, nth = P->n2, nph = P->n3, nt = P->nt;
     const int nb = P->nb < NOPA ? NOPA : P->nb;
     sgrid g;
@@ -199,7 +204,7 @@ int orc_gpu_spher3d_grad(const orc_gpar *P, const float *vel_in, const double *m
             for (int q = 0; q < 8; q++) acc += U[RB(&cr[ir]) + off[q]] * cr[ir].w[q];
             const size_t row = (size_t)k * nr + ir;
             if (dsyn) dsyn[row] = acc;
-            r[row] = acc - dobs[row];
+            r[row] = image < 0 ? acc - dobs[row] : (double)dobs[row]; /* an image back-propagates the data */
         }
     }
     double J = 0;
@@ -235,7 +240,7 @@ int orc_gpu_spher3d_grad(const orc_gpar *P, const float *vel_in, const double *m
                 for (int ith = NOPA; ith < g.n2 - NOPA; ith++)
                     for (int ir = NOPA; ir < g.n1 - NOPA; ir++) {
                         const size_t i = (size_t)iph * sp + (size_t)ith * st + ir;
-                        G[i] += zx[i] * s_lap(&g, Aj, ir, ith, i);
+                        G[i] += zx[i] * (image == 0 ? Aj[i] : s_lap(&g, Aj, ir, ith, i));
                     }
         }
         if (j == 0) break;
@@ -252,7 +257,14 @@ int orc_gpu_spher3d_grad(const orc_gpar *P, const float *vel_in, const double *m
     }
 #undef RB
     memset(grad, 0, (size_t)mn * sizeof(double));
-    for (int iph = 0; iph < g.n3; iph++)
+    for (int iph = 0; iph < g.n3 && image == 0; iph++) /* cross-correlation image: the model window */
+        for (int ith = 0; ith < g.n2; ith++)
+            for (int ir = 0; ir < g.n1; ir++) {
+                const int j1 = ir - nb, j2 = ith - nb, j3 = iph - nb;
+                if (j1 >= 0 && j1 < nra && j2 >= 0 && j2 < nth && j3 >= 0 && j3 < nph)
+                    grad[((size_t)j3 * nth + j2) * nra + j1] = G[(size_t)iph * sp + (size_t)ith * st + ir];
+            }
+    for (int iph = 0; iph < g.n3 && image != 0; iph++)
         for (int ith = 0; ith < g.n2; ith++)
             for (int ir = 0; ir < g.n1; ir++) {
                 const size_t i = (size_t)iph * sp + (size_t)ith * st + ir;
@@ -284,4 +296,17 @@ int orc_gpu_spher3d_grad(const orc_gpar *P, const float *vel_in, const double *m
     free(y);
     free(G);
     return 0;
+}
+
+int orc_gpu_spher3d_grad(const orc_gpar *P, const float *vel_in, const double *m_in, const float *wav, int ns,
+                         const float *sou, int nr, const float *rec, const float *dobs, int every, int bits,
+                         double *grad, double *misfit, double *dsyn) {
+    return spher_impl(P, vel_in, m_in, wav, ns, sou, nr, rec, dobs, every, bits, grad, misfit, dsyn, -1);
+}
+
+/* images of the recorded data `data` (condition 0 cross-correlation, 1 Born) */
+int orc_gpu_spher3d_image(const orc_gpar *P, const float *vel_in, const float *wav, int ns, const float *sou, int nr,
+                          const float *rec, const float *data, int condition, double *image) {
+    double unused = 0;
+    return spher_impl(P, vel_in, NULL, wav, ns, sou, nr, rec, data, 0, 0, image, &unused, NULL, condition);
 }

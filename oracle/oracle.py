@@ -335,6 +335,8 @@ def _adj_lib():
         L.orc_gpu_spher3d_grad.argtypes = [C.POINTER(GPar), fp, dp, fp, C.c_int, fp, C.c_int, fp, fp, C.c_int,
                                            C.c_int, dp, dp, dp]
         L.orc_gpu_spher3d_grad.restype = C.c_int
+        L.orc_gpu_spher3d_image.argtypes = [C.POINTER(GPar), fp, fp, C.c_int, fp, C.c_int, fp, fp, C.c_int, dp]
+        L.orc_gpu_spher3d_image.restype = C.c_int
         _adj = L
     return _adj
 
@@ -441,6 +443,24 @@ def spher3d_gradient(p: dict, vel, wav, sou, rec, dobs, m=None, ckpt_every: int 
     if rc != 0:
         raise ValueError("orc_gpu_spher3d_grad rejected the parameters")
     return grad, J.value, dsyn
+
+
+def spher3d_image(p: dict, vel, wav, sou, rec, data, condition: int):
+    """FP64 images of the spherical GPU-program scheme on its exact adjoint
+    driven by `data` [nt][nrec]: condition 0 = zero-lag cross-correlation
+    (model window), 1 = Born adjoint.  Returns [nph][nth][nr] float64."""
+    q = _gpar_spher(p)
+    vel = np.ascontiguousarray(vel, np.float32)
+    wav = np.ascontiguousarray(wav, np.float32)
+    sou = np.ascontiguousarray(sou, np.float32).reshape(-1, 3)
+    rec = np.ascontiguousarray(rec, np.float32).reshape(-1, 3)
+    data = np.ascontiguousarray(data, np.float32).reshape(q.nt, rec.shape[0])
+    img = np.zeros(vel.shape, np.float64)
+    rc = _adj_lib().orc_gpu_spher3d_image(C.byref(q), _fp(vel), _fp(wav), sou.shape[0], _fp(sou), rec.shape[0],
+                                          _fp(rec), _fp(data), condition, img.ctypes.data_as(C.POINTER(C.c_double)))
+    if rc != 0:
+        raise ValueError("orc_gpu_spher3d_image rejected the parameters")
+    return img
 
 
 def spher3d_fp64(p: dict, vel, wav, sou, rec):

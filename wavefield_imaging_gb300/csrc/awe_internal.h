@@ -131,9 +131,9 @@ void launch_stepA(int geom, bool exact, const float *cur, float *nxt, const floa
                   cudaStream_t s);
 void launch_bcA(bool exact, const float *um, float *uo, float *aux, const StepAParams &p, cudaStream_t s);
 // adjoint of the spherical step (AWE_FAST): Y <- W M (L^T(I c X) + 2 X - W Y),
-// G += X L(A) on the interior (A null: none); receivers z += W M (w r)
+// G += X L(A) on the interior (xcorr: G += X A; A null: none); receivers z += W M (w r)
 void launch_adjA_sph(const float *X, float *Y, const float *A, const float *vel, float2 *G, const StepAParams &p,
-                     cudaStream_t s);
+                     cudaStream_t s, bool xcorr = false);
 void launch_rec_adjA(float *z, const GeoPoint *pts, int nr, const float *r, const StepAParams &p, const long long *off,
                      cudaStream_t s);
 void launch_injectA(bool exact, int ndim, float *u, const GeoPoint *pts, const float *scale, int ns, const float *wav,

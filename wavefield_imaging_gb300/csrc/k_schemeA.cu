@@ -496,7 +496,7 @@ void launch_snapshot_transpose2(const float *u, float *dst, const Grid &g, int f
 // of A stay in registers.
 __global__ void __launch_bounds__(256) k_adjA_sph(const float *__restrict__ X, float *__restrict__ Y,
                                                   const float *__restrict__ A, const float *__restrict__ vel,
-                                                  float2 *__restrict__ G, const StepAParams p) {
+                                                  float2 *__restrict__ G, const StepAParams p, int xcorr) {
     const int i1 = blockIdx.x * blockDim.x + threadIdx.x;
     const int i2 = blockIdx.y * blockDim.y + threadIdx.y;
     const Grid g = p.g;
@@ -551,7 +551,9 @@ __global__ void __launch_bounds__(256) k_adjA_sph(const float *__restrict__ X, f
         float mu = fmaf(-damp_a<false>(1.f, si, p.dtab, p.ftab), yv, fmaf(2.f, xc, lt));
         if (p.mask == 3 && (i1 > g.n1 - p.nb || (i1 < p.spill && (i2 >= 1 || i3 >= 1)))) mu = 0.f;
         Y[i] = damp_a<false>(mu, si, p.dtab, p.ftab);
-        if (A && c_in && ph) {  // the forward's Laplacian of A at this cell
+        if (A && c_in && ph && xcorr) {
+            G[i] = gsum_add(G[i], __fmul_rn(xc, ac));  // zero-lag cross-correlation image
+        } else if (A && c_in && ph) {  // the forward's Laplacian of A at this cell
             const float u2 = ac + ac;
             const float rm = A[i - 1], rp = A[i + 1], tm = A[i - s2], tp = A[i + s2];
             const float pra = (rp - rm) * rd0;
@@ -577,7 +579,7 @@ __global__ void __launch_bounds__(256) k_adjA_sph(const float *__restrict__ X, f
 // from scalar loads, those inside it from the thread's own cells.
 __global__ void __launch_bounds__(256) k_adjA_sph2(const float *__restrict__ X, float *__restrict__ Y,
                                                    const float *__restrict__ A, const float *__restrict__ vel,
-                                                   float2 *__restrict__ G, const StepAParams p) {
+                                                   float2 *__restrict__ G, const StepAParams p, int xcorr) {
     const int i1 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int i2 = blockIdx.y * blockDim.y + threadIdx.y;
     const Grid g = p.g;
@@ -664,7 +666,13 @@ __global__ void __launch_bounds__(256) k_adjA_sph2(const float *__restrict__ X, 
             out[j] = damp_a<false>(m, si, p.dtab, p.ftab);
         }
         *reinterpret_cast<float2 *>(Y + i) = make_float2(out[0], out[1]);
-        if (A && (c0 || c1) && ph) {  // the forward's Laplacian of A at the two cells
+        if (A && (c0 || c1) && ph && xcorr) {  // zero-lag cross-correlation image
+            const float4 gq = *reinterpret_cast<const float4 *>(G + i);
+            float2 g0 = make_float2(gq.x, gq.y), g1 = make_float2(gq.z, gq.w);
+            if (c0) g0 = gsum_add(g0, __fmul_rn(xc.x, ac.x));
+            if (c1) g1 = gsum_add(g1, __fmul_rn(xc.y, ac.y));
+            *reinterpret_cast<float4 *>(G + i) = make_float4(g0.x, g0.y, g1.x, g1.y);
+        } else if (A && (c0 || c1) && ph) {  // the forward's Laplacian of A at the two cells
             const float rm = A[i - 1], rp = A[i + 2];
             const float2 mi = make_float2(rm, ac.x), pl = make_float2(ac.y, rp);
             const float2 tm = ld2(A, i - s2), tp = ld2(A, i + s2);
@@ -691,15 +699,15 @@ __global__ void __launch_bounds__(256) k_adjA_sph2(const float *__restrict__ X, 
 }
 
 void launch_adjA_sph(const float *X, float *Y, const float *A, const float *vel, float2 *G, const StepAParams &p,
-                     cudaStream_t s) {
+                     cudaStream_t s, bool xcorr) {
     const int nchunk = (p.g.n3 + kSphChunk - 1) / kSphChunk;
     if (p.g.n1 % 2 == 0) {
         dim3 b2(32, 8, 1), g2((p.g.n1 / 2 + 31) / 32, (p.g.n2 + 7) / 8, nchunk);
-        k_adjA_sph2<<<g2, b2, 0, s>>>(X, Y, A, vel, G, p);
+        k_adjA_sph2<<<g2, b2, 0, s>>>(X, Y, A, vel, G, p, xcorr ? 1 : 0);
         return;
     }
     dim3 block(64, 4, 1), grid((p.g.n1 + 63) / 64, (p.g.n2 + 3) / 4, nchunk);
-    k_adjA_sph<<<grid, block, 0, s>>>(X, Y, A, vel, G, p);
+    k_adjA_sph<<<grid, block, 0, s>>>(X, Y, A, vel, G, p, xcorr ? 1 : 0);
 }
 
 // receiver term of the spherical adjoint: z += W M (w r) at every corner

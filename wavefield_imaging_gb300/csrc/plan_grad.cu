@@ -220,8 +220,10 @@ static awe_status ckpt_load(awe_plan *p, int idx, float *u, cudaStream_t s) {
 // sweep j = nt .. 0 keeps z_{j+1} and z_{j+2} in two buffers:
 //   z_j = W M (L^T(I c z_{j+1}) + 2 z_{j+1} - W z_{j+2}) + W M R^T r_{j-1},
 //   dJ/dc += z_{j+1} L(A_j),  c = dt^2 v^2, folded to dJ/dm = dJ/dc (-c^2/dt^2).
+// image >= 0: awe_rtm's conditions (the data themselves back-propagated;
+// AWE_IMAGE_XCORR sums z A on the model window, AWE_IMAGE_BORN the gradient formula)
 static awe_status gradient_spher_one(awe_plan *p, const float *d_wav, int ncs, const float *d_dobs, int T, int fmt,
-                                     double *d_grad, double *misfit, float *d_dsyn, cudaStream_t s) {
+                                     double *d_grad, double *misfit, float *d_dsyn, cudaStream_t s, int image) {
     const awe_desc &d = p->d;
     const StepAParams &pa = p->pa;
     AWE_TRY(grad_alloc(p, T, fmt));
@@ -241,9 +243,15 @@ static awe_status gradient_spher_one(awe_plan *p, const float *d_wav, int ncs, c
     };
     AWE_TRY(planA_run(p, d_wav, ncs, dat, nullptr, s, &hook));
     launches += p->launches;
-    launch_residual(dat, d_dobs, st->r, p->nsmp, p->nr, st->row_sum, s);
-    std::vector<double> rows(p->nsmp);
-    CUDA_TRY(cudaMemcpyAsync(rows.data(), st->row_sum, rows.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+    const bool xcorr = image == AWE_IMAGE_XCORR;
+    std::vector<double> rows;
+    if (image < 0) {
+        launch_residual(dat, d_dobs, st->r, p->nsmp, p->nr, st->row_sum, s);
+        rows.resize(p->nsmp);
+        CUDA_TRY(cudaMemcpyAsync(rows.data(), st->row_sum, rows.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+    } else if (p->nr > 0) {
+        CUDA_TRY(cudaMemcpyAsync(st->r, d_dobs, (size_t)p->nsmp * p->nr * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    }
 
     CUDA_TRY(cudaMemsetAsync(st->X, 0, bytes, s));
     CUDA_TRY(cudaMemsetAsync(st->Y, 0, bytes, s));
@@ -265,7 +273,7 @@ static awe_status gradient_spher_one(awe_plan *p, const float *d_wav, int ncs, c
             launches += (p->ns > 0) + (k + 1 < k1);
         }
         for (int j = k1 - 1; j >= k0; j--) {
-            launch_adjA_sph(X, Y, slot + (size_t)(j - k0 + 1) * cells, p->vel, st->G, pa, s);
+            launch_adjA_sph(X, Y, slot + (size_t)(j - k0 + 1) * cells, p->vel, st->G, pa, s, xcorr);
             launches++;
             if (j >= 1) {
                 launch_rec_adjA(Y, p->rec, p->nr, st->r + (size_t)(j - 1) * p->nr, pa, p->corner_off, s);
@@ -274,7 +282,8 @@ static awe_status gradient_spher_one(awe_plan *p, const float *d_wav, int ncs, c
             std::swap(X, Y);
         }
     }
-    launch_grad_fold(st->G, p->vel, d.dt, g, p->nbd, d.n, d.ndim, d_grad, s, true);
+    if (xcorr) launch_image_cut(st->G, g, p->nbd, d.n, d.ndim, d_grad, s);
+    else launch_grad_fold(st->G, p->vel, d.dt, g, p->nbd, d.n, d.ndim, d_grad, s, true);
     launches++;
     CUDA_TRY(cudaStreamSynchronize(s));
     double J = 0;
@@ -289,7 +298,7 @@ static awe_status gradient_spher_one(awe_plan *p, const float *d_wav, int ncs, c
 // (bases moved back to field 0) and its columns of the data; gradients and
 // misfits summed.
 static awe_status plan_gradient_spher(awe_plan *p, const float *d_wav, int ncs, const float *d_dobs, int T, int fmt,
-                                      double *d_grad, double *misfit, float *d_dsyn, cudaStream_t s) {
+                                      double *d_grad, double *misfit, float *d_dsyn, cudaStream_t s, int image) {
     const awe_desc &d = p->d;
     if (d.expl) {
         set_error("awe_gradient: the reflectivity-scaled injection (expl=y) depends on the model; use expl=n");
@@ -300,7 +309,7 @@ static awe_status plan_gradient_spher(awe_plan *p, const float *d_wav, int ncs, 
         return AWE_ERR_UNSUPPORTED;
     }
     const int nshot = p->pa.nshot > 1 ? p->pa.nshot : 1;
-    if (nshot == 1) return gradient_spher_one(p, d_wav, ncs, d_dobs, T, fmt, d_grad, misfit, d_dsyn, s);
+    if (nshot == 1) return gradient_spher_one(p, d_wav, ncs, d_dobs, T, fmt, d_grad, misfit, d_dsyn, s, image);
     const long long cells = p->g.cells();
     const int NS = p->ns, NR = p->nr;
     int max_nr = 1;
@@ -360,7 +369,7 @@ static awe_status plan_gradient_spher(awe_plan *p, const float *d_wav, int ncs, 
             break;
         }
         double Jq = 0;
-        st = gradient_spher_one(p, d_wav, ncs, dobs_s, T, fmt, grad_s, &Jq, dsyn_s, s);
+        st = gradient_spher_one(p, d_wav, ncs, dobs_s, T, fmt, grad_s, &Jq, dsyn_s, s, image);
         if (st != AWE_OK) break;
         launch_add_f64(d_grad, grad_s, (long long)mcells, s);
         if (d_dsyn && nr > 0 &&
@@ -392,10 +401,6 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
         return AWE_ERR_UNSUPPORTED;
     }
     if (spher) {
-        if (image >= 0) {
-            set_error("awe_rtm: the spherical scheme has the gradient only");
-            return AWE_ERR_UNSUPPORTED;
-        }
         if (d.precision != AWE_FAST) {
             set_error("awe_gradient: precision must be AWE_FAST");
             return AWE_ERR_UNSUPPORTED;
@@ -407,7 +412,7 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
             set_error("awe_gradient: unknown checkpoint format %d", o.ckpt_format);
             return AWE_ERR_INVALID;
         }
-        return plan_gradient_spher(p, d_wav, ncs, d_dobs, T, o.ckpt_format, d_grad, misfit, d_dsyn, s);
+        return plan_gradient_spher(p, d_wav, ncs, d_dobs, T, o.ckpt_format, d_grad, misfit, d_dsyn, s, image);
     }
     if (p->den || d.hybrid) {
         set_error("awe_gradient: variable density and the hybrid ABC have no adjoint here");
