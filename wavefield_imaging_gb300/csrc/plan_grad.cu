@@ -348,7 +348,10 @@ static awe_status plan_gradient_spher(awe_plan *p, const float *d_wav, int ncs, 
         set_error("awe_gradient: point upload failed");
         st = AWE_ERR_CUDA;
     }
-    if (st == AWE_OK && cudaMemsetAsync(d_grad, 0, mcells * sizeof(double), s) != cudaSuccess) st = AWE_ERR_CUDA;
+    if (st == AWE_OK && cudaMemsetAsync(d_grad, 0, mcells * sizeof(double), s) != cudaSuccess) {
+        set_error("awe_gradient: clearing the gradient failed");
+        st = AWE_ERR_CUDA;
+    }
     p->pa.nshot = 1;
     p->nr = max_nr;  // sizes the gradient's trace buffers for every shot
     if (st == AWE_OK) st = grad_alloc(p, T, fmt);
@@ -384,7 +387,13 @@ static awe_status plan_gradient_spher(awe_plan *p, const float *d_wav, int ncs, 
         s0 += ns;
         r0 += nr;
     }
-    if (st == AWE_OK && cudaStreamSynchronize(s) != cudaSuccess) st = AWE_ERR_CUDA;
+    if (st == AWE_OK) {
+        const cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            set_error("awe_gradient: %s", cudaGetErrorString(e));
+            st = AWE_ERR_CUDA;
+        }
+    }
     cleanup();
     *misfit = J;
     p->launches = launches;
