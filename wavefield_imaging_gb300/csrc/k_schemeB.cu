@@ -34,6 +34,11 @@ template <int NOP, int NDIM, bool EXACT, bool RHO>
 __global__ void __launch_bounds__(256) k_stepB(const float *__restrict__ cur, float *__restrict__ nxt,
                                                const float *__restrict__ vel, const float *__restrict__ rho,
                                                const StepBParams p) {
+    // programmatic dependent launch (2D): wait for the previous grid before
+    // touching memory (a no-op for an ordinary launch), then let the next
+    // step's grid be scheduled once every block of this one has started
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;");
     const Grid g = p.g;
     const long long s2 = g.n1, s3 = (long long)g.n1 * g.n2;
     if (NDIM == 2 && p.ext_n > 0) {
@@ -143,6 +148,20 @@ static void dispatch_rho(bool rho, const float *cur, float *nxt, const float *ve
     dim3 grid((p.g.n1 + 63) / 64, (p.g.n2 + 3) / 4, NDIM == 3 ? p.g.n3 : 1);
     if (NDIM == 2 && p.ext_n > 0)  // extra rows of blocks gather the receivers
         grid.y += (unsigned)((p.ext_n + grid.x * 256 - 1) / (grid.x * 256));
+    if (NDIM == 2) {  // launch-bound steps: programmatic dependent launch hides the launch gap
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = grid;
+        cfg.blockDim = block;
+        cfg.stream = s;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        if (rho) cudaLaunchKernelEx(&cfg, k_stepB<NOP, NDIM, EXACT, true>, cur, nxt, vel, den, p);
+        else cudaLaunchKernelEx(&cfg, k_stepB<NOP, NDIM, EXACT, false>, cur, nxt, vel, den, p);
+        return;
+    }
     if (rho)
         k_stepB<NOP, NDIM, EXACT, true><<<grid, block, 0, s>>>(cur, nxt, vel, den, p);
     else
