@@ -479,36 +479,42 @@ static void step3d(real *u0, const real *u1, const float *vel, const float *rho,
     }
 }
 
-/* sponge3d_apply, fdutil.c:2248-2310 */
+/* sponge3d_apply, fdutil.c:2248-2310.  Each face pass is split over the
+ * lines of another axis; every cell belongs to one line, which runs its ib
+ * loop in the reference's order, so the products are those of the serial
+ * loops. */
 static void sponge3(real *u, const float *w, int nb, int nzpad, int nxpad, int nypad) {
     const size_t sx = nzpad, sy = (size_t)nzpad * nxpad;
-    for (int ib = 0; ib < nb; ib++) {
-        float wb = w[nb - ib - 1];
-        int ibz = nzpad - ib - 1;
-        for (int iy = 0; iy < nypad; iy++)
+#pragma omp parallel for
+    for (int iy = 0; iy < nypad; iy++)
+        for (int ib = 0; ib < nb; ib++) {
+            float wb = w[nb - ib - 1];
+            int ibz = nzpad - ib - 1;
             for (int ix = 0; ix < nxpad; ix++) {
                 u[iy * sy + ix * sx + ib] *= wb;
                 u[iy * sy + ix * sx + ibz] *= wb;
             }
-    }
-    for (int ib = 0; ib < nb; ib++) {
-        float wb = w[nb - ib - 1];
-        int ibx = nxpad - ib - 1;
-        for (int iy = 0; iy < nypad; iy++)
+        }
+#pragma omp parallel for
+    for (int iy = 0; iy < nypad; iy++)
+        for (int ib = 0; ib < nb; ib++) {
+            float wb = w[nb - ib - 1];
+            int ibx = nxpad - ib - 1;
             for (int iz = 0; iz < nzpad; iz++) {
                 u[iy * sy + ib * sx + iz] *= wb;
                 u[iy * sy + ibx * sx + iz] *= wb;
             }
-    }
-    for (int ib = 0; ib < nb; ib++) {
-        float wb = w[nb - ib - 1];
-        int iby = nypad - ib - 1;
-        for (int ix = 0; ix < nxpad; ix++)
+        }
+#pragma omp parallel for
+    for (int ix = 0; ix < nxpad; ix++)
+        for (int ib = 0; ib < nb; ib++) {
+            float wb = w[nb - ib - 1];
+            int iby = nypad - ib - 1;
             for (int iz = 0; iz < nzpad; iz++) {
                 u[ib * sy + ix * sx + iz] *= wb;
                 u[iby * sy + ix * sx + iz] *= wb;
             }
-    }
+        }
 }
 
 typedef struct {
@@ -517,9 +523,12 @@ typedef struct {
     float *yl, *yh; /* [nxpad][nzpad] */
 } abc3;
 
-/* abcone3d_apply, fdutil.c:2085-2177 (uo = new field, um = current) */
+/* abcone3d_apply, fdutil.c:2085-2177 (uo = new field, um = current).  Each
+ * pass is split over lines that its recurrences never cross (the z pass over
+ * y, the x pass over y, the y pass over x), so the result is the serial one. */
 static void abcone3(real *uo, const real *um, int nop, const abc3 *a, int fsrf, int nzpad, int nxpad, int nypad) {
     const size_t sx = nzpad, sy = (size_t)nzpad * nxpad;
+#pragma omp parallel for
     for (int iy = 0; iy < nypad; iy++)
         for (int ix = 0; ix < nxpad; ix++)
             for (int iop = 0; iop < nop; iop++) {
@@ -532,6 +541,7 @@ static void abcone3(real *uo, const real *um, int nop, const abc3 *a, int fsrf, 
                 int iz = nzpad - nop + iop - 1;
                 uo[c + iz] = um[c + iz - 1] + (um[c + iz] - uo[c + iz - 1]) * bh;
             }
+#pragma omp parallel for
     for (int iy = 0; iy < nypad; iy++)
         for (int iz = 0; iz < nzpad; iz++)
             for (int iop = 0; iop < nop; iop++) {
@@ -543,6 +553,7 @@ static void abcone3(real *uo, const real *um, int nop, const abc3 *a, int fsrf, 
                 c = iy * sy + ix * sx + iz;
                 uo[c] = um[c - sx] + (um[c] - uo[c - sx]) * bh;
             }
+#pragma omp parallel for
     for (int ix = 0; ix < nxpad; ix++)
         for (int iz = 0; iz < nzpad; iz++)
             for (int iop = 0; iop < nop; iop++) {

@@ -628,6 +628,17 @@ static int gpu_spher3d(const orc_gpar *P, const float *vel_in, const float *wav,
     size_t off[8];
     for (int k = 0; k < 8; k++) off[k] = ((k & 1) ? st : 0) + ((k & 2) ? 1 : 0) + ((k & 4) ? sp : 0);
     size_t isnap = 0;
+    float *mA = malloc(nrapad * 4), *mC = malloc(nrapad * 4);
+    float *mB = malloc((size_t)nthpad * nrapad * 4), *mD = malloc((size_t)nthpad * nrapad * 4);
+    for (int ith = 0; ith < nthpad; ith++)
+        for (int ira = 0; ira < nrapad; ira++) {
+            const float ra = dra * ira + orpad, th = dth * ith + othpad;
+            const size_t m = (size_t)ith * nrapad + ira;
+            mA[ira] = 2 / ra;
+            mB[m] = cosf(th) / (ra * ra * sinf(th));
+            mC[ira] = 1 / (ra * ra);
+            mD[m] = 1 / (ra * ra * sinf(th) * sinf(th));
+        }
 #define CS(iph, ith, ira) ((size_t)(iph) * sp + (size_t)(ith) * st + (ira))
     for (int it = 0; it < nt; it++) {
         const float wa = wav[it];
@@ -638,14 +649,19 @@ static int gpu_spher3d(const orc_gpar *P, const float *vel_in, const float *wav,
             if (P->expl) r = refl3(v, npad, (long long)b, st, sp);
             for (int k = 0; k < 8; k++) po[b + off[k]] += P->expl ? wa * c->w[k] * r : wa * c->w[k];
         }
-        /* solve_3D, spher_kernels.cu:455-526 */
+        /* solve_3D, spher_kernels.cu:455-526; the metric factors are the
+         * kernel's own float expressions of (ra, th), evaluated once per
+         * (theta, r) before the loop (mA, mB, mC, mD), so every cell's
+         * operations are the reference's */
+#pragma omp parallel for
         for (int iph = 0; iph < nphpad; iph++)
             for (int ith = 0; ith < nthpad; ith++)
                 for (int ira = 0; ira < nrapad; ira++) {
                     size_t c = CS(iph, ith, ira);
-                    float ra = dra * ira + orpad, th = dth * ith + othpad, vv = v[c], lap;
+                    float vv = v[c], lap;
                     if (ira >= NOPA && ira < nrapad - NOPA && iph >= NOPA && iph < nphpad - NOPA && ith >= NOPA &&
                         ith < nthpad - NOPA) {
+                        const size_t m = (size_t)ith * nrapad + ira;
                         float pra = po[c + 1] - po[c - 1];
                         pra = pra / (2 * dra);
                         float ppra = po[c + 1] - 2 * po[c] + po[c - 1];
@@ -656,8 +672,7 @@ static int gpu_spher3d(const orc_gpar *P, const float *vel_in, const float *wav,
                         ppth = ppth / (dth * dth);
                         float ppph = po[c + sp] - 2 * po[c] + po[c - sp];
                         ppph = ppph / (dph * dph);
-                        lap = (2 / ra) * pra + ppra + (cosf(th) / (ra * ra * sinf(th))) * pth + (1 / (ra * ra)) * ppth +
-                              (1 / (ra * ra * sinf(th) * sinf(th))) * ppph;
+                        lap = mA[ira] * pra + ppra + mB[m] * pth + mC[ira] * ppth + mD[m] * ppph;
                     } else
                         lap = 0.;
                     fpo[c] = (dt * dt) * (vv * vv) * lap + 2 * po[c] - ppo[c];
@@ -667,6 +682,7 @@ static int gpu_spher3d(const orc_gpar *P, const float *vel_in, const float *wav,
         po = fpo;
         fpo = t;
         /* spongeKernel_3D on po, ppo: kernel axes (x, y, z) = (r, phi, theta) */
+#pragma omp parallel for
         for (int iph = 0; iph < nphpad; iph++)
             for (int ith = 0; ith < nthpad; ith++)
                 for (int ira = 0; ira < nrapad; ira++) {
@@ -677,7 +693,8 @@ static int gpu_spher3d(const orc_gpar *P, const float *vel_in, const float *wav,
                     if (P->fsrf && ira > nrapad - nb) po[c] = 0;
                 }
         if (P->fsrf) /* freeSurf_3D past nrapad: first samples of the next r line */
-            for (size_t line = 0; line + 1 < (size_t)nthpad * nphpad; line++)
+#pragma omp parallel for
+            for (size_t line = 0; line < (size_t)nthpad * nphpad - 1; line++)
                 for (int k = 0; k < 8 * ((nrapad + 7) / 8) - nrapad; k++) po[(line + 1) * nrapad + k] = 0;
         for (int r = 0; r < nr; r++) {
             const glint *c = &cr[r];
@@ -700,6 +717,10 @@ static int gpu_spher3d(const orc_gpar *P, const float *vel_in, const float *wav,
         }
     }
 #undef CS
+    free(mA);
+    free(mB);
+    free(mC);
+    free(mD);
     free(v);
     free(po);
     free(ppo);

@@ -17,7 +17,12 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REF_SRC = "/root/reference/CODE"
+# The reference checkout (its CODE/ directory holds the programs): the
+# AWE_REFERENCE environment variable, else a directory named "reference"
+# beside this repository.  Absent (as on a machine without the checkout),
+# build() skips the reference programs.
+REF_SRC = os.path.join(os.environ.get("AWE_REFERENCE") or
+                       os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"), "CODE")
 
 CFLAGS = ["-std=gnu99", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-Wall"]
 

@@ -18,11 +18,12 @@
 // nearest face along the swept axis for onewayBC_2D, and by the sum of the
 // per-axis face distances for onewayBC_3D.
 //
-// Deviations from undefined behaviour of the reference, documented in
-// the cart 3D program leaves most of its y-high one-way
-// coefficients uninitialised (MAWEFDcart3Dgpu.cu:292 writes only the
-// diagonal); here they are filled as the loop evidently intends.  Extraction
-// rows beyond the data buffer (cart 3D pre-incremented row index) are dropped.
+// Two places where the reference's behaviour is undefined are given one
+// definite meaning here, so that fixtures are reproducible: the cart 3D
+// program leaves most of its y-high one-way coefficients uninitialised
+// (MAWEFDcart3Dgpu.cu:292 writes only the diagonal); here they are filled as
+// the loop evidently intends.  Extraction rows beyond the data buffer (cart 3D
+// pre-incremented row index) are dropped instead of written past its end.
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
