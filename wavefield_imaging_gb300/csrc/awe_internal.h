@@ -83,6 +83,31 @@ void launch_hybridB(int ndim, int nop, int nbd, bool exact, int fsrf, float *uo,
 void launch_band_sponge(int ndim, int width, bool exact, float *u, const float *w1, const float *w2,
                         const float *w3, const Grid &g, cudaStream_t s, int zfused = 0);
 
+// The boundary work of a 3D step in one launch (k_boundary3.cu): one-way ABC
+// of the six faces, sponge of the shell the step kernel left unsponged
+// (cells within nop + 2 of a face), the receiver gather of the level the step
+// read, and the injection (ns > 0; only when no source corner lies in that
+// shell, whose cells the ABC reads).  nop = 4.
+struct Bnd3Params {
+    Grid g;
+    float *uo;        // the new level
+    const float *um;  // the level the step read
+    const float *vel; // v^2 dt^2 (injection)
+    const float *zl, *zh, *xl, *xh, *yl, *yh;  // one-way coefficients
+    const float *w1, *w2, *w3;                 // sponge factors (null: no sponge)
+    int top;                                   // axis-1 low face (0 with a free surface)
+    const GeoPoint *rec;
+    int nr, rec_stride;
+    float *rec_row;  // null: no gather this step
+    const GeoPoint *src;
+    int ns, src_stride;
+    const float *wav;
+    int it, ncs, one_wavelet;
+    int n_int, nxr, nzr, rec_blocks;  // set by launch_bnd3
+};
+bool bnd3_eligible(int nop, const Grid &g);
+void launch_bnd3(bool exact, Bnd3Params p, cudaStream_t s);
+
 // injection into the new level scaled by vel (v^2 dt^2): u += (dd*w)*vel.
 // off[c] = flat offset of corner c from the point's base index.
 // stride: distance between consecutive points in pts (moving geometries)

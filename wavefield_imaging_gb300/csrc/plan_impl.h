@@ -49,6 +49,7 @@ struct awe_plan {
     std::vector<awe::GeoPoint> h_src, h_rec;
     std::vector<awe::Lint> h_src_lint;  // source corner indices in the reference's fdm axes
     bool sponge_deferred = false;  // a source node lies in the sponge band outside the boundary shell
+    bool src_in_shell = false;     // a source node lies within nop + 2 of a face (3D)
     // moving geometry (awe_set_moving_geometry): src/rec hold ns*src_rows and
     // nr*rec_rows entries; move_mode < 0 = fixed points
     int move_mode = -1, src_rows = 1, rec_rows = 1;
@@ -145,6 +146,9 @@ awe_status stepB_full(awe_plan *p, const StepBParams &sp, const float *prv, cons
                       int ext_n = 0, int ext_stride = 1, float *ext_row = nullptr);
 // 2D steps add the sources in the step kernel (one launch per step) up to this many sources
 constexpr int kFusedSources = 8;
+// 3D CPU-program scheme with sponge + one-way ABC: the boundary work of a step
+// (ABC, shell sponge, receiver gather, injection) is one launch (k_bnd3)
+bool stepB3_bnd(const awe_plan *p);
 // image < 0: misfit gradient; else awe_image_condition (the residual is the data)
 awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *d_dobs, const awe_grad_opts &o,
                          double *d_grad, double *misfit, float *d_dsyn, cudaStream_t s, int image = -1);

@@ -239,6 +239,7 @@ awe_status set_geometry_common(awe_plan *p, int ns, const float *sou, int nr, co
     // boundary shell would be sponged before its injection by the fused
     // step; such runs defer the whole sponge to after the injection
     p->sponge_deferred = false;
+    p->src_in_shell = false;
     if (d.scheme == AWE_SCHEME_CPU && d.dabc && !d.hybrid) {
         const int shell = (nd == 3) ? p->nop + 2 : 0;
         const int nc = nd == 3 ? 8 : 4;
@@ -255,9 +256,17 @@ awe_status set_geometry_common(awe_plan *p, int ns, const float *sou, int nr, co
                     inshell = inshell || dist < shell;
                 }
                 if (band && !inshell) p->sponge_deferred = true;
+                if (inshell) p->src_in_shell = true;
             }
     }
     return AWE_OK;
+}
+
+bool stepB3_bnd(const awe_plan *p) {
+    const awe_desc &d = p->d;
+    const char *env = std::getenv("AWE_BND3");
+    return d.scheme == AWE_SCHEME_CPU && d.ndim == 3 && d.dabc && !d.hybrid && !p->sponge_deferred &&
+           bnd3_eligible(p->nop, p->g) && !(env && std::strcmp(env, "0") == 0);
 }
 
 StepBParams stepB_params(const awe_plan *p) {
@@ -328,11 +337,48 @@ awe_status stepB_full(awe_plan *p, const StepBParams &sp0, const float *prv, con
     }
     prof_end(p, s);
     launches++;
-    if (p->ns > 0 && !fuse_src) {
+    const bool bnd = stepB3_bnd(p);
+    // the boundary launch injects too, unless a source touches the cells the ABC reads
+    const bool inj_in_bnd = bnd && !p->src_in_shell;
+    if (p->ns > 0 && !fuse_src && !inj_in_bnd) {
         const PointsAt ps = points_at(p, p->src, p->ns, p->src_rows, it);
         launch_injectB_off(d.ndim, exact, nxt, p->vel, ps.pts, p->ns, d_wav, it, ncs, ncs == 1, p->corner_off, s,
                            ps.stride);
         launches++;
+    }
+    if (bnd) {
+        Bnd3Params bp{};
+        bp.g = g;
+        bp.uo = nxt;
+        bp.um = cur;
+        bp.vel = p->vel;
+        bp.zl = p->abc[0];
+        bp.zh = p->abc[1];
+        bp.xl = p->abc[2];
+        bp.xh = p->abc[3];
+        bp.yl = p->abc[4];
+        bp.yh = p->abc[5];
+        bp.w1 = p->w[0];
+        bp.w2 = p->w[1];
+        bp.w3 = p->w[2];
+        bp.top = !d.fsrf;
+        bp.rec = ext_pts;
+        bp.nr = ext_n;
+        bp.rec_stride = ext_stride;
+        bp.rec_row = ext_n > 0 ? ext_row : nullptr;
+        if (inj_in_bnd && p->ns > 0) {
+            const PointsAt ps = points_at(p, p->src, p->ns, p->src_rows, it);
+            bp.src = ps.pts;
+            bp.ns = p->ns;
+            bp.src_stride = ps.stride;
+            bp.wav = d_wav;
+            bp.it = it;
+            bp.ncs = ncs;
+            bp.one_wavelet = ncs == 1;
+        }
+        launch_bnd3(exact, bp, s);
+        launches++;
+        return AWE_OK;
     }
     if (d.dabc) {
         AbcB abc{p->abc[0], p->abc[1], p->abc[2], p->abc[3], p->abc[4], p->abc[5]};
@@ -391,8 +437,8 @@ awe_status planB_run_hooked(awe_plan *p, const float *d_wav, int ncs, float *d_d
     int row = 0, isnap = 0;
     // 2D: the traces of step it (the level the step reads, pending sponge
     // applied, as the reference extracts after its swap) are gathered by the
-    // step's own launch
-    const bool fuse_rec = d.ndim == 2 && p->nr > 0;
+    // step's own launch; 3D: by the step's boundary launch
+    const bool fuse_rec = (d.ndim == 2 || stepB3_bnd(p)) && p->nr > 0;
     for (int it = 0; it < d.nt; it++) {
         if (hook) AWE_TRY((*hook)(it, nxt, cur, s));
         const bool ext = fuse_rec && it % d.jdata == 0;
