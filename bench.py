@@ -14,6 +14,13 @@ interfaces.
           awe_forward with pinned host buffers (H2D of the model and
           wavelet, D2H of the traces inside the timed region)
 
+After the headline (rank 0, one GPU) two more legs go on the same line:
+  batched_gradient  : FWI gradients of the 256-shot survey, batched against
+                      the per-shot loop (the second half of the metric)
+  spherical_forward : the spherical-shell configuration's 16-source track
+and cpu_baseline.gradient times the FP64 adjoint oracle on one survey shot
+and states the engine's gradient error against it.  --no-extras skips them.
+
 --impl reference times the reference CPU implementation of the same update
 (the oracle port of ts_kernel.c step_forward_3d, OpenMP over all host cores)
 on a bounded sample of time steps of the same padded grid.
@@ -169,18 +176,17 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
+# DRAM bytes per cell of one step-kernel launch (k_stepB3_o8, AWE_FAST),
+# from the ncu capture of a 384^3-padded launch: 897.0 MB read + written
+# over 56.62 M padded cells (profiles/k_stepB3_o8_tma_n320.md).  A full
+# 576^3 launch is too large for a capture; DRAM traffic scales with the cells
+# a launch processes.
+STEP_DRAM_BYTES_PER_CELL = 15.842
+
+
 def profiled_traffic(cells):
-    """DRAM bytes per step-kernel launch: the committed ncu capture's bytes
-    per cell (profiles/k_stepB3_o8_tma_n320.md, 384^3 padded) times the
-    launch's cells, or None without it."""
-    path = os.path.join(ROOT, "profiles", "k_stepB3_o8_tma_n320.md")
-    try:
-        for line in open(path):
-            if line.strip().startswith("dram_bytes_per_cell:"):
-                return float(line.split(":", 1)[1].split()[0]) * cells
-    except Exception:
-        pass
-    return None
+    """DRAM bytes of one step-kernel launch over `cells` padded cells."""
+    return STEP_DRAM_BYTES_PER_CELL * cells
 
 
 def cpu_baseline(w, target_s=10.0):
@@ -359,11 +365,162 @@ def run_ours(args):
                         "peak_source": peak_kind, "avg_launch_us": avg_kernel_s * 1e6,
                         "kernel_share": (kern_ms / ms) if ms > 0 else None},
            "gpu_launches": int(launches), "clocks": clocks, "trace_max_abs": check}
+    plan.close()
+    grad_check = None
+    if args.extras and world == 1:
+        # the second half of the metric and the spherical configuration, on the
+        # same GPU after the headline (each leg reports its own failure)
+        for key, fn in (("batched_gradient", extra_batched_gradient), ("spherical_forward", extra_spherical_forward)):
+            try:
+                res = fn(args, local, peak, peak_kind)
+                if key == "batched_gradient":
+                    grad_check = res.pop("_check")
+                out[key] = res
+            except Exception as e:  # noqa: BLE001 - reported in the JSON line
+                out[key] = {"error": "%s: %s" % (type(e).__name__, e)}
+            torch.cuda.empty_cache()
     if args.cpu_baseline:
         v, cores, sample, _ = cpu_baseline(w)
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        if grad_check is not None:
+            try:
+                out["cpu_baseline"]["gradient"] = oracle_gradient_check(grad_check)
+            except Exception as e:  # noqa: BLE001
+                out["cpu_baseline"]["gradient"] = {"error": "%s: %s" % (type(e).__name__, e)}
     print(json.dumps(out))
-    plan.close()
+
+
+def extra_batched_gradient(args, local, peak, peak_kind):
+    """FWI gradients of the 256-shot survey (c1 geometry, c2 physics: true
+    model vs the same smoothed 100 m, BFP16 checkpoints, compensated sums):
+    the batched gradient (all shots per launch) against the plain per-shot
+    loop (awe_gradient shot after shot), the latter timed on 16 evenly spaced
+    shots.  Both from host buffers, host wall clock around the synchronous
+    calls; one untimed call each first."""
+    import torch
+
+    import wavefield_imaging_gb300 as awe
+
+    nt, nz, nshots = 4000, 512, 256
+    vtrue, shots = batch_survey(nshots=nshots, nz=nz)
+    v0 = smooth(vtrue, 100.0 / 5.0)
+    wav = ricker(nt, 0.005, 5.0)
+    desc = awe.make_desc(2, (nz, vtrue.shape[0]), (5.0, 5.0), (0.0, 0.0), nt, 0.005, nb=40, fdorder=8, dabc=1, expl=1,
+                         precision=awe.FAST)
+    with awe.Batch(desc, shots, device=local) as b:
+        b.set_model(vtrue)
+        b.select(4, chunk=64)
+        dobs = b.forward(wav)
+        b.set_model(v0)
+        b.gradient(wav, dobs)
+        torch.cuda.synchronize()
+        reps = 2
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            gb, Jb = b.gradient(wav, dobs)
+        batch_s = (time.perf_counter() - t0) / reps
+    sample = [int(k) for k in np.linspace(0, nshots - 1, 16)]
+    plans = []
+    for k in sample:
+        x0, nx, sou, rec = shots[k]
+        dk = awe.make_desc(2, (nz, nx), (5.0, 5.0), (0.0, x0 * 5.0), nt, 0.005, nb=40, fdorder=8, dabc=1, expl=1,
+                           precision=awe.FAST)
+        p = awe.Plan(dk, device=local)
+        p.set_model(v0[x0:x0 + nx])
+        p.set_geometry(sou, rec)
+        plans.append(p)
+    plans[0].gradient(wav, dobs[sample[0]])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    grads = [p.gradient(wav, dobs[k]) for p, k in zip(plans, sample)]
+    plain_s = (time.perf_counter() - t0) / len(sample)
+    for p in plans:
+        p.close()
+    # the smallest window of the sample, for the FP64 oracle check on the host
+    kmin = min(sample, key=lambda k: shots[k][1])
+    x0, nx, sou, rec = shots[kmin]
+    check = dict(shot=kmin, x0=x0, nx=nx, nz=nz, nt=nt, vel=v0[x0:x0 + nx], wav=wav, sou=sou, rec=rec,
+                 dobs=dobs[kmin], grad=grads[sample.index(kmin)][0])
+    return {"workload": "%d shots on windows nx in [300, 700] x nz 512 of a 6000-column model, 8th order, nt=%d, "
+                        "nb=40, dabc=y; start model = true model smoothed 100 m; BFP16 checkpoints" % (nshots, nt),
+            "batched_shot_gradients_per_s": nshots / batch_s, "batched_s": batch_s,
+            "plain_shot_gradients_per_s": 1.0 / plain_s, "plain_s_per_shot": plain_s,
+            "plain_sample": "16 evenly spaced shots of the survey, awe_gradient one after the other",
+            "speedup_batched_vs_plain": plain_s * nshots / batch_s, "misfit": Jb,
+            "timing": "host wall clock around synchronous calls from host buffers", "_check": check}
+
+
+def oracle_gradient_check(c):
+    """The FP64 adjoint oracle (all forward levels kept in host memory, one
+    thread) on one survey shot: its time is the CPU baseline of the gradient
+    half of the metric, its gradient the reference for the engine's
+    (rel-L2 over the shot's window)."""
+    from oracle import oracle
+
+    nz, nx = c["nz"], c["nx"]
+    npad = (nz + 80) * (nx + 80)
+    try:
+        mem = os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_PHYS_PAGES")
+    except (ValueError, OSError):
+        mem = 64 << 30
+    nt = c["nt"]
+    need = (nt + 1) * npad * 8 * 1.1
+    if need > 0.25 * mem:
+        return {"skipped": "needs %.1f GB of host memory, more than a quarter of %.1f GB" % (need / 1e9, mem / 1e9)}
+    par = dict(n=[nz, nx], d=[5.0, 5.0], o=[0.0, c["x0"] * 5.0], nb=40, nt=nt, dt=0.005, fdorder=8, dabc=1, expl=1)
+    t0 = time.perf_counter()
+    g64, J64, _ = oracle.misfit_gradient(par, c["vel"], c["wav"], c["sou"], c["rec"], c["dobs"])
+    secs = time.perf_counter() - t0
+    g = np.asarray(c["grad"], np.float64)
+    err = float(np.linalg.norm(g - g64) / max(np.linalg.norm(g64), 1e-300))
+    return {"value": 1.0 / secs, "unit": "shot gradients/s", "cores": 1, "kind": "port",
+            "sample": "shot %d of the survey (window of %d columns, nt=%d): FP64 adjoint oracle" % (
+                c["shot"], nx, nt),
+            "rel_l2_engine_bfp16_vs_fp64": err}
+
+
+def extra_spherical_forward(args, local, peak, peak_kind):
+    """The spherical-shell configuration (764 x 576 x 576 padded, scheme of
+    sfAWEFDspher3Dgpu): the 16-source track advancing in one launch per step,
+    200 of its 3000 steps, device-resident; cell-updates/s and the step
+    kernel's HBM roofline."""
+    import torch
+
+    import wavefield_imaging_gb300 as awe
+
+    nt, nshots = 200, 16
+    w = spher_workload(nt)
+    vel = spher_model(w)
+    shots = spher_shots(w, nshots)
+    wav = ricker(nt, w["dt"], w["f0"])
+    desc = awe.make_desc(3, w["n"], w["d"], w["o"], nt, w["dt"], coords=awe.SPHER, scheme=awe.SCHEME_GPU,
+                         nb=w["nb"], expl=0, precision=awe.FAST)
+    with awe.Plan(desc, device=local) as plan:
+        plan.set_model(vel)
+        plan.set_shots(shots)
+        nrec = sum(r.shape[0] for _, r in shots)
+        d_wav = torch.from_numpy(wav).cuda()
+        d_dat = torch.zeros((plan.nsmp, nrec), dtype=torch.float32, device="cuda")
+        stream = torch.cuda.Stream()
+        plan.forward_device(d_wav.data_ptr(), 1, d_dat.data_ptr(), 0, stream.cuda_stream)
+        torch.cuda.synchronize()
+        plan.profile(True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        plan.forward_device(d_wav.data_ptr(), 1, d_dat.data_ptr(), 0, stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        kern_ms, kern_n = plan.profile_read()
+        plan.profile(False)
+    cells = nshots * int(np.prod([n + 2 * w["nb"] for n in w["n"]]))
+    avg = kern_ms / 1e3 / max(kern_n, 1)
+    achieved = BYTES_PER_CELL * cells / avg / 1e9
+    return {"workload": w["name"].replace("1 source", "%d sources along the track, one launch per step" % nshots)
+                        + " (%d of 3000 steps)" % nt,
+            "value": cells * nt / (ms / 1e3), "unit": "cell-updates/s", "ms_per_run": ms,
+            "roofline": {"kernel": "k_stepA_sph_march2", "avg_launch_us": avg * 1e6, "achieved": achieved,
+                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind}}
 
 
 GRAD_METRIC = "FWI gradients/s (misfit gradient, checkpointed fwd + adjoint)"
@@ -945,6 +1102,8 @@ def main():
     ap.add_argument("--nt", type=int, default=3000, help="time steps (the workload is nt=3000)")
     ap.add_argument("--n", type=int, default=512, help="model edge (the workload is 512; smaller for profiling)")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-extras", dest="extras", action="store_false",
+                    help="skip the batched-gradient and spherical legs that follow the headline")
     ap.add_argument("--workload", default="fwd3d", choices=["fwd3d", "fwd2d", "grad3d", "grad2d", "batch2d", "batchgrad2d", "spher3d", "sphergrad3d"],
                     help="fwd3d: the headline forward workload; grad3d/grad2d: misfit gradients; "
                          "batch2d: the batched 2D survey")
