@@ -367,9 +367,11 @@ awe_status awe_batch_gradient(awe_batch *batch, const float *wav, const float *d
  * AWE_SCHEME_CPU, cartesian, no hybrid ABC, no density, no snapshots; the
  * result equals awe_forward's for the same descriptor.  The work is queued on
  * `stream` (a cudaStream_t; NULL = legacy default stream) and is complete when
- * the stream is.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress) with that device current; make that first
- * call before any stream capture.  All calls share the array: each call clears
+ * the stream is.  A call outside stream capture looks up the array's device
+ * address (cudaGetSymbolAddress) with the device current, so a device reset
+ * in between is followed; a call during capture reuses the address of the
+ * last call outside capture on that device, so make one call before the
+ * first capture and after any device reset.  All calls share the array: each call clears
  * what must start at zero, and calls whose work overlaps on the GPU race. */
 awe_status awe_forward2d_noalloc(const awe_desc *desc, const float *d_vel, const float *d_wav, int ncs, int ns,
                                  const float *d_sou, int nr, const float *d_rec, float *d_dat, void *stream);

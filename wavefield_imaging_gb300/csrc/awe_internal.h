@@ -57,6 +57,10 @@ struct StepBParams {
     const GeoPoint *ext;
     int ext_n, ext_stride;
     float *ext_row;
+    // polls allowed to a pipelined kernel's waits for its own copies before it
+    // reports a timeout (< 0: the kernel's default); the drain after a timeout
+    // always keeps the default
+    long long spin;
 };
 
 // [lo, hi): the indices of a sponge factor table whose entries are exactly 1
@@ -301,6 +305,9 @@ Lint lint_make(int ndim, float x, float y, float z, const FdmAxes &f);
 void expand_model(int ndim, const float *a, float *b, int nb, const int *n);
 
 void set_error(const char *fmt, ...);
+// the descriptor checks of awe_plan_create (sizes, spacing, time axis,
+// scheme, order, intervals, precision)
+awe_status check_desc(const awe_desc *d);
 
 // ---- TMA-staged 3D 8th-order step (k_stepB3_tma.cu) ----
 struct Step3Launch {

@@ -59,6 +59,7 @@ struct Step3Params {
     // mu = W lambda), vel = nu_k; lap_v = L(V_k); grad += I nu L(V_k) (FP64)
     const float *lap_v;
     float2 *grad;  // gradient accumulators (compensated pairs)
+    long long spin;  // polls of a compute-side wait before it gives up (the drain keeps SPIN_LIMIT)
 };
 
 template <bool EXACT>
@@ -167,7 +168,7 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
                             }
                         }
                     }
-                    const bool bad = !mbar_wait(&full[slot], ph, SPIN_LIMIT);
+                    const bool bad = !mbar_wait(&full[slot], ph, p.spin);
                     if (bad) atomicExch(p.err, 1);
                     const float4 cq = *reinterpret_cast<const float4 *>(&st[slot].cur[xi + HALO][4 * zq + HALO]);
                     q[u][0] = cq.x;
@@ -454,6 +455,7 @@ static Step3Params step3_params(const StepBParams &sp, const Step3Launch &sh, un
     p.base = base;
     p.err = err;
     p.nxt = nxt;
+    p.spin = sp.spin >= 0 ? sp.spin : s3::SPIN_LIMIT;
     return p;
 }
 
@@ -506,6 +508,7 @@ cudaError_t launch_stepB3_tma_with(bool exact, const CUtensorMap &cur, const CUt
     p.err = err;
     p.nxt = nxt;
     p.lap_out = lap_out;
+    p.spin = sp.spin >= 0 ? sp.spin : s3::SPIN_LIMIT;
     if (exact) {
         cudaFuncSetAttribute(k_stepB3_o8<true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem);
         k_stepB3_o8<true, 0><<<sh.grid, s3::NTHREADS, sh.smem, s>>>(cur, prv, vel, p);

@@ -44,18 +44,27 @@ constexpr size_t kStaticBytes = kOffPts + kStaticMaxPoints * sizeof(GeoPoint);
 
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
 
-// Host-side address of g_static_scratch per device, taken once per device
-// with that device current (the symbol's host name is only a stand-in).
+// Host-side address of g_static_scratch per device (the symbol's host name
+// is only a stand-in).  It is looked up with the device current on every
+// call made outside stream capture, so a context that was torn down and
+// rebuilt (cudaDeviceReset), which may load the module at another address,
+// is followed; a call made during capture uses the address cached by the
+// last call outside capture on that device.
 static std::mutex g_static_mu;
 static void *g_static_addr[64];
 
-static awe_status static_scratch(int dev, unsigned char **out) {
+static awe_status static_scratch(int dev, cudaStream_t s, unsigned char **out) {
     if (dev < 0 || dev >= 64) {
         set_error("device index %d beyond the static-scratch table", dev);
         return AWE_ERR_INVALID;
     }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) {
+        cudaGetLastError();
+        cap = cudaStreamCaptureStatusNone;
+    }
     std::lock_guard<std::mutex> lk(g_static_mu);
-    if (!g_static_addr[dev]) {
+    if (cap == cudaStreamCaptureStatusNone || !g_static_addr[dev]) {
         void *ptr = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&ptr, g_static_scratch);
         if (e != cudaSuccess || !ptr) {
@@ -151,19 +160,21 @@ extern "C" awe_status awe_forward2d_noalloc(const awe_desc *desc, const float *d
         set_error("awe_forward2d_noalloc: null or negative argument");
         return AWE_ERR_INVALID;
     }
+    // awe_plan_create's checks first, then what this path leaves out
+    const awe_status chk = check_desc(desc);
+    if (chk != AWE_OK) return chk;
     const awe_desc &d = *desc;
     if (d.ndim != 2 || d.coords != AWE_CART || d.scheme != AWE_SCHEME_CPU) {
         set_error("awe_forward2d_noalloc: only the 2D cartesian CPU-program scheme is available without allocation");
         return AWE_ERR_UNSUPPORTED;
     }
-    if (d.hybrid || d.jsnap != 0) {
-        set_error("awe_forward2d_noalloc: hybrid ABC and snapshots need awe_forward");
+    if (d.hybrid || d.jsnap != 0 || d.bnds || d.refl) {
+        set_error("awe_forward2d_noalloc: hybrid ABC, snapshots and reflectivity injection need awe_forward");
         return AWE_ERR_UNSUPPORTED;
     }
     const int fdorder = d.fdorder ? d.fdorder : 4;
-    if (fdorder < 2 || fdorder > 2 * kMaxNop || (fdorder & 1) || d.nt < 1 || !(d.dt > 0.f) || d.n[0] < 1 ||
-        d.n[1] < 1 || !(d.d[0] > 0.f) || !(d.d[1] > 0.f) || (ncs != 1 && ncs != ns)) {
-        set_error("awe_forward2d_noalloc: invalid descriptor (fdorder %d, nt %d, ncs %d)", fdorder, d.nt, ncs);
+    if (ncs != 1 && ncs != ns) {
+        set_error("awe_forward2d_noalloc: ncs must be 1 or ns (ncs %d, ns %d)", ncs, ns);
         return AWE_ERR_INVALID;
     }
     const int nop = fdorder / 2;
@@ -182,10 +193,10 @@ extern "C" awe_status awe_forward2d_noalloc(const awe_desc *desc, const float *d
         set_error("awe_forward2d_noalloc: no CUDA device");
         return AWE_ERR_NODEVICE;
     }
-    unsigned char *base = nullptr;
-    awe_status st = static_scratch(dev, &base);
-    if (st != AWE_OK) return st;
     cudaStream_t s = (cudaStream_t)stream;
+    unsigned char *base = nullptr;
+    awe_status st = static_scratch(dev, s, &base);
+    if (st != AWE_OK) return st;
 
     float *u0 = (float *)(base + kOffU0), *u1 = (float *)(base + kOffU1), *vel = (float *)(base + kOffVel);
     float *w1 = (float *)(base + kOffW1), *w2 = (float *)(base + kOffW2), *w3 = (float *)(base + kOffW3);
@@ -236,7 +247,7 @@ extern "C" awe_status awe_forward2d_noalloc(const awe_desc *desc, const float *d
     sp.sponge_new = 0;
     sp.shell = 0;
     const bool exact = d.precision == AWE_EXACT;
-    const int jdata = d.jdata > 0 ? d.jdata : 1;
+    const int jdata = d.jdata > 0 ? d.jdata : 1;  // 0 = the default, 1
     float *cur = u1, *nxt = u0;
     int row = 0;
     for (int it = 0; it < d.nt; it++) {

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <climits>
 #include <cstring>
 #include <vector>
@@ -57,8 +58,27 @@ void plan_graph_drop(awe_plan *p) {
     p->g_ncs = 0;
 }
 
+// Optional cap on the device memory one plan may hold (AWE_DEVICE_BYTES_LIMIT,
+// bytes): a plan that would exceed it fails with AWE_ERR_NOMEM as if the
+// device were full, which lets callers keep a footprint and lets tests take
+// the out-of-memory paths without exhausting a shared GPU.
+static size_t device_bytes_limit() {
+    static const size_t lim = [] {
+        const char *e = std::getenv("AWE_DEVICE_BYTES_LIMIT");
+        return e && *e ? (size_t)std::strtoull(e, nullptr, 10) : (size_t)0;
+    }();
+    return lim;
+}
+
 awe_status dev_alloc(awe_plan *p, void **ptr, size_t bytes) {
     if (bytes == 0) bytes = 16;
+    const size_t lim = device_bytes_limit();
+    if (lim && p->device_bytes + bytes > lim) {
+        *ptr = nullptr;
+        set_error("device memory limit: %zu bytes held + %zu requested > AWE_DEVICE_BYTES_LIMIT %zu",
+                  p->device_bytes, bytes, lim);
+        return AWE_ERR_NOMEM;
+    }
     cudaError_t e = cudaMalloc(ptr, bytes);
     if (e != cudaSuccess) {
         set_error("cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
@@ -158,7 +178,7 @@ static awe_status check_pipeline(awe_plan *p) {
     return AWE_OK;
 }
 
-static awe_status check_desc(const awe_desc *d) {
+awe_status awe::check_desc(const awe_desc *d) {
     if (!d) {
         set_error("null descriptor");
         return AWE_ERR_INVALID;
@@ -207,6 +227,10 @@ static awe_status check_desc(const awe_desc *d) {
     }
     if (d->jsnap < 0 || d->jdata < 0) {
         set_error("jsnap and jdata must be >= 0");
+        return AWE_ERR_INVALID;
+    }
+    if (d->precision != AWE_FAST && d->precision != AWE_EXACT) {
+        set_error("unknown precision %d", d->precision);
         return AWE_ERR_INVALID;
     }
     return AWE_OK;

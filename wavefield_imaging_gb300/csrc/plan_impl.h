@@ -78,6 +78,10 @@ struct awe_plan {
     unsigned long long *sched_counter = nullptr;
     unsigned long long sched_base = 0;
     int *d_err = nullptr;
+    // polls of a pipeline wait before it reports a timeout (AWE_PIPELINE_SPIN_LIMIT;
+    // < 0: the kernel default); a limit of 0 makes every first wait time out,
+    // which the failure tests use to exercise the error path
+    long long spin_limit = -1;
 
     // the forward time loop captured as a CUDA graph (CPU-program scheme, no
     // snapshots, no profiling), replayed while its device pointers stay the same

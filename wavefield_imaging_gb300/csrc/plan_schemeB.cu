@@ -93,6 +93,8 @@ awe_status planB_init(awe_plan *p) {
         CUDA_TRY(cudaMemset(p->d_err, 0, sizeof(int)));
         p->sched_base = 0;
         if (stepB3_tma_maps(p->tmaps, p->u, p->vel, p->g)) p->use_tma = true;
+        const char *spin = std::getenv("AWE_PIPELINE_SPIN_LIMIT");
+        if (spin && *spin) p->spin_limit = std::atoll(spin);
     }
 
     p->nsmp = (d.nt - 1) / d.jdata + 1;
@@ -287,6 +289,7 @@ StepBParams stepB_params(const awe_plan *p) {
         sp.ihi[a] = sponge ? p->whi[a] : (a == 0 ? g.n1 : a == 1 ? g.n2 : g.n3);
     }
     sp.prv = nullptr;
+    sp.spin = p->spin_limit;
     return sp;
 }
 
