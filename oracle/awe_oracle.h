@@ -76,6 +76,12 @@ typedef struct {
 int orc_gpu_spher3d_fp64(const orc_gpar *p, const float *vel, const float *wav, int ns, const float *sou, int nr,
                          const float *rec, double *dat);
 
+/* sfAWEFDspher3Dgpu adj=y (MAWEFDspher3Dgpu.cu:449-566): data [nt][nr]
+ * injected, reversed in time, at the receivers; image [nph][nth][nra] is the
+ * wavefield's model window after step nt-kt; frames as the program writes
+ * them.  Returns the frames written (-1: kt outside [1, nt]). */
+int orc_gpu_spher3d_adj(const orc_gpar *p, const float *vel, const float *data, int nr, const float *rec, int kt,
+                        float *image, float *snaps);
 int orc_gpu_forward(int kind, const orc_gpar *p, const float *vel, const float *rfl, const float *wav, int ns,
                     const float *sou, int nr, const float *rec, float *dat, float *snaps);
 /* sfAWEFDcart2Dgpu's scheme on a moving geometry (expl = refl = 0): sou

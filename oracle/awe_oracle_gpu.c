@@ -603,9 +603,16 @@ static int gpu_polar2d(const orc_gpar *P, const float *vel_in, const float *wav,
 
 /* ------------------------------------------------------------------ */
 /* MAWEFDspher3Dgpu.cu:449-566.  vel [nph][nth][nra]; sou/rec (r, phi, theta);
- * dat [nt][nr] (one row per step). */
-static int gpu_spher3d(const orc_gpar *P, const float *vel_in, const float *wav, int ns, const float *sou, int nr,
-                       const float *rec, float *dat, float *snaps) {
+ * dat [nt][nr] (one row per step).
+ * adj_kt > 0: the program's adj=y branch.  The "sources" are then the
+ * receivers, the series injected at point s in step it is wav[(nt-1-it)*ns + s]
+ * (inject_sources_3D_adj, spher_kernels.cu:367-398: unscaled, the data row
+ * nt-1-it), nothing is extracted, frames are taken at it % jsnap == 0 and at
+ * it == nt-adj_kt, and after step nt-adj_kt the model window of the wavefield
+ * goes to image [nph][nth][nra] and the loop ends (:533-563).  Returns the
+ * frames written. */
+static int gpu_spher3d_impl(const orc_gpar *P, const float *vel_in, const float *wav, int ns, const float *sou, int nr,
+                            const float *rec, float *dat, float *snaps, int adj_kt, float *image) {
     const int nra = P->n1, nth = P->n2, nph = P->n3, nt = P->nt;
     const float dra = P->d1, dth = P->d2, dph = P->d3, dt = P->dt;
     const int nb = P->nb < NOPA ? NOPA : P->nb;
@@ -641,13 +648,14 @@ static int gpu_spher3d(const orc_gpar *P, const float *vel_in, const float *wav,
         }
 #define CS(iph, ith, ira) ((size_t)(iph) * sp + (size_t)(ith) * st + (ira))
     for (int it = 0; it < nt; it++) {
-        const float wa = wav[it];
         for (int s = 0; s < ns; s++) {
+            const float wa = adj_kt > 0 ? wav[(size_t)(nt - 1 - it) * ns + s] : wav[it];
             const glint *c = &cs[s];
             size_t b = CS(c->jy, c->jz, c->jx);
             float r = 1.f;
-            if (P->expl) r = refl3(v, npad, (long long)b, st, sp);
-            for (int k = 0; k < 8; k++) po[b + off[k]] += P->expl ? wa * c->w[k] * r : wa * c->w[k];
+            if (P->expl && adj_kt <= 0) r = refl3(v, npad, (long long)b, st, sp);
+            for (int k = 0; k < 8; k++)
+                po[b + off[k]] += (P->expl && adj_kt <= 0) ? wa * c->w[k] * r : wa * c->w[k];
         }
         /* solve_3D, spher_kernels.cu:455-526; the metric factors are the
          * kernel's own float expressions of (ra, th), evaluated once per
@@ -696,14 +704,14 @@ static int gpu_spher3d(const orc_gpar *P, const float *vel_in, const float *wav,
 #pragma omp parallel for
             for (size_t line = 0; line < (size_t)nthpad * nphpad - 1; line++)
                 for (int k = 0; k < 8 * ((nrapad + 7) / 8) - nrapad; k++) po[(line + 1) * nrapad + k] = 0;
-        for (int r = 0; r < nr; r++) {
+        for (int r = 0; r < nr && adj_kt <= 0; r++) {
             const glint *c = &cr[r];
             size_t b = CS(c->jy, c->jz, c->jx);
             float acc = po[b] * c->w[0];
             for (int k = 1; k < 8; k++) acc = acc + po[b + off[k]] * c->w[k];
             dat[(size_t)it * nr + r] = acc;
         }
-        if (snaps && P->jsnap > 0 && it % P->jsnap == 0) {
+        if (snaps && P->jsnap > 0 && (it % P->jsnap == 0 || (adj_kt > 0 && it == nt - adj_kt))) {
             if (P->bnds) {
                 memcpy(snaps + isnap * npad, po, npad * 4);
             } else {
@@ -714,6 +722,13 @@ static int gpu_spher3d(const orc_gpar *P, const float *vel_in, const float *wav,
                             dst[((size_t)iph * nth + ith) * nra + ira] = po[CS(nb + iph, nb + ith, nb + ira)];
             }
             isnap++;
+        }
+        if (adj_kt > 0 && it == nt - adj_kt) {
+            for (int iph = 0; iph < nph; iph++)
+                for (int ith = 0; ith < nth; ith++)
+                    for (int ira = 0; ira < nra; ira++)
+                        image[((size_t)iph * nth + ith) * nra + ira] = po[CS(nb + iph, nb + ith, nb + ira)];
+            break;
         }
     }
 #undef CS
@@ -727,7 +742,21 @@ static int gpu_spher3d(const orc_gpar *P, const float *vel_in, const float *wav,
     free(fpo);
     free(cs);
     free(cr);
-    return 0;
+    return (int)isnap;
+}
+
+static int gpu_spher3d(const orc_gpar *P, const float *vel_in, const float *wav, int ns, const float *sou, int nr,
+                       const float *rec, float *dat, float *snaps) {
+    return gpu_spher3d_impl(P, vel_in, wav, ns, sou, nr, rec, dat, snaps, 0, NULL) < 0;
+}
+
+/* sfAWEFDspher3Dgpu adj=y: data [nt][nr] back-injected at the receivers;
+ * image [nph][nth][nra]; snaps as the program writes them.  Returns the
+ * frames written, or -1 for kt outside [1, nt]. */
+int orc_gpu_spher3d_adj(const orc_gpar *P, const float *vel, const float *data, int nr, const float *rec, int kt,
+                        float *image, float *snaps) {
+    if (kt < 1 || kt > P->nt) return -1;
+    return gpu_spher3d_impl(P, vel, data, nr, rec, 0, NULL, NULL, snaps, kt, image);
 }
 
 /* The spherical scheme above with FP64 wavefields and arithmetic (inputs,

@@ -468,6 +468,48 @@ def spher3d_image(p: dict, vel, wav, sou, rec, data, condition: int):
     return img
 
 
+def spher3d_adj_frames(nt: int, kt: int, jsnap: int) -> int:
+    """Frames sfAWEFDspher3Dgpu adj=y snap=y writes: steps it <= nt-kt with
+    it % jsnap == 0, and step nt-kt."""
+    last = nt - kt
+    return last // jsnap + 1 + (1 if last % jsnap else 0)
+
+
+def spher3d_adj(p: dict, vel, data, rec, kt: int, use_reference_emulation: bool = False):
+    """sfAWEFDspher3Dgpu adj=y: data [nt][nr] back-injected (reversed in time,
+    unscaled) at the receivers rec [nr][3]; stops after step nt-kt.  p as for
+    gpu_scheme (jsnap > 0 with snap frames, bnds).  Returns (image
+    [nph][nth][nra], frames [nframes][...] or None).  use_reference_emulation
+    runs the reference's own kernels (oracle/_ref/libgpuref.so)."""
+    q = make_gpar(p)
+    vel = np.ascontiguousarray(vel, np.float32)
+    rec = np.ascontiguousarray(rec, np.float32).reshape(-1, 3)
+    nr = rec.shape[0]
+    data = np.ascontiguousarray(data, np.float32).reshape(q.nt, nr)
+    image = np.zeros(vel.shape, np.float32)
+    snaps = None
+    if q.jsnap > 0:
+        _, _, elems = gpu_shapes("spher3d", p, nr)
+        snaps = np.zeros((spher3d_adj_frames(q.nt, kt, q.jsnap), elems), np.float32)
+    if use_reference_emulation:
+        L = C.CDLL(os.path.join(REF_OUT, "libgpuref.so"))
+        fp = C.POINTER(C.c_float)
+        fn = L.gpuref_spher3d_adj
+        fn.argtypes = [C.POINTER(GPar), fp, fp, C.c_int, fp, C.c_int, fp, fp]
+        fn.restype = C.c_int
+    else:
+        fn = lib().orc_gpu_spher3d_adj
+        fn.argtypes = [C.POINTER(GPar), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_float),
+                       C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        fn.restype = C.c_int
+    n = fn(C.byref(q), _fp(vel), _fp(data), nr, _fp(rec), kt, _fp(image), _fp(snaps))
+    if n < 0:
+        raise ValueError("kt must be in [1, nt]")
+    if snaps is not None and n != snaps.shape[0]:
+        raise RuntimeError("adjoint run wrote %d frames, expected %d" % (n, snaps.shape[0]))
+    return image, snaps
+
+
 def spher3d_fp64(p: dict, vel, wav, sou, rec):
     """Traces [nt][nr] (float64) of the spherical GPU-program scheme with FP64
     wavefields; p as for gpu_scheme."""

@@ -528,6 +528,76 @@ int gpuref_spher3d(const gpuref_par *P, const float *vel, const float *wav, int 
 }
 
 // ---------------------------------------------------------------------------
+// sfAWEFDspher3Dgpu adj=y (MAWEFDspher3Dgpu.cu:449-566): data [nt][nr] go back
+// in at the receivers through inject_sources_3D_adj at row nt-it-1, no
+// extraction, frames at it % jsnap == 0 and at it == nt-kt, and after step
+// nt-kt the model window of po is the image.  inject_sources_3D_adj reads its
+// data sample before testing its thread index, so the data sit in a buffer
+// with slack behind them (threads past nr read it and drop it).  Returns the
+// frames written.
+int gpuref_spher3d_adj(const gpuref_par *P, const float *vel, const float *data, int nr, const float *rec, int kt,
+                       float *image, float *snaps) {
+    using namespace ref_spher;
+    const int nra = P->n1, nth = P->n2, nph = P->n3, nt = P->nt;
+    const float dra = P->d1, dth = P->d2, dph = P->d3, dt = P->dt;
+    if (kt < 1 || kt > nt) return -1;
+    int nb = P->nb < NOP ? NOP : P->nb;
+    sf_axis ara = sf_maxa(nra, P->o1, dra), ath = sf_maxa(nth, P->o2, dth), aph = sf_maxa(nph, P->o3, dph);
+    fdm3d fdm = fdutil3d_init(false, P->fsrf, ath, ara, aph, nb, 1);
+    const float oth = fdm->ozpad, ora = fdm->oxpad, oph = fdm->oypad;
+    const int nrapad = fdm->nxpad, nthpad = fdm->nzpad, nphpad = fdm->nypad;
+    const size_t npad = (size_t)nrapad * nthpad * nphpad;
+    std::vector<float> tt1(vel, vel + (size_t)nra * nth * nph), h_vel(npad);
+    expand_cpu_3D(tt1.data(), h_vel.data(), fdm->nb, nra, nrapad, nph, nphpad, nth, nthpad);
+    pt3d *rr = (pt3d *)calloc(nr > 0 ? nr : 1, sizeof(pt3d));
+    for (int i = 0; i < nr; i++) {
+        rr[i].x = rec[3 * i];
+        rr[i].y = rec[3 * i + 1];
+        rr[i].z = rec[3 * i + 2];
+    }
+    lint3d cr = lint3d_make(nr, rr, fdm);
+    std::vector<float> ww((size_t)nt * nr + 1024, 0.f);
+    memcpy(ww.data(), data, (size_t)nt * nr * sizeof(float));
+    std::vector<float> ppo(npad + kSlack, 0.f), po(npad + kSlack, 0.f), fpo(npad + kSlack, 0.f);
+    float ***oslice = sf_floatalloc3(nra, nth, nph);
+    const dim3 g3((unsigned)ceil(nrapad / 8.0f), (unsigned)ceil(nphpad / 8.0f), (unsigned)ceil(nthpad / 8.0f)),
+        b3(8, 8, 8);
+    size_t isnap = 0;
+    for (int it = 0; it < nt; it++) {
+        const int adjt = nt - it - 1;
+        dim3 gS(MIN(nr, (int)ceil(nr / 1024.0f)), 1, 1), bS(MIN(nr, 1024), 1, 1);
+        launch(gS, bS, [&] {
+            inject_sources_3D_adj(po.data(), ww.data(), cr->w000, cr->w001, cr->w010, cr->w011, cr->w100, cr->w101,
+                                  cr->w110, cr->w111, cr->jx, cr->jy, cr->jz, adjt, nr, nrapad, nphpad, nthpad);
+        });
+        launch(g3, b3, [&] {
+            solve_3D(fpo.data(), po.data(), ppo.data(), h_vel.data(), dra, dph, dth, ora, oph, oth, dt, nrapad,
+                     nphpad, nthpad);
+        });
+        launch(g3, b3, [&] { shift_3D(fpo.data(), po.data(), ppo.data(), nrapad, nphpad, nthpad); });
+        launch(g3, b3, [&] { spongeKernel_3D(po.data(), nrapad, nphpad, nthpad, nb); });
+        launch(g3, b3, [&] { spongeKernel_3D(ppo.data(), nrapad, nphpad, nthpad, nb); });
+        if (P->fsrf) launch(g3, b3, [&] { freeSurf_3D(po.data(), nrapad, nphpad, nthpad, nb); });
+        if (snaps && P->jsnap > 0 && (it % P->jsnap == 0 || it == nt - kt)) {
+            if (P->bnds)
+                memcpy(snaps + isnap * npad, po.data(), npad * sizeof(float));
+            else {
+                cut3d_sph(po.data(), oslice, fdm, ath, ara, aph);
+                memcpy(snaps + isnap * (size_t)nra * nth * nph, oslice[0][0],
+                       (size_t)nra * nth * nph * sizeof(float));
+            }
+            isnap++;
+        }
+        if (it == nt - kt) {
+            cut3d_sph(po.data(), oslice, fdm, ath, ara, aph);
+            memcpy(image, oslice[0][0], (size_t)nra * nth * nph * sizeof(float));
+            break;
+        }
+    }
+    return (int)isnap;
+}
+
+// ---------------------------------------------------------------------------
 // sfDYNAWEFDcart2Dgpu (MDYNAWEFDcart2Dgpu.cu:296-432): vel [nx][nz]; sou
 // ns*nst and rec nr*nrt (x, z) points; the kernels of dyn_cart_kernels.cu
 // pick entry k*(it+1) of each table.  Traces of every step go to row it

@@ -148,8 +148,32 @@ def make_dyn_inputs(case):
     return par, vel, wav, sou, rec
 
 
+# sfAWEFDspher3Dgpu adj=y: the traces of a forward run of the same case go
+# back in at the receivers; kt picks the image step nt-kt
+ADJ_CASES = [
+    dict(name="Aadj_spher3d_snap", base="A_spher3d_const", kt=30, jsnap=25, bnds=0, fsrf=0),
+    dict(name="Aadj_spher3d_free_bnds", base="A_spher3d_free_expl_bnds", kt=20, jsnap=20, bnds=1, fsrf=1),
+    dict(name="Aadj_spher3d_first_step", base="A_spher3d_const", kt=100, jsnap=0, bnds=0, fsrf=0),
+]
+
+
 def main(only=None):
     oracle.build(with_reference=True)
+    by_name = {c["name"]: c for c in CASES}
+    for case in ADJ_CASES:
+        if only and case["name"] not in only:
+            continue
+        base = dict(by_name[case["base"]], expl=0, jsnap=0, bnds=0)
+        par, vel, wav, sou, rec, _ = make_inputs(base)
+        data, _ = oracle.gpu_scheme("spher3d", par, vel, wav, sou, rec, use_reference_emulation=True)
+        par = dict(par, jsnap=case["jsnap"], bnds=case["bnds"], fsrf=case["fsrf"], kt=case["kt"])
+        image, snaps = oracle.spher3d_adj(par, vel, data, rec, case["kt"], use_reference_emulation=True)
+        out = dict(par=np.array(json.dumps(par)), vel=vel, data=data, sou=sou, rec=rec, image=image)
+        if snaps is not None:
+            out["snaps"] = snaps
+        np.savez_compressed(os.path.join(HERE, case["name"] + ".npz"), **out)
+        print("%-28s image %s max|image| %.3e frames %s" % (case["name"], image.shape, np.abs(image).max(),
+                                                            None if snaps is None else snaps.shape))
     for case in DYN_CASES:
         if only and case["name"] not in only:
             continue

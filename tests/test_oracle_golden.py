@@ -64,6 +64,24 @@ def test_gpu_scheme_oracle_matches_reference_kernels_bit_exact(path):
         assert np.array_equal(snaps, a["snaps"])
 
 
+GOLDEN_ADJ = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "Aadj_*.npz")))
+
+
+@pytest.mark.parametrize("path", GOLDEN_ADJ, ids=[os.path.basename(p)[:-4] for p in GOLDEN_ADJ])
+def test_spherical_adjoint_oracle_matches_reference_kernels_bit_exact(path):
+    """sfAWEFDspher3Dgpu adj=y: the traces back-injected at the receivers, the
+    image after step nt-kt and the frames, against the reference's kernels
+    run through the host emulation of the program's adj branch."""
+    par, a = load(path)
+    image, snaps = oracle.spher3d_adj(par, a["vel"], a["data"], a["rec"], par["kt"])
+    assert np.abs(a["image"]).max() > 0
+    assert np.array_equal(image, a["image"])
+    if "snaps" in a:
+        assert np.array_equal(snaps, a["snaps"])
+    else:
+        assert snaps is None
+
+
 def test_gpu_scheme_golden_set_covers_programs():
     kinds = {load(p)[0]["kind"] for p in GOLDEN_A}
     assert kinds == {"cart2d", "cart3d", "polar2d", "spher3d", "dyncart2d"}

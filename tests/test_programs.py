@@ -215,3 +215,46 @@ def test_cpu3d_program_adjoint_is_reversed_forward(bindir, tmp_path, fixture):
     assert int(h_adj["n2"]) == par["nt"]
     np.testing.assert_array_equal(d_adj, d_fwd)
     assert np.abs(d_adj).max() > 0
+
+
+def _spher_adj_inputs(tmp, par, a):
+    rsf.write(str(tmp / "vel.rsf"), a["vel"], [(n, o, d) for n, o, d in zip(par["n"], par["o"], par["d"])])
+    rsf.write(str(tmp / "sou.rsf"), a["sou"], [(3, 0.0, 1.0), (a["sou"].shape[0], 0.0, 1.0)])
+    rsf.write(str(tmp / "rec.rsf"), a["rec"], [(3, 0.0, 1.0), (a["rec"].shape[0], 0.0, 1.0)])
+    data = a["data"]
+    rsf.write(str(tmp / "wav.rsf"), data, [(data.shape[1], 0.0, 1.0), (par["nt"], 0.0, par["dt"])])
+    return ["vel=" + str(tmp / "vel.rsf"), "sou=" + str(tmp / "sou.rsf"), "rec=" + str(tmp / "rec.rsf")]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", golden_paths("Aadj_*.npz"), ids=lambda p: os.path.basename(p)[:-4])
+def test_spherical_program_adjoint_matches_reference_outputs(bindir, tmp_path, path):
+    """sfAWEFDspher3Dgpu adj=y: the traces on standard input go back in at the
+    receivers, reversed in time; the image (model window after step nt-kt)
+    and the frames of snap=y equal, bit for bit, what the reference's own
+    kernels give through the host emulation of the program's adj branch."""
+    par, a = load_golden(path)
+    jsnap = par.get("jsnap", 0)
+    args = _spher_adj_inputs(tmp_path, par, a)
+    args += ["adj=y", "kt=%d" % par["kt"], "nb=%d" % par["nb"], "snap=" + yn(jsnap > 0),
+             "bnds=" + yn(par.get("bnds", 0)), "free=" + yn(par.get("fsrf", 0)), "precision=exact"]
+    if jsnap > 0:
+        args.append("jsnap=%d" % jsnap)
+    out = run_program(bindir, "sfAWEFDspher3Dgpu", tmp_path, args)
+    img, hdr = rsf.read(str(out))
+    assert [int(hdr["n%d" % k]) for k in (1, 2, 3)] == list(par["n"])
+    np.testing.assert_array_equal(img.ravel(), a["image"].ravel())
+    if "snaps" in a:
+        wfl, whdr = rsf.read(str(tmp_path / "wfl.rsf"))
+        assert int(whdr["n4"]) == a["snaps"].shape[0]
+        np.testing.assert_array_equal(wfl.ravel(), a["snaps"].ravel())
+
+
+def test_spherical_program_adjoint_needs_a_reachable_image_step(bindir, tmp_path):
+    par, a = load_golden(golden_paths("Aadj_spher3d_snap.npz")[0])
+    args = _spher_adj_inputs(tmp_path, par, a) + ["adj=y", "kt=0", "nb=%d" % par["nb"]]
+    with open(tmp_path / "wav.rsf", "rb") as fin:
+        r = subprocess.run([os.path.join(bindir, "sfAWEFDspher3Dgpu"), *args], stdin=fin, capture_output=True,
+                           timeout=60)
+    assert r.returncode == 1
+    assert b"kt must be in [1, nt]" in r.stderr

@@ -165,8 +165,9 @@ void launch_adjA_sph(const float *X, float *Y, const float *A, const float *vel,
                      cudaStream_t s, bool xcorr = false);
 void launch_rec_adjA(float *z, const GeoPoint *pts, int nr, const float *r, const StepAParams &p, const long long *off,
                      cudaStream_t s);
+// wav [nt][ncs]: ncs = 1 (one wavelet for every source) or ns
 void launch_injectA(bool exact, int ndim, float *u, const GeoPoint *pts, const float *scale, int ns, const float *wav,
-                    int it, bool scaled, const long long *off, cudaStream_t s, int stride = 1);
+                    int it, bool scaled, const long long *off, cudaStream_t s, int stride = 1, int ncs = 1);
 void launch_snapshot_transpose2(const float *u, float *dst, const Grid &g, int f1, int f2, int m1, int m2,
                                 cudaStream_t s);
 

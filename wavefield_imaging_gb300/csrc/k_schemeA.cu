@@ -443,11 +443,13 @@ void launch_bcA(bool exact, const float *um, float *uo, float *aux, const StepAP
 // constant over time and prepared on the host.
 template <bool EXACT>
 __global__ void k_injectA(float *u, const GeoPoint *__restrict__ pts, const float *__restrict__ scale, int ns,
-                          const float *__restrict__ wav, int it, int ncorner, int scaled,
+                          const float *__restrict__ wav, int it, int ncs, int ncorner, int scaled,
                           const long long *__restrict__ off, int stride) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
-    const float wa = wav[it];
     for (int s = 0; s < ns; s++) {
+        // one wavelet for every source (ncs = 1), or one per source (the
+        // back-injected traces of sfAWEFDspher3Dgpu adj=y, row it of [nt][ns])
+        const float wa = wav[(long long)it * ncs + (ncs == 1 ? 0 : s)];
         const GeoPoint pt = pts[(long long)s * stride];
         for (int c = 0; c < ncorner; c++) {
             const long long n = pt.base + off[c];
@@ -459,11 +461,11 @@ __global__ void k_injectA(float *u, const GeoPoint *__restrict__ pts, const floa
 }
 
 void launch_injectA(bool exact, int ndim, float *u, const GeoPoint *pts, const float *scale, int ns, const float *wav,
-                    int it, bool scaled, const long long *off, cudaStream_t s, int stride) {
+                    int it, bool scaled, const long long *off, cudaStream_t s, int stride, int ncs) {
     if (ns <= 0) return;
     const int nc = ndim == 3 ? 8 : 4;
-    if (exact) k_injectA<true><<<1, 32, 0, s>>>(u, pts, scale, ns, wav, it, nc, scaled, off, stride);
-    else k_injectA<false><<<1, 32, 0, s>>>(u, pts, scale, ns, wav, it, nc, scaled, off, stride);
+    if (exact) k_injectA<true><<<1, 32, 0, s>>>(u, pts, scale, ns, wav, it, ncs, nc, scaled, off, stride);
+    else k_injectA<false><<<1, 32, 0, s>>>(u, pts, scale, ns, wav, it, ncs, nc, scaled, off, stride);
 }
 
 // polar snapshots are theta-fastest ([r][theta]) as sfAWEFDspher2Dgpu writes them

@@ -268,7 +268,7 @@ static awe_status gradient_spher_one(awe_plan *p, const float *d_wav, int ncs, c
         AWE_TRY(ckpt_load(p, 2 * seg + 1, slot + cells, s));
         for (int k = k0; k < k1; k++) {
             float *cur = slot + (size_t)(k - k0 + 1) * cells;
-            launch_injectA(false, 3, cur, p->src, nullptr, p->ns, d_wav, k, false, p->corner_off, s);
+            launch_injectA(false, 3, cur, p->src, nullptr, p->ns, d_wav, k, false, p->corner_off, s, 1, ncs);
             if (k + 1 < k1) launch_stepA_oop(pa.geom, false, cur, cur - cells, cur + cells, p->vel, pa, s);
             launches += (p->ns > 0) + (k + 1 < k1);
         }
@@ -310,6 +310,10 @@ static awe_status plan_gradient_spher(awe_plan *p, const float *d_wav, int ncs, 
     }
     const int nshot = p->pa.nshot > 1 ? p->pa.nshot : 1;
     if (nshot == 1) return gradient_spher_one(p, d_wav, ncs, d_dobs, T, fmt, d_grad, misfit, d_dsyn, s, image);
+    if (ncs != 1) {
+        set_error("awe_gradient: the shots of awe_set_shots share one wavelet (ncs = 1)");
+        return AWE_ERR_UNSUPPORTED;
+    }
     const long long cells = p->g.cells();
     const int NS = p->ns, NR = p->nr;
     int max_nr = 1;

@@ -323,7 +323,6 @@ static awe_status prepare_injection(awe_plan *p, bool &scaled) {
 // current level
 awe_status planA_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, float *d_wfl, cudaStream_t s,
                      const StepHook *hook) {
-    (void)ncs;
     const awe_desc &d = p->d;
     const Grid &g = p->g;
     const StepAParams &pa = p->pa;
@@ -347,7 +346,7 @@ awe_status planA_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, flo
         if (p->ns > 0) {
             const PointsAt ps = points_at(p, p->src, p->ns, p->src_rows, it);
             launch_injectA(exact, d.ndim, cur, ps.pts, p->inj_scale, p->ns, d_wav, it, scaled, p->corner_off, s,
-                           ps.stride);
+                           ps.stride, ncs);
             launches++;
         }
         prof_begin(p, s);

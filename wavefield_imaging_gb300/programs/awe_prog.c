@@ -15,7 +15,7 @@
  * Parameters and defaults are those of each program's main() (cited below).
  * Extra parameter: precision=exact|fast (default fast; exact reproduces the
  * reference's float/double evaluation bit for bit).
- * adj=y (backward injection, cpu programs):
+ * adj=y (backward injection):
  *   sfAWEFDcart2Dcpu (MAWEFDcart2Dcpu.c:304-316, :353-369): expl=n injects
  *   the traces on standard input ([nt][nr]) at the receivers, expl=y the
  *   one-component wavelet at the sources, both reversed in time; the run
@@ -25,10 +25,17 @@
  *   writes no image, so kt must be in [1, nt] here.
  *   sfAWEFDcart3Dcpu (MAWEFDcart3Dcpu.c:304-316): the wavelet reversed in
  *   time is injected at the sources; traces and snapshots as in a forward run.
- * Not provided: adj=y for the gpu programs (their back-injection indexes the
- * source weight tables with receiver indices, MAWEFDcart2Dgpu.cu:391-394),
- * sinc=y injection and the snapshot windows nq*=/oq*=/dq*= of the cpu
- * programs (they stop with an error).
+ *   sfAWEFDspher3Dgpu (MAWEFDspher3Dgpu.cu:452-463, :533-563): the traces on
+ *   standard input ([nt][nr]) go back in at the receivers, unscaled and
+ *   reversed in time (inject_sources_3D_adj, spher_kernels.cu:367-398); no
+ *   traces; snap=y writes the frames of the steps it % jsnap == 0 and of step
+ *   nt-kt; after step nt-kt its model window is the image (axes ra, th, ph)
+ *   on standard output.  kt in [1, nt] as above.
+ * Not provided: adj=y for sfAWEFDcart2Dgpu (its back-injection indexes the
+ * source weight tables with receiver indices, MAWEFDcart2Dgpu.cu:391-394) and
+ * the gpu programs that read no adj= (cart 3D, spher 2D), sinc=y injection
+ * and the snapshot windows nq*=/oq*=/dq*= of the cpu programs (they stop with
+ * an error).
  * Header differences: sfAWEFDspher3Dgpu's data and wavefield headers hold
  * the rows and frames actually written (the reference declares nt/jdata rows
  * and one frame more than it writes), and so does sfAWEFDcart2Dcpu adj=y
@@ -49,13 +56,15 @@ static void die(const char *what, const char *msg) {
 
 static rsf_file *g_wfl = NULL;
 
-/* 2D adj=y: the image is the frame of step img_it, cut from the padded
- * frame when bnds=y; snapshot frames go to wfl every wfl_j steps (0: none) */
+/* adj=y image runs (sfAWEFDcart2Dcpu, sfAWEFDspher3Dgpu): the image is the
+ * frame of step img_it, cut from the padded frame when bnds=y; snapshot
+ * frames go to wfl every wfl_j steps (0: none), and with img_frame the frame
+ * of step img_it too */
 static struct {
-    int img_it, wfl_j;
+    int img_it, wfl_j, img_frame;
     float *image;
-    int cut, nb, n1, n2, n1pad;
-} g_adj = {-1, 0, NULL, 0, 0, 0, 0, 0};
+    int cut, nb, n1, n2, n3, n1pad, n2pad;
+} g_adj = {-1, 0, 0, NULL, 0, 0, 0, 0, 1, 0, 0};
 
 static void write_frame(void *user, int isnap, int it, const float *frame, size_t n) {
     (void)user;
@@ -65,12 +74,17 @@ static void write_frame(void *user, int isnap, int it, const float *frame, size_
             if (!g_adj.cut) {
                 memcpy(g_adj.image, frame, n * sizeof(float));
             } else {
-                for (int i2 = 0; i2 < g_adj.n2; i2++)
-                    memcpy(g_adj.image + (size_t)i2 * g_adj.n1,
-                           frame + (size_t)(g_adj.nb + i2) * g_adj.n1pad + g_adj.nb, sizeof(float) * g_adj.n1);
+                const int nb = g_adj.nb, n3b = g_adj.n3 > 1 ? nb : 0;
+                for (int i3 = 0; i3 < g_adj.n3; i3++)
+                    for (int i2 = 0; i2 < g_adj.n2; i2++)
+                        memcpy(g_adj.image + ((size_t)i3 * g_adj.n2 + i2) * g_adj.n1,
+                               frame + ((size_t)(n3b + i3) * g_adj.n2pad + nb + i2) * g_adj.n1pad + nb,
+                               sizeof(float) * g_adj.n1);
             }
         }
-        if (g_adj.wfl_j == 0 || it % g_adj.wfl_j != 0) return;
+        const int periodic = g_adj.wfl_j > 0 && it % g_adj.wfl_j == 0;
+        const int last = g_adj.img_frame && g_adj.wfl_j > 0 && it == g_adj.img_it;
+        if (!periodic && !last) return;
     }
     if (rsf_write(g_wfl, frame, n) != n) die("wfl", "short write");
 }
@@ -113,7 +127,9 @@ int main(int argc, char **argv) {
     rsf_get_bool("adj", &adj);
     rsf_get_bool("verb", &verb);
     rsf_get_bool("sinc", &sinc);
-    if (adj && scheme != AWE_SCHEME_CPU) die(prog, "adj=y (back-injection imaging) is provided for the cpu programs");
+    const int spher3 = spher && ndim == 3;
+    if (adj && scheme != AWE_SCHEME_CPU && !spher3)
+        die(prog, "adj=y (back-injection imaging) is provided for the cpu programs and sfAWEFDspher3Dgpu");
     if (sinc) die(prog, "sinc=y injection is not provided");
     if (dyn) {
         int jd = 1;
@@ -229,7 +245,7 @@ int main(int argc, char **argv) {
      * row nt-1-it of the input with the row length it reads: nr traces for
      * the 2D program with expl=n, else the forward row length (ns, or 1 with
      * expl=y). */
-    const int img2d = adj && ndim == 2;
+    const int img2d = adj && (ndim == 2 || spher3); /* runs that end with an image */
     const int user_jsnap = d.jsnap;
     if (adj) {
         if (img2d) {
@@ -241,7 +257,8 @@ int main(int argc, char **argv) {
             g_adj.img_it = nt - kt;
             d.nt = g_adj.img_it + 1;
         }
-        const int row = img2d && !expl ? nr : wcs;
+        /* sfAWEFDspher3Dgpu reads row nt-1-it with nr samples whatever n1 is */
+        const int row = img2d && (spher3 || !expl) ? nr : wcs;
         if (nwav < (size_t)nt * row) die(prog, "adj=y: standard input holds fewer than nt rows");
         float *bw = malloc(sizeof(float) * (size_t)d.nt * row);
         for (int it = 0; it < d.nt; it++)
@@ -251,21 +268,29 @@ int main(int argc, char **argv) {
         wcs = row;
     }
     if (img2d) {
-        /* frames: the image step, plus the snapshots of snap=y; every step
-         * when the two do not share a period */
+        /* frames: the image step, plus the snapshots of snap=y (the engine
+         * delivers every gcd(jsnap, nt-kt)-th step and the callback keeps
+         * those) */
         g_adj.wfl_j = user_jsnap;
-        if (user_jsnap > 0)
-            d.jsnap = g_adj.img_it % user_jsnap == 0 ? user_jsnap : 1;
-        else
-            d.jsnap = g_adj.img_it > 0 ? g_adj.img_it : 1;
+        g_adj.img_frame = spher3;
+        int a = user_jsnap > 0 ? user_jsnap : g_adj.img_it, b = g_adj.img_it;
+        while (b > 0) {
+            const int t = a % b;
+            a = b;
+            b = t;
+        }
+        d.jsnap = a > 0 ? a : 1;
         d.jdata = 1;
+        if (spher3) d.expl = 0; /* unscaled, as inject_sources_3D_adj */
     }
 
     awe_plan *plan = NULL;
     if (awe_plan_create(&d, gpu, &plan) != AWE_OK) die(prog, awe_last_error());
     if (awe_set_model(plan, vel, den, scheme == AWE_SCHEME_GPU ? rfl : NULL) != AWE_OK) die(prog, awe_last_error());
-    if (img2d) { /* injection at the receivers (expl=n) or the sources (expl=y); no traces */
-        if (awe_set_geometry(plan, expl ? ns : nr, expl ? sou : rec, 0, NULL) != AWE_OK) die(prog, awe_last_error());
+    if (img2d) { /* injection at the receivers (expl=n, spherical) or the sources (expl=y); no traces */
+        const int at_src = expl && !spher3;
+        if (awe_set_geometry(plan, at_src ? ns : nr, at_src ? sou : rec, 0, NULL) != AWE_OK)
+            die(prog, awe_last_error());
     } else if (dyn) {
         if (awe_set_moving_geometry(plan, ns, nst, sou, nr, nrt, rec, AWE_MOVE_DYN) != AWE_OK)
             die(prog, awe_last_error());
@@ -275,18 +300,24 @@ int main(int argc, char **argv) {
     awe_info info;
     awe_plan_info(plan, &info);
     if (img2d) {
-        g_adj.image = calloc((size_t)d.n[0] * d.n[1], sizeof(float));
+        g_adj.image = calloc((size_t)d.n[0] * d.n[1] * d.n[2], sizeof(float));
         g_adj.cut = bnds;
         g_adj.nb = info.nbpad;
         g_adj.n1 = d.n[0];
         g_adj.n2 = d.n[1];
+        g_adj.n3 = d.n[2];
         g_adj.n1pad = info.npad[0];
+        g_adj.n2pad = info.npad[1];
         if (user_jsnap == 0) awe_set_snapshot_callback(plan, write_frame, NULL);
     }
 
     rsf_file *Fdat = rsf_output("out");
     if (!Fdat) die(prog, rsf_error());
-    if (img2d) { /* MAWEFDcart2Dcpu.c:362-363: the model axes */
+    if (img2d && spher3) { /* MAWEFDspher3Dgpu.cu:553-555: the model axes */
+        rsf_set_axis(Fdat, 1, d.n[0], d.o[0], d.d[0], "ra");
+        rsf_set_axis(Fdat, 2, d.n[1], d.o[1], d.d[1], "th");
+        rsf_set_axis(Fdat, 3, d.n[2], d.o[2], d.d[2], "ph");
+    } else if (img2d) { /* MAWEFDcart2Dcpu.c:362-363: the model axes */
         rsf_set_axis(Fdat, 1, d.n[0], d.o[0], d.d[0], "z");
         rsf_set_axis(Fdat, 2, d.n[1], d.o[1], d.d[1], "x");
     } else {
@@ -311,7 +342,9 @@ int main(int argc, char **argv) {
                 rsf_set_axis(g_wfl, a + 1, bnds ? info.npad[a] : d.n[a], o[a], d.d[a], lab[spher][a]);
         }
         if (img2d)
-            rsf_set_axis(g_wfl, ndim + 1, g_adj.img_it / user_jsnap + 1, ot, dt * user_jsnap, "t");
+            rsf_set_axis(g_wfl, ndim + 1,
+                         g_adj.img_it / user_jsnap + 1 + (g_adj.img_frame && g_adj.img_it % user_jsnap != 0), ot,
+                         dt * user_jsnap, "t");
         else
             rsf_set_axis(g_wfl, ndim + 1, info.nsnap, ot, dt * d.jsnap, "t");
         awe_set_snapshot_callback(plan, write_frame, NULL);
@@ -321,7 +354,7 @@ int main(int argc, char **argv) {
                       info.npad[2]);
     if (awe_forward(plan, wav, wcs, dat, NULL) != AWE_OK) die(prog, awe_last_error());
     if (img2d) {
-        const size_t nimg = (size_t)d.n[0] * d.n[1];
+        const size_t nimg = (size_t)d.n[0] * d.n[1] * d.n[2];
         if (rsf_write(Fdat, g_adj.image, nimg) != nimg) die(prog, "short write (image)");
     } else if (rsf_write(Fdat, dat, (size_t)info.nsmp * nr) != (size_t)info.nsmp * nr) {
         die(prog, "short write (dat)");
