@@ -6,8 +6,9 @@ expl=n, free=n (the reference's free-surface kernel writes past the end of
 its last line), traces every step.  Each program runs twice, with nt1 and
 nt2 steps; the difference of the wall times over nt2 - nt1 is the time per
 step, so reading the inputs and setting up cancel.  The traces of the two
-programs at nt2 are compared (rel-L2; the reference evaluates cos/sin of
-theta on the GPU per cell, the engine from host tables).
+programs at nt2 are compared (rel-L2), for the engine's AWE_FAST and
+AWE_EXACT arithmetic (the reference evaluates cos/sin of theta on the GPU per
+cell, the engine from host tables).
 
 Test infrastructure, run on a GPU machine after the build:
 
@@ -47,7 +48,7 @@ def write_inputs(tmp, nt):
     return w, rec.shape[0]
 
 
-def run(binary, tmp, nt, w, label):
+def run(binary, tmp, nt, w, label, precision="fast"):
     t = np.arange(nt) * w["dt"] - 0.1
     a = (np.pi * w["f0"] * t) ** 2
     wav = ((1 - 2 * a) * np.exp(-a)).astype(np.float32).reshape(nt, 1)
@@ -57,8 +58,8 @@ def run(binary, tmp, nt, w, label):
     args = [binary, "vel=" + os.path.join(tmp, "vel.rsf"), "sou=" + os.path.join(tmp, "sou.rsf"),
             "rec=" + os.path.join(tmp, "rec.rsf"), "nb=%d" % w["nb"], "expl=n", "free=n", "snap=n", "jdata=1",
             "gpu=0", "wfl=" + os.path.join(tmp, "wfl_%s.rsf" % label)]
-    if label == "engine":
-        args.append("precision=fast")
+    if label != "reference":
+        args.append("precision=" + precision)
     with open(wpath, "rb") as fin, open(out, "wb") as fout:
         t0 = time.perf_counter()
         r = subprocess.run(args, stdin=fin, stdout=fout, stderr=subprocess.PIPE, timeout=1200)
@@ -79,10 +80,17 @@ def main():
             s1, _ = run(binary, tmp, nt1, w, label)
             s2, d2 = run(binary, tmp, nt2, w, label)
             res[label] = dict(s_nt1=s1, s_nt2=s2, ms_per_step=1e3 * (s2 - s1) / (nt2 - nt1), traces=d2)
+        _, exact = run(eng_bin, tmp, nt2, w, "engine_exact", precision="exact")
     cells = int(np.prod([n + 2 * w["nb"] for n in w["n"]]))
-    ref, eng = res["reference"]["traces"].astype(np.float64), res["engine"]["traces"].astype(np.float64)
-    n = min(ref.size, eng.size)
-    rel = float(np.linalg.norm(eng.ravel()[:n] - ref.ravel()[:n]) / max(np.linalg.norm(ref.ravel()[:n]), 1e-300))
+    ref = res["reference"]["traces"].astype(np.float64).ravel()
+
+    def rel_to_ref(x):
+        x = np.asarray(x, np.float64).ravel()
+        n = min(ref.size, x.size)
+        return float(np.linalg.norm(x[:n] - ref[:n]) / max(np.linalg.norm(ref[:n]), 1e-300)), n
+
+    rel, n = rel_to_ref(res["engine"]["traces"])
+    rel_exact, _ = rel_to_ref(exact)
     out = {"workload": "spherical shell 700 x 512 x 512 (764 x 576 x 576 padded), nb 32, 1 source, %d receivers, "
                        "expl=n free=n, traces every step" % nr,
            "nt": [nt1, nt2], "padded_cells": cells,
@@ -95,7 +103,8 @@ def main():
                               "cell_updates_per_s": cells / (res["engine"]["ms_per_step"] / 1e3),
                               "wall_s": [res["engine"]["s_nt1"], res["engine"]["s_nt2"]]},
            "speedup": res["reference"]["ms_per_step"] / res["engine"]["ms_per_step"],
-           "traces_rel_l2_engine_vs_reference_gpu": rel, "trace_samples_compared": n}
+           "traces_rel_l2_engine_vs_reference_gpu": rel,
+           "traces_rel_l2_engine_exact_vs_reference_gpu": rel_exact, "trace_samples_compared": n}
     print(json.dumps(out))
 
 
