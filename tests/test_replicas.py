@@ -98,3 +98,69 @@ def test_shard_covers_every_shot_once():
     items = list(range(11))
     parts = [shard(items, r, 3) for r in range(3)]
     assert sorted(sum(parts, [])) == items
+
+
+def _engine_survey():
+    import bench
+
+    nt, nz = 300, 96
+    vtrue, shots = bench.batch_survey(nshots=12, nxm=700, nz=nz, seed=9)
+    shots = [(x0, min(nx, 200), sou, rec) for x0, nx, sou, rec in shots]
+    shots = [(max(0, min(700 - nx, int(sou[0, 0] / 5.0) - nx // 2)), nx, sou, rec) for _, nx, sou, rec in shots]
+    v0 = bench.smooth(vtrue, 4.0)
+    wav = bench.ricker(nt, 0.005, 5.0)
+    return vtrue, v0, shots, wav, nt, nz
+
+
+def _engine_desc(awe, vel, nt, nz):
+    return awe.make_desc(2, (nz, vel.shape[0]), (5.0, 5.0), (0.0, 0.0), nt, 0.005, nb=16, fdorder=8, dabc=1, expl=1,
+                         precision=awe.FAST)
+
+
+def _engine_rank(rank, world, port, out):
+    import torch.distributed as dist
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank))
+    import bench
+    import wavefield_imaging_gb300 as awe
+    from wavefield_imaging_gb300.replicas import survey_gradient
+
+    d, _, _, _ = bench.dist_init()
+    vtrue, v0, shots, wav, nt, nz = _engine_survey()
+    desc = _engine_desc(awe, vtrue, nt, nz)
+    with awe.Batch(desc, shots) as b:  # observed data, every shot on every rank
+        b.set_model(vtrue)
+        dobs = b.forward(wav)
+    # both ranks share the one GPU: their kernels never wait on each other;
+    # the gradients meet only in the host-side gloo sum
+    grad, J = survey_gradient(desc, shots, v0, wav, dobs, dist=d, device=0)
+    if rank == 0:
+        np.save(out, grad)
+        with open(out + ".txt", "w") as f:
+            f.write("%r" % J)
+    d.destroy_process_group()
+
+
+@pytest.mark.gpu
+def test_two_ranks_through_the_engine_match_one_process(tmp_path):
+    """The shot split through the engine: two ranks (gloo) each run the
+    batched gradient of half the shots; the reduced gradient and misfit equal
+    one process's batched gradient of all shots (up to the order of the FP64
+    sums)."""
+    import wavefield_imaging_gb300 as awe
+    from wavefield_imaging_gb300.replicas import survey_gradient
+
+    out = str(tmp_path / "g.npy")
+    mp.spawn(_engine_rank, args=(2, _free_port(), out), nprocs=2, join=True)
+    grad2 = np.load(out)
+    J2 = float(open(out + ".txt").read())
+    vtrue, v0, shots, wav, nt, nz = _engine_survey()
+    desc = _engine_desc(awe, vtrue, nt, nz)
+    with awe.Batch(desc, shots) as b:
+        b.set_model(vtrue)
+        dobs = b.forward(wav)
+    grad1, J1 = survey_gradient(desc, shots, v0, wav, dobs)
+    assert J1 > 0 and np.abs(grad1).max() > 0
+    np.testing.assert_allclose(grad2, grad1, rtol=1e-9, atol=1e-12 * np.abs(grad1).max())
+    assert abs(J2 - J1) <= 1e-9 * J1
