@@ -137,13 +137,57 @@ def padded(p: dict):
     return tuple(v.value for v in vals)
 
 
+def snapshot_window(p: dict, nbd: int, npad):
+    """The cpu programs' snapshot window as (count, first padded index,
+    stride) per axis z, x, y.  Parameters nq*, oq*, dq* default to the model
+    axes (MAWEFDcart2Dcpu.c:186-196, MAWEFDcart3Dcpu.c:180-195); first =
+    floor((oq - opad) / d) with opad = o - nb*d, stride = floor(dq / d), all in
+    float32 (fdutil.c:574-604 cut2d, :687-717 cut3d_slice, :292-293 and
+    :348-350 for opad).  3D bnds=y: the padded counts and whole z-x planes, y
+    planes still from oqy, dqy (MAWEFDcart3Dcpu.c:226-233, :341-353)."""
+    ndim = len(p["n"])
+    win = p.get("win", {})
+    out = []
+    f32 = np.float32
+    for a, ax in enumerate("zxy"):
+        if a >= ndim:
+            out.append((1, 0, 0))
+            continue
+        n, o, d = p["n"][a], f32(p["o"][a]), f32(p["d"][a])
+        nq = int(win.get("nq" + ax, n))
+        oq, dq = f32(win.get("oq" + ax, o)), f32(win.get("dq" + ax, d))
+        opad = f32(o - f32(nbd) * d)
+        first, stride = int(np.floor(f32(f32(oq - opad) / d))), int(np.floor(f32(dq / d)))
+        if p.get("bnds") and ndim == 3:
+            nq = npad[a]
+            if a < 2:
+                first, stride = 0, 1
+        if nq < 1 or first < 0 or stride < 0 or first + (nq - 1) * stride >= npad[a]:
+            raise ValueError("snapshot window on %s leaves the padded grid" % ax)
+        out.append((nq, first, stride))
+    return out
+
+
+def cut_window(frame, win, npad):
+    """One padded frame [n3pad][n2pad][n1pad] cut to the window of
+    snapshot_window, in the order the cpu programs write it (y planes, then
+    x columns, z fastest)."""
+    f = np.asarray(frame).reshape(npad[2], npad[1], npad[0])
+    idx = [first + stride * np.arange(n) for n, first, stride in win]
+    return f[np.ix_(idx[2], idx[1], idx[0])].ravel()
+
+
 def cart_cpu(p: dict, vel, wav, sou, rec, den=None, fp64: bool = False):
     """Run the scheme of MAWEFDcart{2D,3D}cpu.c.  Arrays are C-order numpy
     float32 with axis 1 last (vel [n2][n1] or [n3][n2][n1]).  Returns
-    (dat [nt][nr], snaps [nsnap][...] or None)."""
+    (dat [nt][nr], snaps [nsnap][...] or None); with p["win"] (nq*, oq*, dq*)
+    the frames are cut to that snapshot window as the programs write them."""
     q = make_par(p)
     ndim = 3 if q.n3 > 1 else 2
     nbd, n1p, n2p, n3p = padded(p)
+    windowed = bool(p.get("win")) and q.jsnap > 0 and not (ndim == 2 and q.bnds)
+    if windowed:
+        q.bnds = 1  # padded frames, cut below
     vel = np.ascontiguousarray(vel, np.float32)
     den = None if den is None else np.ascontiguousarray(den, np.float32)
     wav = np.ascontiguousarray(wav, np.float32)
@@ -160,6 +204,10 @@ def cart_cpu(p: dict, vel, wav, sou, rec, den=None, fp64: bool = False):
     rc = fn(C.byref(q), _fp(vel), _fp(den), _fp(wav), ns, _fp(sou), nr, _fp(rec), _fp(dat), _fp(snaps))
     if rc != 0:
         raise RuntimeError("oracle returned %d" % rc)
+    if windowed:
+        npad = (n1p, n2p, n3p)
+        win = snapshot_window(p, nbd, npad)
+        snaps = np.stack([cut_window(fr, win, npad) for fr in snaps])
     return dat, snaps
 
 

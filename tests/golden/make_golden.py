@@ -65,6 +65,9 @@ CASES_2D = [
     dict(name="c2d_o8_hybrid", n=(44, 50), nb=14, nt=300, fdorder=8, dabc=1, hybrid=1, expl=1, jsnap=0, seed=5),
     dict(name="c2d_o8_edge_geometry", n=(32, 36), nb=8, nt=200, fdorder=8, dabc=1, expl=1, jsnap=0, seed=6,
          edge=1),
+    # snapshot window reaching into the padding, with strides and a non-node origin
+    dict(name="c2d_o8_window", n=(48, 64), nb=12, nt=200, fdorder=8, dabc=1, expl=1, jsnap=50, seed=7,
+         win=dict(nqz=20, oqz=-20.0, dqz=10.0, nqx=15, oqx=32.5, dqx=15.0)),
 ]
 CASES_3D = [
     dict(name="c3d_o8_sponge", n=(22, 24, 20), nb=8, nt=140, fdorder=8, dabc=1, expl=1, jsnap=70, seed=11),
@@ -77,6 +80,12 @@ CASES_3D = [
     dict(name="c3d_o8_tma_shape", n=(24, 20, 18), nb=8, nt=120, fdorder=8, dabc=1, expl=1, jsnap=60, seed=15),
     dict(name="c3d_o8_tma_free", n=(28, 22, 20), nb=10, nt=100, fdorder=8, dabc=1, fsrf=1, expl=0, ns=2, jsnap=0,
          seed=16),
+    # snapshot window on all three axes, partly in the padding
+    dict(name="c3d_o8_window", n=(24, 20, 18), nb=8, nt=80, fdorder=8, dabc=1, expl=1, jsnap=40, seed=17,
+         win=dict(nqz=10, oqz=-15.0, dqz=10.0, nqx=6, oqx=12.0, dqx=5.0, nqy=4, oqy=-10.0, dqy=15.0)),
+    # bnds=y: whole padded planes; oqy at the padded origin keeps the reference's y planes on the grid
+    dict(name="c3d_o8_bnds", n=(24, 20, 18), nb=8, nt=80, fdorder=8, dabc=1, expl=1, jsnap=40, bnds=1, seed=18,
+         win=dict(oqy=-40.0)),
 ]
 
 
@@ -133,6 +142,8 @@ def make_inputs(case):
                optfd=case.get("optfd", 0), dabc=case.get("dabc", 0), fsrf=case.get("fsrf", 0),
                hybrid=case.get("hybrid", 0), expl=case.get("expl", 0), jsnap=case.get("jsnap", 0),
                bnds=case.get("bnds", 0))
+    if case.get("win"):
+        par["win"] = case["win"]
     return par, vel, den, wav, sou, rec
 
 
@@ -162,6 +173,7 @@ def run_reference(par, vel, den, wav, sou, rec, tmp):
         args.append("cden=y")
     if par["jsnap"] > 0:
         args += ["snap=y", "jsnap=%d" % par["jsnap"], "wfl=wfl.rsf", "bnds=" + yn(par["bnds"])]
+        args += ["%s=%s" % (k, v) for k, v in par.get("win", {}).items()]
     with open(os.path.join(tmp, "wav.rsf")) as fin, open(os.path.join(tmp, "dat.rsf"), "w") as fout:
         subprocess.check_call(args, stdin=fin, stdout=fout, stderr=subprocess.DEVNULL, cwd=tmp)
     dat = np.fromfile(os.path.join(tmp, "dat.rsf@"), dtype="<f4").reshape(nt, rec.shape[0])
@@ -173,7 +185,10 @@ def run_reference(par, vel, den, wav, sou, rec, tmp):
 
 def main():
     oracle.build(with_reference=True)
+    only = set(sys.argv[1:])  # case names to (re)make; all when none are given
     for case in CASES_2D + CASES_3D:
+        if only and case["name"] not in only:
+            continue
         par, vel, den, wav, sou, rec = make_inputs(case)
         with tempfile.TemporaryDirectory() as tmp:
             dat, snaps = run_reference(par, vel, den, wav, sou, rec, tmp)

@@ -96,6 +96,7 @@ def test_cpu_program_matches_reference_outputs(bindir, tmp_path, path):
         args.append("nb=%d" % par["nb"])
     if jsnap > 0:
         args.append("jsnap=%d" % jsnap)
+    args += ["%s=%s" % (k, v) for k, v in par.get("win", {}).items()]  # snapshot window
     name = "sfAWEFDcart%dDcpu" % len(par["n"])
     out = run_program(bindir, name, tmp_path, args)
     dat, _ = rsf.read(str(out))
@@ -105,6 +106,26 @@ def test_cpu_program_matches_reference_outputs(bindir, tmp_path, path):
         np.testing.assert_array_equal(wfl.ravel(), a["snaps"].ravel())
 
 
+@pytest.mark.gpu
+def test_cpu_program_snapshot_window_header_and_errors(bindir, tmp_path):
+    """The window's axes in the wavefield header (sf_maxa(nq, oq, dq),
+    MAWEFDcart2Dcpu.c:194-204), and a window that leaves the padded grid or
+    an adj=y window whose size differs from the model's stops with an error."""
+    par, a = load_golden(golden_paths("c2d_o8_window.npz")[0])
+    base = write_inputs(tmp_path, par, a) + ["fdorder=8", "dabc=y", "expl=y", "nb=%d" % par["nb"], "snap=y",
+                                             "jsnap=%d" % par["jsnap"]]
+    run_program(bindir, "sfAWEFDcart2Dcpu", tmp_path, base + ["%s=%s" % kv for kv in par["win"].items()])
+    _, hdr = rsf.read(str(tmp_path / "wfl.rsf"))
+    w = par["win"]
+    assert [int(hdr["n1"]), int(hdr["n2"]), int(hdr["n3"])] == [w["nqz"], w["nqx"], (par["nt"] - 1) // 50 + 1]
+    assert [float(hdr["o1"]), float(hdr["o2"]), float(hdr["d1"]), float(hdr["d2"])] == [w["oqz"], w["oqx"], w["dqz"],
+                                                                                        w["dqx"]]
+    for bad, msg in ((["oqz=-100"], "outside the padded grid"), (["nqx=40", "dqx=15"], "outside the padded grid"),
+                     (["adj=y", "kt=10", "nqz=20"], "must equal the model's")):
+        with pytest.raises(AssertionError, match=msg):
+            run_program(bindir, "sfAWEFDcart2Dcpu", tmp_path, base + bad)
+
+
 def _run_bare(bindir, name, args):
     return subprocess.run([os.path.join(bindir, name), *args], stdin=subprocess.DEVNULL, capture_output=True,
                           timeout=60)
@@ -112,8 +133,7 @@ def _run_bare(bindir, name, args):
 
 @pytest.mark.parametrize("name,arg,msg", [("sfAWEFDcart2Dgpu", "adj=y", "adj=y"),
                                           ("sfDYNAWEFDcart2Dgpu", "jdata=2", "jdata must be 1"),
-                                          ("sfAWEFDcart2Dcpu", "sinc=y", "sinc=y"),
-                                          ("sfAWEFDcart2Dcpu", "nqz=10", "snapshot windows")])
+                                          ("sfAWEFDcart2Dcpu", "sinc=y", "sinc=y")])
 def test_unsupported_options_stop_with_an_error(bindir, name, arg, msg):
     r = _run_bare(bindir, name, [arg])
     assert r.returncode == 1

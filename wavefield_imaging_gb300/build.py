@@ -98,8 +98,9 @@ def build_programs() -> str:
         srcs = [os.path.join(PROGS, main_src), os.path.join(PROGS, "rsfio.c")]
         deps = srcs + [os.path.join(PROGS, "rsfio.h"), os.path.join(ROOT, "include", "awe.h"), LIB]
         if not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(x) for x in deps):
-            cmd = ["gcc", "-O2", "-std=c11", "-D_GNU_SOURCE", "-Wall", "-I" + os.path.join(ROOT, "include"),
-                   "-I" + PROGS, *srcs, "-o", exe, "-L" + OUT, "-lawe", "-Wl,-rpath,$ORIGIN/.."]
+            cmd = ["gcc", "-O2", "-std=c11", "-D_GNU_SOURCE", "-Wall", "-ffp-contract=off",
+                   "-I" + os.path.join(ROOT, "include"), "-I" + PROGS, *srcs, "-o", exe, "-L" + OUT, "-lawe",
+                   "-lm", "-Wl,-rpath,$ORIGIN/.."]
             r = subprocess.run(cmd, capture_output=True, text=True)
             if r.returncode != 0:
                 raise RuntimeError("program link failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))

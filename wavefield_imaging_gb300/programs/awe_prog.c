@@ -31,17 +31,30 @@
  *   traces; snap=y writes the frames of the steps it % jsnap == 0 and of step
  *   nt-kt; after step nt-kt its model window is the image (axes ra, th, ph)
  *   on standard output.  kt in [1, nt] as above.
+ * Snapshot windows of the cpu programs (snap=y; MAWEFDcart2Dcpu.c:186-205,
+ * MAWEFDcart3Dcpu.c:180-203): nq*, oq*, dq* per axis, defaults the model's
+ * axes; frames hold nq* samples from padded index floor((oq - opad)/d) with
+ * stride floor(dq/d) (fdutil.c cut2d, cut3d_slice; opad = o - nb*d).  bnds=y
+ * writes whole padded frames in 2D (the window then only sets the adj=y
+ * image axes) and, in 3D, whole padded z-x planes of the nypad y planes the
+ * y window picks (MAWEFDcart3Dcpu.c:341-353).  A window that leaves the
+ * padded grid is an error (the reference reads outside its arrays); so is
+ * adj=y with a window whose nqz, nqx differ from the model's (the image
+ * buffer has the window's size, MAWEFDcart2Dcpu.c:247, :356-366).
  * Not provided: adj=y for sfAWEFDcart2Dgpu (its back-injection indexes the
  * source weight tables with receiver indices, MAWEFDcart2Dgpu.cu:391-394) and
- * the gpu programs that read no adj= (cart 3D, spher 2D), sinc=y injection
- * and the snapshot windows nq*=/oq*=/dq*= of the cpu programs (they stop with
- * an error).
+ * the gpu programs that read no adj= (cart 3D, spher 2D) and sinc=y
+ * injection (they stop with an error).
+ * sfAWEFDcart3Dcpu bnds=y without oqy: the reference starts the y planes at
+ * index nb of the padded grid and reads nb planes past its end; here the
+ * nypad planes of the padded grid are written (the frames of oqy = oy - nb*dy).
  * Header differences: sfAWEFDspher3Dgpu's data and wavefield headers hold
  * the rows and frames actually written (the reference declares nt/jdata rows
  * and one frame more than it writes), and so does sfAWEFDcart2Dcpu adj=y
  * snap=y (the reference declares the frames of all nt steps).
  * Errors print to stderr and exit 1, as sf_error. */
 #include <libgen.h>
+#include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -66,6 +79,32 @@ static struct {
     int cut, nb, n1, n2, n3, n1pad, n2pad;
 } g_adj = {-1, 0, 0, NULL, 0, 0, 0, 0, 1, 0, 0};
 
+/* snapshot window (cpu programs): per axis (z, x, y) nq samples from padded
+ * index f with stride j; frames are cut from the engine's padded frames */
+static struct {
+    int on;
+    int n[3], f[3], j[3], npad[3];
+    float *buf;
+} g_win;
+
+static void put_frame(const float *frame, size_t n) {
+    if (!g_win.on) {
+        if (rsf_write(g_wfl, frame, n) != n) die("wfl", "short write");
+        return;
+    }
+    const size_t plane = (size_t)g_win.npad[0] * g_win.npad[1], nout = (size_t)g_win.n[0] * g_win.n[1];
+    if (n != plane * g_win.npad[2]) die("wfl", "frame size differs from the padded grid");
+    for (int iy = 0; iy < g_win.n[2]; iy++) {
+        const float *p = frame + (size_t)(g_win.f[2] + iy * g_win.j[2]) * plane;
+        for (int ix = 0; ix < g_win.n[1]; ix++) {
+            const float *col = p + (size_t)(g_win.f[1] + ix * g_win.j[1]) * g_win.npad[0] + g_win.f[0];
+            float *out = g_win.buf + (size_t)ix * g_win.n[0];
+            for (int iz = 0; iz < g_win.n[0]; iz++) out[iz] = col[(size_t)iz * g_win.j[0]];
+        }
+        if (rsf_write(g_wfl, g_win.buf, nout) != nout) die("wfl", "short write");
+    }
+}
+
 static void write_frame(void *user, int isnap, int it, const float *frame, size_t n) {
     (void)user;
     (void)isnap;
@@ -86,7 +125,7 @@ static void write_frame(void *user, int isnap, int it, const float *frame, size_
         const int last = g_adj.img_frame && g_adj.wfl_j > 0 && it == g_adj.img_it;
         if (!periodic && !last) return;
     }
-    if (rsf_write(g_wfl, frame, n) != n) die("wfl", "short write");
+    put_frame(frame, n);
 }
 
 int main(int argc, char **argv) {
@@ -136,11 +175,17 @@ int main(int argc, char **argv) {
         rsf_get_int("jdata", &jd);
         if (jd != 1) die(prog, "jdata must be 1 (the reference writes every step into a buffer of nt/jdata rows)");
     }
-    {
-        static const char *win[] = {"nqz", "nqx", "nqy", "oqz", "oqx", "oqy", "dqz", "dqx", "dqy"};
-        for (int i = 0; i < 9; i++)
-            if (rsf_get_string(win[i])) die(prog, "snapshot windows (nq*/oq*/dq*) are not provided");
-    }
+    /* snapshot window parameters (read by the cpu programs with snap=y); a
+     * given window makes the engine deliver padded frames, which are cut here
+     * (2D bnds=y frames are written whole) */
+    static const char *win_n[3] = {"nqz", "nqx", "nqy"}, *win_o[3] = {"oqz", "oqx", "oqy"},
+                      *win_d[3] = {"dqz", "dqx", "dqy"};
+    const int windows = scheme == AWE_SCHEME_CPU && snap;
+    int win_given = 0;
+    if (windows)
+        for (int a = 0; a < ndim; a++)
+            win_given |= rsf_get_string(win_n[a]) || rsf_get_string(win_o[a]) || rsf_get_string(win_d[a]);
+    g_win.on = win_given && !(ndim == 2 && bnds);
     const char *prec_s = rsf_get_string("precision");
     const int precision = (prec_s && strcmp(prec_s, "exact") == 0) ? AWE_EXACT : AWE_FAST;
     int gpu = 0;
@@ -184,7 +229,7 @@ int main(int argc, char **argv) {
         d.jsnap = nt;
         rsf_get_int("jsnap", &d.jsnap);
     }
-    d.bnds = bnds;
+    d.bnds = bnds || g_win.on;
     d.fsrf = fsrf;
     d.expl = expl;
     d.refl = refl && expl;
@@ -299,9 +344,52 @@ int main(int argc, char **argv) {
     }
     awe_info info;
     awe_plan_info(plan, &info);
+    /* window axes (n, o, d) per axis; 3D bnds=y keeps the window's o and d
+     * with the padded n (MAWEFDcart3Dcpu.c:226-233) */
+    int wn[3];
+    float wo[3], wd[3];
+    for (int a = 0; a < 3; a++) {
+        wn[a] = d.n[a];
+        wo[a] = d.o[a];
+        wd[a] = d.d[a];
+        if (windows && a < ndim) {
+            rsf_get_int(win_n[a], &wn[a]);
+            rsf_get_float(win_o[a], &wo[a]);
+            rsf_get_float(win_d[a], &wd[a]);
+        }
+    }
+    if (windows && ndim == 3 && bnds)
+        for (int a = 0; a < 3; a++) wn[a] = info.npad[a];
+    if (g_win.on) {
+        static const char *axis[3] = {"z", "x", "y"};
+        for (int a = 0; a < 3; a++) {
+            const float opad = d.o[a] - (float)info.nbpad * d.d[a];
+            int f = a < ndim ? (int)floorf((wo[a] - opad) / d.d[a]) : 0;
+            int j = a < ndim ? (int)floorf(wd[a] / d.d[a]) : 0;
+            if (bnds && a < 2) { /* whole z-x planes */
+                f = 0;
+                j = 1;
+            }
+            const long last = (long)f + (long)(wn[a] - 1) * j;
+            if (wn[a] < 1 || f < 0 || j < 0 || last >= info.npad[a]) {
+                char msg[160];
+                snprintf(msg, sizeof msg, "snapshot window on %s: samples %d..%ld (stride %d) outside the padded "
+                         "grid 0..%d", axis[a], f, last, j, info.npad[a] - 1);
+                die(prog, msg);
+            }
+            g_win.n[a] = wn[a];
+            g_win.f[a] = f;
+            g_win.j[a] = j;
+            g_win.npad[a] = info.npad[a];
+        }
+        g_win.buf = malloc(sizeof(float) * (size_t)g_win.n[0] * g_win.n[1]);
+    }
+    if (img2d && windows && (wn[0] != d.n[0] || wn[1] != d.n[1]))
+        die(prog, "adj=y: the image is written with the snapshot window's axes, so nqz and nqx must equal the "
+                  "model's");
     if (img2d) {
         g_adj.image = calloc((size_t)d.n[0] * d.n[1] * d.n[2], sizeof(float));
-        g_adj.cut = bnds;
+        g_adj.cut = d.bnds;
         g_adj.nb = info.nbpad;
         g_adj.n1 = d.n[0];
         g_adj.n2 = d.n[1];
@@ -317,9 +405,9 @@ int main(int argc, char **argv) {
         rsf_set_axis(Fdat, 1, d.n[0], d.o[0], d.d[0], "ra");
         rsf_set_axis(Fdat, 2, d.n[1], d.o[1], d.d[1], "th");
         rsf_set_axis(Fdat, 3, d.n[2], d.o[2], d.d[2], "ph");
-    } else if (img2d) { /* MAWEFDcart2Dcpu.c:362-363: the model axes */
-        rsf_set_axis(Fdat, 1, d.n[0], d.o[0], d.d[0], "z");
-        rsf_set_axis(Fdat, 2, d.n[1], d.o[1], d.d[1], "x");
+    } else if (img2d) { /* MAWEFDcart2Dcpu.c:362-363: the model axes, or the window's with snap=y */
+        rsf_set_axis(Fdat, 1, d.n[0], wo[0], wd[0], "z");
+        rsf_set_axis(Fdat, 2, d.n[1], wo[1], wd[1], "x");
     } else {
         rsf_set_axis(Fdat, 1, nr, rsf_o(Frec, 2), rsf_d(Frec, 2), "r");
         rsf_set_axis(Fdat, 2, info.nsmp, ot, dt * d.jdata, "t");
@@ -336,6 +424,9 @@ int main(int argc, char **argv) {
         if (spher && ndim == 2) { /* theta fastest */
             rsf_set_axis(g_wfl, 1, bnds ? info.npad[1] : d.n[1], o[1], d.d[1], "th");
             rsf_set_axis(g_wfl, 2, bnds ? info.npad[0] : d.n[0], o[0], d.d[0], "ra");
+        } else if (windows && !(ndim == 2 && bnds)) { /* the window's axes */
+            const char *lab[3] = {"z", "x", "y"};
+            for (int a = 0; a < ndim; a++) rsf_set_axis(g_wfl, a + 1, wn[a], wo[a], wd[a], lab[a]);
         } else {
             const char *lab[2][3] = {{"z", "x", "y"}, {"ra", "th", "ph"}};
             for (int a = 0; a < ndim; a++)
@@ -376,5 +467,6 @@ int main(int argc, char **argv) {
     free(wav);
     free(dat);
     free(g_adj.image);
+    free(g_win.buf);
     return 0;
 }
