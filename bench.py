@@ -559,13 +559,14 @@ def extra_spherical_forward(args, local, peak, peak_kind):
         ms = e0.elapsed_time(e1)
         kern_ms, kern_n = plan.profile_read()
         plan.profile(False)
+        kernel = SPHER_KERNEL[plan.step_kernel]
     cells = nshots * int(np.prod([n + 2 * w["nb"] for n in w["n"]]))
     avg = kern_ms / 1e3 / max(kern_n, 1)
     achieved = BYTES_PER_CELL * cells / avg / 1e9
     return {"workload": w["name"].replace("1 source", "%d sources along the track, one launch per step" % nshots)
                         + " (%d of 3000 steps)" % nt,
             "value": cells * nt / (ms / 1e3), "unit": "cell-updates/s", "ms_per_run": ms,
-            "roofline": {"kernel": "k_stepA_sph_march2", "avg_launch_us": avg * 1e6, "achieved": achieved,
+            "roofline": {"kernel": kernel, "avg_launch_us": avg * 1e6, "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind}}
 
 
@@ -879,6 +880,10 @@ def run_batch_grad(args):
     print(json.dumps(out))
 
 
+# the spherical step kernel a plan runs (Plan.step_kernel)
+SPHER_KERNEL = {"tma_sph": "k_stepA_sph_tma", "simple": "k_stepA_sph_march2"}
+
+
 def spher_workload(nt, nr=700, nang=512):
     return dict(name="3D spherical shell (GPU-program scheme, metric terms), r in [3387.0, 3390.5] km at 5 m, "
                      "theta and phi %d x 0.04/%d rad at the equator, nb=32, nt=%d, 1 source, 64x64 receivers"
@@ -1069,7 +1074,7 @@ def run_spher(args):
            "config": {"workload": w["name"] + (", %d shots in one launch per step" % nshots if nshots > 1 else ""),
                       "padded_cells": cells, "shots": nshots},
            "plain_sequential": plain,
-           "roofline": {"bound": "hbm", "kernel": "k_stepA_sph_march2", "avg_launch_us": avg * 1e6,
+           "roofline": {"bound": "hbm", "kernel": SPHER_KERNEL[plan.step_kernel], "avg_launch_us": avg * 1e6,
                         "achieved": BYTES_PER_CELL * cells / avg / 1e9, "peak": peak, "unit": "GB/s",
                         "frac": BYTES_PER_CELL * cells / avg / 1e9 / peak, "peak_source": peak_kind,
                         "kernel_share": kern_ms / args.steps / ms},

@@ -108,7 +108,7 @@ typedef struct {
     int nsnap;         /* snapshots written by awe_forward */
     size_t snap_elems; /* floats per snapshot */
     size_t device_bytes; /* device memory held by the plan */
-    int step_kernel;     /* 0: one thread per cell; 1: TMA-staged 3D 8th-order kernel */
+    int step_kernel;     /* 0: register kernels; 1: TMA-staged 3D 8th-order kernel; 2: TMA-staged spherical kernel */
 } awe_info;
 
 typedef struct awe_plan awe_plan;

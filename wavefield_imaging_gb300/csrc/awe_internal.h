@@ -336,4 +336,14 @@ bool make_tmap_3d(CUtensorMap *m, const float *base, int n1, int n2, int n3, int
 // tensor-map boxes of the TMA step: the current level's halo box and the tile box
 void stepB3_tma_boxes(int *halo1, int *halo2, int *tile1, int *tile2);
 
+// TMA-staged spherical step (GPU-program scheme, AWE_FAST); Step3Launch's
+// ntz/ntx count the r and theta tiles, items include the shots
+bool sphA_tma_eligible(const Grid &g);
+// maps: [0] u[0] halo box, [1] u[1] halo box, [2] u[0] tile, [3] u[1] tile, [4] vel tile
+bool sphA_tma_maps(CUtensorMap *maps, float *const u[2], const float *vel, const Grid &g, int nshot);
+Step3Launch sphA_tma_shape(const Grid &g, int nshot, int num_sms, int L);
+cudaError_t launch_stepA_sph_tma(const CUtensorMap &cur, const CUtensorMap &prv, const CUtensorMap &vel, float *nxt,
+                                 const StepAParams &pa, const Step3Launch &sh, unsigned long long *counter,
+                                 unsigned long long base, int *err, long long spin, cudaStream_t s);
+
 }  // namespace awe

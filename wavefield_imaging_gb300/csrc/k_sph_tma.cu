@@ -1,0 +1,320 @@
+// Spherical-shell step of the GPU-program scheme (AWE_FAST), TMA-staged.
+//
+// The update is that of spher_kernels.cu:455-526 (solve_3D with the metric
+// terms A = 2/r, C = 1/r^2, B = cos/(r^2 sin), D = 1/(r^2 sin^2), precomputed
+// per (r) and (r, theta)) followed by the sponge of both time levels
+// (spongeKernel_3D, spher_kernels.cu:825) and the free-surface mask, with the
+// engine's two-buffer leapfrog: the new level overwrites the previous one and
+// the previous level's sponge is applied on read.
+//
+// A CTA owns a 64 (r) x 16 (theta) tile of one shot and marches along phi over
+// a chunk of planes.  Per plane one TMA copy (cp.async.bulk.tensor, mbarrier
+// completion) brings the current level's 72 x 18 box - r widened by 4 on each
+// side so the box starts on a 16-byte boundary, theta by 1 - into a 6-deep
+// shared-memory ring, and for the plane being updated the previous level's
+// and the velocity's 64 x 16 boxes, up to five planes ahead of the compute.
+// phi-neighbours come from a 3-plane register queue (each thread owns 4
+// consecutive radii of one theta row), r- and theta-neighbours from the halo
+// box; the 4-cell result is written with one 16-byte store.  Work items
+// (tile, phi chunk, shot) are handed out by a global atomic counter, so the
+// persistent grid (2 CTAs per SM) stays balanced.  Every wait is bounded; a
+// wait that gives up raises the plan's error flag and the CTA drains its
+// copies in flight before it leaves.
+//
+// The arithmetic per cell is that of k_stepA_sph_march2 (packed FP32x2,
+// the same operation order), so both kernels give the same AWE_FAST results.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstddef>
+
+#include "awe_internal.h"
+#include "tma.cuh"
+
+namespace awe {
+
+namespace sp3 {
+constexpr int TR = 64, TT = 16, HR = 4, HT = 1;
+constexpr int WR = TR + 2 * HR, WT = TT + 2 * HT;  // 72 x 18 halo box
+constexpr int RING = 6, NTHREADS = 256;
+constexpr uint32_t BYTES_HALO = WR * WT * 4, BYTES_TILE = TR * TT * 4;
+constexpr long long SPIN_LIMIT = 1ll << 22;
+
+// every box destination starts on a 128-byte boundary
+struct __align__(128) Stage {
+    float cur[WT][WR];
+    float pad[(128 - (WT * WR * 4) % 128) % 128 / 4];
+    float prv[TT][TR];
+    float vel[TT][TR];
+};
+static_assert(sizeof(Stage) % 128 == 0, "stage size");
+static_assert(offsetof(Stage, prv) % 128 == 0 && offsetof(Stage, vel) % 128 == 0, "box alignment");
+static_assert((WR * 4) % 16 == 0 && (TR * 4) % 16 == 0, "box rows are whole 16-byte units");
+}  // namespace sp3
+
+struct SphTmaParams {
+    StepAParams a;  // grid, sponge tables, mask, metric tables, reciprocals, dt^2
+    int L, ntr, ntt, nchunks, nshot;
+    unsigned long long *counter;
+    unsigned long long base;
+    int *err;
+    float *nxt;
+    long long spin;  // polls of a compute-side wait before it gives up (the drain keeps SPIN_LIMIT)
+};
+
+// sponge factor of index i (AWE_FAST: the float table)
+__device__ __forceinline__ float sph_damp(float v, int i, const float *__restrict__ ftab) {
+    return i == 0 ? v : v * ftab[i];
+}
+
+// sponge index over the kernel axes in their priority order (r, phi, theta)
+// = memory axes (1, 3, 2): the first low face in that order, else the first
+// high face (spongeKernel_3D; StepAParams::pri of the spherical grid)
+__device__ __forceinline__ int sph_sponge_index(int r, int ph, int th, int nr, int nph, int nth, int nb) {
+    if (r < nb) return nb - r;
+    if (ph < nb) return nb - ph;
+    if (th < nb) return nb - th;
+    if (r > nr - nb) return r - (nr - nb);
+    if (ph > nph - nb) return ph - (nph - nb);
+    if (th > nth - nb) return th - (nth - nb);
+    return 0;
+}
+
+__global__ void __launch_bounds__(sp3::NTHREADS, 2)
+    k_stepA_sph_tma(const __grid_constant__ CUtensorMap tm_cur, const __grid_constant__ CUtensorMap tm_prv,
+                    const __grid_constant__ CUtensorMap tm_vel, const SphTmaParams p) {
+    using namespace sp3;
+    extern __shared__ unsigned char smem_raw[];
+    Stage *st = reinterpret_cast<Stage *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    __shared__ __align__(8) uint64_t full[RING];
+    __shared__ int s_item;
+
+    const int tid = threadIdx.x;
+    const int rq = tid & 15, ti = tid >> 4;
+    if (tid == 0) {
+        for (int r = 0; r < RING; r++) mbar_init(&full[r], 1);
+        fence_mbar_init();
+        prefetch_tmap(&tm_cur);
+        prefetch_tmap(&tm_prv);
+        prefetch_tmap(&tm_vel);
+    }
+    // an earlier launch that gave up on a wait leaves the flag set: do nothing
+    if (__syncthreads_or(tid == 0 && *(volatile int *)p.err != 0)) return;
+
+    const int n1 = p.a.g.n1, n2 = p.a.g.n2, n3 = p.a.g.n3, nb = p.a.nb;
+    const int per_chunk = p.ntr * p.ntt;
+    const int nitems = per_chunk * p.nchunks * p.nshot;
+    const long long plane = (long long)n1 * n2;
+    const float2 r0v = make_float2(p.a.rd[0], p.a.rd[0]), r1v = make_float2(p.a.rd[1], p.a.rd[1]);
+    const float2 r2v = make_float2(p.a.rd[2], p.a.rd[2]), r3v = make_float2(p.a.rd[3], p.a.rd[3]);
+    const float2 r4v = make_float2(p.a.rd[4], p.a.rd[4]), dt2v = make_float2(p.a.dt2, p.a.dt2);
+    const float2 m1 = make_float2(-1.f, -1.f), m2 = make_float2(-2.f, -2.f);
+    const bool mask3 = p.a.mask == 3;
+
+    // ring position of the current item's first plane: slot and mbarrier parity
+    int slot0 = 0;
+    uint32_t ph0 = 0;
+    for (;;) {
+        if (tid == 0) s_item = (int)(atomicAdd(p.counter, 1ull) - p.base);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= nitems || item < 0) break;
+        const int tile = item % per_chunk, rest = item / per_chunk;
+        const int chunk = rest % p.nchunks, shot = rest / p.nchunks;
+        const int r0 = (tile % p.ntr) * TR, t0 = (tile / p.ntr) * TT;
+        const int y0 = chunk * p.L, y1 = min(y0 + p.L, n3);
+        const int S = (y1 - y0) + 2;  // current-level planes y0-1 .. y1
+        const int fo = shot * n3;     // the shot's first plane in the stacked fields
+
+        // stage s: current-level plane y0-1+s; from s = 2 on also the previous
+        // level and the velocity of plane y0+s-2, the plane updated at stage s
+        auto issue = [&](int s) {
+            const int slot = (slot0 + s) % RING;
+            const bool out = s >= 2;
+            mbar_expect_tx(&full[slot], BYTES_HALO + (out ? 2 * BYTES_TILE : 0));
+            tma_load_3d(&st[slot].cur[0][0], &tm_cur, &full[slot], r0 - HR, t0 - HT, fo + y0 - 1 + s);
+            if (out) {
+                const int y = y0 + s - 2;
+                tma_load_3d(&st[slot].prv[0][0], &tm_prv, &full[slot], r0, t0, fo + y);
+                tma_load_3d(&st[slot].vel[0][0], &tm_vel, &full[slot], r0, t0, y);
+            }
+        };
+        if (tid == 0)
+            for (int s = 0; s < RING && s < S; s++) issue(s);
+
+        // per-thread constants: 4 radii r .. r+3 of theta row t
+        const int r = r0 + 4 * rq, t = t0 + ti;
+        const bool col_ok = r < n1 && t < n2;  // n1 % 4 == 0: the 4 cells exist together
+        const bool th_in = t >= 4 && t < n2 - 4;
+        bool rin[4];
+        bool any_r = false;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            rin[j] = r + j >= 4 && r + j < n1 - 4;
+            any_r = any_r || rin[j];
+        }
+        float4 A2 = make_float4(0.f, 0.f, 0.f, 0.f), Cr = A2, B = A2, D = A2;
+        if (col_ok) {
+            const long long tt = (long long)t * n1 + r;
+            A2 = __ldg(reinterpret_cast<const float4 *>(p.a.tr0 + r));
+            Cr = __ldg(reinterpret_cast<const float4 *>(p.a.tr1 + r));
+            B = __ldg(reinterpret_cast<const float4 *>(p.a.tt0 + tt));
+            D = __ldg(reinterpret_cast<const float4 *>(p.a.tt1 + tt));
+        }
+        // every (r, theta) cell of the tile is outside the r and theta sponge bands
+        const bool tile_undamped = r0 >= nb && r0 + TR - 1 <= n1 - nb && t0 >= nb && t0 + TT - 1 <= n2 - nb;
+        float *dst = p.nxt + ((long long)(fo + y0) * n2 + t) * n1 + r;
+
+        int slot = slot0;  // ring slot and parity of stage s
+        uint32_t ph = ph0;
+        float q[3][4];  // phi queue: the centre values of stage s live in q[s % 3]
+#pragma unroll 1
+        for (int blk = 0; blk < S; blk += 3) {
+#pragma unroll
+            for (int u = 0; u < 3; u++) {
+                const int s = blk + u;
+                if (s < S) {
+                    const bool bad = !mbar_wait(&full[slot], ph, p.spin);
+                    if (bad) atomicExch(p.err, 1);
+                    const float4 cq = *reinterpret_cast<const float4 *>(&st[slot].cur[ti + HT][4 * rq + HR]);
+                    q[u][0] = cq.x;
+                    q[u][1] = cq.y;
+                    q[u][2] = cq.z;
+                    q[u][3] = cq.w;
+                    if (s >= 2) {
+                        const int y = y0 + s - 2;
+                        const int hs = slot == 0 ? RING - 1 : slot - 1;  // stage s-1: plane y and its halo
+                        const float(*H)[WR] = st[hs].cur;
+                        const float *um = q[(u + 1) % 3], *uc = q[(u + 2) % 3], *up = q[u];
+                        const float4 pv = *reinterpret_cast<const float4 *>(&st[slot].prv[ti][4 * rq]);
+                        const float4 vv = *reinterpret_cast<const float4 *>(&st[slot].vel[ti][4 * rq]);
+                        float2 lap01 = make_float2(0.f, 0.f), lap23 = lap01;
+                        const bool ph_in = y >= 4 && y < n3 - 4;
+                        if (th_in && ph_in && any_r) {
+                            const float rm = H[ti + HT][4 * rq + HR - 1], rp = H[ti + HT][4 * rq + HR + 4];
+                            const float4 tm = *reinterpret_cast<const float4 *>(&H[ti][4 * rq + HR]);
+                            const float4 tp = *reinterpret_cast<const float4 *>(&H[ti + 2 * HT][4 * rq + HR]);
+                            // pair (0, 1) and pair (2, 3): r - 1 and r + 1 of both cells
+                            const float2 c01 = make_float2(uc[0], uc[1]), c23 = make_float2(uc[2], uc[3]);
+                            const float2 mi01 = make_float2(rm, uc[0]), pl01 = make_float2(uc[1], uc[2]);
+                            const float2 mi23 = make_float2(uc[1], uc[2]), pl23 = make_float2(uc[3], rp);
+                            auto lap2 = [&](float2 c, float2 mi, float2 pl, float2 tmv, float2 tpv, float2 umv,
+                                            float2 upv, float2 a2, float2 cr, float2 b, float2 dd) {
+                                const float2 pra = __fmul2_rn(__ffma2_rn(mi, m1, pl), r0v);
+                                const float2 ppra = __fmul2_rn(__fadd2_rn(__ffma2_rn(c, m2, pl), mi), r1v);
+                                const float2 pth = __fmul2_rn(__ffma2_rn(tmv, m1, tpv), r2v);
+                                const float2 ppth = __fmul2_rn(__fadd2_rn(__ffma2_rn(c, m2, tpv), tmv), r3v);
+                                const float2 ppph = __fmul2_rn(__fadd2_rn(__ffma2_rn(c, m2, upv), umv), r4v);
+                                float2 l = __ffma2_rn(a2, pra, ppra);
+                                l = __ffma2_rn(b, pth, l);
+                                l = __ffma2_rn(cr, ppth, l);
+                                return __ffma2_rn(dd, ppph, l);
+                            };
+                            lap01 = lap2(c01, mi01, pl01, make_float2(tm.x, tm.y), make_float2(tp.x, tp.y),
+                                         make_float2(um[0], um[1]), make_float2(up[0], up[1]),
+                                         make_float2(A2.x, A2.y), make_float2(Cr.x, Cr.y), make_float2(B.x, B.y),
+                                         make_float2(D.x, D.y));
+                            lap23 = lap2(c23, mi23, pl23, make_float2(tm.z, tm.w), make_float2(tp.z, tp.w),
+                                         make_float2(um[2], um[3]), make_float2(up[2], up[3]),
+                                         make_float2(A2.z, A2.w), make_float2(Cr.z, Cr.w), make_float2(B.z, B.w),
+                                         make_float2(D.z, D.w));
+                            if (!rin[0]) lap01.x = 0.f;
+                            if (!rin[1]) lap01.y = 0.f;
+                            if (!rin[2]) lap23.x = 0.f;
+                            if (!rin[3]) lap23.y = 0.f;
+                        }
+                        const float2 a01 = __fmul2_rn(dt2v, __fmul2_rn(make_float2(vv.x, vv.y), make_float2(vv.x, vv.y)));
+                        const float2 a23 = __fmul2_rn(dt2v, __fmul2_rn(make_float2(vv.z, vv.w), make_float2(vv.z, vv.w)));
+                        const float2 f01 = __ffma2_rn(a01, lap01, __fadd2_rn(make_float2(uc[0], uc[1]),
+                                                                              make_float2(uc[0], uc[1])));
+                        const float2 f23 = __ffma2_rn(a23, lap23, __fadd2_rn(make_float2(uc[2], uc[3]),
+                                                                              make_float2(uc[2], uc[3])));
+                        float f[4] = {f01.x, f01.y, f23.x, f23.y};
+                        const float pr[4] = {pv.x, pv.y, pv.z, pv.w};
+                        const bool undamped = tile_undamped && y >= nb && y <= n3 - nb;
+#pragma unroll
+                        for (int j = 0; j < 4; j++) {
+                            const int si = undamped ? 0 : sph_sponge_index(r + j, y, t, n1, n3, n2, nb);
+                            float v = f[j] - sph_damp(pr[j], si, p.a.ftab);
+                            if (mask3 && (r + j > n1 - nb || (r + j < p.a.spill && (t >= 1 || y >= 1)))) v = 0.f;
+                            f[j] = sph_damp(v, si, p.a.ftab);
+                        }
+                        if (col_ok) *reinterpret_cast<float4 *>(dst) = make_float4(f[0], f[1], f[2], f[3]);
+                        dst += plane;
+                    }
+                    if (__syncthreads_or(bad)) {
+                        // drain: wait (bounded) for every copy still in flight, then leave
+                        if (tid == 0) {
+                            const int issued = min(S, max(RING, s - 1 + RING));
+                            for (int k = s; k < issued; k++) {
+                                const int x = slot0 + k;
+                                mbar_wait(&full[x % RING], ph0 ^ (uint32_t)((x / RING) & 1), SPIN_LIMIT);
+                            }
+                        }
+                        __syncthreads();
+                        return;
+                    }
+                    // stage s-1's slot is free (its centre values are in the queue)
+                    if (tid == 0 && s >= 1 && s - 1 + RING < S) issue(s - 1 + RING);
+                    if (++slot == RING) {
+                        slot = 0;
+                        ph ^= 1u;
+                    }
+                }
+            }
+        }
+        const int x = slot0 + S;
+        ph0 ^= (uint32_t)((x / RING) & 1);
+        slot0 = x % RING;
+    }
+}
+
+bool sphA_tma_eligible(const Grid &g) { return g.n1 % 4 == 0 && g.n1 >= 16 && g.n2 >= 16 && g.n3 >= 3; }
+
+// tensor maps: [0] u[0] halo box, [1] u[1] halo box, [2] u[0] tile, [3] u[1]
+// tile (the level fields of all shots stacked along phi), [4] vel tile
+bool sphA_tma_maps(CUtensorMap *maps, float *const u[2], const float *vel, const Grid &g, int nshot) {
+    using namespace sp3;
+    const int n3s = g.n3 * (nshot > 0 ? nshot : 1);
+    return make_tmap_3d(&maps[0], u[0], g.n1, g.n2, n3s, WR, WT) &&
+           make_tmap_3d(&maps[1], u[1], g.n1, g.n2, n3s, WR, WT) &&
+           make_tmap_3d(&maps[2], u[0], g.n1, g.n2, n3s, TR, TT) &&
+           make_tmap_3d(&maps[3], u[1], g.n1, g.n2, n3s, TR, TT) &&
+           make_tmap_3d(&maps[4], vel, g.n1, g.n2, g.n3, TR, TT);
+}
+
+Step3Launch sphA_tma_shape(const Grid &g, int nshot, int num_sms, int L) {
+    using namespace sp3;
+    Step3Launch s{};
+    s.L = L > 0 ? L : 64;
+    s.ntz = (g.n1 + TR - 1) / TR;
+    s.ntx = (g.n2 + TT - 1) / TT;
+    s.nchunks = (g.n3 + s.L - 1) / s.L;
+    s.items = s.ntz * s.ntx * s.nchunks * (nshot > 0 ? nshot : 1);
+    s.grid = std::min(s.items, 2 * num_sms);
+    s.smem = RING * sizeof(Stage) + 128;
+    return s;
+}
+
+cudaError_t launch_stepA_sph_tma(const CUtensorMap &cur, const CUtensorMap &prv, const CUtensorMap &vel, float *nxt,
+                                 const StepAParams &pa, const Step3Launch &sh, unsigned long long *counter,
+                                 unsigned long long base, int *err, long long spin, cudaStream_t s) {
+    SphTmaParams p{};
+    p.a = pa;
+    p.L = sh.L;
+    p.ntr = sh.ntz;
+    p.ntt = sh.ntx;
+    p.nchunks = sh.nchunks;
+    p.nshot = pa.nshot > 0 ? pa.nshot : 1;
+    p.counter = counter;
+    p.base = base;
+    p.err = err;
+    p.nxt = nxt;
+    p.spin = spin >= 0 ? spin : sp3::SPIN_LIMIT;
+    cudaFuncSetAttribute(k_stepA_sph_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem);
+    k_stepA_sph_tma<<<sh.grid, sp3::NTHREADS, sh.smem, s>>>(cur, prv, vel, p);
+    return cudaGetLastError();
+}
+
+}  // namespace awe

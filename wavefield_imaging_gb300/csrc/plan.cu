@@ -322,7 +322,7 @@ awe_status awe_plan_info(const awe_plan *p, awe_info *info) {
     info->nsnap = p->nsnap;
     info->snap_elems = p->snap_elems;
     info->device_bytes = p->device_bytes;
-    info->step_kernel = p->use_tma ? 1 : 0;
+    info->step_kernel = p->use_tma ? 1 : (p->sph_tma ? 2 : 0);
     return AWE_OK;
 }
 

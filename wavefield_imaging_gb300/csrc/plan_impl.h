@@ -78,6 +78,12 @@ struct awe_plan {
     unsigned long long *sched_counter = nullptr;
     unsigned long long sched_base = 0;
     int *d_err = nullptr;
+    // TMA-staged spherical step (GPU-program scheme, AWE_FAST): maps encoded
+    // per run (the level fields are reallocated when the shot count changes)
+    bool sph_tma = false;
+    int num_sms = 0;
+    CUtensorMap sph_maps[5];
+    awe::Step3Launch sph_shape{};
     // polls of a pipeline wait before it reports a timeout (AWE_PIPELINE_SPIN_LIMIT;
     // < 0: the kernel default); a limit of 0 makes every first wait time out,
     // which the failure tests use to exercise the error path

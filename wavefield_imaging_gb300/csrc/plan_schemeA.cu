@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -171,6 +172,22 @@ awe_status planA_init(awe_plan *p) {
 
     pa.nshot = 1;
     pa.shot_cells = g.cells();
+    // TMA-staged spherical step for AWE_FAST; AWE_STEP_KERNEL=simple keeps the
+    // register-march kernel (the tests compare both)
+    const char *kern = std::getenv("AWE_STEP_KERNEL");
+    const bool force_simple = kern && std::strcmp(kern, "simple") == 0;
+    if (geom == 3 && d.precision == AWE_FAST && !force_simple && sphA_tma_eligible(g) &&
+        sphA_tma_maps(p->sph_maps, p->u, p->vel, g, 1)) {
+        AWE_TRY(dev_alloc(p, (void **)&p->sched_counter, sizeof(unsigned long long)));
+        AWE_TRY(dev_alloc(p, (void **)&p->d_err, sizeof(int)));
+        CUDA_TRY(cudaMemset(p->sched_counter, 0, sizeof(unsigned long long)));
+        CUDA_TRY(cudaMemset(p->d_err, 0, sizeof(int)));
+        cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, p->device);
+        if (p->num_sms < 1) p->num_sms = 1;
+        const char *spin = std::getenv("AWE_PIPELINE_SPIN_LIMIT");
+        if (spin && *spin) p->spin_limit = std::atoll(spin);
+        p->sph_tma = true;
+    }
     // reciprocals of the Laplacian divisors (AWE_FAST multiplies; AWE_EXACT divides as the reference)
     const float dvs[5] = {pa.dd1, pa.dd2, pa.dd3, pa.dd4, pa.dd5};
     for (int j = 0; j < 5; j++) pa.rd[j] = dvs[j] != 0.f ? 1.f / dvs[j] : 0.f;
@@ -337,6 +354,16 @@ awe_status planA_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, flo
         AWE_TRY(dev_alloc(p, (void **)&p->d_snap_tmp, p->snap_elems * sizeof(float)));
     p->snap_pending = -1;  // a frame left queued by a failed run is not delivered
 
+    if (p->sph_tma) {  // maps of this run's level fields; the work counter restarts with every run
+        if (!sphA_tma_maps(p->sph_maps, p->u, p->vel, g, pa.nshot)) {
+            set_error("tensor-map encoding of the spherical step failed");
+            return AWE_ERR_CUDA;
+        }
+        const char *lenv = std::getenv("AWE_TMA_CHUNK");
+        p->sph_shape = sphA_tma_shape(g, pa.nshot, p->num_sms, lenv ? std::atoi(lenv) : 0);
+        CUDA_TRY(cudaMemsetAsync(p->sched_counter, 0, sizeof(unsigned long long), s));
+        p->sched_base = 0;
+    }
     const int jdata = d.jdata > 0 ? d.jdata : 1;
     long long launches = 0;
     float *cur = p->u[1], *nxt = p->u[0];
@@ -350,7 +377,19 @@ awe_status planA_run(awe_plan *p, const float *d_wav, int ncs, float *d_dat, flo
             launches++;
         }
         prof_begin(p, s);
-        launch_stepA(pa.geom, exact, cur, nxt, p->vel, pa, s);
+        if (p->sph_tma) {
+            const int ic = cur == p->u[0] ? 0 : 1;  // nxt is the other level
+            const cudaError_t e =
+                launch_stepA_sph_tma(p->sph_maps[ic], p->sph_maps[2 + (1 - ic)], p->sph_maps[4], nxt, pa,
+                                     p->sph_shape, p->sched_counter, p->sched_base, p->d_err, p->spin_limit, s);
+            p->sched_base += (unsigned long long)p->sph_shape.items + p->sph_shape.grid;
+            if (e != cudaSuccess) {
+                set_error("spherical TMA step launch failed: %s", cudaGetErrorString(e));
+                return AWE_ERR_CUDA;
+            }
+        } else {
+            launch_stepA(pa.geom, exact, cur, nxt, p->vel, pa, s);
+        }
         prof_end(p, s);
         launches++;
         if (pa.shell > 0) {

@@ -174,7 +174,7 @@ class Plan:
         self.nsmp = info.nsmp
         self.nsnap = info.nsnap
         self.snap_elems = info.snap_elems
-        self.step_kernel = "tma3d" if info.step_kernel == 1 else "simple"
+        self.step_kernel = {1: "tma3d", 2: "tma_sph"}.get(info.step_kernel, "simple")
         self._cb = None
         self.ns = self.nr = 0
 
