@@ -53,10 +53,11 @@ def test_oracle_checkpoint_emulation_fp32_is_exact():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("fsrf,nr", [(0, 45), (1, 45), (0, 46), (1, 46)])
+@pytest.mark.parametrize("fsrf,nr", [(0, 45), (1, 45), (0, 46), (1, 46), (0, 48), (1, 48)])
 def test_gradient_matches_fp64_oracle(fsrf, nr):
     """nr = 45: odd padded radius count (one radius per thread); 46: even
-    (two radii per thread, packed arithmetic)."""
+    (two radii per thread, packed arithmetic); 48: padded count a multiple of
+    4 (the TMA-staged forward, recompute and adjoint kernels)."""
     import wavefield_imaging_gb300 as awe
     from oracle import oracle
 
@@ -65,6 +66,7 @@ def test_gradient_matches_fp64_oracle(fsrf, nr):
     gref, Jref, dref = oracle.spher3d_gradient(par, vel, wav, sou, rec, dobs)
     T = int(np.ceil(np.sqrt(par["nt"])))
     with awe.Plan(spher_desc(par)) as p:
+        assert p.step_kernel == ("tma_sph" if (nr + 2 * par["nb"]) % 4 == 0 else "simple")
         p.set_model(vel)
         p.set_geometry(sou, rec)
         g32, J32, d32 = p.gradient(wav, dobs, ckpt_format=awe.CKPT_FP32, return_dsyn=True)
@@ -85,10 +87,11 @@ def test_gradient_matches_fp64_oracle(fsrf, nr):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("every", [1, 7, 1000])
-def test_checkpoint_interval_does_not_change_fp32_gradient(every):
+@pytest.mark.parametrize("nr", [45, 48])
+def test_checkpoint_interval_does_not_change_fp32_gradient(every, nr):
     import wavefield_imaging_gb300 as awe
 
-    par, vel, wav, sou, rec, vtrue = spher_grad_case(nt=60)
+    par, vel, wav, sou, rec, vtrue = spher_grad_case(nt=60, n=(nr, 20, 20))
     dobs = _dobs(par, vtrue, wav, sou, rec)
     with awe.Plan(spher_desc(par)) as p:
         p.set_model(vel)
@@ -115,14 +118,15 @@ def test_reflectivity_injection_is_refused():
 
 
 @pytest.mark.gpu
-def test_several_shots_sum_the_single_shot_gradients():
+@pytest.mark.parametrize("nr", [46, 48])
+def test_several_shots_sum_the_single_shot_gradients(nr):
     """awe_set_shots (the c4 track's layout): the gradient of three shots
     is the sum of the three single-shot gradients, the misfit the sum of
     theirs, the synthetic data each shot's own columns; awe_set_geometry
     afterwards goes back to one shot."""
     import wavefield_imaging_gb300 as awe
 
-    par, vel, wav, sou, rec, vtrue = spher_grad_case(n=(46, 20, 20), nt=80)
+    par, vel, wav, sou, rec, vtrue = spher_grad_case(n=(nr, 20, 20), nt=80)
     d = par["d"]
     shots = [(sou + np.array([[0.0, k * 3 * d[2], 0.0]], np.float32), rec[: 7 - k]) for k in range(3)]
     dobs = [_dobs(par, vtrue, wav, s_, r_) for s_, r_ in shots]
@@ -164,7 +168,7 @@ def test_empty_point_sets():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("nr", [45, 46])
+@pytest.mark.parametrize("nr", [45, 46, 48])
 def test_rtm_images_match_fp64_oracle(nr):
     """awe_rtm on the spherical scheme: zero-lag cross-correlation and Born
     images of recorded data against the FP64 adjoint oracle, and the
@@ -187,3 +191,40 @@ def test_rtm_images_match_fp64_oracle(nr):
     # true model differs by 5 % in one layer), so their FP32 rounding weighs
     # that much more here (the FP64 oracle gives 9e-6 on the same check)
     assert rel_l2(bs - bo, g) <= 5e-4
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fsrf", [0, 1])
+def test_tma_kernels_match_register_kernels(monkeypatch, fsrf):
+    """The TMA-staged forward, recompute and adjoint (k_stepA_sph_tma,
+    k_adjA_sph_tma) against the register-march kernels they replace
+    (AWE_STEP_KERNEL=simple): gradient, misfit, synthetic traces and both
+    images.  The kernels evaluate the same packed FP32x2 expressions, so the
+    bar is rel-L2 1e-6 (float rounding of the order of coincident receiver
+    atomics), with 5-plane phi chunks across the grid."""
+    import wavefield_imaging_gb300 as awe
+
+    par, vel, wav, sou, rec, vtrue = spher_grad_case(fsrf=fsrf, n=(48, 20, 20), nt=90)
+    dobs = _dobs(par, vtrue, wav, sou, rec)
+    out = {}
+    for kern in ("simple", "tma_sph"):
+        if kern == "simple":
+            monkeypatch.setenv("AWE_STEP_KERNEL", "simple")
+        else:
+            monkeypatch.delenv("AWE_STEP_KERNEL", raising=False)
+            monkeypatch.setenv("AWE_TMA_CHUNK", "5")
+        with awe.Plan(spher_desc(par)) as p:
+            assert p.step_kernel == kern
+            p.set_model(vel)
+            p.set_geometry(sou, rec)
+            g, J, d = p.gradient(wav, dobs, ckpt_every=7, ckpt_format=awe.CKPT_FP32, return_dsyn=True)
+            xc = p.rtm(wav, dobs, condition=awe.IMAGE_XCORR, ckpt_format=awe.CKPT_FP32)
+            bo = p.rtm(wav, dobs, condition=awe.IMAGE_BORN, ckpt_format=awe.CKPT_FP32)
+        out[kern] = (g, J, d, xc, bo)
+    (g0, J0, d0, x0, b0), (g1, J1, d1, x1, b1) = out["simple"], out["tma_sph"]
+    assert np.abs(g0).max() > 0 and np.abs(x0).max() > 0
+    assert rel_l2(d1, d0) <= 1e-6
+    assert abs(J1 - J0) <= 1e-5 * abs(J0)
+    assert rel_l2(g1, g0) <= 1e-6
+    assert rel_l2(x1, x0) <= 1e-6
+    assert rel_l2(b1, b0) <= 1e-6

@@ -342,8 +342,22 @@ bool sphA_tma_eligible(const Grid &g);
 // maps: [0] u[0] halo box, [1] u[1] halo box, [2] u[0] tile, [3] u[1] tile, [4] vel tile
 bool sphA_tma_maps(CUtensorMap *maps, float *const u[2], const float *vel, const Grid &g, int nshot);
 Step3Launch sphA_tma_shape(const Grid &g, int nshot, int num_sms, int L);
+// cur_f0, prv_f0: plane offsets of the two levels in their maps (levels
+// stacked along phi, as the gradient's recompute slots); nxt: the new level
 cudaError_t launch_stepA_sph_tma(const CUtensorMap &cur, const CUtensorMap &prv, const CUtensorMap &vel, float *nxt,
                                  const StepAParams &pa, const Step3Launch &sh, unsigned long long *counter,
-                                 unsigned long long base, int *err, long long spin, cudaStream_t s);
+                                 unsigned long long base, int *err, long long spin, cudaStream_t s, int cur_f0 = 0,
+                                 int prv_f0 = 0);
+// adjoint step of the spherical scheme (the k_adjA_sph2 update, TMA-staged):
+// x_halo / v_halo / a_halo = 72 x 18 box maps of z_{j+1}, the velocity and the
+// forward levels (A_j at plane offset a_f0); Y: z_{j+2} in, z_j out; G: the
+// gradient (or image) accumulators
+// halo-box (72 x 18) and, when tile is not null, tile-box (64 x 16) maps of
+// nlevels fields stacked along phi from base
+bool sphA_tma_level_maps(CUtensorMap *halo, CUtensorMap *tile, const float *base, const Grid &g, int nlevels);
+cudaError_t launch_adjA_sph_tma(const CUtensorMap &x_halo, const CUtensorMap &v_halo, const CUtensorMap &a_halo,
+                                int a_f0, float *Y, float2 *G, const StepAParams &pa, const Step3Launch &sh,
+                                unsigned long long *counter, unsigned long long base, int *err, long long spin,
+                                bool xcorr, cudaStream_t s);
 
 }  // namespace awe

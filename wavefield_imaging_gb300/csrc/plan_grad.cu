@@ -47,6 +47,10 @@ struct GradState {
     bool tma = false;
     float *vr = nullptr, *gbuf = nullptr;
     CUtensorMap vr_halo[3], vr_tile[3], g_halo, x_tile, y_tile;
+    // TMA path of the spherical scheme (AWE_FAST): halo and tile maps of the
+    // T + 1 recompute slots stacked along phi, halo maps of X, Y and v
+    bool sph = false;
+    CUtensorMap sl_halo, sl_tile, xy_halo[2], v_halo;
     // receiver / source corners by padded cell for the fused adjoint step
     int *rc_start = nullptr, *sc_start = nullptr;
     int2 *rc_ent = nullptr, *sc_ent = nullptr;
@@ -130,6 +134,16 @@ static awe_status grad_alloc(awe_plan *p, int T, int fmt) {
              make_tmap_3d(&st->x_tile, st->X, g.n1, g.n2, g.n3, t1, t2) &&
              make_tmap_3d(&st->y_tile, st->Y, g.n1, g.n2, g.n3, t1, t2);
         if (!ok) {
+            set_error("awe_gradient: tensor map encoding failed");
+            return AWE_ERR_CUDA;
+        }
+    }
+    if (p->sph_tma) {
+        st->sph = sphA_tma_level_maps(&st->sl_halo, &st->sl_tile, st->slots, p->g, T + 1) &&
+                  sphA_tma_level_maps(&st->xy_halo[0], nullptr, st->X, p->g, 1) &&
+                  sphA_tma_level_maps(&st->xy_halo[1], nullptr, st->Y, p->g, 1) &&
+                  sphA_tma_level_maps(&st->v_halo, nullptr, p->vel, p->g, 1);
+        if (!st->sph) {
             set_error("awe_gradient: tensor map encoding failed");
             return AWE_ERR_CUDA;
         }
@@ -222,6 +236,20 @@ static awe_status ckpt_load(awe_plan *p, int idx, float *u, cudaStream_t s) {
 //   dJ/dc += z_{j+1} L(A_j),  c = dt^2 v^2, folded to dJ/dm = dJ/dc (-c^2/dt^2).
 // image >= 0: awe_rtm's conditions (the data themselves back-propagated;
 // AWE_IMAGE_XCORR sums z A on the model window, AWE_IMAGE_BORN the gradient formula)
+// one TMA spherical step of the recompute: the current level at plane offset
+// cur_f0 of `halo`, the previous at prv_f0 of `tile`, the new level into nxt
+static awe_status sph_tma_step(awe_plan *p, const CUtensorMap &halo, const CUtensorMap &tile, float *nxt, int cur_f0,
+                               int prv_f0, cudaStream_t s) {
+    const cudaError_t e = launch_stepA_sph_tma(halo, tile, p->sph_maps[4], nxt, p->pa, p->sph_shape, p->sched_counter,
+                                               p->sched_base, p->d_err, p->spin_limit, s, cur_f0, prv_f0);
+    p->sched_base += (unsigned long long)p->sph_shape.items + p->sph_shape.grid;
+    if (e != cudaSuccess) {
+        set_error("spherical TMA step launch failed: %s", cudaGetErrorString(e));
+        return AWE_ERR_CUDA;
+    }
+    return AWE_OK;
+}
+
 static awe_status gradient_spher_one(awe_plan *p, const float *d_wav, int ncs, const float *d_dobs, int T, int fmt,
                                      double *d_grad, double *misfit, float *d_dsyn, cudaStream_t s, int image) {
     const awe_desc &d = p->d;
@@ -269,11 +297,29 @@ static awe_status gradient_spher_one(awe_plan *p, const float *d_wav, int ncs, c
         for (int k = k0; k < k1; k++) {
             float *cur = slot + (size_t)(k - k0 + 1) * cells;
             launch_injectA(false, 3, cur, p->src, nullptr, p->ns, d_wav, k, false, p->corner_off, s, 1, ncs);
-            if (k + 1 < k1) launch_stepA_oop(pa.geom, false, cur, cur - cells, cur + cells, p->vel, pa, s);
+            if (k + 1 < k1) {
+                if (st->sph) {  // slot i = k - k0 + 1 from slots i and i - 1, into slot i + 1
+                    const int i = k - k0 + 1;
+                    AWE_TRY(sph_tma_step(p, st->sl_halo, st->sl_tile, cur + cells, i * g.n3, (i - 1) * g.n3, s));
+                } else {
+                    launch_stepA_oop(pa.geom, false, cur, cur - cells, cur + cells, p->vel, pa, s);
+                }
+            }
             launches += (p->ns > 0) + (k + 1 < k1);
         }
         for (int j = k1 - 1; j >= k0; j--) {
-            launch_adjA_sph(X, Y, slot + (size_t)(j - k0 + 1) * cells, p->vel, st->G, pa, s, xcorr);
+            if (st->sph) {
+                const cudaError_t e = launch_adjA_sph_tma(
+                    X == st->X ? st->xy_halo[0] : st->xy_halo[1], st->v_halo, st->sl_halo, (j - k0 + 1) * g.n3, Y,
+                    st->G, pa, p->sph_shape, p->sched_counter, p->sched_base, p->d_err, p->spin_limit, xcorr, s);
+                p->sched_base += (unsigned long long)p->sph_shape.items + p->sph_shape.grid;
+                if (e != cudaSuccess) {
+                    set_error("spherical TMA adjoint launch failed: %s", cudaGetErrorString(e));
+                    return AWE_ERR_CUDA;
+                }
+            } else {
+                launch_adjA_sph(X, Y, slot + (size_t)(j - k0 + 1) * cells, p->vel, st->G, pa, s, xcorr);
+            }
             launches++;
             if (j >= 1) {
                 launch_rec_adjA(Y, p->rec, p->nr, st->r + (size_t)(j - 1) * p->nr, pa, p->corner_off, s);
