@@ -47,6 +47,9 @@ sys.path.insert(0, ROOT)
 METRIC = "cell-updates/s & %HBM peak (3D acoustic)"
 UNIT = "cell-updates/s"
 BYTES_PER_CELL = 16  # read u_cur, read u_prev, read v^2dt^2, write u_next
+# spherical adjoint step: read z_{j+1}, v, A_j, z_{j+2} and the gradient pair
+# (8 B); write z_j and the pair
+ADJ_BYTES_PER_CELL = 36
 
 
 def workload(nt=3000, n=512):
@@ -975,6 +978,7 @@ def run_sphergrad(args):
     torch.cuda.synchronize()
     sampler = ClockSampler(0)
     sampler.start()
+    plan.profile(True)  # events around every step and adjoint kernel launch
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     launches = 0
@@ -984,7 +988,23 @@ def run_sphergrad(args):
     ev1.record(stream)
     torch.cuda.synchronize()
     clocks = sampler.stop()
+    kinds = plan.profile_read_kinds()
+    plan.profile(False)
     ms = ev0.elapsed_time(ev1) / args.steps
+    peak, peak_kind = measured_peak()
+    cells_pad = int(np.prod([n + 2 * w["nb"] for n in w["n"]]))
+    kernels = {}
+    for kind, nbytes, name in (("step", BYTES_PER_CELL, "k_stepA_sph_tma" if plan.step_kernel == "tma_sph"
+                                else "k_stepA_sph_march2"),
+                               ("adjoint", ADJ_BYTES_PER_CELL, "k_adjA_sph_tma" if plan.step_kernel == "tma_sph"
+                                else "k_adjA_sph2")):
+        kms, kn = kinds[kind]
+        if kn:
+            avg = kms / 1e3 / kn
+            kernels[kind] = {"kernel": name, "launches": kn, "ms": kms, "avg_launch_us": avg * 1e6,
+                             "bytes_per_cell": nbytes, "achieved": nbytes * cells_pad / avg / 1e9, "unit": "GB/s",
+                             "frac": nbytes * cells_pad / avg / 1e9 / peak, "peak": peak, "peak_source": peak_kind,
+                             "share_of_gradient": kms / args.steps / ms}
     d_dat = torch.zeros((plan.nsmp, rec.shape[0]), dtype=torch.float32, device="cuda")
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     f0.record(stream)
@@ -1004,6 +1024,7 @@ def run_sphergrad(args):
                       "device_bytes": plan.device_bytes()},
            "split": {"forward_ms": fwd_ms, "gradient_ms": ms, "gradient_over_forward": ms / fwd_ms,
                      "cell_steps_per_s": nshots * cells * nt / (ms / 1e3)},
+           "kernels": kernels,
            "misfit": J, "grad_finite": bool(np.isfinite(g).all()), "grad_max_abs": float(np.abs(g).max()),
            "gpu_launches": int(launches), "clocks": clocks}
     print(json.dumps(out))

@@ -187,12 +187,19 @@ awe_status awe_synchronize(awe_plan *plan);
 /* Number of kernel launches issued by the last awe_forward / awe_forward_device. */
 long long awe_last_launch_count(const awe_plan *plan);
 
-/* Kernel timing: when enabled, the next forward run brackets every launch of
- * the stencil (step) kernel with CUDA events on its stream; awe_profile_read
- * returns their summed duration (ms) and the launch count after the run has
- * completed.  Off by default. */
+/* Kernel timing: when enabled, the next runs bracket every launch of the
+ * stencil (step) kernel - forward steps, and the gradient's recompute steps -
+ * and of the adjoint step kernel of a gradient with CUDA events on their
+ * stream; awe_profile_read returns the step kernels' summed duration (ms) and
+ * launch count after the runs have completed, awe_profile_read_kinds both
+ * kinds (arrays of AWE_PROF_KINDS, indexed by AWE_PROF_STEP and
+ * AWE_PROF_ADJOINT).  Reading resets the record.  Off by default. */
+#define AWE_PROF_STEP 0
+#define AWE_PROF_ADJOINT 1
+#define AWE_PROF_KINDS 2
 awe_status awe_profile_enable(awe_plan *plan, int on);
 awe_status awe_profile_read(awe_plan *plan, double *step_kernel_ms, long long *step_launches);
+awe_status awe_profile_read_kinds(awe_plan *plan, double *kernel_ms, long long *launches);
 
 /* ---- Misfit gradient (no counterpart in the reference: its adj=y mode
  * back-injects data for an image, MAWEFDcart2Dgpu.cu:386-396) ---- */

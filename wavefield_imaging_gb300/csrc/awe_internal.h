@@ -338,7 +338,7 @@ void stepB3_tma_boxes(int *halo1, int *halo2, int *tile1, int *tile2);
 
 // TMA-staged spherical step (GPU-program scheme, AWE_FAST); Step3Launch's
 // ntz/ntx count the r and theta tiles, items include the shots
-bool sphA_tma_eligible(const Grid &g);
+bool sphA_tma_eligible(const Grid &g, int nb);
 // maps: [0] u[0] halo box, [1] u[1] halo box, [2] u[0] tile, [3] u[1] tile, [4] vel tile
 bool sphA_tma_maps(CUtensorMap *maps, float *const u[2], const float *vel, const Grid &g, int nshot);
 Step3Launch sphA_tma_shape(const Grid &g, int nshot, int num_sms, int L);
@@ -350,14 +350,16 @@ cudaError_t launch_stepA_sph_tma(const CUtensorMap &cur, const CUtensorMap &prv,
                                  int prv_f0 = 0);
 // adjoint step of the spherical scheme (the k_adjA_sph2 update, TMA-staged):
 // x_halo / v_halo / a_halo = 72 x 18 box maps of z_{j+1}, the velocity and the
-// forward levels (A_j at plane offset a_f0); Y: z_{j+2} in, z_j out; G: the
-// gradient (or image) accumulators
+// forward levels (A_j at plane offset a_f0); y_tile / g_tile = tile maps of
+// Y (z_{j+2} in, z_j out) and of G (the gradient or image accumulators,
+// sphA_tma_pair_map)
 // halo-box (72 x 18) and, when tile is not null, tile-box (64 x 16) maps of
 // nlevels fields stacked along phi from base
 bool sphA_tma_level_maps(CUtensorMap *halo, CUtensorMap *tile, const float *base, const Grid &g, int nlevels);
+bool sphA_tma_pair_map(CUtensorMap *m, const float2 *base, const Grid &g);
 cudaError_t launch_adjA_sph_tma(const CUtensorMap &x_halo, const CUtensorMap &v_halo, const CUtensorMap &a_halo,
-                                int a_f0, float *Y, float2 *G, const StepAParams &pa, const Step3Launch &sh,
-                                unsigned long long *counter, unsigned long long base, int *err, long long spin,
-                                bool xcorr, cudaStream_t s);
+                                int a_f0, const CUtensorMap &y_tile, const CUtensorMap &g_tile, float *Y, float2 *G,
+                                const StepAParams &pa, const Step3Launch &sh, unsigned long long *counter,
+                                unsigned long long base, int *err, long long spin, bool xcorr, cudaStream_t s);
 
 }  // namespace awe

@@ -41,6 +41,7 @@ constexpr int WR = TR + 2 * HR, WT = TT + 2 * HT;  // 72 x 18 halo box
 constexpr int RING = 6, NTHREADS = 256;
 constexpr uint32_t BYTES_HALO = WR * WT * 4, BYTES_TILE = TR * TT * 4;
 constexpr long long SPIN_LIMIT = 1ll << 22;
+constexpr int FTAB_MAX = 256;  // sponge factors held in shared memory (nb < FTAB_MAX)
 
 // every box destination starts on a 128-byte boundary
 struct __align__(128) Stage {
@@ -65,10 +66,8 @@ struct SphTmaParams {
     long long spin;  // polls of a compute-side wait before it gives up (the drain keeps SPIN_LIMIT)
 };
 
-// sponge factor of index i (AWE_FAST: the float table)
-__device__ __forceinline__ float sph_damp(float v, int i, const float *__restrict__ ftab) {
-    return i == 0 ? v : v * ftab[i];
-}
+// sponge factor of index i (AWE_FAST: the float table, copied to shared memory)
+__device__ __forceinline__ float sph_damp(float v, int i, const float *ftab) { return i == 0 ? v : v * ftab[i]; }
 
 // sponge index over the kernel axes in their priority order (r, phi, theta)
 // = memory axes (1, 3, 2): the first low face in that order, else the first
@@ -91,9 +90,11 @@ __global__ void __launch_bounds__(sp3::NTHREADS, 2)
     Stage *st = reinterpret_cast<Stage *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     __shared__ __align__(8) uint64_t full[RING];
     __shared__ int s_item;
+    __shared__ float s_ftab[FTAB_MAX];
 
     const int tid = threadIdx.x;
     const int rq = tid & 15, ti = tid >> 4;
+    for (int i = tid; i <= p.a.nb && i < FTAB_MAX; i += NTHREADS) s_ftab[i] = p.a.ftab[i];
     if (tid == 0) {
         for (int r = 0; r < RING; r++) mbar_init(&full[r], 1);
         fence_mbar_init();
@@ -238,9 +239,9 @@ __global__ void __launch_bounds__(sp3::NTHREADS, 2)
 #pragma unroll
                         for (int j = 0; j < 4; j++) {
                             const int si = undamped ? 0 : sph_sponge_index(r + j, y, t, n1, n3, n2, nb);
-                            float v = f[j] - sph_damp(pr[j], si, p.a.ftab);
+                            float v = f[j] - sph_damp(pr[j], si, s_ftab);
                             if (mask3 && (r + j > n1 - nb || (r + j < p.a.spill && (t >= 1 || y >= 1)))) v = 0.f;
-                            f[j] = sph_damp(v, si, p.a.ftab);
+                            f[j] = sph_damp(v, si, s_ftab);
                         }
                         if (col_ok) *reinterpret_cast<float4 *>(dst) = make_float4(f[0], f[1], f[2], f[3]);
                         dst += plane;
@@ -272,7 +273,9 @@ __global__ void __launch_bounds__(sp3::NTHREADS, 2)
     }
 }
 
-bool sphA_tma_eligible(const Grid &g) { return g.n1 % 4 == 0 && g.n1 >= 16 && g.n2 >= 16 && g.n3 >= 3; }
+bool sphA_tma_eligible(const Grid &g, int nb) {
+    return g.n1 % 4 == 0 && g.n1 >= 16 && g.n2 >= 16 && g.n3 >= 3 && nb < sp3::FTAB_MAX;
+}
 
 // tensor maps: [0] u[0] halo box, [1] u[1] halo box, [2] u[0] tile, [3] u[1]
 // tile (the level fields of all shots stacked along phi), [4] vel tile
@@ -328,10 +331,10 @@ cudaError_t launch_stepA_sph_tma(const CUtensorMap &cur, const CUtensorMap &prv,
 //   G += z_{j+1} L(A_j)  (or z_{j+1} A_j for the cross-correlation image),
 // on interior cells (at least 4 from every face).  L^T gathers this cell's
 // weight in each neighbour's stencil times the neighbour's I c z.  Per plane
-// the ring holds the 72 x 18 boxes of z_{j+1}, v and A_j; the phi neighbours
-// of I c z and of A come from 3-plane register queues.  z_{j+2} and G are
-// read and written in place with plain 16-byte accesses issued before the
-// ring wait, so their latency overlaps it.
+// the ring holds the 72 x 18 boxes of z_{j+1}, v and A_j, and for the plane
+// being updated the 64 x 16 boxes of z_{j+2} and of G (float pairs, a
+// 128 x 16 float box); the phi neighbours of I c z and of A come from 3-plane
+// register queues.  z_j and G are written back with plain 16-byte stores.
 
 namespace sa3 {
 using sp3::HR;
@@ -340,8 +343,8 @@ using sp3::TR;
 using sp3::TT;
 using sp3::WR;
 using sp3::WT;
-constexpr int RING = 6, NTHREADS = 256;
-constexpr uint32_t BYTES = 3 * WR * WT * 4;
+constexpr int RING = 4, NTHREADS = 256;
+constexpr uint32_t BYTES_HALOS = 3 * WR * WT * 4, BYTES_OUT = TR * TT * 4 + 2 * TR * TT * 4;
 constexpr int PAD = (128 - (WT * WR * 4) % 128) % 128 / 4;
 
 struct __align__(128) Stage {
@@ -351,9 +354,13 @@ struct __align__(128) Stage {
     float pv[PAD];
     float a[WT][WR];
     float pa[PAD];
+    float y[TT][TR];
+    float g[TT][2 * TR];
 };
 static_assert(sizeof(Stage) % 128 == 0, "stage size");
-static_assert(offsetof(Stage, v) % 128 == 0 && offsetof(Stage, a) % 128 == 0, "box alignment");
+static_assert(offsetof(Stage, v) % 128 == 0 && offsetof(Stage, a) % 128 == 0 && offsetof(Stage, y) % 128 == 0 &&
+                  offsetof(Stage, g) % 128 == 0,
+              "box alignment");
 }  // namespace sa3
 
 struct SphAdjParams {
@@ -371,21 +378,26 @@ struct SphAdjParams {
 
 __global__ void __launch_bounds__(sa3::NTHREADS, 2)
     k_adjA_sph_tma(const __grid_constant__ CUtensorMap tm_x, const __grid_constant__ CUtensorMap tm_v,
-                   const __grid_constant__ CUtensorMap tm_a, const SphAdjParams p) {
+                   const __grid_constant__ CUtensorMap tm_a, const __grid_constant__ CUtensorMap tm_y,
+                   const __grid_constant__ CUtensorMap tm_g, const SphAdjParams p) {
     using namespace sa3;
     extern __shared__ unsigned char smem_raw[];
     Stage *st = reinterpret_cast<Stage *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     __shared__ __align__(8) uint64_t full[RING];
     __shared__ int s_item;
+    __shared__ float s_ftab[sp3::FTAB_MAX];
 
     const int tid = threadIdx.x;
     const int rq = tid & 15, ti = tid >> 4;
+    for (int i = tid; i <= p.a.nb && i < sp3::FTAB_MAX; i += NTHREADS) s_ftab[i] = p.a.ftab[i];
     if (tid == 0) {
         for (int r = 0; r < RING; r++) mbar_init(&full[r], 1);
         fence_mbar_init();
         prefetch_tmap(&tm_x);
         prefetch_tmap(&tm_v);
         prefetch_tmap(&tm_a);
+        prefetch_tmap(&tm_y);
+        prefetch_tmap(&tm_g);
     }
     if (__syncthreads_or(tid == 0 && *(volatile int *)p.err != 0)) return;
 
@@ -431,14 +443,20 @@ __global__ void __launch_bounds__(sa3::NTHREADS, 2)
         const int y0 = chunk * p.L, y1 = min(y0 + p.L, n3);
         const int S = (y1 - y0) + 2;
 
-        // stage s: plane y0-1+s of z_{j+1}, v and A_j; plane y0+s-2 is updated at stage s
+        // stage s: plane y0-1+s of z_{j+1}, v and A_j; from s = 2 on also
+        // z_{j+2} and G of plane y0+s-2, the plane updated at stage s
         auto issue = [&](int s) {
             const int slot = (slot0 + s) % RING;
             const int f = y0 - 1 + s;
-            mbar_expect_tx(&full[slot], BYTES);
+            const bool out = s >= 2;
+            mbar_expect_tx(&full[slot], BYTES_HALOS + (out ? BYTES_OUT : 0));
             tma_load_3d(&st[slot].x[0][0], &tm_x, &full[slot], r0 - HR, t0 - HT, f);
             tma_load_3d(&st[slot].v[0][0], &tm_v, &full[slot], r0 - HR, t0 - HT, f);
             tma_load_3d(&st[slot].a[0][0], &tm_a, &full[slot], r0 - HR, t0 - HT, p.a_f0 + f);
+            if (out) {
+                tma_load_3d(&st[slot].y[0][0], &tm_y, &full[slot], r0, t0, f - 1);
+                tma_load_3d(&st[slot].g[0][0], &tm_g, &full[slot], 2 * r0, t0, f - 1);
+            }
         };
         if (tid == 0)
             for (int s = 0; s < RING && s < S; s++) issue(s);
@@ -504,18 +522,11 @@ __global__ void __launch_bounds__(sa3::NTHREADS, 2)
             for (int u = 0; u < 3; u++) {
                 const int s = blk + u;
                 if (s < S) {
-                    // plane y's z_{j+2} and accumulators go out before the wait
                     const int y = y0 + s - 2;
                     const bool upd = s >= 2;
                     const bool phy = upd && pin(y);
                     const bool gok = col_ok && phy && any_c;
-                    float4 yv = make_float4(0.f, 0.f, 0.f, 0.f), g0 = yv, g1 = yv;
                     const long long idx = (long long)y * plane + col;
-                    if (upd && col_ok) yv = __ldcs(reinterpret_cast<const float4 *>(p.Y + idx));
-                    if (gok) {
-                        g0 = __ldcs(reinterpret_cast<const float4 *>(p.G + idx));
-                        g1 = __ldcs(reinterpret_cast<const float4 *>(p.G + idx + 2));
-                    }
                     const bool bad = !mbar_wait(&full[slot], ph, p.spin);
                     if (bad) atomicExch(p.err, 1);
                     {
@@ -576,17 +587,20 @@ __global__ void __launch_bounds__(sa3::NTHREADS, 2)
                         const float2 mu01 = __ffma2_rn(two, make_float2(xc[0], xc[1]), lt01);
                         const float2 mu23 = __ffma2_rn(two, make_float2(xc[2], xc[3]), lt23);
                         float out[4] = {mu01.x, mu01.y, mu23.x, mu23.y};
+                        const float4 yv = *reinterpret_cast<const float4 *>(&st[slot].y[ti][4 * rq]);
                         const float yy[4] = {yv.x, yv.y, yv.z, yv.w};
                         const bool undamped = tile_undamped && y >= nb && y <= n3 - nb;
 #pragma unroll
                         for (int j = 0; j < 4; j++) {
                             const int si = undamped ? 0 : sph_sponge_index(r + j, y, t, n1, n3, n2, nb);
-                            float m = fmaf(-sph_damp(1.f, si, p.a.ftab), yy[j], out[j]);
+                            float m = fmaf(-sph_damp(1.f, si, s_ftab), yy[j], out[j]);
                             if (mask3 && (r + j > n1 - nb || (r + j < p.a.spill && (t >= 1 || y >= 1)))) m = 0.f;
-                            out[j] = sph_damp(m, si, p.a.ftab);
+                            out[j] = sph_damp(m, si, s_ftab);
                         }
                         if (col_ok) __stcs(reinterpret_cast<float4 *>(p.Y + idx), make_float4(out[0], out[1], out[2], out[3]));
                         if (gok) {
+                            const float4 g0 = *reinterpret_cast<const float4 *>(&st[slot].g[ti][8 * rq]);
+                            const float4 g1 = *reinterpret_cast<const float4 *>(&st[slot].g[ti][8 * rq + 4]);
                             float2 ga[4] = {make_float2(g0.x, g0.y), make_float2(g0.z, g0.w), make_float2(g1.x, g1.y),
                                             make_float2(g1.z, g1.w)};
                             float term[4];
@@ -648,14 +662,19 @@ __global__ void __launch_bounds__(sa3::NTHREADS, 2)
 
 bool sphA_tma_level_maps(CUtensorMap *halo, CUtensorMap *tile, const float *base, const Grid &g, int nlevels) {
     const int n3s = g.n3 * (nlevels > 0 ? nlevels : 1);
-    return make_tmap_3d(halo, base, g.n1, g.n2, n3s, sp3::WR, sp3::WT) &&
+    return (!halo || make_tmap_3d(halo, base, g.n1, g.n2, n3s, sp3::WR, sp3::WT)) &&
            (!tile || make_tmap_3d(tile, base, g.n1, g.n2, n3s, sp3::TR, sp3::TT));
 }
 
+// the accumulator pairs as a float field of 2 n1 floats per line, 128 x 16 boxes
+bool sphA_tma_pair_map(CUtensorMap *m, const float2 *base, const Grid &g) {
+    return make_tmap_3d(m, reinterpret_cast<const float *>(base), 2 * g.n1, g.n2, g.n3, 2 * sp3::TR, sp3::TT);
+}
+
 cudaError_t launch_adjA_sph_tma(const CUtensorMap &x_halo, const CUtensorMap &v_halo, const CUtensorMap &a_halo,
-                                int a_f0, float *Y, float2 *G, const StepAParams &pa, const Step3Launch &sh,
-                                unsigned long long *counter, unsigned long long base, int *err, long long spin,
-                                bool xcorr, cudaStream_t s) {
+                                int a_f0, const CUtensorMap &y_tile, const CUtensorMap &g_tile, float *Y, float2 *G,
+                                const StepAParams &pa, const Step3Launch &sh, unsigned long long *counter,
+                                unsigned long long base, int *err, long long spin, bool xcorr, cudaStream_t s) {
     SphAdjParams p{};
     p.a = pa;
     p.L = sh.L;
@@ -672,7 +691,7 @@ cudaError_t launch_adjA_sph_tma(const CUtensorMap &x_halo, const CUtensorMap &v_
     p.spin = spin >= 0 ? spin : sp3::SPIN_LIMIT;
     const int smem = (int)(sa3::RING * sizeof(sa3::Stage) + 128);
     cudaFuncSetAttribute(k_adjA_sph_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    k_adjA_sph_tma<<<sh.grid, sa3::NTHREADS, smem, s>>>(x_halo, v_halo, a_halo, p);
+    k_adjA_sph_tma<<<sh.grid, sa3::NTHREADS, smem, s>>>(x_halo, v_halo, a_halo, y_tile, g_tile, p);
     return cudaGetLastError();
 }
 

@@ -142,9 +142,11 @@ awe_status deliver_snapshot(awe_plan *p, const float *d_frame, int isnap, int it
 
 awe_status flush_snapshots(awe_plan *p) { return p->snap_cb ? snap_deliver_pending(p) : AWE_OK; }
 
-void prof_begin(awe_plan *p, cudaStream_t s) {
+void prof_begin(awe_plan *p, cudaStream_t s, int kind) {
     if (!p->profile) return;
     const size_t need = 2 * (size_t)(p->prof_n + 1);
+    if (p->prof_kind.size() < (size_t)p->prof_n + 1) p->prof_kind.resize((size_t)p->prof_n + 1);
+    p->prof_kind[(size_t)p->prof_n] = kind;
     while (p->prof_ev.size() < need) {
         cudaEvent_t e;
         if (cudaEventCreate(&e) != cudaSuccess) {
@@ -495,19 +497,33 @@ awe_status awe_profile_enable(awe_plan *p, int on) {
     return AWE_OK;
 }
 
-awe_status awe_profile_read(awe_plan *p, double *ms, long long *n) {
+awe_status awe_profile_read_kinds(awe_plan *p, double *ms, long long *n) {
     if (!p || !ms || !n) return AWE_ERR_INVALID;
     CUDA_TRY(cudaSetDevice(p->device));
-    double total = 0.0;
+    for (int k = 0; k < AWE_PROF_KINDS; k++) {
+        ms[k] = 0.0;
+        n[k] = 0;
+    }
     for (long long i = 0; i < p->prof_n; i++) {
         float t = 0.f;
         CUDA_TRY(cudaEventSynchronize(p->prof_ev[2 * i + 1]));
         CUDA_TRY(cudaEventElapsedTime(&t, p->prof_ev[2 * i], p->prof_ev[2 * i + 1]));
-        total += t;
+        const int k = p->prof_kind[(size_t)i];
+        ms[k] += t;
+        n[k]++;
     }
-    *ms = total;
-    *n = p->prof_n;
     p->prof_n = 0;
+    return AWE_OK;
+}
+
+awe_status awe_profile_read(awe_plan *p, double *ms, long long *n) {
+    if (!p || !ms || !n) return AWE_ERR_INVALID;
+    double mk[AWE_PROF_KINDS];
+    long long nk[AWE_PROF_KINDS];
+    const awe_status st = awe_profile_read_kinds(p, mk, nk);
+    if (st != AWE_OK) return st;
+    *ms = mk[AWE_PROF_STEP];
+    *n = nk[AWE_PROF_STEP];
     return AWE_OK;
 }
 

@@ -50,7 +50,7 @@ struct GradState {
     // TMA path of the spherical scheme (AWE_FAST): halo and tile maps of the
     // T + 1 recompute slots stacked along phi, halo maps of X, Y and v
     bool sph = false;
-    CUtensorMap sl_halo, sl_tile, xy_halo[2], v_halo;
+    CUtensorMap sl_halo, sl_tile, xy_halo[2], xy_tile[2], v_halo, g_tile;
     // receiver / source corners by padded cell for the fused adjoint step
     int *rc_start = nullptr, *sc_start = nullptr;
     int2 *rc_ent = nullptr, *sc_ent = nullptr;
@@ -140,9 +140,10 @@ static awe_status grad_alloc(awe_plan *p, int T, int fmt) {
     }
     if (p->sph_tma) {
         st->sph = sphA_tma_level_maps(&st->sl_halo, &st->sl_tile, st->slots, p->g, T + 1) &&
-                  sphA_tma_level_maps(&st->xy_halo[0], nullptr, st->X, p->g, 1) &&
-                  sphA_tma_level_maps(&st->xy_halo[1], nullptr, st->Y, p->g, 1) &&
-                  sphA_tma_level_maps(&st->v_halo, nullptr, p->vel, p->g, 1);
+                  sphA_tma_level_maps(&st->xy_halo[0], &st->xy_tile[0], st->X, p->g, 1) &&
+                  sphA_tma_level_maps(&st->xy_halo[1], &st->xy_tile[1], st->Y, p->g, 1) &&
+                  sphA_tma_level_maps(&st->v_halo, nullptr, p->vel, p->g, 1) &&
+                  sphA_tma_pair_map(&st->g_tile, st->G, p->g);
         if (!st->sph) {
             set_error("awe_gradient: tensor map encoding failed");
             return AWE_ERR_CUDA;
@@ -240,8 +241,10 @@ static awe_status ckpt_load(awe_plan *p, int idx, float *u, cudaStream_t s) {
 // cur_f0 of `halo`, the previous at prv_f0 of `tile`, the new level into nxt
 static awe_status sph_tma_step(awe_plan *p, const CUtensorMap &halo, const CUtensorMap &tile, float *nxt, int cur_f0,
                                int prv_f0, cudaStream_t s) {
+    prof_begin(p, s);
     const cudaError_t e = launch_stepA_sph_tma(halo, tile, p->sph_maps[4], nxt, p->pa, p->sph_shape, p->sched_counter,
                                                p->sched_base, p->d_err, p->spin_limit, s, cur_f0, prv_f0);
+    prof_end(p, s);
     p->sched_base += (unsigned long long)p->sph_shape.items + p->sph_shape.grid;
     if (e != cudaSuccess) {
         set_error("spherical TMA step launch failed: %s", cudaGetErrorString(e));
@@ -302,23 +305,30 @@ static awe_status gradient_spher_one(awe_plan *p, const float *d_wav, int ncs, c
                     const int i = k - k0 + 1;
                     AWE_TRY(sph_tma_step(p, st->sl_halo, st->sl_tile, cur + cells, i * g.n3, (i - 1) * g.n3, s));
                 } else {
+                    prof_begin(p, s);
                     launch_stepA_oop(pa.geom, false, cur, cur - cells, cur + cells, p->vel, pa, s);
+                    prof_end(p, s);
                 }
             }
             launches += (p->ns > 0) + (k + 1 < k1);
         }
         for (int j = k1 - 1; j >= k0; j--) {
             if (st->sph) {
+                const int ix = X == st->X ? 0 : 1;  // Y is the other buffer
+                prof_begin(p, s, AWE_PROF_ADJOINT);
                 const cudaError_t e = launch_adjA_sph_tma(
-                    X == st->X ? st->xy_halo[0] : st->xy_halo[1], st->v_halo, st->sl_halo, (j - k0 + 1) * g.n3, Y,
+                    st->xy_halo[ix], st->v_halo, st->sl_halo, (j - k0 + 1) * g.n3, st->xy_tile[1 - ix], st->g_tile, Y,
                     st->G, pa, p->sph_shape, p->sched_counter, p->sched_base, p->d_err, p->spin_limit, xcorr, s);
+                prof_end(p, s);
                 p->sched_base += (unsigned long long)p->sph_shape.items + p->sph_shape.grid;
                 if (e != cudaSuccess) {
                     set_error("spherical TMA adjoint launch failed: %s", cudaGetErrorString(e));
                     return AWE_ERR_CUDA;
                 }
             } else {
+                prof_begin(p, s, AWE_PROF_ADJOINT);
                 launch_adjA_sph(X, Y, slot + (size_t)(j - k0 + 1) * cells, p->vel, st->G, pa, s, xcorr);
+                prof_end(p, s);
             }
             launches++;
             if (j >= 1) {
@@ -602,9 +612,11 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
             }
             if (st->tma) {
                 launch_adj_g(X, p->vel, st->gbuf, g, p->nop, s);
+                prof_begin(p, s, AWE_PROF_ADJOINT);
                 cudaError_t e = launch_stepB3_adj(st->g_halo, *ymap, *xmap, Y, slot0 + (size_t)(k - k0) * cells,
                                                   st->G, sp, p->tma_shape, p->sched_counter, p->sched_base, p->d_err,
                                                   s);
+                prof_end(p, s);
                 p->sched_base += (unsigned long long)p->tma_shape.items + p->tma_shape.grid;
                 if (e != cudaSuccess) {
                     set_error("TMA adjoint launch failed: %s", cudaGetErrorString(e));
@@ -618,7 +630,9 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
                     ap.wav = (p->ns > 0 && !xcorr) ? d_wav : nullptr;
                     ap.it = k;
                 }
+                prof_begin(p, s, AWE_PROF_ADJOINT);
                 launch_adjB(X, Y, Vk, p->vel, st->G, ap, s);
+                prof_end(p, s);
                 launches++;
             }
             if (d.ndim == 3 && d.dabc) {

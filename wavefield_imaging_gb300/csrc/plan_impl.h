@@ -108,6 +108,7 @@ struct awe_plan {
     // optional per-launch timing of the step kernel
     bool profile = false;
     std::vector<cudaEvent_t> prof_ev;  // pairs (start, stop)
+    std::vector<int> prof_kind;         // AWE_PROF_* of each pair
     long long prof_n = 0;
 };
 
@@ -135,7 +136,7 @@ inline PointsAt points_at(const awe_plan *p, const GeoPoint *tab, int n, int row
 }
 
 // bracket one step-kernel launch with events when profiling is on
-void prof_begin(awe_plan *p, cudaStream_t s);
+void prof_begin(awe_plan *p, cudaStream_t s, int kind = AWE_PROF_STEP);
 void prof_end(awe_plan *p, cudaStream_t s);
 
 awe_status planB_init(awe_plan *p);

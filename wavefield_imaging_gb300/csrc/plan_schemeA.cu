@@ -176,7 +176,7 @@ awe_status planA_init(awe_plan *p) {
     // register-march kernel (the tests compare both)
     const char *kern = std::getenv("AWE_STEP_KERNEL");
     const bool force_simple = kern && std::strcmp(kern, "simple") == 0;
-    if (geom == 3 && d.precision == AWE_FAST && !force_simple && sphA_tma_eligible(g) &&
+    if (geom == 3 && d.precision == AWE_FAST && !force_simple && sphA_tma_eligible(g, nb) &&
         sphA_tma_maps(p->sph_maps, p->u, p->vel, g, 1)) {
         AWE_TRY(dev_alloc(p, (void **)&p->sched_counter, sizeof(unsigned long long)));
         AWE_TRY(dev_alloc(p, (void **)&p->d_err, sizeof(int)));

@@ -96,6 +96,7 @@ def lib():
         L.awe_last_launch_count.restype = C.c_longlong
         L.awe_profile_enable.argtypes = [vp, C.c_int]
         L.awe_profile_read.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
+        L.awe_profile_read_kinds.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
         L.awe_batch_create.argtypes = [C.POINTER(Desc), C.c_int, C.POINTER(Shot), C.c_int, C.POINTER(vp)]
         L.awe_batch_destroy.argtypes = [vp]
         L.awe_batch_set_model.argtypes = [vp, fp]
@@ -130,7 +131,8 @@ def lib():
         L.awe_gradient_device.argtypes = [vp, vp, C.c_int, vp, C.POINTER(GradOpts), vp, dp, vp, vp]
         for name in ("awe_plan_create", "awe_plan_destroy", "awe_plan_info", "awe_set_model", "awe_set_geometry",
                      "awe_forward", "awe_forward_device", "awe_set_snapshot_callback", "awe_synchronize",
-                     "awe_profile_enable", "awe_profile_read", "awe_gradient", "awe_gradient_device"):
+                     "awe_profile_enable", "awe_profile_read", "awe_profile_read_kinds", "awe_gradient",
+                     "awe_gradient_device"):
             getattr(L, name).restype = C.c_int
         _lib = L
     return _lib
@@ -294,6 +296,14 @@ class Plan:
 
     def profile(self, on: bool = True):
         _check(lib().awe_profile_enable(self._h, int(on)))
+
+    def profile_read_kinds(self):
+        """{"step": (ms, launches), "adjoint": (ms, launches)} of the runs since
+        profiling was enabled or last read: step kernels (forward and the
+        gradient's recompute) and the gradient's adjoint step kernels."""
+        ms, n = (C.c_double * 2)(), (C.c_longlong * 2)()
+        _check(lib().awe_profile_read_kinds(self._h, ms, n))
+        return {"step": (ms[0], n[0]), "adjoint": (ms[1], n[1])}
 
     def profile_read(self):
         """(summed step-kernel milliseconds, step-kernel launches) of the last run."""
