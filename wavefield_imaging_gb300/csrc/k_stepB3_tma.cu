@@ -2,9 +2,10 @@
 //
 // A CTA owns a 64 (z) x 16 (x) tile and marches along y over a chunk of
 // planes.  For every plane it TMA-loads (cp.async.bulk.tensor, mbarrier
-// completion) the current level's 72 x 24 halo tile and the previous level
-// and v^2 dt^2 64 x 16 tiles into a 7-deep shared-memory ring, three planes
-// ahead of the compute.  y-neighbours come from a 9-plane register queue
+// completion) the current level's 72 x 24 halo tile into a 9-deep ring (the
+// halo of plane y is read when plane y+4 arrives, so five slots are in use)
+// and, for the plane being updated, the previous level and v^2 dt^2 64 x 16
+// tiles into a 5-deep ring, five planes ahead of the compute.  y-neighbours come from a 9-plane register queue
 // (each thread owns a 4-cell z strip of one x column), z- and x-neighbours
 // from the halo tile in shared memory; the leapfrog update, the sponge of
 // the previous level (applied on read) and of the new level (outside the ABC
@@ -28,18 +29,23 @@
 namespace awe {
 
 namespace s3 {
-constexpr int TZ = 64, TX = 16, HALO = 4, RING = 7, NOPQ = 4;
+constexpr int TZ = 64, TX = 16, HALO = 4, RING = 9, TRING = 5, NOPQ = 4;
 constexpr int HZ = TZ + 2 * HALO, HX = TX + 2 * HALO;
 constexpr int NTHREADS = 256;
 constexpr uint32_t BYTES_HALO = HZ * HX * 4, BYTES_TILE = TZ * TX * 4;
 constexpr long long SPIN_LIMIT = 1ll << 22;
 
-struct __align__(128) Stage {
+struct __align__(128) Stage {  // halo ring entry
     float cur[HX][HZ];
+};
+struct __align__(128) Tile {  // tile ring entry
     float prv[TX][TZ];
     float vel[TX][TZ];
 };
-static_assert(sizeof(Stage) % 128 == 0, "stage size");
+static_assert(sizeof(Stage) % 128 == 0 && sizeof(Tile) % 128 == 0, "stage size");
+// the tile of output plane o is refilled (for o + TRING) only after plane o
+// is computed: the refill is issued after stage o + 2 NOPQ + TRING - RING + NOPQ
+static_assert(TRING >= RING - NOPQ, "tile ring depth");
 }  // namespace s3
 
 struct Step3Params {
@@ -76,6 +82,7 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
     using namespace s3;
     extern __shared__ unsigned char smem_raw[];
     Stage *st = reinterpret_cast<Stage *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    Tile *tl = reinterpret_cast<Tile *>(st + RING);
     __shared__ __align__(8) uint64_t full[RING];
     __shared__ int s_item;
 
@@ -93,8 +100,9 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
 
     const int nitems = p.ntz * p.ntx * p.nchunks;
     const long long plane = (long long)p.n1 * p.n2;
-    // ring position of the current item's first plane: slot and mbarrier parity
-    int slot0 = 0;
+    // ring position of the current item's first plane: slot and mbarrier
+    // parity; tile ring slot of its first output plane
+    int slot0 = 0, tile0 = 0;
     uint32_t ph0 = 0;
     for (;;) {
         if (tid == 0) s_item = (int)(atomicAdd(p.counter, 1ull) - p.base);
@@ -113,8 +121,9 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
             tma_load_3d(&st[slot].cur[0][0], &tm_cur, &full[slot], z0 - HALO, x0 - HALO, y0 - NOPQ + s);
             if (out) {
                 const int pl = y0 + s - 2 * NOPQ;
-                tma_load_3d(&st[slot].prv[0][0], &tm_prv, &full[slot], z0, x0, pl);
-                tma_load_3d(&st[slot].vel[0][0], &tm_vel, &full[slot], z0, x0, pl);
+                Tile &t = tl[(tile0 + s - 2 * NOPQ) % TRING];
+                tma_load_3d(&t.prv[0][0], &tm_prv, &full[slot], z0, x0, pl);
+                tma_load_3d(&t.vel[0][0], &tm_vel, &full[slot], z0, x0, pl);
             }
         };
         if (tid == 0)
@@ -244,8 +253,9 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
                             lap[2] = l23.x;
                             lap[3] = l23.y;
                         }
-                        const float4 pv = *reinterpret_cast<const float4 *>(&st[slot].prv[xi][4 * zq]);
-                        const float4 vv = *reinterpret_cast<const float4 *>(&st[slot].vel[xi][4 * zq]);
+                        const Tile &tp = tl[(tile0 + s - 2 * NOPQ) % TRING];
+                        const float4 pv = *reinterpret_cast<const float4 *>(&tp.prv[xi][4 * zq]);
+                        const float4 vv = *reinterpret_cast<const float4 *>(&tp.vel[xi][4 * zq]);
                         const float prv4[4] = {pv.x, pv.y, pv.z, pv.w}, vel4[4] = {vv.x, vv.y, vv.z, vv.w};
                         const bool yin = y >= NOPQ && y < p.n3 - NOPQ;
                         // every sponge factor of this plane of the tile is 1: the
@@ -352,6 +362,7 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
         const int t = slot0 + S;
         ph0 ^= (uint32_t)((t / RING) & 1);
         slot0 = t % RING;
+        tile0 = (tile0 + (S - 2 * NOPQ)) % TRING;
     }
 }
 // cuTensorMapEncodeTiled, fetched from the driver at run time (no link-time libcuda dependency)
@@ -413,7 +424,7 @@ Step3Launch stepB3_tma_shape(const Grid &g, int num_sms, int L) {
     s.nchunks = (g.n3 + s.L - 1) / s.L;
     s.items = s.ntz * s.ntx * s.nchunks;
     s.grid = std::min(s.items, 2 * num_sms);
-    s.smem = RING * sizeof(Stage) + 128;
+    s.smem = RING * sizeof(Stage) + TRING * sizeof(Tile) + 128;
     return s;
 }
 
