@@ -83,11 +83,13 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
     extern __shared__ unsigned char smem_raw[];
     Stage *st = reinterpret_cast<Stage *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     Tile *tl = reinterpret_cast<Tile *>(st + RING);
+    float *s_w3 = reinterpret_cast<float *>(tl + TRING);  // y sponge factors (1 without a sponge)
     __shared__ __align__(8) uint64_t full[RING];
     __shared__ int s_item;
 
     const int tid = threadIdx.x;
     const int zq = tid & 15, xi = tid >> 4;
+    for (int i = tid; i < p.n3; i += NTHREADS) s_w3[i] = p.w3 ? p.w3[i] : 1.f;
     if (tid == 0) {
         for (int r = 0; r < RING; r++) mbar_init(&full[r], 1);
         fence_mbar_init();
@@ -264,7 +266,7 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
                         float out[4];
                         if constexpr (MODE == 2) {
                             // lambda = 2 I nu + L(I vel2 nu) + W (1 - 2 I) nu_{k+1}; out = W lambda
-                            const float wy = (!undamped && p.w3) ? __ldg(p.w3 + y) : 1.f;
+                            const float wy = undamped ? 1.f : s_w3[y];
                             const float lv4[4] = {lvp.x, lvp.y, lvp.z, lvp.w};
                             float2 ga[4] = {make_float2(gp0.x, gp0.y), make_float2(gp0.z, gp0.w),
                                             make_float2(gp1.x, gp1.y), make_float2(gp1.z, gp1.w)};
@@ -308,7 +310,7 @@ __global__ void __launch_bounds__(s3::NTHREADS, 2)
                                 out[i] = o;
                             }
                         } else {
-                            const float wy = p.w3 ? __ldg(p.w3 + y) : 1.f;
+                            const float wy = s_w3[y];
                             const bool yshell = y < p.shell || y >= p.n3 - p.shell;
 #pragma unroll
                             for (int i = 0; i < 4; i++) {
@@ -402,7 +404,8 @@ void stepB3_tma_boxes(int *halo1, int *halo2, int *tile1, int *tile2) {
 }
 
 bool stepB3_tma_eligible(int ndim, int nop, bool rho, const Grid &g) {
-    return ndim == 3 && nop == 4 && !rho && g.n1 % 4 == 0 && g.n1 >= 16 && g.n2 >= 16 && g.n3 >= 9;
+    // n3 <= 16384: the y sponge factors fit beside the rings in shared memory
+    return ndim == 3 && nop == 4 && !rho && g.n1 % 4 == 0 && g.n1 >= 16 && g.n2 >= 16 && g.n3 >= 9 && g.n3 <= 16384;
 }
 
 // tensor maps: [0] u[0] halo box, [1] u[1] halo box, [2] u[0] tile, [3] u[1] tile, [4] vel tile
@@ -424,7 +427,7 @@ Step3Launch stepB3_tma_shape(const Grid &g, int num_sms, int L) {
     s.nchunks = (g.n3 + s.L - 1) / s.L;
     s.items = s.ntz * s.ntx * s.nchunks;
     s.grid = std::min(s.items, 2 * num_sms);
-    s.smem = RING * sizeof(Stage) + TRING * sizeof(Tile) + 128;
+    s.smem = RING * sizeof(Stage) + TRING * sizeof(Tile) + (size_t)g.n3 * sizeof(float) + 128;
     return s;
 }
 
