@@ -180,11 +180,11 @@ def measured_peak():
 
 
 # DRAM bytes per cell of one step-kernel launch (k_stepB3_o8, AWE_FAST),
-# from the ncu capture of a 384^3-padded launch: 897.0 MB read + written
+# from the ncu capture of a 384^3-padded launch: 895.2 MB read + written
 # over 56.62 M padded cells (profiles/k_stepB3_o8_tma_n320.md).  A full
 # 576^3 launch is too large for a capture; DRAM traffic scales with the cells
 # a launch processes.
-STEP_DRAM_BYTES_PER_CELL = 15.842
+STEP_DRAM_BYTES_PER_CELL = 15.810
 
 
 def profiled_traffic(cells):
