@@ -648,6 +648,7 @@ def run_grad(args):
     sampler = ClockSampler(local)
     sampler.start()
     barrier(dist)
+    plan.profile(True)  # events around every step and adjoint kernel launch
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     launches = 0
@@ -658,6 +659,8 @@ def run_grad(args):
     torch.cuda.synchronize()
     barrier(dist)
     clocks = sampler.stop()
+    kinds = plan.profile_read_kinds()
+    plan.profile(False)
     ms = allmax(dist, ev0.elapsed_time(ev1))
     # the forward alone, for the split
     d_dat = torch.zeros((plan.nsmp, rec.shape[0]), dtype=torch.float32, device="cuda")
@@ -672,6 +675,20 @@ def run_grad(args):
         return
     cells = padded_cells(w)
     g_s = ms / 1e3 / args.steps
+    peak, peak_kind = measured_peak()
+    kernels = {}
+    # 3D: forward steps 16 B per cell, recompute steps (which also store
+    # L(V_k)) 20 B; the adjoint step 36 B (halo of I vel2 nu, nu_{k+1}, nu_k,
+    # L(V_k), the 8-byte gradient pair read and written, mu written)
+    for kind, nbytes in (("step", None), ("adjoint", 36 if nd == 3 else None)):
+        kms, kn = kinds[kind]
+        if kn:
+            avg = kms / 1e3 / kn
+            k = {"launches": kn, "ms": kms, "avg_launch_us": avg * 1e6, "share_of_gradient": kms / args.steps / ms}
+            if nbytes:
+                k.update(bytes_per_cell=nbytes, achieved=nbytes * cells / avg / 1e9, unit="GB/s",
+                         frac=nbytes * cells / avg / 1e9 / peak, peak=peak, peak_source=peak_kind)
+            kernels[kind] = k
     out = {"metric": GRAD_METRIC, "value": args.steps * world / (ms / 1e3), "unit": "gradients/s",
            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32 fields, compensated fp32 sums",
@@ -683,6 +700,7 @@ def run_grad(args):
                      "gradient_over_forward": (ms / args.steps) / fwd_ms,
                      "cell_steps_per_s": cells * w["nt"] / g_s,
                      "algorithmic_GBps": 48.0 * cells * w["nt"] / g_s / 1e9},
+           "kernels": kernels,
            "misfit": J, "gpu_launches": int(launches), "clocks": clocks}
     print(json.dumps(out))
     plan.close()
