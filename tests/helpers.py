@@ -30,16 +30,29 @@ def desc_from_par(par, precision=0, scheme=1, coords=0):
 
 
 def run_engine(par, vel, wav, sou, rec, den=None, precision=0, scheme=1, coords=0, rfl=None):
+    """One engine run of a fixture's case.  A fixture with a snapshot window
+    (par["win"], written by the cpu programs) is run with padded frames, cut
+    to the window as the programs cut them (oracle.snapshot_window)."""
     from wavefield_imaging_gb300 import Plan
 
-    with Plan(desc_from_par(par, precision, scheme, coords)) as p:
+    jsnap = par.get("jsnap", 0)
+    windowed = bool(par.get("win")) and jsnap > 0 and not (len(par["n"]) == 2 and par.get("bnds"))
+    with Plan(desc_from_par(dict(par, bnds=1) if windowed else par, precision, scheme, coords)) as p:
         p.set_model(vel, den=den, rfl=rfl)
         p.set_geometry(sou, rec)
-        if par.get("jsnap", 0) > 0:
+        if jsnap > 0:
             dat, snaps = p.forward(wav, snapshots=True)
         else:
             dat, snaps = p.forward(wav), None
-        return dat, snaps, p.last_launch_count()
+        launches = p.last_launch_count()
+    if windowed:
+        from oracle import oracle
+
+        nbd, n1p, n2p, n3p = oracle.padded(par)
+        win = oracle.snapshot_window(par, nbd, (n1p, n2p, n3p))
+        frames = np.asarray(snaps).reshape(-1, n1p * n2p * n3p)
+        snaps = np.stack([oracle.cut_window(f, win, (n1p, n2p, n3p)) for f in frames])
+    return dat, snaps, launches
 
 
 def rel_l2(a, b):
