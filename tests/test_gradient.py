@@ -175,3 +175,33 @@ def test_empty_point_sets(nd):
         dobs = np.ones((40, rec.shape[0]), np.float32)
         g, J = p.gradient(wav, dobs, ckpt_format=awe.CKPT_FP32)
         assert J == pytest.approx(0.5 * dobs.size) and not g.any()
+
+
+@pytest.mark.parametrize("fsrf,n", [(0, None), (1, None), (0, [120, 40, 30]), (1, [120, 40, 30])])
+def test_single_boundary_launch_matches_separate_launches(monkeypatch, fsrf, n):
+    """3D gradient on the TMA path: the one boundary launch per adjoint step
+    (kappa fold, transposed ABC of the six faces, g = I vel2 nu: k_bnd3_adj)
+    against the separate launches it replaces (AWE_BND3=0), for the gradient
+    and both images; the larger grid has several axis-1 and axis-2 ranges of
+    face blocks.  The fold moves from after the adjoint step to the next
+    step's launch, so only its order against the receiver term may differ."""
+    import wavefield_imaging_gb300 as awe
+
+    # the larger grid needs the steps for the wave to reach its receivers
+    par, vel, wav, sou, rec, vtrue = grad_case(3, fsrf=fsrf, nt=70 if n is None else 260, n=n)
+    dobs = _observed(par, vtrue, wav, sou, rec)
+    out = {}
+    for env in ("0", "1"):
+        monkeypatch.setenv("AWE_BND3", env)
+        with _plan(par, vel, sou, rec) as p:
+            assert p.step_kernel == "tma3d"
+            g, J = p.gradient(wav, dobs, ckpt_every=9, ckpt_format=awe.CKPT_FP32)
+            xc = p.rtm(wav, dobs, condition=awe.IMAGE_XCORR, ckpt_format=awe.CKPT_FP32)
+            bo = p.rtm(wav, dobs, condition=awe.IMAGE_BORN, ckpt_format=awe.CKPT_FP32)
+        out[env] = (g, J, xc, bo)
+    (g0, J0, x0, b0), (g1, J1, x1, b1) = out["0"], out["1"]
+    assert np.abs(g0).max() > 0 and np.abs(x0).max() > 0
+    assert J1 == J0
+    assert rel_l2(g1, g0) <= 1e-6
+    assert rel_l2(x1, x0) <= 1e-6
+    assert rel_l2(b1, b0) <= 1e-6

@@ -112,6 +112,21 @@ struct Bnd3Params {
 bool bnd3_eligible(int nop, const Grid &g);
 void launch_bnd3(bool exact, Bnd3Params p, cudaStream_t s);
 
+// The boundary work before one adjoint step of the 3D gradient in one launch
+// (k_boundary3.cu): mu += W kappa on the shell (kappa = 0), the transposed
+// one-way ABC of the six faces (mu and kappa updated), and g = I vel2 mu on
+// every cell.  nop = 4, bnd3_eligible.
+struct Bnd3AdjParams {
+    Grid g;
+    float *mu, *kap, *gout;
+    const float *vel2;
+    const float *zl, *zh, *xl, *xh, *yl, *yh;
+    const float *w1, *w2, *w3;  // sponge factors of the fold (null: weight 1)
+    int top;                    // axis-1 low face (0 with a free surface)
+    int n_int, nxr, nzr;        // set by launch_bnd3_adj
+};
+void launch_bnd3_adj(Bnd3AdjParams p, cudaStream_t s);
+
 // injection into the new level scaled by vel (v^2 dt^2): u += (dd*w)*vel.
 // off[c] = flat offset of corner c from the point's base index.
 // stride: distance between consecutive points in pts (moving geometries)

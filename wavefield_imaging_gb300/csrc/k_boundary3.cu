@@ -267,4 +267,273 @@ void launch_bnd3(bool exact, Bnd3Params p, cudaStream_t s) {
     else k_bnd3<false><<<grid, NT, 0, s>>>(p);
 }
 
+// ---------------------------------------------------------------------------
+// The boundary work before one adjoint step of the 3D gradient in one launch:
+//  1. fold the previous adjoint step's kappa into mu on the shell (mu += W
+//     kappa, kappa = 0; cells within nop + 2 of a face),
+//  2. the transpose of the one-way ABC (abcone3d_apply, fdutil.c:2085-2177),
+//     passes in reverse order (axis 3, axis 2, axis 1) and updates within a
+//     line in reverse order: t = mu[i]; mu[i] = 0; mu[b] -= c t;
+//     kappa[b] += t; kappa[i] += c t (b the inward neighbour of i),
+//  3. g = I vel2 mu on every cell (I: at least nop from every face), the
+//     field the adjoint step's stencil reads.
+// Block roles as in k_bnd3, so each cell's chain runs in one block: a plane y
+// in [6, n3-6) folds its axis-2 bands, runs the axis-2 lines, then folds and
+// transposes its axis-1 line ends together, then forms g for the plane; a
+// face block (6 axis-3 face planes x 16 columns x 64 cells of axis 1) folds
+// all its cells, runs the axis-3, axis-2 and axis-1 lines it holds, then
+// forms g.  The result does not depend on block order.
+namespace b3a {
+__device__ __forceinline__ void tcell(float &mi, float &mb, float &kb, float &ki, float c) {
+    const float v = mi;
+    mi = 0.f;
+    mb -= c * v;
+    kb += v;
+    ki += c * v;
+}
+
+__device__ __forceinline__ float wcell3(const Bnd3AdjParams &p, int z, int x, int y) {
+    if (!p.w1) return 1.f;
+    return __ldg(p.w1 + z) * __ldg(p.w2 + x) * __ldg(p.w3 + y);
+}
+
+// mu += W kappa, kappa = 0 (cells whose kappa is 0 keep their value)
+__device__ __forceinline__ void fold(const Bnd3AdjParams &p, long long i, int z, int x, int y) {
+    const float kv = p.kap[i];
+    if (kv != 0.f) {
+        p.mu[i] += wcell3(p, z, x, y) * kv;
+        p.kap[i] = 0.f;
+    }
+}
+
+// transpose of one line's ABC updates: cells base + j*st, j = 0..n-1;
+// high face i = n-2 .. n-5 (b = i-1), low face i = 1 .. 4 (b = i+1)
+__device__ __forceinline__ void tline(const Bnd3AdjParams &p, long long base, long long st, int n, float cl, float ch,
+                                      bool low) {
+    for (int i = n - 2; i >= n - 5; i--) {
+        const long long ci = base + i * st, cb = ci - st;
+        float mi = p.mu[ci], mb = p.mu[cb], kb = p.kap[cb], ki = p.kap[ci];
+        tcell(mi, mb, kb, ki, ch);
+        p.mu[ci] = mi;
+        p.mu[cb] = mb;
+        p.kap[cb] = kb;
+        p.kap[ci] = ki;
+    }
+    if (low)
+        for (int i = 1; i <= 4; i++) {
+            const long long ci = base + i * st, cb = ci + st;
+            float mi = p.mu[ci], mb = p.mu[cb], kb = p.kap[cb], ki = p.kap[ci];
+            tcell(mi, mb, kb, ki, cl);
+            p.mu[ci] = mi;
+            p.mu[cb] = mb;
+            p.kap[cb] = kb;
+            p.kap[ci] = ki;
+        }
+}
+
+// axis-1 ends of line `line` (n1 % 4 == 0): optionally fold cells 0..5 and
+// n1-6..n1-1 first, then the transposed updates, in registers
+__device__ __forceinline__ void zends(const Bnd3AdjParams &p, long long line, int x, int y, bool dofold) {
+    const int n1 = p.g.n1, q = n1 / 4;
+    float4 *M = reinterpret_cast<float4 *>(p.mu + line * n1);
+    float4 *K = reinterpret_cast<float4 *>(p.kap + line * n1);
+    auto fold4 = [&](float4 &m, float4 &k, int z0, unsigned mask) {
+        float *mv = &m.x, *kv = &k.x;
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            if (((mask >> j) & 1u) && kv[j] != 0.f) {
+                mv[j] += wcell3(p, z0 + j, x, y) * kv[j];
+                kv[j] = 0.f;
+            }
+    };
+    {  // high end: cells n1-8 .. n1-1
+        float4 ma = M[q - 2], mb = M[q - 1], ka = K[q - 2], kb = K[q - 1];
+        if (dofold) {
+            fold4(ma, ka, n1 - 8, 12u);
+            fold4(mb, kb, n1 - 4, 15u);
+        }
+        const float h = __ldg(p.zh + line);
+        tcell(mb.z, mb.y, kb.y, kb.z, h);
+        tcell(mb.y, mb.x, kb.x, kb.y, h);
+        tcell(mb.x, ma.w, ka.w, kb.x, h);
+        tcell(ma.w, ma.z, ka.z, ka.w, h);
+        M[q - 2] = ma;
+        M[q - 1] = mb;
+        K[q - 2] = ka;
+        K[q - 1] = kb;
+    }
+    {  // low end: cells 0 .. 7
+        float4 ma = M[0], mb = M[1], ka = K[0], kb = K[1];
+        if (dofold) {
+            fold4(ma, ka, 0, 15u);
+            fold4(mb, kb, 4, 3u);
+        }
+        if (p.top) {
+            const float l = __ldg(p.zl + line);
+            tcell(ma.y, ma.z, ka.z, ka.y, l);
+            tcell(ma.z, ma.w, ka.w, ka.z, l);
+            tcell(ma.w, mb.x, kb.x, ka.w, l);
+            tcell(mb.x, mb.y, kb.y, kb.x, l);
+        }
+        M[0] = ma;
+        M[1] = mb;
+        K[0] = ka;
+        K[1] = kb;
+    }
+}
+
+// g = I vel2 mu on cells [c0, c0 + 4 nq) of plane y, z-fastest (c0 % 4 == 0)
+__device__ __forceinline__ void gcells(const Bnd3AdjParams &p, int y, int z, int x) {
+    const int n1 = p.g.n1, n2 = p.g.n2, n3 = p.g.n3;
+    const long long c = ((long long)y * n2 + x) * n1 + z;
+    const float4 m = *reinterpret_cast<const float4 *>(p.mu + c);
+    const float4 v = __ldg(reinterpret_cast<const float4 *>(p.vel2 + c));
+    const bool rest = x >= 4 && x < n2 - 4 && y >= 4 && y < n3 - 4;
+    float4 o;
+    o.x = (rest && z >= 4 && z < n1 - 4) ? v.x * m.x : 0.f;
+    o.y = (rest && z + 1 >= 4 && z + 1 < n1 - 4) ? v.y * m.y : 0.f;
+    o.z = (rest && z + 2 >= 4 && z + 2 < n1 - 4) ? v.z * m.z : 0.f;
+    o.w = (rest && z + 3 >= 4 && z + 3 < n1 - 4) ? v.w * m.w : 0.f;
+    __stcs(reinterpret_cast<float4 *>(p.gout + c), o);
+}
+}  // namespace b3a
+
+__global__ void __launch_bounds__(b3::NT) k_bnd3_adj(const Bnd3AdjParams p) {
+    using namespace b3;
+    using namespace b3a;
+    const int tid = threadIdx.x;
+    const int n1 = p.g.n1, n2 = p.g.n2, n3 = p.g.n3;
+    const long long s2 = n1, s3 = (long long)n1 * n2;
+    int blk = blockIdx.x;
+
+    if (blk < p.n_int) {  // ---- one plane without axis-3 face cells
+        const int y = SHELL + blk;
+        // fold the axis-2 bands (x < 6, x >= n2-6), every z
+        for (int l = tid; l < 2 * SHELL * n1; l += NT) {
+            const int k = l / n1, z = l % n1, x = k < SHELL ? k : n2 - 2 * SHELL + k;
+            fold(p, (long long)y * s3 + (long long)x * s2 + z, z, x, y);
+        }
+        __syncthreads();
+        // axis-2 lines (y, z)
+        for (int z = tid; z < n1; z += NT) {
+            const long long line = (long long)y * n1 + z;
+            tline(p, (long long)y * s3 + z, s2, n2, __ldg(p.xl + line), __ldg(p.xh + line), true);
+        }
+        __syncthreads();
+        // axis-1 ends, folded here for the lines outside the axis-2 bands
+        for (int x = tid; x < n2; x += NT) zends(p, (long long)y * n2 + x, x, y, x >= SHELL && x < n2 - SHELL);
+        __syncthreads();
+        const int nq = n1 / 4;
+        for (int l = tid; l < n2 * nq; l += NT) gcells(p, y, 4 * (l % nq), l / nq);
+        return;
+    }
+    blk -= p.n_int;
+    if (blk < 2 * p.nxr * p.nzr) {  // ---- face block
+        const int f = blk / (p.nxr * p.nzr), r = blk % (p.nxr * p.nzr), xr = r / p.nzr, zr = r % p.nzr;
+        const int xa = xr * XR, xb = xr == p.nxr - 1 ? n2 : xa + XR;
+        const int za = zr * ZR, zb = zr == p.nzr - 1 ? n1 : za + ZR;
+        const int ya = f == 0 ? 0 : n3 - SHELL;
+        const int ncol = xb - xa, nz = zb - za;
+        for (int l = tid; l < SHELL * ncol * nz; l += NT) {  // fold every cell (all in the axis-3 shell)
+            const int y = ya + l / (ncol * nz), k = l % (ncol * nz), x = xa + k / nz, z = za + k % nz;
+            fold(p, (long long)y * s3 + (long long)x * s2 + z, z, x, y);
+        }
+        __syncthreads();
+        // axis 3: columns (x, z) of this block, the face planes only
+        for (int l = tid; l < ncol * nz; l += NT) {
+            const int x = xa + l / nz, z = za + l % nz;
+            const long long c0 = (long long)x * s2 + z;
+            const float b = __ldg((f == 0 ? p.yl : p.yh) + (long long)x * n1 + z);
+            if (f == 0) {
+                for (int i = 1; i <= 4; i++) {
+                    const long long ci = c0 + i * s3, cb = ci + s3;
+                    float mi = p.mu[ci], mb = p.mu[cb], kb = p.kap[cb], ki = p.kap[ci];
+                    tcell(mi, mb, kb, ki, b);
+                    p.mu[ci] = mi;
+                    p.mu[cb] = mb;
+                    p.kap[cb] = kb;
+                    p.kap[ci] = ki;
+                }
+            } else {
+                for (int i = n3 - 2; i >= n3 - 5; i--) {
+                    const long long ci = c0 + i * s3, cb = ci - s3;
+                    float mi = p.mu[ci], mb = p.mu[cb], kb = p.kap[cb], ki = p.kap[ci];
+                    tcell(mi, mb, kb, ki, b);
+                    p.mu[ci] = mi;
+                    p.mu[cb] = mb;
+                    p.kap[cb] = kb;
+                    p.kap[ci] = ki;
+                }
+            }
+        }
+        __syncthreads();
+        // axis 2: the x-ranges holding a face, lines (y, z) of this z-range
+        const bool xlo = xr == 0, xhi = xr == p.nxr - 1;
+        if (xlo || xhi)
+            for (int l = tid; l < SHELL * nz; l += NT) {
+                const int y = ya + l / nz, z = za + l % nz;
+                const long long line = (long long)y * n1 + z, c0 = (long long)y * s3 + z;
+                // a line's two faces belong to the first and the last x-range
+                if (xlo && xhi) {
+                    tline(p, c0, s2, n2, __ldg(p.xl + line), __ldg(p.xh + line), true);
+                } else if (xhi) {
+                    tline(p, c0, s2, n2, 0.f, __ldg(p.xh + line), false);
+                } else {  // low face only: i = 1 .. 4
+                    const float cl = __ldg(p.xl + line);
+                    for (int i = 1; i <= 4; i++) {
+                        const long long ci = c0 + i * s2, cb = ci + s2;
+                        float mi = p.mu[ci], mb = p.mu[cb], kb = p.kap[cb], ki = p.kap[ci];
+                        tcell(mi, mb, kb, ki, cl);
+                        p.mu[ci] = mi;
+                        p.mu[cb] = mb;
+                        p.kap[cb] = kb;
+                        p.kap[ci] = ki;
+                    }
+                }
+            }
+        __syncthreads();
+        // axis 1: the line ends inside this z-range (already folded)
+        const bool zlo = zr == 0, zhi = zr == p.nzr - 1;
+        if (zlo && zhi) {
+            for (int l = tid; l < SHELL * ncol; l += NT) {
+                const int y = ya + l / ncol, x = xa + l % ncol;
+                zends(p, (long long)y * n2 + x, x, y, false);
+            }
+        } else if (zlo || zhi) {
+            for (int l = tid; l < SHELL * ncol; l += NT) {
+                const int y = ya + l / ncol, x = xa + l % ncol;
+                const long long line = (long long)y * n2 + x;
+                if (zhi) {
+                    tline(p, line * n1, 1, n1, 0.f, __ldg(p.zh + line), false);
+                } else if (p.top) {
+                    const float cl = __ldg(p.zl + line);
+                    for (int i = 1; i <= 4; i++) {
+                        const long long ci = line * n1 + i, cb = ci + 1;
+                        float mi = p.mu[ci], mb = p.mu[cb], kb = p.kap[cb], ki = p.kap[ci];
+                        tcell(mi, mb, kb, ki, cl);
+                        p.mu[ci] = mi;
+                        p.mu[cb] = mb;
+                        p.kap[cb] = kb;
+                        p.kap[ci] = ki;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        const int nq = nz / 4;
+        for (int l = tid; l < SHELL * ncol * nq; l += NT) {
+            const int y = ya + l / (ncol * nq), k = l % (ncol * nq);
+            gcells(p, y, za + 4 * (k % nq), xa + k / nq);
+        }
+    }
+}
+
+void launch_bnd3_adj(Bnd3AdjParams p, cudaStream_t s) {
+    using namespace b3;
+    p.n_int = p.g.n3 - 2 * SHELL;
+    p.nxr = p.g.n2 / XR > 0 ? p.g.n2 / XR : 1;
+    p.nzr = p.g.n1 / ZR > 0 ? p.g.n1 / ZR : 1;
+    k_bnd3_adj<<<p.n_int + 2 * p.nxr * p.nzr, NT, 0, s>>>(p);
+}
+
 }  // namespace awe

@@ -534,6 +534,10 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
     // where the grid is small enough for per-cell lists and no ABC transpose
     // follows the step
     const bool fuse_pts = !st->tma && !st->kap && cells <= (1LL << 24);
+    // 3D TMA path: one boundary launch per adjoint step (k_bnd3_adj) instead of
+    // the kappa fold, three ABC-transpose launches and the g pass; AWE_BND3=0
+    // keeps the separate launches (the tests compare both)
+    const bool bnd_adj = st->tma && st->kap && stepB3_bnd(p);
     if (fuse_pts) {
         if (!st->lists_ok) {
             const int nc = d.ndim == 3 ? 8 : 4;
@@ -606,12 +610,26 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
             }
         }
         for (int k = k1 - 1; k >= k0; k--) {
-            if (d.ndim == 3 && d.dabc) {
+            if (bnd_adj) {
+                // kappa of the previous adjoint step folded into this step's nu, the
+                // transposed ABC and g = I vel2 nu in one launch
+                Bnd3AdjParams bp{};
+                bp.g = g;
+                bp.mu = X;
+                bp.kap = st->kap;
+                bp.gout = st->gbuf;
+                bp.vel2 = p->vel;
+                bp.zl = abc.zl, bp.zh = abc.zh, bp.xl = abc.xl, bp.xh = abc.xh, bp.yl = abc.yl, bp.yh = abc.yh;
+                bp.w1 = ap.w1, bp.w2 = ap.w2, bp.w3 = ap.w3;
+                bp.top = !d.fsrf;
+                launch_bnd3_adj(bp, s);
+                launches++;
+            } else if (d.ndim == 3 && d.dabc) {
                 launch_abc_adjB(p->nop, d.fsrf, X, st->kap, abc, g, s);
                 launches += 3;
             }
             if (st->tma) {
-                launch_adj_g(X, p->vel, st->gbuf, g, p->nop, s);
+                if (!bnd_adj) launch_adj_g(X, p->vel, st->gbuf, g, p->nop, s);
                 prof_begin(p, s, AWE_PROF_ADJOINT);
                 cudaError_t e = launch_stepB3_adj(st->g_halo, *ymap, *xmap, Y, slot0 + (size_t)(k - k0) * cells,
                                                   st->G, sp, p->tma_shape, p->sched_counter, p->sched_base, p->d_err,
@@ -622,7 +640,7 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
                     set_error("TMA adjoint launch failed: %s", cudaGetErrorString(e));
                     return AWE_ERR_CUDA;
                 }
-                launches += 2;
+                launches += bnd_adj ? 1 : 2;
             } else {
                 const float *Vk = slot0 + (size_t)(k - k0 + 1) * cells;
                 if (fuse_pts) {
@@ -635,7 +653,7 @@ awe_status plan_gradient(awe_plan *p, const float *d_wav, int ncs, const float *
                 prof_end(p, s);
                 launches++;
             }
-            if (d.ndim == 3 && d.dabc) {
+            if (d.ndim == 3 && d.dabc && !bnd_adj) {  // (bnd_adj: folded by the next step's launch)
                 launch_kap_fold(Y, st->kap, ap, s);
                 launches++;
             }
