@@ -377,7 +377,8 @@ static bool encode_fn() {
     if (g_encode) return true;
     void *fn = nullptr;
     cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &fn, cudaEnableDefault, &q) != cudaSuccess ||
+    // the function as introduced in CUDA 12.0 (its ABI version)
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
         q != cudaDriverEntryPointSuccess || !fn)
         return false;
     g_encode = reinterpret_cast<EncodeTiledFn>(fn);

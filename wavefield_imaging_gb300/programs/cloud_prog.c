@@ -54,7 +54,7 @@ static int window_main(const char *prog, int gpu) {
     long long nw = 0;
     long long *index = malloc(sizeof(long long) * (ng ? ng : 1));
     float *win = malloc(sizeof(float) * AWE_CLOUD_NCO * (ng ? ng : 1));
-    float *wd = fast ? malloc(sizeof(float) * 2 * (nf * ng ? nf * ng : 1)) : NULL;
+    float *wd = fast ? malloc(sizeof(float) * 2 * (nf * ng > 0 ? nf * ng : 1)) : NULL;
     if (awe_cloud_window(gpu, g, ng, o, no, apt, fast ? nf : 0, 2, d, &nw, index, win, wd) != AWE_OK)
         die(prog, awe_last_error());
     rsf_file *Fgou = rsf_output("out");
@@ -124,7 +124,7 @@ static int merge_main(const char *prog, int gpu, int argc, char **argv) {
         rsf_close(Fd);
     }
     float *pts = malloc(sizeof(float) * AWE_CLOUD_NCO * (ntot ? ntot : 1));
-    float *dat = malloc(sizeof(float) * (size_t)ncomp * (ntot * nf ? ntot * nf : 1));
+    float *dat = malloc(sizeof(float) * (size_t)ncomp * (ntot * nf > 0 ? ntot * nf : 1));
     long long p0 = 0;
     for (int c = 0; c < nwin; c++) {
         if (nwp[c] == 0) continue; /* empty windows are skipped (Mbycloudmerge3d.c:199) */
@@ -140,7 +140,7 @@ static int merge_main(const char *prog, int gpu, int argc, char **argv) {
         rsf_close(Fc);
         rsf_close(Fd);
     }
-    float *out = malloc(sizeof(float) * (size_t)ncomp * (nf * na ? nf * na : 1));
+    float *out = malloc(sizeof(float) * (size_t)ncomp * (nf * na > 0 ? nf * na : 1));
     if (awe_cloud_merge(gpu, all, na, nwin, nwp, pts, dat, nf, ncomp, norm, hashscale, out) != AWE_OK)
         die(prog, awe_last_error());
     rsf_file *Fout = rsf_output("out");
