@@ -384,7 +384,8 @@ def run_ours(args):
     if args.extras and world == 1:
         # the second half of the metric and the spherical configuration, on the
         # same GPU after the headline (each leg reports its own failure)
-        for key, fn in (("batched_gradient", extra_batched_gradient), ("spherical_forward", extra_spherical_forward)):
+        for key, fn in (("batched_gradient", extra_batched_gradient), ("spherical_forward", extra_spherical_forward),
+                        ("gradients_3d", extra_gradients_3d)):
             try:
                 res = fn(args, local, peak, peak_kind)
                 if key == "batched_gradient":
@@ -571,6 +572,100 @@ def extra_spherical_forward(args, local, peak, peak_kind):
             "value": cells * nt / (ms / 1e3), "unit": "cell-updates/s", "ms_per_run": ms,
             "roofline": {"kernel": kernel, "avg_launch_us": avg * 1e6, "achieved": achieved,
                          "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind}}
+
+
+def _timed_gradient(plan, wav, dobs, nt, cells, peak, peak_kind, step_bytes, adj_bytes, names):
+    """One untimed and one timed device-resident gradient (BFP16
+    checkpoints) of a plan whose model and geometry are set; the step and
+    adjoint kernels timed with CUDA events on their stream."""
+    import torch
+
+    import wavefield_imaging_gb300 as awe
+
+    d_wav = torch.from_numpy(wav).cuda()
+    d_dobs = torch.from_numpy(np.ascontiguousarray(dobs, np.float32)).cuda()
+    d_grad = torch.zeros(int(plan.desc.n[0]) * int(plan.desc.n[1]) * int(plan.desc.n[2]), dtype=torch.float64,
+                         device="cuda")
+    stream = torch.cuda.Stream()
+
+    def step():
+        return plan.gradient_device(d_wav.data_ptr(), 1, d_dobs.data_ptr(), d_grad.data_ptr(),
+                                    ckpt_format=awe.CKPT_BFP16, stream=stream.cuda_stream)
+
+    step()
+    torch.cuda.synchronize()
+    plan.profile(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    J = step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    kinds = plan.profile_read_kinds()
+    plan.profile(False)
+    ms = e0.elapsed_time(e1)
+    out = {"gradient_ms": ms, "misfit": J, "kernels": {}}
+    for kind, nbytes in (("step", step_bytes), ("adjoint", adj_bytes)):
+        kms, kn = kinds[kind]
+        if kn:
+            avg = kms / 1e3 / kn
+            k = {"kernel": names[kind], "launches": kn, "avg_launch_us": avg * 1e6, "share_of_gradient": kms / ms}
+            if nbytes:
+                k.update(bytes_per_cell=nbytes, achieved=nbytes * cells / avg / 1e9, unit="GB/s",
+                         frac=nbytes * cells / avg / 1e9 / peak, peak=peak, peak_source=peak_kind)
+            out["kernels"][kind] = k
+    return out
+
+
+def extra_gradients_3d(args, local, peak, peak_kind):
+    """The c3 and c4 gradients, each on its full grid for 300 of its 3000
+    steps (one shot, BFP16 checkpoints, start model smoothed 100 m along z or
+    r): gradient time and the step and adjoint kernels' HBM fractions."""
+    from scipy.ndimage import gaussian_filter1d
+
+    import wavefield_imaging_gb300 as awe
+
+    nt = 300
+    res = {}
+    # c3: 512^3 cartesian, 8th order (forward steps 16 B per cell; the
+    # recompute steps also store L(V_k), 20 B; adjoint step 36 B)
+    w = workload(nt, args.n)
+    vtrue = layered_model_3d(w)
+    v0 = gaussian_filter1d(vtrue, 100.0 / 5.0, axis=2, mode="nearest").astype(np.float32)
+    sou, rec = geometry(w)
+    wav = ricker(nt, w["dt"], w["f0"])
+    desc = awe.make_desc(3, w["n"], w["d"], w["o"], nt, w["dt"], nb=w["nb"], fdorder=w["fdorder"], dabc=w["dabc"],
+                         expl=1, precision=awe.FAST)
+    with awe.Plan(desc, device=local) as plan:
+        plan.set_geometry(sou, rec)
+        plan.set_model(vtrue)
+        dobs = plan.forward(wav)
+        plan.set_model(v0)
+        r = _timed_gradient(plan, wav, dobs, nt, padded_cells(w), peak, peak_kind, None, 36,
+                            {"step": "k_stepB3_o8 (forward 16 B, recompute 20 B per cell)",
+                             "adjoint": "k_stepB3_o8 adjoint step"})
+    r["workload"] = w["name"].replace("nt=%d" % nt, "nt=%d of 3000" % nt) + ", gradient, BFP16 checkpoints"
+    res["cartesian"] = r
+    # c4: the spherical shell, one source
+    w = spher_workload(nt)
+    vtrue = spher_model(w)
+    v0 = gaussian_filter1d(vtrue, 100.0 / 5.0, axis=2, mode="nearest").astype(np.float32)
+    sou, rec = spher_shots(w, 1)[0]
+    wav = ricker(nt, w["dt"], w["f0"])
+    desc = awe.make_desc(3, w["n"], w["d"], w["o"], nt, w["dt"], coords=awe.SPHER, scheme=awe.SCHEME_GPU,
+                         nb=w["nb"], expl=0, precision=awe.FAST)
+    cells = int(np.prod([n + 2 * w["nb"] for n in w["n"]]))
+    with awe.Plan(desc, device=local) as plan:
+        plan.set_geometry(sou, rec)
+        plan.set_model(vtrue)
+        dobs = plan.forward(wav)
+        plan.set_model(v0)
+        tma = plan.step_kernel == "tma_sph"
+        r = _timed_gradient(plan, wav, dobs, nt, cells, peak, peak_kind, BYTES_PER_CELL, ADJ_BYTES_PER_CELL,
+                            {"step": SPHER_KERNEL[plan.step_kernel],
+                             "adjoint": "k_adjA_sph_tma" if tma else "k_adjA_sph2"})
+    r["workload"] = w["name"].replace("nt=%d" % nt, "nt=%d of 3000" % nt) + ", gradient, BFP16 checkpoints"
+    res["spherical"] = r
+    return res
 
 
 GRAD_METRIC = "FWI gradients/s (misfit gradient, checkpointed fwd + adjoint)"
