@@ -168,3 +168,48 @@ def test_pipeline_wait_timeout_is_reported_and_the_gpu_stays_usable():
     assert int(status) == 2  # AWE_ERR_CUDA
     assert named == "True"
     assert ok == "True"  # a new plan without the limit runs normally
+
+
+_SPH_TIMEOUT_CODE = r'''
+import os, sys; sys.path.insert(0, ".")
+import numpy as np, wavefield_imaging_gb300 as awe
+n, nt = (40, 30, 28), 40
+d = (0.005, 1.5e-6, 1.5e-6)
+o = (3387.0, np.pi / 2 - 15 * d[1], -14 * d[2])
+vel = np.full(n[::-1], 0.168, np.float32)
+wav = np.sin(np.arange(nt) * 0.3).astype(np.float32)
+sou = np.array([[o[0] + 25 * d[0], o[2] + 14 * d[2], o[1] + 15 * d[1]]], np.float32)
+rec = np.array([[o[0] + 28 * d[0], o[2] + 10 * d[2], o[1] + 12 * d[1]]], np.float32)
+desc = awe.make_desc(3, n, d, o, nt, 0.005, coords=awe.SPHER, scheme=awe.SCHEME_GPU, nb=6, precision=awe.FAST)
+res = []
+with awe.Plan(desc) as p:
+    assert p.step_kernel == "tma_sph"
+    p.set_model(vel); p.set_geometry(sou, rec)
+    for call in ("forward", "gradient"):
+        try:
+            if call == "forward":
+                p.forward(wav)
+            else:
+                p.gradient(wav, np.zeros((nt, 1), np.float32))
+            res.append("0")
+        except awe.AweError as e:
+            res.append("%d:%s" % (e.status, "timed out" in str(e)))
+os.environ.pop("AWE_PIPELINE_SPIN_LIMIT")
+with awe.Plan(desc) as p:
+    p.set_model(vel); p.set_geometry(sou, rec)
+    dat = p.forward(wav)
+    g, J = p.gradient(wav, np.zeros((nt, 1), np.float32))
+print(" ".join(res), bool(np.isfinite(dat).all() and np.abs(dat).max() > 0), bool(np.isfinite(g).all() and J > 0))
+'''
+
+
+@pytest.mark.gpu
+def test_spherical_pipeline_wait_timeouts_are_reported():
+    """The TMA-staged spherical step and adjoint kernels under a zero wait
+    limit: the forward and the gradient both report AWE_ERR_CUDA with the
+    timeout message (their CTAs drain their copies in flight and leave), and
+    a new plan without the limit runs both normally."""
+    out = _probe(_SPH_TIMEOUT_CODE, {"AWE_PIPELINE_SPIN_LIMIT": "0"})
+    fwd, grad, ok_fwd, ok_grad = out.split()
+    assert fwd == "2:True" and grad == "2:True"
+    assert ok_fwd == "True" and ok_grad == "True"
