@@ -1,10 +1,13 @@
 """FP32 error of each configuration against an FP64 CPU run of the same
 scheme (the engine's AWE_FAST traces against liboracle64 / the FP64
 spherical restatement).  Sizes: the 2D configuration in full (512^2, nt=4000);
-the 3D and spherical ones on reduced grids a CPU finishes in seconds.  The
-errors are printed (pytest -s) and bounded at about ten times the measured
-value, so a regression of the FP32 path shows.  The FP32 engine against the
-FP32 oracle at the configurations' full grids is test_full_config_parity.py."""
+the 3D and spherical ones on their full grids with the time axis truncated
+(576^3 padded, 60 steps; 764 x 576 x 576 padded, 40 steps, the Ricker peak
+moved to 0.1 us so the wavefront forms inside the window) and on reduced
+grids over longer runs (96^3 and 120 x 48 x 48, 300 steps).  The errors are
+printed (pytest -s) and bounded at about ten times the measured value, so a
+regression of the FP32 path shows.  The FP32 engine against the FP32 oracle
+at the configurations' full grids is test_full_config_parity.py."""
 import numpy as np
 import pytest
 
@@ -96,3 +99,71 @@ def test_spherical_reduced_config_against_fp64():
     err = rel_l2(dat, ref)
     _report("spherical shell 120x48x48 nt=300 (c4 scheme)", err)
     assert err <= 4e-5  # measured 3.9e-6
+
+
+def _ricker_at(nt, dt, f0, t0):
+    t = np.arange(nt) * dt - t0
+    a = (np.pi * f0 * t) ** 2
+    r = (1 - 2 * a) * np.exp(-a)
+    return (r / np.abs(r).max()).astype(np.float32)
+
+
+def test_3d_full_grid_against_fp64():
+    """c3's grid (512^3, 576^3 padded, nb 32, 128 x 128 receivers), 60 steps:
+    traces and the final padded wavefield against the FP64 oracle."""
+    import bench
+    import wavefield_imaging_gb300 as awe
+    from oracle import oracle
+
+    w = bench.workload(nt=60)
+    vel = bench.layered_model_3d(w)
+    sou, rec = bench.geometry(w)
+    wav = _ricker_at(w["nt"], w["dt"], w["f0"], 0.1)
+    js = w["nt"] - 1
+    par = dict(n=list(w["n"]), d=list(w["d"]), o=list(w["o"]), nb=w["nb"], nt=w["nt"], dt=w["dt"], fdorder=8, dabc=1,
+               expl=1, jsnap=js, bnds=1)
+    desc = awe.make_desc(3, w["n"], w["d"], w["o"], w["nt"], w["dt"], nb=w["nb"], fdorder=8, dabc=1, expl=1,
+                         jsnap=js, bnds=1, precision=awe.FAST)
+    with awe.Plan(desc) as p:
+        assert p.step_kernel == "tma3d"
+        p.set_model(vel)
+        p.set_geometry(sou, rec)
+        dat, snaps = p.forward(wav, snapshots=True)
+    ref, ref_s = oracle.cart_cpu(par, vel, wav, sou, rec, fp64=True)
+    assert np.abs(ref).max() > 0
+    err, err_w = rel_l2(dat, ref), rel_l2(snaps[-1], ref_s[-1])
+    _report("3D 512^3 (576^3 padded) nt=60 traces (c3 grid)", err)
+    _report("3D 512^3 (576^3 padded) nt=60 final wavefield (c3 grid)", err_w)
+    assert err <= 2.5e-6  # measured 2.2e-7
+    assert err_w <= 3.5e-6  # measured 3.3e-7
+
+
+def test_spherical_full_grid_against_fp64():
+    """c4's grid (764 x 576 x 576 padded, nb 32), one source of the track
+    with 64 x 64 receivers and 8 more on its radius, 40 steps: traces against
+    the FP64 spherical restatement."""
+    import bench
+    import wavefield_imaging_gb300 as awe
+    from oracle import oracle
+
+    nt = 40
+    w = bench.spher_workload(nt)
+    vel = bench.spher_model(w)
+    sou, rec = bench.spher_shots(w, 1)[0]
+    rs, ph, th = sou[0]
+    near = np.array([[rs + k * w["d"][0], ph, th] for k in (-8, -6, -4, -2, 2, 4, 6, 8)], np.float32)
+    rec = np.concatenate([rec, near])
+    wav = _ricker_at(nt, w["dt"], w["f0"], 0.1)
+    par = dict(n=list(w["n"]), d=list(w["d"]), o=list(w["o"]), nb=w["nb"], nt=nt, dt=w["dt"])
+    desc = awe.make_desc(3, w["n"], w["d"], w["o"], nt, w["dt"], coords=awe.SPHER, scheme=awe.SCHEME_GPU, nb=w["nb"],
+                         expl=0, precision=awe.FAST)
+    with awe.Plan(desc) as p:
+        assert p.step_kernel == "tma_sph"
+        p.set_model(vel)
+        p.set_geometry(sou, rec)
+        dat = p.forward(wav)
+    ref = oracle.spher3d_fp64(dict(par, expl=0), vel, wav, sou, rec)
+    assert np.abs(ref).max() > 0
+    err = rel_l2(dat, ref)
+    _report("spherical shell 764x576x576 padded nt=40 traces (c4 grid)", err)
+    assert err <= 3.5e-6  # measured 3.1e-7
