@@ -382,12 +382,11 @@ __device__ __forceinline__ void zends(const Bnd3AdjParams &p, long long line, in
     }
 }
 
-// g = I vel2 mu on cells [c0, c0 + 4 nq) of plane y, z-fastest (c0 % 4 == 0)
-__device__ __forceinline__ void gcells(const Bnd3AdjParams &p, int y, int z, int x) {
+// g = I vel2 mu on the 4 cells z .. z+3 of line (y, x) (z % 4 == 0), from
+// loaded values
+__device__ __forceinline__ void gstore(const Bnd3AdjParams &p, int y, int z, int x, float4 m, float4 v) {
     const int n1 = p.g.n1, n2 = p.g.n2, n3 = p.g.n3;
     const long long c = ((long long)y * n2 + x) * n1 + z;
-    const float4 m = *reinterpret_cast<const float4 *>(p.mu + c);
-    const float4 v = __ldg(reinterpret_cast<const float4 *>(p.vel2 + c));
     const bool rest = x >= 4 && x < n2 - 4 && y >= 4 && y < n3 - 4;
     float4 o;
     o.x = (rest && z >= 4 && z < n1 - 4) ? v.x * m.x : 0.f;
@@ -395,6 +394,34 @@ __device__ __forceinline__ void gcells(const Bnd3AdjParams &p, int y, int z, int
     o.z = (rest && z + 2 >= 4 && z + 2 < n1 - 4) ? v.z * m.z : 0.f;
     o.w = (rest && z + 3 >= 4 && z + 3 < n1 - 4) ? v.w * m.w : 0.f;
     __stcs(reinterpret_cast<float4 *>(p.gout + c), o);
+}
+
+__device__ __forceinline__ void gcells(const Bnd3AdjParams &p, int y, int z, int x) {
+    const long long c = ((long long)y * p.g.n2 + x) * p.g.n1 + z;
+    gstore(p, y, z, x, *reinterpret_cast<const float4 *>(p.mu + c), __ldg(reinterpret_cast<const float4 *>(p.vel2 + c)));
+}
+
+// g of a whole plane y, four groups of 4 cells per thread in flight
+__device__ __forceinline__ void gplane(const Bnd3AdjParams &p, int y, int tid) {
+    const int n1 = p.g.n1, n2 = p.g.n2, nq = n1 / 4, total = n2 * nq;
+    const long long base = (long long)y * n2 * n1;
+    for (int l0 = tid; l0 < total; l0 += 4 * b3::NT) {
+        float4 m[4], v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int l = l0 + u * b3::NT;
+            if (l < total) {
+                const long long c = base + 4LL * l;  // line l / nq, cells 4 (l % nq) ..: contiguous in the plane
+                m[u] = *reinterpret_cast<const float4 *>(p.mu + c);
+                v[u] = __ldg(reinterpret_cast<const float4 *>(p.vel2 + c));
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int l = l0 + u * b3::NT;
+            if (l < total) gstore(p, y, 4 * (l % nq), l / nq, m[u], v[u]);
+        }
+    }
 }
 }  // namespace b3a
 
@@ -423,8 +450,7 @@ __global__ void __launch_bounds__(b3::NT) k_bnd3_adj(const Bnd3AdjParams p) {
         // axis-1 ends, folded here for the lines outside the axis-2 bands
         for (int x = tid; x < n2; x += NT) zends(p, (long long)y * n2 + x, x, y, x >= SHELL && x < n2 - SHELL);
         __syncthreads();
-        const int nq = n1 / 4;
-        for (int l = tid; l < n2 * nq; l += NT) gcells(p, y, 4 * (l % nq), l / nq);
+        gplane(p, y, tid);
         return;
     }
     blk -= p.n_int;
