@@ -103,3 +103,26 @@ def test_moving_geometry_oracle_modes():
     assert np.array_equal(d1, r1)
     d0, _ = oracle.gpu_cart2d_moving(par, a["vel"], a["wav"], a["sou"][:1], 1, a["rec"][:1], 1, 1)
     assert not np.array_equal(d0, r1)
+
+
+def test_snapshot_window_rule():
+    """The cpu programs' window rule restated in the oracle: first padded index
+    floor((oq - opad)/d), stride floor(dq/d), float32 arithmetic; defaults the
+    model window; 3D bnds=y takes the padded counts and whole z-x planes; a
+    window leaving the padded grid is an error."""
+    p = dict(n=[48, 64], d=[5.0, 5.0], o=[0.0, 0.0], nb=12, jsnap=10)
+    npad = (72, 88, 1)
+    assert oracle.snapshot_window(p, 12, npad) == [(48, 12, 1), (64, 12, 1), (1, 0, 0)]
+    p["win"] = dict(nqz=20, oqz=-20.0, dqz=10.0, nqx=15, oqx=32.5, dqx=15.0)
+    assert oracle.snapshot_window(p, 12, npad) == [(20, 8, 2), (15, 18, 3), (1, 0, 0)]
+    p["win"] = dict(oqz=-61.0)
+    with pytest.raises(ValueError):
+        oracle.snapshot_window(p, 12, npad)
+    p3 = dict(n=[24, 20, 18], d=[5.0] * 3, o=[0.0] * 3, nb=8, jsnap=10, bnds=1, win=dict(oqy=-40.0))
+    assert oracle.snapshot_window(p3, 8, (40, 36, 34)) == [(40, 0, 1), (36, 0, 1), (34, 0, 1)]
+    p3["win"] = {}  # the reference's default oqy = oy starts at plane nb: outside the grid
+    with pytest.raises(ValueError):
+        oracle.snapshot_window(p3, 8, (40, 36, 34))
+    frame = np.arange(72 * 88, dtype=np.float32)
+    cut = oracle.cut_window(frame, [(2, 8, 2), (3, 18, 3), (1, 0, 0)], npad)
+    assert cut.tolist() == [18 * 72 + 8, 18 * 72 + 10, 21 * 72 + 8, 21 * 72 + 10, 24 * 72 + 8, 24 * 72 + 10]

@@ -176,7 +176,10 @@ awe_status planA_init(awe_plan *p) {
     // register-march kernel (the tests compare both)
     const char *kern = std::getenv("AWE_STEP_KERNEL");
     const bool force_simple = kern && std::strcmp(kern, "simple") == 0;
-    if (geom == 3 && d.precision == AWE_FAST && !force_simple && sphA_tma_eligible(g, nb) &&
+    // (the TMA kernels' sponge index walks the axes in this grid's priority
+    // order (r, phi, theta) = memory axes (1, 3, 2))
+    const bool pri_rpt = pa.pri[0] == 0 && pa.pri[1] == 2 && pa.pri[2] == 1;
+    if (geom == 3 && d.precision == AWE_FAST && !force_simple && pri_rpt && sphA_tma_eligible(g, nb) &&
         sphA_tma_maps(p->sph_maps, p->u, p->vel, g, 1)) {
         AWE_TRY(dev_alloc(p, (void **)&p->sched_counter, sizeof(unsigned long long)));
         AWE_TRY(dev_alloc(p, (void **)&p->d_err, sizeof(int)));

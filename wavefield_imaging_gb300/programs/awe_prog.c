@@ -383,6 +383,7 @@ int main(int argc, char **argv) {
             g_win.npad[a] = info.npad[a];
         }
         g_win.buf = malloc(sizeof(float) * (size_t)g_win.n[0] * g_win.n[1]);
+        if (!g_win.buf) die(prog, "out of host memory (snapshot window)");
     }
     if (img2d && windows && (wn[0] != d.n[0] || wn[1] != d.n[1]))
         die(prog, "adj=y: the image is written with the snapshot window's axes, so nqz and nqx must equal the "
