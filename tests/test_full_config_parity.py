@@ -6,7 +6,7 @@ full run would take the oracle minutes.  Both the traces and the final
 wavefield (the whole padded grid) are compared:
 
 * AWE_EXACT: bit for bit;
-* AWE_FAST: relative L2 <= 1e-5 (the benchmark spec's bound), and, for the
+* AWE_FAST: relative L2 <= 1e-5 (the FP32 parity bound), and, for the
   wavefield, <= 1e-4 in every 72^3 block that carries energy, so an error
   confined to one tile or one y-chunk cannot hide in the global norm.  One
   stated exception: the last frame of the full 4000-step 2D run, where the
@@ -26,7 +26,7 @@ from helpers import rel_l2
 
 pytestmark = pytest.mark.gpu
 
-BOUND = 1e-5  # spec rel-L2 bound, FP32 FAST vs the reference's FP32 order
+BOUND = 1e-5  # rel-L2 parity bound, FP32 FAST vs the reference's FP32 order
 BLOCK_BOUND = 1e-4
 
 

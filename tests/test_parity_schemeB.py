@@ -10,7 +10,7 @@ import pytest
 from helpers import desc_from_par, golden_paths, load_golden, rel_l2, run_engine
 
 pytestmark = pytest.mark.gpu
-TOL = 1e-5  # rel-L2, FP32 (the spec parity bound)
+TOL = 1e-5  # rel-L2, FP32 (the parity bound for FAST arithmetic)
 GOLDEN = golden_paths()
 
 
