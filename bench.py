@@ -406,7 +406,7 @@ def run_ours(args):
 
 
 def extra_batched_gradient(args, local, peak, peak_kind):
-    """FWI gradients of the 256-shot survey (c1 geometry, c2 physics: true
+    """FWI gradients of the 256-shot survey (the survey's geometry, the 2D gradient's physics: true
     model vs the same smoothed 100 m, BFP16 checkpoints, compensated sums):
     the batched gradient (all shots per launch) against the plain per-shot
     loop (awe_gradient shot after shot), the latter timed on 16 evenly spaced
@@ -617,7 +617,7 @@ def _timed_gradient(plan, wav, dobs, nt, cells, peak, peak_kind, step_bytes, adj
 
 
 def extra_gradients_3d(args, local, peak, peak_kind):
-    """The c3 and c4 gradients, each on its full grid for 300 of its 3000
+    """The 512^3 cartesian and the spherical-shell gradients, each on its full grid for 300 of its 3000
     steps (one shot, BFP16 checkpoints, start model smoothed 100 m along z or
     r): gradient time and the step and adjoint kernels' HBM fractions."""
     from scipy.ndimage import gaussian_filter1d
@@ -626,7 +626,7 @@ def extra_gradients_3d(args, local, peak, peak_kind):
 
     nt = 300
     res = {}
-    # c3: 512^3 cartesian, 8th order (forward steps 16 B per cell; the
+    # the 512^3 cube, 8th order (forward steps 16 B per cell; the
     # recompute steps also store L(V_k), 20 B; adjoint step 36 B)
     w = workload(nt, args.n)
     vtrue = layered_model_3d(w)
@@ -645,7 +645,7 @@ def extra_gradients_3d(args, local, peak, peak_kind):
                              "adjoint": "k_stepB3_o8 adjoint step"})
     r["workload"] = w["name"].replace("nt=%d" % nt, "nt=%d of 3000" % nt) + ", gradient, BFP16 checkpoints"
     res["cartesian"] = r
-    # c4: the spherical shell, one source
+    # the spherical shell, one source
     w = spher_workload(nt)
     vtrue = spher_model(w)
     v0 = gaussian_filter1d(vtrue, 100.0 / 5.0, axis=2, mode="nearest").astype(np.float32)
@@ -805,7 +805,7 @@ BATCH_METRIC = "batched 2D forward shots/s (uneven windows, one graph-replayed l
 
 
 def batch_survey(nshots=256, nxm=6000, nz=512, seed=5):
-    """The c1-style survey: a seeded layered model 6000 columns wide, shots
+    """The 256-shot survey: a seeded layered model 6000 columns wide, shots
     every 20 m (4 columns) along a straight track, each on its own window of
     nx in [300, 700] columns centred on the source, 128 receivers centred on
     the source at z = 50 m, source at z = 50 m."""
@@ -1046,7 +1046,7 @@ def spher_shots(w, nshots):
 
 
 def run_sphergrad(args):
-    """--workload sphergrad3d: misfit gradient of the spherical shell (c4
+    """--workload sphergrad3d: misfit gradient of the spherical shell (700 x 512 x 512
     grid and scheme; --shots sources along the track, default 1): forward
     with checkpoints, segment recompute, adjoint of the spherical step, shot
     after shot.  Start model: the true model smoothed along r (100 m).  One
@@ -1146,7 +1146,7 @@ def run_sphergrad(args):
 
 def run_spher(args):
     """--workload spher3d: one shot of the spherical-shell forward (scheme of
-    sfAWEFDspher3Dgpu) on the c4 grid."""
+    sfAWEFDspher3Dgpu) on the 700 x 512 x 512 shell."""
     import torch
 
     import wavefield_imaging_gb300 as awe

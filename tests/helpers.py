@@ -107,7 +107,7 @@ def tapered_direction(shape, rng, margin=3):
 
 def spher_grad_case(fsrf=0, nt=150, seed=3, n=(45, 20, 20), nb=8):
     """A small seeded gradient problem of the spherical GPU-program scheme:
-    the c4 spacing (5 m in r, 0.04/512 rad in theta and phi) on a (r, theta,
+    the 700 x 512 x 512 shell's spacing (5 m in r, 0.04/512 rad in theta and phi) on a (r, theta,
     phi) = n grid near r = 3388 km, ice over basalt with 2 % noise, one
     source and 7 receivers above it, close to the free surface.  Returns
     (par, vel, wav, sou, rec, vtrue); models are [nphi][ntheta][nr]."""

@@ -42,7 +42,7 @@ def test_2d_full_config_against_fp64():
         dat = p.forward(wav)
     ref, _ = oracle.cart_cpu(par, vel, wav, sou, rec, fp64=True)
     err = rel_l2(dat, ref)
-    _report("2D 512^2 nt=4000 8th order (c0/c1/c2 grid)", err)
+    _report("2D 512^2 nt=4000 8th order (the 2D forward, survey and gradient grid)", err)
     assert err <= 1.5e-5  # measured 1.5e-6
 
 
@@ -68,7 +68,7 @@ def test_3d_reduced_config_against_fp64():
         dat = p.forward(wav)
     ref, _ = oracle.cart_cpu(par, vel, wav, sou, rec, fp64=True)
     err = rel_l2(dat, ref)
-    _report("3D 96^3 nt=300 8th order, TMA kernel (c3 scheme)", err)
+    _report("3D 96^3 nt=300 8th order, TMA kernel", err)
     assert err <= 2.5e-6  # measured 2.2e-7
 
 
@@ -97,7 +97,7 @@ def test_spherical_reduced_config_against_fp64():
         dat = p.forward(wav)
     ref = oracle.spher3d_fp64(par, vel, wav, sou, rec)
     err = rel_l2(dat, ref)
-    _report("spherical shell 120x48x48 nt=300 (c4 scheme)", err)
+    _report("spherical shell 120x48x48 nt=300", err)
     assert err <= 4e-5  # measured 3.9e-6
 
 
@@ -109,7 +109,7 @@ def _ricker_at(nt, dt, f0, t0):
 
 
 def test_3d_full_grid_against_fp64():
-    """c3's grid (512^3, 576^3 padded, nb 32, 128 x 128 receivers), 60 steps:
+    """The 512^3 grid (512^3, 576^3 padded, nb 32, 128 x 128 receivers), 60 steps:
     traces and the final padded wavefield against the FP64 oracle."""
     import bench
     import wavefield_imaging_gb300 as awe
@@ -132,14 +132,14 @@ def test_3d_full_grid_against_fp64():
     ref, ref_s = oracle.cart_cpu(par, vel, wav, sou, rec, fp64=True)
     assert np.abs(ref).max() > 0
     err, err_w = rel_l2(dat, ref), rel_l2(snaps[-1], ref_s[-1])
-    _report("3D 512^3 (576^3 padded) nt=60 traces (c3 grid)", err)
-    _report("3D 512^3 (576^3 padded) nt=60 final wavefield (c3 grid)", err_w)
+    _report("3D 512^3 (576^3 padded) nt=60 traces", err)
+    _report("3D 512^3 (576^3 padded) nt=60 final wavefield", err_w)
     assert err <= 2.5e-6  # measured 2.2e-7
     assert err_w <= 3.5e-6  # measured 3.3e-7
 
 
 def test_spherical_full_grid_against_fp64():
-    """c4's grid (764 x 576 x 576 padded, nb 32), one source of the track
+    """The spherical shell's full grid (764 x 576 x 576 padded, nb 32), one source of the track
     with 64 x 64 receivers and 8 more on its radius, 40 steps: traces against
     the FP64 spherical restatement."""
     import bench
@@ -165,5 +165,5 @@ def test_spherical_full_grid_against_fp64():
     ref = oracle.spher3d_fp64(dict(par, expl=0), vel, wav, sou, rec)
     assert np.abs(ref).max() > 0
     err = rel_l2(dat, ref)
-    _report("spherical shell 764x576x576 padded nt=40 traces (c4 grid)", err)
+    _report("spherical shell 764x576x576 padded nt=40 traces", err)
     assert err <= 3.5e-6  # measured 3.1e-7

@@ -11,13 +11,13 @@ wavefield (the whole padded grid) are compared:
   confined to one tile or one y-chunk cannot hide in the global norm.  One
   stated exception: the last frame of the full 4000-step 2D run, where the
   reference's own FP32 rounding noise (against FP64) exceeds 1e-5; there
-  FAST is held to that noise instead (see the c0 test).
+  FAST is held to that noise instead (see the 2D test).
 
 Truncated runs use the configuration's 5 MHz Ricker wavelet with its peak
 moved to 0.1 us (step 20) so the wavefront is well formed inside the window.
-The grid-scale configurations: c0 2D 512^2 (nt = 4000, the full run), c1 the
-256-shot survey (nt = 4000, three shots checked), c3 512^3 (576^3 padded,
-nt = 60), c4 the spherical shell 700 x 512 x 512 (764 x 576 x 576 padded,
+The grid-scale workloads: 2D 512^2 (nt = 4000, the full run), the
+256-shot survey (nt = 4000, three shots checked), 512^3 (576^3 padded,
+nt = 60), the spherical shell 700 x 512 x 512 (764 x 576 x 576 padded,
 nt = 40, the 16-shot track in one launch)."""
 import numpy as np
 import pytest
@@ -82,8 +82,8 @@ def _engine(awe, desc, vel, wav, sou, rec, shots=None):
     return dat, snaps, kern
 
 
-def test_c0_2d_512_full_run_matches_the_oracle():
-    """c0: 512^2 at 5 m, nb 40, 8th order, dabc, nt = 4000 (the whole run),
+def test_2d_512_full_run_matches_the_oracle():
+    """2D 512^2 at 5 m, nb 40, 8th order, dabc, nt = 4000 (the whole run),
     source at x = centre, z = 50 m, 512 receivers at z = 50 m, snapshots
     every 100 steps (interior)."""
     import bench
@@ -118,8 +118,8 @@ def test_c0_2d_512_full_run_matches_the_oracle():
     assert diff <= max(BOUND, 2.0 * ref_noise)
 
 
-def test_c1_256_shot_survey_full_run_matches_the_oracle():
-    """c1: all 256 shots in one batched launch per step (column march),
+def test_256_shot_survey_full_run_matches_the_oracle():
+    """The survey: all 256 shots in one batched launch per step (column march),
     nt = 4000; shots 0, 128 and 255 against the oracle run on their windows."""
     import bench
     import wavefield_imaging_gb300 as awe
@@ -142,7 +142,7 @@ def test_c1_256_shot_survey_full_run_matches_the_oracle():
         assert rel_l2(dat[k], ref) <= BOUND, k
 
 
-def _c3_case(lattice):
+def _cube_case(lattice):
     import bench
 
     w = bench.workload(nt=60)
@@ -160,14 +160,14 @@ def _c3_case(lattice):
 
 
 @pytest.mark.parametrize("lattice", [False, True], ids=["config_source", "source_lattice"])
-def test_c3_512_cube_matches_the_oracle(lattice):
-    """c3: 512^3 at 5 m (576^3 padded), nb 32, 8th order, dabc, 128 x 128
+def test_512_cube_matches_the_oracle(lattice):
+    """512^3 at 5 m (576^3 padded), nb 32, 8th order, dabc, 128 x 128
     receivers at z = 50 m, nt = 60, on the TMA-staged step kernel; the final
     padded wavefield is compared whole and per 72^3 block."""
     import wavefield_imaging_gb300 as awe
     from oracle import oracle
 
-    w, vel, sou, rec, wav = _c3_case(lattice)
+    w, vel, sou, rec, wav = _cube_case(lattice)
     js = w["nt"] - 1  # frames at it = 0 and it = nt - 1
     ref, ref_s = oracle.cart_cpu(_cart_par(w, js, 1), vel, wav, sou, rec)
     assert np.abs(ref).max() > 0 and np.abs(ref_s[-1]).max() > 0
@@ -182,14 +182,14 @@ def test_c3_512_cube_matches_the_oracle(lattice):
     assert rel_l2(fa_s[-1], ref_s[-1]) <= BOUND
     npad = tuple(n + 2 * w["nb"] for n in w["n"])[::-1]
     worst, lit, nblk = block_errors(fa_s[-1], ref_s[-1], npad)
-    print("\nc3 %s: %d of %d blocks lit, worst block rel-L2 %.2e" % ("lattice" if lattice else "config", lit, nblk,
+    print("\n512^3 %s: %d of %d blocks lit, worst block rel-L2 %.2e" % ("lattice" if lattice else "config", lit, nblk,
                                                                    worst))
     assert worst <= BLOCK_BOUND
     if lattice:
         assert lit == nblk  # every block of the padded grid carries energy
 
 
-def _c4_case(nt, nshots):
+def _shell_case(nt, nshots):
     import bench
 
     w = bench.spher_workload(nt)
@@ -210,8 +210,8 @@ def _spher_desc(awe, w, precision, jsnap=0, bnds=0):
                          nb=w["nb"], expl=0, jsnap=jsnap, bnds=bnds, precision=precision)
 
 
-def test_c4_spherical_shell_matches_the_oracle():
-    """c4: r 700 x theta 512 x phi 512 (764 x 576 x 576 padded), nb 32,
+def test_spherical_shell_764x576x576_matches_the_oracle():
+    """Spherical shell: r 700 x theta 512 x phi 512 (764 x 576 x 576 padded), nb 32,
     nt = 40.  The 16-shot track advances in one launch per step; shots 0 and
     15 are checked against oracle runs, shot 0 also alone in both precisions
     with its final padded wavefield."""
@@ -219,7 +219,7 @@ def test_c4_spherical_shell_matches_the_oracle():
     from oracle import oracle
 
     nt = 40
-    w, vel, shots, wav = _c4_case(nt, 16)
+    w, vel, shots, wav = _shell_case(nt, 16)
     js = nt - 1
     par = dict(n=list(w["n"]), d=list(w["d"]), o=list(w["o"]), nb=w["nb"], nt=nt, dt=w["dt"], jsnap=js, bnds=1)
     ref0, ref0_s = oracle.gpu_scheme("spher3d", par, vel, wav, *shots[0])
@@ -234,7 +234,7 @@ def test_c4_spherical_shell_matches_the_oracle():
     assert rel_l2(fa_s[-1], ref0_s[-1]) <= BOUND
     npad = tuple(n + 2 * w["nb"] for n in w["n"])[::-1]
     worst, lit, nblk = block_errors(fa_s[-1], ref0_s[-1], npad)
-    print("\nc4 single shot: %d of %d blocks lit, worst block rel-L2 %.2e" % (lit, nblk, worst))
+    print("\nshell single shot: %d of %d blocks lit, worst block rel-L2 %.2e" % (lit, nblk, worst))
     assert worst <= BLOCK_BOUND
     del fa_s, ref0_s
     # the 16-shot track in one launch per step

@@ -28,7 +28,7 @@ def _scaled(d2, d1):
 
 @pytest.mark.gpu
 def test_3d_512_cube_traces_scale_with_the_wavelet():
-    """c3 grid: 512^3 (576^3 padded), nb=32, 8th order, dabc, 128x128
+    """512^3 (576^3 padded), nb=32, 8th order, dabc, 128x128
     receivers, on the TMA-staged step kernel."""
     import bench
     import wavefield_imaging_gb300 as awe
@@ -50,7 +50,7 @@ def test_3d_512_cube_traces_scale_with_the_wavelet():
 
 @pytest.mark.gpu
 def test_256_shot_survey_scales_with_the_wavelet_and_shots_match_single_runs():
-    """c1 survey: 256 shots on windows of 300-700 columns x nz 512 of a
+    """The survey: 256 shots on windows of 300-700 columns x nz 512 of a
     6000-column model, column-march kernel; two shots checked against
     single-shot plans."""
     import bench
@@ -80,7 +80,7 @@ def test_256_shot_survey_scales_with_the_wavelet_and_shots_match_single_runs():
 
 @pytest.mark.gpu
 def test_spherical_c4_grid_traces_scale_with_the_wavelet():
-    """c4 grid: r 700 x theta 512 x phi 512 (764 x 576 x 576 padded), one
+    """Spherical shell: r 700 x theta 512 x phi 512 (764 x 576 x 576 padded), one
     source and 64 x 64 receivers."""
     import bench
     import wavefield_imaging_gb300 as awe
@@ -101,7 +101,7 @@ def test_spherical_c4_grid_traces_scale_with_the_wavelet():
 
 @pytest.mark.gpu
 def test_3d_512_cube_gradient_is_a_difference_of_born_images():
-    """c3 grid, a short time axis: the misfit gradient of dobs equals
+    """512^3 grid, a short time axis: the misfit gradient of dobs equals
     Born(dsyn) - Born(dobs) (the adjoint is linear in the data)."""
     import bench
     import wavefield_imaging_gb300 as awe

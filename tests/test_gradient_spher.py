@@ -1,5 +1,5 @@
 """Misfit gradient of the spherical GPU-program scheme (sfAWEFDspher3Dgpu's
-step, the c4 configuration's scheme) on the engine's discrete adjoint,
+step, the scheme of the spherical-shell workload) on the engine's discrete adjoint,
 against the FP64 adjoint oracle (oracle/awe_adjoint_sph.c), which is pinned
 by finite differences of its own FP64 misfit."""
 import numpy as np
@@ -120,7 +120,7 @@ def test_reflectivity_injection_is_refused():
 @pytest.mark.gpu
 @pytest.mark.parametrize("nr", [46, 48])
 def test_several_shots_sum_the_single_shot_gradients(nr):
-    """awe_set_shots (the c4 track's layout): the gradient of three shots
+    """awe_set_shots (the spherical track's layout): the gradient of three shots
     is the sum of the three single-shot gradients, the misfit the sum of
     theirs, the synthetic data each shot's own columns; awe_set_geometry
     afterwards goes back to one shot."""
