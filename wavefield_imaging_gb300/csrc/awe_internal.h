@@ -87,6 +87,18 @@ void launch_hybridB(int ndim, int nop, int nbd, bool exact, int fsrf, float *uo,
 void launch_band_sponge(int ndim, int width, bool exact, float *u, const float *w1, const float *w2,
                         const float *w3, const Grid &g, cudaStream_t s, int zfused = 0);
 
+// Model preparation of the CPU-program scheme on the device (k_model.cu):
+// padded v^2 dt^2 (free-surface rows zeroed) or a plain padded copy, and the
+// one-way ABC coefficient tables, from the model as passed ([n3][n2][n1]).
+struct ModelPrep {
+    Grid g;                 // padded grid
+    int n1, n2, n3, nb, nd;  // model size, padding, dimensions
+    float dt, dt2, d1, d2, d3;
+    int zero1;              // axis-1 samples set to 0 on every line (free surface), 0: none
+};
+void launch_model_pad(const float *raw, float *out, const ModelPrep &m, bool vel2, cudaStream_t s);
+void launch_model_abc(const float *raw, const ModelPrep &m, float *const abc[6], cudaStream_t s);
+
 // The boundary work of a 3D step in one launch (k_boundary3.cu): one-way ABC
 // of the six faces, sponge of the shell the step kernel left unsponged
 // (cells within nop + 2 of a face), the receiver gather of the level the step

@@ -333,9 +333,19 @@ awe_status awe_set_model(awe_plan *p, const float *vel, const float *den, const 
         set_error("null plan or velocity");
         return AWE_ERR_INVALID;
     }
-    plan_graph_drop(p);  // the captured time loop baked in the old state
+    // The captured time loop of the CPU-program scheme reads the model through
+    // its device buffers, which a new model refills in place: the loop is kept
+    // unless a buffer moved (the first model, or a density added).
+    const bool cpu = p->d.scheme == AWE_SCHEME_CPU;
+    const void *before[8] = {p->vel, p->den, p->abc[0], p->abc[1], p->abc[2], p->abc[3], p->abc[4], p->abc[5]};
+    if (cpu) plan_gradient_graph_drop(p);
+    else plan_graph_drop(p);
     CUDA_TRY(cudaSetDevice(p->device));
-    awe_status st = (p->d.scheme == AWE_SCHEME_CPU) ? planB_model(p, vel, den) : planA_model(p, vel, rfl);
+    awe_status st = cpu ? planB_model(p, vel, den) : planA_model(p, vel, rfl);
+    if (cpu) {
+        const void *after[8] = {p->vel, p->den, p->abc[0], p->abc[1], p->abc[2], p->abc[3], p->abc[4], p->abc[5]};
+        if (st != AWE_OK || std::memcmp(before, after, sizeof before) != 0) plan_graph_drop(p);
+    }
     if (st == AWE_OK) p->model_set = true;
     return st;
 }
@@ -361,11 +371,30 @@ awe_status awe_set_geometry(awe_plan *p, int ns, const float *sou, int nr, const
         set_error("bad geometry arguments");
         return AWE_ERR_INVALID;
     }
-    plan_graph_drop(p);  // the captured time loop baked in the old state
+    // the captured time loop baked in the point buffers, their counts and the
+    // flags the points set; it is kept when none of them changes (the same
+    // acquisition run again, or points that only moved within their buffers)
+    auto key = [&](long long *k) {
+        k[0] = (long long)(uintptr_t)p->src;
+        k[1] = (long long)(uintptr_t)p->rec;
+        k[2] = p->ns;
+        k[3] = p->nr;
+        k[4] = p->move_mode;
+        k[5] = p->src_rows;
+        k[6] = p->rec_rows;
+        k[7] = p->sponge_deferred;
+        k[8] = p->src_in_shell;
+        k[9] = p->pa.nshot;
+    };
+    long long before[10], after[10];
+    key(before);
+    plan_gradient_graph_drop(p);  // its per-cell point lists follow the geometry
     CUDA_TRY(cudaSetDevice(p->device));
     set_move_mode(p, -1, 1, 1);
     awe_status st = set_geometry_common(p, ns, sou, nr, rec);
     if (st == AWE_OK) st = single_shot(p, ns, nr);
+    key(after);
+    if (st != AWE_OK || std::memcmp(before, after, sizeof before) != 0) plan_graph_drop(p);
     if (st == AWE_OK) p->geom_set = true;
     return st;
 }

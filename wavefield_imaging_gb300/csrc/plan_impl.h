@@ -50,6 +50,7 @@ struct awe_plan {
     std::vector<awe::Lint> h_src_lint;  // source corner indices in the reference's fdm axes
     bool sponge_deferred = false;  // a source node lies in the sponge band outside the boundary shell
     bool src_in_shell = false;     // a source node lies within nop + 2 of a face (3D)
+    int src_cap = 0, rec_cap = 0;  // points the src / rec device buffers hold
     // moving geometry (awe_set_moving_geometry): src/rec hold ns*src_rows and
     // nr*rec_rows entries; move_mode < 0 = fixed points
     int move_mode = -1, src_rows = 1, rec_rows = 1;

@@ -117,62 +117,51 @@ awe_status planB_init(awe_plan *p) {
 }
 
 awe_status planB_model(awe_plan *p, const float *vel, const float *den) {
+    // The model goes to the device as passed, into a level buffer (the levels
+    // are cleared at the start of every run), and the padded tables are made
+    // there (k_model.cu): the same float operations as the host restatement
+    // of fdutil.c's expand / abcone*_make, without a host pass over the
+    // padded grid.
     const awe_desc &d = p->d;
     const Grid &g = p->g;
     const size_t cells = (size_t)g.cells();
-    std::vector<float> v(cells);
-    expand_model(d.ndim, vel, v.data(), p->nbd, d.n);
-    const float dt = d.dt;
-    const int nb = p->nbd;
+    const size_t raw = (size_t)d.n[0] * d.n[1] * (d.ndim == 3 ? d.n[2] : 1);
+    cudaStream_t s = p->stream;
+    ModelPrep m{};
+    m.g = g;
+    m.n1 = d.n[0];
+    m.n2 = d.n[1];
+    m.n3 = d.ndim == 3 ? d.n[2] : 1;
+    m.nb = p->nbd;
+    m.nd = d.ndim;
+    m.dt = d.dt;
+    m.dt2 = d.dt * d.dt;
+    m.d1 = d.d[0];
+    m.d2 = d.d[1];
+    m.d3 = d.ndim == 3 ? d.d[2] : 1.f;
+    m.zero1 = (d.fsrf && !d.hybrid) ? std::min(p->nbd + 1, g.n1) : 0;
+    float *stage = p->u[1];
+    // no earlier work of this plan (on any stream) may still read the level
+    // buffers or the model tables
+    CUDA_TRY(cudaDeviceSynchronize());
+    CUDA_TRY(cudaMemcpyAsync(stage, vel, raw * sizeof(float), cudaMemcpyHostToDevice, s));
     if (d.dabc) {
-        // abcone2d_make / abcone3d_make(nbd, dt, vel) on the raw velocity
-        // (fdutil.c:1919-2019): b = (1 - v dt/d) / (1 + v dt/d) at the first
-        // interior sample of each face
-        const long long s2 = g.n1, s3 = (long long)g.n1 * g.n2;
-        std::vector<float> zl((size_t)g.n2 * g.n3), zh(zl.size()), xl((size_t)g.n1 * g.n3), xh(xl.size()),
-            yl((size_t)g.n1 * g.n2), yh(yl.size());
-        auto coef = [](float vv, float dt_, float dd) {
-            float q = vv * dt_ / dd;
-            return (1 - q) / (1 + q);
-        };
-        for (int i3 = 0; i3 < g.n3; i3++)
-            for (int i2 = 0; i2 < g.n2; i2++) {
-                zl[(size_t)i3 * g.n2 + i2] = coef(v[i3 * s3 + i2 * s2 + nb], dt, d.d[0]);
-                zh[(size_t)i3 * g.n2 + i2] = coef(v[i3 * s3 + i2 * s2 + g.n1 - nb - 1], dt, d.d[0]);
-            }
-        for (int i3 = 0; i3 < g.n3; i3++)
-            for (int i1 = 0; i1 < g.n1; i1++) {
-                xl[(size_t)i3 * g.n1 + i1] = coef(v[i3 * s3 + nb * s2 + i1], dt, d.d[1]);
-                xh[(size_t)i3 * g.n1 + i1] = coef(v[i3 * s3 + (g.n2 - nb - 1) * s2 + i1], dt, d.d[1]);
-            }
-        if (d.ndim == 3)
-            for (int i2 = 0; i2 < g.n2; i2++)
-                for (int i1 = 0; i1 < g.n1; i1++) {
-                    yl[(size_t)i2 * g.n1 + i1] = coef(v[nb * s3 + i2 * s2 + i1], dt, d.d[2]);
-                    yh[(size_t)i2 * g.n1 + i1] = coef(v[(g.n3 - nb - 1) * s3 + i2 * s2 + i1], dt, d.d[2]);
-                }
-        AWE_TRY(upload(p, &p->abc[0], zl.data(), zl.size()));
-        AWE_TRY(upload(p, &p->abc[1], zh.data(), zh.size()));
-        AWE_TRY(upload(p, &p->abc[2], xl.data(), xl.size()));
-        AWE_TRY(upload(p, &p->abc[3], xh.data(), xh.size()));
-        if (d.ndim == 3) {
-            AWE_TRY(upload(p, &p->abc[4], yl.data(), yl.size()));
-            AWE_TRY(upload(p, &p->abc[5], yh.data(), yh.size()));
-        }
+        const size_t sz[6] = {(size_t)g.n2 * g.n3, (size_t)g.n2 * g.n3, (size_t)g.n1 * g.n3, (size_t)g.n1 * g.n3,
+                              (size_t)g.n1 * g.n2, (size_t)g.n1 * g.n2};
+        for (int k = 0; k < (d.ndim == 3 ? 6 : 4); k++)
+            if (!p->abc[k]) AWE_TRY(dev_alloc(p, (void **)&p->abc[k], sz[k] * sizeof(float)));
+        float *const tabs[6] = {p->abc[0], p->abc[1], p->abc[2], p->abc[3], p->abc[4], p->abc[5]};
+        launch_model_abc(stage, m, tabs, s);
     }
-    // v <- v^2 dt^2 (MAWEFDcart2Dcpu.c:290-291); free surface zeroes the
-    // first nb+1 samples of every axis-1 line (:292-295)
-    const float dt2 = dt * dt;
-    for (size_t i = 0; i < cells; i++) v[i] *= v[i] * dt2;
-    if (d.fsrf && !d.hybrid)
-        for (size_t line = 0; line < (size_t)g.n2 * g.n3; line++)
-            for (int i1 = 0; i1 < nb + 1 && i1 < g.n1; i1++) v[line * g.n1 + i1] = 0.f;
-    AWE_TRY(upload(p, &p->vel, v.data(), cells));
+    if (!p->vel) AWE_TRY(dev_alloc(p, (void **)&p->vel, cells * sizeof(float)));
+    launch_model_pad(stage, p->vel, m, true, s);
     if (den) {
-        std::vector<float> r(cells);
-        expand_model(d.ndim, den, r.data(), p->nbd, d.n);
-        AWE_TRY(upload(p, &p->den, r.data(), cells));
+        CUDA_TRY(cudaMemcpyAsync(stage, den, raw * sizeof(float), cudaMemcpyHostToDevice, s));
+        if (!p->den) AWE_TRY(dev_alloc(p, (void **)&p->den, cells * sizeof(float)));
+        launch_model_pad(stage, p->den, m, false, s);
     }
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(s));
     return AWE_OK;
 }
 
@@ -227,11 +216,24 @@ awe_status set_geometry_common(awe_plan *p, int ns, const float *sou, int nr, co
     };
     make(sou, ns, p->h_src, &p->h_src_lint);
     make(rec, nr, p->h_rec, nullptr);
-    if (p->src) dev_free(p, p->src);
-    if (p->rec) dev_free(p, p->rec);
-    p->src = p->rec = nullptr;
-    AWE_TRY(dev_alloc(p, (void **)&p->src, (ns > 0 ? ns : 1) * sizeof(GeoPoint)));
-    AWE_TRY(dev_alloc(p, (void **)&p->rec, (nr > 0 ? nr : 1) * sizeof(GeoPoint)));
+    // the point buffers are kept while large enough (a captured time loop
+    // that read them stays valid)
+    const int need_s = ns > 0 ? ns : 1, need_r = nr > 0 ? nr : 1;
+    if (!p->src || p->src_cap < need_s) {
+        if (p->src) dev_free(p, p->src);
+        p->src = nullptr;
+        p->src_cap = 0;
+        AWE_TRY(dev_alloc(p, (void **)&p->src, need_s * sizeof(GeoPoint)));
+        p->src_cap = need_s;
+    }
+    if (!p->rec || p->rec_cap < need_r) {
+        if (p->rec) dev_free(p, p->rec);
+        p->rec = nullptr;
+        p->rec_cap = 0;
+        AWE_TRY(dev_alloc(p, (void **)&p->rec, need_r * sizeof(GeoPoint)));
+        p->rec_cap = need_r;
+    }
+    CUDA_TRY(cudaDeviceSynchronize());  // earlier runs may still read the old points
     if (ns) CUDA_TRY(cudaMemcpy(p->src, p->h_src.data(), ns * sizeof(GeoPoint), cudaMemcpyHostToDevice));
     if (nr) CUDA_TRY(cudaMemcpy(p->rec, p->h_rec.data(), nr * sizeof(GeoPoint), cudaMemcpyHostToDevice));
     p->ns = ns;
