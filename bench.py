@@ -394,7 +394,7 @@ def run_ours(args):
             except Exception as e:  # noqa: BLE001 - reported in the JSON line
                 out[key] = {"error": "%s: %s" % (type(e).__name__, e)}
             torch.cuda.empty_cache()
-    if args.cpu_baseline:
+    if args.cpu_baseline and world == 1:  # the host-core baseline belongs to the one-GPU line
         v, cores, sample, _ = cpu_baseline(w)
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
         if grad_check is not None:
