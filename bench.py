@@ -236,6 +236,59 @@ def allmax(dist, x):
     return float(t.item())
 
 
+# the reference's own sfAWEFDcart3Dcpu, built from its sources by
+# oracle/ref/Makefile.cpu (absent: the oracle port is timed instead)
+REF_CPU_PROGRAM = os.path.join(ROOT, "oracle", "_ref", "sfAWEFDcart3Dcpu_ref")
+
+
+def _time_reference_program(args, w, cores, extra_steps=40):
+    """The reference CPU program on the workload: vel, sources and receivers
+    as RSF files, run with 2 and with 2 + extra_steps time steps; the wall-time
+    difference per step excludes reading the inputs and setting up.  Returns
+    (seconds per time step of each timed pair, sample text)."""
+    import shutil
+    import subprocess
+    import tempfile
+
+    from wavefield_imaging_gb300 import rsf
+
+    tmp = tempfile.mkdtemp(dir="/dev/shm" if os.path.isdir("/dev/shm") else None)
+    try:
+        vel = layered_model_3d(w)
+        sou, rec = geometry(w)
+        rsf.write(os.path.join(tmp, "vel.rsf"), vel, [(n, o, d) for n, o, d in zip(w["n"], w["o"], w["d"])])
+        rsf.write(os.path.join(tmp, "sou.rsf"), sou, [(3, 0.0, 1.0), (sou.shape[0], 0.0, 1.0)])
+        rsf.write(os.path.join(tmp, "rec.rsf"), rec, [(3, 0.0, 1.0), (rec.shape[0], 0.0, 1.0)])
+        del vel
+
+        def run(nt):
+            wpath = os.path.join(tmp, "wav_%d.rsf" % nt)
+            if not os.path.exists(wpath):
+                rsf.write(wpath, ricker(nt, w["dt"], w["f0"]).reshape(nt, 1), [(1, 0.0, 1.0), (nt, 0.0, w["dt"])])
+            cmd = [REF_CPU_PROGRAM, "vel=vel.rsf", "sou=sou.rsf", "rec=rec.rsf", "fdorder=%d" % w["fdorder"],
+                   "dabc=y", "free=n", "expl=y", "cden=y", "snap=n", "nb=%d" % w["nb"], "ompnth=%d" % cores,
+                   "verb=n"]
+            with open(wpath, "rb") as fin, open(os.path.join(tmp, "dat.rsf"), "wb") as fout:
+                t0 = time.perf_counter()
+                r = subprocess.run(cmd, stdin=fin, stdout=fout, stderr=subprocess.PIPE, cwd=tmp, timeout=600)
+                t1 = time.perf_counter()
+            if r.returncode != 0:
+                raise RuntimeError("reference program failed: %s" % r.stderr.decode()[-300:])
+            return t1 - t0
+
+        for _ in range(args.warmup):
+            run(2)
+        per_step = [(run(2 + extra_steps) - run(2)) / extra_steps for _ in range(args.steps)]
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    sample = ("%d-step difference of the reference's sfAWEFDcart3Dcpu (built from its sources, -O3 -fopenmp, "
+              "%d OpenMP threads) on the workload's %dx%dx%d padded grid, 2 against %d steps per bench step, "
+              "input reading and set-up cancelled" % (extra_steps, cores, w["n"][0] + 2 * w["nb"],
+                                                      w["n"][1] + 2 * w["nb"], w["n"][2] + 2 * w["nb"],
+                                                      2 + extra_steps))
+    return per_step, sample
+
+
 def run_reference(args):
     dist, rank, world, local = dist_init()
     if rank != 0:
@@ -245,6 +298,23 @@ def run_reference(args):
 
     oracle.build(with_reference=False)
     cores = os.cpu_count() or 1
+    if os.access(REF_CPU_PROGRAM, os.X_OK):
+        try:
+            per_step, sample = _time_reference_program(args, w, cores)
+            cells = float(np.prod([n + 2 * w["nb"] for n in w["n"]]))
+            value = cells * len(per_step) / sum(per_step)
+            out = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+                   "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(per_step) / len(per_step),
+                   "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+                   "data": "synthetic", "config": {"workload": w["name"], "sample": sample,
+                                                   "ms_per_step": "one time step of the reference program"},
+                   "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "reference",
+                                    "sample": sample},
+                   "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            print(json.dumps(out))
+            return
+        except Exception as e:  # noqa: BLE001 - the port is timed instead
+            print("reference program not timed (%s); timing the oracle port" % e, file=sys.stderr)
     npad = [n + 2 * w["nb"] for n in w["n"]]
     cells = float(np.prod(npad))
     t1 = oracle.cart3d_steps_seconds(npad[0], npad[1], npad[2], w["fdorder"], 1, cores)
