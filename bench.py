@@ -300,7 +300,10 @@ def run_reference(args):
     cores = os.cpu_count() or 1
     if os.access(REF_CPU_PROGRAM, os.X_OK):
         try:
-            per_step, sample = _time_reference_program(args, w, cores)
+            # a pair costs about two set-ups (2.8 s each on 16 Grace cores) plus
+            # the extra steps (0.17 s each): 40 extra steps up to 8 bench steps,
+            # 20 beyond, so that --steps 20 still ends within about 3 minutes
+            per_step, sample = _time_reference_program(args, w, cores, extra_steps=40 if args.steps <= 8 else 20)
             cells = float(np.prod([n + 2 * w["nb"] for n in w["n"]]))
             value = cells * len(per_step) / sum(per_step)
             out = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
