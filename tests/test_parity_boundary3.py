@@ -2,8 +2,10 @@
 faces, sponge of the shell the step kernel leaves unsponged, receiver
 gather and, when no source touches that shell, injection): against the
 oracle (EXACT bit for bit, FAST within rel-L2 1e-5), against the separate
-boundary launches (AWE_BND3=0), and run twice (results must not depend on
-the order in which blocks run).  Grids at the edges of the block split (an
+boundary launches (AWE_BND3=0), with the line ends of the level the step
+read taken from that level instead of the compact copy the previous launch
+wrote (AWE_BND_ENDS=0), and run twice (results must not depend on the order
+in which blocks run).  Grids at the edges of the block split (an
 axis-1 length that is not a multiple of 64, an axis-2 length that is not a
 multiple of 16), sources inside the shell, in the sponge band, on top of
 each other and across tile edges, receivers on the faces and outside the
@@ -104,6 +106,18 @@ def test_boundary_launch_matches_oracle_and_separate_launches(monkeypatch, case)
     fa, fa_s, _ = _run(awe, n, nb, nt, fsrf, jdata, expl, awe.FAST, vel, wav, sou, rec)
     assert rel_l2(fa, ref) <= TOL
     assert rel_l2(fa_s[-1], rsnaps[-1]) <= TOL
+
+    # the line ends of the level the step read taken from the level itself
+    # instead of the compact copy the previous launch wrote (AWE_BND_ENDS=0):
+    # the same values, so bit for bit in both precisions
+    monkeypatch.setenv("AWE_BND_ENDS", "0")
+    le, le_s, _ = _run(awe, n, nb, nt, fsrf, jdata, expl, awe.EXACT, vel, wav, sou, rec)
+    np.testing.assert_array_equal(le, ex)
+    np.testing.assert_array_equal(le_s, ex_s)
+    lf, lf_s, _ = _run(awe, n, nb, nt, fsrf, jdata, expl, awe.FAST, vel, wav, sou, rec)
+    np.testing.assert_array_equal(lf, fa)
+    np.testing.assert_array_equal(lf_s, fa_s)
+    monkeypatch.delenv("AWE_BND_ENDS")
 
     monkeypatch.setenv("AWE_BND3", "0")
     sep, sep_s, sep_launches = _run(awe, n, nb, nt, fsrf, jdata, expl, awe.EXACT, vel, wav, sou, rec)

@@ -120,6 +120,11 @@ struct Bnd3Params {
     const float *wav;
     int it, ncs, one_wavelet;
     int n_int, nxr, nzr, rec_blocks;  // set by launch_bnd3
+    // compact copies of the line ends ([n3][n2][16]: axis-1 cells 0..7, then
+    // n1-8..n1-1) of um (em: written by the previous step's launch; null:
+    // read um itself) and of the new level once final (eo; null: none)
+    const float *em;
+    float *eo;
 };
 bool bnd3_eligible(int nop, const Grid &g);
 void launch_bnd3(bool exact, Bnd3Params p, cudaStream_t s);

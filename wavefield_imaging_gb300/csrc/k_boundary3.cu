@@ -20,6 +20,13 @@
 //    or write cells no pass touches.
 // Every cell is written by one block only, so the result does not depend on
 // the order in which blocks run.
+//
+// The axis-1 ends (8 cells at each end of every line, 32 bytes of every
+// n1*4-byte line) are the scattered part of the work.  Within a forward run
+// each launch also writes the final ends of the new level to a compact
+// [n3][n2][16] copy, and the next step's launch reads the ends of the level
+// its step read (the same values) from that copy with coalesced loads
+// instead of one scattered sector per line end.
 #include <cuda_runtime.h>
 
 #include "awe_internal.h"
@@ -103,8 +110,24 @@ __device__ __forceinline__ void b3_xline(const Bnd3Params &p, long long c0, int 
     for (int k = 1; k <= 4; k++) p.uo[c0 + (long long)(xa + k * dx) * s2] = v[k];
 }
 
+// float4 `part` of line `line`'s ends (parts 0, 1: cells 0..7; 2, 3: cells
+// n1-8..n1-1) of the level the step read: from the compact copy of its line
+// ends the previous step's launch wrote (em), else from the level itself
+__device__ __forceinline__ float4 b3_mend(const Bnd3Params &p, long long line, int part) {
+    if (p.em) return __ldg(reinterpret_cast<const float4 *>(p.em) + line * 4 + part);
+    const float4 *m = reinterpret_cast<const float4 *>(p.um + line * p.g.n1);
+    return __ldg(m + (part < 2 ? part : p.g.n1 / 4 - 4 + part));
+}
+
+// the compact copy of the new level's line ends (eo), read back from uo once
+// the line's cells are final
+__device__ __forceinline__ void b3_eput_from_uo(const Bnd3Params &p, long long line, int part) {
+    const float4 *o = reinterpret_cast<const float4 *>(p.uo + line * p.g.n1);
+    reinterpret_cast<float4 *>(p.eo)[line * 4 + part] = o[part < 2 ? part : p.g.n1 / 4 - 4 + part];
+}
+
 template <bool EXACT>
-__global__ void __launch_bounds__(b3::NT) k_bnd3(const Bnd3Params p) {
+__global__ void __launch_bounds__(b3::NT, 4) k_bnd3(const Bnd3Params p) {
     using namespace b3;
     const int tid = threadIdx.x;
     const int n1 = p.g.n1, n2 = p.g.n2, n3 = p.g.n3;
@@ -118,34 +141,53 @@ __global__ void __launch_bounds__(b3::NT) k_bnd3(const Bnd3Params p) {
         for (int x = tid; x < n2; x += NT) {
             const long long line = (long long)y * n2 + x;
             float4 *o = reinterpret_cast<float4 *>(p.uo + line * n1);
-            const float4 *m = reinterpret_cast<const float4 *>(p.um + line * n1);
             // lines in the axis-2 shell are sponged by the axis-2 pass below
-            const bool damp = p.w1 && x >= SHELL && x < n2 - SHELL;
+            const bool xshell = x < SHELL || x >= n2 - SHELL;
+            const bool damp = p.w1 && !xshell;
             const float wx = damp ? __ldg(p.w2 + x) : 1.f;
+            float4 lo0 = make_float4(0.f, 0.f, 0.f, 0.f), lo1 = lo0;  // cells 0..7 as left
             if (p.top || damp) {
-                float4 a = o[0], b = o[1];
-                if (p.top) b3_zlow<EXACT>(a, b, __ldg(m), __ldg(m + 1), __ldg(p.zl + line));
+                lo0 = o[0];
+                lo1 = o[1];
+                if (p.top) b3_zlow<EXACT>(lo0, lo1, b3_mend(p, line, 0), b3_mend(p, line, 1), __ldg(p.zl + line));
                 if (damp) {
-                    b3_damp4<EXACT>(a, p.w1, 0, wx, wy, 15u);
-                    b3_damp4<EXACT>(b, p.w1, 4, wx, wy, 3u);
+                    b3_damp4<EXACT>(lo0, p.w1, 0, wx, wy, 15u);
+                    b3_damp4<EXACT>(lo1, p.w1, 4, wx, wy, 3u);
                 }
-                o[0] = a;
-                o[1] = b;
+                o[0] = lo0;
+                o[1] = lo1;
             }
             float4 a = o[q - 2], b = o[q - 1];
-            b3_zhigh<EXACT>(a, b, __ldg(m + q - 2), __ldg(m + q - 1), __ldg(p.zh + line));
+            b3_zhigh<EXACT>(a, b, b3_mend(p, line, 2), b3_mend(p, line, 3), __ldg(p.zh + line));
             if (damp) {
                 b3_damp4<EXACT>(a, p.w1, n1 - 8, wx, wy, 12u);
                 b3_damp4<EXACT>(b, p.w1, n1 - 4, wx, wy, 15u);
             }
             o[q - 2] = a;
             o[q - 1] = b;
+            // final unless the axis-2 pass changes the line (the axis-2 shell);
+            // without a sponge and with a free surface the low end is not
+            // read (nor needed: the next step's low-end ABC is off)
+            if (p.eo && !xshell) {
+                float4 *e = reinterpret_cast<float4 *>(p.eo) + line * 4;
+                e[0] = lo0;
+                e[1] = lo1;
+                e[2] = a;
+                e[3] = b;
+            }
         }
         __syncthreads();  // the axis-2 pass reads the axis-1 results of lines x = 1..5
         for (int z = tid; z < n1; z += NT) {
             const long long c0 = (long long)y * s3 + z;
             b3_xline<EXACT>(p, c0, y, z, true, p.w1 != nullptr);
             b3_xline<EXACT>(p, c0, y, z, false, p.w1 != nullptr);
+        }
+        if (p.eo) {  // the axis-2 shell lines' ends, final now
+            __syncthreads();
+            for (int l = tid; l < 2 * SHELL * 4; l += NT) {
+                const int k = l >> 2, x = k < SHELL ? k : n2 - 2 * SHELL + k;
+                b3_eput_from_uo(p, (long long)y * n2 + x, l & 3);
+            }
         }
         return;
     }
@@ -163,16 +205,15 @@ __global__ void __launch_bounds__(b3::NT) k_bnd3(const Bnd3Params p) {
                 const int y = ya + l / ncol, x = xa + l % ncol;
                 const long long line = (long long)y * n2 + x;
                 float4 *o = reinterpret_cast<float4 *>(p.uo + line * n1);
-                const float4 *m = reinterpret_cast<const float4 *>(p.um + line * n1);
                 if (zlo) {
                     float4 a = o[0], b = o[1];
-                    b3_zlow<EXACT>(a, b, __ldg(m), __ldg(m + 1), __ldg(p.zl + line));
+                    b3_zlow<EXACT>(a, b, b3_mend(p, line, 0), b3_mend(p, line, 1), __ldg(p.zl + line));
                     o[0] = a;
                     o[1] = b;
                 }
                 if (zhi) {
                     float4 a = o[q - 2], b = o[q - 1];
-                    b3_zhigh<EXACT>(a, b, __ldg(m + q - 2), __ldg(m + q - 1), __ldg(p.zh + line));
+                    b3_zhigh<EXACT>(a, b, b3_mend(p, line, 2), b3_mend(p, line, 3), __ldg(p.zh + line));
                     o[q - 2] = a;
                     o[q - 1] = b;
                 }
@@ -204,16 +245,25 @@ __global__ void __launch_bounds__(b3::NT) k_bnd3(const Bnd3Params p) {
                 mprev = mc;
             }
         }
-        if (!p.w1) return;
-        __syncthreads();
-        // sponge of every cell of the block (all lie in the axis-3 shell)
-        const int nq = nz / 4;
-        for (int l = tid; l < SHELL * ncol * nq; l += NT) {
-            const int y = ya + l / (ncol * nq), k = l % (ncol * nq), x = xa + k / nq, z = za + 4 * (k % nq);
-            float4 *c = reinterpret_cast<float4 *>(p.uo + (long long)y * s3 + (long long)x * s2 + z);
-            float4 v = *c;
-            b3_damp4<EXACT>(v, p.w1, z, __ldg(p.w2 + x), __ldg(p.w3 + y), 15u);
-            *c = v;
+        if (p.w1) {
+            __syncthreads();
+            // sponge of every cell of the block (all lie in the axis-3 shell)
+            const int nq = nz / 4;
+            for (int l = tid; l < SHELL * ncol * nq; l += NT) {
+                const int y = ya + l / (ncol * nq), k = l % (ncol * nq), x = xa + k / nq, z = za + 4 * (k % nq);
+                float4 *c = reinterpret_cast<float4 *>(p.uo + (long long)y * s3 + (long long)x * s2 + z);
+                float4 v = *c;
+                b3_damp4<EXACT>(v, p.w1, z, __ldg(p.w2 + x), __ldg(p.w3 + y), 15u);
+                *c = v;
+            }
+        }
+        if (p.eo && (zr == 0 || zr == p.nzr - 1)) {  // the line ends this block holds, final now
+            __syncthreads();
+            for (int l = tid; l < SHELL * ncol * 4; l += NT) {
+                const int k = l >> 2, part = l & 3;
+                if (part < 2 ? zr != 0 : zr != p.nzr - 1) continue;
+                b3_eput_from_uo(p, (long long)(ya + k / ncol) * n2 + xa + k % ncol, part);
+            }
         }
         return;
     }

@@ -79,6 +79,13 @@ struct awe_plan {
     unsigned long long *sched_counter = nullptr;
     unsigned long long sched_base = 0;
     int *d_err = nullptr;
+    // compact copies of the axis-1 line ends of the last two levels (3D
+    // boundary launch, [n3][n2][16] each): inside a forward run (ends_run) the
+    // boundary launch of step it reads the ends of its step's current level
+    // from ends[ends_idx] and writes those of the new level to the other one
+    float *ends[2] = {nullptr, nullptr};
+    bool ends_run = false;
+    int ends_idx = 0;
     // TMA-staged spherical step (GPU-program scheme, AWE_FAST): maps encoded
     // per run (the level fields are reallocated when the shot count changes)
     bool sph_tma = false;

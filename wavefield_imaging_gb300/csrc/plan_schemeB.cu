@@ -96,6 +96,12 @@ awe_status planB_init(awe_plan *p) {
         const char *spin = std::getenv("AWE_PIPELINE_SPIN_LIMIT");
         if (spin && *spin) p->spin_limit = std::atoll(spin);
     }
+    // line-end copies of the 3D boundary launch (made before any capture of
+    // the time loop; AWE_BND_ENDS=0: the launch reads the level itself)
+    const char *eenv = std::getenv("AWE_BND_ENDS");
+    if (d.ndim == 3 && d.dabc && !d.hybrid && bnd3_eligible(p->nop, p->g) && !(eenv && std::strcmp(eenv, "0") == 0))
+        for (int k = 0; k < 2; k++)
+            AWE_TRY(dev_alloc(p, (void **)&p->ends[k], (size_t)p->g.n2 * p->g.n3 * 16 * sizeof(float)));
 
     p->nsmp = (d.nt - 1) / d.jdata + 1;
     p->nsnap = d.jsnap > 0 ? (d.nt - 1) / d.jsnap + 1 : 0;
@@ -367,6 +373,11 @@ awe_status stepB_full(awe_plan *p, const StepBParams &sp0, const float *prv, con
         bp.w2 = p->w[1];
         bp.w3 = p->w[2];
         bp.top = !d.fsrf;
+        if (p->ends_run) {
+            bp.em = p->ends[p->ends_idx];
+            bp.eo = p->ends[1 - p->ends_idx];
+            p->ends_idx ^= 1;
+        }
         bp.rec = ext_pts;
         bp.nr = ext_n;
         bp.rec_stride = ext_stride;
@@ -429,6 +440,18 @@ awe_status planB_run_hooked(awe_plan *p, const float *d_wav, int ncs, float *d_d
     if (p->use_tma) {  // the TMA kernel's work counter restarts with every run (graph replays included)
         CUDA_TRY(cudaMemsetAsync(p->sched_counter, 0, sizeof(unsigned long long), s));
         p->sched_base = 0;
+    }
+    // the boundary launches pass the line ends from step to step; the first
+    // step reads those of the zero level
+    struct EndsOff {
+        awe_plan *p;
+        ~EndsOff() { p->ends_run = false; }
+    } ends_off{p};
+    p->ends_run = false;
+    if (p->ends[0] && stepB3_bnd(p)) {
+        CUDA_TRY(cudaMemsetAsync(p->ends[0], 0, (size_t)g.n2 * g.n3 * 16 * sizeof(float), s));
+        p->ends_idx = 0;
+        p->ends_run = true;
     }
     if (p->nsnap > 0 && !d_wfl && p->snap_cb && !p->d_snap_tmp)
         AWE_TRY(dev_alloc(p, (void **)&p->d_snap_tmp, p->snap_elems * sizeof(float)));
