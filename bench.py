@@ -282,11 +282,34 @@ def _time_reference_program(args, w, cores, extra_steps=40):
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
     sample = ("%d-step difference of the reference's sfAWEFDcart3Dcpu (built from its sources, -O3 -fopenmp, "
-              "%d OpenMP threads) on the workload's %dx%dx%d padded grid, 2 against %d steps per bench step, "
+              "%d OpenMP threads) on the workload's %dx%dx%d padded grid, runs of 2 and %d steps per timed pair, "
               "input reading and set-up cancelled" % (extra_steps, cores, w["n"][0] + 2 * w["nb"],
                                                       w["n"][1] + 2 * w["nb"], w["n"][2] + 2 * w["nb"],
                                                       2 + extra_steps))
     return per_step, sample
+
+
+def host_baseline(w):
+    """The engine line's host-core baseline: one 2- and 42-step pair of the
+    reference's own sfAWEFDcart3Dcpu (about 13 s on 16 Grace cores), else
+    the oracle port of its update."""
+    from types import SimpleNamespace
+
+    cores = os.cpu_count() or 1
+    note = None
+    if os.access(REF_CPU_PROGRAM, os.X_OK):
+        try:
+            per_step, sample = _time_reference_program(SimpleNamespace(steps=1, warmup=0), w, cores)
+            cells = float(np.prod([n + 2 * w["nb"] for n in w["n"]]))
+            return {"value": cells / per_step[0], "unit": UNIT, "cores": cores, "kind": "reference",
+                    "sample": sample}
+        except Exception as e:  # noqa: BLE001 - the port is timed instead
+            note = "reference program not timed (%s: %s)" % (type(e).__name__, e)
+    v, cores, sample, _ = cpu_baseline(w)
+    out = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+    if note:
+        out["note"] = note
+    return out
 
 
 def run_reference(args):
@@ -468,8 +491,7 @@ def run_ours(args):
                 out[key] = {"error": "%s: %s" % (type(e).__name__, e)}
             torch.cuda.empty_cache()
     if args.cpu_baseline and world == 1:  # the host-core baseline belongs to the one-GPU line
-        v, cores, sample, _ = cpu_baseline(w)
-        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        out["cpu_baseline"] = host_baseline(w)
         if grad_check is not None:
             try:
                 out["cpu_baseline"]["gradient"] = oracle_gradient_check(grad_check)
